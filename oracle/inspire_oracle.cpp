@@ -1,0 +1,1072 @@
+// TEST INFRASTRUCTURE — the CPU oracle for the InspiRING respond path.
+//
+// Only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline / reference legs may
+// load this library, as the checker and as the timed CPU baseline. The product library
+// (inspire-rs_gb300/) never links or calls it.
+//
+// A from-scratch C++ restatement of the reference crate raven-inspire (hisoka-io/inspire-rs)
+// for single-prime parameter sets. File:line citations point into the reference:
+//   math/ntt.rs            NTT (Montgomery R=2^64, bit-reversed twiddle ladder, CT/GS)
+//   math/poly.rs           ring ops, seed expansion, tight coefficient codec
+//   inspiring/inspiring2.rs  PackParams, offline keys, rotation sums, backward recursion,
+//                            online gather, client key body
+//   inspiring/shard_store.rs packing store: step-1 sums, tags, scan + b fold, gather
+//   pir/respond.rs         pack_shard (both branches), ServerResponse wire
+//   pir/mod_switch.rs      response mod switch
+//   pir/setup.rs, pir/session.rs, rgsw/types.rs, pir/encode_db.rs, params.rs
+//                          client-side regeneration of the KAT inputs
+// Parity pins: tests/fixtures/respond_byte_identity_d256.bin (FNV 0x796a80ca60d31a52) and
+// the single-prime lines of tests/fixtures/packing_seat_response_kat.txt, replayed by
+// tests/test_oracle_pins.py.
+#include <omp.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <memory>
+#include <random>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "oracle_rng.hpp"
+
+namespace orc {
+
+typedef std::vector<u64> Vec;
+
+static inline u64 mulmod(u64 a, u64 b, u64 q) { return (u64)((u128)a * b % q); }
+static inline u64 powmod(u64 b, u64 e, u64 m) {
+  u64 r = 1;
+  b %= m;
+  while (e) {
+    if (e & 1) r = mulmod(r, b, m);
+    b = mulmod(b, b, m);
+    e >>= 1;
+  }
+  return r;
+}
+static inline u64 addmod(u64 a, u64 b, u64 q) {
+  u64 s = a + b;
+  return s >= q ? s - q : s;
+}
+static inline u64 submod(u64 a, u64 b, u64 q) { return a >= b ? a - b : a + q - b; }
+
+// Extended-gcd inverse (inspiring2.rs:1853-1860); 0 when none exists.
+static u64 mod_inverse(u64 a, u64 m) {
+  __int128 t = 0, nt = 1, r = m, nr = a % m;
+  while (nr != 0) {
+    __int128 qq = r / nr;
+    __int128 tmp = t - qq * nt;
+    t = nt;
+    nt = tmp;
+    tmp = r - qq * nr;
+    r = nr;
+    nr = tmp;
+  }
+  if (r != 1) return 0;
+  if (t < 0) t += m;
+  return (u64)t;
+}
+
+// ---------------------------------------------------------------------------------------
+// NTT context: math/ntt.rs:35-146 (construction), 247-349 (butterflies), 688-694 (REDC),
+// 743-752 (root search), 806-833 (Montgomery twiddle ladder).
+struct Ntt {
+  size_t n;
+  unsigned logn;
+  u64 q, qinv_neg, r2;
+  Vec psi_pow, psi_inv_pow;
+  u64 n_inv_mont;
+
+  u64 mont(u64 a, u64 b) const {
+    u128 ab = (u128)a * b;
+    u64 m = (u64)ab * qinv_neg;
+    u64 t = (u64)((ab + (u128)m * q) >> 64);
+    return t >= q ? t - q : t;
+  }
+  u64 to_mont(u64 a) const { return mont(a, r2); }
+  u64 from_mont(u64 a) const { return mont(a, 1); }
+
+  static u64 find_root(u64 order, u64 q) {
+    u64 e = (q - 1) / order;
+    for (u64 g = 2; g < (1ull << 16) && g < q; g++) {
+      u64 c = powmod(g, e, q);
+      if (powmod(c, order, q) == 1 && powmod(c, order / 2, q) != 1) return c;
+    }
+    throw std::runtime_error("no primitive root");
+  }
+
+  Vec ladder(u64 psi_m) const {
+    Vec f(n, 0);
+    f[1] = to_mont(1);
+    for (size_t m = 1; m < n; m++) {
+      if ((m & (m - 1)) == 0) {
+        size_t e = n / (2 * m);
+        u64 p = to_mont(1);
+        for (size_t k = 0; k < e; k++) p = mont(p, psi_m);
+        f[m] = p;
+      } else {
+        f[m] = mont(f[m & (m - 1)], f[m & (~m + 1)]);
+      }
+    }
+    return f;
+  }
+
+  Ntt(size_t n_, u64 q_) : n(n_), q(q_) {
+    if ((q - 1) % (2 * n) != 0) throw std::runtime_error("q != 1 mod 2n");
+    logn = 0;
+    while ((size_t(1) << logn) < n) logn++;
+    u64 y = 1;
+    for (int i = 1; i < 64; i++) y |= (y * q) & (1ull << i);
+    qinv_neg = (u64)0 - y;
+    u64 rmod = (u64)(((u128)1 << 64) % q);
+    r2 = mulmod(rmod, rmod, q);
+    u64 psi = find_root(2 * n, q);
+    psi_pow = ladder(to_mont(psi));
+    psi_inv_pow = ladder(to_mont(powmod(psi, q - 2, q)));
+    n_inv_mont = to_mont(powmod(n, q - 2, q));
+  }
+
+  // Forward: standard-form coefficients in, Montgomery-form evaluations out.
+  void forward(u64* c) const {
+    for (size_t i = 0; i < n; i++) c[i] = to_mont(c[i]);
+    size_t t = n;
+    for (size_t m = 1; m < n; m <<= 1) {
+      t >>= 1;
+      for (size_t i = 0; i < m; i++) {
+        size_t j1 = 2 * i * t;
+        u64 w = psi_pow[m + i];
+        for (size_t j = j1; j < j1 + t; j++) {
+          u64 u = c[j], v = mont(c[j + t], w);
+          c[j] = addmod(u, v, q);
+          c[j + t] = submod(u, v, q);
+        }
+      }
+    }
+  }
+  // Inverse: Montgomery-form evaluations in, standard-form coefficients out.
+  void inverse(u64* c) const {
+    size_t t = 1;
+    for (size_t m = n; m > 1;) {
+      m >>= 1;
+      for (size_t i = 0; i < m; i++) {
+        size_t j2 = i * 2 * t;
+        u64 w = psi_inv_pow[m + i];
+        for (size_t j = j2; j < j2 + t; j++) {
+          u64 u = c[j], v = c[j + t];
+          c[j] = addmod(u, v, q);
+          c[j + t] = mont(submod(u, v, q), w);
+        }
+      }
+      t <<= 1;
+    }
+    for (size_t i = 0; i < n; i++) c[i] = mont(mont(c[i], n_inv_mont), 1);
+  }
+  Vec fwd(Vec v) const {
+    forward(v.data());
+    return v;
+  }
+  Vec inv(Vec v) const {
+    inverse(v.data());
+    return v;
+  }
+  // mul_acc_ntt_domain scalar loop (poly.rs:1032-1040).
+  void mul_acc(u64* acc, const u64* a, const u64* b) const {
+    for (size_t i = 0; i < n; i++) {
+      u64 s = acc[i] + mont(a[i], b[i]);
+      acc[i] = s >= q ? s - q : s;
+    }
+  }
+  // Negacyclic product through the transform (poly.rs:900-928).
+  Vec mul(const Vec& a, const Vec& b) const {
+    Vec x = fwd(a), y = fwd(b), r(n);
+    for (size_t i = 0; i < n; i++) r[i] = mont(x[i], y[i]);
+    inverse(r.data());
+    return r;
+  }
+};
+
+// ---------------------------------------------------------------------------------------
+// Parameter set (params.rs:137-196) restricted to one prime.
+struct Params {
+  size_t n;
+  u64 q;
+  u64 p;
+  double sigma;
+  u64 gadget_base;
+  size_t gadget_len;  // packing_gadget_len (== query_gadget_len in every shipped set)
+  bool approx;        // approximate_packing_gadget
+  size_t dropped() const { return approx ? 1 : 0; }
+  size_t key_rows() const { return gadget_len - dropped(); }
+  u64 delta() const { return q / p; }
+};
+
+static u64 gadget_power(const Params& P, size_t i) {
+  u128 r = 1;
+  for (size_t k = 0; k < i; k++) r = r * P.gadget_base % P.q;
+  return (u64)r;
+}
+
+// ---------------------------------------------------------------------------------------
+// PackParams (inspiring2.rs:209-286) and derive_automorph_tables (330-379).
+struct PackParams {
+  Params P;
+  std::shared_ptr<Ntt> ntt;
+  size_t gamma;
+  u64 generator;
+  std::vector<u64> gen_pows;
+  u64 mod_inv_gamma;
+  Vec mod_inv_poly_ntt;
+  std::vector<Vec> mono_ntt, neg_mono_ntt;
+  // tables[(t-1)/2][i]: source slot of slot i under tau_t, built for the odd t the path
+  // reads (the generator powers); every other entry stays empty.
+  std::vector<std::vector<uint32_t>> tables;
+
+  const std::vector<uint32_t>& table(u64 t) const { return tables[(t - 1) / 2]; }
+};
+
+static std::shared_ptr<PackParams> make_pack_params(const Params& P, size_t gamma) {
+  auto pp = std::make_shared<PackParams>();
+  size_t n = P.n;
+  if (gamma == 0 || (gamma & (gamma - 1)) || gamma > n / 2) throw std::runtime_error("illegal width");
+  pp->P = P;
+  pp->ntt = std::make_shared<Ntt>(n, P.q);
+  pp->gamma = gamma;
+  pp->generator = 2 * n / gamma + 1;
+  u64 two_n = 2 * n, v = 1;
+  for (size_t i = 0; i < n; i++) {
+    pp->gen_pows.push_back(v);
+    v = v * pp->generator % two_n;
+  }
+  pp->mod_inv_gamma = mod_inverse(gamma, P.q);
+  Vec c(n, 0);
+  c[0] = pp->mod_inv_gamma;
+  pp->mod_inv_poly_ntt = pp->ntt->fwd(c);
+  pp->mono_ntt.resize(n);
+  pp->neg_mono_ntt.resize(n);
+#pragma omp parallel for schedule(static)
+  for (long j = 0; j < (long)n; j++) {
+    Vec m(n, 0);
+    m[j] = 1;
+    pp->mono_ntt[j] = pp->ntt->fwd(m);
+    m[j] = P.q - 1;
+    pp->neg_mono_ntt[j] = pp->ntt->fwd(m);
+  }
+  // Slot j of NTT(X^k) for k in [0, 2n), via X^(k+n) = -X^k.
+  auto slot_value = [&](size_t k, size_t j) -> u64 {
+    if (k < n) return pp->mono_ntt[k][j];
+    u64 v = pp->mono_ntt[k - n][j];
+    return (P.q - v) % P.q;
+  };
+  std::vector<std::pair<u64, u64>> powers;  // (value, odd exponent) of w_0
+  for (size_t e = 1; e < two_n; e += 2) powers.push_back({slot_value(e, 0), e});
+  std::sort(powers.begin(), powers.end());
+  for (size_t i = 1; i < powers.size(); i++)
+    if (powers[i].first == powers[i - 1].first) throw std::runtime_error("tables underivable");
+  std::vector<u64> exps(n);
+  std::vector<size_t> slot_of_exp(n, SIZE_MAX);
+  for (size_t j = 0; j < n; j++) {
+    u64 root = slot_value(1, j);
+    auto it = std::lower_bound(powers.begin(), powers.end(), std::make_pair(root, (u64)0));
+    if (it == powers.end() || it->first != root) throw std::runtime_error("tables underivable");
+    u64 e = it->second;
+    slot_of_exp[e / 2] = j;
+    exps[j] = e;
+  }
+  pp->tables.resize(n);
+  for (size_t i = 0; i < n && i < gamma; i++) {
+    u64 t = pp->gen_pows[i];
+    auto& tb = pp->tables[(t - 1) / 2];
+    if (!tb.empty()) continue;
+    tb.resize(n);
+    for (size_t j = 0; j < n; j++) tb[j] = (uint32_t)slot_of_exp[((t * exps[j]) % two_n) / 2];
+  }
+  return pp;
+}
+
+// ---------------------------------------------------------------------------------------
+// Offline packing keys (inspiring2.rs:537-598, 839-887).
+struct OfflineKeys {
+  std::vector<std::vector<Vec>> w_all_ntt;  // [gamma-1][key_rows]
+  std::vector<Vec> w_mask;                  // coefficient form, key_rows polys
+};
+
+static std::vector<Vec> expand_mask(const uint8_t seed[32], u64 stream, size_t n, u64 q, size_t count) {
+  ChaCha20Rng rng = ChaCha20Rng::from_seed(seed);
+  rng.set_stream(stream);
+  std::vector<Vec> out;
+  for (size_t k = 0; k < count; k++) {
+    Vec c(n);
+    for (size_t i = 0; i < n; i++) c[i] = rng.next_u64() % q;
+    out.push_back(c);
+  }
+  return out;
+}
+
+static std::vector<Vec> kept_mask_rows(const uint8_t seed[32], const Params& P, size_t gamma) {
+  u64 stream = P.dropped() == 0 ? 0 : (u64)gamma;
+  auto all = expand_mask(seed, stream, P.n, P.q, P.gadget_len);
+  return std::vector<Vec>(all.begin() + P.dropped(), all.end());
+}
+
+static Vec permute(const Vec& src, const std::vector<uint32_t>& tb) {
+  Vec r(src.size());
+  for (size_t i = 0; i < src.size(); i++) r[i] = src[tb[i]];
+  return r;
+}
+
+static OfflineKeys make_offline_keys(const PackParams& pp, const uint8_t w_seed[32]) {
+  OfflineKeys k;
+  k.w_mask = kept_mask_rows(w_seed, pp.P, pp.gamma);
+  std::vector<Vec> w_mask_ntt;
+  for (auto& w : k.w_mask) w_mask_ntt.push_back(pp.ntt->fwd(w));
+  for (size_t i = 0; i + 1 < pp.gamma; i++) {
+    const auto& tb = pp.table(pp.gen_pows[i]);
+    std::vector<Vec> row;
+    for (auto& w : w_mask_ntt) row.push_back(permute(w, tb));
+    k.w_all_ntt.push_back(row);
+  }
+  return k;
+}
+
+// ---------------------------------------------------------------------------------------
+// rotation_sums (inspiring2.rs:964-1004).
+static std::vector<Vec> rotation_sums(const PackParams& pp, const std::vector<Vec>& inputs_ntt) {
+  size_t n = pp.P.n, gamma = pp.gamma;
+  std::vector<Vec> out(gamma);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (long i = 0; i < (long)gamma; i++) {
+    Vec r(n, 0);
+    size_t exp_index = (n - (size_t)i) % n;
+    for (size_t j = 0; j < inputs_ntt.size(); j++) {
+      size_t index = (j * pp.gen_pows[exp_index]) % (2 * n);
+      const Vec& mono = index < n ? pp.mono_ntt[index % n] : pp.neg_mono_ntt[index % n];
+      pp.ntt->mul_acc(r.data(), mono.data(), inputs_ntt[j].data());
+    }
+    Vec scaled(n);
+    for (size_t t = 0; t < n; t++) scaled[t] = pp.ntt->mont(r[t], pp.mod_inv_poly_ntt[t]);
+    out[i] = permute(scaled, pp.table(pp.gen_pows[i]));
+  }
+  return out;
+}
+
+// Gadget decomposition (rgsw/external_product.rs:30-99) and its rounded variant
+// (inspiring2.rs:1167-1225).
+static std::vector<Vec> gadget_decompose(const Params& P, const Vec& coeffs) {
+  std::vector<Vec> d(P.gadget_len, Vec(P.n));
+  for (size_t j = 0; j < P.n; j++) {
+    u64 val = coeffs[j];
+    for (size_t k = 0; k < P.gadget_len; k++) {
+      d[k][j] = (val % P.gadget_base) % P.q;
+      val /= P.gadget_base;
+    }
+  }
+  return d;
+}
+
+static std::vector<Vec> gadget_decompose_rounded(const Params& P, const Vec& coeffs, size_t dropped) {
+  size_t rows = P.gadget_len - dropped;
+  std::vector<Vec> d(rows, Vec(P.n, 0));
+  u128 base = P.gadget_base, unit = 1;
+  for (size_t k = 0; k < dropped; k++) unit *= base;
+  for (size_t j = 0; j < P.n; j++) {
+    u128 rounded = ((u128)coeffs[j] + unit / 2) / unit;
+    for (size_t r = 0; r + 1 < rows; r++) {
+      d[r][j] = (u64)(rounded % base);
+      rounded /= base;
+    }
+    d[rows - 1][j] = (u64)rounded;
+  }
+  // Poly::from_coeffs_moduli reduces each digit row mod q.
+  for (auto& row : d)
+    for (auto& x : row) x %= P.q;
+  return d;
+}
+
+struct Precomp {
+  Vec a_hat;                              // coefficient form
+  std::vector<std::vector<Vec>> bold_t_ntt;  // [gamma-1][key_rows]
+};
+
+// fold_rotations_backward (inspiring2.rs:1014-1085) with LastDigitNtt (1094-1161).
+static Precomp fold_rotations_backward(const PackParams& pp, const OfflineKeys& keys, std::vector<Vec> r_all) {
+  const Params& P = pp.P;
+  const Ntt& ntt = *pp.ntt;
+  size_t gamma = pp.gamma, n = P.n;
+  bool use_last = false;
+  Vec of_sum;
+  std::vector<Vec> of_digit;
+  if (gamma > P.gadget_len + 1 && P.dropped() == 0) {
+    u128 q = P.q, base = P.gadget_base, span = 1, power = 1;
+    std::vector<u128> powers;
+    bool ok = base >= 2;
+    for (size_t k = 0; k < P.gadget_len; k++) {
+      powers.push_back(power);
+      power = power * (base % q) % q;
+      span = span > (((u128)1 << 120) / base) ? ((u128)1 << 120) : span * base;
+    }
+    if (ok && span >= q) {
+      u64 inverse = mod_inverse((u64)powers.back(), P.q);
+      if (inverse != 0) {
+        use_last = true;
+        auto constant = [&](u64 v) {
+          Vec c(n, 0);
+          c[0] = v;
+          return ntt.fwd(c);
+        };
+        of_sum = constant(inverse);
+        for (size_t k = 0; k + 1 < P.gadget_len; k++)
+          of_digit.push_back(constant((u64)((q - (u128)inverse * powers[k] % q) % q)));
+      }
+    }
+  }
+  Precomp pc;
+  pc.bold_t_ntt.resize(gamma - 1);
+  for (long i = (long)gamma - 2; i >= 0; i--) {
+    Vec r_coeff = ntt.inv(r_all[i + 1]);
+    std::vector<Vec> digits = P.dropped() == 0 ? gadget_decompose(P, r_coeff)
+                                               : gadget_decompose_rounded(P, r_coeff, P.dropped());
+    size_t transformed = use_last ? digits.size() - 1 : digits.size();
+    std::vector<Vec> dn;
+    for (size_t k = 0; k < transformed; k++) dn.push_back(ntt.fwd(digits[k]));
+    if (use_last) {
+      Vec last(n, 0);
+      ntt.mul_acc(last.data(), r_all[i + 1].data(), of_sum.data());
+      for (size_t k = 0; k < dn.size() && k < of_digit.size(); k++)
+        ntt.mul_acc(last.data(), dn[k].data(), of_digit[k].data());
+      dn.push_back(last);
+    }
+    for (size_t k = 0; k < dn.size() && k < keys.w_all_ntt[i].size(); k++)
+      ntt.mul_acc(r_all[i].data(), dn[k].data(), keys.w_all_ntt[i][k].data());
+    pc.bold_t_ntt[i] = dn;
+  }
+  pc.a_hat = ntt.inv(r_all[0]);
+  return pc;
+}
+
+// packing_online_gather (inspiring2.rs:1393-1485), returning the final b.
+static Vec packing_online_gather(const PackParams& pp, const Precomp& pc, const std::vector<Vec>& y_body_ntt,
+                                 const Vec& b_poly) {
+  size_t n = pp.P.n;
+  const Ntt& ntt = *pp.ntt;
+  Vec acc(n, 0);
+  for (size_t i = 0; i + 1 < pp.gamma; i++) {
+    const auto& tb = pp.table(pp.gen_pows[i]);
+    for (size_t k = 0; k < y_body_ntt.size(); k++) {
+      const Vec& y = y_body_ntt[k];
+      const Vec& t = pc.bold_t_ntt[i][k];
+      for (size_t j = 0; j < n; j++) acc[j] = addmod(acc[j], ntt.mont(y[tb[j]], t[j]), pp.P.q);
+    }
+  }
+  Vec sum_b = ntt.inv(acc);
+  Vec out(n);
+  for (size_t j = 0; j < n; j++) out[j] = addmod(b_poly[j], sum_b[j], pp.P.q);
+  return out;
+}
+
+// ---------------------------------------------------------------------------------------
+// Packing store (shard_store.rs:86-156, 197-264, 282-342, 378-427).
+static const u64 TAG_PRIME = (1ull << 61) - 1;
+
+struct Store {
+  std::vector<Vec> column_sums_ntt;
+  Vec tag_key;
+  std::vector<u64> column_tags;
+};
+
+static u64 column_tag(const u64* words, size_t n, const u64* key) {
+  u128 sum = 0;
+  for (size_t k = 0; k < n; k++) sum += (u128)(words[k] & 0xffffffffull) * key[2 * k] + (u128)(words[k] >> 32) * key[2 * k + 1];
+  return (u64)(sum % TAG_PRIME);
+}
+
+static Store build_store(const PackParams& pp, const std::vector<Vec>& columns, u64 key_seed) {
+  Store s;
+  size_t n = pp.P.n;
+  // The reference keys the tags from OS entropy; any key in [0, 2^61-1) serves.
+  ChaCha20Rng rng = ChaCha20Rng::seed_from_u64(key_seed);
+  for (size_t i = 0; i < 2 * n; i++) {
+    u64 c;
+    do c = rng.next_u64() >> 3;
+    while (c >= TAG_PRIME);
+    s.tag_key.push_back(c);
+  }
+  for (auto& col : columns) s.column_tags.push_back(column_tag(col.data(), n, s.tag_key.data()));
+  std::vector<Vec> cols_ntt(columns.size());
+#pragma omp parallel for
+  for (long j = 0; j < (long)columns.size(); j++) cols_ntt[j] = pp.ntt->fwd(columns[j]);
+  s.column_sums_ntt = rotation_sums(pp, cols_ntt);
+  return s;
+}
+
+// check_columns_and_fold_b: returns false on a tag mismatch.
+static bool check_and_fold_b(const PackParams& pp, const Store& s, const std::vector<Vec>& columns, const Vec& b,
+                             Vec& b_poly) {
+  size_t n = pp.P.n;
+  u64 q = pp.P.q;
+  Vec b_rev(n);
+  for (size_t k = 0; k < n; k++) b_rev[k] = k == 0 ? b[0] % q : (q - b[n - k] % q) % q;
+  b_poly.assign(n, 0);
+  std::vector<u64> tags(columns.size());
+#pragma omp parallel for
+  for (long j = 0; j < (long)columns.size(); j++) {
+    const Vec& col = columns[j];
+    u128 tag = 0, low = 0, high = 0;
+    for (size_t k = 0; k < n; k++) {
+      tag += (u128)(col[k] & 0xffffffffull) * s.tag_key[2 * k] + (u128)(col[k] >> 32) * s.tag_key[2 * k + 1];
+      u128 prod = (u128)col[k] * b_rev[k];
+      low += (u64)prod;
+      high += (u64)(prod >> 64);
+    }
+    u128 qq = q;
+    u128 coeff0 = ((high % qq) * ((((u128)1) << 64) % qq) + low % qq) % qq;
+    tags[j] = (u64)(tag % TAG_PRIME);
+    b_poly[j] = (u64)coeff0;
+  }
+  for (size_t j = 0; j < columns.size(); j++)
+    if (tags[j] != s.column_tags[j]) return false;
+  return true;
+}
+
+static Precomp store_packing_offline(const PackParams& pp, const Store& s, const OfflineKeys& keys, const Vec& a) {
+  size_t n = pp.P.n;
+  Vec a_ntt = pp.ntt->fwd(a);
+  std::vector<Vec> r_all(pp.gamma, Vec(n));
+#pragma omp parallel for
+  for (long i = 0; i < (long)pp.gamma; i++) {
+    const auto& tb = pp.table(pp.gen_pows[i]);
+    for (size_t k = 0; k < n; k++) r_all[i][k] = pp.ntt->mont(a_ntt[tb[k]], s.column_sums_ntt[i][k]);
+  }
+  return fold_rotations_backward(pp, keys, r_all);
+}
+
+// ---------------------------------------------------------------------------------------
+// pack_shard (respond.rs:770-863): returns (a_hat, b).
+struct Packed {
+  Vec a, b;
+};
+
+static Packed pack_per_query(const PackParams& pp, const OfflineKeys& keys, const std::vector<Vec>& columns,
+                             const Vec& a, const Vec& b, const std::vector<Vec>& y_body) {
+  size_t n = pp.P.n, gamma = pp.gamma;
+  const Ntt& ntt = *pp.ntt;
+  // plaintext_multiply_columns + sample_extract_coeff0 + b_poly assembly.
+  std::vector<Vec> a_ct(gamma);
+  Vec b_poly(n, 0);
+#pragma omp parallel for
+  for (long j = 0; j < (long)gamma; j++) {
+    a_ct[j] = ntt.mul(a, columns[j]);
+    Vec bj = ntt.mul(b, columns[j]);
+    b_poly[j] = bj[0];
+  }
+  std::vector<Vec> a_ntt(gamma);
+#pragma omp parallel for
+  for (long j = 0; j < (long)gamma; j++) a_ntt[j] = ntt.fwd(a_ct[j]);
+  auto r_all = rotation_sums(pp, a_ntt);
+  Precomp pc = fold_rotations_backward(pp, keys, r_all);
+  std::vector<Vec> y_ntt;
+  for (auto& y : y_body) y_ntt.push_back(ntt.fwd(y));
+  Packed out;
+  out.a = pc.a_hat;
+  out.b = packing_online_gather(pp, pc, y_ntt, b_poly);
+  return out;
+}
+
+static bool pack_with_store(const PackParams& pp, const OfflineKeys& keys, const Store& s,
+                            const std::vector<Vec>& columns, const Vec& a, const Vec& b,
+                            const std::vector<Vec>& y_body, Packed& out) {
+  Vec b_poly;
+  if (!check_and_fold_b(pp, s, columns, b, b_poly)) return false;
+  Precomp pc = store_packing_offline(pp, s, keys, a);
+  std::vector<Vec> y_ntt;
+  for (auto& y : y_body) y_ntt.push_back(pp.ntt->fwd(y));
+  out.a = pc.a_hat;
+  out.b = packing_online_gather(pp, pc, y_ntt, b_poly);
+  return true;
+}
+
+// mod_switch_poly (mod_switch.rs:148-176).
+static Vec mod_switch(const Vec& c, u64 q_old, u64 q_new) {
+  Vec o(c.size());
+  for (size_t i = 0; i < c.size(); i++) {
+    u128 scaled = (u128)c[i] * q_new + q_old / 2;
+    o[i] = (u64)((scaled / q_old) % q_new);
+  }
+  return o;
+}
+
+// ---------------------------------------------------------------------------------------
+// bincode 1.3 fixint little-endian writer and the tight coefficient codec (poly.rs:166-225).
+struct Bin {
+  std::vector<uint8_t> b;
+  void u8(uint8_t v) { b.push_back(v); }
+  void u32(uint32_t v) {
+    for (int i = 0; i < 4; i++) b.push_back((uint8_t)(v >> (8 * i)));
+  }
+  void u64_(u64 v) {
+    for (int i = 0; i < 8; i++) b.push_back((uint8_t)(v >> (8 * i)));
+  }
+  void bytes(const std::vector<uint8_t>& v) {
+    u64_(v.size());
+    b.insert(b.end(), v.begin(), v.end());
+  }
+};
+
+static std::vector<uint8_t> pack_tight(const u64* c, size_t count, u64 modulus) {
+  unsigned bits = 64 - clz64(modulus - 1);
+  size_t nbytes = (count * bits + 7) / 8;
+  std::vector<uint8_t> out(nbytes, 0);
+  for (size_t i = 0; i < count; i++) {
+    size_t bit = i * bits;
+    u128 v = (u128)c[i] << (bit % 8);
+    size_t by = bit / 8;
+    for (size_t k = 0; k < 10 && by + k < nbytes; k++) out[by + k] |= (uint8_t)(v >> (8 * k));
+  }
+  return out;
+}
+
+static void write_poly(Bin& w, const Vec& c, u64 modulus) {
+  w.bytes(pack_tight(c.data(), c.size(), modulus));
+  w.u64_(1);
+  w.u64_(modulus);
+  w.u64_(modulus);  // q = product of the one modulus
+  w.u64_(c.size());
+  w.u64_(0);  // crt_q0_inv_mod_q1
+  w.u8(0);    // is_ntt
+}
+
+// ServerResponse tight wire (respond.rs:111-176): Packed{a, b_prefix, retained}, no
+// column ciphertexts, Some(PackingMode::Inspiring).
+static std::vector<uint8_t> response_bytes(const Vec& a, const Vec& b, size_t retained, u64 modulus) {
+  Bin w;
+  w.u32(1);
+  write_poly(w, a, modulus);
+  w.bytes(pack_tight(b.data(), retained, modulus));
+  w.u32((uint32_t)retained);
+  w.u64_(0);
+  w.u8(1);
+  w.u32(0);
+  return w.b;
+}
+
+static std::vector<uint8_t> key_bytes(const std::vector<Vec>& y_body, size_t gamma, u64 modulus) {
+  Bin w;
+  w.u64_(y_body.size());
+  for (auto& y : y_body) write_poly(w, y, modulus);
+  w.u64_(0);
+  w.u8(0);
+  w.u64_(gamma);
+  return w.b;
+}
+
+// ---------------------------------------------------------------------------------------
+// Client-side regeneration of KAT inputs.
+
+static Vec sample_gaussian_poly(GaussianSampler& g, size_t n, u64 q) {
+  Vec c(n);
+  for (size_t i = 0; i < n; i++) c[i] = from_signed(g.sample(), q);
+  return c;
+}
+
+// apply_automorphism in the coefficient domain (rlwe/galois.rs:12-45).
+static Vec automorphism_coeff(const Vec& p, u64 g, u64 q) {
+  size_t d = p.size();
+  Vec r(d, 0);
+  for (size_t i = 0; i < d; i++) {
+    size_t idx = (size_t)((g * i) % (2 * d));
+    if (idx < d)
+      r[idx] = addmod(r[idx], p[i], q);
+    else
+      r[idx - d] = submod(r[idx - d], p[i], q);
+  }
+  return r;
+}
+
+// inverse_monomial (encode_db.rs:43-70): X^(-k) in Z_q[X]/(X^d + 1).
+static Vec inverse_monomial(size_t k, size_t d, u64 q) {
+  Vec c(d, 0);
+  k %= 2 * d;
+  if (k == 0)
+    c[0] = 1;
+  else if (k <= d)
+    c[d - k] = q - 1;
+  else
+    c[2 * d - k] = 1;
+  return c;
+}
+
+// Poly::from_seed_moduli (poly.rs:657-686): ChaCha20 from the seed, gen_range(0..q) per coeff.
+static Vec expand_seed(const uint8_t seed[32], size_t n, u64 q) {
+  ChaCha20Rng rng = ChaCha20Rng::from_seed(seed);
+  Vec c(n);
+  for (size_t i = 0; i < n; i++) c[i] = gen_range_u64(rng, 0, q);
+  return c;
+}
+
+struct Cell {
+  Params P;
+  size_t entry_size, gamma, num_shards;
+  std::vector<uint8_t> db;
+  uint8_t w_seed[32];
+  std::shared_ptr<PackParams> pp;
+  OfflineKeys keys;
+  std::vector<std::vector<Vec>> shards;  // [shard][column] coefficient form
+  Vec sk;
+  std::vector<Vec> y_body;
+  GaussianSampler sampler;
+  ChaCha20Rng rng;
+  std::vector<std::unique_ptr<Store>> stores;
+};
+
+static size_t num_columns(size_t entry) { return entry == 0 ? 1 : (entry + 1) / 2; }
+
+static Cell* cell_build(const Params& P, size_t entry_size, u64 seed, size_t entries) {
+  auto* c = new Cell();
+  c->P = P;
+  c->entry_size = entry_size;
+  size_t n = P.n;
+  // tests/packing_key_fixture/mod.rs:65-69 database formula.
+  c->db.resize(entries * entry_size);
+  for (size_t i = 0; i < c->db.size(); i++) c->db[i] = (uint8_t)(((u64)i * 0x9E3779B9ull + seed) >> 7);
+  c->sampler = GaussianSampler::with_seed(P.sigma, seed);
+  c->rng = ChaCha20Rng::seed_from_u64(seed ^ 0x5eed);
+  // setup_with_rng (pir/setup.rs:408-495): secret key, then one error polynomial per
+  // Galois-key row (their `a` come from OS entropy and never reach a response), then the
+  // two public seeds.
+  c->sk = sample_gaussian_poly(c->sampler, n, P.q);
+  size_t log_d = 0;
+  while ((size_t(1) << (log_d + 1)) <= n) log_d++;
+  for (size_t i = 0; i < log_d; i++)
+    for (size_t r = 0; r < P.gadget_len; r++)
+      for (size_t k = 0; k < n; k++) c->sampler.sample();
+  c->rng.fill_bytes(c->w_seed, 32);
+  uint8_t v_seed[32];
+  c->rng.fill_bytes(v_seed, 32);
+  c->gamma = num_columns(entry_size);
+  c->pp = make_pack_params(P, c->gamma);
+  c->keys = make_offline_keys(*c->pp, c->w_seed);
+  // encode_database (encode_db.rs:74-134): one record per coefficient, 16-bit columns.
+  size_t total = c->db.size() / entry_size;
+  c->num_shards = (total + n - 1) / n;
+  for (size_t s = 0; s < c->num_shards; s++) {
+    std::vector<Vec> cols(c->gamma, Vec(n, 0));
+    for (size_t col = 0; col < c->gamma; col++)
+      for (size_t l = 0; l < n && s * n + l < total; l++) {
+        const uint8_t* e = &c->db[(s * n + l) * entry_size];
+        size_t off = col * 2;
+        u64 v = 0;
+        if (off + 1 < entry_size)
+          v = (u64)e[off] | ((u64)e[off + 1] << 8);
+        else if (off < entry_size)
+          v = e[off];
+        cols[col][l] = v % P.q;
+      }
+    c->shards.push_back(cols);
+  }
+  // ClientSession::new -> ClientPackingKeys::generate_once (inspiring2.rs:764-791) and
+  // generate_ksk_body (893-929).
+  const Ntt& ntt = *c->pp->ntt;
+  u64 gen = c->pp->generator % (2 * n);
+  Vec tau_s = automorphism_coeff(c->sk, gen, P.q);
+  for (size_t row = 0; row < c->keys.w_mask.size(); row++) {
+    u64 gp = gadget_power(P, P.dropped() + row);
+    Vec s_w = ntt.mul(c->sk, c->keys.w_mask[row]);
+    Vec e = sample_gaussian_poly(c->sampler, n, P.q);
+    Vec y(n);
+    for (size_t i = 0; i < n; i++) y[i] = addmod(addmod(mulmod(tau_s[i], gp, P.q), (P.q - s_w[i]) % P.q, P.q), e[i], P.q);
+    c->y_body.push_back(y);
+  }
+  // The probe query_seeded(0): its `a` seed is OS entropy, its error draws n samples.
+  for (size_t k = 0; k < n; k++) c->sampler.sample();
+  c->stores.resize(c->num_shards);
+  return c;
+}
+
+// Cell::next_query (tests/packing_key_fixture/mod.rs:126-146) with
+// SeededRgswCiphertext::encrypt_with_rng (rgsw/types.rs:345-388).
+static void cell_next_query(Cell* c, u64 index, uint32_t* shard_id, uint8_t seed[32], u64* b_out) {
+  const Params& P = c->P;
+  size_t n = P.n;
+  *shard_id = (uint32_t)(index / n);
+  size_t local = (size_t)(index % n);
+  Vec scaled = inverse_monomial(local, n, P.q);
+  for (auto& x : scaled) x = mulmod(x, P.delta(), P.q);
+  c->rng.fill_bytes(seed, 32);
+  Vec a = expand_seed(seed, n, P.q);
+  Vec e = sample_gaussian_poly(c->sampler, n, P.q);
+  Vec as = c->pp->ntt->mul(a, c->sk);
+  for (size_t i = 0; i < n; i++) b_out[i] = addmod(addmod((P.q - as[i]) % P.q, e[i], P.q), scaled[i], P.q);
+}
+
+// extract_inspiring (pir/extract.rs:229-263): decrypt, round, reassemble the record.
+static bool cell_decode(const Cell* c, u64 index, const u64* a, const u64* b, uint8_t* record_out) {
+  const Params& P = c->P;
+  size_t n = P.n;
+  Vec av(a, a + n);
+  Vec as = c->pp->ntt->mul(av, c->sk);
+  u64 delta = P.delta();
+  std::vector<u64> vals;
+  for (size_t col = 0; col < c->gamma; col++) {
+    u64 noisy = addmod(as[col], b[col], P.q);
+    u128 num = (u128)noisy + delta / 2;
+    vals.push_back((u64)(num / delta) % P.p);
+  }
+  std::vector<uint8_t> entry(c->entry_size, 0);
+  for (size_t col = 0; col < vals.size(); col++) {
+    size_t off = col * 2;
+    if (off < c->entry_size) entry[off] = (uint8_t)(vals[col] & 0xff);
+    if (off + 1 < c->entry_size) entry[off + 1] = (uint8_t)((vals[col] >> 8) & 0xff);
+  }
+  memcpy(record_out, entry.data(), entry.size());
+  return memcmp(entry.data(), &c->db[index * c->entry_size], c->entry_size) == 0;
+}
+
+}  // namespace orc
+
+// =======================================================================================
+// C API for the Python test harness (ctypes).
+using namespace orc;
+
+struct OrcCache {
+  std::shared_ptr<PackParams> pp;
+  OfflineKeys keys;
+};
+
+static Params make_params(u64 n, u64 q, u64 p, double sigma, u64 base, u64 glen, int approx) {
+  Params P;
+  P.n = n;
+  P.q = q;
+  P.p = p;
+  P.sigma = sigma;
+  P.gadget_base = base;
+  P.gadget_len = glen;
+  P.approx = approx != 0;
+  return P;
+}
+
+static thread_local std::string g_err;
+
+extern "C" {
+
+const char* orc_last_error() { return g_err.c_str(); }
+
+void orc_set_threads(int t) { omp_set_num_threads(t); }
+int orc_max_threads() { return omp_get_max_threads(); }
+
+u64 orc_fnv1a(const uint8_t* p, size_t n) { return fnv1a(p, n); }
+
+// FNV-1a of `count` Gaussian samples (i64 LE) from GaussianSampler::with_seed(sigma, seed):
+// the reference pins these streams in src/math/gaussian.rs:335-351.
+u64 orc_gaussian_stream_fnv(double sigma, u64 seed, u64 count) {
+  GaussianSampler g = GaussianSampler::with_seed(sigma, seed);
+  u64 h = 0xcbf29ce484222325ULL;
+  for (u64 i = 0; i < count; i++) {
+    i64 x = g.sample();
+    for (int k = 0; k < 8; k++) {
+      h ^= (uint8_t)((u64)x >> (8 * k));
+      h *= 0x00000100000001b3ULL;
+    }
+  }
+  return h;
+}
+
+void orc_expand_seed(const uint8_t* seed, u64 n, u64 q, u64* out) {
+  Vec a = expand_seed(seed, n, q);
+  memcpy(out, a.data(), n * 8);
+}
+
+void orc_chacha_u64s(const uint8_t* seed, u64 stream, u64 count, u64* out) {
+  ChaCha20Rng r = ChaCha20Rng::from_seed(seed);
+  r.set_stream(stream);
+  for (u64 i = 0; i < count; i++) out[i] = r.next_u64();
+}
+
+// NTT of one polynomial, Montgomery-form output, exactly as NttContext::forward.
+int orc_ntt_forward(u64 n, u64 q, u64* c) {
+  try {
+    Ntt ntt(n, q);
+    ntt.forward(c);
+    return 0;
+  } catch (std::exception& e) {
+    g_err = e.what();
+    return -1;
+  }
+}
+int orc_ntt_inverse(u64 n, u64 q, u64* c) {
+  try {
+    Ntt ntt(n, q);
+    ntt.inverse(c);
+    return 0;
+  } catch (std::exception& e) {
+    g_err = e.what();
+    return -1;
+  }
+}
+
+void* orc_cache_new(u64 n, u64 q, u64 p, double sigma, u64 base, u64 glen, int approx, u64 gamma,
+                    const uint8_t* w_seed) {
+  try {
+    auto* c = new OrcCache();
+    c->pp = make_pack_params(make_params(n, q, p, sigma, base, glen, approx), gamma);
+    c->keys = make_offline_keys(*c->pp, w_seed);
+    return c;
+  } catch (std::exception& e) {
+    g_err = e.what();
+    return nullptr;
+  }
+}
+void orc_cache_free(void* c) { delete (OrcCache*)c; }
+
+// Slot tables the path reads: out[i*n + t] = source slot of t under tau_{g^i}, i < gamma.
+void orc_cache_tables(void* cv, uint32_t* out) {
+  auto* c = (OrcCache*)cv;
+  size_t n = c->pp->P.n;
+  for (size_t i = 0; i < c->pp->gamma; i++) {
+    const auto& tb = c->pp->table(c->pp->gen_pows[i]);
+    memcpy(out + i * n, tb.data(), n * 4);
+  }
+}
+
+// Offline key rotations in Montgomery NTT form: out[((i*rows)+k)*n + t].
+void orc_cache_w_all_ntt(void* cv, u64* out) {
+  auto* c = (OrcCache*)cv;
+  size_t n = c->pp->P.n, rows = c->pp->P.key_rows();
+  for (size_t i = 0; i + 1 < c->pp->gamma; i++)
+    for (size_t k = 0; k < rows; k++) memcpy(out + (i * rows + k) * n, c->keys.w_all_ntt[i][k].data(), n * 8);
+}
+
+static std::vector<Vec> unpack_polys(const u64* p, size_t count, size_t n) {
+  std::vector<Vec> v;
+  for (size_t i = 0; i < count; i++) v.push_back(Vec(p + i * n, p + (i + 1) * n));
+  return v;
+}
+
+// pack_shard on the per-query branch (no store). a is the expanded query `a` (coefficient
+// form); columns gamma x n; y_body key_rows x n (coefficient form).
+int orc_respond_per_query(void* cv, const u64* columns, const u64* a, const u64* b, const u64* y_body,
+                          u64* a_out, u64* b_out) {
+  auto* c = (OrcCache*)cv;
+  size_t n = c->pp->P.n;
+  try {
+    Packed r = pack_per_query(*c->pp, c->keys, unpack_polys(columns, c->pp->gamma, n), Vec(a, a + n), Vec(b, b + n),
+                              unpack_polys(y_body, c->pp->P.key_rows(), n));
+    memcpy(a_out, r.a.data(), n * 8);
+    memcpy(b_out, r.b.data(), n * 8);
+    return 0;
+  } catch (std::exception& e) {
+    g_err = e.what();
+    return -1;
+  }
+}
+
+struct OrcStore {
+  Store s;
+  std::vector<Vec> columns;  // the columns as the shard holds them now
+};
+
+void* orc_store_build(void* cv, const u64* columns, u64 key_seed) {
+  auto* c = (OrcCache*)cv;
+  auto* st = new OrcStore();
+  st->columns = unpack_polys(columns, c->pp->gamma, c->pp->P.n);
+  st->s = build_store(*c->pp, st->columns, key_seed);
+  return st;
+}
+void orc_store_free(void* s) { delete (OrcStore*)s; }
+
+// Step-1 sums in Montgomery NTT form: out[i*n + t].
+void orc_store_sums(void* cv, void* sv, u64* out) {
+  auto* c = (OrcCache*)cv;
+  auto* st = (OrcStore*)sv;
+  size_t n = c->pp->P.n;
+  for (size_t i = 0; i < c->pp->gamma; i++) memcpy(out + i * n, st->s.column_sums_ntt[i].data(), n * 8);
+}
+
+// Store branch of pack_shard against `columns` (the live columns). Returns 1 when the tag
+// check refuses the columns.
+int orc_respond_store(void* cv, void* sv, const u64* columns, const u64* a, const u64* b, const u64* y_body,
+                      u64* a_out, u64* b_out) {
+  auto* c = (OrcCache*)cv;
+  auto* st = (OrcStore*)sv;
+  size_t n = c->pp->P.n;
+  Packed r;
+  if (!pack_with_store(*c->pp, c->keys, st->s, unpack_polys(columns, c->pp->gamma, n), Vec(a, a + n),
+                       Vec(b, b + n), unpack_polys(y_body, c->pp->P.key_rows(), n), r))
+    return 1;
+  memcpy(a_out, r.a.data(), n * 8);
+  memcpy(b_out, r.b.data(), n * 8);
+  return 0;
+}
+
+// Scan only: tags check + b fold. Returns 1 on a tag mismatch.
+int orc_store_scan(void* cv, void* sv, const u64* columns, const u64* b, u64* b_poly_out) {
+  auto* c = (OrcCache*)cv;
+  auto* st = (OrcStore*)sv;
+  size_t n = c->pp->P.n;
+  Vec bp;
+  bool ok = check_and_fold_b(*c->pp, st->s, unpack_polys(columns, c->pp->gamma, n), Vec(b, b + n), bp);
+  memcpy(b_poly_out, bp.data(), n * 8);
+  return ok ? 0 : 1;
+}
+
+void orc_mod_switch(const u64* c, u64 count, u64 q_old, u64 q_new, u64* out) {
+  Vec r = mod_switch(Vec(c, c + count), q_old, q_new);
+  memcpy(out, r.data(), count * 8);
+}
+
+// ServerResponse bytes for coefficient-form (a, b) over `modulus`; returns the length and
+// writes at most `cap` bytes.
+u64 orc_response_bytes(const u64* a, const u64* b, u64 n, u64 retained, u64 modulus, uint8_t* out, u64 cap) {
+  auto v = response_bytes(Vec(a, a + n), Vec(b, b + n), retained, modulus);
+  if (out) memcpy(out, v.data(), std::min<u64>(cap, v.size()));
+  return v.size();
+}
+
+// -- KAT cells --------------------------------------------------------------------------
+void* orc_cell_build(u64 n, u64 q, u64 p, double sigma, u64 base, u64 glen, int approx, u64 entry_size, u64 seed,
+                     u64 entries) {
+  try {
+    return cell_build(make_params(n, q, p, sigma, base, glen, approx), entry_size, seed, entries);
+  } catch (std::exception& e) {
+    g_err = e.what();
+    return nullptr;
+  }
+}
+void orc_cell_free(void* c) { delete (Cell*)c; }
+void orc_cell_info(void* cv, u64* gamma, u64* num_shards, u64* key_rows, uint8_t* w_seed) {
+  auto* c = (Cell*)cv;
+  *gamma = c->gamma;
+  *num_shards = c->num_shards;
+  *key_rows = c->P.key_rows();
+  memcpy(w_seed, c->w_seed, 32);
+}
+void orc_cell_columns(void* cv, u64 shard, u64* out) {
+  auto* c = (Cell*)cv;
+  for (size_t j = 0; j < c->gamma; j++) memcpy(out + j * c->P.n, c->shards[shard][j].data(), c->P.n * 8);
+}
+void orc_cell_keys(void* cv, u64* out) {
+  auto* c = (Cell*)cv;
+  for (size_t k = 0; k < c->y_body.size(); k++) memcpy(out + k * c->P.n, c->y_body[k].data(), c->P.n * 8);
+}
+void orc_cell_secret(void* cv, u64* out) {
+  auto* c = (Cell*)cv;
+  memcpy(out, c->sk.data(), c->P.n * 8);
+}
+u64 orc_cell_key_bytes(void* cv, uint8_t* out, u64 cap) {
+  auto* c = (Cell*)cv;
+  auto v = key_bytes(c->y_body, c->gamma, c->P.q);
+  if (out) memcpy(out, v.data(), std::min<u64>(cap, v.size()));
+  return v.size();
+}
+void orc_cell_next_query(void* cv, u64 index, uint32_t* shard_id, uint8_t* seed, u64* b_out) {
+  cell_next_query((Cell*)cv, index, shard_id, seed, b_out);
+}
+int orc_cell_decode(void* cv, u64 index, const u64* a, const u64* b, uint8_t* record_out) {
+  return cell_decode((const Cell*)cv, index, a, b, record_out) ? 1 : 0;
+}
+void orc_cell_record(void* cv, u64 index, uint8_t* out) {
+  auto* c = (Cell*)cv;
+  memcpy(out, &c->db[index * c->entry_size], c->entry_size);
+}
+
+}  // extern "C"

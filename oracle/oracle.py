@@ -1,0 +1,292 @@
+"""ctypes front of the CPU oracle (test infrastructure only).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU legs import this module, as the
+checker and the timed CPU baseline. The product package never imports it.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+
+DEFAULT_Q = 1152921504606830593
+MOD_SWITCH_TARGET_36BIT = 68_718_428_161
+
+_u64p = ctypes.POINTER(ctypes.c_uint64)
+_u8p = ctypes.POINTER(ctypes.c_uint8)
+_u32p = ctypes.POINTER(ctypes.c_uint32)
+_lib = None
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = ctypes.CDLL(LIB_PATH)
+        V, P, U64, I = ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int
+        sig = {
+            "orc_last_error": (ctypes.c_char_p, []),
+            "orc_set_threads": (None, [I]),
+            "orc_max_threads": (I, []),
+            "orc_fnv1a": (U64, [P, U64]),
+            "orc_gaussian_stream_fnv": (U64, [ctypes.c_double, U64, U64]),
+            "orc_expand_seed": (None, [P, U64, U64, P]),
+            "orc_chacha_u64s": (None, [P, U64, U64, P]),
+            "orc_ntt_forward": (I, [U64, U64, P]),
+            "orc_ntt_inverse": (I, [U64, U64, P]),
+            "orc_cache_new": (V, [U64, U64, U64, ctypes.c_double, U64, U64, I, U64, P]),
+            "orc_cache_free": (None, [V]),
+            "orc_cache_tables": (None, [V, P]),
+            "orc_cache_w_all_ntt": (None, [V, P]),
+            "orc_respond_per_query": (I, [V, P, P, P, P, P, P]),
+            "orc_store_build": (V, [V, P, U64]),
+            "orc_store_free": (None, [V]),
+            "orc_store_sums": (None, [V, V, P]),
+            "orc_respond_store": (I, [V, V, P, P, P, P, P, P]),
+            "orc_store_scan": (I, [V, V, P, P, P]),
+            "orc_mod_switch": (None, [P, U64, U64, U64, P]),
+            "orc_response_bytes": (U64, [P, P, U64, U64, U64, P, U64]),
+            "orc_cell_build": (V, [U64, U64, U64, ctypes.c_double, U64, U64, I, U64, U64, U64]),
+            "orc_cell_free": (None, [V]),
+            "orc_cell_info": (None, [V, P, P, P, P]),
+            "orc_cell_columns": (None, [V, U64, P]),
+            "orc_cell_keys": (None, [V, P]),
+            "orc_cell_secret": (None, [V, P]),
+            "orc_cell_key_bytes": (U64, [V, P, U64]),
+            "orc_cell_next_query": (None, [V, U64, P, P, P]),
+            "orc_cell_decode": (I, [V, U64, P, P, P]),
+            "orc_cell_record": (None, [V, U64, P]),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def fnv1a(b: bytes) -> int:
+    arr = np.frombuffer(b, dtype=np.uint8)
+    return lib().orc_fnv1a(_p(arr), len(b))
+
+
+class Params:
+    """Single-prime InspireParams (params.rs:137-196 of the reference)."""
+
+    def __init__(self, n=2048, q=DEFAULT_Q, p=65537, sigma=6.4, gadget_base=1 << 20, gadget_len=3,
+                 approx=False):
+        self.n, self.q, self.p, self.sigma = n, q, p, sigma
+        self.gadget_base, self.gadget_len, self.approx = gadget_base, gadget_len, approx
+
+    @property
+    def key_rows(self):
+        return self.gadget_len - (1 if self.approx else 0)
+
+    def args(self):
+        return (self.n, self.q, self.p, self.sigma, self.gadget_base, self.gadget_len, int(self.approx))
+
+    @staticmethod
+    def d2048():
+        return Params()
+
+    @staticmethod
+    def d2048_approximate_gadget():
+        return Params(approx=True)
+
+
+class Cache:
+    """PackParams + OfflinePackingKeys for (params, gamma, w_seed)."""
+
+    def __init__(self, params: Params, gamma: int, w_seed: bytes):
+        self.params, self.gamma = params, gamma
+        seed = np.frombuffer(bytes(w_seed), dtype=np.uint8).copy()
+        self.h = lib().orc_cache_new(*params.args(), gamma, _p(seed))
+        if not self.h:
+            raise RuntimeError(lib().orc_last_error().decode())
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_cache_free(self.h)
+
+    def tables(self):
+        out = np.zeros((self.gamma, self.params.n), dtype=np.uint32)
+        lib().orc_cache_tables(self.h, _p(out))
+        return out
+
+    def w_all_ntt(self):
+        out = np.zeros((self.gamma - 1, self.params.key_rows, self.params.n), dtype=np.uint64)
+        lib().orc_cache_w_all_ntt(self.h, _p(out))
+        return out
+
+    def respond_per_query(self, columns, a, b, y_body):
+        n = self.params.n
+        columns = np.ascontiguousarray(columns, dtype=np.uint64)
+        a = np.ascontiguousarray(a, dtype=np.uint64)
+        b = np.ascontiguousarray(b, dtype=np.uint64)
+        y = np.ascontiguousarray(y_body, dtype=np.uint64)
+        ao = np.zeros(n, dtype=np.uint64)
+        bo = np.zeros(n, dtype=np.uint64)
+        rc = lib().orc_respond_per_query(self.h, _p(columns), _p(a), _p(b), _p(y), _p(ao), _p(bo))
+        if rc:
+            raise RuntimeError(lib().orc_last_error().decode())
+        return ao, bo
+
+
+class Store:
+    """ShardPackingStore restated: step-1 sums + tags over one shard's columns."""
+
+    def __init__(self, cache: Cache, columns, key_seed=0x7A6):
+        self.cache = cache
+        cols = np.ascontiguousarray(columns, dtype=np.uint64)
+        self.h = lib().orc_store_build(cache.h, _p(cols), key_seed)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_store_free(self.h)
+
+    def sums(self):
+        out = np.zeros((self.cache.gamma, self.cache.params.n), dtype=np.uint64)
+        lib().orc_store_sums(self.cache.h, self.h, _p(out))
+        return out
+
+    def respond(self, columns, a, b, y_body):
+        n = self.cache.params.n
+        cols = np.ascontiguousarray(columns, dtype=np.uint64)
+        a = np.ascontiguousarray(a, dtype=np.uint64)
+        b = np.ascontiguousarray(b, dtype=np.uint64)
+        y = np.ascontiguousarray(y_body, dtype=np.uint64)
+        ao = np.zeros(n, dtype=np.uint64)
+        bo = np.zeros(n, dtype=np.uint64)
+        rc = lib().orc_respond_store(self.cache.h, self.h, _p(cols), _p(a), _p(b), _p(y), _p(ao), _p(bo))
+        if rc:
+            raise ValueError("packing store refused: a column is not the column the store was built from")
+        return ao, bo
+
+    def scan(self, columns, b):
+        n = self.cache.params.n
+        cols = np.ascontiguousarray(columns, dtype=np.uint64)
+        b = np.ascontiguousarray(b, dtype=np.uint64)
+        out = np.zeros(n, dtype=np.uint64)
+        rc = lib().orc_store_scan(self.cache.h, self.h, _p(cols), _p(b), _p(out))
+        return rc == 0, out
+
+
+def expand_seed(seed: bytes, n: int, q: int = DEFAULT_Q):
+    s = np.frombuffer(bytes(seed), dtype=np.uint8).copy()
+    out = np.zeros(n, dtype=np.uint64)
+    lib().orc_expand_seed(_p(s), n, q, _p(out))
+    return out
+
+
+def chacha_u64s(seed: bytes, stream: int, count: int):
+    s = np.frombuffer(bytes(seed), dtype=np.uint8).copy()
+    out = np.zeros(count, dtype=np.uint64)
+    lib().orc_chacha_u64s(_p(s), stream, count, _p(out))
+    return out
+
+
+def ntt_forward(c, q=DEFAULT_Q):
+    c = np.array(c, dtype=np.uint64)
+    if lib().orc_ntt_forward(len(c), q, _p(c)):
+        raise RuntimeError(lib().orc_last_error().decode())
+    return c
+
+
+def ntt_inverse(c, q=DEFAULT_Q):
+    c = np.array(c, dtype=np.uint64)
+    if lib().orc_ntt_inverse(len(c), q, _p(c)):
+        raise RuntimeError(lib().orc_last_error().decode())
+    return c
+
+
+def mod_switch(c, q_old=DEFAULT_Q, q_new=MOD_SWITCH_TARGET_36BIT):
+    c = np.ascontiguousarray(c, dtype=np.uint64)
+    out = np.zeros_like(c)
+    lib().orc_mod_switch(_p(c), len(c), q_old, q_new, _p(out))
+    return out
+
+
+def response_bytes(a, b, retained, modulus=DEFAULT_Q) -> bytes:
+    a = np.ascontiguousarray(a, dtype=np.uint64)
+    b = np.ascontiguousarray(b, dtype=np.uint64)
+    L = lib().orc_response_bytes(_p(a), _p(b), len(a), retained, modulus, None, 0)
+    out = np.zeros(L, dtype=np.uint8)
+    lib().orc_response_bytes(_p(a), _p(b), len(a), retained, modulus, _p(out), L)
+    return out.tobytes()
+
+
+class Cell:
+    """A KAT cell: database, setup, client session and the reproducible query stream of the
+    reference's tests/packing_key_fixture/mod.rs:90-146."""
+
+    def __init__(self, params: Params, entry_size: int, seed: int, entries=None):
+        self.params, self.entry_size, self.seed = params, entry_size, seed
+        entries = 3 * params.n if entries is None else entries
+        self.h = lib().orc_cell_build(*params.args(), entry_size, seed, entries)
+        if not self.h:
+            raise RuntimeError(lib().orc_last_error().decode())
+        g, ns, kr = (ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64())
+        w = np.zeros(32, dtype=np.uint8)
+        lib().orc_cell_info(self.h, ctypes.byref(g), ctypes.byref(ns), ctypes.byref(kr), _p(w))
+        self.gamma, self.num_shards, self.key_rows = g.value, ns.value, kr.value
+        self.w_seed = w.tobytes()
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_cell_free(self.h)
+
+    def columns(self, shard):
+        out = np.zeros((self.gamma, self.params.n), dtype=np.uint64)
+        lib().orc_cell_columns(self.h, shard, _p(out))
+        return out
+
+    def keys(self):
+        out = np.zeros((self.key_rows, self.params.n), dtype=np.uint64)
+        lib().orc_cell_keys(self.h, _p(out))
+        return out
+
+    def secret(self):
+        out = np.zeros(self.params.n, dtype=np.uint64)
+        lib().orc_cell_secret(self.h, _p(out))
+        return out
+
+    def key_bytes(self) -> bytes:
+        L = lib().orc_cell_key_bytes(self.h, None, 0)
+        out = np.zeros(L, dtype=np.uint8)
+        lib().orc_cell_key_bytes(self.h, _p(out), L)
+        return out.tobytes()
+
+    def next_query(self, index):
+        sid = ctypes.c_uint32()
+        seed = np.zeros(32, dtype=np.uint8)
+        b = np.zeros(self.params.n, dtype=np.uint64)
+        lib().orc_cell_next_query(self.h, index, ctypes.byref(sid), _p(seed), _p(b))
+        return sid.value, seed.tobytes(), b
+
+    def decode(self, index, a, b):
+        a = np.ascontiguousarray(a, dtype=np.uint64)
+        b = np.ascontiguousarray(b, dtype=np.uint64)
+        rec = np.zeros(self.entry_size, dtype=np.uint8)
+        ok = lib().orc_cell_decode(self.h, index, _p(a), _p(b), _p(rec))
+        return bool(ok), rec.tobytes()
+
+    def record(self, index):
+        out = np.zeros(self.entry_size, dtype=np.uint8)
+        lib().orc_cell_record(self.h, index, _p(out))
+        return out.tobytes()
+
+
+def gaussian_stream_fnv(sigma, seed, count):
+    return lib().orc_gaussian_stream_fnv(sigma, seed, count)
