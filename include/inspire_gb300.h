@@ -1,0 +1,157 @@
+/* inspire_gb300.h — C ABI of the GB300-native InsPIRe respond path.
+ *
+ * One shared library (libinspire_gb300.so) exposes the server respond path of
+ * raven-inspire (hisoka-io/inspire-rs) to any host language over plain pointers and
+ * sizes. Each entry point names the reference interface it replaces (file:line in the
+ * reference crate). All polynomials are arrays of ring_dim u64 coefficients in
+ * coefficient form; multi-polynomial arguments are row-major (row r at offset r*ring_dim).
+ *
+ * Errors: every call returns IG_OK (0) or an IG_ERR_* code, and stores an actionable
+ * message retrievable with ig_last_error(). A refused batch produces no partial output
+ * (respond.rs:1187). Device faults are never used to signal refusals: kernels report
+ * through status words the host reads back.
+ *
+ * Threading: a context serialises its calls internally; distinct contexts may be used
+ * from distinct threads. Handles (CRS, database, session store, seat) are owned by the
+ * context that made them and freed with the matching *_destroy / ig_seat_remove.
+ */
+#ifndef INSPIRE_GB300_H
+#define INSPIRE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum ig_status {
+  IG_OK = 0,
+  IG_ERR_ARG = 1,           /* null pointer, zero count, bad size */
+  IG_ERR_SHAPE = 2,         /* wire shape refused: ring, moduli, row count (respond.rs:409-611) */
+  IG_ERR_WIDTH = 3,         /* packing width / key width mismatch (session.rs:766-826) */
+  IG_ERR_HANDLE = 4,        /* unknown CRS/db/store/seat handle (respond.rs:1117-1134) */
+  IG_ERR_STORE_REFUSED = 5, /* columns differ from the store's (shard_store.rs:247-257) */
+  IG_ERR_CUDA = 6,          /* CUDA runtime error */
+  IG_ERR_UNSUPPORTED = 7,   /* parameter set outside what the GPU path serves */
+  IG_ERR_NOMEM = 8,         /* device allocation failed (admission refused) */
+  IG_ERR_DEVICE = 9,        /* a kernel reported an internal status */
+  IG_ERR_EXHAUSTED = 10     /* handle space exhausted (session.rs:722-737) */
+};
+
+typedef struct ig_ctx ig_ctx;
+
+/* ---- context ------------------------------------------------------------------------ */
+int ig_ctx_create(int device, ig_ctx** out);
+void ig_ctx_destroy(ig_ctx* ctx);
+/* Copies the last error message of this context (NUL-terminated, truncated to len). */
+int ig_last_error(const ig_ctx* ctx, char* buf, size_t len);
+/* The CUDA stream (cudaStream_t) every kernel of this context is launched on. */
+void* ig_ctx_stream(ig_ctx* ctx);
+/* Device bytes held by this context's objects (stores, shards, seats, scratch). */
+uint64_t ig_ctx_device_bytes(const ig_ctx* ctx);
+
+/* ---- CRS / ServerInspiringCache ------------------------------------------------------
+ * Replaces ServerInspiringCache::new (respond.rs:926-941) = PackParams::try_new
+ * (inspiring2.rs:171-183, 209-286) + OfflinePackingKeys::generate (537-598): builds the
+ * twiddle ladders, slot tables and the w_seed mask rows on the device once per
+ * (params, gamma, w_seed). Supported: q = 2^60-2^14+1 single prime, gadget base 2^20,
+ * packing gadget length 3, ring_dim 256..2048, gamma a power of two <= ring_dim/2. */
+int ig_crs_create(ig_ctx* ctx, uint32_t ring_dim, uint64_t q, uint64_t p, uint64_t gadget_base,
+                  uint32_t packing_gadget_len, int approximate_packing_gadget, uint32_t gamma,
+                  const uint8_t w_seed[32], uint64_t* crs_out);
+int ig_crs_destroy(ig_ctx* ctx, uint64_t crs);
+/* Packing-key rows the CRS expects: InspireParams::packing_key_rows (params.rs:484-487). */
+int ig_crs_key_rows(ig_ctx* ctx, uint64_t crs, uint32_t* rows_out);
+
+/* ---- EncodedDatabase / ShardData ----------------------------------------------------
+ * A device-resident database of num_shards shards of gamma column polynomials
+ * (EncodedDatabase, setup.rs:272-289). Columns hold raw u64 words as encode_database
+ * produced them (encode_db.rs:74-134); words >= q are served as their residue. */
+int ig_db_create(ig_ctx* ctx, uint64_t crs, uint32_t num_shards, uint64_t* db_out);
+int ig_db_destroy(ig_ctx* ctx, uint64_t db);
+/* Uploads (or replaces) shard `shard_id`'s gamma x ring_dim columns. Replacing columns
+ * keeps any store, which the next respond then refuses (shard_store.rs:247-257). */
+int ig_db_set_shard(ig_ctx* ctx, uint64_t db, uint32_t shard_id, const uint64_t* columns);
+/* Same, from a device pointer (columns already in HBM). */
+int ig_db_set_shard_device(ig_ctx* ctx, uint64_t db, uint32_t shard_id, const uint64_t* d_columns);
+/* ShardData::precompute_packing (setup.rs:335-340) -> ShardPackingStore::build
+ * (shard_store.rs:86-156): step-1 sums in HBM plus keyed column tags. */
+int ig_db_precompute_packing(ig_ctx* ctx, uint64_t db, uint32_t shard_id);
+/* All shards at once (the serving bring-up). */
+int ig_db_precompute_packing_all(ig_ctx* ctx, uint64_t db);
+/* ShardData::drop_packing_store (setup.rs:372-375). */
+int ig_db_drop_packing_store(ig_ctx* ctx, uint64_t db, uint32_t shard_id);
+/* 1 when the shard has a store (ShardData::packing_store, setup.rs:367-369). */
+int ig_db_has_store(ig_ctx* ctx, uint64_t db, uint32_t shard_id, int* out);
+
+/* ---- ServerSessionStore ---------------------------------------------------------------
+ * session.rs:700-895. Handles come from one process-global monotonic counter and are
+ * never reissued. A seat keeps y_body in NTT form on the device (49,152 B at 3 rows,
+ * 32,768 B under the approximate gadget). */
+int ig_session_store_create(ig_ctx* ctx, uint64_t* store_out);
+int ig_session_store_destroy(ig_ctx* ctx, uint64_t store);
+/* ServerSessionStore::register_server_side (session.rs:848-856) via
+ * PackingKeySeat::from_wire (592-625): y_body is key_rows x ring_dim coefficient-form. */
+int ig_session_register(ig_ctx* ctx, uint64_t store, uint64_t crs, const uint64_t* y_body, uint32_t rows,
+                        uint32_t num_to_pack, uint64_t* handle_out);
+/* ServerSessionStore::remove (879-886); *removed = 1 when the handle was present. */
+int ig_session_remove(ig_ctx* ctx, uint64_t store, uint64_t handle, int* removed);
+/* ServerSessionStore::len (888-890). */
+int ig_session_len(ig_ctx* ctx, uint64_t store, uint64_t* len_out);
+/* ServerSessionStore::get (858-866) as a presence test; *present = 0/1. */
+int ig_session_contains(ig_ctx* ctx, uint64_t store, uint64_t handle, int* present);
+
+/* ---- respond ---------------------------------------------------------------------------
+ * Packing key of a call: seat `handle` from `store` (PackingKeySource::Registered), or an
+ * inline key body (PackingKeySource::Inline) when inline_y_body != NULL, which is checked
+ * into a request-scoped seat (resolve_packing_seat, respond.rs:1144-1157).
+ *
+ * ig_respond_seeded_batch replaces respond_seeded_batch (respond.rs:1189-1202): queries
+ * answered in order, all or nothing. A one-query call is respond_seeded_inspiring
+ * (respond.rs:1218-1226). Per query: shard_ids[i], seeds[32*i..] (the SeededRlweCiphertext
+ * seed of the one RGSW row) and bs[i*ring_dim..] (its b). Outputs: the packed ciphertext's
+ * a (a_out[i*ring_dim..]) and b (b_out[i*ring_dim..], the first gamma coefficients are the
+ * response's b prefix). mod_switch_target != 0 applies mod_switch_response_checked
+ * (mod_switch.rs:178-186) to both, e.g. 68718428161 (MOD_SWITCH_TARGET_36BIT). */
+int ig_respond_seeded_batch(ig_ctx* ctx, uint64_t db, uint64_t store, uint64_t handle, const uint64_t* inline_y_body,
+                            uint32_t inline_rows, uint32_t inline_num_to_pack, uint32_t count,
+                            const uint32_t* shard_ids, const uint8_t* seeds, const uint64_t* bs,
+                            uint64_t mod_switch_target, uint64_t* a_out, uint64_t* b_out);
+
+/* The unseeded form: respond_inspiring_cached_with_session over ClientQuery rows whose
+ * `a` travels in full (respond.rs:1053-1091); as[i*ring_dim..] replaces the seed. */
+int ig_respond_batch(ig_ctx* ctx, uint64_t db, uint64_t store, uint64_t handle, const uint64_t* inline_y_body,
+                     uint32_t inline_rows, uint32_t inline_num_to_pack, uint32_t count, const uint32_t* shard_ids,
+                     const uint64_t* as, const uint64_t* bs, uint64_t mod_switch_target, uint64_t* a_out,
+                     uint64_t* b_out);
+
+/* Same batch with every input and output already in device memory (d_* pointers); the
+ * call only enqueues work on the context stream and returns. Per-query status words land
+ * in d_status (0 = served, 1 = store refused the shard's columns); the host must check
+ * them before using the outputs. The queried shards must hold packing stores. */
+int ig_respond_seeded_batch_device(ig_ctx* ctx, uint64_t db, uint64_t store, uint64_t handle, uint32_t count,
+                                   const uint32_t* shard_ids, const uint8_t* d_seeds, const uint64_t* d_bs,
+                                   uint64_t mod_switch_target, uint64_t* d_a_out, uint64_t* d_b_out,
+                                   uint32_t* d_status);
+
+/* ---- wire ------------------------------------------------------------------------------
+ * ServerResponse bincode bytes of a packed response (respond.rs:111-176, tight codec
+ * poly.rs:166-225): Packed{a, b_prefix (first `retained` b coefficients), retained}, no
+ * column ciphertexts, Some(PackingMode::Inspiring). `modulus` is the ciphertext modulus
+ * (the mod-switch target after a switch). Writes at most cap bytes; *len_out = size. */
+int ig_response_encode(const uint64_t* a, const uint64_t* b, uint32_t ring_dim, uint32_t retained, uint64_t modulus,
+                       uint8_t* out, size_t cap, size_t* len_out);
+
+/* ---- test hooks --------------------------------------------------------------------------
+ * Forces the word-by-word `a` expansion the kernel otherwise takes only after a rejected
+ * ChaCha word, so tests can check that path against the vectorised one. */
+int ig_debug_force_serial_expand(ig_ctx* ctx, int on);
+/* Copies a shard's store sums (gamma x ring_dim, NTT form times 2^64 mod q, the
+ * reference's Montgomery layout) to host memory. */
+int ig_debug_store_sums(ig_ctx* ctx, uint64_t db, uint32_t shard_id, uint64_t* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,497 @@
+"""inspire_gb300 — the InsPIRe server respond path on one GB300 (sm_103a).
+
+Python front of libinspire_gb300.so (C ABI: include/inspire_gb300.h), mirroring the
+reference crate's public API for this path (raven-inspire, src/lib.rs:37-48):
+
+    ServerInspiringCache.new(crs, encoded_db)          respond.rs:926-941
+    ShardData.precompute_packing(...)                  setup.rs:335-340
+    ServerSessionStore.register_server_side/get/remove/len   session.rs:829-895
+    respond_seeded_inspiring(crs, encoded_db, query)   respond.rs:1218-1226
+    respond_seeded_batch(crs, encoded_db, batch, cache, session_store)  respond.rs:1189-1202
+    mod_switch_response_checked(params, response, target)  fused: mod_switch_target= on the
+                                                       respond calls (mod_switch.rs:178-186)
+    ServerResponse.to_binary()                         respond.rs:387-390
+
+Every refusal raises PirError with the reference's message. Compute runs only in the
+CUDA library: when it cannot be loaded (no build, no GPU) the calls raise, and there is
+no CPU fallback.
+"""
+import ctypes
+import math
+import os
+
+import numpy as np
+
+from . import build as _build
+
+__all__ = [
+    "PirError", "InspireParams", "ServerCrs", "ShardData", "EncodedDatabase", "ServerInspiringCache",
+    "ServerSessionStore", "ServerSessionHandle", "ClientPackingKeys", "SeededBatchQuery", "SeededClientQuery",
+    "SeededQueryBatch", "PackingKeySource", "ServerResponse", "respond_seeded_inspiring", "respond_seeded_batch", "respond_inspiring",
+    "check_mod_switch_noise_budget", "ClientQuery", "Context", "DEFAULT_Q",
+    "MOD_SWITCH_TARGET_36BIT", "MOD_SWITCH_TARGET_45BIT", "library_path",
+]
+
+DEFAULT_Q = 1152921504606830593
+MOD_SWITCH_TARGET_36BIT = 68_718_428_161
+MOD_SWITCH_TARGET_45BIT = 35_184_372_060_161
+
+IG_OK = 0
+IG_ERR_STORE_REFUSED = 5
+
+
+class PirError(Exception):
+    """PirError(String) of the reference (src/pir/error.rs): every refusal."""
+
+    def __init__(self, message, code=None):
+        super().__init__(message)
+        self.code = code
+
+
+_lib = None
+
+
+def library_path():
+    return _build.LIB
+
+
+def _load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.build()
+    L = ctypes.CDLL(path)
+    P, U64, U32, I = ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_int
+    pu64 = ctypes.POINTER(ctypes.c_uint64)
+    sig = {
+        "ig_ctx_create": (I, [I, ctypes.POINTER(P)]),
+        "ig_ctx_destroy": (None, [P]),
+        "ig_last_error": (I, [P, ctypes.c_char_p, ctypes.c_size_t]),
+        "ig_ctx_stream": (P, [P]),
+        "ig_ctx_device_bytes": (U64, [P]),
+        "ig_crs_create": (I, [P, U32, U64, U64, U64, U32, I, U32, P, pu64]),
+        "ig_crs_destroy": (I, [P, U64]),
+        "ig_crs_key_rows": (I, [P, U64, ctypes.POINTER(U32)]),
+        "ig_db_create": (I, [P, U64, U32, pu64]),
+        "ig_db_destroy": (I, [P, U64]),
+        "ig_db_set_shard": (I, [P, U64, U32, P]),
+        "ig_db_set_shard_device": (I, [P, U64, U32, P]),
+        "ig_db_precompute_packing": (I, [P, U64, U32]),
+        "ig_db_precompute_packing_all": (I, [P, U64]),
+        "ig_db_drop_packing_store": (I, [P, U64, U32]),
+        "ig_db_has_store": (I, [P, U64, U32, ctypes.POINTER(I)]),
+        "ig_session_store_create": (I, [P, pu64]),
+        "ig_session_store_destroy": (I, [P, U64]),
+        "ig_session_register": (I, [P, U64, U64, P, U32, U32, pu64]),
+        "ig_session_remove": (I, [P, U64, U64, ctypes.POINTER(I)]),
+        "ig_session_len": (I, [P, U64, pu64]),
+        "ig_session_contains": (I, [P, U64, U64, ctypes.POINTER(I)]),
+        "ig_respond_seeded_batch": (I, [P, U64, U64, U64, P, U32, U32, U32, P, P, P, U64, P, P]),
+        "ig_respond_seeded_batch_device": (I, [P, U64, U64, U64, U32, P, P, P, U64, P, P, P]),
+        "ig_respond_batch": (I, [P, U64, U64, U64, P, U32, U32, U32, P, P, P, U64, P, P]),
+        "ig_response_encode": (I, [P, P, U32, U32, U64, P, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
+        "ig_debug_force_serial_expand": (I, [P, I]),
+        "ig_debug_store_sums": (I, [P, U64, U32, P]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def _ptr(a):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None else None
+
+
+def _u64(a, shape=None):
+    a = np.ascontiguousarray(a, dtype=np.uint64)
+    if shape is not None and a.shape != shape:
+        raise PirError(f"wire shape refused: expected an array of shape {shape}, got {a.shape}")
+    return a
+
+
+class Context:
+    """One device and one CUDA stream; every object below lives in one context."""
+
+    _default = {}
+
+    def __init__(self, device=0):
+        L = _load()
+        h = ctypes.c_void_p()
+        rc = L.ig_ctx_create(device, ctypes.byref(h))
+        if rc != IG_OK:
+            raise PirError(f"cannot open CUDA device {device} (status {rc}); the respond path has no CPU fallback",
+                           rc)
+        self.h, self.device, self._lib = h, device, L
+
+    @classmethod
+    def default(cls, device=0):
+        if device not in cls._default:
+            cls._default[device] = Context(device)
+        return cls._default[device]
+
+    def check(self, rc):
+        if rc != IG_OK:
+            buf = ctypes.create_string_buffer(2048)
+            self._lib.ig_last_error(self.h, buf, 2048)
+            raise PirError(buf.value.decode(), rc)
+
+    @property
+    def stream(self):
+        return self._lib.ig_ctx_stream(self.h)
+
+    @property
+    def device_bytes(self):
+        return self._lib.ig_ctx_device_bytes(self.h)
+
+    def close(self):
+        if self.h:
+            self._lib.ig_ctx_destroy(self.h)
+            self.h = None
+
+
+class InspireParams:
+    """InspireParams (params.rs:137-196), the single-prime sets the GPU serves."""
+
+    def __init__(self, ring_dim=2048, q=DEFAULT_Q, p=65537, sigma=6.4, gadget_base=1 << 20,
+                 packing_gadget_len=3, approximate_packing_gadget=False):
+        self.ring_dim, self.q, self.p, self.sigma = ring_dim, q, p, sigma
+        self.gadget_base, self.packing_gadget_len = gadget_base, packing_gadget_len
+        self.approximate_packing_gadget = approximate_packing_gadget
+
+    @staticmethod
+    def d2048():
+        return InspireParams()
+
+    @staticmethod
+    def d2048_approximate_gadget():
+        return InspireParams(approximate_packing_gadget=True)
+
+    def moduli(self):
+        return [self.q]
+
+    def delta(self):
+        return self.q // self.p
+
+    def packing_key_rows(self):
+        return self.packing_gadget_len - (1 if self.approximate_packing_gadget else 0)
+
+
+class ServerCrs:
+    """The public parameters a responder needs (setup.rs:75-96): params, w_seed, width."""
+
+    def __init__(self, params: InspireParams, inspiring_w_seed: bytes, inspiring_num_columns: int):
+        if len(inspiring_w_seed) != 32:
+            raise PirError("inspiring_w_seed must be 32 bytes")
+        self.params, self.inspiring_w_seed = params, bytes(inspiring_w_seed)
+        self.inspiring_num_columns = int(inspiring_num_columns)
+
+    def ring_dim(self):
+        return self.params.ring_dim
+
+    def modulus(self):
+        return self.params.q
+
+
+class ServerInspiringCache:
+    """Per-CRS device constants: pack params and offline keys (respond.rs:869-1013)."""
+
+    def __init__(self, crs: ServerCrs, ctx: Context = None):
+        self.ctx = ctx or Context.default()
+        self.crs = crs
+        p = crs.params
+        seed = np.frombuffer(crs.inspiring_w_seed, dtype=np.uint8).copy()
+        h = ctypes.c_uint64()
+        self.ctx.check(self.ctx._lib.ig_crs_create(
+            self.ctx.h, p.ring_dim, p.q, p.p, p.gadget_base, p.packing_gadget_len,
+            int(p.approximate_packing_gadget), crs.inspiring_num_columns, _ptr(seed), ctypes.byref(h)))
+        self.h = h.value
+
+    @staticmethod
+    def new(crs: ServerCrs, encoded_db=None, ctx: Context = None):
+        if encoded_db is not None and encoded_db.num_columns != crs.inspiring_num_columns:
+            raise PirError(f"ServerInspiringCache::new: shard column count {encoded_db.num_columns} != CRS width "
+                           f"{crs.inspiring_num_columns}")
+        return ServerInspiringCache(crs, ctx)
+
+    @property
+    def key_rows(self):
+        r = ctypes.c_uint32()
+        self.ctx.check(self.ctx._lib.ig_crs_key_rows(self.ctx.h, self.h, ctypes.byref(r)))
+        return r.value
+
+
+class ShardData:
+    """One shard of the device-resident database (setup.rs:280-375)."""
+
+    def __init__(self, db, shard_id):
+        self.db, self.id = db, shard_id
+
+    def precompute_packing(self):
+        self.db.ctx.check(self.db.ctx._lib.ig_db_precompute_packing(self.db.ctx.h, self.db.h, self.id))
+
+    def drop_packing_store(self):
+        self.db.ctx.check(self.db.ctx._lib.ig_db_drop_packing_store(self.db.ctx.h, self.db.h, self.id))
+
+    def packing_store(self):
+        out = ctypes.c_int()
+        self.db.ctx.check(self.db.ctx._lib.ig_db_has_store(self.db.ctx.h, self.db.h, self.id, ctypes.byref(out)))
+        return bool(out.value)
+
+    def set_columns(self, columns):
+        self.db.set_shard(self.id, columns)
+
+
+class EncodedDatabase:
+    """Shards of gamma column polynomials (setup.rs:272-289) held in HBM."""
+
+    def __init__(self, cache: ServerInspiringCache, num_shards: int):
+        self.ctx, self.cache = cache.ctx, cache
+        self.num_shards = int(num_shards)
+        self.num_columns = cache.crs.inspiring_num_columns
+        self.ring_dim = cache.crs.params.ring_dim
+        h = ctypes.c_uint64()
+        self.ctx.check(self.ctx._lib.ig_db_create(self.ctx.h, cache.h, self.num_shards, ctypes.byref(h)))
+        self.h = h.value
+        self.shards = [ShardData(self, i) for i in range(self.num_shards)]
+
+    @staticmethod
+    def from_columns(cache, shard_columns):
+        db = EncodedDatabase(cache, len(shard_columns))
+        for i, cols in enumerate(shard_columns):
+            db.set_shard(i, cols)
+        return db
+
+    def set_shard(self, shard_id, columns):
+        cols = _u64(columns, (self.num_columns, self.ring_dim))
+        self.ctx.check(self.ctx._lib.ig_db_set_shard(self.ctx.h, self.h, shard_id, _ptr(cols)))
+
+    def set_shard_device(self, shard_id, device_ptr: int):
+        self.ctx.check(self.ctx._lib.ig_db_set_shard_device(self.ctx.h, self.h, shard_id, ctypes.c_void_p(device_ptr)))
+
+    def precompute_packing_all(self):
+        self.ctx.check(self.ctx._lib.ig_db_precompute_packing_all(self.ctx.h, self.h))
+
+    def store_sums(self, shard_id):
+        out = np.zeros((self.num_columns, self.ring_dim), dtype=np.uint64)
+        self.ctx.check(self.ctx._lib.ig_debug_store_sums(self.ctx.h, self.h, shard_id, _ptr(out)))
+        return out
+
+
+class ServerSessionHandle(int):
+    """ServerSessionHandle(u64) (query.rs:98)."""
+
+
+class ClientPackingKeys:
+    """The uploaded key body (inspiring2.rs:684-698): key_rows x ring_dim coefficients."""
+
+    def __init__(self, y_body, num_to_pack):
+        self.y_body = np.ascontiguousarray(y_body, dtype=np.uint64)
+        self.num_to_pack = int(num_to_pack)
+
+
+class ServerSessionStore:
+    """Registered packing-key seats by handle (session.rs:700-895)."""
+
+    def __init__(self, ctx: Context = None):
+        self.ctx = ctx or Context.default()
+        h = ctypes.c_uint64()
+        self.ctx.check(self.ctx._lib.ig_session_store_create(self.ctx.h, ctypes.byref(h)))
+        self.h = h.value
+
+    @staticmethod
+    def new(ctx=None):
+        return ServerSessionStore(ctx)
+
+    def register_server_side(self, keys: ClientPackingKeys, cache: ServerInspiringCache):
+        y = np.ascontiguousarray(keys.y_body, dtype=np.uint64)
+        if y.ndim != 2 or y.shape[1] != cache.crs.params.ring_dim:
+            raise PirError(f"packing-key y_body dimension {y.shape[-1] if y.ndim else 0}, expected "
+                           f"{cache.crs.params.ring_dim}; rebuild the keys from the current CRS")
+        h = ctypes.c_uint64()
+        self.ctx.check(self.ctx._lib.ig_session_register(self.ctx.h, self.h, cache.h, _ptr(y), y.shape[0],
+                                                         keys.num_to_pack, ctypes.byref(h)))
+        return ServerSessionHandle(h.value)
+
+    def get(self, handle):
+        out = ctypes.c_int()
+        self.ctx.check(self.ctx._lib.ig_session_contains(self.ctx.h, self.h, int(handle), ctypes.byref(out)))
+        return bool(out.value)
+
+    def remove(self, handle):
+        out = ctypes.c_int()
+        self.ctx.check(self.ctx._lib.ig_session_remove(self.ctx.h, self.h, int(handle), ctypes.byref(out)))
+        return bool(out.value)
+
+    def __len__(self):
+        out = ctypes.c_uint64()
+        self.ctx.check(self.ctx._lib.ig_session_len(self.ctx.h, self.h, ctypes.byref(out)))
+        return out.value
+
+    def is_empty(self):
+        return len(self) == 0
+
+
+class SeededBatchQuery:
+    """One seeded row request (query.rs:141-171): shard_id, the `a` seed and b."""
+
+    def __init__(self, shard_id, seed: bytes, b):
+        if len(seed) != 32:
+            raise PirError("seeded RGSW row seed must be 32 bytes")
+        self.shard_id, self.seed = int(shard_id), bytes(seed)
+        self.b = np.ascontiguousarray(b, dtype=np.uint64)
+
+
+class ClientQuery:
+    """An unseeded query row (query.rs:103-120): `a` travels in full."""
+
+    def __init__(self, shard_id, a, b, inspiring_packing_keys=None, session_handle=None):
+        self.shard_id = int(shard_id)
+        self.a = np.ascontiguousarray(a, dtype=np.uint64)
+        self.b = np.ascontiguousarray(b, dtype=np.uint64)
+        self.seed = None
+        self.inspiring_packing_keys, self.session_handle = inspiring_packing_keys, session_handle
+
+
+class SeededClientQuery(SeededBatchQuery):
+    """A single query with its packing key inline or by handle (query.rs:103-135)."""
+
+    def __init__(self, shard_id, seed, b, inspiring_packing_keys=None, session_handle=None):
+        super().__init__(shard_id, seed, b)
+        self.inspiring_packing_keys, self.session_handle = inspiring_packing_keys, session_handle
+
+
+class PackingKeySource:
+    """PackingKeySource::{Inline, Registered} (query.rs:176-181)."""
+
+    def __init__(self, inline: ClientPackingKeys = None, registered=None):
+        if (inline is None) == (registered is None):
+            raise PirError("a packing key source is either inline keys or a registered handle")
+        self.inline, self.registered = inline, registered
+
+    @staticmethod
+    def Inline(keys):
+        return PackingKeySource(inline=keys)
+
+    @staticmethod
+    def Registered(handle):
+        return PackingKeySource(registered=handle)
+
+
+class SeededQueryBatch:
+    """Queries answered under one packing key (query.rs:186-211)."""
+
+    def __init__(self, packing_key: PackingKeySource, queries):
+        self.packing_key, self.queries = packing_key, list(queries)
+
+
+class ServerResponse:
+    """A packed InspiRING response: a, b (the first `packed_coefficients` b words cross
+    the wire) over `modulus` (respond.rs:27-41)."""
+
+    def __init__(self, a, b, packed_coefficients, modulus=DEFAULT_Q):
+        self.a, self.b = a, b
+        self.packed_coefficients, self.modulus = int(packed_coefficients), int(modulus)
+
+    def to_binary(self) -> bytes:
+        L = _load()
+        a = np.ascontiguousarray(self.a, dtype=np.uint64)
+        b = np.ascontiguousarray(self.b, dtype=np.uint64)
+        n = ctypes.c_size_t()
+        rc = L.ig_response_encode(_ptr(a), _ptr(b), len(a), self.packed_coefficients, self.modulus, None, 0,
+                                  ctypes.byref(n))
+        if rc:
+            raise PirError(f"ServerResponse encode refused (status {rc}): coefficients must be canonical")
+        out = np.zeros(n.value, dtype=np.uint8)
+        L.ig_response_encode(_ptr(a), _ptr(b), len(a), self.packed_coefficients, self.modulus, _ptr(out), n.value,
+                             ctypes.byref(n))
+        return out.tobytes()
+
+
+def check_mod_switch_noise_budget(params: InspireParams, target_modulus: int):
+    """mod_switch.rs:111-146: refuse a target whose rounding noise can break decryption."""
+    if target_modulus <= 0 or target_modulus > params.q or target_modulus < params.p:
+        raise PirError(f"mod-switch target_modulus {target_modulus} outside [p, q]")
+    if target_modulus % (2 * params.ring_dim) != 1:
+        raise PirError(f"mod-switch target_modulus {target_modulus} is not NTT-friendly: must satisfy "
+                       f"q' == 1 (mod 2*d) where d={params.ring_dim}")
+    d, p, q_old, q_new, sigma = float(params.ring_dim), float(params.p), float(params.q), float(target_modulus), params.sigma
+    s_max = 7.0 * sigma
+    round_noise = 0.5 + d * 0.5 * s_max
+    scaled_old = (q_new / q_old) * (q_old / (4.0 * p))
+    total = round_noise + scaled_old + float(target_modulus % params.p)
+    budget = q_new / (2.0 * p)
+    if total >= budget:
+        raise PirError(f"mod-switch noise-budget violation: total_noise={total:.0f} >= budget={budget:.0f}")
+
+
+def _batch(crs, encoded_db, queries, packing_key, session_store, mod_switch_target):
+    cache = encoded_db.cache
+    ctx = encoded_db.ctx
+    if cache.crs is not crs and (cache.crs.inspiring_w_seed != crs.inspiring_w_seed or
+                                 cache.crs.inspiring_num_columns != crs.inspiring_num_columns):
+        raise PirError("cached pack params do not match CRS params")
+    n = crs.params.ring_dim
+    count = len(queries)
+    if count == 0:
+        raise PirError("empty batch")
+    shard_ids = np.array([q.shard_id for q in queries], dtype=np.uint32)
+    unseeded = queries[0].seed is None
+    if any((q.seed is None) != unseeded for q in queries):
+        raise PirError("a batch is all seeded or all unseeded queries")
+    if unseeded:
+        seeds = np.stack([_u64(q.a, (n,)) for q in queries])
+    else:
+        seeds = np.frombuffer(b"".join(q.seed for q in queries), dtype=np.uint8).copy()
+    bs = np.stack([_u64(q.b, (n,)) for q in queries])
+    a_out = np.zeros((count, n), dtype=np.uint64)
+    b_out = np.zeros((count, n), dtype=np.uint64)
+    if packing_key.inline is not None:
+        y = _u64(packing_key.inline.y_body)
+        if y.ndim != 2 or y.shape[1] != n:
+            raise PirError(f"packing-key y_body must be key_rows x {n} coefficients")
+        args = (0, 0, _ptr(y), y.shape[0], packing_key.inline.num_to_pack)
+    else:
+        if session_store is None:
+            raise PirError(f"query references session_handle {int(packing_key.registered)} but no "
+                           "ServerSessionStore was supplied to respond_*_with_session")
+        args = (session_store.h, int(packing_key.registered), None, 0, 0)
+    ms = int(mod_switch_target or 0)
+    if ms:
+        check_mod_switch_noise_budget(crs.params, ms)
+    fn = ctx._lib.ig_respond_batch if unseeded else ctx._lib.ig_respond_seeded_batch
+    ctx.check(fn(ctx.h, encoded_db.h, *args, count, _ptr(shard_ids), _ptr(seeds), _ptr(bs), ms, _ptr(a_out),
+                 _ptr(b_out)))
+    modulus = ms or crs.params.q
+    return [ServerResponse(a_out[i], b_out[i], crs.inspiring_num_columns, modulus) for i in range(count)]
+
+
+def respond_seeded_batch(crs: ServerCrs, encoded_db: EncodedDatabase, batch: SeededQueryBatch,
+                         cache: ServerInspiringCache = None, session_store: ServerSessionStore = None,
+                         mod_switch_target: int = 0):
+    """respond_seeded_batch (respond.rs:1189-1202): every query under the batch's one
+    packing key, in order; refused whole on the first error."""
+    return _batch(crs, encoded_db, batch.queries, batch.packing_key, session_store, mod_switch_target)
+
+
+def respond_inspiring(crs: ServerCrs, encoded_db: EncodedDatabase, query: ClientQuery,
+                      session_store: ServerSessionStore = None, mod_switch_target: int = 0):
+    """respond_inspiring / respond_inspiring_cached_with_session (respond.rs:736-759,
+    1053-1091) for an unseeded query."""
+    return respond_seeded_inspiring(crs, encoded_db, query, session_store, mod_switch_target)
+
+
+def respond_seeded_inspiring(crs: ServerCrs, encoded_db: EncodedDatabase, query: SeededClientQuery,
+                             session_store: ServerSessionStore = None, mod_switch_target: int = 0):
+    """respond_seeded_inspiring (respond.rs:1218-1226) and its _with_session sibling
+    (1238-1248): one query, key inline or by handle."""
+    keys, handle = query.inspiring_packing_keys, query.session_handle
+    if keys is not None and handle is not None:
+        raise PirError(f"query has both inlined inspiring_packing_keys AND session_handle {int(handle)}; "
+                       "exactly one must be set")
+    if keys is None and handle is None:
+        raise PirError("InspiRING client packing keys missing from query (neither inlined nor session_handle set)")
+    src = PackingKeySource.Inline(keys) if keys is not None else PackingKeySource.Registered(handle)
+    return _batch(crs, encoded_db, [query], src, session_store, mod_switch_target)[0]

@@ -1,0 +1,518 @@
+// Kernels of the InspiRING respond path on sm_103a.
+//
+// Work map (reference call sites in src/):
+//   ntt_rows      negacyclic forward NTT of many rows: the seat's key body
+//                 (pir/session.rs:600-625), the offline mask rows
+//                 (inspiring/inspiring2.rs:537-598) and a shard's columns before its
+//                 store is folded (inspiring/shard_store.rs:139-144).
+//   store_fold    step 1 of the offline phase folded over one shard's columns
+//                 (inspiring/inspiring2.rs:964-1004 via shard_store.rs:145), computed per
+//                 slot as a length-gamma cyclic DFT instead of gamma^2 monomial products.
+//   shard_scan    the store's column check and b fold (shard_store.rs:197-264): one HBM
+//                 pass over the queried shard's columns per query.
+//   respond       one CTA per query: the query's `a` expansion (math/poly.rs:657-686),
+//                 the store gather (shard_store.rs:282-342), the backward recursion
+//                 (inspiring2.rs:1014-1085) with the online gather fused into each link
+//                 (inspiring2.rs:1393-1485), the final inverse transforms and the 36-bit
+//                 mod switch (pir/mod_switch.rs:148-176).
+#include <cuda_runtime.h>
+
+#include "ig_kernels.cuh"
+
+namespace igk {
+using namespace ig;
+
+// ------------------------------------------------------------------------------------
+// Negacyclic transforms in shared memory. Forward: Cooley-Tukey over the bit-reversed
+// ladder psi^brv(m) (math/ntt.rs:600-623 order); inverse: Gentleman-Sande over the
+// inverse ladder (math/ntt.rs:626-654) without the final n^-1, which consumers fold into
+// their first use. Both are linear in standard form; all words canonical.
+
+template <int LOGN, int NT>
+__device__ __forceinline__ void ntt_fwd(u64* x, const u64* tw, const u64* twp) {
+  constexpr int N = 1 << LOGN;
+#pragma unroll 1
+  for (int s = 0; s < LOGN; s++) {
+    const int tlog = LOGN - 1 - s;
+    const int t = 1 << tlog;
+    const int m = 1 << s;
+#pragma unroll
+    for (int b = threadIdx.x; b < N / 2; b += NT) {
+      const int i = b >> tlog;
+      const int j1 = (i << (tlog + 1)) | (b & (t - 1));
+      const u64 w = tw[m + i], wp = twp[m + i];
+      const u64 u = x[j1];
+      const u64 v = shoup(x[j1 + t], w, wp);
+      x[j1] = addq(u, v);
+      x[j1 + t] = subq(u, v);
+    }
+    __syncthreads();
+  }
+}
+
+template <int LOGN, int NT>
+__device__ __forceinline__ void ntt_fwd2(u64* x, u64* y, const u64* tw, const u64* twp) {
+  constexpr int N = 1 << LOGN;
+#pragma unroll 1
+  for (int s = 0; s < LOGN; s++) {
+    const int tlog = LOGN - 1 - s;
+    const int t = 1 << tlog;
+    const int m = 1 << s;
+#pragma unroll
+    for (int b = threadIdx.x; b < N / 2; b += NT) {
+      const int i = b >> tlog;
+      const int j1 = (i << (tlog + 1)) | (b & (t - 1));
+      const u64 w = tw[m + i], wp = twp[m + i];
+      const u64 u0 = x[j1], u1 = y[j1];
+      const u64 v0 = shoup(x[j1 + t], w, wp);
+      const u64 v1 = shoup(y[j1 + t], w, wp);
+      x[j1] = addq(u0, v0);
+      x[j1 + t] = subq(u0, v0);
+      y[j1] = addq(u1, v1);
+      y[j1 + t] = subq(u1, v1);
+    }
+    __syncthreads();
+  }
+}
+
+template <int LOGN, int NT>
+__device__ __forceinline__ void ntt_inv(u64* x, const u64* itw, const u64* itwp) {
+  constexpr int N = 1 << LOGN;
+#pragma unroll 1
+  for (int s = 0; s < LOGN; s++) {
+    const int t = 1 << s;
+    const int m = N >> (s + 1);
+#pragma unroll
+    for (int b = threadIdx.x; b < N / 2; b += NT) {
+      const int i = b >> s;
+      const int j2 = (i << (s + 1)) | (b & (t - 1));
+      const u64 w = itw[m + i], wp = itwp[m + i];
+      const u64 u = x[j2], v = x[j2 + t];
+      x[j2] = addq(u, v);
+      x[j2 + t] = shoup(subq(u, v), w, wp);
+    }
+    __syncthreads();
+  }
+}
+
+template <int LOGN, int NT>
+__device__ __forceinline__ void ntt_inv2(u64* x, u64* y, const u64* itw, const u64* itwp) {
+  constexpr int N = 1 << LOGN;
+#pragma unroll 1
+  for (int s = 0; s < LOGN; s++) {
+    const int t = 1 << s;
+    const int m = N >> (s + 1);
+#pragma unroll
+    for (int b = threadIdx.x; b < N / 2; b += NT) {
+      const int i = b >> s;
+      const int j2 = (i << (s + 1)) | (b & (t - 1));
+      const u64 w = itw[m + i], wp = itwp[m + i];
+      const u64 u0 = x[j2], v0 = x[j2 + t];
+      const u64 u1 = y[j2], v1 = y[j2 + t];
+      x[j2] = addq(u0, v0);
+      x[j2 + t] = shoup(subq(u0, v0), w, wp);
+      y[j2] = addq(u1, v1);
+      y[j2 + t] = shoup(subq(u1, v1), w, wp);
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------------------------------
+// Batched forward NTT: one CTA per row.
+template <int LOGN>
+__global__ void __launch_bounds__((1 << LOGN) / 4) k_ntt_rows(CrsDev c, const u64* in, u64* out, u64 scale,
+                                                              u64 scalep) {
+  constexpr int N = 1 << LOGN, NT = N / 4;
+  extern __shared__ __align__(16) u64 sm[];
+  u64* x = sm;
+  u64* tw = sm + N;
+  u64* twp = sm + 2 * N;
+  const u64* row = in + (size_t)blockIdx.x * N;
+  for (int k = threadIdx.x; k < N; k += NT) {
+    x[k] = reduce128(row[k]);
+    tw[k] = c.tw[k];
+    twp[k] = c.twp[k];
+  }
+  __syncthreads();
+  ntt_fwd<LOGN, NT>(x, tw, twp);
+  u64* o = out + (size_t)blockIdx.x * N;
+  for (int k = threadIdx.x; k < N; k += NT) o[k] = shoup(x[k], scale, scalep);
+}
+
+// ------------------------------------------------------------------------------------
+// Store fold. For slot t with root w_t = w0^e_t, step 1 at rotation i reads
+//   acc_i[t] = sum_j w_t^(j * c_i) H_j[t],  c_i = g^-i mod 2n = 1 + m_i * (2n/gamma),
+// so with u_j = w0^(e_t j) H_j[t] and zeta = w0^(2n/gamma) (order gamma),
+//   acc_i[t] = DFT_zeta(u)[(e_t * m_i) mod gamma].
+// The sum lands at S_i[t'] with table_i[t'] = t, i.e. t' = slot of exponent c_i * e_t,
+// scaled by gamma^-1 and stored in R-form.
+constexpr int FOLD_TILE = 2048;
+constexpr int FOLD_THREADS = 256;
+
+template <int LOGN>
+__global__ void __launch_bounds__(FOLD_THREADS) k_store_fold(CrsDev c, const u64* H, u64* sums_R, u32 SL) {
+  constexpr int N = 1 << LOGN;
+  constexpr u32 M2N = 2 * N - 1;
+  extern __shared__ __align__(16) u64 sm[];
+  const u32 gamma = c.gamma;
+  const u32 tile = SL * gamma;   // SL slots per CTA, tile <= FOLD_TILE words
+  u64* x = sm;                   // [slot][j]
+  u64* pw = sm + FOLD_TILE;      // w0^e R-form, 2N words
+  const u32 t0 = blockIdx.x * SL;
+  u32 lg = 0;
+  while ((1u << lg) < gamma) lg++;
+  for (int k = threadIdx.x; k < 2 * N; k += FOLD_THREADS) pw[k] = c.pow_root_R[k];
+  __syncthreads();
+  for (u32 idx = threadIdx.x; idx < tile; idx += FOLD_THREADS) {
+    const u32 j = idx / SL, s = idx % SL;
+    const u32 t = t0 + s;
+    const u32 e = c.slot_exp[t];
+    const u64 h = H[(size_t)j * N + t];
+    x[s * gamma + j] = mont(h, pw[(e * j) & M2N]);
+  }
+  __syncthreads();
+  // Gentleman-Sande DFT of length gamma per slot, bit-reversed output.
+  for (u32 len = gamma >> 1; len >= 1; len >>= 1) {
+    const u32 half_total = SL * (gamma >> 1);
+    for (u32 b = threadIdx.x; b < half_total; b += FOLD_THREADS) {
+      const u32 s = b / (gamma >> 1);
+      const u32 bb = b % (gamma >> 1);
+      const u32 blk = bb / len, j = bb % len;
+      const u32 i0 = s * gamma + blk * 2 * len + j;
+      const u64 u = x[i0], v = x[i0 + len];
+      x[i0] = addq(u, v);
+      x[i0 + len] = mont(subq(u, v), pw[(j * (N / len)) & M2N]);
+    }
+    __syncthreads();
+  }
+  for (u32 idx = threadIdx.x; idx < tile; idx += FOLD_THREADS) {
+    const u32 i = idx / SL, s = idx % SL;
+    const u32 t = t0 + s;
+    const u32 e = c.slot_exp[t];
+    const u32 k = (e * c.m_of_i[i]) & (gamma - 1);
+    const u32 kr = lg ? (__brev(k) >> (32 - lg)) : 0;
+    const u64 val = x[s * gamma + kr];
+    const u32 tp = c.exp_slot[((c.cpow[i] * e) & M2N) >> 1];
+    sums_R[(size_t)i * N + tp] = shoup(val, c.inv_gamma_R, c.inv_gamma_Rp);
+  }
+}
+
+// ------------------------------------------------------------------------------------
+// Shard scan: one warp per (query, column). Per word w_k of column j:
+//   tag  += lo32(w_k) key[2k] + hi32(w_k) key[2k+1]            (mod 2^61 - 1 at the end)
+//   fold += w_k * b_rev[k],  b_rev[0] = b_0, b_rev[k] = -b_{n-k}  (mod q at the end)
+// Accumulators are exact 128-bit sums; the fold keeps low and high product halves apart.
+constexpr int SCAN_COLS = 8;  // columns (warps) per CTA
+constexpr u64 TAG_PRIME = (1ULL << 61) - 1;
+
+__device__ __forceinline__ u128 shfl_xor_u128(u128 v, int m) {
+  u64 lo = (u64)v, hi = (u64)(v >> 64);
+  lo = __shfl_xor_sync(0xffffffffu, lo, m);
+  hi = __shfl_xor_sync(0xffffffffu, hi, m);
+  return ((u128)hi << 64) | lo;
+}
+
+template <int LOGN>
+__global__ void __launch_bounds__(SCAN_COLS * 32) k_scan(CrsDev c, const QueryDev* queries, const ShardDev* shards,
+                                                         u64* b_fold, u32* status, int build, u64* tags_out) {
+  constexpr int N = 1 << LOGN;
+  const u32 qi = blockIdx.y;
+  const QueryDev qd = queries[qi];
+  const ShardDev sh = shards[qd.shard];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const u32 j = blockIdx.x * SCAN_COLS + warp;
+  if (j >= c.gamma) return;
+  const u64* col = sh.columns + (size_t)j * N;
+  const u64* key = sh.tag_key;
+  const u64* b = qd.b;
+  u128 tag = 0, flo = 0, fhi = 0;
+#pragma unroll 4
+  for (int k0 = lane * 2; k0 < N; k0 += 64) {
+    const ulonglong2 w = *reinterpret_cast<const ulonglong2*>(col + k0);
+    const ulonglong2 ka = *reinterpret_cast<const ulonglong2*>(key + 2 * k0);
+    const ulonglong2 kb = *reinterpret_cast<const ulonglong2*>(key + 2 * k0 + 2);
+    tag += (u128)(w.x & 0xffffffffULL) * ka.x + (u128)(w.x >> 32) * ka.y;
+    tag += (u128)(w.y & 0xffffffffULL) * kb.x + (u128)(w.y >> 32) * kb.y;
+    if (b) {
+      const u64 r0 = k0 == 0 ? reduce128(b[0]) : negq(reduce128(b[N - k0]));
+      const u64 r1 = negq(reduce128(b[N - k0 - 1]));
+      const u128 p0 = (u128)w.x * r0, p1 = (u128)w.y * r1;
+      flo += (u128)(u64)p0 + (u64)p1;
+      fhi += (p0 >> 64) + (p1 >> 64);
+    }
+  }
+#pragma unroll
+  for (int m = 16; m >= 1; m >>= 1) {
+    tag += shfl_xor_u128(tag, m);
+    flo += shfl_xor_u128(flo, m);
+    fhi += shfl_xor_u128(fhi, m);
+  }
+  if (lane == 0) {
+    u128 t = tag;
+    t = (t & TAG_PRIME) + (t >> 61);
+    t = (t & TAG_PRIME) + (t >> 61);
+    u64 tv = (u64)t;
+    while (tv >= TAG_PRIME) tv -= TAG_PRIME;
+    if (build) {
+      tags_out[j] = tv;
+    } else {
+      if (sh.tags && tv != sh.tags[j]) atomicOr(status + qi, (u32)DEV_TAG_MISMATCH);
+      // fold = fhi * 2^64 + flo (mod q)
+      const u64 r64 = (u64)((((u128)1) << 64) % Q);
+      const u64 hq = reduce128(fhi), lq = reduce128(flo);
+      b_fold[(size_t)qi * c.gamma + j] = reduce128((u128)hq * r64 + lq);
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------
+// Mod switch c' = floor((c q' + floor(q/2)) / q) mod q' (exact; q' < 2^62).
+__device__ __forceinline__ u64 mod_switch_word(u64 cv, u64 qn) {
+  const u128 x = (u128)cv * qn + (Q >> 1);
+  u64 quo = (u64)(x >> 60);
+  u128 r = x - (u128)quo * Q;
+  while (r >= Q) {
+    r -= Q;
+    quo++;
+  }
+  return quo % qn;
+}
+
+// ------------------------------------------------------------------------------------
+template <int LOGN>
+__global__ void __launch_bounds__((1 << LOGN) / 4, 1)
+    k_respond(CrsDev c, const QueryDev* queries, const ShardDev* shards, const u64* b_fold, u64 ms_target, u64* a_out, u64* b_out, u32* status, int force_serial) {
+  constexpr int N = 1 << LOGN, NT = N / 4;
+  constexpr u32 M2N = 2 * N - 1;
+  constexpr u64 DMASK = (1ULL << 20) - 1;
+  extern __shared__ __align__(16) u64 sm[];
+  u64* bufA = sm;
+  u64* bufB = sm + N;
+  u64* a_ntt = sm + 2 * N;
+  u64* tw = sm + 3 * N;
+  u64* twp = sm + 4 * N;
+  u64* itw = sm + 5 * N;
+  u64* itwp = sm + 6 * N;
+  const u32 rows = c.rows;
+  u64* Wm = sm + 7 * N;
+  u64* Y = Wm + rows * N;
+  uint16_t* e_tab = reinterpret_cast<uint16_t*>(Y + rows * N);
+  uint16_t* s_tab = e_tab + N;
+
+  const int tid = threadIdx.x;
+  const u32 qi = blockIdx.x;
+  const QueryDev qd = queries[qi];
+  const ShardDev sh = shards[qd.shard];
+  const u64* yR = qd.seat_R;
+  const u32 gamma = c.gamma;
+
+  for (int k = tid; k < N; k += NT) {
+    tw[k] = c.tw[k];
+    twp[k] = c.twp[k];
+    itw[k] = c.itw[k];
+    itwp[k] = c.itwp[k];
+    e_tab[k] = c.slot_exp[k];
+    s_tab[k] = c.exp_slot[k];
+  }
+  for (u32 k = tid; k < rows * N; k += NT) {
+    Wm[k] = c.wmask_R[k];
+    Y[k] = yR[k];
+  }
+
+  // Query `a`: ChaCha20 keystream of the seed, u64 words in order, each accepted by
+  // rand's gen_range(0..q) rule. Block b of the stream yields words 8b..8b+7.
+  bool rejected = false;
+  if (qd.a) {
+    for (int k = tid; k < N; k += NT) a_ntt[k] = reduce128(qd.a[k]);
+  } else if (tid < N / 8) {
+    u32 blk[16];
+    u32 key[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) key[k] = qd.seed[k];
+    chacha20_block(key, (u64)tid, 0, blk);
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      const u64 v = (u64)blk[2 * k] | ((u64)blk[2 * k + 1] << 32);
+      if (v * Q > RANGE_ZONE) rejected = true;
+      a_ntt[tid * 8 + k] = mulhi(v, Q);
+    }
+  }
+  if (__syncthreads_or(rejected || (force_serial && !qd.a))) {
+    // A rejected word shifts every later coefficient: redo the walk word by word.
+    if (tid == 0) {
+      u32 blk[16], key[8];
+      for (int k = 0; k < 8; k++) key[k] = qd.seed[k];
+      u64 have = ~0ULL, cand = 0;
+      int filled = 0;
+      const u64 limit = (u64)N + 65536;
+      while (filled < N && cand < limit) {
+        const u64 bi = cand >> 3;
+        if (bi != have) {
+          chacha20_block(key, bi, 0, blk);
+          have = bi;
+        }
+        const int k = (int)(cand & 7);
+        const u64 v = (u64)blk[2 * k] | ((u64)blk[2 * k + 1] << 32);
+        if (v * Q <= RANGE_ZONE) a_ntt[filled++] = mulhi(v, Q);
+        cand++;
+      }
+      if (filled < N) {
+        atomicOr(status + qi, (u32)DEV_EXPAND_EXHAUSTED);
+        for (; filled < N; filled++) a_ntt[filled] = 0;
+      }
+    }
+    __syncthreads();
+  }
+  ntt_fwd<LOGN, NT>(a_ntt, tw, twp);
+
+  u64 cur[4], sb[4];
+  u32 et[4];
+#pragma unroll
+  for (int k = 0; k < 4; k++) et[k] = e_tab[tid + k * NT];
+  {
+    const u32 gp = c.gpow[gamma - 1];
+    const u64* Srow = sh.sums_R + (size_t)(gamma - 1) * N;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const int t = tid + k * NT;
+      const u32 tb = s_tab[((gp * et[k]) & M2N) >> 1];
+      cur[k] = mont(a_ntt[tb], Srow[t]);
+      sb[k] = 0;
+    }
+  }
+  const bool exact = c.approx == 0;
+#pragma unroll 1
+  for (int i = (int)gamma - 2; i >= 0; i--) {
+    const u64* Srow = sh.sums_R + (size_t)i * N;
+    u64 sv[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) sv[k] = Srow[tid + k * NT];
+    const u32 gp = c.gpow[i];
+#pragma unroll
+    for (int k = 0; k < 4; k++) bufA[tid + k * NT] = cur[k];
+    __syncthreads();
+    ntt_inv<LOGN, NT>(bufA, itw, itwp);
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const int t = tid + k * NT;
+      const u64 r = shoup(bufA[t], c.ninv, c.ninvp);
+      if (exact) {
+        bufB[t] = r & DMASK;
+        bufA[t] = (r >> 20) & DMASK;
+      } else {
+        const u64 rr = (r + (1ULL << 19)) >> 20;
+        bufB[t] = rr & DMASK;
+        bufA[t] = rr >> 20;
+      }
+    }
+    __syncthreads();
+    ntt_fwd2<LOGN, NT>(bufB, bufA, tw, twp);
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const int t = tid + k * NT;
+      const u32 tb = s_tab[((gp * et[k]) & M2N) >> 1];
+      const u64 d0 = bufB[t], d1 = bufA[t];
+      u64 nb = addq(mont(d0, Y[tb]), mont(d1, Y[N + tb]));
+      u64 nc = addq(mont(a_ntt[tb], sv[k]), addq(mont(d0, Wm[tb]), mont(d1, Wm[N + tb])));
+      if (exact) {
+        const u64 d2 = addq(addq(shoup(cur[k], c.ld_inv, c.ld_invp), shoup(d0, c.ld_c0, c.ld_c0p)),
+                            shoup(d1, c.ld_c1, c.ld_c1p));
+        nb = addq(nb, mont(d2, Y[2 * N + tb]));
+        nc = addq(nc, mont(d2, Wm[2 * N + tb]));
+      }
+      sb[k] = addq(sb[k], nb);
+      cur[k] = nc;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    bufA[tid + k * NT] = cur[k];
+    bufB[tid + k * NT] = sb[k];
+  }
+  __syncthreads();
+  ntt_inv2<LOGN, NT>(bufA, bufB, itw, itwp);
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const int t = tid + k * NT;
+    u64 av = shoup(bufA[t], c.ninv, c.ninvp);
+    u64 bv = shoup(bufB[t], c.ninv, c.ninvp);
+    if ((u32)t < gamma) bv = addq(bv, b_fold[(size_t)qi * gamma + t]);
+    if (ms_target) {
+      av = mod_switch_word(av, ms_target);
+      bv = mod_switch_word(bv, ms_target);
+    }
+    a_out[(size_t)qi * N + t] = av;
+    b_out[(size_t)qi * N + t] = bv;
+  }
+}
+
+// ------------------------------------------------------------------------------------
+// Launchers.
+
+#define IG_DISPATCH_LOGN(logn, ...)                   \
+  switch (logn) {                                     \
+    case 8: { constexpr int L = 8; __VA_ARGS__; } break;   \
+    case 9: { constexpr int L = 9; __VA_ARGS__; } break;   \
+    case 10: { constexpr int L = 10; __VA_ARGS__; } break; \
+    case 11: { constexpr int L = 11; __VA_ARGS__; } break; \
+    default: return cudaErrorInvalidValue;                 \
+  }
+
+cudaError_t ntt_rows(const CrsDev& c, const u64* in, u64* out, u32 rows, u64 scale, u64 scalep, cudaStream_t s) {
+  if (rows == 0) return cudaSuccess;
+  const size_t smem = 3 * (size_t)c.n * 8;
+  IG_DISPATCH_LOGN(c.logn, {
+    auto k = k_ntt_rows<L>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k<<<rows, (1 << L) / 4, smem, s>>>(c, in, out, scale, scalep);
+  });
+  return cudaGetLastError();
+}
+
+cudaError_t store_fold(const CrsDev& c, const u64* H, u64* sums_R, cudaStream_t s) {
+  if (c.gamma > (u32)FOLD_TILE || c.gamma == 0 || c.gamma > c.n) return cudaErrorInvalidValue;
+  u32 SL = FOLD_TILE / c.gamma;
+  if (SL > c.n) SL = c.n;
+  if (c.n % SL) return cudaErrorInvalidValue;
+  const u32 blocks = c.n / SL;
+  const size_t smem = (FOLD_TILE + 2 * (size_t)c.n) * 8;
+  IG_DISPATCH_LOGN(c.logn, {
+    auto k = k_store_fold<L>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k<<<blocks, FOLD_THREADS, smem, s>>>(c, H, sums_R, SL);
+  });
+  return cudaGetLastError();
+}
+
+cudaError_t shard_scan(const CrsDev& c, const QueryDev* queries, const ShardDev* shards, u32 nq, u64* b_fold,
+                       u32* status, int mode_build, u64* tags_out, cudaStream_t s) {
+  if (nq == 0) return cudaSuccess;
+  dim3 grid((c.gamma + SCAN_COLS - 1) / SCAN_COLS, nq);
+  IG_DISPATCH_LOGN(c.logn, {
+    k_scan<L><<<grid, SCAN_COLS * 32, 0, s>>>(c, queries, shards, b_fold, status, mode_build, tags_out);
+  });
+  return cudaGetLastError();
+}
+
+size_t respond_smem_bytes(const CrsDev& c) {
+  return (size_t)(7 + 2 * c.rows) * c.n * 8 + 2 * (size_t)c.n * 2;
+}
+
+cudaError_t respond(const CrsDev& c, const QueryDev* queries, const ShardDev* shards, u32 nq, const u64* b_fold, u64 ms_target, u64* a_out, u64* b_out, u32* status,
+                    int force_serial_expand, cudaStream_t s) {
+  if (nq == 0) return cudaSuccess;
+  const size_t smem = respond_smem_bytes(c);
+  IG_DISPATCH_LOGN(c.logn, {
+    auto k = k_respond<L>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k<<<nq, (1 << L) / 4, smem, s>>>(c, queries, shards, b_fold, ms_target, a_out, b_out, status,
+                                     force_serial_expand);
+  });
+  return cudaGetLastError();
+}
+
+}  // namespace igk

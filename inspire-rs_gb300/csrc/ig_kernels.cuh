@@ -1,0 +1,80 @@
+// Device-side structures shared by the kernels and the runtime.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "ig_arith.cuh"
+
+namespace ig {
+
+// Status words a kernel writes for the host; 0 = ok.
+enum DeviceStatus : u32 {
+  DEV_OK = 0,
+  DEV_TAG_MISMATCH = 1,     // a column is not the column the store was built from
+  DEV_EXPAND_EXHAUSTED = 2  // query `a` expansion ran past its candidate budget
+};
+
+// Per parameter-set constants, resident in device memory.
+struct CrsDev {
+  u32 n, logn, gamma, rows, approx;
+  const u64 *tw, *twp;    // forward ladder psi^brv(m), Shoup companions (index m in [1, n))
+  const u64 *itw, *itwp;  // inverse ladder
+  u64 ninv, ninvp;        // n^-1 mod q, Shoup
+  const uint16_t* slot_exp;  // odd exponent e_t of slot t's root relative to slot 0's
+  const uint16_t* exp_slot;  // slot holding exponent e, indexed e/2
+  const u32* gpow;           // g^i mod 2n, i < gamma
+  const u32* cpow;           // g^-i mod 2n, i < gamma
+  const u32* m_of_i;         // (g^-i - 1) / (2n/gamma)
+  const u64* pow_root_R;     // w0^e * 2^64 mod q for e < 2n (w0 = slot 0's root)
+  u64 inv_gamma_R, inv_gamma_Rp;  // gamma^-1 * 2^64 mod q, Shoup
+  const u64* wmask_R;        // rows x n: NTT of the kept mask rows, R-form
+  // NTT of the last exact-gadget digit from the others (base^-2 (R - D0 - base D1)).
+  u64 ld_inv, ld_invp, ld_c0, ld_c0p, ld_c1, ld_c1p;
+};
+
+// One query of a launch.
+struct QueryDev {
+  u32 shard;          // index into the launch's shard table
+  u32 reserved;
+  const u32* seed;    // 8 ChaCha20 key words of the query's `a` seed
+  const u64* b;       // coefficient-form b of the query (n words)
+  const u64* seat_R;  // rows x n key body in R-form NTT (the packing-key seat)
+  const u64* a;       // explicit coefficient-form `a` (unseeded query), or null
+};
+
+struct ShardDev {
+  const u64* columns;  // gamma x n raw column words
+  const u64* sums_R;   // gamma x n step-1 sums, R-form NTT (the packing store)
+  const u64* tag_key;  // 2n key words
+  const u64* tags;     // gamma column tags
+};
+
+}  // namespace ig
+
+// Launchers (ig_kernels.cu). Every launcher enqueues on `stream` and returns the
+// launch status.
+namespace igk {
+using namespace ig;
+
+// Forward NTT of `rows` polynomials: out[r] = scale * NTT(in[r] mod q), scale given with
+// its Shoup companion (scale = 1 for standard form, 2^64 mod q for R-form).
+cudaError_t ntt_rows(const CrsDev& c, const u64* in, u64* out, u32 rows, u64 scale, u64 scalep,
+                     cudaStream_t s);
+
+// Shard scan over `nq` queries: for query q and column j, recomputes the column's tag and
+// b_fold[q][j] = coeff0(b_q * column_j). mode_build = 1 writes the tags of shard 0 of the
+// table into `tags_out` instead of checking.
+cudaError_t shard_scan(const CrsDev& c, const QueryDev* queries, const ShardDev* shards, u32 nq,
+                       u64* b_fold, u32* status, int mode_build, u64* tags_out, cudaStream_t s);
+
+// Step-1 sums of one shard from the NTTs of its columns (H: gamma x n standard form).
+cudaError_t store_fold(const CrsDev& c, const u64* H, u64* sums_R, cudaStream_t s);
+
+// Fused per-query respond: expansion of `a`, store gather, backward recursion with the
+// online gather, final transforms, optional mod switch. One CTA per query.
+cudaError_t respond(const CrsDev& c, const QueryDev* queries, const ShardDev* shards,
+                    u32 nq, const u64* b_fold, u64 ms_target,
+                    u64* a_out, u64* b_out, u32* status, int force_serial_expand, cudaStream_t s);
+
+size_t respond_smem_bytes(const CrsDev& c);
+}  // namespace igk

@@ -1,0 +1,1028 @@
+// Host runtime behind the C ABI of include/inspire_gb300.h: device residency of the
+// per-parameter-set constants, shards, packing stores and seats, request validation with
+// the reference's refusal rules, and the launch sequence of a respond batch.
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <random>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/inspire_gb300.h"
+#include "ig_kernels.cuh"
+
+using namespace ig;
+
+namespace {
+
+// ---------------------------------------------------------------------------------------
+// Host modular helpers over q.
+u64 mulmod(u64 a, u64 b) { return (u64)((u128)a * b % Q); }
+u64 powmod(u64 b, u64 e) {
+  u64 r = 1;
+  b %= Q;
+  while (e) {
+    if (e & 1) r = mulmod(r, b);
+    b = mulmod(b, b);
+    e >>= 1;
+  }
+  return r;
+}
+u64 invmod(u64 a) { return powmod(a, Q - 2); }
+const u64 R_MOD_Q = (u64)((((u128)1) << 64) % Q);
+
+// Least root of the search NttContext::find_primitive_root makes (math/ntt.rs:743-752),
+// so the slot order matches the reference's transform.
+u64 find_root(u64 order) {
+  const u64 e = (Q - 1) / order;
+  for (u64 g = 2; g < (1u << 16); g++) {
+    u64 c = powmod(g, e);
+    if (powmod(c, order) == 1 && powmod(c, order / 2) != 1) return c;
+  }
+  return 0;
+}
+
+// Bit-reversed power ladder f[m] (math/ntt.rs:780-804).
+std::vector<u64> ladder(size_t n, u64 psi) {
+  std::vector<u64> f(n, 0);
+  f[1] = 1;
+  for (size_t m = 1; m < n; m++) {
+    if ((m & (m - 1)) == 0)
+      f[m] = powmod(psi, n / (2 * m));
+    else
+      f[m] = mulmod(f[m & (m - 1)], f[m & (~m + 1)]);
+  }
+  return f;
+}
+
+void host_ntt(std::vector<u64>& x, const std::vector<u64>& tw) {
+  size_t n = x.size(), t = n;
+  for (size_t m = 1; m < n; m <<= 1) {
+    t >>= 1;
+    for (size_t i = 0; i < m; i++) {
+      size_t j1 = 2 * i * t;
+      for (size_t j = j1; j < j1 + t; j++) {
+        u64 u = x[j], v = mulmod(x[j + t], tw[m + i]);
+        x[j] = addq(u, v);
+        x[j + t] = subq(u, v);
+      }
+    }
+  }
+}
+
+struct HostChaCha {
+  u32 key[8];
+  u64 stream, word = 0;
+  u32 blk[16];
+  u64 have = ~0ULL;
+  HostChaCha(const uint8_t seed[32], u64 s) : stream(s) {
+    for (int i = 0; i < 8; i++) memcpy(&key[i], seed + 4 * i, 4);
+  }
+  u32 next_u32() {
+    u64 b = word / 16;
+    if (b != have) {
+      chacha20_block(key, b, stream, blk);
+      have = b;
+    }
+    return blk[word++ % 16];
+  }
+  u64 next_u64() {
+    u64 lo = next_u32();
+    return lo | ((u64)next_u32() << 32);
+  }
+};
+
+// ---------------------------------------------------------------------------------------
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+struct CrsObj {
+  u32 n = 0, logn = 0, gamma = 0, rows = 0, approx = 0;
+  u64 p = 0;
+  CrsDev dev{};
+  std::vector<void*> allocs;
+  size_t bytes = 0;
+};
+
+struct ShardSlot {
+  u64* cols = nullptr;
+  u64* sums = nullptr;
+  u64* tag_key = nullptr;
+  u64* tags = nullptr;
+};
+
+struct DbObj {
+  u64 crs = 0;
+  u32 num_shards = 0;
+  std::vector<ShardSlot> shards;
+  ShardDev* d_table = nullptr;
+  size_t bytes = 0;
+};
+
+struct SeatObj {
+  u64 crs = 0;
+  u32 n = 0, rows = 0, num_to_pack = 0;
+  u64* yR = nullptr;
+};
+
+struct StoreObj {
+  std::unordered_map<u64, SeatObj> seats;
+};
+
+std::atomic<u64> g_next_handle{0};  // process-global, monotonic (session.rs:715-738)
+std::atomic<u64> g_next_object{1};
+
+}  // namespace
+
+struct ig_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::mutex mu;
+  std::string err;
+  std::unordered_map<u64, CrsObj> crs;
+  std::unordered_map<u64, DbObj> dbs;
+  std::unordered_map<u64, StoreObj> stores;
+  std::unordered_map<std::string, DevBuf> scratch;
+  u64* zero_key = nullptr;
+  size_t zero_key_words = 0;
+  size_t obj_bytes = 0;
+  int force_serial = 0;
+};
+
+namespace {
+
+int fail(ig_ctx* c, int code, const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (c) c->err = buf;
+  return code;
+}
+
+#define IG_CUDA(ctx, call)                                                                        \
+  do {                                                                                            \
+    cudaError_t e_ = (call);                                                                      \
+    if (e_ != cudaSuccess)                                                                        \
+      return fail(ctx, e_ == cudaErrorMemoryAllocation ? IG_ERR_NOMEM : IG_ERR_CUDA, "%s: %s (%s:%d)", \
+                  #call, cudaGetErrorString(e_), __FILE__, __LINE__);                             \
+  } while (0)
+
+int dalloc(ig_ctx* c, void** p, size_t bytes, size_t* counter) {
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    cudaGetLastError();
+    return fail(c, IG_ERR_NOMEM, "device allocation of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+  }
+  if (counter) *counter += bytes;
+  c->obj_bytes += bytes;
+  return IG_OK;
+}
+
+void dfree(ig_ctx* c, void* p, size_t bytes) {
+  if (p) {
+    cudaFree(p);
+    c->obj_bytes -= bytes;
+  }
+}
+
+// Grow-only scratch buffer by name.
+int scratch(ig_ctx* c, const char* name, size_t bytes, void** out) {
+  DevBuf& b = c->scratch[name];
+  if (b.bytes < bytes) {
+    if (b.p) dfree(c, b.p, b.bytes);
+    b.p = nullptr;
+    b.bytes = 0;
+    size_t want = bytes + bytes / 4;
+    int rc = dalloc(c, &b.p, want, nullptr);
+    if (rc) return rc;
+    b.bytes = want;
+  }
+  *out = b.p;
+  return IG_OK;
+}
+
+int zero_key(ig_ctx* c, size_t words, u64** out) {
+  if (c->zero_key_words < words) {
+    if (c->zero_key) dfree(c, c->zero_key, c->zero_key_words * 8);
+    c->zero_key = nullptr;
+    int rc = dalloc(c, (void**)&c->zero_key, words * 8, nullptr);
+    if (rc) return rc;
+    c->zero_key_words = words;
+    IG_CUDA(c, cudaMemset(c->zero_key, 0, words * 8));
+  }
+  *out = c->zero_key;
+  return IG_OK;
+}
+
+template <class T>
+int upload(ig_ctx* c, CrsObj& o, const std::vector<T>& v, const T** dst) {
+  void* p;
+  int rc = dalloc(c, &p, v.size() * sizeof(T), &o.bytes);
+  if (rc) return rc;
+  o.allocs.push_back(p);
+  IG_CUDA(c, cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+  *dst = (const T*)p;
+  return IG_OK;
+}
+
+CrsObj* get_crs(ig_ctx* c, u64 h) {
+  auto it = c->crs.find(h);
+  return it == c->crs.end() ? nullptr : &it->second;
+}
+DbObj* get_db(ig_ctx* c, u64 h) {
+  auto it = c->dbs.find(h);
+  return it == c->dbs.end() ? nullptr : &it->second;
+}
+
+int sync_table_entry(ig_ctx* c, DbObj& db, u32 s) {
+  ShardDev d{db.shards[s].cols, db.shards[s].sums, db.shards[s].tag_key, db.shards[s].tags};
+  IG_CUDA(c, cudaMemcpyAsync(db.d_table + s, &d, sizeof d, cudaMemcpyHostToDevice, c->stream));
+  IG_CUDA(c, cudaStreamSynchronize(c->stream));
+  return IG_OK;
+}
+
+// Folds step 1 over `cols` into `sums` (gamma x n, R-form): gamma forward transforms,
+// then the per-slot DFT fold.
+int fold_store(ig_ctx* c, CrsObj& o, const u64* cols, u64* sums) {
+  void* H;
+  int rc = scratch(c, "fold_H", (size_t)o.gamma * o.n * 8, &H);
+  if (rc) return rc;
+  IG_CUDA(c, igk::ntt_rows(o.dev, cols, (u64*)H, o.gamma, 1, shoup_companion(1), c->stream));
+  IG_CUDA(c, igk::store_fold(o.dev, (const u64*)H, sums, c->stream));
+  return IG_OK;
+}
+
+int build_store(ig_ctx* c, DbObj& db, CrsObj& o, u32 s) {
+  ShardSlot& sl = db.shards[s];
+  if (!sl.cols)
+    return fail(c, IG_ERR_ARG, "shard %u: no columns uploaded; precompute_packing needs the shard's columns", s);
+  const size_t n = o.n, g = o.gamma;
+  if (!sl.sums) {
+    int rc = dalloc(c, (void**)&sl.sums, g * n * 8, &db.bytes);
+    if (rc) return rc;
+    rc = dalloc(c, (void**)&sl.tag_key, 2 * n * 8, &db.bytes);
+    if (rc) return rc;
+    rc = dalloc(c, (void**)&sl.tags, g * 8, &db.bytes);
+    if (rc) return rc;
+  }
+  // Tag key: two words per column word below 2^61 - 1, drawn from OS entropy and never
+  // leaving the device (shard_store.rs:127-135).
+  std::random_device rd;
+  uint8_t seed[32];
+  for (int i = 0; i < 8; i++) {
+    u32 v = rd();
+    memcpy(seed + 4 * i, &v, 4);
+  }
+  HostChaCha rng(seed, 0);
+  std::vector<u64> key(2 * n);
+  for (auto& k : key) {
+    u64 cand;
+    do cand = rng.next_u64() >> 3;
+    while (cand >= (1ULL << 61) - 1);
+    k = cand;
+  }
+  IG_CUDA(c, cudaMemcpyAsync(sl.tag_key, key.data(), key.size() * 8, cudaMemcpyHostToDevice, c->stream));
+  // Tags through the scan kernel in build mode.
+  ShardDev sd{sl.cols, nullptr, sl.tag_key, nullptr};
+  QueryDev qd{};
+  qd.shard = 0;
+  void *dq, *ds;
+  int rc = scratch(c, "build_q", sizeof(QueryDev), &dq);
+  if (rc) return rc;
+  rc = scratch(c, "build_s", sizeof(ShardDev), &ds);
+  if (rc) return rc;
+  IG_CUDA(c, cudaMemcpyAsync(dq, &qd, sizeof qd, cudaMemcpyHostToDevice, c->stream));
+  IG_CUDA(c, cudaMemcpyAsync(ds, &sd, sizeof sd, cudaMemcpyHostToDevice, c->stream));
+  IG_CUDA(c, igk::shard_scan(o.dev, (const QueryDev*)dq, (const ShardDev*)ds, 1, nullptr, nullptr, 1, sl.tags,
+                             c->stream));
+  rc = fold_store(c, o, sl.cols, sl.sums);
+  if (rc) return rc;
+  IG_CUDA(c, cudaStreamSynchronize(c->stream));
+  return sync_table_entry(c, db, s);
+}
+
+}  // namespace
+
+// =========================================================================================
+extern "C" {
+
+int ig_ctx_create(int device, ig_ctx** out) {
+  if (!out) return IG_ERR_ARG;
+  *out = nullptr;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+    cudaGetLastError();
+    return IG_ERR_CUDA;
+  }
+  if (device < 0 || device >= count) return IG_ERR_ARG;
+  if (cudaSetDevice(device) != cudaSuccess) return IG_ERR_CUDA;
+  auto* c = new ig_ctx();
+  c->device = device;
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return IG_ERR_CUDA;
+  }
+  *out = c;
+  return IG_OK;
+}
+
+void ig_ctx_destroy(ig_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  for (auto& kv : c->crs)
+    for (void* p : kv.second.allocs) cudaFree(p);
+  for (auto& kv : c->dbs) {
+    for (auto& s : kv.second.shards) {
+      cudaFree(s.cols);
+      cudaFree(s.sums);
+      cudaFree(s.tag_key);
+      cudaFree(s.tags);
+    }
+    cudaFree(kv.second.d_table);
+  }
+  for (auto& kv : c->stores)
+    for (auto& s : kv.second.seats) cudaFree(s.second.yR);
+  for (auto& kv : c->scratch) cudaFree(kv.second.p);
+  cudaFree(c->zero_key);
+  cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+int ig_last_error(const ig_ctx* c, char* buf, size_t len) {
+  if (!c || !buf || len == 0) return IG_ERR_ARG;
+  snprintf(buf, len, "%s", c->err.c_str());
+  return IG_OK;
+}
+
+void* ig_ctx_stream(ig_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+uint64_t ig_ctx_device_bytes(const ig_ctx* c) { return c ? c->obj_bytes : 0; }
+
+int ig_crs_create(ig_ctx* c, uint32_t n, uint64_t q, uint64_t p, uint64_t gadget_base, uint32_t glen, int approx,
+                  uint32_t gamma, const uint8_t w_seed[32], uint64_t* crs_out) {
+  if (!c || !w_seed || !crs_out) return fail(c, IG_ERR_ARG, "ig_crs_create: null argument");
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  if (q != Q)
+    return fail(c, IG_ERR_UNSUPPORTED, "ciphertext modulus %llu is not served on the GPU path; only q = 2^60-2^14+1",
+                (unsigned long long)q);
+  if (gadget_base != (1ULL << 20) || glen != 3)
+    return fail(c, IG_ERR_UNSUPPORTED, "packing gadget base %llu length %u is not served; only base 2^20 length 3",
+                (unsigned long long)gadget_base, glen);
+  if (n < 256 || n > 2048 || (n & (n - 1)))
+    return fail(c, IG_ERR_UNSUPPORTED, "ring_dim %u is not served; the GPU path covers powers of two in [256, 2048]", n);
+  if (gamma == 0 || (gamma & (gamma - 1)) || gamma > n / 2)
+    return fail(c, IG_ERR_WIDTH,
+                "InspiRING packing width %u is illegal at ring_dim %u: the width must be a power of two in [1, %u]",
+                gamma, n, n / 2);
+  if (p < 2 || p >= q) return fail(c, IG_ERR_ARG, "plaintext modulus %llu outside [2, q)", (unsigned long long)p);
+  CrsObj o;
+  o.n = n;
+  o.logn = 0;
+  while ((1u << o.logn) < n) o.logn++;
+  o.gamma = gamma;
+  o.approx = approx ? 1 : 0;
+  o.rows = glen - o.approx;
+  o.p = p;
+  const u64 two_n = 2ULL * n;
+  const u64 psi = find_root(two_n);
+  std::vector<u64> tw = ladder(n, psi), itw = ladder(n, invmod(psi));
+  std::vector<u64> twp(n), itwp(n);
+  for (u32 m = 0; m < n; m++) {
+    twp[m] = shoup_companion(tw[m]);
+    itwp[m] = shoup_companion(itw[m]);
+  }
+  // Slot roots: slot t of the forward transform of X holds root w_t = w0^e_t.
+  std::vector<u64> X(n, 0);
+  X[1] = 1;
+  host_ntt(X, tw);
+  std::unordered_map<u64, u32> exp_of;
+  u64 w0 = X[0], w0sq = mulmod(w0, w0), pw = w0;
+  for (u64 e = 1; e < two_n; e += 2) {
+    exp_of[pw] = (u32)e;
+    pw = mulmod(pw, w0sq);
+  }
+  std::vector<uint16_t> slot_exp(n), exp_slot(n, 0xffff);
+  for (u32 t = 0; t < n; t++) {
+    auto it = exp_of.find(X[t]);
+    if (it == exp_of.end()) return fail(c, IG_ERR_UNSUPPORTED, "automorphism tables are undefined at ring_dim %u", n);
+    slot_exp[t] = (uint16_t)it->second;
+    exp_slot[it->second / 2] = (uint16_t)t;
+  }
+  // Slots and odd exponents must pair one to one: the kernels index shared memory by
+  // these tables.
+  for (u32 e = 0; e < n; e++)
+    if (exp_slot[e] >= n)
+      return fail(c, IG_ERR_UNSUPPORTED, "automorphism tables are undefined at ring_dim %u: slot roots repeat", n);
+  const u64 g = two_n / gamma + 1;
+  u64 ginv = 1;  // g^(gamma-1) = g^-1 in Z*_2n
+  for (u32 k = 0; k + 1 < gamma; k++) ginv = ginv * g % two_n;
+  std::vector<u32> gpow(gamma), cpow(gamma), m_of_i(gamma);
+  u64 a = 1, b = 1;
+  const u64 L = two_n / gamma;
+  for (u32 i = 0; i < gamma; i++) {
+    gpow[i] = (u32)a;
+    cpow[i] = (u32)b;
+    if ((b - 1) % L != 0) return fail(c, IG_ERR_UNSUPPORTED, "generator subgroup is not 1 mod 2n/gamma");
+    m_of_i[i] = (u32)((b - 1) / L);
+    a = a * g % two_n;
+    b = b * ginv % two_n;
+  }
+  std::vector<u64> pow_root_R(two_n);
+  u64 acc = 1;
+  for (u64 e = 0; e < two_n; e++) {
+    pow_root_R[e] = mulmod(acc, R_MOD_Q);
+    acc = mulmod(acc, w0);
+  }
+  // Offline mask rows: ChaCha20(w_seed) on stream 0 (exact) or gamma (approximate),
+  // next_u64 mod q, the dropped digits' rows skipped (inspiring2.rs:839-887).
+  HostChaCha rng(w_seed, o.approx ? gamma : 0);
+  std::vector<u64> mask;
+  for (u32 r = 0; r < glen; r++)
+    for (u32 k = 0; k < n; k++) {
+      u64 v = rng.next_u64() % Q;
+      if (r >= o.approx) mask.push_back(v);
+    }
+  CrsDev& d = o.dev;
+  d.n = n;
+  d.logn = o.logn;
+  d.gamma = gamma;
+  d.rows = o.rows;
+  d.approx = o.approx;
+  int rc;
+  if ((rc = upload(c, o, tw, &d.tw)) || (rc = upload(c, o, twp, &d.twp)) || (rc = upload(c, o, itw, &d.itw)) ||
+      (rc = upload(c, o, itwp, &d.itwp)) || (rc = upload(c, o, slot_exp, &d.slot_exp)) ||
+      (rc = upload(c, o, exp_slot, &d.exp_slot)) || (rc = upload(c, o, gpow, &d.gpow)) ||
+      (rc = upload(c, o, cpow, &d.cpow)) || (rc = upload(c, o, m_of_i, &d.m_of_i)) ||
+      (rc = upload(c, o, pow_root_R, &d.pow_root_R))) {
+    for (void* p2 : o.allocs) cudaFree(p2);
+    return rc;
+  }
+  d.ninv = invmod(n);
+  d.ninvp = shoup_companion(d.ninv);
+  d.inv_gamma_R = mulmod(invmod(gamma), R_MOD_Q);
+  d.inv_gamma_Rp = shoup_companion(d.inv_gamma_R);
+  // Last exact digit: base^-2 (R - D0 - base D1) (inspiring2.rs:1094-1161).
+  const u64 inv = invmod(1ULL << 40);
+  d.ld_inv = inv;
+  d.ld_c0 = negq(inv);
+  d.ld_c1 = negq(mulmod(inv, 1ULL << 20));
+  d.ld_invp = shoup_companion(d.ld_inv);
+  d.ld_c0p = shoup_companion(d.ld_c0);
+  d.ld_c1p = shoup_companion(d.ld_c1);
+  // Mask rows -> NTT, R-form.
+  void* mraw;
+  rc = scratch(c, "mask_raw", mask.size() * 8, &mraw);
+  if (rc) return rc;
+  void* wm;
+  rc = dalloc(c, &wm, mask.size() * 8, &o.bytes);
+  if (rc) return rc;
+  o.allocs.push_back(wm);
+  IG_CUDA(c, cudaMemcpyAsync(mraw, mask.data(), mask.size() * 8, cudaMemcpyHostToDevice, c->stream));
+  IG_CUDA(c, igk::ntt_rows(d, (const u64*)mraw, (u64*)wm, o.rows, R_MOD_Q, shoup_companion(R_MOD_Q), c->stream));
+  IG_CUDA(c, cudaStreamSynchronize(c->stream));
+  d.wmask_R = (const u64*)wm;
+  const u64 h = g_next_object++;
+  c->crs[h] = o;
+  *crs_out = h;
+  return IG_OK;
+}
+
+int ig_crs_destroy(ig_ctx* c, uint64_t crs) {
+  if (!c) return IG_ERR_ARG;
+  std::lock_guard<std::mutex> lk(c->mu);
+  auto it = c->crs.find(crs);
+  if (it == c->crs.end()) return fail(c, IG_ERR_HANDLE, "unknown CRS handle %llu", (unsigned long long)crs);
+  cudaStreamSynchronize(c->stream);
+  for (void* p : it->second.allocs) cudaFree(p);
+  c->obj_bytes -= it->second.bytes;
+  c->crs.erase(it);
+  return IG_OK;
+}
+
+int ig_crs_key_rows(ig_ctx* c, uint64_t crs, uint32_t* rows) {
+  if (!c || !rows) return IG_ERR_ARG;
+  std::lock_guard<std::mutex> lk(c->mu);
+  CrsObj* o = get_crs(c, crs);
+  if (!o) return fail(c, IG_ERR_HANDLE, "unknown CRS handle %llu", (unsigned long long)crs);
+  *rows = o->rows;
+  return IG_OK;
+}
+
+int ig_db_create(ig_ctx* c, uint64_t crs, uint32_t num_shards, uint64_t* db_out) {
+  if (!c || !db_out || num_shards == 0) return fail(c, IG_ERR_ARG, "ig_db_create: null output or zero shards");
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  if (!get_crs(c, crs)) return fail(c, IG_ERR_HANDLE, "unknown CRS handle %llu", (unsigned long long)crs);
+  DbObj db;
+  db.crs = crs;
+  db.num_shards = num_shards;
+  db.shards.resize(num_shards);
+  int rc = dalloc(c, (void**)&db.d_table, num_shards * sizeof(ShardDev), &db.bytes);
+  if (rc) return rc;
+  IG_CUDA(c, cudaMemset(db.d_table, 0, num_shards * sizeof(ShardDev)));
+  const u64 h = g_next_object++;
+  c->dbs[h] = std::move(db);
+  *db_out = h;
+  return IG_OK;
+}
+
+int ig_db_destroy(ig_ctx* c, uint64_t dbh) {
+  if (!c) return IG_ERR_ARG;
+  std::lock_guard<std::mutex> lk(c->mu);
+  auto it = c->dbs.find(dbh);
+  if (it == c->dbs.end()) return fail(c, IG_ERR_HANDLE, "unknown database handle %llu", (unsigned long long)dbh);
+  cudaStreamSynchronize(c->stream);
+  for (auto& s : it->second.shards) {
+    cudaFree(s.cols);
+    cudaFree(s.sums);
+    cudaFree(s.tag_key);
+    cudaFree(s.tags);
+  }
+  cudaFree(it->second.d_table);
+  c->obj_bytes -= it->second.bytes;
+  c->dbs.erase(it);
+  return IG_OK;
+}
+
+static int set_shard(ig_ctx* c, uint64_t dbh, uint32_t s, const uint64_t* cols, cudaMemcpyKind kind) {
+  if (!c || !cols) return fail(c, IG_ERR_ARG, "ig_db_set_shard: null columns");
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  DbObj* db = get_db(c, dbh);
+  if (!db) return fail(c, IG_ERR_HANDLE, "unknown database handle %llu", (unsigned long long)dbh);
+  if (s >= db->num_shards)
+    return fail(c, IG_ERR_ARG, "shard %u not found at dense position %u; encoded database has %u shards", s, s,
+                db->num_shards);
+  CrsObj* o = get_crs(c, db->crs);
+  const size_t bytes = (size_t)o->gamma * o->n * 8;
+  ShardSlot& sl = db->shards[s];
+  if (!sl.cols) {
+    int rc = dalloc(c, (void**)&sl.cols, bytes, &db->bytes);
+    if (rc) return rc;
+  }
+  IG_CUDA(c, cudaMemcpyAsync(sl.cols, cols, bytes, kind, c->stream));
+  IG_CUDA(c, cudaStreamSynchronize(c->stream));
+  return sync_table_entry(c, *db, s);
+}
+
+int ig_db_set_shard(ig_ctx* c, uint64_t db, uint32_t s, const uint64_t* cols) {
+  return set_shard(c, db, s, cols, cudaMemcpyHostToDevice);
+}
+int ig_db_set_shard_device(ig_ctx* c, uint64_t db, uint32_t s, const uint64_t* cols) {
+  return set_shard(c, db, s, cols, cudaMemcpyDeviceToDevice);
+}
+
+int ig_db_precompute_packing(ig_ctx* c, uint64_t dbh, uint32_t s) {
+  if (!c) return IG_ERR_ARG;
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  DbObj* db = get_db(c, dbh);
+  if (!db) return fail(c, IG_ERR_HANDLE, "unknown database handle %llu", (unsigned long long)dbh);
+  if (s >= db->num_shards) return fail(c, IG_ERR_ARG, "shard %u out of range (%u shards)", s, db->num_shards);
+  return build_store(c, *db, *get_crs(c, db->crs), s);
+}
+
+int ig_db_precompute_packing_all(ig_ctx* c, uint64_t dbh) {
+  if (!c) return IG_ERR_ARG;
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  DbObj* db = get_db(c, dbh);
+  if (!db) return fail(c, IG_ERR_HANDLE, "unknown database handle %llu", (unsigned long long)dbh);
+  CrsObj* o = get_crs(c, db->crs);
+  for (u32 s = 0; s < db->num_shards; s++) {
+    int rc = build_store(c, *db, *o, s);
+    if (rc) return rc;
+  }
+  return IG_OK;
+}
+
+int ig_db_drop_packing_store(ig_ctx* c, uint64_t dbh, uint32_t s) {
+  if (!c) return IG_ERR_ARG;
+  std::lock_guard<std::mutex> lk(c->mu);
+  DbObj* db = get_db(c, dbh);
+  if (!db) return fail(c, IG_ERR_HANDLE, "unknown database handle %llu", (unsigned long long)dbh);
+  if (s >= db->num_shards) return fail(c, IG_ERR_ARG, "shard %u out of range", s);
+  CrsObj* o = get_crs(c, db->crs);
+  cudaStreamSynchronize(c->stream);
+  ShardSlot& sl = db->shards[s];
+  const size_t g = o->gamma, n = o->n;
+  if (sl.sums) {
+    cudaFree(sl.sums);
+    cudaFree(sl.tag_key);
+    cudaFree(sl.tags);
+    const size_t freed = g * n * 8 + 2 * n * 8 + g * 8;
+    db->bytes -= freed;
+    c->obj_bytes -= freed;
+    sl.sums = sl.tag_key = sl.tags = nullptr;
+  }
+  return sync_table_entry(c, *db, s);
+}
+
+int ig_db_has_store(ig_ctx* c, uint64_t dbh, uint32_t s, int* out) {
+  if (!c || !out) return IG_ERR_ARG;
+  std::lock_guard<std::mutex> lk(c->mu);
+  DbObj* db = get_db(c, dbh);
+  if (!db) return fail(c, IG_ERR_HANDLE, "unknown database handle %llu", (unsigned long long)dbh);
+  if (s >= db->num_shards) return fail(c, IG_ERR_ARG, "shard %u out of range", s);
+  *out = db->shards[s].sums != nullptr;
+  return IG_OK;
+}
+
+// ---- session store -------------------------------------------------------------------
+int ig_session_store_create(ig_ctx* c, uint64_t* out) {
+  if (!c || !out) return IG_ERR_ARG;
+  std::lock_guard<std::mutex> lk(c->mu);
+  const u64 h = g_next_object++;
+  c->stores[h] = StoreObj();
+  *out = h;
+  return IG_OK;
+}
+
+int ig_session_store_destroy(ig_ctx* c, uint64_t st) {
+  if (!c) return IG_ERR_ARG;
+  std::lock_guard<std::mutex> lk(c->mu);
+  auto it = c->stores.find(st);
+  if (it == c->stores.end()) return fail(c, IG_ERR_HANDLE, "unknown session store %llu", (unsigned long long)st);
+  cudaStreamSynchronize(c->stream);
+  for (auto& s : it->second.seats) dfree(c, s.second.yR, (size_t)s.second.rows * s.second.n * 8);
+  c->stores.erase(it);
+  return IG_OK;
+}
+
+// PackingKeySeat::build checks (session.rs:600-625, 661-697, 766-826), then the key
+// body's NTT in R-form on the device.
+static int make_seat(ig_ctx* c, CrsObj& o, const uint64_t* y_body, uint32_t rows, uint32_t num_to_pack, u64* dst,
+                     bool y_on_device) {
+  if (rows != o.rows)
+    return fail(c, IG_ERR_WIDTH,
+                "packing-key material mismatch: client sent %u y_body polynomials, the server decomposes into %u "
+                "digits, and every digit needs its key polynomial. The client must re-derive its packing keys "
+                "against the current CRS.",
+                rows, o.rows);
+  if (num_to_pack != o.gamma)
+    return fail(c, IG_ERR_WIDTH,
+                "packing-key width mismatch: client keys declare gamma = %u, server pack params use gamma = %u. "
+                "The client must re-derive its packing keys against the current CRS.",
+                num_to_pack, o.gamma);
+  const u64* src = y_body;
+  if (!y_on_device) {
+    void* raw;
+    int rc = scratch(c, "seat_raw", (size_t)rows * o.n * 8, &raw);
+    if (rc) return rc;
+    IG_CUDA(c, cudaMemcpyAsync(raw, y_body, (size_t)rows * o.n * 8, cudaMemcpyHostToDevice, c->stream));
+    src = (const u64*)raw;
+  }
+  IG_CUDA(c, igk::ntt_rows(o.dev, src, dst, rows, R_MOD_Q, shoup_companion(R_MOD_Q), c->stream));
+  return IG_OK;
+}
+
+int ig_session_register(ig_ctx* c, uint64_t st, uint64_t crs, const uint64_t* y_body, uint32_t rows,
+                        uint32_t num_to_pack, uint64_t* handle_out) {
+  if (!c || !y_body || !handle_out) return fail(c, IG_ERR_ARG, "ig_session_register: null argument");
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  auto it = c->stores.find(st);
+  if (it == c->stores.end()) return fail(c, IG_ERR_HANDLE, "unknown session store %llu", (unsigned long long)st);
+  CrsObj* o = get_crs(c, crs);
+  if (!o) return fail(c, IG_ERR_HANDLE, "unknown CRS handle %llu", (unsigned long long)crs);
+  SeatObj seat;
+  seat.crs = crs;
+  seat.n = o->n;
+  seat.rows = rows;
+  seat.num_to_pack = num_to_pack;
+  if (rows == o->rows) {
+    int rc = dalloc(c, (void**)&seat.yR, (size_t)rows * o->n * 8, nullptr);
+    if (rc) return rc;
+  }
+  int rc = make_seat(c, *o, y_body, rows, num_to_pack, seat.yR, false);
+  if (rc) {
+    dfree(c, seat.yR, (size_t)rows * o->n * 8);
+    return rc;
+  }
+  IG_CUDA(c, cudaStreamSynchronize(c->stream));
+  u64 h = g_next_handle.load();
+  do {
+    if (h == ~0ULL) {
+      dfree(c, seat.yR, (size_t)rows * o->n * 8);
+      return fail(c, IG_ERR_EXHAUSTED,
+                  "ServerSessionStore handle space exhausted at %llu; refusing the session handshake because "
+                  "handle reuse could resolve stale clients to another client's packing keys",
+                  (unsigned long long)h);
+    }
+  } while (!g_next_handle.compare_exchange_weak(h, h + 1));
+  it->second.seats[h] = seat;
+  *handle_out = h;
+  return IG_OK;
+}
+
+int ig_session_remove(ig_ctx* c, uint64_t st, uint64_t handle, int* removed) {
+  if (!c || !removed) return IG_ERR_ARG;
+  std::lock_guard<std::mutex> lk(c->mu);
+  auto it = c->stores.find(st);
+  if (it == c->stores.end()) return fail(c, IG_ERR_HANDLE, "unknown session store %llu", (unsigned long long)st);
+  auto s = it->second.seats.find(handle);
+  *removed = s != it->second.seats.end();
+  if (*removed) {
+    cudaStreamSynchronize(c->stream);
+    dfree(c, s->second.yR, (size_t)s->second.rows * s->second.n * 8);
+    it->second.seats.erase(s);
+  }
+  return IG_OK;
+}
+
+int ig_session_len(ig_ctx* c, uint64_t st, uint64_t* len) {
+  if (!c || !len) return IG_ERR_ARG;
+  std::lock_guard<std::mutex> lk(c->mu);
+  auto it = c->stores.find(st);
+  if (it == c->stores.end()) return fail(c, IG_ERR_HANDLE, "unknown session store %llu", (unsigned long long)st);
+  *len = it->second.seats.size();
+  return IG_OK;
+}
+
+int ig_session_contains(ig_ctx* c, uint64_t st, uint64_t handle, int* present) {
+  if (!c || !present) return IG_ERR_ARG;
+  std::lock_guard<std::mutex> lk(c->mu);
+  auto it = c->stores.find(st);
+  if (it == c->stores.end()) return fail(c, IG_ERR_HANDLE, "unknown session store %llu", (unsigned long long)st);
+  *present = it->second.seats.count(handle) ? 1 : 0;
+  return IG_OK;
+}
+
+// ---- respond ---------------------------------------------------------------------------
+static int resolve_seat(ig_ctx* c, CrsObj& o, uint64_t st, uint64_t handle, const uint64_t* inline_y,
+                        uint32_t inline_rows, uint32_t inline_ntp, const u64** seat_out) {
+  if (inline_y) {
+    void* p;
+    int rc = scratch(c, "inline_seat", (size_t)o.rows * o.n * 8, &p);
+    if (rc) return rc;
+    rc = make_seat(c, o, inline_y, inline_rows, inline_ntp, (u64*)p, false);
+    if (rc) return rc;
+    *seat_out = (const u64*)p;
+    return IG_OK;
+  }
+  auto it = c->stores.find(st);
+  if (it == c->stores.end())
+    return fail(c, IG_ERR_HANDLE,
+                "query references session_handle %llu but no ServerSessionStore was supplied to "
+                "respond_*_with_session",
+                (unsigned long long)handle);
+  auto s = it->second.seats.find(handle);
+  if (s == it->second.seats.end())
+    return fail(c, IG_ERR_HANDLE, "ServerSessionStore has no entry for session_handle %llu",
+                (unsigned long long)handle);
+  const SeatObj& seat = s->second;
+  if (seat.n != o.n || seat.rows != o.rows)
+    return fail(c, IG_ERR_SHAPE,
+                "packing-key seat is for another ring or gadget: it holds %u key rows on ring_dim %u, the server "
+                "packs %u rows on ring_dim %u. The client must re-derive its packing keys against the current CRS.",
+                seat.rows, seat.n, o.rows, o.n);
+  if (seat.num_to_pack != o.gamma)
+    return fail(c, IG_ERR_WIDTH,
+                "packing-key width mismatch: client keys declare gamma = %u, server pack params use gamma = %u.",
+                seat.num_to_pack, o.gamma);
+  *seat_out = seat.yR;
+  return IG_OK;
+}
+
+static int respond_host(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_t handle, const uint64_t* inline_y,
+                        uint32_t inline_rows, uint32_t inline_ntp, uint32_t count, const uint32_t* shard_ids,
+                        const uint8_t* seeds, const uint64_t* as, const uint64_t* bs, uint64_t ms_target,
+                        uint64_t* a_out, uint64_t* b_out) {
+  if (!c) return IG_ERR_ARG;
+  if (count == 0 || !shard_ids || (!seeds && !as) || !bs || !a_out || !b_out)
+    return fail(c, IG_ERR_ARG, "respond: empty batch or null buffer");
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  DbObj* db = get_db(c, dbh);
+  if (!db) return fail(c, IG_ERR_HANDLE, "unknown database handle %llu", (unsigned long long)dbh);
+  CrsObj& o = *get_crs(c, db->crs);
+  const size_t n = o.n, g = o.gamma;
+  if (ms_target && (ms_target >= Q || ms_target < o.p || ms_target % (2 * n) != 1))
+    return fail(c, IG_ERR_ARG, "mod-switch target_modulus %llu must be in [p, q) and 1 mod 2d",
+                (unsigned long long)ms_target);
+  const u64* seat;
+  int rc = resolve_seat(c, o, st, handle, inline_y, inline_rows, inline_ntp, &seat);
+  if (rc) return rc;
+  // checked_shard (respond.rs:601-611) for every query before any work.
+  std::unordered_map<u32, u32> local;
+  std::vector<u32> distinct;
+  for (u32 i = 0; i < count; i++) {
+    const u32 s = shard_ids[i];
+    if (s >= db->num_shards)
+      return fail(c, IG_ERR_ARG,
+                  "respond_seeded_with_seat: shard %u not found at dense position %u; encoded database has %u shards",
+                  s, s, db->num_shards);
+    if (!db->shards[s].cols)
+      return fail(c, IG_ERR_ARG, "respond_seeded_with_seat: shard %u holds no columns", s);
+    if (!local.count(s)) {
+      local[s] = (u32)distinct.size();
+      distinct.push_back(s);
+    }
+  }
+  // Shard table for this launch; shards without a store get a transient fold.
+  std::vector<ShardDev> table(distinct.size());
+  u32 transient = 0;
+  for (u32 s : distinct)
+    if (!db->shards[s].sums) transient++;
+  void* tsums = nullptr;
+  if (transient) {
+    rc = scratch(c, "transient_sums", (size_t)transient * g * n * 8, &tsums);
+    if (rc) return rc;
+  }
+  u64* zkey;
+  rc = zero_key(c, 2 * n, &zkey);
+  if (rc) return rc;
+  u32 tk = 0;
+  for (size_t k = 0; k < distinct.size(); k++) {
+    const ShardSlot& sl = db->shards[distinct[k]];
+    if (sl.sums) {
+      table[k] = ShardDev{sl.cols, sl.sums, sl.tag_key, sl.tags};
+    } else {
+      u64* sums = (u64*)tsums + (size_t)tk++ * g * n;
+      rc = fold_store(c, o, sl.cols, sums);
+      if (rc) return rc;
+      table[k] = ShardDev{sl.cols, sums, zkey, nullptr};
+    }
+  }
+  void *d_table, *d_q, *d_seeds, *d_bs, *d_a, *d_b, *d_fold, *d_status;
+  const size_t seed_bytes = as ? (size_t)count * n * 8 : (size_t)count * 32;
+  if ((rc = scratch(c, "table", table.size() * sizeof(ShardDev), &d_table)) ||
+      (rc = scratch(c, "queries", count * sizeof(QueryDev), &d_q)) || (rc = scratch(c, "seeds", seed_bytes, &d_seeds)) ||
+      (rc = scratch(c, "bs", count * n * 8, &d_bs)) || (rc = scratch(c, "a_out", count * n * 8, &d_a)) ||
+      (rc = scratch(c, "b_out", count * n * 8, &d_b)) || (rc = scratch(c, "fold", count * g * 8, &d_fold)) ||
+      (rc = scratch(c, "status", count * 4, &d_status)))
+    return rc;
+  std::vector<QueryDev> qs(count);
+  for (u32 i = 0; i < count; i++) {
+    qs[i].shard = local[shard_ids[i]];
+    qs[i].reserved = 0;
+    qs[i].seed = as ? nullptr : (const u32*)((const uint8_t*)d_seeds + (size_t)i * 32);
+    qs[i].a = as ? (const u64*)d_seeds + (size_t)i * n : nullptr;
+    qs[i].b = (const u64*)d_bs + (size_t)i * n;
+    qs[i].seat_R = seat;
+  }
+  cudaStream_t s = c->stream;
+  IG_CUDA(c, cudaMemcpyAsync(d_table, table.data(), table.size() * sizeof(ShardDev), cudaMemcpyHostToDevice, s));
+  IG_CUDA(c, cudaMemcpyAsync(d_q, qs.data(), count * sizeof(QueryDev), cudaMemcpyHostToDevice, s));
+  IG_CUDA(c, cudaMemcpyAsync(d_seeds, as ? (const void*)as : (const void*)seeds, seed_bytes, cudaMemcpyHostToDevice, s));
+  IG_CUDA(c, cudaMemcpyAsync(d_bs, bs, (size_t)count * n * 8, cudaMemcpyHostToDevice, s));
+  IG_CUDA(c, cudaMemsetAsync(d_status, 0, count * 4, s));
+  IG_CUDA(c, igk::shard_scan(o.dev, (const QueryDev*)d_q, (const ShardDev*)d_table, count, (u64*)d_fold,
+                             (u32*)d_status, 0, nullptr, s));
+  IG_CUDA(c, igk::respond(o.dev, (const QueryDev*)d_q, (const ShardDev*)d_table, count, (const u64*)d_fold, ms_target,
+                          (u64*)d_a, (u64*)d_b, (u32*)d_status, c->force_serial, s));
+  std::vector<u32> status(count);
+  IG_CUDA(c, cudaMemcpyAsync(status.data(), d_status, count * 4, cudaMemcpyDeviceToHost, s));
+  IG_CUDA(c, cudaStreamSynchronize(s));
+  for (u32 i = 0; i < count; i++) {
+    if (status[i] & DEV_TAG_MISMATCH)
+      return fail(c, IG_ERR_STORE_REFUSED,
+                  "shard %u: packing store refused: a column is not the column the store was built from. The shard "
+                  "changed after the build; rebuild the store before serving it",
+                  shard_ids[i]);
+    if (status[i]) return fail(c, IG_ERR_DEVICE, "query %u: respond kernel status %u", i, status[i]);
+  }
+  IG_CUDA(c, cudaMemcpyAsync(a_out, d_a, (size_t)count * n * 8, cudaMemcpyDeviceToHost, s));
+  IG_CUDA(c, cudaMemcpyAsync(b_out, d_b, (size_t)count * n * 8, cudaMemcpyDeviceToHost, s));
+  IG_CUDA(c, cudaStreamSynchronize(s));
+  return IG_OK;
+}
+
+int ig_respond_seeded_batch(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_t handle, const uint64_t* inline_y,
+                            uint32_t inline_rows, uint32_t inline_ntp, uint32_t count, const uint32_t* shard_ids,
+                            const uint8_t* seeds, const uint64_t* bs, uint64_t ms_target, uint64_t* a_out,
+                            uint64_t* b_out) {
+  if (!seeds && c) return fail(c, IG_ERR_ARG, "ig_respond_seeded_batch: null seeds");
+  return respond_host(c, dbh, st, handle, inline_y, inline_rows, inline_ntp, count, shard_ids, seeds, nullptr, bs,
+                      ms_target, a_out, b_out);
+}
+
+int ig_respond_batch(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_t handle, const uint64_t* inline_y,
+                     uint32_t inline_rows, uint32_t inline_ntp, uint32_t count, const uint32_t* shard_ids,
+                     const uint64_t* as, const uint64_t* bs, uint64_t ms_target, uint64_t* a_out, uint64_t* b_out) {
+  if (!as && c) return fail(c, IG_ERR_ARG, "ig_respond_batch: null a");
+  return respond_host(c, dbh, st, handle, inline_y, inline_rows, inline_ntp, count, shard_ids, nullptr, as, bs,
+                      ms_target, a_out, b_out);
+}
+
+int ig_respond_seeded_batch_device(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_t handle, uint32_t count,
+                                   const uint32_t* shard_ids, const uint8_t* d_seeds, const uint64_t* d_bs,
+                                   uint64_t ms_target, uint64_t* d_a, uint64_t* d_b, uint32_t* d_status) {
+  if (!c) return IG_ERR_ARG;
+  if (count == 0 || !shard_ids || !d_seeds || !d_bs || !d_a || !d_b || !d_status)
+    return fail(c, IG_ERR_ARG, "ig_respond_seeded_batch_device: empty batch or null buffer");
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  DbObj* db = get_db(c, dbh);
+  if (!db) return fail(c, IG_ERR_HANDLE, "unknown database handle %llu", (unsigned long long)dbh);
+  CrsObj& o = *get_crs(c, db->crs);
+  const size_t n = o.n, g = o.gamma;
+  if (ms_target && (ms_target >= Q || ms_target < o.p || ms_target % (2 * n) != 1))
+    return fail(c, IG_ERR_ARG, "mod-switch target_modulus %llu must be in [p, q) and 1 mod 2d",
+                (unsigned long long)ms_target);
+  const u64* seat;
+  int rc = resolve_seat(c, o, st, handle, nullptr, 0, 0, &seat);
+  if (rc) return rc;
+  for (u32 i = 0; i < count; i++) {
+    const u32 s = shard_ids[i];
+    if (s >= db->num_shards) return fail(c, IG_ERR_ARG, "shard %u not found; encoded database has %u shards", s, db->num_shards);
+    if (!db->shards[s].sums)
+      return fail(c, IG_ERR_ARG, "shard %u has no packing store; the device-resident path serves stored shards", s);
+  }
+  void *d_q, *d_fold;
+  if ((rc = scratch(c, "dev_queries", count * sizeof(QueryDev), &d_q)) ||
+      (rc = scratch(c, "dev_fold", count * g * 8, &d_fold)))
+    return rc;
+  std::vector<QueryDev> qs(count);
+  for (u32 i = 0; i < count; i++) {
+    qs[i].shard = shard_ids[i];
+    qs[i].reserved = 0;
+    qs[i].seed = (const u32*)(d_seeds + (size_t)i * 32);
+    qs[i].a = nullptr;
+    qs[i].b = d_bs + (size_t)i * n;
+    qs[i].seat_R = seat;
+  }
+  cudaStream_t s = c->stream;
+  IG_CUDA(c, cudaMemcpyAsync(d_q, qs.data(), count * sizeof(QueryDev), cudaMemcpyHostToDevice, s));
+  IG_CUDA(c, cudaMemsetAsync(d_status, 0, count * 4, s));
+  IG_CUDA(c, igk::shard_scan(o.dev, (const QueryDev*)d_q, db->d_table, count, (u64*)d_fold, d_status, 0, nullptr, s));
+  IG_CUDA(c, igk::respond(o.dev, (const QueryDev*)d_q, db->d_table, count, (const u64*)d_fold, ms_target, d_a, d_b,
+                          d_status, c->force_serial, s));
+  return IG_OK;
+}
+
+// ---- wire -------------------------------------------------------------------------------
+static void put_u64(std::vector<uint8_t>& w, u64 v) {
+  for (int i = 0; i < 8; i++) w.push_back((uint8_t)(v >> (8 * i)));
+}
+static void put_u32(std::vector<uint8_t>& w, u32 v) {
+  for (int i = 0; i < 4; i++) w.push_back((uint8_t)(v >> (8 * i)));
+}
+static bool put_tight(std::vector<uint8_t>& w, const u64* c, size_t count, u64 modulus) {
+  const unsigned bits = 64 - __builtin_clzll(modulus - 1);
+  const size_t nbytes = (count * bits + 7) / 8;
+  put_u64(w, nbytes);
+  const size_t base = w.size();
+  w.resize(base + nbytes, 0);
+  for (size_t i = 0; i < count; i++) {
+    if (c[i] >= modulus) return false;
+    const size_t bit = i * bits;
+    const u128 v = (u128)c[i] << (bit % 8);
+    for (size_t k = 0; k < 10 && bit / 8 + k < nbytes; k++) w[base + bit / 8 + k] |= (uint8_t)(v >> (8 * k));
+  }
+  return true;
+}
+
+int ig_response_encode(const uint64_t* a, const uint64_t* b, uint32_t n, uint32_t retained, uint64_t modulus,
+                       uint8_t* out, size_t cap, size_t* len_out) {
+  if (!a || !b || !len_out || n == 0 || modulus < 2 || retained == 0 || retained > n) return IG_ERR_ARG;
+  std::vector<uint8_t> w;
+  put_u32(w, 1);  // ResponseCiphertextWire::Packed
+  if (!put_tight(w, a, n, modulus)) return IG_ERR_SHAPE;
+  put_u64(w, 1);  // moduli
+  put_u64(w, modulus);
+  put_u64(w, modulus);  // q
+  put_u64(w, n);        // dim
+  put_u64(w, 0);        // crt_q0_inv_mod_q1
+  w.push_back(0);       // is_ntt
+  if (!put_tight(w, b, retained, modulus)) return IG_ERR_SHAPE;
+  put_u32(w, retained);
+  put_u64(w, 0);  // column_ciphertexts
+  w.push_back(1);  // Some(
+  put_u32(w, 0);   //   PackingMode::Inspiring)
+  *len_out = w.size();
+  if (out) memcpy(out, w.data(), w.size() < cap ? w.size() : cap);
+  return IG_OK;
+}
+
+int ig_debug_force_serial_expand(ig_ctx* c, int on) {
+  if (!c) return IG_ERR_ARG;
+  std::lock_guard<std::mutex> lk(c->mu);
+  c->force_serial = on ? 1 : 0;
+  return IG_OK;
+}
+
+int ig_debug_store_sums(ig_ctx* c, uint64_t dbh, uint32_t s, uint64_t* out) {
+  if (!c || !out) return IG_ERR_ARG;
+  std::lock_guard<std::mutex> lk(c->mu);
+  DbObj* db = get_db(c, dbh);
+  if (!db) return fail(c, IG_ERR_HANDLE, "unknown database handle");
+  if (s >= db->num_shards || !db->shards[s].sums) return fail(c, IG_ERR_ARG, "shard %u has no store", s);
+  CrsObj* o = get_crs(c, db->crs);
+  IG_CUDA(c, cudaMemcpy(out, db->shards[s].sums, (size_t)o->gamma * o->n * 8, cudaMemcpyDeviceToHost));
+  return IG_OK;
+}
+
+}  // extern "C"
