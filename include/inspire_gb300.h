@@ -143,6 +143,17 @@ int ig_respond_seeded_batch_device(ig_ctx* ctx, uint64_t db, uint64_t store, uin
 int ig_response_encode(const uint64_t* a, const uint64_t* b, uint32_t ring_dim, uint32_t retained, uint64_t modulus,
                        uint8_t* out, size_t cap, size_t* len_out);
 
+/* ---- observability ------------------------------------------------------------------------
+ * Per-region device timing of respond calls, the GPU form of the reference's
+ * RAVEN_PROFILE_RESPOND regions (respond.rs:1295-1345): with profiling on, each kernel
+ * launch is bracketed by CUDA events on the context stream. ig_profile_read synchronises,
+ * writes the summed milliseconds and launch counts of regions 0..regions-1 (0 = shard scan,
+ * 1 = recursion/respond, 2 = store fold) and, when reset != 0, clears the record. */
+int ig_profile_enable(ig_ctx* ctx, int on);
+int ig_profile_read(ig_ctx* ctx, double* ms, uint64_t* counts, int regions, int reset);
+/* Kernel launches this context has made so far. */
+uint64_t ig_launch_count(const ig_ctx* ctx);
+
 /* ---- test hooks --------------------------------------------------------------------------
  * Forces the word-by-word `a` expansion the kernel otherwise takes only after a rejected
  * ChaCha word, so tests can check that path against the vectorised one. */

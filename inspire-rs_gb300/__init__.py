@@ -91,6 +91,9 @@ def _load():
         "ig_respond_batch": (I, [P, U64, U64, U64, P, U32, U32, U32, P, P, P, U64, P, P]),
         "ig_response_encode": (I, [P, P, U32, U32, U64, P, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
         "ig_debug_force_serial_expand": (I, [P, I]),
+        "ig_profile_enable": (I, [P, I]),
+        "ig_profile_read": (I, [P, P, P, I, I]),
+        "ig_launch_count": (U64, [P]),
         "ig_debug_store_sums": (I, [P, U64, U32, P]),
     }
     for name, (res, args) in sig.items():
@@ -145,6 +148,20 @@ class Context:
     @property
     def device_bytes(self):
         return self._lib.ig_ctx_device_bytes(self.h)
+
+    @property
+    def launch_count(self):
+        return self._lib.ig_launch_count(self.h)
+
+    def profile(self, on=True):
+        self.check(self._lib.ig_profile_enable(self.h, int(on)))
+
+    def profile_read(self, reset=True):
+        """Summed device milliseconds and launch counts per region: scan, respond, fold."""
+        ms = np.zeros(3, dtype=np.float64)
+        cnt = np.zeros(3, dtype=np.uint64)
+        self.check(self._lib.ig_profile_read(self.h, _ptr(ms), _ptr(cnt), 3, int(reset)))
+        return {name: (float(ms[i]), int(cnt[i])) for i, name in enumerate(["scan", "respond", "fold"])}
 
     def close(self):
         if self.h:

@@ -154,9 +154,35 @@ struct ig_ctx {
   size_t zero_key_words = 0;
   size_t obj_bytes = 0;
   int force_serial = 0;
+  // Per-region CUDA-event timing of the device respond path (RegionProfile of
+  // respond.rs:1295-1345 on the GPU): pairs of events around each kernel launch.
+  int profile = 0;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_pool;
+  std::vector<std::pair<int, size_t>> ev_used;  // (region, pool index)
+  u64 launches = 0;
 };
 
 namespace {
+
+enum Region { REGION_SCAN = 0, REGION_RESPOND = 1, REGION_FOLD = 2, REGION_COUNT = 3 };
+
+// Starts a profiled region on the context stream; returns the pool slot or -1.
+long prof_begin(ig_ctx* c, int region) {
+  c->launches++;
+  if (!c->profile) return -1;
+  size_t k = c->ev_used.size();
+  if (k == c->ev_pool.size()) {
+    cudaEvent_t a, b;
+    if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) return -1;
+    c->ev_pool.push_back({a, b});
+  }
+  c->ev_used.push_back({region, k});
+  cudaEventRecord(c->ev_pool[k].first, c->stream);
+  return (long)k;
+}
+void prof_end(ig_ctx* c, long k) {
+  if (k >= 0) cudaEventRecord(c->ev_pool[k].second, c->stream);
+}
 
 int fail(ig_ctx* c, int code, const char* fmt, ...) {
   char buf[1024];
@@ -257,8 +283,11 @@ int fold_store(ig_ctx* c, CrsObj& o, const u64* cols, u64* sums) {
   void* H;
   int rc = scratch(c, "fold_H", (size_t)o.gamma * o.n * 8, &H);
   if (rc) return rc;
+  long k = prof_begin(c, REGION_FOLD);
+  c->launches++;
   IG_CUDA(c, igk::ntt_rows(o.dev, cols, (u64*)H, o.gamma, 1, shoup_companion(1), c->stream));
   IG_CUDA(c, igk::store_fold(o.dev, (const u64*)H, sums, c->stream));
+  prof_end(c, k);
   return IG_OK;
 }
 
@@ -879,10 +908,14 @@ static int respond_host(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_t handle, c
   IG_CUDA(c, cudaMemcpyAsync(d_seeds, as ? (const void*)as : (const void*)seeds, seed_bytes, cudaMemcpyHostToDevice, s));
   IG_CUDA(c, cudaMemcpyAsync(d_bs, bs, (size_t)count * n * 8, cudaMemcpyHostToDevice, s));
   IG_CUDA(c, cudaMemsetAsync(d_status, 0, count * 4, s));
+  long pk = prof_begin(c, REGION_SCAN);
   IG_CUDA(c, igk::shard_scan(o.dev, (const QueryDev*)d_q, (const ShardDev*)d_table, count, (u64*)d_fold,
                              (u32*)d_status, 0, nullptr, s));
+  prof_end(c, pk);
+  pk = prof_begin(c, REGION_RESPOND);
   IG_CUDA(c, igk::respond(o.dev, (const QueryDev*)d_q, (const ShardDev*)d_table, count, (const u64*)d_fold, ms_target,
                           (u64*)d_a, (u64*)d_b, (u32*)d_status, c->force_serial, s));
+  prof_end(c, pk);
   std::vector<u32> status(count);
   IG_CUDA(c, cudaMemcpyAsync(status.data(), d_status, count * 4, cudaMemcpyDeviceToHost, s));
   IG_CUDA(c, cudaStreamSynchronize(s));
@@ -957,9 +990,13 @@ int ig_respond_seeded_batch_device(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_
   cudaStream_t s = c->stream;
   IG_CUDA(c, cudaMemcpyAsync(d_q, qs.data(), count * sizeof(QueryDev), cudaMemcpyHostToDevice, s));
   IG_CUDA(c, cudaMemsetAsync(d_status, 0, count * 4, s));
+  long pk = prof_begin(c, REGION_SCAN);
   IG_CUDA(c, igk::shard_scan(o.dev, (const QueryDev*)d_q, db->d_table, count, (u64*)d_fold, d_status, 0, nullptr, s));
+  prof_end(c, pk);
+  pk = prof_begin(c, REGION_RESPOND);
   IG_CUDA(c, igk::respond(o.dev, (const QueryDev*)d_q, db->d_table, count, (const u64*)d_fold, ms_target, d_a, d_b,
                           d_status, c->force_serial, s));
+  prof_end(c, pk);
   return IG_OK;
 }
 
@@ -1006,6 +1043,35 @@ int ig_response_encode(const uint64_t* a, const uint64_t* b, uint32_t n, uint32_
   if (out) memcpy(out, w.data(), w.size() < cap ? w.size() : cap);
   return IG_OK;
 }
+
+int ig_profile_enable(ig_ctx* c, int on) {
+  if (!c) return IG_ERR_ARG;
+  std::lock_guard<std::mutex> lk(c->mu);
+  c->profile = on ? 1 : 0;
+  return IG_OK;
+}
+
+int ig_profile_read(ig_ctx* c, double* ms, uint64_t* counts, int regions, int reset) {
+  if (!c || !ms || !counts || regions <= 0) return IG_ERR_ARG;
+  std::lock_guard<std::mutex> lk(c->mu);
+  IG_CUDA(c, cudaStreamSynchronize(c->stream));
+  for (int r = 0; r < regions; r++) {
+    ms[r] = 0;
+    counts[r] = 0;
+  }
+  for (auto& u : c->ev_used) {
+    if (u.first >= regions) continue;
+    float t = 0;
+    if (cudaEventElapsedTime(&t, c->ev_pool[u.second].first, c->ev_pool[u.second].second) == cudaSuccess) {
+      ms[u.first] += t;
+      counts[u.first]++;
+    }
+  }
+  if (reset) c->ev_used.clear();
+  return IG_OK;
+}
+
+uint64_t ig_launch_count(const ig_ctx* c) { return c ? c->launches : 0; }
 
 int ig_debug_force_serial_expand(ig_ctx* c, int on) {
   if (!c) return IG_ERR_ARG;
