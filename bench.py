@@ -1,0 +1,335 @@
+"""Benchmark of the InsPIRe respond path on GB300.
+
+Workload (the reference's headline serving configuration): InspireParams::d2048, 512-byte
+records (gamma = 256 columns per shard), 2^20 records = 512 shards, a packing store folded
+on every shard, one session key registered by handle, one batch of 64 queries with
+uniform indices per step answered through respond_seeded_batch, responses mod-switched to
+36 bits. Inputs are seeded synthetic data of those shapes: uniform 16-bit column words
+(the encoding of uniform random record bytes), uniform key and query words mod q.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Prints one JSON line. `value` = queries/s over K device-resident batches (CUDA events on
+the library's stream); `e2e` = the same through the public API with host buffers;
+`cpu_baseline` = the CPU oracle (a port of the reference's respond path) on a bounded
+sample on this host's cores. `--impl reference` times that CPU port alone.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_RING = 2048
+GAMMA = 256
+ENTRY_BYTES = 512
+NUM_SHARDS = 512  # 2^20 records / 2048 per shard
+BATCH = 64
+Q = 1152921504606830593
+MS_TARGET = 68_718_428_161
+SHARD_DB_BYTES = N_RING * ENTRY_BYTES  # the queried shard's records: 1 MiB
+METRIC = "respond queries/s (served batch of 64, d2048, 512 B records, 2^20 records, 36-bit mod switch)"
+CONFIG = {"workload": "d2048 TwoPacking, 512-byte records x 2^20 (512 shards, gamma 256), packing store on "
+                      "every shard, batch 64 under one registered key, uniform indices, 36-bit mod switch",
+          "ring_dim": N_RING, "gamma": GAMMA, "records": 1 << 20, "shards": NUM_SHARDS, "batch": BATCH,
+          "mod_switch_bits": 36, "l2": "inputs larger than L2: each step reads 64 random shards' columns and "
+                                       "stores (8 MiB per query, 512 MiB per step)"}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def rand_words(rng, shape):
+    return rng.integers(0, Q, size=shape, dtype=np.uint64)
+
+
+# ------------------------------------------------------------------------------------
+# CPU oracle leg (the reference's algorithm restated; test infrastructure only here as
+# the timed CPU baseline).
+def cpu_sample(steps, warmup, queries_per_step=8, shards=4, seed=11):
+    from oracle import oracle as O
+
+    O.build()
+    cores = O.lib().orc_max_threads()
+    rng = np.random.default_rng(seed)
+    P = O.Params.d2048()
+    w_seed = rng.integers(0, 256, 32, dtype=np.uint8).tobytes()
+    cache = O.Cache(P, GAMMA, w_seed)
+    cols = [rng.integers(0, 1 << 16, size=(GAMMA, N_RING), dtype=np.uint64) for _ in range(shards)]
+    stores = [O.Store(cache, c) for c in cols]
+    y = rand_words(rng, (3, N_RING))
+    times = []
+    for step in range(warmup + steps):
+        t0 = time.perf_counter()
+        for k in range(queries_per_step):
+            s = k % shards
+            seed_b = rng.integers(0, 256, 32, dtype=np.uint8).tobytes()
+            a = O.expand_seed(seed_b, N_RING)
+            b = rand_words(rng, N_RING)
+            ao, bo = stores[s].respond(cols[s], a, b, y)
+            O.mod_switch(ao, Q, MS_TARGET)
+            O.mod_switch(bo, Q, MS_TARGET)
+        if step >= warmup:
+            times.append(time.perf_counter() - t0)
+    qps = queries_per_step * len(times) / sum(times)
+    return {"value": qps, "unit": "queries/s", "cores": int(cores), "kind": "port",
+            "sample": f"{queries_per_step} queries per step over {shards} stored shards, {steps} steps "
+                      "(oracle store path + 36-bit switch, OpenMP over the reference's rayon sites)"}
+
+
+# ------------------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device, self.proc, self.lines = device, None, []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup(n_gpus):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if os.environ.get("IG_BENCH_BACKEND", "nccl") == "nccl" else "gloo"
+        dist.init_process_group(backend)
+    return rank, world
+
+
+def max_over_ranks(x, world):
+    """Largest value of x over all ranks (the slowest rank sets whole-job throughput)."""
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+# ------------------------------------------------------------------------------------
+def run_gb300(args, rank, world):
+    import torch
+
+    from __graft_entry__ import _package
+    pkg = _package()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    ctx = pkg.Context(local)
+    g = torch.Generator(device="cuda")
+    g.manual_seed(1 + rank)
+    rng = np.random.default_rng(1000 + rank)
+
+    params = pkg.InspireParams.d2048()
+    w_seed = rng.integers(0, 256, 32, dtype=np.uint8).tobytes()
+    crs = pkg.ServerCrs(params, w_seed, GAMMA)
+    cache = pkg.ServerInspiringCache.new(crs, ctx=ctx)
+    db = pkg.EncodedDatabase(cache, args.shards)
+    t_setup = time.perf_counter()
+    for s in range(args.shards):
+        cols = torch.randint(0, 1 << 16, (GAMMA, N_RING), generator=g, device="cuda", dtype=torch.int64)
+        torch.cuda.current_stream().synchronize()
+        db.set_shard_device(s, cols.data_ptr())
+    db.precompute_packing_all()
+    setup_s = time.perf_counter() - t_setup
+    store = pkg.ServerSessionStore.new(ctx)
+    keys = pkg.ClientPackingKeys(rand_words(rng, (3, N_RING)), GAMMA)
+    handle = store.register_server_side(keys, cache)
+
+    total = args.warmup + args.steps
+    shard_ids = [rng.integers(0, args.shards * N_RING, size=BATCH) // N_RING for _ in range(total)]
+    shard_ids = [np.ascontiguousarray(x, dtype=np.uint32) for x in shard_ids]
+    seeds_h = rng.integers(0, 256, size=(total, BATCH, 32), dtype=np.uint8)
+    bs_h = rand_words(rng, (total, BATCH, N_RING))
+    d_seeds = torch.from_numpy(seeds_h).cuda()
+    d_bs = torch.from_numpy(bs_h.view(np.int64)).cuda()
+    d_a = torch.empty((BATCH, N_RING), dtype=torch.int64, device="cuda")
+    d_b = torch.empty((BATCH, N_RING), dtype=torch.int64, device="cuda")
+    d_status = torch.zeros(BATCH, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    lib = ctx._lib
+    stream = torch.cuda.ExternalStream(ctx.stream)
+
+    def step(i):
+        ctx.check(lib.ig_respond_seeded_batch_device(
+            ctx.h, db.h, store.h, int(handle), BATCH, shard_ids[i].ctypes.data, d_seeds[i].data_ptr(),
+            d_bs[i].data_ptr(), MS_TARGET, d_a.data_ptr(), d_b.data_ptr(), d_status.data_ptr()))
+
+    for i in range(args.warmup):
+        step(i)
+    torch.cuda.synchronize()
+    ctx.profile(True)
+    ctx.profile_read(reset=True)
+    launches0 = ctx.launch_count
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        torch.cuda.profiler.start()  # bounds an ncu --profile-from-start off capture
+        with torch.cuda.stream(stream):
+            ev0.record(stream)
+            for i in range(args.warmup, total):
+                step(i)
+            ev1.record(stream)
+        torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
+    barrier(world)
+    ms_total = ev0.elapsed_time(ev1)
+    launches = ctx.launch_count - launches0
+    prof = ctx.profile_read(reset=True)
+    ctx.profile(False)
+    if int(d_status.abs().sum().item()) != 0:
+        raise RuntimeError("a batch was refused during the timed region")
+    ms_max = max_over_ranks(ms_total, world)
+    value = world * BATCH * args.steps / (ms_max / 1e3)
+
+    # e2e: public API with host buffers (H2D of seeds and b, D2H of a and b).
+    e2e_queries = [[pkg.SeededBatchQuery(int(shard_ids[i][k]), seeds_h[i, k].tobytes(), bs_h[i, k])
+                    for k in range(BATCH)] for i in range(total)]
+    batches = [pkg.SeededQueryBatch(pkg.PackingKeySource.Registered(handle), qs) for qs in e2e_queries]
+    for i in range(args.warmup):
+        pkg.respond_seeded_batch(crs, db, batches[i], cache, store, mod_switch_target=MS_TARGET)
+    barrier(world)
+    t0 = time.perf_counter()
+    for i in range(args.warmup, total):
+        out = pkg.respond_seeded_batch(crs, db, batches[i], cache, store, mod_switch_target=MS_TARGET)
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
+    e2e_value = world * BATCH * args.steps / e2e_s
+    assert len(out) == BATCH
+
+    scan_ms, scan_n = prof["scan"]
+    resp_ms, resp_n = prof["respond"]
+    scan_avg = scan_ms / max(scan_n, 1)
+    resp_avg = resp_ms / max(resp_n, 1)
+    # Algorithmic bytes of one scan launch: per query the gamma columns (u64 words), the
+    # shard's tag key (2n words) and the query's b (n words), plus gamma folded words out.
+    scan_bytes = BATCH * (GAMMA * N_RING * 8 + 2 * N_RING * 8 + N_RING * 8 + GAMMA * 8)
+    hbm_peak, peak_kind = peaks()
+    achieved = scan_bytes / (scan_avg / 1e3) / 1e9
+    # Recursion: 3 transforms of n/2 log n butterflies per link + 16 pointwise products.
+    links = GAMMA - 1
+    modmul_per_query = links * (3 * (N_RING // 2) * 11 + 16 * N_RING) + 3 * (N_RING // 2) * 11
+    resp_gmodmul = BATCH * modmul_per_query / (resp_avg / 1e3) / 1e9
+    return {
+        "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u64 (exact mod q = 2^60-2^14+1)",
+        "data": "synthetic: uniform 16-bit column words (uniform record bytes), uniform key/query words mod q",
+        "config": dict(CONFIG, parallelism=f"replicas x{world}" if world > 1 else "single GPU",
+                       **({"shards": args.shards, "records": args.shards * N_RING} if args.shards != NUM_SHARDS
+                          else {})),
+        "db_gbs": value * SHARD_DB_BYTES / 1e9,
+        "e2e": {"value": e2e_value, "unit": "queries/s",
+                "h2d_bytes_per_step": BATCH * (32 + N_RING * 8 + 4),
+                "d2h_bytes_per_step": BATCH * 2 * N_RING * 8},
+        "roofline": {"kernel": "shard_scan", "bound": "hbm", "achieved": achieved, "peak": hbm_peak,
+                     "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": None,
+                     "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
+                     "avg_launch_ms": scan_avg, "algorithmic_bytes_per_launch": scan_bytes},
+        "roofline_dominant": {"kernel": "respond (fused recursion + online gather)", "bound": "integer issue",
+                              "achieved": resp_gmodmul, "unit": "G modmul/s", "avg_launch_ms": resp_avg,
+                              "modmul_per_query": modmul_per_query,
+                              "share_of_step": resp_ms / max(ms_total, 1e-9)},
+        "gpu_launches": int(launches),
+        "setup_s": setup_s,
+        "clocks": clk.summary(),
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--shards", type=int, default=NUM_SHARDS,
+                    help="shards in the database (smaller values only for profiling captures)")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank, world = dist_setup(args.gpus)
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        cb = cpu_sample(args.steps, args.warmup)
+        line = {"metric": METRIC, "value": cb["value"], "unit": "queries/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "u64 (exact mod q)", "data": "synthetic, same shapes", "config": CONFIG,
+                "impl": "reference", "cpu_baseline": cb,
+                "e2e": {"value": cb["value"], "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+    line = run_gb300(args, rank, world)
+    if rank == 0:
+        if not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_sample(steps=3, warmup=1)
+        print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()
