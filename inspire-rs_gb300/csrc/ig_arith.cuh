@@ -49,11 +49,29 @@ IG_HD u64 negq(u64 a) { return a == 0 ? 0 : Q - a; }
 // hi * q mod 2^64 with q's shape: (hi << 60) - (hi << 14) + hi.
 IG_HD u64 mul_q_lo(u64 hi) { return (hi << 60) - (hi << 14) + hi; }
 
-// a * w mod q, w < q, w' = floor(w * 2^64 / q); any a < 2^64.
-IG_HD u64 shoup(u64 a, u64 w, u64 wp) {
-  u64 est = mulhi(a, wp);
-  return csub(a * w - mul_q_lo(est));
+// q held in a register the compiler cannot see through, so est * q issues as an integer
+// multiply (FMA pipe) rather than shifts and adds (ALU pipe).
+IG_HD u64 q_opaque() {
+#ifdef __CUDA_ARCH__
+  u64 r;
+  asm("mov.b64 %0, %1;" : "=l"(r) : "l"(Q));
+  return r;
+#else
+  return Q;
+#endif
 }
+
+// a * w mod q up to one q: in [0, 2q) for any a < 2^64 (Shoup, w' = floor(w 2^64 / q)).
+IG_HD u64 shoup_lazy(u64 a, u64 w, u64 wp) {
+  const u64 est = mulhi(a, wp);
+  return a * w - est * q_opaque();
+}
+
+// a * w mod q, w < q; any a < 2^64.
+IG_HD u64 shoup(u64 a, u64 w, u64 wp) { return csub(shoup_lazy(a, w, wp)); }
+
+// x - 2q when x >= 2q.
+IG_HD u64 csub2(u64 x) { return x >= 2 * Q ? x - 2 * Q : x; }
 
 // a * b * 2^-64 mod q for a, b < q.
 IG_HD u64 mont(u64 a, u64 b) {
@@ -64,6 +82,16 @@ IG_HD u64 mont(u64 a, u64 b) {
   u64 t = hi + mulhi(m, Q) + (lo != 0 ? 1 : 0);
   return csub(t);
 }
+
+// Montgomery reduction of a 128-bit sum of products: x * 2^-64 mod q for x < q * 2^64
+// (any sum of up to 15 products of words below q).
+IG_HD u64 redc(u128 x) {
+  const u64 lo = (u64)x, hi = (u64)(x >> 64);
+  const u64 m = lo * QINV_NEG;
+  return csub(hi + mulhi(m, Q) + (lo != 0 ? 1 : 0));
+}
+
+IG_HD u128 wide(u64 a, u64 b) { return (u128)a * b; }
 
 // Shoup companion floor(w * 2^64 / q).
 IG_HD u64 shoup_companion(u64 w) { return (u64)(((u128)w << 64) / Q); }

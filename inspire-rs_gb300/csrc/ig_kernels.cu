@@ -26,93 +26,118 @@ using namespace ig;
 // Negacyclic transforms in shared memory. Forward: Cooley-Tukey over the bit-reversed
 // ladder psi^brv(m) (math/ntt.rs:600-623 order); inverse: Gentleman-Sande over the
 // inverse ladder (math/ntt.rs:626-654) without the final n^-1, which consumers fold into
-// their first use. Both are linear in standard form; all words canonical.
+// their first use. Both are linear in standard form.
+//
+// Radix-4 transforms: each thread carries one 4-element unit through two
+// consecutive stages in registers (N/4 threads), halving shared-memory round trips and
+// barriers against a stage-per-barrier radix-2 schedule. Odd log n adds one radix-2 stage
+// (first in the forward, last in the inverse). The butterflies are Harvey's lazy ones: the
+// forward keeps words in [0, 4q) and the inverse in [0, 2q) (inputs canonical), reducing
+// only where the bound requires; results agree with the reference transform mod q.
 
-template <int LOGN, int NT>
-__device__ __forceinline__ void ntt_fwd(u64* x, const u64* tw, const u64* twp) {
+// Forward CT butterfly on lazy words: X, Y < 4q in, both outputs < 4q.
+__device__ __forceinline__ void bf_fwd(u64& X, u64& Y, u64 w, u64 wp) {
+  const u64 x = csub2(X);
+  const u64 t = shoup_lazy(Y, w, wp);
+  X = x + t;
+  Y = x - t + 2 * Q;
+}
+
+// Inverse GS butterfly: X, Y < 2q in, both outputs < 2q.
+__device__ __forceinline__ void bf_inv(u64& X, u64& Y, u64 w, u64 wp) {
+  const u64 u = csub2(X + Y);
+  Y = shoup_lazy(X - Y + 2 * Q, w, wp);
+  X = u;
+}
+
+template <int LOGN, int NT, int NB>
+__device__ __forceinline__ void ntt_fwd_r4(u64* const (&x)[NB], const u64* tw, const u64* twp) {
   constexpr int N = 1 << LOGN;
-#pragma unroll 1
-  for (int s = 0; s < LOGN; s++) {
-    const int tlog = LOGN - 1 - s;
-    const int t = 1 << tlog;
-    const int m = 1 << s;
+  static_assert(NT == N / 4, "one radix-4 unit per thread");
+  const int tid = threadIdx.x;
+  int s = 0;
+  if (LOGN & 1) {
+    constexpr int t = N / 2;
+    const u64 w = tw[1], wp = twp[1];
 #pragma unroll
-    for (int b = threadIdx.x; b < N / 2; b += NT) {
-      const int i = b >> tlog;
-      const int j1 = (i << (tlog + 1)) | (b & (t - 1));
-      const u64 w = tw[m + i], wp = twp[m + i];
-      const u64 u = x[j1];
-      const u64 v = shoup(x[j1 + t], w, wp);
-      x[j1] = addq(u, v);
-      x[j1 + t] = subq(u, v);
+    for (int r = 0; r < 2; r++) {
+      const int b = tid + r * NT;
+#pragma unroll
+      for (int k = 0; k < NB; k++) {
+        u64 a = x[k][b], c = x[k][b + t];
+        bf_fwd(a, c, w, wp);
+        x[k][b] = a;
+        x[k][b + t] = c;
+      }
+    }
+    __syncthreads();
+    s = 1;
+  }
+#pragma unroll 1
+  for (; s < LOGN; s += 2) {
+    const int t = N >> (s + 1), m = 1 << s, h = t >> 1;
+    const int i = tid / h, o = tid - i * h;
+    const int e0 = i * 2 * t + o;
+    const u64 wa = tw[m + i], wap = twp[m + i];
+    const u64 wb = tw[2 * m + 2 * i], wbp = twp[2 * m + 2 * i];
+    const u64 wc = tw[2 * m + 2 * i + 1], wcp = twp[2 * m + 2 * i + 1];
+#pragma unroll
+    for (int k = 0; k < NB; k++) {
+      u64 a0 = x[k][e0], a1 = x[k][e0 + h], a2 = x[k][e0 + t], a3 = x[k][e0 + t + h];
+      bf_fwd(a0, a2, wa, wap);
+      bf_fwd(a1, a3, wa, wap);
+      bf_fwd(a0, a1, wb, wbp);
+      bf_fwd(a2, a3, wc, wcp);
+      x[k][e0] = a0;
+      x[k][e0 + h] = a1;
+      x[k][e0 + t] = a2;
+      x[k][e0 + t + h] = a3;
     }
     __syncthreads();
   }
 }
 
-template <int LOGN, int NT>
-__device__ __forceinline__ void ntt_fwd2(u64* x, u64* y, const u64* tw, const u64* twp) {
+template <int LOGN, int NT, int NB>
+__device__ __forceinline__ void ntt_inv_r4(u64* const (&x)[NB], const u64* itw, const u64* itwp) {
   constexpr int N = 1 << LOGN;
+  static_assert(NT == N / 4, "one radix-4 unit per thread");
+  const int tid = threadIdx.x;
+  int s = 0;
 #pragma unroll 1
-  for (int s = 0; s < LOGN; s++) {
-    const int tlog = LOGN - 1 - s;
-    const int t = 1 << tlog;
-    const int m = 1 << s;
+  for (; s + 1 < LOGN; s += 2) {
+    const int t = 1 << s, m = N >> (s + 1);
+    const int B = tid >> s, o = tid & (t - 1);
+    const int e0 = B * 4 * t + o;
+    const u64 w0 = itw[m + 2 * B], w0p = itwp[m + 2 * B];
+    const u64 w1 = itw[m + 2 * B + 1], w1p = itwp[m + 2 * B + 1];
+    const u64 w2 = itw[(m >> 1) + B], w2p = itwp[(m >> 1) + B];
 #pragma unroll
-    for (int b = threadIdx.x; b < N / 2; b += NT) {
-      const int i = b >> tlog;
-      const int j1 = (i << (tlog + 1)) | (b & (t - 1));
-      const u64 w = tw[m + i], wp = twp[m + i];
-      const u64 u0 = x[j1], u1 = y[j1];
-      const u64 v0 = shoup(x[j1 + t], w, wp);
-      const u64 v1 = shoup(y[j1 + t], w, wp);
-      x[j1] = addq(u0, v0);
-      x[j1 + t] = subq(u0, v0);
-      y[j1] = addq(u1, v1);
-      y[j1 + t] = subq(u1, v1);
+    for (int k = 0; k < NB; k++) {
+      u64 a0 = x[k][e0], a1 = x[k][e0 + t], a2 = x[k][e0 + 2 * t], a3 = x[k][e0 + 3 * t];
+      bf_inv(a0, a1, w0, w0p);
+      bf_inv(a2, a3, w1, w1p);
+      bf_inv(a0, a2, w2, w2p);
+      bf_inv(a1, a3, w2, w2p);
+      x[k][e0] = a0;
+      x[k][e0 + t] = a1;
+      x[k][e0 + 2 * t] = a2;
+      x[k][e0 + 3 * t] = a3;
     }
     __syncthreads();
   }
-}
-
-template <int LOGN, int NT>
-__device__ __forceinline__ void ntt_inv(u64* x, const u64* itw, const u64* itwp) {
-  constexpr int N = 1 << LOGN;
-#pragma unroll 1
-  for (int s = 0; s < LOGN; s++) {
-    const int t = 1 << s;
-    const int m = N >> (s + 1);
+  if (LOGN & 1) {
+    constexpr int t = N / 2;
+    const u64 w = itw[1], wp = itwp[1];
 #pragma unroll
-    for (int b = threadIdx.x; b < N / 2; b += NT) {
-      const int i = b >> s;
-      const int j2 = (i << (s + 1)) | (b & (t - 1));
-      const u64 w = itw[m + i], wp = itwp[m + i];
-      const u64 u = x[j2], v = x[j2 + t];
-      x[j2] = addq(u, v);
-      x[j2 + t] = shoup(subq(u, v), w, wp);
-    }
-    __syncthreads();
-  }
-}
-
-template <int LOGN, int NT>
-__device__ __forceinline__ void ntt_inv2(u64* x, u64* y, const u64* itw, const u64* itwp) {
-  constexpr int N = 1 << LOGN;
-#pragma unroll 1
-  for (int s = 0; s < LOGN; s++) {
-    const int t = 1 << s;
-    const int m = N >> (s + 1);
+    for (int r = 0; r < 2; r++) {
+      const int b = tid + r * NT;
 #pragma unroll
-    for (int b = threadIdx.x; b < N / 2; b += NT) {
-      const int i = b >> s;
-      const int j2 = (i << (s + 1)) | (b & (t - 1));
-      const u64 w = itw[m + i], wp = itwp[m + i];
-      const u64 u0 = x[j2], v0 = x[j2 + t];
-      const u64 u1 = y[j2], v1 = y[j2 + t];
-      x[j2] = addq(u0, v0);
-      x[j2 + t] = shoup(subq(u0, v0), w, wp);
-      y[j2] = addq(u1, v1);
-      y[j2 + t] = shoup(subq(u1, v1), w, wp);
+      for (int k = 0; k < NB; k++) {
+        u64 a = x[k][b], c = x[k][b + t];
+        bf_inv(a, c, w, wp);
+        x[k][b] = a;
+        x[k][b + t] = c;
+      }
     }
     __syncthreads();
   }
@@ -135,7 +160,10 @@ __global__ void __launch_bounds__((1 << LOGN) / 4) k_ntt_rows(CrsDev c, const u6
     twp[k] = c.twp[k];
   }
   __syncthreads();
-  ntt_fwd<LOGN, NT>(x, tw, twp);
+  {
+    u64* const bufs[1] = {x};
+    ntt_fwd_r4<LOGN, NT, 1>(bufs, tw, twp);
+  }
   u64* o = out + (size_t)blockIdx.x * N;
   for (int k = threadIdx.x; k < N; k += NT) o[k] = shoup(x[k], scale, scalep);
 }
@@ -364,7 +392,10 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
     }
     __syncthreads();
   }
-  ntt_fwd<LOGN, NT>(a_ntt, tw, twp);
+  {
+    u64* const bufs[1] = {a_ntt};
+    ntt_fwd_r4<LOGN, NT, 1>(bufs, tw, twp);
+  }
 
   u64 cur[4], sb[4];
   u32 et[4];
@@ -392,7 +423,10 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
 #pragma unroll
     for (int k = 0; k < 4; k++) bufA[tid + k * NT] = cur[k];
     __syncthreads();
-    ntt_inv<LOGN, NT>(bufA, itw, itwp);
+    {
+      u64* const bufs[1] = {bufA};
+      ntt_inv_r4<LOGN, NT, 1>(bufs, itw, itwp);
+    }
 #pragma unroll
     for (int k = 0; k < 4; k++) {
       const int t = tid + k * NT;
@@ -407,22 +441,25 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
       }
     }
     __syncthreads();
-    ntt_fwd2<LOGN, NT>(bufB, bufA, tw, twp);
+    {
+      u64* const bufs[2] = {bufB, bufA};
+      ntt_fwd_r4<LOGN, NT, 2>(bufs, tw, twp);
+    }
+    // Pointwise link: every sum of products reduced once (lazy Montgomery).
 #pragma unroll
     for (int k = 0; k < 4; k++) {
       const int t = tid + k * NT;
       const u32 tb = s_tab[((gp * et[k]) & M2N) >> 1];
       const u64 d0 = bufB[t], d1 = bufA[t];
-      u64 nb = addq(mont(d0, Y[tb]), mont(d1, Y[N + tb]));
-      u64 nc = addq(mont(a_ntt[tb], sv[k]), addq(mont(d0, Wm[tb]), mont(d1, Wm[N + tb])));
+      u128 nb = wide(d0, Y[tb]) + wide(d1, Y[N + tb]);
+      u128 nc = wide(a_ntt[tb], sv[k]) + wide(d0, Wm[tb]) + wide(d1, Wm[N + tb]);
       if (exact) {
-        const u64 d2 = addq(addq(shoup(cur[k], c.ld_inv, c.ld_invp), shoup(d0, c.ld_c0, c.ld_c0p)),
-                            shoup(d1, c.ld_c1, c.ld_c1p));
-        nb = addq(nb, mont(d2, Y[2 * N + tb]));
-        nc = addq(nc, mont(d2, Wm[2 * N + tb]));
+        const u64 d2 = redc(wide(cur[k], c.ld_inv_R) + wide(d0, c.ld_c0_R) + wide(d1, c.ld_c1_R));
+        nb += wide(d2, Y[2 * N + tb]);
+        nc += wide(d2, Wm[2 * N + tb]);
       }
-      sb[k] = addq(sb[k], nb);
-      cur[k] = nc;
+      sb[k] = addq(sb[k], redc(nb));
+      cur[k] = redc(nc);
     }
   }
 #pragma unroll
@@ -431,7 +468,10 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
     bufB[tid + k * NT] = sb[k];
   }
   __syncthreads();
-  ntt_inv2<LOGN, NT>(bufA, bufB, itw, itwp);
+  {
+    u64* const bufs[2] = {bufA, bufB};
+    ntt_inv_r4<LOGN, NT, 2>(bufs, itw, itwp);
+  }
 #pragma unroll
   for (int k = 0; k < 4; k++) {
     const int t = tid + k * NT;

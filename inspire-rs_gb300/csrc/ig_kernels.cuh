@@ -28,8 +28,9 @@ struct CrsDev {
   const u64* pow_root_R;     // w0^e * 2^64 mod q for e < 2n (w0 = slot 0's root)
   u64 inv_gamma_R, inv_gamma_Rp;  // gamma^-1 * 2^64 mod q, Shoup
   const u64* wmask_R;        // rows x n: NTT of the kept mask rows, R-form
-  // NTT of the last exact-gadget digit from the others (base^-2 (R - D0 - base D1)).
-  u64 ld_inv, ld_invp, ld_c0, ld_c0p, ld_c1, ld_c1p;
+  // NTT of the last exact-gadget digit from the others (base^-2 (R - D0 - base D1)):
+  // the three constants in R-form, for one lazy Montgomery reduction.
+  u64 ld_inv_R, ld_c0_R, ld_c1_R;
 };
 
 // One query of a launch.

@@ -160,6 +160,15 @@ struct ig_ctx {
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_pool;
   std::vector<std::pair<int, size_t>> ev_used;  // (region, pool index)
   u64 launches = 0;
+  // Pinned staging ring for host->device copies issued on the stream: slot k is reused
+  // only after the copy that last read it has completed.
+  struct Staging {
+    void* host = nullptr;
+    size_t bytes = 0;
+    cudaEvent_t done = nullptr;
+  };
+  std::vector<Staging> staging;
+  size_t staging_next = 0;
 };
 
 namespace {
@@ -234,6 +243,29 @@ int scratch(ig_ctx* c, const char* name, size_t bytes, void** out) {
     b.bytes = want;
   }
   *out = b.p;
+  return IG_OK;
+}
+
+// Copies `bytes` from host memory to `dst` on the context stream through a pinned slot,
+// so the call returns without waiting for the device.
+int stage_h2d(ig_ctx* c, void* dst, const void* src, size_t bytes) {
+  if (bytes == 0) return IG_OK;
+  if (c->staging.empty()) c->staging.resize(8);
+  ig_ctx::Staging& sl = c->staging[c->staging_next];
+  c->staging_next = (c->staging_next + 1) % c->staging.size();
+  if (sl.done) IG_CUDA(c, cudaEventSynchronize(sl.done));
+  if (sl.bytes < bytes) {
+    if (sl.host) cudaFreeHost(sl.host);
+    sl.host = nullptr;
+    sl.bytes = 0;
+    size_t want = bytes + bytes / 2;
+    IG_CUDA(c, cudaHostAlloc(&sl.host, want, cudaHostAllocDefault));
+    sl.bytes = want;
+  }
+  if (!sl.done) IG_CUDA(c, cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming));
+  memcpy(sl.host, src, bytes);
+  IG_CUDA(c, cudaMemcpyAsync(dst, sl.host, bytes, cudaMemcpyHostToDevice, c->stream));
+  IG_CUDA(c, cudaEventRecord(sl.done, c->stream));
   return IG_OK;
 }
 
@@ -383,6 +415,14 @@ void ig_ctx_destroy(ig_ctx* c) {
   for (auto& kv : c->stores)
     for (auto& s : kv.second.seats) cudaFree(s.second.yR);
   for (auto& kv : c->scratch) cudaFree(kv.second.p);
+  for (auto& st : c->staging) {
+    if (st.host) cudaFreeHost(st.host);
+    if (st.done) cudaEventDestroy(st.done);
+  }
+  for (auto& ev : c->ev_pool) {
+    cudaEventDestroy(ev.first);
+    cudaEventDestroy(ev.second);
+  }
   cudaFree(c->zero_key);
   cudaStreamDestroy(c->stream);
   delete c;
@@ -504,12 +544,9 @@ int ig_crs_create(ig_ctx* c, uint32_t n, uint64_t q, uint64_t p, uint64_t gadget
   d.inv_gamma_Rp = shoup_companion(d.inv_gamma_R);
   // Last exact digit: base^-2 (R - D0 - base D1) (inspiring2.rs:1094-1161).
   const u64 inv = invmod(1ULL << 40);
-  d.ld_inv = inv;
-  d.ld_c0 = negq(inv);
-  d.ld_c1 = negq(mulmod(inv, 1ULL << 20));
-  d.ld_invp = shoup_companion(d.ld_inv);
-  d.ld_c0p = shoup_companion(d.ld_c0);
-  d.ld_c1p = shoup_companion(d.ld_c1);
+  d.ld_inv_R = mulmod(inv, R_MOD_Q);
+  d.ld_c0_R = mulmod(negq(inv), R_MOD_Q);
+  d.ld_c1_R = mulmod(negq(mulmod(inv, 1ULL << 20)), R_MOD_Q);
   // Mask rows -> NTT, R-form.
   void* mraw;
   rc = scratch(c, "mask_raw", mask.size() * 8, &mraw);
@@ -903,10 +940,11 @@ static int respond_host(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_t handle, c
     qs[i].seat_R = seat;
   }
   cudaStream_t s = c->stream;
-  IG_CUDA(c, cudaMemcpyAsync(d_table, table.data(), table.size() * sizeof(ShardDev), cudaMemcpyHostToDevice, s));
-  IG_CUDA(c, cudaMemcpyAsync(d_q, qs.data(), count * sizeof(QueryDev), cudaMemcpyHostToDevice, s));
-  IG_CUDA(c, cudaMemcpyAsync(d_seeds, as ? (const void*)as : (const void*)seeds, seed_bytes, cudaMemcpyHostToDevice, s));
-  IG_CUDA(c, cudaMemcpyAsync(d_bs, bs, (size_t)count * n * 8, cudaMemcpyHostToDevice, s));
+  if ((rc = stage_h2d(c, d_table, table.data(), table.size() * sizeof(ShardDev))) ||
+      (rc = stage_h2d(c, d_q, qs.data(), count * sizeof(QueryDev))) ||
+      (rc = stage_h2d(c, d_seeds, as ? (const void*)as : (const void*)seeds, seed_bytes)) ||
+      (rc = stage_h2d(c, d_bs, bs, (size_t)count * n * 8)))
+    return rc;
   IG_CUDA(c, cudaMemsetAsync(d_status, 0, count * 4, s));
   long pk = prof_begin(c, REGION_SCAN);
   IG_CUDA(c, igk::shard_scan(o.dev, (const QueryDev*)d_q, (const ShardDev*)d_table, count, (u64*)d_fold,
@@ -988,7 +1026,7 @@ int ig_respond_seeded_batch_device(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_
     qs[i].seat_R = seat;
   }
   cudaStream_t s = c->stream;
-  IG_CUDA(c, cudaMemcpyAsync(d_q, qs.data(), count * sizeof(QueryDev), cudaMemcpyHostToDevice, s));
+  if ((rc = stage_h2d(c, d_q, qs.data(), count * sizeof(QueryDev)))) return rc;
   IG_CUDA(c, cudaMemsetAsync(d_status, 0, count * 4, s));
   long pk = prof_begin(c, REGION_SCAN);
   IG_CUDA(c, igk::shard_scan(o.dev, (const QueryDev*)d_q, db->d_table, count, (u64*)d_fold, d_status, 0, nullptr, s));
