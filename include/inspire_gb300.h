@@ -50,6 +50,11 @@ int ig_last_error(const ig_ctx* ctx, char* buf, size_t len);
 void* ig_ctx_stream(ig_ctx* ctx);
 /* Device bytes held by this context's objects (stores, shards, seats, scratch). */
 uint64_t ig_ctx_device_bytes(const ig_ctx* ctx);
+/* Launch-shape knob: respond batches of at most max_queries queries run two CTAs per
+ * query (a thread-block cluster) so small batches still occupy most SMs; larger batches
+ * run one CTA per query. Default: half the device's SM count; 0 disables the pair form.
+ * Responses are identical either way. */
+int ig_ctx_set_pair_threshold(ig_ctx* ctx, uint32_t max_queries);
 
 /* ---- CRS / ServerInspiringCache ------------------------------------------------------
  * Replaces ServerInspiringCache::new (respond.rs:926-941) = PackParams::try_new

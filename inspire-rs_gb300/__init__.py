@@ -94,6 +94,7 @@ def _load():
         "ig_profile_enable": (I, [P, I]),
         "ig_profile_read": (I, [P, P, P, I, I]),
         "ig_launch_count": (U64, [P]),
+        "ig_ctx_set_pair_threshold": (I, [P, U32]),
         "ig_debug_store_sums": (I, [P, U64, U32, P]),
     }
     for name, (res, args) in sig.items():
@@ -148,6 +149,10 @@ class Context:
     @property
     def device_bytes(self):
         return self._lib.ig_ctx_device_bytes(self.h)
+
+    def set_pair_threshold(self, max_queries):
+        """Batches of at most max_queries run two CTAs per query (0: never)."""
+        self.check(self._lib.ig_ctx_set_pair_threshold(self.h, int(max_queries)))
 
     @property
     def launch_count(self):

@@ -15,6 +15,7 @@
 //                 (inspiring2.rs:1014-1085) with the online gather fused into each link
 //                 (inspiring2.rs:1393-1485), the final inverse transforms and the 36-bit
 //                 mod switch (pir/mod_switch.rs:148-176).
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include "ig_kernels.cuh"
@@ -97,8 +98,17 @@ __device__ __forceinline__ void ntt_fwd_r4(u64* const (&x)[NB], const u64* tw, c
   }
 }
 
+// Inverse ladder entry m from the forward one: psi^-brv(m) = q - f[3*2^s - 1 - m] for m in
+// [2^s, 2^(s+1)), and the Shoup companion of q - w is the bitwise complement of w's.
+__device__ __forceinline__ void inv_twiddle(const u64* tw, const u64* twp, int m, u64& w, u64& wp) {
+  const int s = 31 - __clz(m);
+  const int mp = 3 * (1 << s) - 1 - m;
+  w = Q - tw[mp];
+  wp = ~twp[mp];
+}
+
 template <int LOGN, int NT, int NB>
-__device__ __forceinline__ void ntt_inv_r4(u64* const (&x)[NB], const u64* itw, const u64* itwp) {
+__device__ __forceinline__ void ntt_inv_r4(u64* const (&x)[NB], const u64* tw, const u64* twp) {
   constexpr int N = 1 << LOGN;
   static_assert(NT == N / 4, "one radix-4 unit per thread");
   const int tid = threadIdx.x;
@@ -108,9 +118,10 @@ __device__ __forceinline__ void ntt_inv_r4(u64* const (&x)[NB], const u64* itw, 
     const int t = 1 << s, m = N >> (s + 1);
     const int B = tid >> s, o = tid & (t - 1);
     const int e0 = B * 4 * t + o;
-    const u64 w0 = itw[m + 2 * B], w0p = itwp[m + 2 * B];
-    const u64 w1 = itw[m + 2 * B + 1], w1p = itwp[m + 2 * B + 1];
-    const u64 w2 = itw[(m >> 1) + B], w2p = itwp[(m >> 1) + B];
+    u64 w0, w0p, w1, w1p, w2, w2p;
+    inv_twiddle(tw, twp, m + 2 * B, w0, w0p);
+    inv_twiddle(tw, twp, m + 2 * B + 1, w1, w1p);
+    inv_twiddle(tw, twp, (m >> 1) + B, w2, w2p);
 #pragma unroll
     for (int k = 0; k < NB; k++) {
       u64 a0 = x[k][e0], a1 = x[k][e0 + t], a2 = x[k][e0 + 2 * t], a3 = x[k][e0 + 3 * t];
@@ -127,7 +138,8 @@ __device__ __forceinline__ void ntt_inv_r4(u64* const (&x)[NB], const u64* itw, 
   }
   if (LOGN & 1) {
     constexpr int t = N / 2;
-    const u64 w = itw[1], wp = itwp[1];
+    u64 w, wp;
+    inv_twiddle(tw, twp, 1, w, wp);
 #pragma unroll
     for (int r = 0; r < 2; r++) {
       const int b = tid + r * NT;
@@ -307,55 +319,35 @@ __device__ __forceinline__ u64 mod_switch_word(u64 cv, u64 qn) {
   return quo % qn;
 }
 
-// ------------------------------------------------------------------------------------
-template <int LOGN>
-__global__ void __launch_bounds__((1 << LOGN) / 4, 1)
-    k_respond(CrsDev c, const QueryDev* queries, const ShardDev* shards, const u64* b_fold, u64 ms_target, u64* a_out, u64* b_out, u32* status, int force_serial) {
-  constexpr int N = 1 << LOGN, NT = N / 4;
-  constexpr u32 M2N = 2 * N - 1;
-  constexpr u64 DMASK = (1ULL << 20) - 1;
-  extern __shared__ __align__(16) u64 sm[];
-  u64* bufA = sm;
-  u64* bufB = sm + N;
-  u64* a_ntt = sm + 2 * N;
-  u64* tw = sm + 3 * N;
-  u64* twp = sm + 4 * N;
-  u64* itw = sm + 5 * N;
-  u64* itwp = sm + 6 * N;
-  const u32 rows = c.rows;
-  u64* Wm = sm + 7 * N;
-  u64* Y = Wm + rows * N;
-  uint16_t* e_tab = reinterpret_cast<uint16_t*>(Y + rows * N);
-  uint16_t* s_tab = e_tab + N;
-
-  const int tid = threadIdx.x;
-  const u32 qi = blockIdx.x;
-  const QueryDev qd = queries[qi];
-  const ShardDev sh = shards[qd.shard];
-  const u64* yR = qd.seat_R;
-  const u32 gamma = c.gamma;
-
-  for (int k = tid; k < N; k += NT) {
+// Per-query constants into shared memory: forward ladder, slot tables, the mask rows and
+// the seat's key rows (both R-form NTT).
+template <int N, int NT>
+__device__ __forceinline__ void stage_constants(const CrsDev& c, const u64* yR, u64* tw, u64* twp, u64* Wm, u64* Y,
+                                                uint16_t* e_tab, uint16_t* s_tab) {
+  for (int k = threadIdx.x; k < N; k += NT) {
     tw[k] = c.tw[k];
     twp[k] = c.twp[k];
-    itw[k] = c.itw[k];
-    itwp[k] = c.itwp[k];
     e_tab[k] = c.slot_exp[k];
     s_tab[k] = c.exp_slot[k];
   }
-  for (u32 k = tid; k < rows * N; k += NT) {
+  for (u32 k = threadIdx.x; k < c.rows * N; k += NT) {
     Wm[k] = c.wmask_R[k];
     Y[k] = yR[k];
   }
+}
 
-  // Query `a`: ChaCha20 keystream of the seed, u64 words in order, each accepted by
-  // rand's gen_range(0..q) rule. Block b of the stream yields words 8b..8b+7.
+// The query's `a` in coefficient form: the ChaCha20 keystream of its seed as u64 words
+// in order, each accepted by rand's gen_range(0..q) rule (math/poly.rs:657-671). Block b
+// of the stream yields words 8b..8b+7; a rejected word (probability ~2^-46) shifts every
+// later coefficient, and the walk is then redone word by word. Ends with a barrier.
+template <int N, int NT>
+__device__ __forceinline__ void expand_a(const QueryDev& qd, u64* a, u32* status, u32 qi, int force_serial) {
+  const int tid = threadIdx.x;
   bool rejected = false;
   if (qd.a) {
-    for (int k = tid; k < N; k += NT) a_ntt[k] = reduce128(qd.a[k]);
+    for (int k = tid; k < N; k += NT) a[k] = reduce128(qd.a[k]);
   } else if (tid < N / 8) {
-    u32 blk[16];
-    u32 key[8];
+    u32 blk[16], key[8];
 #pragma unroll
     for (int k = 0; k < 8; k++) key[k] = qd.seed[k];
     chacha20_block(key, (u64)tid, 0, blk);
@@ -363,11 +355,10 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
     for (int k = 0; k < 8; k++) {
       const u64 v = (u64)blk[2 * k] | ((u64)blk[2 * k + 1] << 32);
       if (v * Q > RANGE_ZONE) rejected = true;
-      a_ntt[tid * 8 + k] = mulhi(v, Q);
+      a[tid * 8 + k] = mulhi(v, Q);
     }
   }
   if (__syncthreads_or(rejected || (force_serial && !qd.a))) {
-    // A rejected word shifts every later coefficient: redo the walk word by word.
     if (tid == 0) {
       u32 blk[16], key[8];
       for (int k = 0; k < 8; k++) key[k] = qd.seed[k];
@@ -382,16 +373,68 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
         }
         const int k = (int)(cand & 7);
         const u64 v = (u64)blk[2 * k] | ((u64)blk[2 * k + 1] << 32);
-        if (v * Q <= RANGE_ZONE) a_ntt[filled++] = mulhi(v, Q);
+        if (v * Q <= RANGE_ZONE) a[filled++] = mulhi(v, Q);
         cand++;
       }
       if (filled < N) {
         atomicOr(status + qi, (u32)DEV_EXPAND_EXHAUSTED);
-        for (; filled < N; filled++) a_ntt[filled] = 0;
+        for (; filled < N; filled++) a[filled] = 0;
       }
     }
     __syncthreads();
   }
+}
+
+__device__ __forceinline__ u64 finish_a(const CrsDev& c, u64 x, u64 ms) {
+  const u64 v = shoup(x, c.ninv, c.ninvp);
+  return ms ? mod_switch_word(v, ms) : v;
+}
+__device__ __forceinline__ u64 finish_b(const CrsDev& c, u64 x, u32 t, u32 qi, const u64* b_fold, u64 ms) {
+  u64 v = shoup(x, c.ninv, c.ninvp);
+  if (t < c.gamma) v = addq(v, b_fold[(size_t)qi * c.gamma + t]);
+  return ms ? mod_switch_word(v, ms) : v;
+}
+
+// ------------------------------------------------------------------------------------
+// One CTA per query (batches that fill the GPU). Each link of the recursion (i from
+// gamma-2 down to 0) holds R_{i+1} in NTT form (`cur`, four slots per thread):
+//   r = INTT(R_{i+1});  d_k = base-2^20 digits of r (rounded, top carry kept, when the
+//   lowest digit is dropped);  D_k = NTT(d_k);
+//   sum_b += sum_k Y_k[tau_i(t)] D_k[t];
+//   R_i[t] = a_ntt[tau_i(t)] S_i[t] + sum_k W_k[tau_i(t)] D_k[t]
+// with tau_i the slot permutation of the automorphism X -> X^(g^i), S the packing store,
+// W the mask rows and Y the seat. Each sum of products takes one Montgomery reduction.
+// All digits are transformed (the reference derives the last one from the others; on
+// this machine a transform costs less than the three products that derivation takes).
+template <int LOGN>
+__global__ void __launch_bounds__((1 << LOGN) / 4, 1)
+    k_respond(CrsDev c, const QueryDev* queries, const ShardDev* shards, const u64* b_fold, u64 ms_target,
+              u64* a_out, u64* b_out, u32* status, int force_serial) {
+  constexpr int N = 1 << LOGN, NT = N / 4;
+  constexpr u32 M2N = 2 * N - 1;
+  constexpr u64 DMASK = (1ULL << 20) - 1;
+  extern __shared__ __align__(16) u64 sm[];
+  u64* bufA = sm;
+  u64* bufB = sm + N;
+  u64* bufC = sm + 2 * N;
+  u64* a_ntt = sm + 3 * N;
+  u64* tw = sm + 4 * N;
+  u64* twp = sm + 5 * N;
+  const u32 rows = c.rows;
+  u64* Wm = sm + 6 * N;
+  u64* Y = Wm + rows * N;
+  uint16_t* e_tab = reinterpret_cast<uint16_t*>(Y + rows * N);
+  uint16_t* s_tab = e_tab + N;
+
+  const int tid = threadIdx.x;
+  const u32 qi = blockIdx.x;
+  const QueryDev qd = queries[qi];
+  const ShardDev sh = shards[qd.shard];
+  const u32 gamma = c.gamma;
+  const bool exact = c.approx == 0;
+
+  stage_constants<N, NT>(c, qd.seat_R, tw, twp, Wm, Y, e_tab, s_tab);
+  expand_a<N, NT>(qd, a_ntt, status, qi, force_serial);
   {
     u64* const bufs[1] = {a_ntt};
     ntt_fwd_r4<LOGN, NT, 1>(bufs, tw, twp);
@@ -412,7 +455,6 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
       sb[k] = 0;
     }
   }
-  const bool exact = c.approx == 0;
 #pragma unroll 1
   for (int i = (int)gamma - 2; i >= 0; i--) {
     const u64* Srow = sh.sums_R + (size_t)i * N;
@@ -425,7 +467,7 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
     __syncthreads();
     {
       u64* const bufs[1] = {bufA};
-      ntt_inv_r4<LOGN, NT, 1>(bufs, itw, itwp);
+      ntt_inv_r4<LOGN, NT, 1>(bufs, tw, twp);
     }
 #pragma unroll
     for (int k = 0; k < 4; k++) {
@@ -433,28 +475,31 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
       const u64 r = shoup(bufA[t], c.ninv, c.ninvp);
       if (exact) {
         bufB[t] = r & DMASK;
-        bufA[t] = (r >> 20) & DMASK;
+        bufC[t] = (r >> 20) & DMASK;
+        bufA[t] = r >> 40;
       } else {
         const u64 rr = (r + (1ULL << 19)) >> 20;
         bufB[t] = rr & DMASK;
-        bufA[t] = rr >> 20;
+        bufC[t] = rr >> 20;
       }
     }
     __syncthreads();
-    {
-      u64* const bufs[2] = {bufB, bufA};
+    if (exact) {
+      u64* const bufs[3] = {bufB, bufC, bufA};
+      ntt_fwd_r4<LOGN, NT, 3>(bufs, tw, twp);
+    } else {
+      u64* const bufs[2] = {bufB, bufC};
       ntt_fwd_r4<LOGN, NT, 2>(bufs, tw, twp);
     }
-    // Pointwise link: every sum of products reduced once (lazy Montgomery).
 #pragma unroll
     for (int k = 0; k < 4; k++) {
       const int t = tid + k * NT;
       const u32 tb = s_tab[((gp * et[k]) & M2N) >> 1];
-      const u64 d0 = bufB[t], d1 = bufA[t];
+      const u64 d0 = bufB[t], d1 = bufC[t];
       u128 nb = wide(d0, Y[tb]) + wide(d1, Y[N + tb]);
       u128 nc = wide(a_ntt[tb], sv[k]) + wide(d0, Wm[tb]) + wide(d1, Wm[N + tb]);
       if (exact) {
-        const u64 d2 = redc(wide(cur[k], c.ld_inv_R) + wide(d0, c.ld_c0_R) + wide(d1, c.ld_c1_R));
+        const u64 d2 = bufA[t];
         nb += wide(d2, Y[2 * N + tb]);
         nc += wide(d2, Wm[2 * N + tb]);
       }
@@ -470,20 +515,160 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
   __syncthreads();
   {
     u64* const bufs[2] = {bufA, bufB};
-    ntt_inv_r4<LOGN, NT, 2>(bufs, itw, itwp);
+    ntt_inv_r4<LOGN, NT, 2>(bufs, tw, twp);
   }
 #pragma unroll
   for (int k = 0; k < 4; k++) {
     const int t = tid + k * NT;
-    u64 av = shoup(bufA[t], c.ninv, c.ninvp);
-    u64 bv = shoup(bufB[t], c.ninv, c.ninvp);
-    if ((u32)t < gamma) bv = addq(bv, b_fold[(size_t)qi * gamma + t]);
-    if (ms_target) {
-      av = mod_switch_word(av, ms_target);
-      bv = mod_switch_word(bv, ms_target);
+    a_out[(size_t)qi * N + t] = finish_a(c, bufA[t], ms_target);
+    b_out[(size_t)qi * N + t] = finish_b(c, bufB[t], t, qi, b_fold, ms_target);
+  }
+}
+
+// ------------------------------------------------------------------------------------
+// Two CTAs per query (a thread-block cluster), for batches that leave SMs idle with one
+// CTA each. Both CTAs hold R_{i+1} whole and run the inverse transform; CTA r then
+// transforms gadget digit r only and owns half of the slots for the pointwise link. The
+// peer's digit transform and R's other half cross through distributed shared memory, with
+// two cluster barriers per link:
+//   X (own half of R) written -> barrier -> peer half read into bufA -> INTT -> digit r ->
+//   NTT -> barrier -> peer's D read at own slots -> pointwise.
+// X is rewritten only after the second barrier of the previous link, when the peer has
+// read it; bufB (this CTA's D) only after the first barrier of the next link, when the
+// peer has consumed it. With the exact gadget the third digit's transform comes from the
+// other two: D_2 = base^-2 (R_{i+1} - D_0 - base D_1) (inspiring2.rs:1094-1161).
+template <int LOGN>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
+    k_respond_pair(CrsDev c, const QueryDev* queries, const ShardDev* shards, const u64* b_fold, u64 ms_target,
+                   u64* a_out, u64* b_out, u32* status, int force_serial) {
+  namespace cg = cooperative_groups;
+  constexpr int N = 1 << LOGN, NT = N / 4, H = N / 2;
+  constexpr u32 M2N = 2 * N - 1;
+  constexpr u64 DMASK = (1ULL << 20) - 1;
+  extern __shared__ __align__(16) u64 sm[];
+  u64* bufA = sm;
+  u64* bufB = sm + N;
+  u64* X = sm + 2 * N;  // H words
+  u64* a_ntt = X + H;
+  u64* tw = a_ntt + N;
+  u64* twp = tw + N;
+  const u32 rows = c.rows;
+  u64* Wm = twp + N;
+  u64* Y = Wm + rows * N;
+  uint16_t* e_tab = reinterpret_cast<uint16_t*>(Y + rows * N);
+  uint16_t* s_tab = e_tab + N;
+
+  cg::cluster_group cluster = cg::this_cluster();
+  const u32 rank = cluster.block_rank();
+  const u64* peerX = cluster.map_shared_rank(X, (int)(rank ^ 1));
+  const u64* peerB = cluster.map_shared_rank(bufB, (int)(rank ^ 1));
+  const int tid = threadIdx.x;
+  const u32 qi = blockIdx.x >> 1;
+  const QueryDev qd = queries[qi];
+  const ShardDev sh = shards[qd.shard];
+  const u32 gamma = c.gamma;
+  const bool exact = c.approx == 0;
+  const int own = (int)rank * H, other = (int)(rank ^ 1) * H;
+
+  stage_constants<N, NT>(c, qd.seat_R, tw, twp, Wm, Y, e_tab, s_tab);
+  expand_a<N, NT>(qd, a_ntt, status, qi, force_serial);
+  {
+    u64* const bufs[1] = {a_ntt};
+    ntt_fwd_r4<LOGN, NT, 1>(bufs, tw, twp);
+  }
+  u64 cur[2], sb[2];
+  u32 et[2];
+#pragma unroll
+  for (int k = 0; k < 2; k++) et[k] = e_tab[own + tid + k * NT];
+  {
+    const u32 gp = c.gpow[gamma - 1];
+    const u64* Srow = sh.sums_R + (size_t)(gamma - 1) * N;
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+      const int t = own + tid + k * NT;
+      const u32 tb = s_tab[((gp * et[k]) & M2N) >> 1];
+      cur[k] = mont(a_ntt[tb], Srow[t]);
+      sb[k] = 0;
     }
-    a_out[(size_t)qi * N + t] = av;
-    b_out[(size_t)qi * N + t] = bv;
+  }
+#pragma unroll 1
+  for (int i = (int)gamma - 2; i >= 0; i--) {
+    const u64* Srow = sh.sums_R + (size_t)i * N;
+    u64 sv[2];
+#pragma unroll
+    for (int k = 0; k < 2; k++) sv[k] = Srow[own + tid + k * NT];
+    const u32 gp = c.gpow[i];
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+      X[tid + k * NT] = cur[k];
+      bufA[own + tid + k * NT] = cur[k];
+    }
+    cluster.sync();
+#pragma unroll
+    for (int k = 0; k < 2; k++) bufA[other + tid + k * NT] = peerX[tid + k * NT];
+    __syncthreads();
+    {
+      u64* const bufs[1] = {bufA};
+      ntt_inv_r4<LOGN, NT, 1>(bufs, tw, twp);
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const int t = tid + k * NT;
+      const u64 r = shoup(bufA[t], c.ninv, c.ninvp);
+      u64 d;
+      if (exact) {
+        d = rank == 0 ? (r & DMASK) : ((r >> 20) & DMASK);
+      } else {
+        const u64 rr = (r + (1ULL << 19)) >> 20;
+        d = rank == 0 ? (rr & DMASK) : (rr >> 20);
+      }
+      bufB[t] = d;
+    }
+    __syncthreads();
+    {
+      u64* const bufs[1] = {bufB};
+      ntt_fwd_r4<LOGN, NT, 1>(bufs, tw, twp);
+    }
+    cluster.sync();
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+      const int t = own + tid + k * NT;
+      const u32 tb = s_tab[((gp * et[k]) & M2N) >> 1];
+      const u64 mine = bufB[t], theirs = peerB[t];
+      const u64 d0 = rank == 0 ? mine : theirs;
+      const u64 d1 = rank == 0 ? theirs : mine;
+      u128 nb = wide(d0, Y[tb]) + wide(d1, Y[N + tb]);
+      u128 nc = wide(a_ntt[tb], sv[k]) + wide(d0, Wm[tb]) + wide(d1, Wm[N + tb]);
+      if (exact) {
+        const u64 d2 = redc(wide(cur[k], c.ld_inv_R) + wide(d0, c.ld_c0_R) + wide(d1, c.ld_c1_R));
+        nb += wide(d2, Y[2 * N + tb]);
+        nc += wide(d2, Wm[2 * N + tb]);
+      }
+      sb[k] = addq(sb[k], redc(nb));
+      cur[k] = redc(nc);
+    }
+  }
+  // Final transforms: rank 0 assembles R_0 (-> a), rank 1 the online sum (-> b).
+#pragma unroll
+  for (int k = 0; k < 2; k++) {
+    X[tid + k * NT] = rank == 0 ? sb[k] : cur[k];
+    bufA[own + tid + k * NT] = rank == 0 ? cur[k] : sb[k];
+  }
+  cluster.sync();
+#pragma unroll
+  for (int k = 0; k < 2; k++) bufA[other + tid + k * NT] = peerX[tid + k * NT];
+  cluster.sync();  // each CTA's X stays alive until its peer has read it
+  {
+    u64* const bufs[1] = {bufA};
+    ntt_inv_r4<LOGN, NT, 1>(bufs, tw, twp);
+  }
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const int t = tid + k * NT;
+    if (rank == 0)
+      a_out[(size_t)qi * N + t] = finish_a(c, bufA[t], ms_target);
+    else
+      b_out[(size_t)qi * N + t] = finish_b(c, bufA[t], t, qi, b_fold, ms_target);
   }
 }
 
@@ -537,22 +722,33 @@ cudaError_t shard_scan(const CrsDev& c, const QueryDev* queries, const ShardDev*
   return cudaGetLastError();
 }
 
-size_t respond_smem_bytes(const CrsDev& c) {
-  return (size_t)(7 + 2 * c.rows) * c.n * 8 + 2 * (size_t)c.n * 2;
+size_t respond_smem_bytes(const CrsDev& c, bool pair) {
+  const size_t words = pair ? (size_t)(5 * c.n + c.n / 2) : (size_t)(6 * c.n);
+  return (words + 2 * (size_t)c.rows * c.n) * 8 + 2 * (size_t)c.n * 2;
 }
 
-cudaError_t respond(const CrsDev& c, const QueryDev* queries, const ShardDev* shards, u32 nq, const u64* b_fold, u64 ms_target, u64* a_out, u64* b_out, u32* status,
-                    int force_serial_expand, cudaStream_t s) {
+cudaError_t respond(const CrsDev& c, const QueryDev* queries, const ShardDev* shards, u32 nq,
+                    const u64* b_fold, u64 ms_target, u64* a_out, u64* b_out, u32* status,
+                    int force_serial_expand, bool pair, cudaStream_t s) {
   if (nq == 0) return cudaSuccess;
-  const size_t smem = respond_smem_bytes(c);
+  const size_t smem = respond_smem_bytes(c, pair);
   IG_DISPATCH_LOGN(c.logn, {
-    auto k = k_respond<L>;
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    k<<<nq, (1 << L) / 4, smem, s>>>(c, queries, shards, b_fold, ms_target, a_out, b_out, status,
-                                     force_serial_expand);
+    if (pair) {
+      auto k = k_respond_pair<L>;
+      cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+      k<<<2 * nq, (1 << L) / 4, smem, s>>>(c, queries, shards, b_fold, ms_target, a_out, b_out, status,
+                                           force_serial_expand);
+    } else {
+      auto k = k_respond<L>;
+      cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+      k<<<nq, (1 << L) / 4, smem, s>>>(c, queries, shards, b_fold, ms_target, a_out, b_out, status,
+                                       force_serial_expand);
+    }
   });
   return cudaGetLastError();
 }
+
 
 }  // namespace igk

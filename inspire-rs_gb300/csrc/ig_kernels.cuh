@@ -18,7 +18,6 @@ enum DeviceStatus : u32 {
 struct CrsDev {
   u32 n, logn, gamma, rows, approx;
   const u64 *tw, *twp;    // forward ladder psi^brv(m), Shoup companions (index m in [1, n))
-  const u64 *itw, *itwp;  // inverse ladder
   u64 ninv, ninvp;        // n^-1 mod q, Shoup
   const uint16_t* slot_exp;  // odd exponent e_t of slot t's root relative to slot 0's
   const uint16_t* exp_slot;  // slot holding exponent e, indexed e/2
@@ -73,9 +72,10 @@ cudaError_t store_fold(const CrsDev& c, const u64* H, u64* sums_R, cudaStream_t 
 
 // Fused per-query respond: expansion of `a`, store gather, backward recursion with the
 // online gather, final transforms, optional mod switch. One CTA per query.
+// `pair` selects two CTAs per query (a cluster of 2), for batches of at most half the SMs.
 cudaError_t respond(const CrsDev& c, const QueryDev* queries, const ShardDev* shards,
                     u32 nq, const u64* b_fold, u64 ms_target,
-                    u64* a_out, u64* b_out, u32* status, int force_serial_expand, cudaStream_t s);
+                    u64* a_out, u64* b_out, u32* status, int force_serial_expand, bool pair, cudaStream_t s);
 
-size_t respond_smem_bytes(const CrsDev& c);
+size_t respond_smem_bytes(const CrsDev& c, bool pair);
 }  // namespace igk

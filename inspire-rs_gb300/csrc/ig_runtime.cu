@@ -169,6 +169,9 @@ struct ig_ctx {
   };
   std::vector<Staging> staging;
   size_t staging_next = 0;
+  // Batches of at most this many queries run two CTAs per query (a cluster of two), so
+  // a batch smaller than the SM count still occupies most SMs. Default: half the SMs.
+  u32 pair_threshold = 0;
 };
 
 namespace {
@@ -389,6 +392,9 @@ int ig_ctx_create(int device, ig_ctx** out) {
   if (cudaSetDevice(device) != cudaSuccess) return IG_ERR_CUDA;
   auto* c = new ig_ctx();
   c->device = device;
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  c->pair_threshold = (u32)(sms / 2);
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
     delete c;
     return IG_ERR_CUDA;
@@ -466,12 +472,9 @@ int ig_crs_create(ig_ctx* c, uint32_t n, uint64_t q, uint64_t p, uint64_t gadget
   o.p = p;
   const u64 two_n = 2ULL * n;
   const u64 psi = find_root(two_n);
-  std::vector<u64> tw = ladder(n, psi), itw = ladder(n, invmod(psi));
-  std::vector<u64> twp(n), itwp(n);
-  for (u32 m = 0; m < n; m++) {
-    twp[m] = shoup_companion(tw[m]);
-    itwp[m] = shoup_companion(itw[m]);
-  }
+  std::vector<u64> tw = ladder(n, psi);
+  std::vector<u64> twp(n);
+  for (u32 m = 0; m < n; m++) twp[m] = shoup_companion(tw[m]);
   // Slot roots: slot t of the forward transform of X holds root w_t = w0^e_t.
   std::vector<u64> X(n, 0);
   X[1] = 1;
@@ -530,8 +533,7 @@ int ig_crs_create(ig_ctx* c, uint32_t n, uint64_t q, uint64_t p, uint64_t gadget
   d.rows = o.rows;
   d.approx = o.approx;
   int rc;
-  if ((rc = upload(c, o, tw, &d.tw)) || (rc = upload(c, o, twp, &d.twp)) || (rc = upload(c, o, itw, &d.itw)) ||
-      (rc = upload(c, o, itwp, &d.itwp)) || (rc = upload(c, o, slot_exp, &d.slot_exp)) ||
+  if ((rc = upload(c, o, tw, &d.tw)) || (rc = upload(c, o, twp, &d.twp)) || (rc = upload(c, o, slot_exp, &d.slot_exp)) ||
       (rc = upload(c, o, exp_slot, &d.exp_slot)) || (rc = upload(c, o, gpow, &d.gpow)) ||
       (rc = upload(c, o, cpow, &d.cpow)) || (rc = upload(c, o, m_of_i, &d.m_of_i)) ||
       (rc = upload(c, o, pow_root_R, &d.pow_root_R))) {
@@ -952,7 +954,7 @@ static int respond_host(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_t handle, c
   prof_end(c, pk);
   pk = prof_begin(c, REGION_RESPOND);
   IG_CUDA(c, igk::respond(o.dev, (const QueryDev*)d_q, (const ShardDev*)d_table, count, (const u64*)d_fold, ms_target,
-                          (u64*)d_a, (u64*)d_b, (u32*)d_status, c->force_serial, s));
+                          (u64*)d_a, (u64*)d_b, (u32*)d_status, c->force_serial, count <= c->pair_threshold, s));
   prof_end(c, pk);
   std::vector<u32> status(count);
   IG_CUDA(c, cudaMemcpyAsync(status.data(), d_status, count * 4, cudaMemcpyDeviceToHost, s));
@@ -1033,7 +1035,7 @@ int ig_respond_seeded_batch_device(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_
   prof_end(c, pk);
   pk = prof_begin(c, REGION_RESPOND);
   IG_CUDA(c, igk::respond(o.dev, (const QueryDev*)d_q, db->d_table, count, (const u64*)d_fold, ms_target, d_a, d_b,
-                          d_status, c->force_serial, s));
+                          d_status, c->force_serial, count <= c->pair_threshold, s));
   prof_end(c, pk);
   return IG_OK;
 }
@@ -1079,6 +1081,13 @@ int ig_response_encode(const uint64_t* a, const uint64_t* b, uint32_t n, uint32_
   put_u32(w, 0);   //   PackingMode::Inspiring)
   *len_out = w.size();
   if (out) memcpy(out, w.data(), w.size() < cap ? w.size() : cap);
+  return IG_OK;
+}
+
+int ig_ctx_set_pair_threshold(ig_ctx* c, uint32_t max_queries) {
+  if (!c) return IG_ERR_ARG;
+  std::lock_guard<std::mutex> lk(c->mu);
+  c->pair_threshold = max_queries;
   return IG_OK;
 }
 

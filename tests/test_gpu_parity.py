@@ -63,8 +63,16 @@ def test_d256_fixture_on_gpu(pkg, oracle, ctx):
     assert (db.store_sums(0) == ost.sums()).all()
 
 
+@pytest.fixture(params=["pair", "single"])
+def launch_shape(request, ctx):
+    """Both respond kernels: two CTAs per query (small batches) and one CTA per query."""
+    ctx.set_pair_threshold(1 << 20 if request.param == "pair" else 0)
+    yield request.param
+    ctx.set_pair_threshold(76)
+
+
 @pytest.mark.parametrize("entry,seed", D2048_CELLS)
-def test_d2048_seat_kat_cells_on_gpu(pkg, oracle, ctx, recorded_lines, entry, seed):
+def test_d2048_seat_kat_cells_on_gpu(pkg, oracle, ctx, recorded_lines, launch_shape, entry, seed):
     P = oracle.Params.d2048()
     n = P.n
     cell, crs, cache, db, keys = gpu_cell(pkg, oracle, P, entry, seed)
@@ -99,7 +107,7 @@ def test_d2048_seat_kat_cells_on_gpu(pkg, oracle, ctx, recorded_lines, entry, se
     assert store.remove(h) and not store.get(h) and len(store) == 0
 
 
-def test_mod_switched_batch_matches_oracle(pkg, oracle, ctx):
+def test_mod_switched_batch_matches_oracle(pkg, oracle, ctx, launch_shape):
     P = oracle.Params.d2048()
     cell, crs, cache, db, keys = gpu_cell(pkg, oracle, P, 512, 0x4D53)
     db.precompute_packing_all()
@@ -118,7 +126,7 @@ def test_mod_switched_batch_matches_oracle(pkg, oracle, ctx):
     assert wires == refs
 
 
-def test_approximate_gadget_matches_oracle(pkg, oracle, ctx):
+def test_approximate_gadget_matches_oracle(pkg, oracle, ctx, launch_shape):
     P = oracle.Params.d2048_approximate_gadget()
     cell, crs, cache, db, keys = gpu_cell(pkg, oracle, P, 64, 0xA9, approx=True)
     assert cache.key_rows == 2
@@ -130,7 +138,7 @@ def test_approximate_gadget_matches_oracle(pkg, oracle, ctx):
         assert cell.decode(idx, r.a, r.b)[0]
 
 
-def test_serial_expansion_path_matches(pkg, oracle, ctx):
+def test_serial_expansion_path_matches(pkg, oracle, ctx, launch_shape):
     P = oracle.Params.d2048()
     cell, crs, cache, db, keys = gpu_cell(pkg, oracle, P, 32, 0x5E1)
     sid, seed, b = cell.next_query(77)
@@ -203,7 +211,7 @@ def test_refusals(pkg, oracle, ctx):
     assert h2 > h1 and len(store) == 2
 
 
-def test_batch_across_many_shards(pkg, oracle, ctx):
+def test_batch_across_many_shards(pkg, oracle, ctx, launch_shape):
     P = oracle.Params.d2048()
     cell, crs, cache, db, keys = gpu_cell(pkg, oracle, P, 512, 0x5A5A, entries=2048 * 8)
     db.precompute_packing_all()
