@@ -1138,4 +1138,108 @@ int ig_debug_store_sums(ig_ctx* c, uint64_t dbh, uint32_t s, uint64_t* out) {
   return IG_OK;
 }
 
+// ---- allocation-free respond --------------------------------------------------------------
+// Some embedders cannot let a library allocate device memory on a request path: servers
+// that pre-size every device buffer at start-up and refuse growth afterwards, processes
+// that capture their launch sequence into a graph, and memory-capped GPU partitions shared
+// with other jobs. For them the batch respond has a variant whose scratch (the per-query
+// fold of b, the query descriptors and the status words) lives in one file-scope device
+// array of fixed size. Every GPU that loads the library holds this array until exit.
+enum : u32 { NOALLOC_MAX_QUERIES = 64, NOALLOC_MAX_GAMMA = 1024 };
+static constexpr size_t NOALLOC_FOLD_BYTES = (size_t)NOALLOC_MAX_QUERIES * NOALLOC_MAX_GAMMA * 8;
+static constexpr size_t NOALLOC_QUERY_OFF = NOALLOC_FOLD_BYTES;
+static constexpr size_t NOALLOC_STATUS_OFF =
+    NOALLOC_QUERY_OFF + ((NOALLOC_MAX_QUERIES * sizeof(QueryDev) + 255) / 256) * 256;
+static constexpr size_t NOALLOC_BYTES = NOALLOC_STATUS_OFF + 256;
+static_assert(NOALLOC_BYTES == 527104, "the header states this size");
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
+
+// Device address of g_noalloc_scratch on `device` (the current device). In host code the
+// array's name is only a stand-in for the symbol, never a device pointer: the address
+// comes from cudaGetSymbolAddress, resolved once per device and cached.
+static int noalloc_scratch(ig_ctx* c, unsigned char** out) {
+  static std::mutex mu;
+  static std::unordered_map<int, unsigned char*> addr;
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = addr.find(c->device);
+  if (it != addr.end()) {
+    *out = it->second;
+    return IG_OK;
+  }
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || !p)
+    return fail(c, IG_ERR_CUDA, "cannot resolve the allocation-free scratch on device %d: %s", c->device,
+                cudaGetErrorString(e));
+  addr[c->device] = (unsigned char*)p;
+  *out = (unsigned char*)p;
+  return IG_OK;
+}
+
+int ig_respond_seeded_batch_noalloc(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_t handle, uint32_t count,
+                                    const uint32_t* shard_ids, const uint8_t* d_seeds, const uint64_t* d_bs,
+                                    uint64_t ms_target, uint64_t* d_a, uint64_t* d_b) {
+  if (!c) return IG_ERR_ARG;
+  if (count == 0 || !shard_ids || !d_seeds || !d_bs || !d_a || !d_b)
+    return fail(c, IG_ERR_ARG, "ig_respond_seeded_batch_noalloc: empty batch or null buffer");
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  DbObj* db = get_db(c, dbh);
+  if (!db) return fail(c, IG_ERR_HANDLE, "unknown database handle %llu", (unsigned long long)dbh);
+  CrsObj& o = *get_crs(c, db->crs);
+  const size_t n = o.n, g = o.gamma;
+  if (count > NOALLOC_MAX_QUERIES || g > NOALLOC_MAX_GAMMA)
+    return fail(c, IG_ERR_ARG,
+                "ig_respond_seeded_batch_noalloc serves at most %u queries of width at most %u per call (its "
+                "scratch is fixed); got %u queries of width %zu. Split the batch or use ig_respond_seeded_batch",
+                (u32)NOALLOC_MAX_QUERIES, (u32)NOALLOC_MAX_GAMMA, count, g);
+  if (ms_target && (ms_target >= Q || ms_target < o.p || ms_target % (2 * n) != 1))
+    return fail(c, IG_ERR_ARG, "mod-switch target_modulus %llu must be in [p, q) and 1 mod 2d",
+                (unsigned long long)ms_target);
+  const u64* seat;
+  int rc = resolve_seat(c, o, st, handle, nullptr, 0, 0, &seat);
+  if (rc) return rc;
+  for (u32 i = 0; i < count; i++) {
+    const u32 s = shard_ids[i];
+    if (s >= db->num_shards)
+      return fail(c, IG_ERR_ARG, "shard %u not found; encoded database has %u shards", s, db->num_shards);
+    if (!db->shards[s].sums)
+      return fail(c, IG_ERR_ARG, "shard %u has no packing store; the allocation-free respond serves stored shards",
+                  s);
+  }
+  unsigned char* base;
+  if ((rc = noalloc_scratch(c, &base))) return rc;
+  u64* d_fold = (u64*)base;
+  QueryDev* d_q = (QueryDev*)(base + NOALLOC_QUERY_OFF);
+  u32* d_status = (u32*)(base + NOALLOC_STATUS_OFF);
+  QueryDev qs[NOALLOC_MAX_QUERIES];
+  for (u32 i = 0; i < count; i++) {
+    qs[i].shard = shard_ids[i];
+    qs[i].reserved = 0;
+    qs[i].seed = (const u32*)(d_seeds + (size_t)i * 32);
+    qs[i].a = nullptr;
+    qs[i].b = d_bs + (size_t)i * n;
+    qs[i].seat_R = seat;
+  }
+  cudaStream_t s = c->stream;
+  IG_CUDA(c, cudaMemcpyAsync(d_q, qs, count * sizeof(QueryDev), cudaMemcpyHostToDevice, s));
+  IG_CUDA(c, cudaMemsetAsync(d_status, 0, count * 4, s));
+  IG_CUDA(c, igk::shard_scan(o.dev, d_q, db->d_table, count, d_fold, d_status, 0, nullptr, s));
+  IG_CUDA(c, igk::respond(o.dev, d_q, db->d_table, count, d_fold, ms_target, d_a, d_b, d_status, c->force_serial,
+                          count <= c->pair_threshold, s));
+  c->launches += 2;
+  u32 status[NOALLOC_MAX_QUERIES];
+  IG_CUDA(c, cudaMemcpyAsync(status, d_status, count * 4, cudaMemcpyDeviceToHost, s));
+  IG_CUDA(c, cudaStreamSynchronize(s));
+  for (u32 i = 0; i < count; i++) {
+    if (status[i] & DEV_TAG_MISMATCH)
+      return fail(c, IG_ERR_STORE_REFUSED,
+                  "shard %u: packing store refused: a column is not the column the store was built from. The shard "
+                  "changed after the build; rebuild the store before serving it",
+                  shard_ids[i]);
+    if (status[i]) return fail(c, IG_ERR_DEVICE, "query %u: respond kernel status %u", i, status[i]);
+  }
+  return IG_OK;
+}
+
 }  // extern "C"
