@@ -290,3 +290,145 @@ class Cell:
 
 def gaussian_stream_fnv(sigma, seed, count):
     return lib().orc_gaussian_stream_fnv(sigma, seed, count)
+
+
+# ---------------------------------------------------------------------------------------
+# special_modulus (src/special_modulus/ of the reference): ring 2048, q = 536813569,
+# p = 2147389441, 256-byte cells, 246-byte records, gamma 512.
+SM_D, SM_GAMMA, SM_Q, SM_P, SM_CELL, SM_RECORD = 2048, 512, 536813569, 2147389441, 256, 246
+_sm_bound = False
+
+
+def _sm_lib():
+    global _sm_bound
+    L = lib()
+    if not _sm_bound:
+        V, P, U64 = ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64
+        sig = {
+            "orc_sm_server_new": (V, []), "orc_sm_server_free": (None, [V]),
+            "orc_sm_client_new": (V, [P]), "orc_sm_client_free": (None, [V]),
+            "orc_sm_client_key": (None, [V, P, P, P]), "orc_sm_client_key_bytes": (U64, [V, P, U64]),
+            "orc_sm_client_query": (None, [V, U64, P, P]), "orc_sm_client_decode": (U64, [V, P, P, P]),
+            "orc_sm_table_new": (V, [V, P, U64]), "orc_sm_table_free": (None, [V]),
+            "orc_sm_table_step1": (None, [V, P]),
+            "orc_sm_seat_new": (V, [V, P, P, P]), "orc_sm_seat_free": (None, [V]),
+            "orc_sm_respond": (None, [V, V, V, P, P, P, P]),
+            "orc_sm_query_bytes": (U64, [P, P, P, U64]), "orc_sm_response_bytes": (U64, [P, P, P, U64]),
+            "orc_sm_kat_cells": (None, [U64, U64, P]),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _sm_bound = True
+    return L
+
+
+def _bytes_of(fn, *args):
+    n = fn(*args, None, 0)
+    out = np.zeros(n, dtype=np.uint8)
+    fn(*args, _p(out), n)
+    return out.tobytes()
+
+
+class SmServer:
+    def __init__(self):
+        self.h = _sm_lib().orc_sm_server_new()
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            _sm_lib().orc_sm_server_free(self.h)
+
+    def table(self, cells: bytes):
+        return SmTable(self, cells)
+
+    def seat(self, key):
+        return SmSeat(self, key)
+
+    def respond(self, table, seat, seed: bytes, body):
+        s = np.frombuffer(seed, dtype=np.uint8).copy()
+        b = np.ascontiguousarray(body, dtype=np.uint32)
+        mask = np.zeros(SM_D, dtype=np.uint32)
+        out = np.zeros(2 * SM_RECORD, dtype=np.uint32)
+        _sm_lib().orc_sm_respond(self.h, table.h, seat.h, _p(s), _p(b), _p(mask), _p(out))
+        return mask, out
+
+
+class SmTable:
+    def __init__(self, server, cells: bytes):
+        c = np.frombuffer(cells, dtype=np.uint8).copy()
+        self.h = _sm_lib().orc_sm_table_new(server.h, _p(c), len(cells))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            _sm_lib().orc_sm_table_free(self.h)
+
+    def step1(self):
+        out = np.zeros((SM_GAMMA, SM_D), dtype=np.uint32)
+        _sm_lib().orc_sm_table_step1(self.h, _p(out))
+        return out
+
+
+class SmSeat:
+    def __init__(self, server, key):
+        ms = np.frombuffer(key[0], dtype=np.uint8).copy()
+        kq = np.ascontiguousarray(key[1], dtype=np.uint32)
+        kp = np.ascontiguousarray(key[2], dtype=np.uint32)
+        self.h = _sm_lib().orc_sm_seat_new(server.h, _p(ms), _p(kq), _p(kp))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            _sm_lib().orc_sm_seat_free(self.h)
+
+
+class SmClient:
+    """Client::from_seed of the reference (special_modulus/client.rs:137-143)."""
+
+    def __init__(self, seed: bytes):
+        s = np.frombuffer(seed, dtype=np.uint8).copy()
+        self.h = _sm_lib().orc_sm_client_new(_p(s))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            _sm_lib().orc_sm_client_free(self.h)
+
+    def key(self):
+        ms = np.zeros(32, dtype=np.uint8)
+        kq = np.zeros(SM_D, dtype=np.uint32)
+        kp = np.zeros(SM_D, dtype=np.uint32)
+        _sm_lib().orc_sm_client_key(self.h, _p(ms), _p(kq), _p(kp))
+        return ms.tobytes(), kq, kp
+
+    def key_bytes(self):
+        return _bytes_of(_sm_lib().orc_sm_client_key_bytes, self.h)
+
+    def query(self, row):
+        seed = np.zeros(32, dtype=np.uint8)
+        body = np.zeros(SM_D, dtype=np.uint32)
+        _sm_lib().orc_sm_client_query(self.h, row, _p(seed), _p(body))
+        return seed.tobytes(), body
+
+    def decode(self, mask, body):
+        m = np.ascontiguousarray(mask, dtype=np.uint32)
+        b = np.ascontiguousarray(body, dtype=np.uint32)
+        out = np.zeros(SM_RECORD, dtype=np.uint8)
+        n = _sm_lib().orc_sm_client_decode(self.h, _p(m), _p(b), _p(out))
+        return out[:n].tobytes()
+
+
+def sm_query_bytes(seed, body):
+    s = np.frombuffer(seed, dtype=np.uint8).copy()
+    b = np.ascontiguousarray(body, dtype=np.uint32)
+    return _bytes_of(_sm_lib().orc_sm_query_bytes, _p(s), _p(b))
+
+
+def sm_response_bytes(mask, body):
+    m = np.ascontiguousarray(mask, dtype=np.uint32)
+    b = np.ascontiguousarray(body, dtype=np.uint32)
+    return _bytes_of(_sm_lib().orc_sm_response_bytes, _p(m), _p(b))
+
+
+def sm_kat_cells(seed, rows):
+    out = np.zeros(rows * SM_CELL, dtype=np.uint8)
+    _sm_lib().orc_sm_kat_cells(seed, rows, _p(out))
+    return out.tobytes()

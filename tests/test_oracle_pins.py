@@ -129,3 +129,24 @@ def test_mod_switched_response_size(oracle):
     for c in [0, 1, P.q // 2, P.q - 1, 123456789123]:
         want = ((c * t + P.q // 2) // P.q) % t
         assert int(oracle.mod_switch(np.array([c], dtype=np.uint64))[0]) == want
+
+
+def test_special_modulus_pinned_wire_digests(oracle):
+    """tests/special_modulus_kat.rs:349-380: Client::from_seed([42; 32]), 2048 cells from
+    seed_from_u64(42), row 1234 — key, query and response bytes pinned by FNV-1a."""
+    pins = dict(line.split() for line in open(os.path.join(GOLDEN, "special_modulus_pins.txt")))
+    client = oracle.SmClient(bytes([42] * 32))
+    server = oracle.SmServer()
+    cells = oracle.sm_kat_cells(42, 2048)
+    table = server.table(cells)
+    seat = server.seat(client.key())
+    kb = client.key_bytes()
+    seed, body = client.query(1234)
+    qb = oracle.sm_query_bytes(seed, body)
+    mask, rbody = server.respond(table, seat, seed, body)
+    rb = oracle.sm_response_bytes(mask, rbody)
+    assert (len(kb), len(qb), len(rb)) == (15_394, 7_456, 9_208)
+    assert oracle.fnv1a(kb) == int(pins["key"], 16)
+    assert oracle.fnv1a(qb) == int(pins["query"], 16)
+    assert oracle.fnv1a(rb) == int(pins["response"], 16)
+    assert client.decode(mask, rbody) == cells[1234 * 256:1234 * 256 + 246]
