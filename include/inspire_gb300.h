@@ -158,6 +158,45 @@ int ig_respond_seeded_batch_noalloc(ig_ctx* ctx, uint64_t db, uint64_t store, ui
                                     const uint32_t* shard_ids, const uint8_t* d_seeds, const uint64_t* d_bs,
                                     uint64_t mod_switch_target, uint64_t* d_a_out, uint64_t* d_b_out);
 
+/* ---- special_modulus ------------------------------------------------------------------
+ * The two-prime packed variant of src/special_modulus/ (mod.rs, server.rs): ciphertext
+ * prime q < 2^29, special prime p < 2^31, 4-bit signed nibbles, all words 32-bit.
+ *
+ * Server::new / with_kernel (server.rs:145-164) over Params (mod.rs:62-159); the GPU path
+ * serves ring_dim 2048 (Params::ring2048_cell256: gamma 512, q 536813569,
+ * p 2147389441, 256-byte cells, 246-byte records, key-mask version 2). */
+int ig_sm_server_create(ig_ctx* ctx, uint32_t ring_dim, uint32_t gamma, uint64_t q, uint64_t special_prime,
+                        uint32_t cell_bytes, uint32_t record_bytes, uint32_t key_mask_version, uint64_t* server_out);
+int ig_sm_server_destroy(ig_ctx* ctx, uint64_t server);
+/* Server::seat (server.rs:177-203): the decoded PackingKey (mask seed, q limb, p limb, each
+ * limb ring_dim residues) -> a 32,768-byte device seat (both limbs and the key's own mask,
+ * NTT, Montgomery form). Refuses non-residues. */
+int ig_sm_seat(ig_ctx* ctx, uint64_t server, const uint8_t mask_seed[32], const uint32_t* key_q,
+               const uint32_t* key_p, uint64_t* seat_out);
+int ig_sm_seat_destroy(ig_ctx* ctx, uint64_t seat);
+/* Server::table (server.rs:211-249) -> ShardTable: at most ring_dim cells of cell_bytes,
+ * bytes past each record zero; the step-1 table (4 MiB) and the nibbles (1 MiB) in HBM. */
+int ig_sm_table(ig_ctx* ctx, uint64_t server, const uint8_t* cells, size_t nbytes, uint64_t* table_out);
+int ig_sm_table_destroy(ig_ctx* ctx, uint64_t table);
+/* Test hook: the table's step-1 words (gamma x ring_dim, Montgomery form, as the reference
+ * holds them) copied to host memory. */
+int ig_sm_table_step1(ig_ctx* ctx, uint64_t table, uint32_t* out);
+/* Server::respond (server.rs:252-279) for `count` queries: query i reads tables[i] under
+ * seats[i], its Query = seeds[32 i..] and bodies[ring_dim i..]; the Response is
+ * mask_out[ring_dim i..] and body_out[2 record_bytes i..]. All or nothing. */
+int ig_sm_respond_batch(ig_ctx* ctx, uint64_t server, uint32_t count, const uint64_t* tables, const uint64_t* seats,
+                        const uint8_t* seeds, const uint32_t* bodies, uint32_t* mask_out, uint32_t* body_out);
+/* Same with device-resident inputs and outputs; enqueues and returns, status words in
+ * d_status (0 = served). */
+int ig_sm_respond_batch_device(ig_ctx* ctx, uint64_t server, uint32_t count, const uint64_t* tables,
+                               const uint64_t* seats, const uint8_t* d_seeds, const uint32_t* d_bodies,
+                               uint32_t* d_mask_out, uint32_t* d_body_out, uint32_t* d_status);
+
+/* Response::to_bytes (special_modulus/wire.rs:120-125): mask (n words) then body (nb
+ * words), each packed at q's bit width; 9,208 bytes at the served set. */
+int ig_sm_response_encode(const uint32_t* mask, uint32_t n, const uint32_t* body, uint32_t nb, uint64_t q,
+                          uint8_t* out, size_t cap, size_t* len_out);
+
 /* ---- wire ------------------------------------------------------------------------------
  * ServerResponse bincode bytes of a packed response (respond.rs:111-176, tight codec
  * poly.rs:166-225): Packed{a, b_prefix (first `retained` b coefficients), retained}, no

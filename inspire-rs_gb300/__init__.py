@@ -29,7 +29,7 @@ __all__ = [
     "ServerSessionStore", "ServerSessionHandle", "ClientPackingKeys", "SeededBatchQuery", "SeededClientQuery",
     "SeededQueryBatch", "PackingKeySource", "ServerResponse", "respond_seeded_inspiring", "respond_seeded_batch", "respond_inspiring",
     "check_mod_switch_noise_budget", "ClientQuery", "Context", "DEFAULT_Q",
-    "MOD_SWITCH_TARGET_36BIT", "MOD_SWITCH_TARGET_45BIT", "library_path",
+    "MOD_SWITCH_TARGET_36BIT", "MOD_SWITCH_TARGET_45BIT", "library_path", "special_modulus",
 ]
 
 DEFAULT_Q = 1152921504606830593
@@ -95,6 +95,16 @@ def _load():
         "ig_profile_read": (I, [P, P, P, I, I]),
         "ig_launch_count": (U64, [P]),
         "ig_ctx_set_pair_threshold": (I, [P, U32]),
+        "ig_sm_server_create": (I, [P, U32, U32, U64, U64, U32, U32, U32, pu64]),
+        "ig_sm_server_destroy": (I, [P, U64]),
+        "ig_sm_seat": (I, [P, U64, P, P, P, pu64]),
+        "ig_sm_seat_destroy": (I, [P, U64]),
+        "ig_sm_table": (I, [P, U64, P, ctypes.c_size_t, pu64]),
+        "ig_sm_table_destroy": (I, [P, U64]),
+        "ig_sm_table_step1": (I, [P, U64, P]),
+        "ig_sm_respond_batch": (I, [P, U64, U32, P, P, P, P, P, P]),
+        "ig_sm_respond_batch_device": (I, [P, U64, U32, P, P, P, P, P, P, P]),
+        "ig_sm_response_encode": (I, [P, U32, P, U32, U64, P, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
         "ig_debug_store_sums": (I, [P, U64, U32, P]),
     }
     for name, (res, args) in sig.items():
@@ -517,3 +527,109 @@ def respond_seeded_inspiring(crs: ServerCrs, encoded_db: EncodedDatabase, query:
         raise PirError("InspiRING client packing keys missing from query (neither inlined nor session_handle set)")
     src = PackingKeySource.Inline(keys) if keys is not None else PackingKeySource.Registered(handle)
     return _batch(crs, encoded_db, [query], src, session_store, mod_switch_target)[0]
+
+
+class _SpecialModulus:
+    """The special_modulus variant (reference src/special_modulus/): Params, Server,
+    ShardTable, KeySeat, Query and Response over 32-bit words, run on the GPU."""
+
+    class Params:
+        """Params::ring2048_cell256 (special_modulus/mod.rs:84-95)."""
+
+        def __init__(self, ring_dim=2048, gamma=512, q=536_813_569, special_prime=2_147_389_441, cell_bytes=256,
+                     record_bytes=246, sigma=6.4, key_mask_version=2):
+            self.ring_dim, self.gamma, self.q, self.special_prime = ring_dim, gamma, q, special_prime
+            self.cell_bytes, self.record_bytes, self.sigma = cell_bytes, record_bytes, sigma
+            self.key_mask_version = key_mask_version
+
+        @staticmethod
+        def ring2048_cell256():
+            return _SpecialModulus.Params()
+
+        def body_coefficients(self):
+            return 2 * self.record_bytes
+
+    class PackingKey:
+        """A decoded packing key (wire.rs:37-43): mask seed and the two limbs."""
+
+        def __init__(self, mask_seed: bytes, q, p):
+            self.mask_seed = bytes(mask_seed)
+            self.q = np.ascontiguousarray(q, dtype=np.uint32)
+            self.p = np.ascontiguousarray(p, dtype=np.uint32)
+
+    class Query:
+        def __init__(self, seed: bytes, body):
+            self.seed = bytes(seed)
+            self.body = np.ascontiguousarray(body, dtype=np.uint32)
+
+    class Response:
+        def __init__(self, mask, body, q):
+            self.mask, self.body, self.q = mask, body, q
+
+        def to_bytes(self) -> bytes:
+            L = _load()
+            m = np.ascontiguousarray(self.mask, dtype=np.uint32)
+            b = np.ascontiguousarray(self.body, dtype=np.uint32)
+            n = ctypes.c_size_t()
+            if L.ig_sm_response_encode(_ptr(m), len(m), _ptr(b), len(b), self.q, None, 0, ctypes.byref(n)):
+                raise PirError("response coefficient is not a residue")
+            out = np.zeros(n.value, dtype=np.uint8)
+            L.ig_sm_response_encode(_ptr(m), len(m), _ptr(b), len(b), self.q, _ptr(out), n.value, ctypes.byref(n))
+            return out.tobytes()
+
+    class Server:
+        """Server::new (server.rs:145-164): seat, table and respond on one device."""
+
+        def __init__(self, params=None, ctx: Context = None):
+            self.ctx = ctx or Context.default()
+            self.params = params or _SpecialModulus.Params()
+            p = self.params
+            h = ctypes.c_uint64()
+            self.ctx.check(self.ctx._lib.ig_sm_server_create(
+                self.ctx.h, p.ring_dim, p.gamma, p.q, p.special_prime, p.cell_bytes, p.record_bytes,
+                p.key_mask_version, ctypes.byref(h)))
+            self.h = h.value
+
+        def seat(self, key):
+            h = ctypes.c_uint64()
+            ms = np.frombuffer(key.mask_seed, dtype=np.uint8).copy()
+            if len(key.q) != self.params.ring_dim or len(key.p) != self.params.ring_dim:
+                raise PirError(f"packing key needs {self.params.ring_dim} coefficients per limb")
+            self.ctx.check(self.ctx._lib.ig_sm_seat(self.ctx.h, self.h, _ptr(ms), _ptr(key.q), _ptr(key.p),
+                                                    ctypes.byref(h)))
+            return h.value
+
+        def table(self, cells: bytes):
+            h = ctypes.c_uint64()
+            c = np.frombuffer(bytes(cells), dtype=np.uint8).copy()
+            self.ctx.check(self.ctx._lib.ig_sm_table(self.ctx.h, self.h, _ptr(c) if len(c) else None, len(c),
+                                                     ctypes.byref(h)))
+            return h.value
+
+        def table_step1(self, table):
+            out = np.zeros((self.params.gamma, self.params.ring_dim), dtype=np.uint32)
+            self.ctx.check(self.ctx._lib.ig_sm_table_step1(self.ctx.h, table, _ptr(out)))
+            return out
+
+        def respond(self, table, seat, query):
+            return self.respond_batch([table], [seat], [query])[0]
+
+        def respond_batch(self, tables, seats, queries):
+            n, nb = self.params.ring_dim, self.params.body_coefficients()
+            count = len(queries)
+            if count == 0 or len(tables) != count or len(seats) != count:
+                raise PirError("a batch needs one table and one seat per query")
+            th = np.array(tables, dtype=np.uint64)
+            sh = np.array(seats, dtype=np.uint64)
+            seeds = np.frombuffer(b"".join(q.seed for q in queries), dtype=np.uint8).copy()
+            bodies = np.stack([q.body for q in queries]).astype(np.uint32)
+            if bodies.shape != (count, n):
+                raise PirError("query does not fit the set")
+            mask = np.zeros((count, n), dtype=np.uint32)
+            body = np.zeros((count, nb), dtype=np.uint32)
+            self.ctx.check(self.ctx._lib.ig_sm_respond_batch(self.ctx.h, self.h, count, _ptr(th), _ptr(sh),
+                                                             _ptr(seeds), _ptr(bodies), _ptr(mask), _ptr(body)))
+            return [_SpecialModulus.Response(mask[i], body[i], self.params.q) for i in range(count)]
+
+
+special_modulus = _SpecialModulus

@@ -10,7 +10,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libinspire_gb300.so")
-SOURCES = ["ig_kernels.cu", "ig_runtime.cu"]
+SOURCES = ["ig_kernels.cu", "ig_runtime.cu", "ig_sm_kernels.cu", "ig_sm_runtime.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
 

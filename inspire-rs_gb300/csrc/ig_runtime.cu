@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "../../include/inspire_gb300.h"
+#include "ig_internal.hpp"
 #include "ig_kernels.cuh"
 
 using namespace ig;
@@ -172,6 +173,9 @@ struct ig_ctx {
   // Batches of at most this many queries run two CTAs per query (a cluster of two), so
   // a batch smaller than the SM count still occupies most SMs. Default: half the SMs.
   u32 pair_threshold = 0;
+  // special_modulus objects (ig_sm_runtime.cu) and their destructor.
+  void* sm = nullptr;
+  void (*sm_destroy)(ig_ctx*, void*) = nullptr;
 };
 
 namespace {
@@ -377,6 +381,28 @@ int build_store(ig_ctx* c, DbObj& db, CrsObj& o, u32 s) {
 
 }  // namespace
 
+namespace igint {
+int fail(ig_ctx* c, int code, const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (c) c->err = buf;
+  return code;
+}
+cudaStream_t stream(ig_ctx* c) { return c->stream; }
+int device(ig_ctx* c) { return c->device; }
+std::mutex& mutex(ig_ctx* c) { return c->mu; }
+int dalloc(ig_ctx* c, void** p, size_t bytes) { return ::dalloc(c, p, bytes, nullptr); }
+void dfree(ig_ctx* c, void* p, size_t bytes) { ::dfree(c, p, bytes); }
+int scratch(ig_ctx* c, const char* name, size_t bytes, void** out) { return ::scratch(c, name, bytes, out); }
+int stage_h2d(ig_ctx* c, void* dst, const void* src, size_t bytes) { return ::stage_h2d(c, dst, src, bytes); }
+void add_launches(ig_ctx* c, unsigned n) { c->launches += n; }
+void*& sm_slot(ig_ctx* c) { return c->sm; }
+void set_sm_destructor(ig_ctx* c, void (*fn)(ig_ctx*, void*)) { c->sm_destroy = fn; }
+}  // namespace igint
+
 // =========================================================================================
 extern "C" {
 
@@ -407,6 +433,7 @@ void ig_ctx_destroy(ig_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
+  if (c->sm && c->sm_destroy) c->sm_destroy(c, c->sm);
   for (auto& kv : c->crs)
     for (void* p : kv.second.allocs) cudaFree(p);
   for (auto& kv : c->dbs) {

@@ -1,0 +1,423 @@
+// Kernels of the special_modulus respond path (reference src/special_modulus/server.rs).
+//
+//   ntt_rows      forward Ntt32 of many rows (seat limbs, key mask, table columns)
+//   table_columns nibble decode of a shard's cells (mod.rs:366-371, server.rs:211-249)
+//   table_fold    step 1 folded over the columns (server.rs:331-383) as a per-slot DFT
+//   body_fold     the response body's column fold over the shard's nibbles (server.rs:401-411)
+//   respond       the 2n-link two-prime recursion and final transforms (server.rs:386-498)
+//
+// Every word is a canonical residue; products are Montgomery with R = 2^32 as in Prime32.
+#include <cuda_runtime.h>
+
+#include "ig_arith.cuh"
+#include "ig_sm.cuh"
+
+namespace igsmk {
+using namespace igsm;
+
+// ------------------------------------------------------------------------------------
+// Ntt32 in shared memory, radix-4 (one 4-word unit per thread, N/4 threads). The stage
+// schedule and twiddle indices are those of arith.rs:169-251: forward Cooley-Tukey over
+// fwd[m + i], inverse Gentleman-Sande over inv[h + i] with the last stage carrying 1/n.
+template <int LOGN>
+__device__ __forceinline__ void fwd32(u32* x, const Ntt32Dev& T, const u32* tw) {
+  constexpr int N = 1 << LOGN, NT = N / 4;
+  static_assert(LOGN & 1, "odd log n: one radix-2 stage then radix-4 pairs");
+  const Prime32 P = T.p;
+  const int tid = threadIdx.x;
+  {
+    constexpr int t = N / 2;
+    const u32 w = tw[1];
+#pragma unroll
+    for (int r = 0; r < 2; r++) {
+      const int b = tid + r * NT;
+      const u32 u = x[b], v = P.mont(x[b + t], w);
+      x[b] = P.add(u, v);
+      x[b + t] = P.sub(u, v);
+    }
+    __syncthreads();
+  }
+#pragma unroll 1
+  for (int s = 1; s < LOGN; s += 2) {
+    const int t = N >> (s + 1), m = 1 << s, h = t >> 1;
+    const int i = tid / h, o = tid - i * h;
+    const int e0 = i * 2 * t + o;
+    const u32 wa = tw[m + i], wb = tw[2 * m + 2 * i], wc = tw[2 * m + 2 * i + 1];
+    u32 a0 = x[e0], a1 = x[e0 + h], a2 = x[e0 + t], a3 = x[e0 + t + h];
+    u32 v = P.mont(a2, wa);
+    a2 = P.sub(a0, v);
+    a0 = P.add(a0, v);
+    v = P.mont(a3, wa);
+    a3 = P.sub(a1, v);
+    a1 = P.add(a1, v);
+    v = P.mont(a1, wb);
+    x[e0] = P.add(a0, v);
+    x[e0 + h] = P.sub(a0, v);
+    v = P.mont(a3, wc);
+    x[e0 + t] = P.add(a2, v);
+    x[e0 + t + h] = P.sub(a2, v);
+    __syncthreads();
+  }
+}
+
+template <int LOGN>
+__device__ __forceinline__ void inv32(u32* x, const Ntt32Dev& T, const u32* itw) {
+  constexpr int N = 1 << LOGN, NT = N / 4;
+  static_assert(LOGN & 1, "odd log n: radix-4 pairs then the fused radix-2 stage");
+  const Prime32 P = T.p;
+  const int tid = threadIdx.x;
+#pragma unroll 1
+  for (int s = 0; s + 1 < LOGN; s += 2) {
+    const int t = 1 << s, m = N >> (s + 1);
+    const int B = tid >> s, o = tid & (t - 1);
+    const int e0 = B * 4 * t + o;
+    const u32 w0 = itw[m + 2 * B], w1 = itw[m + 2 * B + 1], w2 = itw[(m >> 1) + B];
+    u32 a0 = x[e0], a1 = x[e0 + t], a2 = x[e0 + 2 * t], a3 = x[e0 + 3 * t];
+    const u32 d01 = P.mont(a0 + P.m - a1, w0);
+    a0 = P.add(a0, a1);
+    const u32 d23 = P.mont(a2 + P.m - a3, w1);
+    a2 = P.add(a2, a3);
+    x[e0] = P.add(a0, a2);
+    x[e0 + 2 * t] = P.mont(a0 + P.m - a2, w2);
+    x[e0 + t] = P.add(d01, d23);
+    x[e0 + 3 * t] = P.mont(d01 + P.m - d23, w2);
+    __syncthreads();
+  }
+  {
+    constexpr int t = N / 2;
+#pragma unroll
+    for (int r = 0; r < 2; r++) {
+      const int b = tid + r * NT;
+      const u32 u = x[b], v = x[b + t];
+      x[b] = P.mont(u + v, T.n_inv);
+      x[b + t] = P.mont(u + P.m - v, T.last);
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------------------------------
+template <int LOGN>
+__global__ void __launch_bounds__((1 << LOGN) / 4) k_sm_ntt_rows(SmDev c, int which, const u32* in, u32* out,
+                                                                 int to_mont) {
+  constexpr int N = 1 << LOGN, NT = N / 4;
+  __shared__ u32 x[N];
+  __shared__ u32 tw[N];
+  const Ntt32Dev& T = which ? c.lp : c.lq;
+  const u32* row = in + (size_t)blockIdx.x * N;
+  for (int k = threadIdx.x; k < N; k += NT) {
+    x[k] = row[k] % T.p.m;
+    tw[k] = T.fwd[k];
+  }
+  __syncthreads();
+  fwd32<LOGN>(x, T, tw);
+  // to_mont: mont(x, 2^64 mod m) = x 2^32 mod m.
+  const u32 r2 = (u32)((((unsigned __int128)1) << 64) % T.p.m);
+  u32* o = out + (size_t)blockIdx.x * N;
+  for (int k = threadIdx.x; k < N; k += NT) o[k] = to_mont ? T.p.mont(x[k], r2) : x[k];
+}
+
+// values[m][j] for m < n (zero past `rows`), colq[j][m] = the nibble as a residue mod q.
+__global__ void k_sm_columns(SmDev c, const uint8_t* cells, u32 rows, u32 cell_bytes, int8_t* values, u32* colq) {
+  const u32 idx = blockIdx.x * blockDim.x + threadIdx.x;  // over n rows x gamma/2 bytes
+  const u32 half = c.gamma / 2;
+  if (idx >= c.n * half) return;
+  const u32 m = idx / half, byte = idx % half;
+  const uint8_t b = m < rows && byte < cell_bytes ? cells[(size_t)m * cell_bytes + byte] : 0;
+  const int8_t lo = (int8_t)((int8_t)(uint8_t)(b << 4) >> 4);
+  const int8_t hi = (int8_t)((int8_t)b >> 4);
+  values[(size_t)m * c.gamma + 2 * byte] = lo;
+  values[(size_t)m * c.gamma + 2 * byte + 1] = hi;
+  colq[(size_t)(2 * byte) * c.n + m] = c.lq.p.small(lo);
+  colq[(size_t)(2 * byte + 1) * c.n + m] = c.lq.p.small(hi);
+}
+
+// Step 1 per slot t (root w_t = w0^e_t): acc_i[t] = sum_j w_t^(j c_i) H_j[t] with
+// c_i = g^-i = 1 + m_i (2n/gamma), i.e. a length-gamma DFT of u_j = w0^(e_t j) H_j[t] read
+// at (e_t m_i) mod gamma; then S_i[t'] = gamma^-1 acc_i[t] at the slot t' whose image under
+// tau_{g^i} is t, in R-form.
+constexpr int SM_FOLD_TILE = 2048;
+constexpr int SM_FOLD_THREADS = 256;
+
+template <int LOGN>
+__global__ void __launch_bounds__(SM_FOLD_THREADS) k_sm_fold(SmDev c, const u32* H, u32* step1_R, u32 SL) {
+  constexpr int N = 1 << LOGN;
+  constexpr u32 M2N = 2 * N - 1;
+  __shared__ u32 x[SM_FOLD_TILE];
+  __shared__ u32 pw[2 * N];
+  const u32 gamma = c.gamma, tile = SL * gamma, t0 = blockIdx.x * SL;
+  const Prime32 P = c.lq.p;
+  u32 lg = 0;
+  while ((1u << lg) < gamma) lg++;
+  for (int k = threadIdx.x; k < 2 * N; k += SM_FOLD_THREADS) pw[k] = c.pow_root_R[k];
+  __syncthreads();
+  for (u32 idx = threadIdx.x; idx < tile; idx += SM_FOLD_THREADS) {
+    const u32 j = idx / SL, s = idx % SL;
+    const u32 e = c.slot_exp[t0 + s];
+    x[s * gamma + j] = P.mont(H[(size_t)j * N + t0 + s], pw[(e * j) & M2N]);
+  }
+  __syncthreads();
+  for (u32 len = gamma >> 1; len >= 1; len >>= 1) {
+    for (u32 b = threadIdx.x; b < SL * (gamma >> 1); b += SM_FOLD_THREADS) {
+      const u32 s = b / (gamma >> 1), bb = b % (gamma >> 1);
+      const u32 blk = bb / len, j = bb % len;
+      const u32 i0 = s * gamma + blk * 2 * len + j;
+      const u32 u = x[i0], v = x[i0 + len];
+      x[i0] = P.add(u, v);
+      x[i0 + len] = P.mont(P.sub(u, v), pw[(j * (N / len)) & M2N]);
+    }
+    __syncthreads();
+  }
+  for (u32 idx = threadIdx.x; idx < tile; idx += SM_FOLD_THREADS) {
+    const u32 i = idx / SL, s = idx % SL;
+    const u32 e = c.slot_exp[t0 + s];
+    const u32 k = (e * c.m_of_i[i]) & (gamma - 1);
+    const u32 kr = lg ? (__brev(k) >> (32 - lg)) : 0;
+    const u32 tp = c.exp_slot[((c.cpow[i] * e) & M2N) >> 1];
+    step1_R[(size_t)i * N + tp] = P.mont(x[s * gamma + kr], c.inv_gamma_RR);
+  }
+}
+
+// ------------------------------------------------------------------------------------
+// Body fold: thread k < nb sums c_m values[m][k] over the shard's rows (exact in i64).
+__global__ void __launch_bounds__(512) k_sm_body_fold(SmDev c, const SmQueryDev* queries, i64* fold) {
+  const SmQueryDev qd = queries[blockIdx.x];
+  const u32 k = threadIdx.x;
+  if (k >= c.nb) return;
+  const Prime32 P = c.lq.p;
+  i64 acc = 0;
+#pragma unroll 8
+  for (u32 m = 0; m < qd.rows; m++) {
+    const u32 bw = qd.body[m == 0 ? 0 : c.n - m];
+    const i64 cm = m == 0 ? P.centred(bw) : -P.centred(bw);
+    acc += cm * (i64)qd.values[(size_t)m * c.gamma + k];
+  }
+  fold[(size_t)blockIdx.x * c.nb + k] = acc;
+}
+
+// ------------------------------------------------------------------------------------
+// expand_uniform (mod.rs:225-237) on the query seed's stream 0: accept u < floor(2^64/q) q,
+// take u mod q. Word w of the stream is keystream words 2w, 2w+1. A rejection (probability
+// below 2^-35 per word) shifts the rest, and the walk is redone word by word.
+template <int N, int NT>
+__device__ __forceinline__ void sm_expand(const SmQueryDev& qd, u32 q, u32* a, u32* status, u32 qi) {
+  const int tid = threadIdx.x;
+  const u64 zone = (~0ULL / q) * q;
+  bool rejected = false;
+  u32 key[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) key[k] = qd.seed[k];
+  if (tid < N / 8) {
+    u32 blk[16];
+    ig::chacha20_block(key, (u64)tid, 0, blk);
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      const u64 v = (u64)blk[2 * k] | ((u64)blk[2 * k + 1] << 32);
+      if (v >= zone) rejected = true;
+      a[tid * 8 + k] = (u32)(v % q);
+    }
+  }
+  if (__syncthreads_or(rejected)) {
+    if (tid == 0) {
+      u32 blk[16];
+      u64 have = ~0ULL, cand = 0;
+      int filled = 0;
+      const u64 limit = (u64)N + 65536;
+      while (filled < N && cand < limit) {
+        const u64 bi = cand >> 3;
+        if (bi != have) {
+          ig::chacha20_block(key, bi, 0, blk);
+          have = bi;
+        }
+        const int k = (int)(cand & 7);
+        const u64 v = (u64)blk[2 * k] | ((u64)blk[2 * k + 1] << 32);
+        if (v < zone) a[filled++] = (u32)(v % q);
+        cand++;
+      }
+      if (filled < N) {
+        atomicOr(status + qi, 2u);
+        for (; filled < N; filled++) a[filled] = 0;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// p_to_q_centred / q_to_p_centred (mod.rs:334-355).
+__device__ __forceinline__ u32 p_to_q(const SmDev& c, u32 r) {
+  const Prime32 Q = c.lq.p;
+  u32 base = r;
+  for (u32 k = 0; k < c.p_over_q; k++) base = Q.csub(base);
+  return r > (c.lp.p.m >> 1) ? Q.add(base, c.neg_off) : base;
+}
+__device__ __forceinline__ u32 q_to_p(const SmDev& c, u32 x) {
+  return x > (c.lq.p.m >> 1) ? x + (c.lp.p.m - c.lq.p.m) : x;
+}
+
+// One CTA per query. Each link i = gamma-2 .. 0 (server.rs:434-487):
+//   tp = NTT_p(lift(INTT_q(R_{i+1})));  cp = INTT_p(tp . w_p[tau_i]);  rq = NTT_q(lift(cp));
+//   R_i = a[tau_i] S_i + (R_{i+1} w_q[tau_i] - rq) / p;
+//   acc_q += R_{i+1} key_q[tau_i];  acc_p += tp key_p[tau_i].
+template <int LOGN>
+__global__ void __launch_bounds__((1 << LOGN) / 4, 2)
+    k_sm_respond(SmDev c, const SmQueryDev* queries, const i64* fold, u32* mask_out, u32* body_out, u32* status) {
+  constexpr int N = 1 << LOGN, NT = N / 4;
+  constexpr u32 M2N = 2 * N - 1;
+  extern __shared__ __align__(16) u32 smw[];
+  u32* buf = smw;
+  u32* a = smw + N;
+  u32* kq = smw + 2 * N;
+  u32* kp = smw + 3 * N;
+  u32* wq = smw + 4 * N;
+  u32* wp = smw + 5 * N;
+  u32* fq = smw + 6 * N;
+  u32* iq = smw + 7 * N;
+  u32* fp = smw + 8 * N;
+  u32* ip = smw + 9 * N;
+  uint16_t* e_tab = reinterpret_cast<uint16_t*>(smw + 10 * N);
+  uint16_t* s_tab = e_tab + N;
+  const int tid = threadIdx.x;
+  const u32 qi = blockIdx.x;
+  const SmQueryDev qd = queries[qi];
+  const Prime32 PQ = c.lq.p, PP = c.lp.p;
+  for (int k = tid; k < N; k += NT) {
+    kq[k] = qd.seat[k];
+    kp[k] = qd.seat[N + k];
+    wq[k] = qd.seat[2 * N + k];
+    wp[k] = qd.seat[3 * N + k];
+    fq[k] = c.lq.fwd[k];
+    iq[k] = c.lq.inv[k];
+    fp[k] = c.lp.fwd[k];
+    ip[k] = c.lp.inv[k];
+    e_tab[k] = c.slot_exp[k];
+    s_tab[k] = c.exp_slot[k];
+  }
+  sm_expand<N, NT>(qd, PQ.m, a, status, qi);
+  fwd32<LOGN>(a, c.lq, fq);
+
+  u32 cur[4], accq[4], accp[4], et[4];
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const int t = tid + k * NT;
+    et[k] = e_tab[t];
+    const u32 tb = s_tab[((c.gpow[c.gamma - 1] * et[k]) & M2N) >> 1];
+    cur[k] = PQ.mont(a[tb], qd.step1_R[(size_t)(c.gamma - 1) * N + t]);
+    accq[k] = 0;
+    accp[k] = 0;
+  }
+#pragma unroll 1
+  for (int i = (int)c.gamma - 2; i >= 0; i--) {
+    const u32* Srow = qd.step1_R + (size_t)i * N;
+    u32 sv[4], tb[4];
+    const u32 gp = c.gpow[i];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const int t = tid + k * NT;
+      sv[k] = Srow[t];
+      tb[k] = s_tab[((gp * et[k]) & M2N) >> 1];
+      buf[t] = cur[k];
+    }
+    __syncthreads();
+    inv32<LOGN>(buf, c.lq, iq);
+#pragma unroll
+    for (int k = 0; k < 4; k++) buf[tid + k * NT] = q_to_p(c, buf[tid + k * NT]);
+    __syncthreads();
+    fwd32<LOGN>(buf, c.lp, fp);
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const int t = tid + k * NT;
+      const u32 tpv = buf[t];
+      accp[k] = PP.add(accp[k], PP.mont(tpv, kp[tb[k]]));
+      buf[t] = PP.mont(tpv, wp[tb[k]]);
+    }
+    __syncthreads();
+    inv32<LOGN>(buf, c.lp, ip);
+#pragma unroll
+    for (int k = 0; k < 4; k++) buf[tid + k * NT] = p_to_q(c, buf[tid + k * NT]);
+    __syncthreads();
+    fwd32<LOGN>(buf, c.lq, fq);
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const int t = tid + k * NT;
+      const u32 rq = buf[t];
+      const u32 cq = PQ.mont(cur[k], wq[tb[k]]);
+      accq[k] = PQ.add(accq[k], PQ.mont(cur[k], kq[tb[k]]));
+      cur[k] = PQ.add(PQ.mont(a[tb[k]], sv[k]), PQ.mont(PQ.sub(cq, rq), c.p_inv_R));
+    }
+  }
+  // mask = INTT_q(R_0); body = mod_down(INTT_q(acc_q), INTT_p(acc_p)) + fold.
+#pragma unroll
+  for (int k = 0; k < 4; k++) buf[tid + k * NT] = cur[k];
+  __syncthreads();
+  inv32<LOGN>(buf, c.lq, iq);
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const int t = tid + k * NT;
+    mask_out[(size_t)qi * N + t] = buf[t];
+    buf[t] = accq[k];
+  }
+  __syncthreads();
+  inv32<LOGN>(buf, c.lq, iq);
+  u32 xq[4];
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const int t = tid + k * NT;
+    xq[k] = buf[t];
+    buf[t] = accp[k];
+  }
+  __syncthreads();
+  inv32<LOGN>(buf, c.lp, ip);
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const int t = tid + k * NT;
+    if ((u32)t < c.nb) {
+      const u32 down = PQ.mont(PQ.sub(xq[k], p_to_q(c, buf[t])), c.p_inv_R);
+      i64 f = fold[(size_t)qi * c.nb + t] % (i64)PQ.m;
+      if (f < 0) f += PQ.m;
+      body_out[(size_t)qi * c.nb + t] = PQ.add(down, (u32)f);
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------
+cudaError_t ntt_rows(const SmDev& c, int which, const u32* in, u32* out, u32 rows, int to_mont, cudaStream_t s) {
+  if (rows == 0) return cudaSuccess;
+  if (c.logn != 11) return cudaErrorInvalidValue;
+  k_sm_ntt_rows<11><<<rows, 512, 0, s>>>(c, which, in, out, to_mont);
+  return cudaGetLastError();
+}
+
+cudaError_t table_columns(const SmDev& c, const uint8_t* cells, u32 rows, u32 cell_bytes, int8_t* values, u32* colq,
+                          cudaStream_t s) {
+  const u32 total = c.n * (c.gamma / 2);
+  k_sm_columns<<<(total + 255) / 256, 256, 0, s>>>(c, cells, rows, cell_bytes, values, colq);
+  return cudaGetLastError();
+}
+
+cudaError_t table_fold(const SmDev& c, const u32* H, u32* step1_R, cudaStream_t s) {
+  if (c.logn != 11 || c.gamma == 0 || c.gamma > (u32)SM_FOLD_TILE) return cudaErrorInvalidValue;
+  u32 SL = SM_FOLD_TILE / c.gamma;
+  if (SL > c.n) SL = c.n;
+  k_sm_fold<11><<<c.n / SL, SM_FOLD_THREADS, 0, s>>>(c, H, step1_R, SL);
+  return cudaGetLastError();
+}
+
+cudaError_t body_fold(const SmDev& c, const SmQueryDev* queries, u32 nq, i64* fold, cudaStream_t s) {
+  if (nq == 0) return cudaSuccess;
+  if (c.nb > 512) return cudaErrorInvalidValue;
+  k_sm_body_fold<<<nq, 512, 0, s>>>(c, queries, fold);
+  return cudaGetLastError();
+}
+
+cudaError_t respond(const SmDev& c, const SmQueryDev* queries, u32 nq, const i64* fold, u32* mask_out, u32* body_out,
+                    u32* status, cudaStream_t s) {
+  if (nq == 0) return cudaSuccess;
+  if (c.logn != 11) return cudaErrorInvalidValue;
+  const size_t smem = (10 * (size_t)c.n) * 4 + 2 * (size_t)c.n * 2;
+  cudaError_t e = cudaFuncSetAttribute(k_sm_respond<11>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k_sm_respond<11><<<nq, 512, smem, s>>>(c, queries, fold, mask_out, body_out, status);
+  return cudaGetLastError();
+}
+
+}  // namespace igsmk
