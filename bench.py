@@ -301,6 +301,122 @@ def run_gb300(args, rank, world):
     }
 
 
+# ------------------------------------------------------------------------------------
+# special_modulus workload (configs[2]): ring2048_cell256, 2^22 cells of 256 bytes
+# (2048 shards, 1 GiB), a ShardTable per shard, 8 seated keys, batches of 256 uniform rows.
+SM_METRIC = "special_modulus respond queries/s (batch 256, 2^22 x 256 B cells, 8 seated keys)"
+SM_CONFIG = {"workload": "special_modulus ring2048_cell256: 2^22 cells x 256 B (2048 shards), ShardTable per "
+                         "shard, 8 seated keys, batch 256 uniform rows",
+             "ring_dim": 2048, "gamma": 512, "cells": 1 << 22, "shards": 2048, "batch": 256, "keys": 8,
+             "l2": "inputs larger than L2: each step reads 256 random shards' tables (5 MiB each)"}
+
+
+def sm_cpu_sample(steps, warmup, queries_per_step=4, seed=12):
+    from oracle import oracle as O
+
+    O.build()
+    rng = np.random.default_rng(seed)
+    server = O.SmServer()
+    cells = np.zeros((2048, 256), dtype=np.uint8)
+    cells[:, :246] = rng.integers(0, 256, (2048, 246), dtype=np.uint8)
+    table = server.table(cells.tobytes())
+    client = O.SmClient(rng.bytes(32))
+    seat = server.seat(client.key())
+    times = []
+    for step in range(warmup + steps):
+        qs = [client.query(int(rng.integers(0, 2048))) for _ in range(queries_per_step)]
+        t0 = time.perf_counter()
+        for seed_b, body in qs:
+            server.respond(table, seat, seed_b, body)
+        if step >= warmup:
+            times.append(time.perf_counter() - t0)
+    return {"value": queries_per_step * len(times) / sum(times), "unit": "queries/s", "cores": 1, "kind": "port",
+            "sample": f"{queries_per_step} queries per step, {steps} steps, one shard table (oracle, one thread as "
+                      "the reference's respond_impl)"}
+
+
+def run_sm(args, rank, world):
+    import torch
+
+    from __graft_entry__ import _package
+    pkg = _package()
+    sm = pkg.special_modulus
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    ctx = pkg.Context(local)
+    rng = np.random.default_rng(2 + rank)
+    server = sm.Server(ctx=ctx)
+    shards = args.shards if args.shards != NUM_SHARDS else 2048
+    t_setup = time.perf_counter()
+    tables = []
+    for s in range(shards):
+        cells = np.zeros((2048, 256), dtype=np.uint8)
+        cells[:, :246] = rng.integers(0, 256, (2048, 246), dtype=np.uint8)
+        tables.append(server.table(cells.tobytes()))
+    seats = []
+    for k in range(8):
+        key = sm.PackingKey(rng.bytes(32), rng.integers(0, 536_813_569, 2048, dtype=np.uint32),
+                            rng.integers(0, 2_147_389_441, 2048, dtype=np.uint32))
+        seats.append(server.seat(key))
+    setup_s = time.perf_counter() - t_setup
+    B = 256
+    total = args.warmup + args.steps
+    tsel = [np.array([tables[i] for i in rng.integers(0, shards, B)], dtype=np.uint64) for _ in range(total)]
+    ssel = [np.array([seats[i] for i in rng.integers(0, 8, B)], dtype=np.uint64) for _ in range(total)]
+    seeds_h = rng.integers(0, 256, (total, B, 32), dtype=np.uint8)
+    bodies_h = rng.integers(0, 536_813_569, (total, B, 2048), dtype=np.uint32)
+    d_seeds = torch.from_numpy(seeds_h).cuda()
+    d_bodies = torch.from_numpy(bodies_h.view(np.int32)).cuda()
+    d_mask = torch.empty((B, 2048), dtype=torch.int32, device="cuda")
+    d_body = torch.empty((B, 492), dtype=torch.int32, device="cuda")
+    d_status = torch.zeros(B, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    lib = ctx._lib
+
+    def step(i):
+        ctx.check(lib.ig_sm_respond_batch_device(ctx.h, server.h, B, tsel[i].ctypes.data, ssel[i].ctypes.data,
+                                                  d_seeds[i].data_ptr(), d_bodies[i].data_ptr(), d_mask.data_ptr(),
+                                                  d_body.data_ptr(), d_status.data_ptr()))
+
+    for i in range(args.warmup):
+        step(i)
+    torch.cuda.synchronize()
+    launches0 = ctx.launch_count
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier(world)
+    with ClockSampler(local) as clk:
+        with torch.cuda.stream(stream):
+            ev0.record(stream)
+            for i in range(args.warmup, total):
+                step(i)
+            ev1.record(stream)
+        torch.cuda.synchronize()
+    barrier(world)
+    if int(d_status.abs().sum().item()) != 0:
+        raise RuntimeError("a special-modulus batch reported a device status")
+    ms = max_over_ranks(ev0.elapsed_time(ev1), world)
+    value = world * B * args.steps / (ms / 1e3)
+    qobjs = [[sm.Query(seeds_h[i, k].tobytes(), bodies_h[i, k]) for k in range(B)] for i in range(total)]
+    for i in range(args.warmup):
+        server.respond_batch(list(tsel[i]), list(ssel[i]), qobjs[i])
+    t0 = time.perf_counter()
+    for i in range(args.warmup, total):
+        server.respond_batch(list(tsel[i]), list(ssel[i]), qobjs[i])
+    e2e = world * B * args.steps / max_over_ranks(time.perf_counter() - t0, world)
+    return {
+        "metric": SM_METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32 (exact mod q and p)",
+        "data": "synthetic: uniform record bytes, uniform key and query words",
+        "config": dict(SM_CONFIG, shards=shards),
+        "db_gbs": value * 2048 * 256 / 1e9,
+        "e2e": {"value": e2e, "unit": "queries/s", "h2d_bytes_per_step": B * (32 + 2048 * 4),
+                "d2h_bytes_per_step": B * (2048 + 492) * 4},
+        "gpu_launches": int(ctx.launch_count - launches0), "setup_s": setup_s, "clocks": clk.summary(),
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -308,6 +424,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--config", type=int, default=2, choices=[2, 3],
+                    help="2: served InspiRING batch (the headline); 3: special_modulus batch")
     ap.add_argument("--shards", type=int, default=NUM_SHARDS,
                     help="shards in the database (smaller values only for profiling captures)")
     args = ap.parse_args()
@@ -323,6 +441,13 @@ def main():
                 "impl": "reference", "cpu_baseline": cb,
                 "e2e": {"value": cb["value"], "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
+        return
+    if args.config == 3:
+        line = run_sm(args, rank, world)
+        if rank == 0:
+            if not args.no_cpu_baseline:
+                line["cpu_baseline"] = sm_cpu_sample(steps=3, warmup=1)
+            print(json.dumps(line))
         return
     line = run_gb300(args, rank, world)
     if rank == 0:
