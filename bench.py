@@ -173,6 +173,65 @@ def barrier(world):
 
 
 # ------------------------------------------------------------------------------------
+def serve_leg(pkg, ctx, crs, db, store, handle, queries, ms, slots=2, max_batch=BATCH):
+    """The continuous-batching loop (ig_serve_*) under two arrival patterns, with host
+    buffers: a closed loop keeping 4 x slots x max_batch requests outstanding (saturation
+    throughput), and Poisson arrivals at half that rate from a submitting thread (latency
+    under load). Latency runs from submit to result in the caller's buffer."""
+    import threading
+
+    out = {"slots": slots, "max_batch": max_batch, "requests": len(queries)}
+    with pkg.ServingLoop(ctx, slots=slots, max_batch=max_batch) as loop:
+        for q in queries[:2 * max_batch]:  # warm-up
+            loop.wait(loop.submit(crs, db, q, store, handle, mod_switch_target=ms))
+        loop.stats(reset=True)
+        window = 4 * slots * max_batch  # outstanding requests, below the loop's admission limit
+        t0 = time.perf_counter()
+        pending = []
+        for q in queries:
+            if len(pending) == window:
+                loop.wait(pending.pop(0))
+            pending.append(loop.submit(crs, db, q, store, handle, mod_switch_target=ms))
+        for t in pending:
+            loop.wait(t)
+        sat_s = time.perf_counter() - t0
+        st = loop.stats(reset=True)
+        sat_qps = len(queries) / sat_s
+        out["saturation"] = {"queries_per_s": sat_qps, "p50_ms": st["p50_us"] / 1e3, "p99_ms": st["p99_us"] / 1e3,
+                             "mean_batch": st["mean_batch"]}
+        rate = 0.5 * sat_qps
+        gaps = np.random.default_rng(7).exponential(1.0 / rate, size=len(queries))
+        tickets = [None] * len(queries)
+        dropped = [0]
+
+        def submitter():
+            t_next = time.perf_counter()
+            for i, q in enumerate(queries):
+                t_next += gaps[i]
+                while time.perf_counter() < t_next:
+                    pass
+                try:
+                    tickets[i] = loop.submit(crs, db, q, store, handle, mod_switch_target=ms)
+                except pkg.PirError as e:
+                    if e.code != 8:  # only an admission refusal is an expected outcome
+                        raise
+                    dropped[0] += 1
+
+        th = threading.Thread(target=submitter)
+        t0 = time.perf_counter()
+        th.start()
+        th.join()
+        for t in tickets:
+            if t is not None:
+                loop.wait(t)
+        open_s = time.perf_counter() - t0
+        st = loop.stats(reset=True)
+        out["poisson_half_load"] = {"offered_per_s": rate, "queries_per_s": len(queries) / open_s,
+                                    "p50_ms": st["p50_us"] / 1e3, "p99_ms": st["p99_us"] / 1e3,
+                                    "mean_batch": st["mean_batch"], "admission_refused": dropped[0]}
+    return out
+
+
 def run_gb300(args, rank, world):
     import torch
 
@@ -262,6 +321,8 @@ def run_gb300(args, rank, world):
     e2e_value = world * BATCH * args.steps / e2e_s
     assert len(out) == BATCH
 
+    serving = serve_leg(pkg, ctx, crs, db, store, handle, [q for qs in e2e_queries for q in qs], MS_TARGET)
+
     scan_ms, scan_n = prof["scan"]
     resp_ms, resp_n = prof["respond"]
     scan_avg = scan_ms / max(scan_n, 1)
@@ -298,6 +359,7 @@ def run_gb300(args, rank, world):
         "gpu_launches": int(launches),
         "setup_s": setup_s,
         "clocks": clk.summary(),
+        "serving": serving,
     }
 
 

@@ -36,7 +36,8 @@ enum ig_status {
   IG_ERR_UNSUPPORTED = 7,   /* parameter set outside what the GPU path serves */
   IG_ERR_NOMEM = 8,         /* device allocation failed (admission refused) */
   IG_ERR_DEVICE = 9,        /* a kernel reported an internal status */
-  IG_ERR_EXHAUSTED = 10     /* handle space exhausted (session.rs:722-737) */
+  IG_ERR_EXHAUSTED = 10,    /* handle space exhausted (session.rs:722-737) */
+  IG_ERR_PENDING = 11       /* serving ticket not finished within the wait's timeout */
 };
 
 typedef struct ig_ctx ig_ctx;
@@ -196,6 +197,38 @@ int ig_sm_respond_batch_device(ig_ctx* ctx, uint64_t server, uint32_t count, con
  * words), each packed at q's bit width; 9,208 bytes at the served set. */
 int ig_sm_response_encode(const uint32_t* mask, uint32_t n, const uint32_t* body, uint32_t nb, uint64_t q,
                           uint8_t* out, size_t cap, size_t* len_out);
+
+/* ---- serving loop (continuous batching) ----------------------------------------------------
+ * No single counterpart in the reference, whose server answers one respond_seeded_batch call
+ * at a time (respond.rs:1189-1202); this loop batches individually arriving queries instead.
+ * Each request is one seeded query under a seat registered in `store`, on a shard whose
+ * packing store was built. A dispatcher thread forms batches of waiting requests that share a
+ * parameter set and mod-switch target (databases, shards and seats may differ) and launches
+ * each on one of `slots` streams, so batches overlap on the device; device and pinned buffers
+ * for every slot are allocated at create time, and create refuses (IG_ERR_NOMEM) when they
+ * exceed hbm_budget_bytes (0 = no budget). A request's result equals ig_respond_seeded_batch's
+ * for the same query. Databases, shards and seats named by a request must stay alive until
+ * the request's ticket is finished.
+ *
+ * ig_serve_submit copies seed (32 B) and b (ring_dim words) and returns a ticket; a_out and
+ * b_out (ring_dim words each) are written before the ticket finishes. Admission is refused
+ * (IG_ERR_NOMEM) while 8 x slots x max_batch requests are waiting.
+ * ig_serve_wait blocks up to timeout_ms (< 0: no limit) and returns the request's status
+ * (IG_ERR_PENDING on timeout, the ticket stays valid); err receives the refusal message.
+ * ig_serve_stats reports counts and latency percentiles from submit to result; reset != 0
+ * clears them. ig_serve_destroy finishes every submitted request, then frees the slots. */
+typedef struct ig_serve ig_serve;
+typedef struct ig_serve_stats_t {
+  uint64_t served, refused, batches, waiting, device_bytes;
+  double mean_batch, p50_us, p99_us, max_us;
+} ig_serve_stats_t;
+int ig_serve_create(ig_ctx* ctx, uint32_t slots, uint32_t max_batch, uint64_t hbm_budget_bytes, ig_serve** out);
+int ig_serve_submit(ig_serve* s, uint64_t db, uint64_t store, uint64_t handle, uint32_t shard_id,
+                    const uint8_t* seed, const uint64_t* b, uint32_t ring_dim, uint64_t mod_switch_target,
+                    uint64_t* a_out, uint64_t* b_out, uint64_t* ticket_out);
+int ig_serve_wait(ig_serve* s, uint64_t ticket, int64_t timeout_ms, uint64_t* latency_ns, char* err, size_t err_len);
+int ig_serve_stats(ig_serve* s, ig_serve_stats_t* out, int reset);
+int ig_serve_destroy(ig_serve* s);
 
 /* ---- wire ------------------------------------------------------------------------------
  * ServerResponse bincode bytes of a packed response (respond.rs:111-176, tight codec

@@ -11,6 +11,8 @@ reference crate's public API for this path (raven-inspire, src/lib.rs:37-48):
     mod_switch_response_checked(params, response, target)  fused: mod_switch_target= on the
                                                        respond calls (mod_switch.rs:178-186)
     ServerResponse.to_binary()                         respond.rs:387-390
+    ServingLoop.submit/wait/stats                      continuous batching of single queries
+                                                       (no single counterpart in the reference)
 
 Every refusal raises PirError with the reference's message. Compute runs only in the
 CUDA library: when it cannot be loaded (no build, no GPU) the calls raise, and there is
@@ -29,7 +31,8 @@ __all__ = [
     "ServerSessionStore", "ServerSessionHandle", "ClientPackingKeys", "SeededBatchQuery", "SeededClientQuery",
     "SeededQueryBatch", "PackingKeySource", "ServerResponse", "respond_seeded_inspiring", "respond_seeded_batch", "respond_inspiring",
     "check_mod_switch_noise_budget", "ClientQuery", "Context", "DEFAULT_Q",
-    "MOD_SWITCH_TARGET_36BIT", "MOD_SWITCH_TARGET_45BIT", "library_path", "special_modulus",
+    "MOD_SWITCH_TARGET_36BIT", "MOD_SWITCH_TARGET_45BIT", "library_path", "special_modulus", "ServingLoop",
+    "ServeTicket",
 ]
 
 DEFAULT_Q = 1152921504606830593
@@ -38,6 +41,7 @@ MOD_SWITCH_TARGET_45BIT = 35_184_372_060_161
 
 IG_OK = 0
 IG_ERR_STORE_REFUSED = 5
+IG_ERR_PENDING = 11
 
 
 class PirError(Exception):
@@ -53,6 +57,12 @@ _lib = None
 
 def library_path():
     return _build.LIB
+
+
+class ServeStats(ctypes.Structure):
+    _fields_ = [("served", ctypes.c_uint64), ("refused", ctypes.c_uint64), ("batches", ctypes.c_uint64),
+                ("waiting", ctypes.c_uint64), ("device_bytes", ctypes.c_uint64), ("mean_batch", ctypes.c_double),
+                ("p50_us", ctypes.c_double), ("p99_us", ctypes.c_double), ("max_us", ctypes.c_double)]
 
 
 def _load():
@@ -106,6 +116,11 @@ def _load():
         "ig_sm_respond_batch_device": (I, [P, U64, U32, P, P, P, P, P, P, P]),
         "ig_sm_response_encode": (I, [P, U32, P, U32, U64, P, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
         "ig_debug_store_sums": (I, [P, U64, U32, P]),
+        "ig_serve_create": (I, [P, U32, U32, U64, ctypes.POINTER(P)]),
+        "ig_serve_submit": (I, [P, U64, U64, U64, U32, P, P, U32, U64, P, P, pu64]),
+        "ig_serve_wait": (I, [P, U64, ctypes.c_int64, pu64, ctypes.c_char_p, ctypes.c_size_t]),
+        "ig_serve_stats": (I, [P, ctypes.POINTER(ServeStats), I]),
+        "ig_serve_destroy": (I, [P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -527,6 +542,96 @@ def respond_seeded_inspiring(crs: ServerCrs, encoded_db: EncodedDatabase, query:
         raise PirError("InspiRING client packing keys missing from query (neither inlined nor session_handle set)")
     src = PackingKeySource.Inline(keys) if keys is not None else PackingKeySource.Registered(handle)
     return _batch(crs, encoded_db, [query], src, session_store, mod_switch_target)[0]
+
+
+class ServeTicket:
+    """One submitted request of a ServingLoop; owns the buffers its result lands in."""
+
+    def __init__(self, loop, ticket, a_out, b_out, modulus, packed):
+        self.loop, self.ticket = loop, ticket
+        self._a, self._b, self._modulus, self._packed = a_out, b_out, modulus, packed
+        self.latency_us = None
+        self.done = False
+
+
+class ServingLoop:
+    """Continuous batching of individually arriving seeded queries (the C ABI's ig_serve_*).
+
+    The reference's server answers one respond_seeded_batch call at a time
+    (respond.rs:1189-1202); here requests are submitted one by one, a dispatcher thread
+    groups waiting requests that share a parameter set and mod-switch target into batches,
+    and `slots` batches run concurrently on their own streams. Every slot's buffers are
+    allocated up front; `hbm_budget_bytes` (0 = none) refuses a loop that would exceed it.
+    A request's response equals respond_seeded_batch's for the same query."""
+
+    def __init__(self, ctx: Context = None, slots=2, max_batch=64, hbm_budget_bytes=0):
+        self.ctx = ctx or Context.default()
+        self.h = None
+        self._live = {}  # tickets whose result buffers the loop may still write
+        h = ctypes.c_void_p()
+        self.ctx.check(self.ctx._lib.ig_serve_create(self.ctx.h, slots, max_batch, hbm_budget_bytes,
+                                                     ctypes.byref(h)))
+        self.h = h
+
+    def submit(self, crs: ServerCrs, encoded_db: EncodedDatabase, query: SeededBatchQuery,
+               session_store: ServerSessionStore, handle, mod_switch_target: int = 0) -> ServeTicket:
+        if self.h is None:
+            raise PirError("serving loop is closed")
+        n = crs.params.ring_dim
+        if query.seed is None or len(query.seed) != 32:
+            raise PirError("the serving loop takes seeded queries (32-byte seed)")
+        b = _u64(query.b, (n,))
+        seed = np.frombuffer(bytes(query.seed), dtype=np.uint8).copy()
+        ms = int(mod_switch_target or 0)
+        if ms:
+            check_mod_switch_noise_budget(crs.params, ms)
+        a_out = np.zeros(n, dtype=np.uint64)
+        b_out = np.zeros(n, dtype=np.uint64)
+        t = ctypes.c_uint64()
+        self.ctx.check(self.ctx._lib.ig_serve_submit(self.h, encoded_db.h, session_store.h, int(handle),
+                                                     int(query.shard_id), _ptr(seed), _ptr(b), n, ms, _ptr(a_out),
+                                                     _ptr(b_out), ctypes.byref(t)))
+        ticket = ServeTicket(self, t.value, a_out, b_out, ms or crs.params.q, crs.inspiring_num_columns)
+        self._live[t.value] = ticket
+        return ticket
+
+    def wait(self, ticket: ServeTicket, timeout_ms: int = -1) -> ServerResponse:
+        """Blocks until the request finishes; raises PirError with the refusal otherwise."""
+        if self.h is None:
+            raise PirError("serving loop is closed")
+        lat = ctypes.c_uint64()
+        err = ctypes.create_string_buffer(1024)
+        rc = self.ctx._lib.ig_serve_wait(self.h, ticket.ticket, int(timeout_ms), ctypes.byref(lat), err, len(err))
+        if rc != IG_ERR_PENDING:
+            ticket.done = True
+            self._live.pop(ticket.ticket, None)
+        if rc != 0:
+            raise PirError(err.value.decode(errors="replace"), rc)
+        ticket.latency_us = lat.value / 1e3
+        return ServerResponse(ticket._a, ticket._b, ticket._packed, ticket._modulus)
+
+    def stats(self, reset=False) -> dict:
+        st = ServeStats()
+        self.ctx.check(self.ctx._lib.ig_serve_stats(self.h, ctypes.byref(st), 1 if reset else 0))
+        return {k: getattr(st, k) for k, _ in ServeStats._fields_}
+
+    def close(self):
+        if self.h is not None:
+            self.ctx._lib.ig_serve_destroy(self.h)  # finishes every submitted request first
+            self.h = None
+            self._live.clear()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class _SpecialModulus:

@@ -10,7 +10,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libinspire_gb300.so")
-SOURCES = ["ig_kernels.cu", "ig_runtime.cu", "ig_sm_kernels.cu", "ig_sm_runtime.cu"]
+SOURCES = ["ig_kernels.cu", "ig_runtime.cu", "ig_sm_kernels.cu", "ig_sm_runtime.cu", "ig_serve.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
 
@@ -51,7 +51,7 @@ def build(force=False, verbose=False):
     with concurrent.futures.ThreadPoolExecutor(len(SOURCES)) as ex:
         objs = list(ex.map(compile_one, SOURCES))
     tmp = LIB + ".tmp"
-    cmd = [exe, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
+    cmd = [exe, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

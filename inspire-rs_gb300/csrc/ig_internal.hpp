@@ -3,7 +3,10 @@
 #include <cuda_runtime.h>
 
 #include <cstddef>
+#include <cstdint>
 #include <mutex>
+
+#include "ig_kernels.cuh"
 
 struct ig_ctx;
 
@@ -20,4 +23,20 @@ void add_launches(ig_ctx* c, unsigned n);
 // One extension slot per context for the special_modulus objects, freed at destroy.
 void*& sm_slot(ig_ctx* c);
 void set_sm_destructor(ig_ctx* c, void (*fn)(ig_ctx*, void*));
+
+// One served request resolved against the context's objects (takes the context lock):
+// the parameter set's device constants, the shard's device pointers, the seat's device
+// words, and the shard's store state. Returns an IG_* status; on refusal `err` holds the
+// reference's message.
+struct RequestView {
+  ig::CrsDev crs;
+  ig::ShardDev shard;
+  const uint64_t* seat;
+  uint64_t crs_handle;
+  uint64_t p;
+  bool has_store;
+  char err[512];
+};
+int resolve_request(ig_ctx* c, uint64_t db, uint64_t store, uint64_t handle, uint32_t shard, RequestView* out);
+int pair_threshold(ig_ctx* c);
 }  // namespace igint

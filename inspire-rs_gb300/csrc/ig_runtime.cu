@@ -147,6 +147,7 @@ struct ig_ctx {
   cudaStream_t stream = nullptr;
   std::mutex mu;
   std::string err;
+  mutable std::mutex err_mu;  // err is written by the serving threads too
   std::unordered_map<u64, CrsObj> crs;
   std::unordered_map<u64, DbObj> dbs;
   std::unordered_map<u64, StoreObj> stores;
@@ -160,7 +161,7 @@ struct ig_ctx {
   int profile = 0;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_pool;
   std::vector<std::pair<int, size_t>> ev_used;  // (region, pool index)
-  u64 launches = 0;
+  std::atomic<u64> launches{0};
   // Pinned staging ring for host->device copies issued on the stream: slot k is reused
   // only after the copy that last read it has completed.
   struct Staging {
@@ -206,7 +207,10 @@ int fail(ig_ctx* c, int code, const char* fmt, ...) {
   va_start(ap, fmt);
   vsnprintf(buf, sizeof buf, fmt, ap);
   va_end(ap);
-  if (c) c->err = buf;
+  if (c) {
+    std::lock_guard<std::mutex> lk(c->err_mu);
+    c->err = buf;
+  }
   return code;
 }
 
@@ -388,7 +392,10 @@ int fail(ig_ctx* c, int code, const char* fmt, ...) {
   va_start(ap, fmt);
   vsnprintf(buf, sizeof buf, fmt, ap);
   va_end(ap);
-  if (c) c->err = buf;
+  if (c) {
+    std::lock_guard<std::mutex> lk(c->err_mu);
+    c->err = buf;
+  }
   return code;
 }
 cudaStream_t stream(ig_ctx* c) { return c->stream; }
@@ -400,6 +407,7 @@ int scratch(ig_ctx* c, const char* name, size_t bytes, void** out) { return ::sc
 int stage_h2d(ig_ctx* c, void* dst, const void* src, size_t bytes) { return ::stage_h2d(c, dst, src, bytes); }
 void add_launches(ig_ctx* c, unsigned n) { c->launches += n; }
 void*& sm_slot(ig_ctx* c) { return c->sm; }
+int pair_threshold(ig_ctx* c) { return (int)c->pair_threshold; }
 void set_sm_destructor(ig_ctx* c, void (*fn)(ig_ctx*, void*)) { c->sm_destroy = fn; }
 }  // namespace igint
 
@@ -463,6 +471,7 @@ void ig_ctx_destroy(ig_ctx* c) {
 
 int ig_last_error(const ig_ctx* c, char* buf, size_t len) {
   if (!c || !buf || len == 0) return IG_ERR_ARG;
+  std::lock_guard<std::mutex> lk(c->err_mu);
   snprintf(buf, len, "%s", c->err.c_str());
   return IG_OK;
 }
@@ -1145,7 +1154,7 @@ int ig_profile_read(ig_ctx* c, double* ms, uint64_t* counts, int regions, int re
   return IG_OK;
 }
 
-uint64_t ig_launch_count(const ig_ctx* c) { return c ? c->launches : 0; }
+uint64_t ig_launch_count(const ig_ctx* c) { return c ? c->launches.load() : 0; }
 
 int ig_debug_force_serial_expand(ig_ctx* c, int on) {
   if (!c) return IG_ERR_ARG;
@@ -1164,6 +1173,45 @@ int ig_debug_store_sums(ig_ctx* c, uint64_t dbh, uint32_t s, uint64_t* out) {
   IG_CUDA(c, cudaMemcpy(out, db->shards[s].sums, (size_t)o->gamma * o->n * 8, cudaMemcpyDeviceToHost));
   return IG_OK;
 }
+
+}  // extern "C"
+
+namespace igint {
+static int resolve_request_locked(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_t handle, uint32_t shard,
+                                  RequestView* out) {
+  DbObj* db = get_db(c, dbh);
+  if (!db) return fail(c, IG_ERR_HANDLE, "unknown database handle %llu", (unsigned long long)dbh);
+  CrsObj& o = *get_crs(c, db->crs);
+  const u64* seat;
+  int rc = resolve_seat(c, o, st, handle, nullptr, 0, 0, &seat);
+  if (rc) return rc;
+  if (shard >= db->num_shards)
+    return fail(c, IG_ERR_ARG, "shard %u not found at dense position %u; encoded database has %u shards", shard,
+                shard, db->num_shards);
+  const ShardSlot& sl = db->shards[shard];
+  if (!sl.cols) return fail(c, IG_ERR_ARG, "shard %u holds no columns", shard);
+  out->crs = o.dev;
+  out->shard = ShardDev{sl.cols, sl.sums, sl.tag_key, sl.tags};
+  out->seat = seat;
+  out->crs_handle = db->crs;
+  out->p = o.p;
+  out->has_store = sl.sums != nullptr;
+  return IG_OK;
+}
+
+int resolve_request(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_t handle, uint32_t shard, RequestView* out) {
+  std::lock_guard<std::mutex> lk(c->mu);
+  const int rc = resolve_request_locked(c, dbh, st, handle, shard, out);
+  out->err[0] = 0;
+  if (rc) {
+    std::lock_guard<std::mutex> elk(c->err_mu);
+    snprintf(out->err, sizeof out->err, "%s", c->err.c_str());
+  }
+  return rc;
+}
+}  // namespace igint
+
+extern "C" {
 
 // ---- allocation-free respond --------------------------------------------------------------
 // Some embedders cannot let a library allocate device memory on a request path: servers
