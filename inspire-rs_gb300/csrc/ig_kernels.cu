@@ -526,17 +526,121 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
 }
 
 // ------------------------------------------------------------------------------------
+// Split transforms for the two-CTA kernel. The inverse (Gentleman-Sande, from t = 1
+// upward) combines indices within blocks of growing size: its stages 0 .. logn-2 stay
+// inside each half of N/2 words, and only the last stage (t = N/2) mixes the halves. The
+// forward (Cooley-Tukey, from t = N/2 downward) mixes the halves in its first stage only.
+// So each CTA of a pair runs the local stages on the half of the slots it owns, and the
+// two cross stages run once per link, fused with the digit split. Unit and butterfly
+// numbering is the full transform's, so the twiddles are the full transform's.
+
+// Inverse radix-4 pass (stages s, s+1) over this CTA's half xh (N/2 words, local index);
+// threads below N/8 carry one unit each. Ends with a barrier.
+template <int LOGN>
+__device__ __forceinline__ void inv_half_r4(u64* xh, int s, int rank, const u64* tw, const u64* twp) {
+  constexpr int N = 1 << LOGN, HU = N / 8;
+  const int tid = threadIdx.x;
+  if (tid < HU) {
+    const int u = rank * HU + tid;
+    const int t = 1 << s, m = N >> (s + 1);
+    const int B = u >> s, o = u & (t - 1);
+    const int e0 = B * 4 * t + o - rank * (N / 2);
+    u64 w0, w0p, w1, w1p, w2, w2p;
+    inv_twiddle(tw, twp, m + 2 * B, w0, w0p);
+    inv_twiddle(tw, twp, m + 2 * B + 1, w1, w1p);
+    inv_twiddle(tw, twp, (m >> 1) + B, w2, w2p);
+    u64 a0 = xh[e0], a1 = xh[e0 + t], a2 = xh[e0 + 2 * t], a3 = xh[e0 + 3 * t];
+    bf_inv(a0, a1, w0, w0p);
+    bf_inv(a2, a3, w1, w1p);
+    bf_inv(a0, a2, w2, w2p);
+    bf_inv(a1, a3, w2, w2p);
+    xh[e0] = a0;
+    xh[e0 + t] = a1;
+    xh[e0 + 2 * t] = a2;
+    xh[e0 + 3 * t] = a3;
+  }
+  __syncthreads();
+}
+
+// Inverse radix-2 stage s over this CTA's half (even logn: the last local stage); one
+// butterfly per thread. Ends with a barrier.
+template <int LOGN>
+__device__ __forceinline__ void inv_half_r2(u64* xh, int s, int rank, const u64* tw, const u64* twp) {
+  constexpr int N = 1 << LOGN;
+  const int v = rank * (N / 4) + (int)threadIdx.x;
+  const int t = 1 << s, m = N >> (s + 1);
+  const int B = v >> s, o = v & (t - 1);
+  const int e = B * 2 * t + o - rank * (N / 2);
+  u64 w, wp;
+  inv_twiddle(tw, twp, m + B, w, wp);
+  u64 a = xh[e], b = xh[e + t];
+  bf_inv(a, b, w, wp);
+  xh[e] = a;
+  xh[e + t] = b;
+  __syncthreads();
+}
+
+// Forward radix-4 pass (stages s, s+1; s >= 1) over this CTA's half of two buffers
+// D[0..N/2) and D[N/2..N); one unit per thread. Ends with a barrier.
+template <int LOGN>
+__device__ __forceinline__ void fwd_half_r4(u64* D, int s, int rank, const u64* tw, const u64* twp) {
+  constexpr int N = 1 << LOGN, HU = N / 8;
+  const int tid = threadIdx.x;
+  u64* x = D + (tid >= HU ? N / 2 : 0);
+  const int u = rank * HU + (tid & (HU - 1));
+  const int lt = LOGN - s - 1;  // log2 t
+  const int t = 1 << lt, m = 1 << s, h = t >> 1;
+  const int i = u >> (lt - 1), o = u & (h - 1);
+  const int e0 = i * 2 * t + o - rank * (N / 2);
+  const u64 wa = tw[m + i], wap = twp[m + i];
+  const u64 wb = tw[2 * m + 2 * i], wbp = twp[2 * m + 2 * i];
+  const u64 wc = tw[2 * m + 2 * i + 1], wcp = twp[2 * m + 2 * i + 1];
+  u64 a0 = x[e0], a1 = x[e0 + h], a2 = x[e0 + t], a3 = x[e0 + t + h];
+  bf_fwd(a0, a2, wa, wap);
+  bf_fwd(a1, a3, wa, wap);
+  bf_fwd(a0, a1, wb, wbp);
+  bf_fwd(a2, a3, wc, wcp);
+  x[e0] = a0;
+  x[e0 + h] = a1;
+  x[e0 + t] = a2;
+  x[e0 + t + h] = a3;
+  __syncthreads();
+}
+
+// Forward radix-2 stage s (even logn: s = 1) over this CTA's half of both buffers; one
+// butterfly per buffer per thread. Ends with a barrier.
+template <int LOGN>
+__device__ __forceinline__ void fwd_half_r2(u64* D, int s, int rank, const u64* tw, const u64* twp) {
+  constexpr int N = 1 << LOGN;
+  const int v = rank * (N / 4) + (int)threadIdx.x;
+  const int lt = LOGN - s - 1;
+  const int t = 1 << lt, m = 1 << s;
+  const int i = v >> lt, o = v & (t - 1);
+  const int e = i * 2 * t + o - rank * (N / 2);
+  const u64 w = tw[m + i], wp = twp[m + i];
+#pragma unroll
+  for (int k = 0; k < 2; k++) {
+    u64* x = D + k * (N / 2);
+    u64 a = x[e], b = x[e + t];
+    bf_fwd(a, b, w, wp);
+    x[e] = a;
+    x[e + t] = b;
+  }
+  __syncthreads();
+}
+
+// ------------------------------------------------------------------------------------
 // Two CTAs per query (a thread-block cluster), for batches that leave SMs idle with one
-// CTA each. Both CTAs hold R_{i+1} whole and run the inverse transform; CTA r then
-// transforms gadget digit r only and owns half of the slots for the pointwise link. The
-// peer's digit transform and R's other half cross through distributed shared memory, with
-// two cluster barriers per link:
-//   X (own half of R) written -> barrier -> peer half read into bufA -> INTT -> digit r ->
-//   NTT -> barrier -> peer's D read at own slots -> pointwise.
-// X is rewritten only after the second barrier of the previous link, when the peer has
-// read it; bufB (this CTA's D) only after the first barrier of the next link, when the
-// peer has consumed it. With the exact gadget the third digit's transform comes from the
-// other two: D_2 = base^-2 (R_{i+1} - D_0 - base D_1) (inspiring2.rs:1094-1161).
+// CTA each. CTA r owns slots [r N/2, (r+1) N/2) of every NTT-domain vector. Per link:
+//   own half of R_{i+1} -> local inverse stages -> cluster barrier -> cross stage over
+//   (own half, peer's half read through distributed shared memory), n^-1, digit split and
+//   the forward cross stage, keeping this CTA's half of digits 0 and 1 -> local forward
+//   stages -> pointwise at own slots.
+// One cluster barrier per link: the exchange buffer X alternates between two halves by
+// link parity, so a CTA rewrites the half its peer read at link i only at link i-2, after
+// both passed the barrier of link i-1. With the exact gadget the third digit's transform
+// comes from the other two: D_2 = base^-2 (R_{i+1} - D_0 - base D_1)
+// (inspiring2.rs:1094-1161).
 template <int LOGN>
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
     k_respond_pair(CrsDev c, const QueryDev* queries, const ShardDev* shards, const u64* b_fold, u64 ms_target,
@@ -546,10 +650,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
   constexpr u32 M2N = 2 * N - 1;
   constexpr u64 DMASK = (1ULL << 20) - 1;
   extern __shared__ __align__(16) u64 sm[];
-  u64* bufA = sm;
-  u64* bufB = sm + N;
-  u64* X = sm + 2 * N;  // H words
-  u64* a_ntt = X + H;
+  u64* X = sm;      // [2][H] own half of the inverse, by link parity
+  u64* D = sm + N;  // [2][H] own half of the transformed digits 0 and 1; N words at the end
+  u64* a_ntt = D + N;
   u64* tw = a_ntt + N;
   u64* twp = tw + N;
   const u32 rows = c.rows;
@@ -559,16 +662,15 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
   uint16_t* s_tab = e_tab + N;
 
   cg::cluster_group cluster = cg::this_cluster();
-  const u32 rank = cluster.block_rank();
-  const u64* peerX = cluster.map_shared_rank(X, (int)(rank ^ 1));
-  const u64* peerB = cluster.map_shared_rank(bufB, (int)(rank ^ 1));
+  const int rank = (int)cluster.block_rank();
+  const u64* peerX = cluster.map_shared_rank(X, rank ^ 1);
   const int tid = threadIdx.x;
   const u32 qi = blockIdx.x >> 1;
   const QueryDev qd = queries[qi];
   const ShardDev sh = shards[qd.shard];
   const u32 gamma = c.gamma;
   const bool exact = c.approx == 0;
-  const int own = (int)rank * H, other = (int)(rank ^ 1) * H;
+  const int own = rank * H, other = (rank ^ 1) * H;
 
   stage_constants<N, NT>(c, qd.seat_R, tw, twp, Wm, Y, e_tab, s_tab);
   expand_a<N, NT>(qd, a_ntt, status, qi, force_serial);
@@ -591,6 +693,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
       sb[k] = 0;
     }
   }
+  u64 wi, wip;
+  inv_twiddle(tw, twp, 1, wi, wip);
+  const u64 wf = tw[1], wfp = twp[1];
 #pragma unroll 1
   for (int i = (int)gamma - 2; i >= 0; i--) {
     const u64* Srow = sh.sums_R + (size_t)i * N;
@@ -598,45 +703,58 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
 #pragma unroll
     for (int k = 0; k < 2; k++) sv[k] = Srow[own + tid + k * NT];
     const u32 gp = c.gpow[i];
+    const int par = (i & 1) * H;
+    u64* xh = X + par;
 #pragma unroll
-    for (int k = 0; k < 2; k++) {
-      X[tid + k * NT] = cur[k];
-      bufA[own + tid + k * NT] = cur[k];
-    }
-    cluster.sync();
-#pragma unroll
-    for (int k = 0; k < 2; k++) bufA[other + tid + k * NT] = peerX[tid + k * NT];
+    for (int k = 0; k < 2; k++) xh[tid + k * NT] = cur[k];
     __syncthreads();
+    int s = 0;
+#pragma unroll 1
+    for (; s + 1 <= LOGN - 2; s += 2) inv_half_r4<LOGN>(xh, s, rank, tw, twp);
+    if (s == LOGN - 2) inv_half_r2<LOGN>(xh, s, rank, tw, twp);
+    cluster.sync();
     {
-      u64* const bufs[1] = {bufA};
-      ntt_inv_r4<LOGN, NT, 1>(bufs, tw, twp);
-    }
+      // Elements [0, H) of the inverse live in rank 0's X, elements [H, N) in rank 1's.
+      const u64* lo = (rank == 0 ? (const u64*)X : peerX) + par;
+      const u64* hi = (rank == 0 ? peerX : (const u64*)X) + par;
 #pragma unroll
-    for (int k = 0; k < 4; k++) {
-      const int t = tid + k * NT;
-      const u64 r = shoup(bufA[t], c.ninv, c.ninvp);
-      u64 d;
-      if (exact) {
-        d = rank == 0 ? (r & DMASK) : ((r >> 20) & DMASK);
-      } else {
-        const u64 rr = (r + (1ULL << 19)) >> 20;
-        d = rank == 0 ? (rr & DMASK) : (rr >> 20);
+      for (int j = 0; j < 2; j++) {
+        const int b = tid + j * NT;
+        u64 x0 = lo[b], x1 = hi[b];
+        bf_inv(x0, x1, wi, wip);
+        const u64 r0 = shoup(x0, c.ninv, c.ninvp), r1 = shoup(x1, c.ninv, c.ninvp);
+        u64 p0, p1, q0, q1;  // digits 0 and 1 of coefficients b and b + H
+        if (exact) {
+          p0 = r0 & DMASK;
+          p1 = (r0 >> 20) & DMASK;
+          q0 = r1 & DMASK;
+          q1 = (r1 >> 20) & DMASK;
+        } else {
+          const u64 rr0 = (r0 + (1ULL << 19)) >> 20, rr1 = (r1 + (1ULL << 19)) >> 20;
+          p0 = rr0 & DMASK;
+          p1 = rr0 >> 20;
+          q0 = rr1 & DMASK;
+          q1 = rr1 >> 20;
+        }
+        // Forward cross stage: slot b gets p + w q, slot b + H gets p - w q.
+        const u64 t0 = shoup_lazy(q0, wf, wfp), t1 = shoup_lazy(q1, wf, wfp);
+        D[b] = rank == 0 ? p0 + t0 : p0 + 2 * Q - t0;
+        D[H + b] = rank == 0 ? p1 + t1 : p1 + 2 * Q - t1;
       }
-      bufB[t] = d;
     }
     __syncthreads();
-    {
-      u64* const bufs[1] = {bufB};
-      ntt_fwd_r4<LOGN, NT, 1>(bufs, tw, twp);
+    s = 1;
+    if (!(LOGN & 1)) {
+      fwd_half_r2<LOGN>(D, 1, rank, tw, twp);
+      s = 2;
     }
-    cluster.sync();
+#pragma unroll 1
+    for (; s < LOGN; s += 2) fwd_half_r4<LOGN>(D, s, rank, tw, twp);
 #pragma unroll
     for (int k = 0; k < 2; k++) {
-      const int t = own + tid + k * NT;
+      const int lt = tid + k * NT;
       const u32 tb = s_tab[((gp * et[k]) & M2N) >> 1];
-      const u64 mine = bufB[t], theirs = peerB[t];
-      const u64 d0 = rank == 0 ? mine : theirs;
-      const u64 d1 = rank == 0 ? theirs : mine;
+      const u64 d0 = D[lt], d1 = D[H + lt];
       u128 nb = wide(d0, Y[tb]) + wide(d1, Y[N + tb]);
       u128 nc = wide(a_ntt[tb], sv[k]) + wide(d0, Wm[tb]) + wide(d1, Wm[N + tb]);
       if (exact) {
@@ -648,27 +766,31 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
       cur[k] = redc(nc);
     }
   }
-  // Final transforms: rank 0 assembles R_0 (-> a), rank 1 the online sum (-> b).
+  // Final transforms: rank 0 assembles R_0 (-> a), rank 1 the online sum (-> b), each
+  // from its own half and the peer's half (exchanged through the half of X that link 0
+  // did not use; the peer read it last at link 1, before the barrier of link 0).
+  u64* xf = X + H;
+  const u64* pf = peerX + H;
 #pragma unroll
   for (int k = 0; k < 2; k++) {
-    X[tid + k * NT] = rank == 0 ? sb[k] : cur[k];
-    bufA[own + tid + k * NT] = rank == 0 ? cur[k] : sb[k];
+    xf[tid + k * NT] = rank == 0 ? sb[k] : cur[k];
+    D[own + tid + k * NT] = rank == 0 ? cur[k] : sb[k];
   }
   cluster.sync();
 #pragma unroll
-  for (int k = 0; k < 2; k++) bufA[other + tid + k * NT] = peerX[tid + k * NT];
+  for (int k = 0; k < 2; k++) D[other + tid + k * NT] = pf[tid + k * NT];
   cluster.sync();  // each CTA's X stays alive until its peer has read it
   {
-    u64* const bufs[1] = {bufA};
+    u64* const bufs[1] = {D};
     ntt_inv_r4<LOGN, NT, 1>(bufs, tw, twp);
   }
 #pragma unroll
   for (int k = 0; k < 4; k++) {
     const int t = tid + k * NT;
     if (rank == 0)
-      a_out[(size_t)qi * N + t] = finish_a(c, bufA[t], ms_target);
+      a_out[(size_t)qi * N + t] = finish_a(c, D[t], ms_target);
     else
-      b_out[(size_t)qi * N + t] = finish_b(c, bufA[t], t, qi, b_fold, ms_target);
+      b_out[(size_t)qi * N + t] = finish_b(c, D[t], t, qi, b_fold, ms_target);
   }
 }
 
@@ -723,7 +845,7 @@ cudaError_t shard_scan(const CrsDev& c, const QueryDev* queries, const ShardDev*
 }
 
 size_t respond_smem_bytes(const CrsDev& c, bool pair) {
-  const size_t words = pair ? (size_t)(5 * c.n + c.n / 2) : (size_t)(6 * c.n);
+  const size_t words = pair ? (size_t)(5 * c.n) : (size_t)(6 * c.n);
   return (words + 2 * (size_t)c.rows * c.n) * 8 + 2 * (size_t)c.n * 2;
 }
 
