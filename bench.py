@@ -327,9 +327,11 @@ def run_gb300(args, rank, world):
     resp_ms, resp_n = prof["respond"]
     scan_avg = scan_ms / max(scan_n, 1)
     resp_avg = resp_ms / max(resp_n, 1)
-    # Algorithmic bytes of one scan launch: per query the gamma columns (u64 words), the
-    # shard's tag key (2n words) and the query's b (n words), plus gamma folded words out.
-    scan_bytes = BATCH * (GAMMA * N_RING * 8 + 2 * N_RING * 8 + N_RING * 8 + GAMMA * 8)
+    # Algorithmic bytes of one scan launch. The shards hold 16-bit record words, which the
+    # library keeps as a u16 copy for the scan: per query the gamma columns at 2 bytes a
+    # word, the even tag-key words (the odd ones multiply the high halves, all zero), the
+    # query's b (n words), and gamma folded words out.
+    scan_bytes = BATCH * (GAMMA * N_RING * 2 + N_RING * 8 + N_RING * 8 + GAMMA * 8)
     hbm_peak, peak_kind = peaks()
     achieved = scan_bytes / (scan_avg / 1e3) / 1e9
     # Recursion: 3 transforms of n/2 log n butterflies per link + 16 pointwise products.

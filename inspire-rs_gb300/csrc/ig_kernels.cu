@@ -239,11 +239,22 @@ __global__ void __launch_bounds__(FOLD_THREADS) k_store_fold(CrsDev c, const u64
 }
 
 // ------------------------------------------------------------------------------------
-// Shard scan: one warp per (query, column). Per word w_k of column j:
+// Shard scan (shard_store.rs:197-264). Per word w_k of column j:
 //   tag  += lo32(w_k) key[2k] + hi32(w_k) key[2k+1]            (mod 2^61 - 1 at the end)
 //   fold += w_k * b_rev[k],  b_rev[0] = b_0, b_rev[k] = -b_{n-k}  (mod q at the end)
-// Accumulators are exact 128-bit sums; the fold keeps low and high product halves apart.
-constexpr int SCAN_COLS = 8;  // columns (warps) per CTA
+// Each warp takes SCAN_ROWS consecutive columns of one query.
+//
+// Compact shards (every word below 2^16, kept as a u16 copy, so hi32(w) = 0): the tag and
+// fold are a matrix-vector product of the column words with (key[2k], b_rev[k]). Each
+// vector word is split into 32-bit limbs and staged once per CTA in shared memory; every
+// product w * limb is below 2^48, so a lane's 64-bit accumulators hold 2^16 products
+// exactly, and the limbs recombine into 128-bit sums at the end. The vector layout
+// V[k & 7][k >> 3] lets lane l read positions 8m..8m+7 (m = l + 32 it) conflict-free
+// while loading the same positions of a column as one 16-byte word.
+//
+// Other shards take the exact 128-bit path over the u64 words.
+constexpr int SCAN_WARPS = 8;
+constexpr int SCAN_ROWS = 4;  // columns per warp
 constexpr u64 TAG_PRIME = (1ULL << 61) - 1;
 
 __device__ __forceinline__ u128 shfl_xor_u128(u128 v, int m) {
@@ -253,57 +264,152 @@ __device__ __forceinline__ u128 shfl_xor_u128(u128 v, int m) {
   return ((u128)hi << 64) | lo;
 }
 
+// Lane 0's end of a column: the tag check (or the tag itself in build mode) and the fold.
+__device__ __forceinline__ void scan_finish(const CrsDev& c, const ShardDev& sh, u32 qi, u32 j, u128 tag, u128 fold,
+                                            u64* b_fold, u32* status, int build, u64* tags_out) {
+  u128 t = tag;
+  t = (t & TAG_PRIME) + (t >> 61);
+  t = (t & TAG_PRIME) + (t >> 61);
+  u64 tv = (u64)t;
+  while (tv >= TAG_PRIME) tv -= TAG_PRIME;
+  if (build) {
+    tags_out[j] = tv;
+  } else {
+    if (sh.tags && tv != sh.tags[j]) atomicOr(status + qi, (u32)DEV_TAG_MISMATCH);
+    b_fold[(size_t)qi * c.gamma + j] = reduce128(fold);
+  }
+}
+
 template <int LOGN>
-__global__ void __launch_bounds__(SCAN_COLS * 32) k_scan(CrsDev c, const QueryDev* queries, const ShardDev* shards,
-                                                         u64* b_fold, u32* status, int build, u64* tags_out) {
-  constexpr int N = 1 << LOGN;
+__global__ void __launch_bounds__(SCAN_WARPS * 32) k_scan(CrsDev c, const QueryDev* queries, const ShardDev* shards,
+                                                          u64* b_fold, u32* status, int build, u64* tags_out) {
+  constexpr int N = 1 << LOGN, M = N / 8;
+  __shared__ __align__(16) uint4 V[N];  // [8][M]: key[2k] lo, hi, b_rev[k] lo, hi
   const u32 qi = blockIdx.y;
   const QueryDev qd = queries[qi];
   const ShardDev sh = shards[qd.shard];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const u32 j = blockIdx.x * SCAN_COLS + warp;
-  if (j >= c.gamma) return;
-  const u64* col = sh.columns + (size_t)j * N;
+  const u32 j0 = (blockIdx.x * SCAN_WARPS + warp) * SCAN_ROWS;
   const u64* key = sh.tag_key;
   const u64* b = qd.b;
-  u128 tag = 0, flo = 0, fhi = 0;
-#pragma unroll 4
-  for (int k0 = lane * 2; k0 < N; k0 += 64) {
-    const ulonglong2 w = *reinterpret_cast<const ulonglong2*>(col + k0);
-    const ulonglong2 ka = *reinterpret_cast<const ulonglong2*>(key + 2 * k0);
-    const ulonglong2 kb = *reinterpret_cast<const ulonglong2*>(key + 2 * k0 + 2);
-    tag += (u128)(w.x & 0xffffffffULL) * ka.x + (u128)(w.x >> 32) * ka.y;
-    tag += (u128)(w.y & 0xffffffffULL) * kb.x + (u128)(w.y >> 32) * kb.y;
-    if (b) {
-      const u64 r0 = k0 == 0 ? reduce128(b[0]) : negq(reduce128(b[N - k0]));
-      const u64 r1 = negq(reduce128(b[N - k0 - 1]));
-      const u128 p0 = (u128)w.x * r0, p1 = (u128)w.y * r1;
-      flo += (u128)(u64)p0 + (u64)p1;
-      fhi += (p0 >> 64) + (p1 >> 64);
+
+  if (sh.cols16 && b && !build) {
+    for (int k = threadIdx.x; k < N; k += SCAN_WARPS * 32) {
+      const u64 kv = key[2 * k];
+      const u64 bv = k == 0 ? reduce128(b[0]) : negq(reduce128(b[N - k]));
+      V[(k & 7) * M + (k >> 3)] = make_uint4((u32)kv, (u32)(kv >> 32), (u32)bv, (u32)(bv >> 32));
     }
-  }
+    __syncthreads();
+    if (j0 >= c.gamma) return;
+    const int rows = min(SCAN_ROWS, (int)(c.gamma - j0));
+    u64 tl[SCAN_ROWS], th[SCAN_ROWS], fl[SCAN_ROWS], fh[SCAN_ROWS];
 #pragma unroll
-  for (int m = 16; m >= 1; m >>= 1) {
-    tag += shfl_xor_u128(tag, m);
-    flo += shfl_xor_u128(flo, m);
-    fhi += shfl_xor_u128(fhi, m);
+    for (int r = 0; r < SCAN_ROWS; r++) tl[r] = th[r] = fl[r] = fh[r] = 0;
+    const uint16_t* col = sh.cols16 + (size_t)j0 * N;
+#pragma unroll 2
+    for (int m = lane; m < M; m += 32) {
+      uint4 w[SCAN_ROWS];
+#pragma unroll
+      for (int r = 0; r < SCAN_ROWS; r++)
+        w[r] = r < rows ? *reinterpret_cast<const uint4*>(col + (size_t)r * N + 8 * m) : make_uint4(0, 0, 0, 0);
+#pragma unroll
+      for (int p = 0; p < 8; p++) {
+        const uint4 v = V[p * M + m];
+#pragma unroll
+        for (int r = 0; r < SCAN_ROWS; r++) {
+          const u32 word = p & 1 ? (((&w[r].x)[p >> 1]) >> 16) : (((&w[r].x)[p >> 1]) & 0xffffu);
+          tl[r] += (u64)word * v.x;
+          th[r] += (u64)word * v.y;
+          fl[r] += (u64)word * v.z;
+          fh[r] += (u64)word * v.w;
+        }
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < SCAN_ROWS; r++) {
+#pragma unroll
+      for (int s = 16; s >= 1; s >>= 1) {
+        tl[r] += __shfl_xor_sync(0xffffffffu, tl[r], s);
+        th[r] += __shfl_xor_sync(0xffffffffu, th[r], s);
+        fl[r] += __shfl_xor_sync(0xffffffffu, fl[r], s);
+        fh[r] += __shfl_xor_sync(0xffffffffu, fh[r], s);
+      }
+    }
+    if (lane < rows) {
+      u64 a = tl[0], bh = th[0], f0 = fl[0], f1 = fh[0];
+#pragma unroll
+      for (int r = 1; r < SCAN_ROWS; r++)
+        if (lane == r) {
+          a = tl[r];
+          bh = th[r];
+          f0 = fl[r];
+          f1 = fh[r];
+        }
+      const u128 tag = (u128)a + ((u128)bh << 32);
+      const u128 fold = (u128)f0 + ((u128)f1 << 32);
+      scan_finish(c, sh, qi, j0 + lane, tag, fold, b_fold, status, build, tags_out);
+    }
+    return;
   }
-  if (lane == 0) {
-    u128 t = tag;
-    t = (t & TAG_PRIME) + (t >> 61);
-    t = (t & TAG_PRIME) + (t >> 61);
-    u64 tv = (u64)t;
-    while (tv >= TAG_PRIME) tv -= TAG_PRIME;
-    if (build) {
-      tags_out[j] = tv;
-    } else {
-      if (sh.tags && tv != sh.tags[j]) atomicOr(status + qi, (u32)DEV_TAG_MISMATCH);
+
+#pragma unroll 1
+  for (int r = 0; r < SCAN_ROWS; r++) {
+    const u32 j = j0 + r;
+    if (j >= c.gamma) return;
+    const u64* col = sh.columns + (size_t)j * N;
+    u128 tag = 0, flo = 0, fhi = 0;
+#pragma unroll 4
+    for (int k0 = lane * 2; k0 < N; k0 += 64) {
+      const ulonglong2 w = *reinterpret_cast<const ulonglong2*>(col + k0);
+      const ulonglong2 ka = *reinterpret_cast<const ulonglong2*>(key + 2 * k0);
+      const ulonglong2 kb = *reinterpret_cast<const ulonglong2*>(key + 2 * k0 + 2);
+      tag += (u128)(w.x & 0xffffffffULL) * ka.x + (u128)(w.x >> 32) * ka.y;
+      tag += (u128)(w.y & 0xffffffffULL) * kb.x + (u128)(w.y >> 32) * kb.y;
+      if (b) {
+        const u64 r0 = k0 == 0 ? reduce128(b[0]) : negq(reduce128(b[N - k0]));
+        const u64 r1 = negq(reduce128(b[N - k0 - 1]));
+        const u128 p0 = (u128)w.x * r0, p1 = (u128)w.y * r1;
+        flo += (u128)(u64)p0 + (u64)p1;
+        fhi += (p0 >> 64) + (p1 >> 64);
+      }
+    }
+#pragma unroll
+    for (int m = 16; m >= 1; m >>= 1) {
+      tag += shfl_xor_u128(tag, m);
+      flo += shfl_xor_u128(flo, m);
+      fhi += shfl_xor_u128(fhi, m);
+    }
+    if (lane == 0) {
       // fold = fhi * 2^64 + flo (mod q)
       const u64 r64 = (u64)((((u128)1) << 64) % Q);
       const u64 hq = reduce128(fhi), lq = reduce128(flo);
-      b_fold[(size_t)qi * c.gamma + j] = reduce128((u128)hq * r64 + lq);
+      scan_finish(c, sh, qi, j, tag, (u128)hq * r64 + lq, b_fold, status, build, tags_out);
     }
   }
+}
+
+// Compact copy of a shard's columns: out[k] = w[k] when every word is below 2^16; any
+// larger word sets *wide. Eight words per thread.
+__global__ void k_compact16(const u64* cols, size_t groups, uint16_t* out, u32* wide) {
+  const size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= groups) return;
+  const ulonglong2* src = reinterpret_cast<const ulonglong2*>(cols + 8 * g);
+  u64 w[8];
+  bool big = false;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const ulonglong2 v = src[k];
+    w[2 * k] = v.x;
+    w[2 * k + 1] = v.y;
+    big |= (v.x | v.y) >> 16 != 0;
+  }
+  if (big) atomicOr(wide, 1u);
+  uint4 o;
+  o.x = (u32)w[0] | ((u32)w[1] << 16);
+  o.y = (u32)w[2] | ((u32)w[3] << 16);
+  o.z = (u32)w[4] | ((u32)w[5] << 16);
+  o.w = (u32)w[6] | ((u32)w[7] << 16);
+  reinterpret_cast<uint4*>(out)[g] = o;
 }
 
 // ------------------------------------------------------------------------------------
@@ -636,6 +742,9 @@ __device__ __forceinline__ void fwd_half_r2(u64* D, int s, int rank, const u64* 
 //   (own half, peer's half read through distributed shared memory), n^-1, digit split and
 //   the forward cross stage, keeping this CTA's half of digits 0 and 1 -> local forward
 //   stages -> pointwise at own slots.
+// Thread pair (2u, 2u+1) owns local slots 4u..4u+3, two each: the first inverse pass
+// (stages 0 and 1, one 4-slot unit) and the last forward pass (same units, one digit per
+// lane) run in registers with one lane exchange, next to the pointwise link.
 // One cluster barrier per link: the exchange buffer X alternates between two halves by
 // link parity, so a CTA rewrites the half its peer read at link i only at link i-2, after
 // both passed the barrier of link i-1. With the exact gadget the third digit's transform
@@ -646,7 +755,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
     k_respond_pair(CrsDev c, const QueryDev* queries, const ShardDev* shards, const u64* b_fold, u64 ms_target,
                    u64* a_out, u64* b_out, u32* status, int force_serial) {
   namespace cg = cooperative_groups;
-  constexpr int N = 1 << LOGN, NT = N / 4, H = N / 2;
+  constexpr int N = 1 << LOGN, NT = N / 4, H = N / 2, HU = N / 8;
   constexpr u32 M2N = 2 * N - 1;
   constexpr u64 DMASK = (1ULL << 20) - 1;
   extern __shared__ __align__(16) u64 sm[];
@@ -671,6 +780,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
   const u32 gamma = c.gamma;
   const bool exact = c.approx == 0;
   const int own = rank * H, other = (rank ^ 1) * H;
+  const int u = tid >> 1, dg = tid & 1;
+  const int ls = 4 * u + 2 * dg;  // local slots ls, ls + 1
+  const int ug = rank * HU + u;   // global unit index of slots 4u..4u+3
 
   stage_constants<N, NT>(c, qd.seat_R, tw, twp, Wm, Y, e_tab, s_tab);
   expand_a<N, NT>(qd, a_ntt, status, qi, force_serial);
@@ -681,34 +793,48 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
   u64 cur[2], sb[2];
   u32 et[2];
 #pragma unroll
-  for (int k = 0; k < 2; k++) et[k] = e_tab[own + tid + k * NT];
+  for (int k = 0; k < 2; k++) et[k] = e_tab[own + ls + k];
   {
     const u32 gp = c.gpow[gamma - 1];
     const u64* Srow = sh.sums_R + (size_t)(gamma - 1) * N;
 #pragma unroll
     for (int k = 0; k < 2; k++) {
-      const int t = own + tid + k * NT;
       const u32 tb = s_tab[((gp * et[k]) & M2N) >> 1];
-      cur[k] = mont(a_ntt[tb], Srow[t]);
+      cur[k] = mont(a_ntt[tb], Srow[own + ls + k]);
       sb[k] = 0;
     }
   }
+  // Twiddles of the register passes: inverse stages 0-1 of unit ug, forward stages
+  // logn-2, logn-1 of unit ug (fixed per thread).
+  u64 wl1, wl1p, wl2, wl2p;
+  inv_twiddle(tw, twp, H + 2 * ug + dg, wl1, wl1p);
+  inv_twiddle(tw, twp, H / 2 + ug, wl2, wl2p);
+  constexpr int MF = 1 << (LOGN - 2);
+  const u64 fa = tw[MF + ug], fap = twp[MF + ug];
+  const u64 fb = tw[2 * MF + 2 * ug], fbp = twp[2 * MF + 2 * ug];
+  const u64 fc = tw[2 * MF + 2 * ug + 1], fcp = twp[2 * MF + 2 * ug + 1];
   u64 wi, wip;
   inv_twiddle(tw, twp, 1, wi, wip);
   const u64 wf = tw[1], wfp = twp[1];
 #pragma unroll 1
   for (int i = (int)gamma - 2; i >= 0; i--) {
     const u64* Srow = sh.sums_R + (size_t)i * N;
-    u64 sv[2];
-#pragma unroll
-    for (int k = 0; k < 2; k++) sv[k] = Srow[own + tid + k * NT];
+    const ulonglong2 sv = *reinterpret_cast<const ulonglong2*>(Srow + own + ls);
     const u32 gp = c.gpow[i];
     const int par = (i & 1) * H;
     u64* xh = X + par;
-#pragma unroll
-    for (int k = 0; k < 2; k++) xh[tid + k * NT] = cur[k];
+    {
+      // Inverse stages 0-1 of unit ug: lane dg holds slots 4u + 2dg, +1.
+      u64 p = cur[0], q = cur[1];
+      bf_inv(p, q, wl1, wl1p);
+      const u64 recv = __shfl_xor_sync(0xffffffffu, dg == 0 ? q : p, 1);
+      u64 x0 = dg == 0 ? p : recv, x1 = dg == 0 ? recv : q;  // (slot 4u, 4u+2) or (4u+1, 4u+3)
+      bf_inv(x0, x1, wl2, wl2p);
+      xh[4 * u + dg] = x0;
+      xh[4 * u + dg + 2] = x1;
+    }
     __syncthreads();
-    int s = 0;
+    int s = 2;
 #pragma unroll 1
     for (; s + 1 <= LOGN - 2; s += 2) inv_half_r4<LOGN>(xh, s, rank, tw, twp);
     if (s == LOGN - 2) inv_half_r2<LOGN>(xh, s, rank, tw, twp);
@@ -749,16 +875,34 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
       s = 2;
     }
 #pragma unroll 1
-    for (; s < LOGN; s += 2) fwd_half_r4<LOGN>(D, s, rank, tw, twp);
+    for (; s < LOGN - 2; s += 2) fwd_half_r4<LOGN>(D, s, rank, tw, twp);
+    // Forward stages logn-2, logn-1 of unit ug for digit dg, then each lane takes the other
+    // digit at its own two slots from its partner.
+    u64 d0[2], d1[2];
+    {
+      const u64* x = D + dg * H + 4 * u;
+      const ulonglong2 v01 = *reinterpret_cast<const ulonglong2*>(x);
+      const ulonglong2 v23 = *reinterpret_cast<const ulonglong2*>(x + 2);
+      u64 a0 = v01.x, a1 = v01.y, a2 = v23.x, a3 = v23.y;
+      bf_fwd(a0, a2, fa, fap);
+      bf_fwd(a1, a3, fa, fap);
+      bf_fwd(a0, a1, fb, fbp);
+      bf_fwd(a2, a3, fc, fcp);
+      const u64 g0 = __shfl_xor_sync(0xffffffffu, dg == 0 ? a2 : a0, 1);
+      const u64 g1 = __shfl_xor_sync(0xffffffffu, dg == 0 ? a3 : a1, 1);
+      const u64 m0 = dg == 0 ? a0 : a2, m1 = dg == 0 ? a1 : a3;
+      d0[0] = dg == 0 ? m0 : g0;
+      d0[1] = dg == 0 ? m1 : g1;
+      d1[0] = dg == 0 ? g0 : m0;
+      d1[1] = dg == 0 ? g1 : m1;
+    }
 #pragma unroll
     for (int k = 0; k < 2; k++) {
-      const int lt = tid + k * NT;
       const u32 tb = s_tab[((gp * et[k]) & M2N) >> 1];
-      const u64 d0 = D[lt], d1 = D[H + lt];
-      u128 nb = wide(d0, Y[tb]) + wide(d1, Y[N + tb]);
-      u128 nc = wide(a_ntt[tb], sv[k]) + wide(d0, Wm[tb]) + wide(d1, Wm[N + tb]);
+      u128 nb = wide(d0[k], Y[tb]) + wide(d1[k], Y[N + tb]);
+      u128 nc = wide(a_ntt[tb], k == 0 ? sv.x : sv.y) + wide(d0[k], Wm[tb]) + wide(d1[k], Wm[N + tb]);
       if (exact) {
-        const u64 d2 = redc(wide(cur[k], c.ld_inv_R) + wide(d0, c.ld_c0_R) + wide(d1, c.ld_c1_R));
+        const u64 d2 = redc(wide(cur[k], c.ld_inv_R) + wide(d0[k], c.ld_c0_R) + wide(d1[k], c.ld_c1_R));
         nb += wide(d2, Y[2 * N + tb]);
         nc += wide(d2, Wm[2 * N + tb]);
       }
@@ -769,12 +913,13 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
   // Final transforms: rank 0 assembles R_0 (-> a), rank 1 the online sum (-> b), each
   // from its own half and the peer's half (exchanged through the half of X that link 0
   // did not use; the peer read it last at link 1, before the barrier of link 0).
+  __syncthreads();  // every lane is past its last read of D
   u64* xf = X + H;
   const u64* pf = peerX + H;
 #pragma unroll
   for (int k = 0; k < 2; k++) {
-    xf[tid + k * NT] = rank == 0 ? sb[k] : cur[k];
-    D[own + tid + k * NT] = rank == 0 ? cur[k] : sb[k];
+    xf[ls + k] = rank == 0 ? sb[k] : cur[k];
+    D[own + ls + k] = rank == 0 ? cur[k] : sb[k];
   }
   cluster.sync();
 #pragma unroll
@@ -837,10 +982,19 @@ cudaError_t store_fold(const CrsDev& c, const u64* H, u64* sums_R, cudaStream_t 
 cudaError_t shard_scan(const CrsDev& c, const QueryDev* queries, const ShardDev* shards, u32 nq, u64* b_fold,
                        u32* status, int mode_build, u64* tags_out, cudaStream_t s) {
   if (nq == 0) return cudaSuccess;
-  dim3 grid((c.gamma + SCAN_COLS - 1) / SCAN_COLS, nq);
+  constexpr u32 per_cta = SCAN_WARPS * SCAN_ROWS;
+  dim3 grid((c.gamma + per_cta - 1) / per_cta, nq);
   IG_DISPATCH_LOGN(c.logn, {
-    k_scan<L><<<grid, SCAN_COLS * 32, 0, s>>>(c, queries, shards, b_fold, status, mode_build, tags_out);
+    k_scan<L><<<grid, SCAN_WARPS * 32, 0, s>>>(c, queries, shards, b_fold, status, mode_build, tags_out);
   });
+  return cudaGetLastError();
+}
+
+cudaError_t compact16(const u64* cols, size_t words, uint16_t* out, u32* wide, cudaStream_t s) {
+  if (words == 0 || words % 8) return cudaErrorInvalidValue;
+  const size_t groups = words / 8;
+  const unsigned threads = 256;
+  k_compact16<<<(unsigned)((groups + threads - 1) / threads), threads, 0, s>>>(cols, groups, out, wide);
   return cudaGetLastError();
 }
 

@@ -43,10 +43,11 @@ struct QueryDev {
 };
 
 struct ShardDev {
-  const u64* columns;  // gamma x n raw column words
-  const u64* sums_R;   // gamma x n step-1 sums, R-form NTT (the packing store)
-  const u64* tag_key;  // 2n key words
-  const u64* tags;     // gamma column tags
+  const u64* columns;        // gamma x n raw column words
+  const u64* sums_R;         // gamma x n step-1 sums, R-form NTT (the packing store)
+  const u64* tag_key;        // 2n key words
+  const u64* tags;           // gamma column tags
+  const uint16_t* cols16;    // the same words as u16 when all are below 2^16, else null
 };
 
 }  // namespace ig
@@ -66,6 +67,10 @@ cudaError_t ntt_rows(const CrsDev& c, const u64* in, u64* out, u32 rows, u64 sca
 // table into `tags_out` instead of checking.
 cudaError_t shard_scan(const CrsDev& c, const QueryDev* queries, const ShardDev* shards, u32 nq,
                        u64* b_fold, u32* status, int mode_build, u64* tags_out, cudaStream_t s);
+
+// Compact u16 copy of `words` column words (a multiple of 8); sets *wide when a word is
+// 2^16 or above (the copy is then unusable).
+cudaError_t compact16(const u64* cols, size_t words, uint16_t* out, u32* wide, cudaStream_t s);
 
 // Step-1 sums of one shard from the NTTs of its columns (H: gamma x n standard form).
 cudaError_t store_fold(const CrsDev& c, const u64* H, u64* sums_R, cudaStream_t s);

@@ -117,6 +117,10 @@ struct ShardSlot {
   u64* sums = nullptr;
   u64* tag_key = nullptr;
   u64* tags = nullptr;
+  uint16_t* cols16 = nullptr;  // u16 copy of the columns; valid when `compact`
+  bool compact = false;
+  // The device table entry of this shard.
+  ShardDev dev() const { return ShardDev{cols, sums, tag_key, tags, compact ? cols16 : nullptr}; }
 };
 
 struct DbObj {
@@ -314,7 +318,7 @@ DbObj* get_db(ig_ctx* c, u64 h) {
 }
 
 int sync_table_entry(ig_ctx* c, DbObj& db, u32 s) {
-  ShardDev d{db.shards[s].cols, db.shards[s].sums, db.shards[s].tag_key, db.shards[s].tags};
+  const ShardDev d = db.shards[s].dev();
   IG_CUDA(c, cudaMemcpyAsync(db.d_table + s, &d, sizeof d, cudaMemcpyHostToDevice, c->stream));
   IG_CUDA(c, cudaStreamSynchronize(c->stream));
   return IG_OK;
@@ -653,6 +657,7 @@ int ig_db_destroy(ig_ctx* c, uint64_t dbh) {
     cudaFree(s.sums);
     cudaFree(s.tag_key);
     cudaFree(s.tags);
+    cudaFree(s.cols16);
   }
   cudaFree(it->second.d_table);
   c->obj_bytes -= it->second.bytes;
@@ -676,8 +681,23 @@ static int set_shard(ig_ctx* c, uint64_t dbh, uint32_t s, const uint64_t* cols, 
     int rc = dalloc(c, (void**)&sl.cols, bytes, &db->bytes);
     if (rc) return rc;
   }
+  if (!sl.cols16) {
+    int rc = dalloc(c, (void**)&sl.cols16, bytes / 4, &db->bytes);
+    if (rc) return rc;
+  }
+  void* wide;
+  int rc = scratch(c, "compact_flag", 4, &wide);
+  if (rc) return rc;
   IG_CUDA(c, cudaMemcpyAsync(sl.cols, cols, bytes, kind, c->stream));
+  // Shards whose words all fit 16 bits (encoded records always do) are scanned from a
+  // u16 copy: the same tags and folds from a quarter of the bytes.
+  IG_CUDA(c, cudaMemsetAsync(wide, 0, 4, c->stream));
+  IG_CUDA(c, igk::compact16(sl.cols, bytes / 8, sl.cols16, (u32*)wide, c->stream));
+  c->launches++;
+  u32 wide_h = 1;
+  IG_CUDA(c, cudaMemcpyAsync(&wide_h, wide, 4, cudaMemcpyDeviceToHost, c->stream));
   IG_CUDA(c, cudaStreamSynchronize(c->stream));
+  sl.compact = wide_h == 0;
   return sync_table_entry(c, *db, s);
 }
 
@@ -952,12 +972,12 @@ static int respond_host(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_t handle, c
   for (size_t k = 0; k < distinct.size(); k++) {
     const ShardSlot& sl = db->shards[distinct[k]];
     if (sl.sums) {
-      table[k] = ShardDev{sl.cols, sl.sums, sl.tag_key, sl.tags};
+      table[k] = sl.dev();
     } else {
       u64* sums = (u64*)tsums + (size_t)tk++ * g * n;
       rc = fold_store(c, o, sl.cols, sums);
       if (rc) return rc;
-      table[k] = ShardDev{sl.cols, sums, zkey, nullptr};
+      table[k] = ShardDev{sl.cols, sums, zkey, nullptr, sl.compact ? sl.cols16 : nullptr};
     }
   }
   void *d_table, *d_q, *d_seeds, *d_bs, *d_a, *d_b, *d_fold, *d_status;
@@ -1191,7 +1211,7 @@ static int resolve_request_locked(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_t
   const ShardSlot& sl = db->shards[shard];
   if (!sl.cols) return fail(c, IG_ERR_ARG, "shard %u holds no columns", shard);
   out->crs = o.dev;
-  out->shard = ShardDev{sl.cols, sl.sums, sl.tag_key, sl.tags};
+  out->shard = sl.dev();
   out->seat = seat;
   out->crs_handle = db->crs;
   out->p = o.p;
