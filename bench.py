@@ -232,6 +232,25 @@ def serve_leg(pkg, ctx, crs, db, store, handle, queries, ms, slots=2, max_batch=
     return out
 
 
+def plain_leg(pkg, crs, db, keys, queries, ms):
+    """One query per call through respond_seeded_inspiring with the packing key inline
+    (respond.rs:1218-1226): per call the key's seat is built, the shard scanned and the
+    query answered alone. Host buffers; latency per call."""
+    lat = []
+    calls = [pkg.SeededClientQuery(q.shard_id, q.seed, q.b, inspiring_packing_keys=keys) for q in queries]
+    for q in calls[:3]:
+        pkg.respond_seeded_inspiring(crs, db, q, mod_switch_target=ms)
+    t0 = time.perf_counter()
+    for q in calls:
+        t = time.perf_counter()
+        pkg.respond_seeded_inspiring(crs, db, q, mod_switch_target=ms)
+        lat.append(time.perf_counter() - t)
+    total = time.perf_counter() - t0
+    lat.sort()
+    return {"calls": len(calls), "queries_per_s": len(calls) / total, "p50_ms": 1e3 * lat[len(lat) // 2],
+            "p99_ms": 1e3 * lat[min(len(lat) - 1, int(0.99 * len(lat)))]}
+
+
 def run_gb300(args, rank, world):
     import torch
 
@@ -322,6 +341,7 @@ def run_gb300(args, rank, world):
     assert len(out) == BATCH
 
     serving = serve_leg(pkg, ctx, crs, db, store, handle, [q for qs in e2e_queries for q in qs], MS_TARGET)
+    plain = plain_leg(pkg, crs, db, keys, [q for qs in e2e_queries for q in qs][:64], MS_TARGET)
 
     scan_ms, scan_n = prof["scan"]
     resp_ms, resp_n = prof["respond"]
@@ -338,6 +358,9 @@ def run_gb300(args, rank, world):
     links = GAMMA - 1
     modmul_per_query = links * (3 * (N_RING // 2) * 11 + 16 * N_RING) + 3 * (N_RING // 2) * 11
     resp_gmodmul = BATCH * modmul_per_query / (resp_avg / 1e3) / 1e9
+    # Integer ceiling, measured now on this GPU: register-resident lazy butterflies (one
+    # Shoup product mod q each) with eight independent chains per thread.
+    peak_gmodmul = ctx.butterfly_peak() / 1e9
     return {
         "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -355,13 +378,18 @@ def run_gb300(args, rank, world):
                      "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
                      "avg_launch_ms": scan_avg, "algorithmic_bytes_per_launch": scan_bytes},
         "roofline_dominant": {"kernel": "respond (fused recursion + online gather)", "bound": "integer issue",
-                              "achieved": resp_gmodmul, "unit": "G modmul/s", "avg_launch_ms": resp_avg,
+                              "achieved": resp_gmodmul, "unit": "G modmul/s", "peak": peak_gmodmul,
+                              "frac": resp_gmodmul / peak_gmodmul,
+                              "peak_source": "measured in this run: lazy mod-q butterflies in registers "
+                                             "(ig_butterfly_peak)",
+                              "avg_launch_ms": resp_avg,
                               "modmul_per_query": modmul_per_query,
                               "share_of_step": resp_ms / max(ms_total, 1e-9)},
         "gpu_launches": int(launches),
         "setup_s": setup_s,
         "clocks": clk.summary(),
         "serving": serving,
+        "plain": plain,
     }
 
 

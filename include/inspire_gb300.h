@@ -246,6 +246,11 @@ int ig_response_encode(const uint64_t* a, const uint64_t* b, uint32_t ring_dim, 
  * 1 = recursion/respond, 2 = store fold) and, when reset != 0, clears the record. */
 int ig_profile_enable(ig_ctx* ctx, int on);
 int ig_profile_read(ig_ctx* ctx, double* ms, uint64_t* counts, int regions, int reset);
+/* Integer roofline probe: runs blocks_per_sm x SMs CTAs of 256 threads, each thread iters
+ * rounds of eight lazy butterflies (one Shoup product mod q each) on register-resident
+ * words, and stores the measured butterflies per second. The respond kernels' transform
+ * and product rates are reported against it. */
+int ig_butterfly_peak(ig_ctx* ctx, int blocks_per_sm, int iters, double* per_s);
 /* Kernel launches this context has made so far. */
 uint64_t ig_launch_count(const ig_ctx* ctx);
 

@@ -121,6 +121,7 @@ def _load():
         "ig_serve_wait": (I, [P, U64, ctypes.c_int64, pu64, ctypes.c_char_p, ctypes.c_size_t]),
         "ig_serve_stats": (I, [P, ctypes.POINTER(ServeStats), I]),
         "ig_serve_destroy": (I, [P]),
+        "ig_butterfly_peak": (I, [P, I, I, ctypes.POINTER(ctypes.c_double)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -178,6 +179,13 @@ class Context:
     def set_pair_threshold(self, max_queries):
         """Batches of at most max_queries run two CTAs per query (0: never)."""
         self.check(self._lib.ig_ctx_set_pair_threshold(self.h, int(max_queries)))
+
+    def butterfly_peak(self, blocks_per_sm=4, iters=4096):
+        """Measured rate of lazy mod-q butterflies (one Shoup product each) in registers, per
+        second: the integer ceiling of the transform work."""
+        v = ctypes.c_double()
+        self.check(self._lib.ig_butterfly_peak(self.h, blocks_per_sm, iters, ctypes.byref(v)))
+        return v.value
 
     @property
     def launch_count(self):

@@ -254,7 +254,7 @@ __global__ void __launch_bounds__(FOLD_THREADS) k_store_fold(CrsDev c, const u64
 //
 // Other shards take the exact 128-bit path over the u64 words.
 constexpr int SCAN_WARPS = 8;
-constexpr int SCAN_ROWS = 4;  // columns per warp
+constexpr int SCAN_ROWS = 8;  // columns per warp: 64 per CTA, two CTAs resident per SM
 constexpr u64 TAG_PRIME = (1ULL << 61) - 1;
 
 __device__ __forceinline__ u128 shfl_xor_u128(u128 v, int m) {
@@ -281,7 +281,7 @@ __device__ __forceinline__ void scan_finish(const CrsDev& c, const ShardDev& sh,
 }
 
 template <int LOGN>
-__global__ void __launch_bounds__(SCAN_WARPS * 32) k_scan(CrsDev c, const QueryDev* queries, const ShardDev* shards,
+__global__ void __launch_bounds__(SCAN_WARPS * 32, 2) k_scan(CrsDev c, const QueryDev* queries, const ShardDev* shards,
                                                           u64* b_fold, u32* status, int build, u64* tags_out) {
   constexpr int N = 1 << LOGN, M = N / 8;
   __shared__ __align__(16) uint4 V[N];  // [8][M]: key[2k] lo, hi, b_rev[k] lo, hi
@@ -294,6 +294,7 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32) k_scan(CrsDev c, const QueryD
   const u64* b = qd.b;
 
   if (sh.cols16 && b && !build) {
+#pragma unroll
     for (int k = threadIdx.x; k < N; k += SCAN_WARPS * 32) {
       const u64 kv = key[2 * k];
       const u64 bv = k == 0 ? reduce128(b[0]) : negq(reduce128(b[N - k]));
@@ -306,7 +307,7 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32) k_scan(CrsDev c, const QueryD
 #pragma unroll
     for (int r = 0; r < SCAN_ROWS; r++) tl[r] = th[r] = fl[r] = fh[r] = 0;
     const uint16_t* col = sh.cols16 + (size_t)j0 * N;
-#pragma unroll 2
+#pragma unroll 1
     for (int m = lane; m < M; m += 32) {
       uint4 w[SCAN_ROWS];
 #pragma unroll
@@ -940,6 +941,28 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
 }
 
 // ------------------------------------------------------------------------------------
+// Integer roofline probe: lazy forward butterflies (one Shoup product, two 64-bit adds and
+// a conditional subtraction each, the transforms' unit of work) on values held in
+// registers, eight independent chains per thread, no memory traffic. Its rate is the
+// ceiling the respond kernels' butterflies are measured against.
+__global__ void __launch_bounds__(256) k_butterfly_peak(u64* out, int iters, u64 w, u64 wp) {
+  u64 x[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) x[k] = (u64)(blockIdx.x * 8191u + threadIdx.x * 131u + k) * 0x9E3779B97F4A7C15ULL % Q;
+#pragma unroll 1
+  for (int it = 0; it < iters; it++) {
+#pragma unroll
+    for (int k = 0; k < 8; k += 2) bf_fwd(x[k], x[k + 1], w, wp);
+#pragma unroll
+    for (int k = 0; k < 4; k++) bf_fwd(x[k], x[k + 4], w, wp);
+  }
+  u64 acc = 0;
+#pragma unroll
+  for (int k = 0; k < 8; k++) acc ^= x[k];
+  if (acc == 0x123456789ULL) out[0] = acc;  // keeps the chains live; practically never taken
+}
+
+// ------------------------------------------------------------------------------------
 // Launchers.
 
 #define IG_DISPATCH_LOGN(logn, ...)                   \
@@ -995,6 +1018,12 @@ cudaError_t compact16(const u64* cols, size_t words, uint16_t* out, u32* wide, c
   const size_t groups = words / 8;
   const unsigned threads = 256;
   k_compact16<<<(unsigned)((groups + threads - 1) / threads), threads, 0, s>>>(cols, groups, out, wide);
+  return cudaGetLastError();
+}
+
+cudaError_t butterfly_peak(u64* out, int blocks, int iters, cudaStream_t s) {
+  const u64 w = 0x0123456789ABCDEULL % Q;
+  k_butterfly_peak<<<blocks, 256, 0, s>>>(out, iters, w, shoup_companion(w));
   return cudaGetLastError();
 }
 

@@ -83,4 +83,7 @@ cudaError_t respond(const CrsDev& c, const QueryDev* queries, const ShardDev* sh
                     u64* a_out, u64* b_out, u32* status, int force_serial_expand, bool pair, cudaStream_t s);
 
 size_t respond_smem_bytes(const CrsDev& c, bool pair);
+
+// Integer roofline probe: blocks x 256 threads x iters x 8 lazy butterflies in registers.
+cudaError_t butterfly_peak(u64* out, int blocks, int iters, cudaStream_t s);
 }  // namespace igk

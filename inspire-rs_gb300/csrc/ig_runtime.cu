@@ -1183,6 +1183,33 @@ int ig_debug_force_serial_expand(ig_ctx* c, int on) {
   return IG_OK;
 }
 
+int ig_butterfly_peak(ig_ctx* c, int blocks_per_sm, int iters, double* per_s) {
+  if (!c || !per_s || blocks_per_sm <= 0 || iters <= 0) return IG_ERR_ARG;
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  int sms = 0;
+  IG_CUDA(c, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
+  void* out;
+  int rc = scratch(c, "peak_out", 8, &out);
+  if (rc) return rc;
+  cudaEvent_t e0, e1;
+  IG_CUDA(c, cudaEventCreate(&e0));
+  IG_CUDA(c, cudaEventCreate(&e1));
+  const int blocks = sms * blocks_per_sm;
+  IG_CUDA(c, igk::butterfly_peak((u64*)out, blocks, iters / 8 + 1, c->stream));  // warm-up
+  IG_CUDA(c, cudaEventRecord(e0, c->stream));
+  IG_CUDA(c, igk::butterfly_peak((u64*)out, blocks, iters, c->stream));
+  IG_CUDA(c, cudaEventRecord(e1, c->stream));
+  IG_CUDA(c, cudaEventSynchronize(e1));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  c->launches += 2;
+  *per_s = (double)blocks * 256.0 * (double)iters * 8.0 / ((double)ms / 1e3);
+  return IG_OK;
+}
+
 int ig_debug_store_sums(ig_ctx* c, uint64_t dbh, uint32_t s, uint64_t* out) {
   if (!c || !out) return IG_ERR_ARG;
   std::lock_guard<std::mutex> lk(c->mu);
