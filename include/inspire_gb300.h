@@ -56,6 +56,15 @@ uint64_t ig_ctx_device_bytes(const ig_ctx* ctx);
  * run one CTA per query. Default: half the device's SM count; 0 disables the pair form.
  * Responses are identical either way. */
 int ig_ctx_set_pair_threshold(ig_ctx* ctx, uint32_t max_queries);
+/* Device-path lanes (1..8, default 1). With lanes > 1, consecutive
+ * ig_respond_seeded_batch_device calls rotate over that many streams, each with its own
+ * scratch, so a batch's scan and recursion overlap the batches before it and batches of
+ * fewer queries than SMs still fill the GPU. Each call's work starts after everything
+ * queued on the context stream before it; call ig_ctx_join before reading a lane's
+ * outputs on the context stream. Responses are identical for any lane count. */
+int ig_ctx_set_lanes(ig_ctx* ctx, uint32_t lanes);
+/* Orders the context stream after all work queued on the lanes. */
+int ig_ctx_join(ig_ctx* ctx);
 
 /* ---- CRS / ServerInspiringCache ------------------------------------------------------
  * Replaces ServerInspiringCache::new (respond.rs:926-941) = PackParams::try_new

@@ -122,6 +122,8 @@ def _load():
         "ig_serve_stats": (I, [P, ctypes.POINTER(ServeStats), I]),
         "ig_serve_destroy": (I, [P]),
         "ig_butterfly_peak": (I, [P, I, I, ctypes.POINTER(ctypes.c_double)]),
+        "ig_ctx_set_lanes": (I, [P, U32]),
+        "ig_ctx_join": (I, [P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -179,6 +181,14 @@ class Context:
     def set_pair_threshold(self, max_queries):
         """Batches of at most max_queries run two CTAs per query (0: never)."""
         self.check(self._lib.ig_ctx_set_pair_threshold(self.h, int(max_queries)))
+
+    def set_lanes(self, lanes):
+        """Streams the device-resident batch entry rotates over (1 = the context stream)."""
+        self.check(self._lib.ig_ctx_set_lanes(self.h, int(lanes)))
+
+    def join(self):
+        """Orders the context stream after all lane work."""
+        self.check(self._lib.ig_ctx_join(self.h))
 
     def butterfly_peak(self, blocks_per_sm=4, iters=4096):
         """Measured rate of lazy mod-q butterflies (one Shoup product each) in registers, per

@@ -39,4 +39,5 @@ struct RequestView {
 };
 int resolve_request(ig_ctx* c, uint64_t db, uint64_t store, uint64_t handle, uint32_t shard, RequestView* out);
 int pair_threshold(ig_ctx* c);
+int sm_count(ig_ctx* c);
 }  // namespace igint

@@ -503,32 +503,35 @@ __device__ __forceinline__ u64 finish_b(const CrsDev& c, u64 x, u32 t, u32 qi, c
 }
 
 // ------------------------------------------------------------------------------------
-// One CTA per query (batches that fill the GPU). Each link of the recursion (i from
-// gamma-2 down to 0) holds R_{i+1} in NTT form (`cur`, four slots per thread):
+// One CTA per query (batches that fill the GPU). Thread u owns slots 4u..4u+3 of every
+// NTT-domain vector (one transform unit). Each link of the recursion (i from gamma-2 down
+// to 0) holds R_{i+1} in NTT form (`cur`, in registers):
 //   r = INTT(R_{i+1});  d_k = base-2^20 digits of r (rounded, top carry kept, when the
 //   lowest digit is dropped);  D_k = NTT(d_k);
 //   sum_b += sum_k Y_k[tau_i(t)] D_k[t];
 //   R_i[t] = a_ntt[tau_i(t)] S_i[t] + sum_k W_k[tau_i(t)] D_k[t]
 // with tau_i the slot permutation of the automorphism X -> X^(g^i), S the packing store,
 // W the mask rows and Y the seat. Each sum of products takes one Montgomery reduction.
-// All digits are transformed (the reference derives the last one from the others; on
-// this machine a transform costs less than the three products that derivation takes).
+// The inverse's first two stages and the forward's last two act within each thread's unit
+// and run in registers; the inverse's last stage, n^-1, the digit split and the forward's
+// first stage fuse into one pass. Digits 0 and 1 are transformed; with the exact gadget
+// digit 2's transform comes from them, D_2 = base^-2 (R_{i+1} - D_0 - base D_1)
+// (inspiring2.rs:1094-1161).
 template <int LOGN>
 __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
     k_respond(CrsDev c, const QueryDev* queries, const ShardDev* shards, const u64* b_fold, u64 ms_target,
               u64* a_out, u64* b_out, u32* status, int force_serial) {
-  constexpr int N = 1 << LOGN, NT = N / 4;
+  constexpr int N = 1 << LOGN, NT = N / 4, H = N / 2;
   constexpr u32 M2N = 2 * N - 1;
   constexpr u64 DMASK = (1ULL << 20) - 1;
   extern __shared__ __align__(16) u64 sm[];
-  u64* bufA = sm;
-  u64* bufB = sm + N;
-  u64* bufC = sm + 2 * N;
-  u64* a_ntt = sm + 3 * N;
-  u64* tw = sm + 4 * N;
-  u64* twp = sm + 5 * N;
+  u64* X = sm;       // N: the inverse in progress
+  u64* D = sm + N;   // 2N: digits 0 and 1 (forward in progress)
+  u64* a_ntt = D + 2 * N;
+  u64* tw = a_ntt + N;
+  u64* twp = tw + N;
   const u32 rows = c.rows;
-  u64* Wm = sm + 6 * N;
+  u64* Wm = twp + N;
   u64* Y = Wm + rows * N;
   uint16_t* e_tab = reinterpret_cast<uint16_t*>(Y + rows * N);
   uint16_t* s_tab = e_tab + N;
@@ -539,6 +542,7 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
   const ShardDev sh = shards[qd.shard];
   const u32 gamma = c.gamma;
   const bool exact = c.approx == 0;
+  const int l0 = 4 * tid;
 
   stage_constants<N, NT>(c, qd.seat_R, tw, twp, Wm, Y, e_tab, s_tab);
   expand_a<N, NT>(qd, a_ntt, status, qi, force_serial);
@@ -550,63 +554,188 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
   u64 cur[4], sb[4];
   u32 et[4];
 #pragma unroll
-  for (int k = 0; k < 4; k++) et[k] = e_tab[tid + k * NT];
+  for (int k = 0; k < 4; k++) et[k] = e_tab[l0 + k];
   {
     const u32 gp = c.gpow[gamma - 1];
     const u64* Srow = sh.sums_R + (size_t)(gamma - 1) * N;
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-      const int t = tid + k * NT;
       const u32 tb = s_tab[((gp * et[k]) & M2N) >> 1];
-      cur[k] = mont(a_ntt[tb], Srow[t]);
+      cur[k] = mont(a_ntt[tb], Srow[l0 + k]);
       sb[k] = 0;
     }
   }
+  constexpr int MF = 1 << (LOGN - 2);
+  u64 wi, wip;
+  inv_twiddle(tw, twp, 1, wi, wip);
+  const u64 wf = tw[1], wfp = twp[1];
 #pragma unroll 1
   for (int i = (int)gamma - 2; i >= 0; i--) {
-    const u64* Srow = sh.sums_R + (size_t)i * N;
-    u64 sv[4];
-#pragma unroll
-    for (int k = 0; k < 4; k++) sv[k] = Srow[tid + k * NT];
+    const u64* Srow = sh.sums_R + (size_t)i * N + l0;
+    const ulonglong2 sv01 = *reinterpret_cast<const ulonglong2*>(Srow);
+    const ulonglong2 sv23 = *reinterpret_cast<const ulonglong2*>(Srow + 2);
     const u32 gp = c.gpow[i];
-#pragma unroll
-    for (int k = 0; k < 4; k++) bufA[tid + k * NT] = cur[k];
-    __syncthreads();
     {
-      u64* const bufs[1] = {bufA};
-      ntt_inv_r4<LOGN, NT, 1>(bufs, tw, twp);
-    }
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-      const int t = tid + k * NT;
-      const u64 r = shoup(bufA[t], c.ninv, c.ninvp);
-      if (exact) {
-        bufB[t] = r & DMASK;
-        bufC[t] = (r >> 20) & DMASK;
-        bufA[t] = r >> 40;
-      } else {
-        const u64 rr = (r + (1ULL << 19)) >> 20;
-        bufB[t] = rr & DMASK;
-        bufC[t] = rr >> 20;
-      }
+      // Inverse stages 0-1 of unit tid (block B = tid, m = N/2).
+      u64 w0, w0p, w1, w1p, w2, w2p;
+      inv_twiddle(tw, twp, H + 2 * tid, w0, w0p);
+      inv_twiddle(tw, twp, H + 2 * tid + 1, w1, w1p);
+      inv_twiddle(tw, twp, H / 2 + tid, w2, w2p);
+      u64 a0 = cur[0], a1 = cur[1], a2 = cur[2], a3 = cur[3];
+      bf_inv(a0, a1, w0, w0p);
+      bf_inv(a2, a3, w1, w1p);
+      bf_inv(a0, a2, w2, w2p);
+      bf_inv(a1, a3, w2, w2p);
+      *reinterpret_cast<ulonglong2*>(X + l0) = make_ulonglong2(a0, a1);
+      *reinterpret_cast<ulonglong2*>(X + l0 + 2) = make_ulonglong2(a2, a3);
     }
     __syncthreads();
-    if (exact) {
-      u64* const bufs[3] = {bufB, bufC, bufA};
-      ntt_fwd_r4<LOGN, NT, 3>(bufs, tw, twp);
-    } else {
-      u64* const bufs[2] = {bufB, bufC};
-      ntt_fwd_r4<LOGN, NT, 2>(bufs, tw, twp);
+    // Inverse stages 2 .. logn-2 (radix-4 pairs, a radix-2 stage last when logn is even).
+    int s = 2;
+#pragma unroll 1
+    for (; s + 1 <= LOGN - 2; s += 2) {
+      const int t = 1 << s, m = N >> (s + 1);
+      const int B = tid >> s, o = tid & (t - 1);
+      const int e0 = B * 4 * t + o;
+      u64 w0, w0p, w1, w1p, w2, w2p;
+      inv_twiddle(tw, twp, m + 2 * B, w0, w0p);
+      inv_twiddle(tw, twp, m + 2 * B + 1, w1, w1p);
+      inv_twiddle(tw, twp, (m >> 1) + B, w2, w2p);
+      u64 a0 = X[e0], a1 = X[e0 + t], a2 = X[e0 + 2 * t], a3 = X[e0 + 3 * t];
+      bf_inv(a0, a1, w0, w0p);
+      bf_inv(a2, a3, w1, w1p);
+      bf_inv(a0, a2, w2, w2p);
+      bf_inv(a1, a3, w2, w2p);
+      X[e0] = a0;
+      X[e0 + t] = a1;
+      X[e0 + 2 * t] = a2;
+      X[e0 + 3 * t] = a3;
+      __syncthreads();
     }
+    if (s == LOGN - 2) {
+      const int t = 1 << s, m = N >> (s + 1);
+#pragma unroll
+      for (int r = 0; r < 2; r++) {
+        const int v = tid + r * NT;
+        const int B = v >> s, o = v & (t - 1);
+        const int e = B * 2 * t + o;
+        u64 w, wp;
+        inv_twiddle(tw, twp, m + B, w, wp);
+        u64 a = X[e], b = X[e + t];
+        bf_inv(a, b, w, wp);
+        X[e] = a;
+        X[e + t] = b;
+      }
+      __syncthreads();
+    }
+    // Inverse stage logn-1, n^-1, digit split and forward stage 0, per pair (b, b + N/2).
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+      const int b = tid + j * NT;
+      u64 x0 = X[b], x1 = X[b + H];
+      bf_inv(x0, x1, wi, wip);
+      const u64 r0 = shoup(x0, c.ninv, c.ninvp), r1 = shoup(x1, c.ninv, c.ninvp);
+      u64 p0, p1, q0, q1;  // digits 0 and 1 of coefficients b and b + N/2
+      if (exact) {
+        p0 = r0 & DMASK;
+        p1 = (r0 >> 20) & DMASK;
+        q0 = r1 & DMASK;
+        q1 = (r1 >> 20) & DMASK;
+      } else {
+        const u64 rr0 = (r0 + (1ULL << 19)) >> 20, rr1 = (r1 + (1ULL << 19)) >> 20;
+        p0 = rr0 & DMASK;
+        p1 = rr0 >> 20;
+        q0 = rr1 & DMASK;
+        q1 = rr1 >> 20;
+      }
+      const u64 t0 = shoup_lazy(q0, wf, wfp), t1 = shoup_lazy(q1, wf, wfp);
+      D[b] = p0 + t0;
+      D[b + H] = p0 + 2 * Q - t0;
+      D[N + b] = p1 + t1;
+      D[N + b + H] = p1 + 2 * Q - t1;
+    }
+    __syncthreads();
+    // Forward stages 1 .. logn-3 (a radix-2 stage first when logn is even), both digits.
+    s = 1;
+    if (!(LOGN & 1)) {
+      const int lt = LOGN - 2, t = 1 << lt;
+#pragma unroll
+      for (int r = 0; r < 2; r++) {
+        const int v = tid + r * NT;
+        const int ib = v >> lt, o = v & (t - 1);
+        const int e = ib * 2 * t + o;
+        const u64 w = tw[2 + ib], wp = twp[2 + ib];
+#pragma unroll
+        for (int k = 0; k < 2; k++) {
+          u64* x = D + k * N;
+          u64 a = x[e], b = x[e + t];
+          bf_fwd(a, b, w, wp);
+          x[e] = a;
+          x[e + t] = b;
+        }
+      }
+      __syncthreads();
+      s = 2;
+    }
+#pragma unroll 1
+    for (; s < LOGN - 2; s += 2) {
+      const int t = N >> (s + 1), m = 1 << s, h = t >> 1;
+      const int ib = tid / h, o = tid - ib * h;
+      const int e0 = ib * 2 * t + o;
+      const u64 wa = tw[m + ib], wap = twp[m + ib];
+      const u64 wb = tw[2 * m + 2 * ib], wbp = twp[2 * m + 2 * ib];
+      const u64 wc = tw[2 * m + 2 * ib + 1], wcp = twp[2 * m + 2 * ib + 1];
+      u64* x0 = D + e0;
+      u64* x1 = D + N + e0;
+      u64 a0 = x0[0], a1 = x0[h], a2 = x0[t], a3 = x0[t + h];
+      u64 c0 = x1[0], c1 = x1[h], c2 = x1[t], c3 = x1[t + h];
+      bf_fwd(a0, a2, wa, wap);
+      bf_fwd(c0, c2, wa, wap);
+      bf_fwd(a1, a3, wa, wap);
+      bf_fwd(c1, c3, wa, wap);
+      bf_fwd(a0, a1, wb, wbp);
+      bf_fwd(c0, c1, wb, wbp);
+      bf_fwd(a2, a3, wc, wcp);
+      bf_fwd(c2, c3, wc, wcp);
+      x0[0] = a0;
+      x0[h] = a1;
+      x0[t] = a2;
+      x0[t + h] = a3;
+      x1[0] = c0;
+      x1[h] = c1;
+      x1[t] = c2;
+      x1[t + h] = c3;
+      __syncthreads();
+    }
+    // Forward stages logn-2, logn-1 of unit tid, both digits, in registers.
+    u64 d0[4], d1[4];
+    {
+      const u64 fa = tw[MF + tid], fap = twp[MF + tid];
+      const u64 fb = tw[2 * MF + 2 * tid], fbp = twp[2 * MF + 2 * tid];
+      const u64 fc = tw[2 * MF + 2 * tid + 1], fcp = twp[2 * MF + 2 * tid + 1];
+      const ulonglong2 v01 = *reinterpret_cast<const ulonglong2*>(D + l0);
+      const ulonglong2 v23 = *reinterpret_cast<const ulonglong2*>(D + l0 + 2);
+      const ulonglong2 g01 = *reinterpret_cast<const ulonglong2*>(D + N + l0);
+      const ulonglong2 g23 = *reinterpret_cast<const ulonglong2*>(D + N + l0 + 2);
+      d0[0] = v01.x, d0[1] = v01.y, d0[2] = v23.x, d0[3] = v23.y;
+      d1[0] = g01.x, d1[1] = g01.y, d1[2] = g23.x, d1[3] = g23.y;
+      bf_fwd(d0[0], d0[2], fa, fap);
+      bf_fwd(d1[0], d1[2], fa, fap);
+      bf_fwd(d0[1], d0[3], fa, fap);
+      bf_fwd(d1[1], d1[3], fa, fap);
+      bf_fwd(d0[0], d0[1], fb, fbp);
+      bf_fwd(d1[0], d1[1], fb, fbp);
+      bf_fwd(d0[2], d0[3], fc, fcp);
+      bf_fwd(d1[2], d1[3], fc, fcp);
+    }
+    const u64 sv[4] = {sv01.x, sv01.y, sv23.x, sv23.y};
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-      const int t = tid + k * NT;
       const u32 tb = s_tab[((gp * et[k]) & M2N) >> 1];
-      const u64 d0 = bufB[t], d1 = bufC[t];
-      u128 nb = wide(d0, Y[tb]) + wide(d1, Y[N + tb]);
-      u128 nc = wide(a_ntt[tb], sv[k]) + wide(d0, Wm[tb]) + wide(d1, Wm[N + tb]);
+      u128 nb = wide(d0[k], Y[tb]) + wide(d1[k], Y[N + tb]);
+      u128 nc = wide(a_ntt[tb], sv[k]) + wide(d0[k], Wm[tb]) + wide(d1[k], Wm[N + tb]);
       if (exact) {
-        const u64 d2 = bufA[t];
+        const u64 d2 = redc(wide(cur[k], c.ld_inv_R) + wide(d0[k], c.ld_c0_R) + wide(d1[k], c.ld_c1_R));
         nb += wide(d2, Y[2 * N + tb]);
         nc += wide(d2, Wm[2 * N + tb]);
       }
@@ -614,21 +743,22 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
       cur[k] = redc(nc);
     }
   }
+  __syncthreads();  // every thread is past its last read of D
 #pragma unroll
   for (int k = 0; k < 4; k++) {
-    bufA[tid + k * NT] = cur[k];
-    bufB[tid + k * NT] = sb[k];
+    D[l0 + k] = cur[k];
+    D[N + l0 + k] = sb[k];
   }
   __syncthreads();
   {
-    u64* const bufs[2] = {bufA, bufB};
+    u64* const bufs[2] = {D, D + N};
     ntt_inv_r4<LOGN, NT, 2>(bufs, tw, twp);
   }
 #pragma unroll
   for (int k = 0; k < 4; k++) {
     const int t = tid + k * NT;
-    a_out[(size_t)qi * N + t] = finish_a(c, bufA[t], ms_target);
-    b_out[(size_t)qi * N + t] = finish_b(c, bufB[t], t, qi, b_fold, ms_target);
+    a_out[(size_t)qi * N + t] = finish_a(c, D[t], ms_target);
+    b_out[(size_t)qi * N + t] = finish_b(c, D[N + t], t, qi, b_fold, ms_target);
   }
 }
 

@@ -146,6 +146,8 @@ std::atomic<u64> g_next_object{1};
 
 }  // namespace
 
+enum : u32 { IG_MAX_LANES = 8 };
+
 struct ig_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -178,6 +180,13 @@ struct ig_ctx {
   // Batches of at most this many queries run two CTAs per query (a cluster of two), so
   // a batch smaller than the SM count still occupies most SMs. Default: half the SMs.
   u32 pair_threshold = 0;
+  // Device-path lanes: with lanes > 1, consecutive ig_respond_seeded_batch_device calls
+  // rotate over that many streams, each with its own scratch, so batches overlap on the
+  // device; ig_ctx_join orders the context stream after all of them.
+  u32 lanes = 1, lane_next = 0, sms = 0;
+  cudaStream_t lane_stream[IG_MAX_LANES] = {};
+  cudaEvent_t lane_in[IG_MAX_LANES] = {}, lane_done[IG_MAX_LANES] = {};
+  bool lane_used[IG_MAX_LANES] = {};
   // special_modulus objects (ig_sm_runtime.cu) and their destructor.
   void* sm = nullptr;
   void (*sm_destroy)(ig_ctx*, void*) = nullptr;
@@ -188,7 +197,7 @@ namespace {
 enum Region { REGION_SCAN = 0, REGION_RESPOND = 1, REGION_FOLD = 2, REGION_COUNT = 3 };
 
 // Starts a profiled region on the context stream; returns the pool slot or -1.
-long prof_begin(ig_ctx* c, int region) {
+long prof_begin(ig_ctx* c, int region, cudaStream_t st = nullptr) {
   c->launches++;
   if (!c->profile) return -1;
   size_t k = c->ev_used.size();
@@ -198,11 +207,11 @@ long prof_begin(ig_ctx* c, int region) {
     c->ev_pool.push_back({a, b});
   }
   c->ev_used.push_back({region, k});
-  cudaEventRecord(c->ev_pool[k].first, c->stream);
+  cudaEventRecord(c->ev_pool[k].first, st ? st : c->stream);
   return (long)k;
 }
-void prof_end(ig_ctx* c, long k) {
-  if (k >= 0) cudaEventRecord(c->ev_pool[k].second, c->stream);
+void prof_end(ig_ctx* c, long k, cudaStream_t st = nullptr) {
+  if (k >= 0) cudaEventRecord(c->ev_pool[k].second, st ? st : c->stream);
 }
 
 int fail(ig_ctx* c, int code, const char* fmt, ...) {
@@ -412,6 +421,7 @@ int stage_h2d(ig_ctx* c, void* dst, const void* src, size_t bytes) { return ::st
 void add_launches(ig_ctx* c, unsigned n) { c->launches += n; }
 void*& sm_slot(ig_ctx* c) { return c->sm; }
 int pair_threshold(ig_ctx* c) { return (int)c->pair_threshold; }
+int sm_count(ig_ctx* c) { return (int)c->sms; }
 void set_sm_destructor(ig_ctx* c, void (*fn)(ig_ctx*, void*)) { c->sm_destroy = fn; }
 }  // namespace igint
 
@@ -433,6 +443,7 @@ int ig_ctx_create(int device, ig_ctx** out) {
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
   c->pair_threshold = (u32)(sms / 2);
+  c->sms = (u32)sms;
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
     delete c;
     return IG_ERR_CUDA;
@@ -445,6 +456,14 @@ void ig_ctx_destroy(ig_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
+  for (u32 k = 0; k < IG_MAX_LANES; k++) {
+    if (c->lane_stream[k]) {
+      cudaStreamSynchronize(c->lane_stream[k]);
+      cudaStreamDestroy(c->lane_stream[k]);
+      cudaEventDestroy(c->lane_in[k]);
+      cudaEventDestroy(c->lane_done[k]);
+    }
+  }
   if (c->sm && c->sm_destroy) c->sm_destroy(c, c->sm);
   for (auto& kv : c->crs)
     for (void* p : kv.second.allocs) cudaFree(p);
@@ -454,6 +473,7 @@ void ig_ctx_destroy(ig_ctx* c) {
       cudaFree(s.sums);
       cudaFree(s.tag_key);
       cudaFree(s.tags);
+      cudaFree(s.cols16);
     }
     cudaFree(kv.second.d_table);
   }
@@ -1070,9 +1090,20 @@ int ig_respond_seeded_batch_device(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_
     if (!db->shards[s].sums)
       return fail(c, IG_ERR_ARG, "shard %u has no packing store; the device-resident path serves stored shards", s);
   }
+  // Lane of this call (lanes > 1): its stream and scratch. The lane's scratch is reused
+  // only after the lane's previous batch has finished with it.
+  int lane = -1;
+  cudaStream_t s = c->stream;
+  if (c->lanes > 1) {
+    lane = (int)(c->lane_next++ % c->lanes);
+    s = c->lane_stream[lane];
+    if (c->lane_used[lane]) IG_CUDA(c, cudaStreamWaitEvent(c->stream, c->lane_done[lane], 0));
+  }
+  char qname[32], fname[32];
+  snprintf(qname, sizeof qname, "dev_queries%d", lane);
+  snprintf(fname, sizeof fname, "dev_fold%d", lane);
   void *d_q, *d_fold;
-  if ((rc = scratch(c, "dev_queries", count * sizeof(QueryDev), &d_q)) ||
-      (rc = scratch(c, "dev_fold", count * g * 8, &d_fold)))
+  if ((rc = scratch(c, qname, count * sizeof(QueryDev), &d_q)) || (rc = scratch(c, fname, count * g * 8, &d_fold)))
     return rc;
   std::vector<QueryDev> qs(count);
   for (u32 i = 0; i < count; i++) {
@@ -1083,16 +1114,53 @@ int ig_respond_seeded_batch_device(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_
     qs[i].b = d_bs + (size_t)i * n;
     qs[i].seat_R = seat;
   }
-  cudaStream_t s = c->stream;
   if ((rc = stage_h2d(c, d_q, qs.data(), count * sizeof(QueryDev)))) return rc;
+  if (lane >= 0) {
+    IG_CUDA(c, cudaEventRecord(c->lane_in[lane], c->stream));
+    IG_CUDA(c, cudaStreamWaitEvent(s, c->lane_in[lane], 0));
+  }
   IG_CUDA(c, cudaMemsetAsync(d_status, 0, count * 4, s));
-  long pk = prof_begin(c, REGION_SCAN);
+  long pk = prof_begin(c, REGION_SCAN, s);
   IG_CUDA(c, igk::shard_scan(o.dev, (const QueryDev*)d_q, db->d_table, count, (u64*)d_fold, d_status, 0, nullptr, s));
-  prof_end(c, pk);
-  pk = prof_begin(c, REGION_RESPOND);
+  prof_end(c, pk, s);
+  // Two CTAs per query only while every lane's batch still leaves SMs for them.
+  const bool pair = (u64)count * c->lanes <= c->pair_threshold;
+  pk = prof_begin(c, REGION_RESPOND, s);
   IG_CUDA(c, igk::respond(o.dev, (const QueryDev*)d_q, db->d_table, count, (const u64*)d_fold, ms_target, d_a, d_b,
-                          d_status, c->force_serial, count <= c->pair_threshold, s));
-  prof_end(c, pk);
+                          d_status, c->force_serial, pair, s));
+  prof_end(c, pk, s);
+  if (lane >= 0) {
+    IG_CUDA(c, cudaEventRecord(c->lane_done[lane], s));
+    c->lane_used[lane] = true;
+  }
+  return IG_OK;
+}
+
+int ig_ctx_set_lanes(ig_ctx* c, uint32_t lanes) {
+  if (!c) return IG_ERR_ARG;
+  if (lanes == 0 || lanes > IG_MAX_LANES)
+    return fail(c, IG_ERR_ARG, "ig_ctx_set_lanes: lanes must be 1..%u", (unsigned)IG_MAX_LANES);
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  for (u32 k = 0; k < lanes; k++) {
+    if (c->lane_stream[k]) continue;
+    IG_CUDA(c, cudaStreamCreateWithFlags(&c->lane_stream[k], cudaStreamNonBlocking));
+    IG_CUDA(c, cudaEventCreateWithFlags(&c->lane_in[k], cudaEventDisableTiming));
+    IG_CUDA(c, cudaEventCreateWithFlags(&c->lane_done[k], cudaEventDisableTiming));
+  }
+  // Work already queued on lanes stays ordered before anything the context does next.
+  for (u32 k = 0; k < IG_MAX_LANES; k++)
+    if (c->lane_used[k]) IG_CUDA(c, cudaStreamWaitEvent(c->stream, c->lane_done[k], 0));
+  c->lanes = lanes;
+  c->lane_next = 0;
+  return IG_OK;
+}
+
+int ig_ctx_join(ig_ctx* c) {
+  if (!c) return IG_ERR_ARG;
+  std::lock_guard<std::mutex> lk(c->mu);
+  for (u32 k = 0; k < IG_MAX_LANES; k++)
+    if (c->lane_used[k]) IG_CUDA(c, cudaStreamWaitEvent(c->stream, c->lane_done[k], 0));
   return IG_OK;
 }
 
@@ -1158,6 +1226,8 @@ int ig_profile_read(ig_ctx* c, double* ms, uint64_t* counts, int regions, int re
   if (!c || !ms || !counts || regions <= 0) return IG_ERR_ARG;
   std::lock_guard<std::mutex> lk(c->mu);
   IG_CUDA(c, cudaStreamSynchronize(c->stream));
+  for (u32 k = 0; k < IG_MAX_LANES; k++)
+    if (c->lane_used[k]) IG_CUDA(c, cudaStreamSynchronize(c->lane_stream[k]));
   for (int r = 0; r < regions; r++) {
     ms[r] = 0;
     counts[r] = 0;

@@ -74,6 +74,7 @@ struct Slot {
   u32* h_status = nullptr;
   std::vector<Req*> reqs;
   int launch_err = 0;
+  u32 ctas = 0;  // CTAs of the batch in flight
   bool busy = false;
 };
 
@@ -93,6 +94,7 @@ struct ig_serve {
   std::thread dispatcher, completer;
   u64 next_ticket = 1;
   u64 served = 0, refused = 0, batches = 0, batched_queries = 0;
+  u32 inflight_ctas = 0;  // CTAs of all batches in flight
   std::vector<u64> latencies;
   size_t device_bytes = 0;
 };
@@ -269,6 +271,16 @@ void dispatch_loop(ig_serve* s) {
     Slot& sl = s->slots[k];
     const u32 count = (u32)sl.reqs.size();
     const size_t n = crs.n;
+    // Two CTAs per query only while the SMs left by the batches in flight hold them; with
+    // other batches running, one CTA per query does the same work on fewer SMs.
+    bool pair;
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      pair = (int)count <= igint::pair_threshold(s->ctx) &&
+             s->inflight_ctas + 2 * count <= (u32)igint::sm_count(s->ctx);
+      sl.ctas = pair ? 2 * count : count;
+      s->inflight_ctas += sl.ctas;
+    }
     for (u32 i = 0; i < count; i++) {
       memcpy(sl.h_seeds + (size_t)i * 32, sl.reqs[i]->seed, 32);
       memcpy(sl.h_bs + i * n, sl.reqs[i]->b.data(), n * 8);
@@ -285,8 +297,7 @@ void dispatch_loop(ig_serve* s) {
     if (e == cudaSuccess) e = cudaMemsetAsync(sl.d_status, 0, count * 4, st);
     if (e == cudaSuccess) e = igk::shard_scan(crs, sl.d_q, sl.d_table, count, sl.d_fold, sl.d_status, 0, nullptr, st);
     if (e == cudaSuccess)
-      e = igk::respond(crs, sl.d_q, sl.d_table, count, sl.d_fold, ms, sl.d_a, sl.d_b, sl.d_status, 0,
-                       (int)count <= igint::pair_threshold(s->ctx), st);
+      e = igk::respond(crs, sl.d_q, sl.d_table, count, sl.d_fold, ms, sl.d_a, sl.d_b, sl.d_status, 0, pair, st);
     if (e == cudaSuccess) {
       igint::add_launches(s->ctx, 2);
       e = cudaMemcpyAsync(sl.h_status, sl.d_status, count * 4, cudaMemcpyDeviceToHost, st);
@@ -346,6 +357,8 @@ void complete_loop(ig_serve* s) {
       }
       sl.reqs.clear();
       sl.busy = false;
+      s->inflight_ctas -= sl.ctas;
+      sl.ctas = 0;
     }
     s->cv_slot.notify_all();
     s->cv_done.notify_all();

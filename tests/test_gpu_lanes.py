@@ -1,0 +1,63 @@
+"""Device-resident batches over several lanes (ig_ctx_set_lanes): consecutive batches
+rotate over streams and overlap on the device, and with more than one lane they run one
+CTA per query. Every batch's responses must equal the host-buffer respond_seeded_batch
+answers for the same queries, for one lane and for three."""
+import numpy as np
+import pytest
+
+from conftest import load_package
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def pkg():
+    return load_package()
+
+
+@pytest.mark.parametrize("batch", [8, 32])  # 8 x 3 lanes: two CTAs per query; 32 x 3: one
+def test_lanes_give_the_same_responses(pkg, oracle, batch):
+    torch = pytest.importorskip("torch")
+    ctx = pkg.Context.default()
+    P = oracle.Params.d2048()
+    cell = oracle.Cell(P, 256, 0x1A2E)
+    crs = pkg.ServerCrs(pkg.InspireParams(ring_dim=P.n, p=P.p), cell.w_seed, cell.gamma)
+    cache = pkg.ServerInspiringCache.new(crs, ctx=ctx)
+    db = pkg.EncodedDatabase.from_columns(cache, [cell.columns(s) for s in range(cell.num_shards)])
+    db.precompute_packing_all()
+    store = pkg.ServerSessionStore.new(ctx)
+    h = store.register_server_side(pkg.ClientPackingKeys(cell.keys(), cell.gamma), cache)
+    n, nbatches = P.n, 6
+    total = cell.num_shards * n
+    qs = [[pkg.SeededBatchQuery(*cell.next_query((j * batch + k) * 389 % total)) for k in range(batch)]
+          for j in range(nbatches)]
+    ms = pkg.MOD_SWITCH_TARGET_36BIT
+    want = []
+    for j in range(nbatches):
+        out = pkg.respond_seeded_batch(crs, db, pkg.SeededQueryBatch(pkg.PackingKeySource.Registered(h), qs[j]),
+                                       cache, store, mod_switch_target=ms)
+        want.append((np.stack([r.a for r in out]), np.stack([r.b for r in out])))
+    sids = [np.ascontiguousarray([q.shard_id for q in qs[j]], dtype=np.uint32) for j in range(nbatches)]
+    seeds = torch.from_numpy(np.stack([np.frombuffer(b"".join(q.seed for q in qs[j]), dtype=np.uint8)
+                                       for j in range(nbatches)]).copy()).cuda()
+    bs = torch.from_numpy(np.stack([np.stack([q.b for q in qs[j]]) for j in range(nbatches)]).view(np.int64)).cuda()
+    for lanes in (1, 3):
+        a = torch.zeros((nbatches, batch, n), dtype=torch.int64, device="cuda")
+        b = torch.zeros_like(a)
+        st = torch.ones((nbatches, batch), dtype=torch.int32, device="cuda")
+        torch.cuda.synchronize()
+        ctx.set_lanes(lanes)
+        try:
+            for j in range(nbatches):
+                ctx.check(ctx._lib.ig_respond_seeded_batch_device(
+                    ctx.h, db.h, store.h, int(h), batch, sids[j].ctypes.data, seeds[j].data_ptr(), bs[j].data_ptr(),
+                    ms, a[j].data_ptr(), b[j].data_ptr(), st[j].data_ptr()))
+            ctx.join()
+            torch.cuda.ExternalStream(ctx.stream).synchronize()
+        finally:
+            ctx.set_lanes(1)
+        assert int(st.abs().sum().item()) == 0
+        got_a = a.cpu().numpy().view(np.uint64)
+        got_b = b.cpu().numpy().view(np.uint64)
+        for j in range(nbatches):
+            assert (got_a[j] == want[j][0]).all() and (got_b[j] == want[j][1]).all(), (lanes, j)
