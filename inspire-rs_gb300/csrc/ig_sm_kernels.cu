@@ -258,10 +258,16 @@ __device__ __forceinline__ u32 q_to_p(const SmDev& c, u32 x) {
 //   tp = NTT_p(lift(INTT_q(R_{i+1})));  cp = INTT_p(tp . w_p[tau_i]);  rq = NTT_q(lift(cp));
 //   R_i = a[tau_i] S_i + (R_{i+1} w_q[tau_i] - rq) / p;
 //   acc_q += R_{i+1} key_q[tau_i];  acc_p += tp key_p[tau_i].
+// Thread u owns slots 4u..4u+3 (one transform unit), so the passes that act within a unit
+// run in registers beside the pointwise steps: the first inverse pass of INTT_q, the last
+// forward pass of NTT_p with the products by key_p and w_p and the first inverse pass of
+// INTT_p, and the last forward pass of NTT_q with the link's update. Each inverse's last
+// stage (t = n/2, carrying 1/n), the limb lift and the next forward's first stage (the
+// same index pairs) run as one pass in place.
 template <int LOGN>
 __global__ void __launch_bounds__((1 << LOGN) / 4, 2)
     k_sm_respond(SmDev c, const SmQueryDev* queries, const i64* fold, u32* mask_out, u32* body_out, u32* status) {
-  constexpr int N = 1 << LOGN, NT = N / 4;
+  constexpr int N = 1 << LOGN, NT = N / 4, H = N / 2;
   constexpr u32 M2N = 2 * N - 1;
   extern __shared__ __align__(16) u32 smw[];
   u32* buf = smw;
@@ -295,76 +301,166 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 2)
   sm_expand<N, NT>(qd, PQ.m, a, status, qi);
   fwd32<LOGN>(a, c.lq, fq);
 
+  const int l0 = 4 * tid;
   u32 cur[4], accq[4], accp[4], et[4];
 #pragma unroll
   for (int k = 0; k < 4; k++) {
-    const int t = tid + k * NT;
-    et[k] = e_tab[t];
+    et[k] = e_tab[l0 + k];
     const u32 tb = s_tab[((c.gpow[c.gamma - 1] * et[k]) & M2N) >> 1];
-    cur[k] = PQ.mont(a[tb], qd.step1_R[(size_t)(c.gamma - 1) * N + t]);
+    cur[k] = PQ.mont(a[tb], qd.step1_R[(size_t)(c.gamma - 1) * N + l0 + k]);
     accq[k] = 0;
     accp[k] = 0;
   }
+  // Inverse stages 0-1 of unit tid (t = 1, block tid), in registers, to buf[l0..l0+3].
+  auto inv_first = [&](const Prime32& P, const u32* itw, u32 a0, u32 a1, u32 a2, u32 a3) {
+    const u32 w0 = itw[H + 2 * tid], w1 = itw[H + 2 * tid + 1], w2 = itw[H / 2 + tid];
+    const u32 d01 = P.mont(a0 + P.m - a1, w0);
+    a0 = P.add(a0, a1);
+    const u32 d23 = P.mont(a2 + P.m - a3, w1);
+    a2 = P.add(a2, a3);
+    *reinterpret_cast<uint4*>(buf + l0) =
+        make_uint4(P.add(a0, a2), P.add(d01, d23), P.mont(a0 + P.m - a2, w2), P.mont(d01 + P.m - d23, w2));
+  };
+  // Inverse stages 2 .. logn-2 over buf (radix-4 pairs; logn is odd).
+  auto inv_middle = [&](const Prime32& P, const u32* itw) {
+#pragma unroll 1
+    for (int s = 2; s + 1 < LOGN; s += 2) {
+      const int t = 1 << s, m = N >> (s + 1);
+      const int B = tid >> s, o = tid & (t - 1);
+      const int e0 = B * 4 * t + o;
+      const u32 w0 = itw[m + 2 * B], w1 = itw[m + 2 * B + 1], w2 = itw[(m >> 1) + B];
+      u32 a0 = buf[e0], a1 = buf[e0 + t], a2 = buf[e0 + 2 * t], a3 = buf[e0 + 3 * t];
+      const u32 d01 = P.mont(a0 + P.m - a1, w0);
+      a0 = P.add(a0, a1);
+      const u32 d23 = P.mont(a2 + P.m - a3, w1);
+      a2 = P.add(a2, a3);
+      buf[e0] = P.add(a0, a2);
+      buf[e0 + 2 * t] = P.mont(a0 + P.m - a2, w2);
+      buf[e0 + t] = P.add(d01, d23);
+      buf[e0 + 3 * t] = P.mont(d01 + P.m - d23, w2);
+      __syncthreads();
+    }
+  };
+  // Forward stages 1 .. logn-3 over buf.
+  auto fwd_middle = [&](const Prime32& P, const u32* tw) {
+#pragma unroll 1
+    for (int s = 1; s < LOGN - 2; s += 2) {
+      const int t = N >> (s + 1), m = 1 << s, h = t >> 1;
+      const int i = tid / h, o = tid - i * h;
+      const int e0 = i * 2 * t + o;
+      const u32 wa = tw[m + i], wb = tw[2 * m + 2 * i], wc = tw[2 * m + 2 * i + 1];
+      u32 a0 = buf[e0], a1 = buf[e0 + h], a2 = buf[e0 + t], a3 = buf[e0 + t + h];
+      u32 v = P.mont(a2, wa);
+      a2 = P.sub(a0, v);
+      a0 = P.add(a0, v);
+      v = P.mont(a3, wa);
+      a3 = P.sub(a1, v);
+      a1 = P.add(a1, v);
+      v = P.mont(a1, wb);
+      buf[e0] = P.add(a0, v);
+      buf[e0 + h] = P.sub(a0, v);
+      v = P.mont(a3, wc);
+      buf[e0 + t] = P.add(a2, v);
+      buf[e0 + t + h] = P.sub(a2, v);
+      __syncthreads();
+    }
+  };
+  // Forward stages logn-2, logn-1 of unit tid, in registers, from buf[l0..l0+3].
+  auto fwd_last = [&](const Prime32& P, const u32* tw, u32 (&x)[4]) {
+    constexpr int MF = 1 << (LOGN - 2);
+    const u32 wa = tw[MF + tid], wb = tw[2 * MF + 2 * tid], wc = tw[2 * MF + 2 * tid + 1];
+    const uint4 v4 = *reinterpret_cast<const uint4*>(buf + l0);
+    u32 a0 = v4.x, a1 = v4.y, a2 = v4.z, a3 = v4.w;
+    u32 v = P.mont(a2, wa);
+    a2 = P.sub(a0, v);
+    a0 = P.add(a0, v);
+    v = P.mont(a3, wa);
+    a3 = P.sub(a1, v);
+    a1 = P.add(a1, v);
+    v = P.mont(a1, wb);
+    x[0] = P.add(a0, v);
+    x[1] = P.sub(a0, v);
+    v = P.mont(a3, wc);
+    x[2] = P.add(a2, v);
+    x[3] = P.sub(a2, v);
+  };
 #pragma unroll 1
   for (int i = (int)c.gamma - 2; i >= 0; i--) {
-    const u32* Srow = qd.step1_R + (size_t)i * N;
-    u32 sv[4], tb[4];
+    const uint4 sv4 = *reinterpret_cast<const uint4*>(qd.step1_R + (size_t)i * N + l0);
+    const u32 sv[4] = {sv4.x, sv4.y, sv4.z, sv4.w};
+    u32 tb[4];
     const u32 gp = c.gpow[i];
 #pragma unroll
-    for (int k = 0; k < 4; k++) {
-      const int t = tid + k * NT;
-      sv[k] = Srow[t];
-      tb[k] = s_tab[((gp * et[k]) & M2N) >> 1];
-      buf[t] = cur[k];
+    for (int k = 0; k < 4; k++) tb[k] = s_tab[((gp * et[k]) & M2N) >> 1];
+    inv_first(PQ, iq, cur[0], cur[1], cur[2], cur[3]);
+    __syncthreads();
+    inv_middle(PQ, iq);
+    // INTT_q's last stage with 1/n, the lift to p, and NTT_p's first stage, pair (b, b + n/2).
+#pragma unroll
+    for (int r = 0; r < 2; r++) {
+      const int b = tid + r * NT;
+      const u32 u = buf[b], v = buf[b + H];
+      const u32 y0 = q_to_p(c, PQ.mont(u + v, c.lq.n_inv));
+      const u32 y1 = q_to_p(c, PQ.mont(u + PQ.m - v, c.lq.last));
+      const u32 z = PP.mont(y1, fp[1]);
+      buf[b] = PP.add(y0, z);
+      buf[b + H] = PP.sub(y0, z);
     }
     __syncthreads();
-    inv32<LOGN>(buf, c.lq, iq);
+    fwd_middle(PP, fp);
+    {
+      u32 tp[4], y[4];
+      fwd_last(PP, fp, tp);
 #pragma unroll
-    for (int k = 0; k < 4; k++) buf[tid + k * NT] = q_to_p(c, buf[tid + k * NT]);
-    __syncthreads();
-    fwd32<LOGN>(buf, c.lp, fp);
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-      const int t = tid + k * NT;
-      const u32 tpv = buf[t];
-      accp[k] = PP.add(accp[k], PP.mont(tpv, kp[tb[k]]));
-      buf[t] = PP.mont(tpv, wp[tb[k]]);
+      for (int k = 0; k < 4; k++) {
+        accp[k] = PP.add(accp[k], PP.mont(tp[k], kp[tb[k]]));
+        y[k] = PP.mont(tp[k], wp[tb[k]]);
+      }
+      inv_first(PP, ip, y[0], y[1], y[2], y[3]);
     }
     __syncthreads();
-    inv32<LOGN>(buf, c.lp, ip);
+    inv_middle(PP, ip);
+    // INTT_p's last stage with 1/n, the lift to q, and NTT_q's first stage.
 #pragma unroll
-    for (int k = 0; k < 4; k++) buf[tid + k * NT] = p_to_q(c, buf[tid + k * NT]);
+    for (int r = 0; r < 2; r++) {
+      const int b = tid + r * NT;
+      const u32 u = buf[b], v = buf[b + H];
+      const u32 y0 = p_to_q(c, PP.mont(u + v, c.lp.n_inv));
+      const u32 y1 = p_to_q(c, PP.mont(u + PP.m - v, c.lp.last));
+      const u32 z = PQ.mont(y1, fq[1]);
+      buf[b] = PQ.add(y0, z);
+      buf[b + H] = PQ.sub(y0, z);
+    }
     __syncthreads();
-    fwd32<LOGN>(buf, c.lq, fq);
+    fwd_middle(PQ, fq);
+    u32 rq[4];
+    fwd_last(PQ, fq, rq);
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-      const int t = tid + k * NT;
-      const u32 rq = buf[t];
       const u32 cq = PQ.mont(cur[k], wq[tb[k]]);
       accq[k] = PQ.add(accq[k], PQ.mont(cur[k], kq[tb[k]]));
-      cur[k] = PQ.add(PQ.mont(a[tb[k]], sv[k]), PQ.mont(PQ.sub(cq, rq), c.p_inv_R));
+      cur[k] = PQ.add(PQ.mont(a[tb[k]], sv[k]), PQ.mont(PQ.sub(cq, rq[k]), c.p_inv_R));
     }
   }
   // mask = INTT_q(R_0); body = mod_down(INTT_q(acc_q), INTT_p(acc_p)) + fold.
+  __syncthreads();  // every thread is past its last read of buf
 #pragma unroll
-  for (int k = 0; k < 4; k++) buf[tid + k * NT] = cur[k];
+  for (int k = 0; k < 4; k++) buf[l0 + k] = cur[k];
   __syncthreads();
   inv32<LOGN>(buf, c.lq, iq);
 #pragma unroll
-  for (int k = 0; k < 4; k++) {
-    const int t = tid + k * NT;
-    mask_out[(size_t)qi * N + t] = buf[t];
-    buf[t] = accq[k];
-  }
+  for (int k = 0; k < 4; k++) mask_out[(size_t)qi * N + tid + k * NT] = buf[tid + k * NT];
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < 4; k++) buf[l0 + k] = accq[k];
   __syncthreads();
   inv32<LOGN>(buf, c.lq, iq);
   u32 xq[4];
 #pragma unroll
-  for (int k = 0; k < 4; k++) {
-    const int t = tid + k * NT;
-    xq[k] = buf[t];
-    buf[t] = accp[k];
-  }
+  for (int k = 0; k < 4; k++) xq[k] = buf[tid + k * NT];
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < 4; k++) buf[l0 + k] = accp[k];
   __syncthreads();
   inv32<LOGN>(buf, c.lp, ip);
 #pragma unroll
