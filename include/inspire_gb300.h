@@ -90,6 +90,14 @@ int ig_db_destroy(ig_ctx* ctx, uint64_t db);
 int ig_db_set_shard(ig_ctx* ctx, uint64_t db, uint32_t shard_id, const uint64_t* columns);
 /* Same, from a device pointer (columns already in HBM). */
 int ig_db_set_shard_device(ig_ctx* ctx, uint64_t db, uint32_t shard_id, const uint64_t* d_columns);
+/* encode_database (pir/encode_db.rs:74-134) on the GPU: `nbytes` of concatenated entries
+ * of entry_size bytes, split into shards of ring_dim entries (the last may be partial) and
+ * into ceil(entry_size / 2) columns of 16-bit little-endian words (encode_db.rs:152-168),
+ * written straight into shards 0.. of the database. entry_size must give the CRS's gamma;
+ * the entries must fit the database's shards. records is a host pointer, or a device
+ * pointer when on_device != 0. Existing stores are kept, as with ig_db_set_shard. */
+int ig_db_encode_records(ig_ctx* ctx, uint64_t db, const uint8_t* records, size_t nbytes, uint32_t entry_size,
+                         int on_device);
 /* ShardData::precompute_packing (setup.rs:335-340) -> ShardPackingStore::build
  * (shard_store.rs:86-156): step-1 sums in HBM plus keyed column tags. */
 int ig_db_precompute_packing(ig_ctx* ctx, uint64_t db, uint32_t shard_id);

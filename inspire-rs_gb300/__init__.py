@@ -86,6 +86,7 @@ def _load():
         "ig_db_destroy": (I, [P, U64]),
         "ig_db_set_shard": (I, [P, U64, U32, P]),
         "ig_db_set_shard_device": (I, [P, U64, U32, P]),
+        "ig_db_encode_records": (I, [P, U64, P, ctypes.c_size_t, U32, I]),
         "ig_db_precompute_packing": (I, [P, U64, U32]),
         "ig_db_precompute_packing_all": (I, [P, U64]),
         "ig_db_drop_packing_store": (I, [P, U64, U32]),
@@ -328,6 +329,26 @@ class EncodedDatabase:
         for i, cols in enumerate(shard_columns):
             db.set_shard(i, cols)
         return db
+
+    @staticmethod
+    def from_records(cache, records: bytes, entry_size: int, num_shards: int = None):
+        """encode_database (encode_db.rs:74-134) on the GPU: concatenated entries of
+        entry_size bytes split into shards of ring_dim entries and 16-bit columns."""
+        entries = len(records) // entry_size
+        ring = cache.crs.params.ring_dim
+        db = EncodedDatabase(cache, num_shards or max(1, (entries + ring - 1) // ring))
+        db.encode_records(records, entry_size)
+        return db
+
+    def encode_records(self, records, entry_size: int, device_ptr: int = None, nbytes: int = None):
+        """Writes shards 0.. from concatenated entries (host bytes, or a device pointer with
+        its byte count)."""
+        if device_ptr is not None:
+            self.ctx.check(self.ctx._lib.ig_db_encode_records(self.ctx.h, self.h, ctypes.c_void_p(device_ptr),
+                                                              int(nbytes), int(entry_size), 1))
+            return
+        buf = np.frombuffer(bytes(records), dtype=np.uint8)
+        self.ctx.check(self.ctx._lib.ig_db_encode_records(self.ctx.h, self.h, _ptr(buf), buf.size, int(entry_size), 0))
 
     def set_shard(self, shard_id, columns):
         cols = _u64(columns, (self.num_columns, self.ring_dim))

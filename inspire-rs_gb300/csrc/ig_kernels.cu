@@ -280,11 +280,27 @@ __device__ __forceinline__ void scan_finish(const CrsDev& c, const ShardDev& sh,
   }
 }
 
+// Shared memory of the compact path: the vector V, then per warp a two-stage ring of the
+// column chunks its lanes copy ahead (cp.async), so the next step's loads are in flight
+// while the current step's products run.
+constexpr int SCAN_STAGES = 2;
+__host__ __device__ constexpr size_t scan_smem_bytes(int n) {
+  return (size_t)n * 16 + (size_t)SCAN_WARPS * SCAN_STAGES * SCAN_ROWS * 32 * 16;
+}
+
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
+  const unsigned addr = (unsigned)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(addr), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
 template <int LOGN>
 __global__ void __launch_bounds__(SCAN_WARPS * 32, 2) k_scan(CrsDev c, const QueryDev* queries, const ShardDev* shards,
                                                           u64* b_fold, u32* status, int build, u64* tags_out) {
-  constexpr int N = 1 << LOGN, M = N / 8;
-  __shared__ __align__(16) uint4 V[N];  // [8][M]: key[2k] lo, hi, b_rev[k] lo, hi
+  constexpr int N = 1 << LOGN, M = N / 8, ITER = M / 32;
+  extern __shared__ __align__(16) uint4 scan_sm[];
+  uint4* V = scan_sm;  // [8][M]: key[2k] lo, hi, b_rev[k] lo, hi
   const u32 qi = blockIdx.y;
   const QueryDev qd = queries[qi];
   const ShardDev sh = shards[qd.shard];
@@ -294,6 +310,20 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32, 2) k_scan(CrsDev c, const Que
   const u64* b = qd.b;
 
   if (sh.cols16 && b && !build) {
+    const int rows = j0 < c.gamma ? min(SCAN_ROWS, (int)(c.gamma - j0)) : 0;
+    const uint16_t* col = sh.cols16 + (size_t)j0 * N;
+    uint4* ring = scan_sm + N + (size_t)warp * SCAN_STAGES * SCAN_ROWS * 32;
+    // Lane l copies, for step it, the 16-byte chunk at positions 8m..8m+7 (m = l + 32 it)
+    // of each of the warp's rows into its own ring slots.
+    auto issue = [&](int it) {
+      if (it < ITER) {
+        uint4* dst = ring + (it % SCAN_STAGES) * SCAN_ROWS * 32 + lane;
+        const int m = lane + 32 * it;
+        for (int r = 0; r < rows; r++) cp_async16(dst + r * 32, col + (size_t)r * N + 8 * m);
+      }
+      cp_async_commit();
+    };
+    issue(0);
 #pragma unroll
     for (int k = threadIdx.x; k < N; k += SCAN_WARPS * 32) {
       const u64 kv = key[2 * k];
@@ -301,18 +331,22 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32, 2) k_scan(CrsDev c, const Que
       V[(k & 7) * M + (k >> 3)] = make_uint4((u32)kv, (u32)(kv >> 32), (u32)bv, (u32)(bv >> 32));
     }
     __syncthreads();
-    if (j0 >= c.gamma) return;
-    const int rows = min(SCAN_ROWS, (int)(c.gamma - j0));
+    if (rows == 0) {
+      asm volatile("cp.async.wait_all;\n" ::: "memory");
+      return;
+    }
     u64 tl[SCAN_ROWS], th[SCAN_ROWS], fl[SCAN_ROWS], fh[SCAN_ROWS];
 #pragma unroll
     for (int r = 0; r < SCAN_ROWS; r++) tl[r] = th[r] = fl[r] = fh[r] = 0;
-    const uint16_t* col = sh.cols16 + (size_t)j0 * N;
 #pragma unroll 1
-    for (int m = lane; m < M; m += 32) {
+    for (int it = 0; it < ITER; it++) {
+      issue(it + 1);
+      cp_async_wait_one();  // step it's copies have landed (only step it+1's may be pending)
+      const int m = lane + 32 * it;
+      const uint4* src = ring + (it % SCAN_STAGES) * SCAN_ROWS * 32 + lane;
       uint4 w[SCAN_ROWS];
 #pragma unroll
-      for (int r = 0; r < SCAN_ROWS; r++)
-        w[r] = r < rows ? *reinterpret_cast<const uint4*>(col + (size_t)r * N + 8 * m) : make_uint4(0, 0, 0, 0);
+      for (int r = 0; r < SCAN_ROWS; r++) w[r] = r < rows ? src[r * 32] : make_uint4(0, 0, 0, 0);
 #pragma unroll
       for (int p = 0; p < 8; p++) {
         const uint4 v = V[p * M + m];
@@ -326,6 +360,7 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32, 2) k_scan(CrsDev c, const Que
         }
       }
     }
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
 #pragma unroll
     for (int r = 0; r < SCAN_ROWS; r++) {
 #pragma unroll
@@ -387,6 +422,27 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32, 2) k_scan(CrsDev c, const Que
       scan_finish(c, sh, qi, j, tag, (u128)hq * r64 + lq, b_fold, status, build, tags_out);
     }
   }
+}
+
+// encode_database's column split (pir/encode_db.rs:74-168) for one shard: column j, row k
+// holds bytes 2j and 2j+1 of entry k little-endian (one byte when the entry ends there,
+// zero past it), rows past `entries` are zero. Writes the u64 words and their u16 copy.
+__global__ void k_encode_records(const uint8_t* rec, u32 entries, u32 entry_size, u32 n, u32 gamma, u64* cols,
+                                 uint16_t* cols16) {
+  const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (size_t)gamma * n) return;
+  const u32 j = (u32)(idx / n), k = (u32)(idx % n);
+  u32 v = 0;
+  if (k < entries) {
+    const uint8_t* e = rec + (size_t)k * entry_size;
+    const u32 off = 2 * j;
+    if (off + 1 < entry_size)
+      v = (u32)e[off] | ((u32)e[off + 1] << 8);
+    else if (off < entry_size)
+      v = e[off];
+  }
+  cols[idx] = v;
+  cols16[idx] = (uint16_t)v;
 }
 
 // Compact copy of a shard's columns: out[k] = w[k] when every word is below 2^16; any
@@ -1137,9 +1193,20 @@ cudaError_t shard_scan(const CrsDev& c, const QueryDev* queries, const ShardDev*
   if (nq == 0) return cudaSuccess;
   constexpr u32 per_cta = SCAN_WARPS * SCAN_ROWS;
   dim3 grid((c.gamma + per_cta - 1) / per_cta, nq);
+  const size_t smem = scan_smem_bytes((int)c.n);
   IG_DISPATCH_LOGN(c.logn, {
-    k_scan<L><<<grid, SCAN_WARPS * 32, 0, s>>>(c, queries, shards, b_fold, status, mode_build, tags_out);
+    auto k = k_scan<L>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k<<<grid, SCAN_WARPS * 32, smem, s>>>(c, queries, shards, b_fold, status, mode_build, tags_out);
   });
+  return cudaGetLastError();
+}
+
+cudaError_t encode_records(const uint8_t* rec, u32 entries, u32 entry_size, u32 n, u32 gamma, u64* cols,
+                           uint16_t* cols16, cudaStream_t s) {
+  const size_t words = (size_t)gamma * n;
+  k_encode_records<<<(unsigned)((words + 255) / 256), 256, 0, s>>>(rec, entries, entry_size, n, gamma, cols, cols16);
   return cudaGetLastError();
 }
 

@@ -68,6 +68,11 @@ cudaError_t ntt_rows(const CrsDev& c, const u64* in, u64* out, u32 rows, u64 sca
 cudaError_t shard_scan(const CrsDev& c, const QueryDev* queries, const ShardDev* shards, u32 nq,
                        u64* b_fold, u32* status, int mode_build, u64* tags_out, cudaStream_t s);
 
+// One shard's columns from its records (entries of entry_size bytes, at most n of them):
+// the gamma x n u64 words and their u16 copy.
+cudaError_t encode_records(const uint8_t* rec, u32 entries, u32 entry_size, u32 n, u32 gamma, u64* cols,
+                           uint16_t* cols16, cudaStream_t s);
+
 // Compact u16 copy of `words` column words (a multiple of 8); sets *wide when a word is
 // 2^16 or above (the copy is then unusable).
 cudaError_t compact16(const u64* cols, size_t words, uint16_t* out, u32* wide, cudaStream_t s);

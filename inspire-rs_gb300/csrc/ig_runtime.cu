@@ -3,6 +3,7 @@
 // the reference's refusal rules, and the launch sequence of a respond batch.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <atomic>
 #include <cstdarg>
 #include <cstdio>
@@ -719,6 +720,63 @@ static int set_shard(ig_ctx* c, uint64_t dbh, uint32_t s, const uint64_t* cols, 
   IG_CUDA(c, cudaStreamSynchronize(c->stream));
   sl.compact = wide_h == 0;
   return sync_table_entry(c, *db, s);
+}
+
+int ig_db_encode_records(ig_ctx* c, uint64_t dbh, const uint8_t* records, size_t nbytes, uint32_t entry_size,
+                         int on_device) {
+  if (!c) return IG_ERR_ARG;
+  if (!records || entry_size == 0) return fail(c, IG_ERR_ARG, "encode_database: null records or entry_size 0");
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  DbObj* db = get_db(c, dbh);
+  if (!db) return fail(c, IG_ERR_HANDLE, "unknown database handle %llu", (unsigned long long)dbh);
+  CrsObj& o = *get_crs(c, db->crs);
+  const u32 n = o.n, g = o.gamma;
+  const u32 columns = (entry_size + 1) / 2;  // num_columns (lib.rs): one column per 16 bits
+  if (columns != g)
+    return fail(c, IG_ERR_WIDTH,
+                "encode_database: entry_size %u gives %u columns, the server packs gamma = %u (the CRS's "
+                "inspiring_num_columns)",
+                entry_size, columns, g);
+  const size_t entries = nbytes / entry_size;
+  const size_t shards = (entries + n - 1) / n;
+  if (shards > db->num_shards)
+    return fail(c, IG_ERR_ARG, "encode_database: %zu entries fill %zu shards of %u; the database holds %u", entries,
+                shards, n, db->num_shards);
+  const size_t shard_bytes = (size_t)n * entry_size;
+  void* staging = nullptr;
+  if (!on_device) {
+    int rc = scratch(c, "encode_records", shard_bytes, &staging);
+    if (rc) return rc;
+  }
+  for (size_t s = 0; s < shards; s++) {
+    ShardSlot& sl = db->shards[s];
+    const size_t words = (size_t)g * n;
+    if (!sl.cols) {
+      int rc = dalloc(c, (void**)&sl.cols, words * 8, &db->bytes);
+      if (rc) return rc;
+    }
+    if (!sl.cols16) {
+      int rc = dalloc(c, (void**)&sl.cols16, words * 2, &db->bytes);
+      if (rc) return rc;
+    }
+    const size_t first = s * n;
+    const u32 count = (u32)std::min<size_t>(n, entries - first);
+    const uint8_t* src = records + first * entry_size;
+    if (!on_device) {
+      int rc = stage_h2d(c, staging, src, (size_t)count * entry_size);
+      if (rc) return rc;
+      src = (const uint8_t*)staging;
+    }
+    IG_CUDA(c, igk::encode_records(src, count, entry_size, n, g, sl.cols, sl.cols16, c->stream));
+    c->launches++;
+    sl.compact = true;
+    // The staging buffer is reused by the next shard only after this encode has read it.
+    if (!on_device) IG_CUDA(c, cudaStreamSynchronize(c->stream));
+    int rc = sync_table_entry(c, *db, (u32)s);
+    if (rc) return rc;
+  }
+  return IG_OK;
 }
 
 int ig_db_set_shard(ig_ctx* c, uint64_t db, uint32_t s, const uint64_t* cols) {

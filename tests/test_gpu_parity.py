@@ -229,3 +229,30 @@ def test_batch_across_many_shards(pkg, oracle, ctx, launch_shape):
         assert cell.decode(i, r.a, r.b)[0]
         if k < 6:
             assert r.to_binary() == oracle_bytes(oracle, cell, P, *raw[k])
+
+
+def test_d256_single_prime_kat_lines_on_gpu(pkg, oracle, ctx, recorded_lines, launch_shape):
+    """The reference's d256 single-prime RESP lines (gamma 1, 2, 16, 32 and 128) from the GPU,
+    per-query branch and store branch: small and partial scan rows, a one-link and a
+    no-link recursion, and the even-log-n transforms."""
+    P = oracle.Params(n=256)
+    rec = set(recorded_lines)
+    for entry in [2, 4, 32, 64, 256]:
+        seed = 0x534D4100 + entry
+        cell, crs, cache, db, keys = gpu_cell(pkg, oracle, P, entry, seed)
+        qs = []
+        for idx in [0, 255, 256, 511, 700]:
+            sid, qseed, b = cell.next_query(idx)
+            qs.append((idx, pkg.SeededBatchQuery(sid, qseed, b)))
+        for idx, q in qs:
+            r = pkg.respond_seeded_inspiring(crs, db, pkg.SeededClientQuery(q.shard_id, q.seed, q.b,
+                                                                            inspiring_packing_keys=keys))
+            wire = r.to_binary()
+            line = f"RESP d256-single-l3 entry={entry} seed={seed:#x} index={idx} len={len(wire)} fnv={oracle.fnv1a(wire):#018x}"
+            assert line in rec, line
+        db.precompute_packing_all()
+        batch = pkg.SeededQueryBatch(pkg.PackingKeySource.Inline(keys), [q for _, q in qs])
+        for (idx, _), r in zip(qs, pkg.respond_seeded_batch(crs, db, batch, cache)):
+            wire = r.to_binary()
+            line = f"RESP d256-single-l3 entry={entry} seed={seed:#x} index={idx} len={len(wire)} fnv={oracle.fnv1a(wire):#018x}"
+            assert line in rec, line
