@@ -539,6 +539,97 @@ def run_sm(args, rank, world):
     }
 
 
+# ------------------------------------------------------------------------------------
+# Serving sweep (the survey's config 5): 2^25 records of 512 B (16,384 shards, 16 GiB of
+# records) encoded on the GPU, a store on every shard, 1000 registered seats, requests with
+# uniform index and seat through the continuous-batching loop, driven natively: a closed
+# loop to saturation, then Poisson arrivals at fractions of the saturation rate.
+C5_SHARDS = 16384
+C5_SEATS = 1000
+C5_METRIC = ("served queries/s at saturation (continuous batching, 2^25 x 512 B records, 16,384 shards, "
+             "1000 seats, 36-bit mod switch)")
+
+
+def run_cfg5(args, rank, world):
+    import torch
+
+    from __graft_entry__ import _package
+    pkg = _package()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    ctx = pkg.Context(local)
+    shards = args.shards if args.shards != NUM_SHARDS else C5_SHARDS
+    rng = np.random.default_rng(6 + rank)
+    crs = pkg.ServerCrs(pkg.InspireParams.d2048(), rng.integers(0, 256, 32, dtype=np.uint8).tobytes(), GAMMA)
+    cache = pkg.ServerInspiringCache.new(crs, ctx=ctx)
+    db = pkg.EncodedDatabase(cache, shards)
+    g = torch.Generator(device="cuda")
+    g.manual_seed(6 + rank)
+    t0 = time.perf_counter()
+    chunk = 512  # shards per piece of records generated on the device (512 MiB)
+    for s0 in range(0, shards, chunk):
+        k = min(chunk, shards - s0)
+        rec = torch.randint(0, 256, (k * N_RING * ENTRY_BYTES,), dtype=torch.uint8, device="cuda", generator=g)
+        torch.cuda.current_stream().synchronize()
+        db.encode_records(None, ENTRY_BYTES, device_ptr=rec.data_ptr(), nbytes=rec.numel(), first_shard=s0)
+        del rec
+    encode_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    db.precompute_packing_all()
+    store_s = time.perf_counter() - t0
+    torch.cuda.empty_cache()
+    store = pkg.ServerSessionStore.new(ctx)
+    seats = [store.register_server_side(pkg.ClientPackingKeys(rand_words(rng, (3, N_RING)), GAMMA), cache)
+             for _ in range(C5_SEATS)]
+    count = args.requests
+    shard_ids = rng.integers(0, shards, count).astype(np.uint32)
+    handles = np.array([int(seats[i]) for i in rng.integers(0, C5_SEATS, count)], dtype=np.uint64)
+    seeds = rng.integers(0, 256, (count, 32), dtype=np.uint8)
+    bs = rand_words(rng, (count, N_RING))
+    out = {"metric": C5_METRIC, "unit": "queries/s", "n_gpus": world, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "u64 (exact mod q = 2^60-2^14+1)",
+           "data": "synthetic: uniform record bytes encoded on the GPU, uniform key and query words",
+           "config": {"workload": "d2048 TwoPacking, 512-byte records x 2^25 (16,384 shards), store on every "
+                                  "shard, 1000 seats, uniform index and seat per request, 36-bit mod switch",
+                      "shards": shards, "records": shards * N_RING, "seats": C5_SEATS, "requests": count,
+                      "slots": 3, "max_batch": BATCH},
+           "setup_s": {"encode_records": encode_s, "precompute_packing": store_s},
+           "device_bytes": ctx.device_bytes}
+    with pkg.ServingLoop(ctx, slots=3, max_batch=BATCH) as loop:
+        w = min(count, 512)
+        loop.replay(db, store, shard_ids[:w], handles[:w], seeds[:w], bs[:w], MS_TARGET, window=256)  # warm-up
+        with ClockSampler(local) as clk:
+            _, _, lat, el = loop.replay(db, store, shard_ids, handles, seeds, bs, MS_TARGET, window=4 * 3 * BATCH)
+        sat = count / el
+        lat_ms = np.sort(lat) / 1e6
+        out["value"] = sat
+        out["saturation"] = {"queries_per_s": sat, "p50_ms": float(lat_ms[len(lat_ms) // 2]),
+                             "p99_ms": float(lat_ms[int(0.99 * (len(lat_ms) - 1))]),
+                             "window": 4 * 3 * BATCH}
+        out["clocks"] = clk.summary()
+        sweep = []
+        for frac in (0.25, 0.5, 0.75, 0.9):
+            rate = frac * sat
+            n = min(count, max(256, int(rate * 0.6)))
+            arr = np.cumsum(rng.exponential(1e9 / rate, n)).astype(np.uint64)
+            _, _, lat, el = loop.replay(db, store, shard_ids[:n], handles[:n], seeds[:n], bs[:n], MS_TARGET,
+                                        arrival_ns=arr)
+            lat_ms = np.sort(lat) / 1e6
+            sweep.append({"offered_per_s": rate, "queries_per_s": n / el, "requests": n,
+                          "p50_ms": float(lat_ms[len(lat_ms) // 2]),
+                          "p99_ms": float(lat_ms[int(0.99 * (len(lat_ms) - 1))])})
+        out["poisson_sweep"] = sweep
+        st = loop.stats()
+        out["mean_batch"] = st["mean_batch"]
+    out["e2e"] = {"value": out["value"], "unit": "queries/s", "h2d_bytes_per_step": BATCH * (32 + N_RING * 8 + 8),
+                  "d2h_bytes_per_step": BATCH * 2 * N_RING * 8,
+                  "note": "the loop's closed-loop rate: host buffers in, host buffers out"}
+    out["steps"] = count // BATCH
+    out["warmup"] = 1
+    out["ms_per_step"] = 1e3 * BATCH / out["value"]
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -548,8 +639,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--lanes", type=int, default=3,
                     help="streams consecutive batches rotate over in the device-resident timed region")
-    ap.add_argument("--config", type=int, default=2, choices=[2, 3],
-                    help="2: served InspiRING batch (the headline); 3: special_modulus batch")
+    ap.add_argument("--config", type=int, default=2, choices=[2, 3, 5],
+                    help="2: served InspiRING batch (the headline); 3: special_modulus batch; "
+                         "5: serving sweep over 16,384 shards and 1000 seats")
+    ap.add_argument("--requests", type=int, default=16384, help="trace length of the serving sweep (config 5)")
     ap.add_argument("--shards", type=int, default=NUM_SHARDS,
                     help="shards in the database (smaller values only for profiling captures)")
     args = ap.parse_args()
@@ -565,6 +658,11 @@ def main():
                 "impl": "reference", "cpu_baseline": cb,
                 "e2e": {"value": cb["value"], "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
+        return
+    if args.config == 5:
+        line = run_cfg5(args, rank, world)
+        if rank == 0:
+            print(json.dumps(line))
         return
     if args.config == 3:
         line = run_sm(args, rank, world)

@@ -93,11 +93,12 @@ int ig_db_set_shard_device(ig_ctx* ctx, uint64_t db, uint32_t shard_id, const ui
 /* encode_database (pir/encode_db.rs:74-134) on the GPU: `nbytes` of concatenated entries
  * of entry_size bytes, split into shards of ring_dim entries (the last may be partial) and
  * into ceil(entry_size / 2) columns of 16-bit little-endian words (encode_db.rs:152-168),
- * written straight into shards 0.. of the database. entry_size must give the CRS's gamma;
- * the entries must fit the database's shards. records is a host pointer, or a device
- * pointer when on_device != 0. Existing stores are kept, as with ig_db_set_shard. */
-int ig_db_encode_records(ig_ctx* ctx, uint64_t db, const uint8_t* records, size_t nbytes, uint32_t entry_size,
-                         int on_device);
+ * written straight into shards first_shard.. of the database (a large database is encoded
+ * in pieces of whole shards). entry_size must give the CRS's gamma; the entries must fit
+ * the database's shards. records is a host pointer, or a device pointer when
+ * on_device != 0. Existing stores are kept, as with ig_db_set_shard. */
+int ig_db_encode_records(ig_ctx* ctx, uint64_t db, uint32_t first_shard, const uint8_t* records, size_t nbytes,
+                         uint32_t entry_size, int on_device);
 /* ShardData::precompute_packing (setup.rs:335-340) -> ShardPackingStore::build
  * (shard_store.rs:86-156): step-1 sums in HBM plus keyed column tags. */
 int ig_db_precompute_packing(ig_ctx* ctx, uint64_t db, uint32_t shard_id);
@@ -245,6 +246,17 @@ int ig_serve_submit(ig_serve* s, uint64_t db, uint64_t store, uint64_t handle, u
                     uint64_t* a_out, uint64_t* b_out, uint64_t* ticket_out);
 int ig_serve_wait(ig_serve* s, uint64_t ticket, int64_t timeout_ms, uint64_t* latency_ns, char* err, size_t err_len);
 int ig_serve_stats(ig_serve* s, ig_serve_stats_t* out, int reset);
+/* Native load driver for the loop: submits a trace of `count` requests (request i reads
+ * shard_ids[i] under seat handles[i] with seed seeds[32 i..] and b bs[ring_dim i..]) from
+ * the calling thread, each at t0 + arrival_ns[i] when arrival_ns is given (open loop), and
+ * with at most `window` requests outstanding when window != 0 (closed loop). Returns when
+ * every request has finished; a_out/b_out receive the responses (ring_dim words each),
+ * latency_ns (optional) each request's submit-to-result time, elapsed_s the trace's
+ * duration. The status is the first request's failure, IG_OK when all were served. */
+int ig_serve_replay(ig_serve* s, uint64_t db, uint64_t store, uint32_t count, const uint32_t* shard_ids,
+                    const uint64_t* handles, const uint8_t* seeds, const uint64_t* bs, uint32_t ring_dim,
+                    uint64_t mod_switch_target, const uint64_t* arrival_ns, uint32_t window, uint64_t* a_out,
+                    uint64_t* b_out, uint64_t* latency_ns, double* elapsed_s);
 int ig_serve_destroy(ig_serve* s);
 
 /* ---- wire ------------------------------------------------------------------------------
@@ -254,6 +266,15 @@ int ig_serve_destroy(ig_serve* s);
  * (the mod-switch target after a switch). Writes at most cap bytes; *len_out = size. */
 int ig_response_encode(const uint64_t* a, const uint64_t* b, uint32_t ring_dim, uint32_t retained, uint64_t modulus,
                        uint8_t* out, size_t cap, size_t* len_out);
+/* The same bytes for `count` device-resident responses (d_a, d_b: count x ring_dim words)
+ * into d_out (count x *len_out bytes, response r at r * *len_out), enqueued on the context
+ * stream: the wire is built next to the responses, and only its bytes cross to the host
+ * (10,446 B per query at the 36-bit switch instead of 32 KiB of words). d_status[r] gets
+ * bit 1 when a coefficient is not below the modulus. With d_out null, only *len_out is
+ * set. modulus must be at least 2^8. */
+int ig_response_encode_device(ig_ctx* ctx, uint32_t count, const uint64_t* d_a, const uint64_t* d_b,
+                              uint32_t ring_dim, uint32_t retained, uint64_t modulus, uint8_t* d_out,
+                              size_t* len_out, uint32_t* d_status);
 
 /* ---- observability ------------------------------------------------------------------------
  * Per-region device timing of respond calls, the GPU form of the reference's

@@ -86,7 +86,7 @@ def _load():
         "ig_db_destroy": (I, [P, U64]),
         "ig_db_set_shard": (I, [P, U64, U32, P]),
         "ig_db_set_shard_device": (I, [P, U64, U32, P]),
-        "ig_db_encode_records": (I, [P, U64, P, ctypes.c_size_t, U32, I]),
+        "ig_db_encode_records": (I, [P, U64, U32, P, ctypes.c_size_t, U32, I]),
         "ig_db_precompute_packing": (I, [P, U64, U32]),
         "ig_db_precompute_packing_all": (I, [P, U64]),
         "ig_db_drop_packing_store": (I, [P, U64, U32]),
@@ -101,6 +101,7 @@ def _load():
         "ig_respond_seeded_batch_device": (I, [P, U64, U64, U64, U32, P, P, P, U64, P, P, P]),
         "ig_respond_batch": (I, [P, U64, U64, U64, P, U32, U32, U32, P, P, P, U64, P, P]),
         "ig_response_encode": (I, [P, P, U32, U32, U64, P, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
+        "ig_response_encode_device": (I, [P, U32, P, P, U32, U32, U64, P, ctypes.POINTER(ctypes.c_size_t), P]),
         "ig_debug_force_serial_expand": (I, [P, I]),
         "ig_profile_enable": (I, [P, I]),
         "ig_profile_read": (I, [P, P, P, I, I]),
@@ -122,6 +123,8 @@ def _load():
         "ig_serve_wait": (I, [P, U64, ctypes.c_int64, pu64, ctypes.c_char_p, ctypes.c_size_t]),
         "ig_serve_stats": (I, [P, ctypes.POINTER(ServeStats), I]),
         "ig_serve_destroy": (I, [P]),
+        "ig_serve_replay": (I, [P, U64, U64, U32, P, P, P, P, U32, U64, P, U32, P, P, P,
+                                ctypes.POINTER(ctypes.c_double)]),
         "ig_butterfly_peak": (I, [P, I, I, ctypes.POINTER(ctypes.c_double)]),
         "ig_ctx_set_lanes": (I, [P, U32]),
         "ig_ctx_join": (I, [P]),
@@ -182,6 +185,22 @@ class Context:
     def set_pair_threshold(self, max_queries):
         """Batches of at most max_queries run two CTAs per query (0: never)."""
         self.check(self._lib.ig_ctx_set_pair_threshold(self.h, int(max_queries)))
+
+    def response_wire_len(self, ring_dim, retained, modulus):
+        """Bytes of one ServerResponse wire (respond.rs:111-176) at these sizes."""
+        n = ctypes.c_size_t()
+        self.check(self._lib.ig_response_encode_device(self.h, 0, None, None, ring_dim, retained, modulus, None,
+                                                       ctypes.byref(n), None))
+        return n.value
+
+    def response_wire_device(self, count, d_a, d_b, ring_dim, retained, modulus, d_out, d_status):
+        """Encodes `count` device-resident responses into d_out on the context stream
+        (ig_response_encode_device); returns the bytes per response."""
+        n = ctypes.c_size_t()
+        self.check(self._lib.ig_response_encode_device(self.h, count, ctypes.c_void_p(d_a), ctypes.c_void_p(d_b),
+                                                       ring_dim, retained, modulus, ctypes.c_void_p(d_out),
+                                                       ctypes.byref(n), ctypes.c_void_p(d_status)))
+        return n.value
 
     def set_lanes(self, lanes):
         """Streams the device-resident batch entry rotates over (1 = the context stream)."""
@@ -340,15 +359,18 @@ class EncodedDatabase:
         db.encode_records(records, entry_size)
         return db
 
-    def encode_records(self, records, entry_size: int, device_ptr: int = None, nbytes: int = None):
-        """Writes shards 0.. from concatenated entries (host bytes, or a device pointer with
-        its byte count)."""
+    def encode_records(self, records, entry_size: int, device_ptr: int = None, nbytes: int = None,
+                       first_shard: int = 0):
+        """Writes shards first_shard.. from concatenated entries (host bytes, or a device
+        pointer with its byte count)."""
         if device_ptr is not None:
-            self.ctx.check(self.ctx._lib.ig_db_encode_records(self.ctx.h, self.h, ctypes.c_void_p(device_ptr),
-                                                              int(nbytes), int(entry_size), 1))
+            self.ctx.check(self.ctx._lib.ig_db_encode_records(self.ctx.h, self.h, int(first_shard),
+                                                              ctypes.c_void_p(device_ptr), int(nbytes),
+                                                              int(entry_size), 1))
             return
         buf = np.frombuffer(bytes(records), dtype=np.uint8)
-        self.ctx.check(self.ctx._lib.ig_db_encode_records(self.ctx.h, self.h, _ptr(buf), buf.size, int(entry_size), 0))
+        self.ctx.check(self.ctx._lib.ig_db_encode_records(self.ctx.h, self.h, int(first_shard), _ptr(buf), buf.size,
+                                                          int(entry_size), 0))
 
     def set_shard(self, shard_id, columns):
         cols = _u64(columns, (self.num_columns, self.ring_dim))
@@ -648,6 +670,26 @@ class ServingLoop:
             raise PirError(err.value.decode(errors="replace"), rc)
         ticket.latency_us = lat.value / 1e3
         return ServerResponse(ticket._a, ticket._b, ticket._packed, ticket._modulus)
+
+    def replay(self, encoded_db, session_store, shard_ids, handles, seeds, bs, mod_switch_target=0,
+               arrival_ns=None, window=0):
+        """Native load driver (ig_serve_replay): submits the trace on schedule (arrival_ns,
+        open loop) or with `window` requests outstanding (closed loop) and returns
+        (a, b, latency_ns, elapsed_s)."""
+        shard_ids = np.ascontiguousarray(shard_ids, dtype=np.uint32)
+        handles = np.ascontiguousarray(handles, dtype=np.uint64)
+        seeds = np.ascontiguousarray(seeds, dtype=np.uint8)
+        bs = np.ascontiguousarray(bs, dtype=np.uint64)
+        count, n = bs.shape
+        arr = None if arrival_ns is None else np.ascontiguousarray(arrival_ns, dtype=np.uint64)
+        a = np.zeros((count, n), dtype=np.uint64)
+        b = np.zeros((count, n), dtype=np.uint64)
+        lat = np.zeros(count, dtype=np.uint64)
+        el = ctypes.c_double()
+        self.ctx.check(self.ctx._lib.ig_serve_replay(
+            self.h, encoded_db.h, session_store.h, count, _ptr(shard_ids), _ptr(handles), _ptr(seeds), _ptr(bs), n,
+            int(mod_switch_target or 0), _ptr(arr), int(window), _ptr(a), _ptr(b), _ptr(lat), ctypes.byref(el)))
+        return a, b, lat, el.value
 
     def stats(self, reset=False) -> dict:
         st = ServeStats()

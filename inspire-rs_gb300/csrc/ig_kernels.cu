@@ -424,6 +424,35 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32, 2) k_scan(CrsDev c, const Que
   }
 }
 
+// ServerResponse wire on the device (respond.rs:111-176, tight codec poly.rs:166-225):
+// `tmpl` is the response with zero coefficients (header, lengths and trailer already in
+// place); byte k of a packed region takes bits [8k, 8k+8) of the coefficients laid end to
+// end at `bits` each, least significant first. One thread per output byte; a coefficient at
+// or above the modulus sets status bit 1 of its response.
+__global__ void k_wire(const u64* a, const u64* b, u32 n, u32 retained, u32 bits, u64 modulus, const uint8_t* tmpl,
+                       u32 len, u32 a_off, u32 a_bytes, u32 b_off, u32 b_bytes, uint8_t* out, u32* status) {
+  const u32 r = blockIdx.y;
+  const u32 k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= len) return;
+  u32 v = tmpl[k];
+  const u64* c = nullptr;
+  u32 count = 0, byte = 0;
+  if (k >= a_off && k < a_off + a_bytes) {
+    c = a + (size_t)r * n, count = n, byte = k - a_off;
+  } else if (k >= b_off && k < b_off + b_bytes) {
+    c = b + (size_t)r * n, count = retained, byte = k - b_off;
+  }
+  if (c) {
+    const u64 bit = (u64)byte * 8;
+    const u32 i0 = (u32)(bit / bits), sh = (u32)(bit - (u64)i0 * bits);
+    u64 x = c[i0] >> sh;
+    if (c[i0] >= modulus) atomicOr(status + r, 1u);
+    if (sh + 8 > bits && i0 + 1 < count) x |= c[i0 + 1] << (bits - sh);
+    v |= (u32)(x & 0xff);
+  }
+  out[(size_t)r * len + k] = (uint8_t)v;
+}
+
 // encode_database's column split (pir/encode_db.rs:74-168) for one shard: column j, row k
 // holds bytes 2j and 2j+1 of entry k little-endian (one byte when the entry ends there,
 // zero past it), rows past `entries` are zero. Writes the u64 words and their u16 copy.
@@ -1207,6 +1236,16 @@ cudaError_t encode_records(const uint8_t* rec, u32 entries, u32 entry_size, u32 
                            uint16_t* cols16, cudaStream_t s) {
   const size_t words = (size_t)gamma * n;
   k_encode_records<<<(unsigned)((words + 255) / 256), 256, 0, s>>>(rec, entries, entry_size, n, gamma, cols, cols16);
+  return cudaGetLastError();
+}
+
+cudaError_t wire(const u64* a, const u64* b, u32 count, u32 n, u32 retained, u32 bits, u64 modulus,
+                 const uint8_t* tmpl, u32 len, u32 a_off, u32 a_bytes, u32 b_off, u32 b_bytes, uint8_t* out,
+                 u32* status, cudaStream_t s) {
+  if (count == 0) return cudaSuccess;
+  dim3 grid((len + 255) / 256, count);
+  k_wire<<<grid, 256, 0, s>>>(a, b, n, retained, bits, modulus, tmpl, len, a_off, a_bytes, b_off, b_bytes, out,
+                              status);
   return cudaGetLastError();
 }
 

@@ -73,6 +73,12 @@ cudaError_t shard_scan(const CrsDev& c, const QueryDev* queries, const ShardDev*
 cudaError_t encode_records(const uint8_t* rec, u32 entries, u32 entry_size, u32 n, u32 gamma, u64* cols,
                            uint16_t* cols16, cudaStream_t s);
 
+// ServerResponse bytes of `count` responses into out[len * r ..] from the zero-coefficient
+// template (a: n coefficients at a_off, b: `retained` at b_off, `bits` each).
+cudaError_t wire(const u64* a, const u64* b, u32 count, u32 n, u32 retained, u32 bits, u64 modulus,
+                 const uint8_t* tmpl, u32 len, u32 a_off, u32 a_bytes, u32 b_off, u32 b_bytes, uint8_t* out,
+                 u32* status, cudaStream_t s);
+
 // Compact u16 copy of `words` column words (a multiple of 8); sets *wide when a word is
 // 2^16 or above (the copy is then unusable).
 cudaError_t compact16(const u64* cols, size_t words, uint16_t* out, u32* wide, cudaStream_t s);

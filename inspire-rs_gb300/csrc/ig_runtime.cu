@@ -722,8 +722,8 @@ static int set_shard(ig_ctx* c, uint64_t dbh, uint32_t s, const uint64_t* cols, 
   return sync_table_entry(c, *db, s);
 }
 
-int ig_db_encode_records(ig_ctx* c, uint64_t dbh, const uint8_t* records, size_t nbytes, uint32_t entry_size,
-                         int on_device) {
+int ig_db_encode_records(ig_ctx* c, uint64_t dbh, uint32_t first_shard, const uint8_t* records, size_t nbytes,
+                         uint32_t entry_size, int on_device) {
   if (!c) return IG_ERR_ARG;
   if (!records || entry_size == 0) return fail(c, IG_ERR_ARG, "encode_database: null records or entry_size 0");
   std::lock_guard<std::mutex> lk(c->mu);
@@ -740,9 +740,10 @@ int ig_db_encode_records(ig_ctx* c, uint64_t dbh, const uint8_t* records, size_t
                 entry_size, columns, g);
   const size_t entries = nbytes / entry_size;
   const size_t shards = (entries + n - 1) / n;
-  if (shards > db->num_shards)
-    return fail(c, IG_ERR_ARG, "encode_database: %zu entries fill %zu shards of %u; the database holds %u", entries,
-                shards, n, db->num_shards);
+  if ((size_t)first_shard + shards > db->num_shards)
+    return fail(c, IG_ERR_ARG,
+                "encode_database: %zu entries fill %zu shards of %u from shard %u; the database holds %u", entries,
+                shards, n, first_shard, db->num_shards);
   const size_t shard_bytes = (size_t)n * entry_size;
   void* staging = nullptr;
   if (!on_device) {
@@ -750,7 +751,7 @@ int ig_db_encode_records(ig_ctx* c, uint64_t dbh, const uint8_t* records, size_t
     if (rc) return rc;
   }
   for (size_t s = 0; s < shards; s++) {
-    ShardSlot& sl = db->shards[s];
+    ShardSlot& sl = db->shards[first_shard + s];
     const size_t words = (size_t)g * n;
     if (!sl.cols) {
       int rc = dalloc(c, (void**)&sl.cols, words * 8, &db->bytes);
@@ -773,7 +774,7 @@ int ig_db_encode_records(ig_ctx* c, uint64_t dbh, const uint8_t* records, size_t
     sl.compact = true;
     // The staging buffer is reused by the next shard only after this encode has read it.
     if (!on_device) IG_CUDA(c, cudaStreamSynchronize(c->stream));
-    int rc = sync_table_entry(c, *db, (u32)s);
+    int rc = sync_table_entry(c, *db, first_shard + (u32)s);
     if (rc) return rc;
   }
   return IG_OK;
@@ -1242,6 +1243,38 @@ static bool put_tight(std::vector<uint8_t>& w, const u64* c, size_t count, u64 m
     for (size_t k = 0; k < 10 && bit / 8 + k < nbytes; k++) w[base + bit / 8 + k] |= (uint8_t)(v >> (8 * k));
   }
   return true;
+}
+
+int ig_response_encode_device(ig_ctx* c, uint32_t count, const uint64_t* d_a, const uint64_t* d_b, uint32_t n,
+                              uint32_t retained, uint64_t modulus, uint8_t* d_out, size_t* len_out,
+                              uint32_t* d_status) {
+  if (!c) return IG_ERR_ARG;
+  if (!len_out || n == 0 || modulus < 256 || retained == 0 || retained > n)
+    return fail(c, IG_ERR_ARG, "ig_response_encode_device: ring_dim, retained or modulus out of range");
+  // The template: the same response with zero coefficients, from the host encoder.
+  std::vector<u64> za(n, 0), zb(retained, 0);
+  size_t len = 0;
+  int rc = ig_response_encode(za.data(), zb.data(), n, retained, modulus, nullptr, 0, &len);
+  if (rc) return fail(c, rc, "ig_response_encode_device: template refused");
+  *len_out = len;
+  if (!d_out) return IG_OK;  // size query
+  if (count == 0 || !d_a || !d_b || !d_status)
+    return fail(c, IG_ERR_ARG, "ig_response_encode_device: empty batch or null buffer");
+  std::vector<uint8_t> tmpl(len);
+  ig_response_encode(za.data(), zb.data(), n, retained, modulus, tmpl.data(), len, &len);
+  const unsigned bits = 64 - __builtin_clzll(modulus - 1);
+  const u32 a_bytes = (u32)(((u64)n * bits + 7) / 8), b_bytes = (u32)(((u64)retained * bits + 7) / 8);
+  const u32 a_off = 4 + 8, b_off = a_off + a_bytes + 41 + 8;
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  void* d_t;
+  if ((rc = scratch(c, "wire_template", len, &d_t))) return rc;
+  if ((rc = stage_h2d(c, d_t, tmpl.data(), len))) return rc;
+  IG_CUDA(c, cudaMemsetAsync(d_status, 0, (size_t)count * 4, c->stream));
+  IG_CUDA(c, igk::wire(d_a, d_b, count, n, retained, bits, modulus, (const uint8_t*)d_t, (u32)len, a_off, a_bytes,
+                       b_off, b_bytes, d_out, d_status, c->stream));
+  c->launches++;
+  return IG_OK;
 }
 
 int ig_response_encode(const uint64_t* a, const uint64_t* b, uint32_t n, uint32_t retained, uint64_t modulus,

@@ -482,6 +482,52 @@ int ig_serve_wait(ig_serve* s, uint64_t ticket, int64_t timeout_ms, uint64_t* la
   return st;
 }
 
+int ig_serve_replay(ig_serve* s, uint64_t db, uint64_t store, uint32_t count, const uint32_t* shard_ids,
+                    const uint64_t* handles, const uint8_t* seeds, const uint64_t* bs, uint32_t ring_dim,
+                    uint64_t mod_switch_target, const uint64_t* arrival_ns, uint32_t window, uint64_t* a_out,
+                    uint64_t* b_out, uint64_t* latency_ns, double* elapsed_s) {
+  if (!s) return IG_ERR_ARG;
+  if (!shard_ids || !handles || !seeds || !bs || !a_out || !b_out || count == 0 || ring_dim == 0 ||
+      (!arrival_ns && window == 0))
+    return igint::fail(s->ctx, IG_ERR_ARG, "ig_serve_replay: null buffer, empty trace, or neither arrivals nor window");
+  std::vector<u64> tickets(count);
+  const auto t0 = clk::now();
+  int first_err = IG_OK;
+  u32 waited = 0;  // requests [0, waited) already collected
+  auto collect = [&](u32 i) {
+    u64 lat = 0;
+    const int rc = ig_serve_wait(s, tickets[i], -1, &lat, nullptr, 0);
+    if (latency_ns) latency_ns[i] = lat;
+    if (rc != IG_OK && first_err == IG_OK) first_err = rc;
+  };
+  for (u32 i = 0; i < count; i++) {
+    if (arrival_ns) {
+      const auto due = t0 + std::chrono::nanoseconds(arrival_ns[i]);
+      while (clk::now() < due) {
+        const auto left = due - clk::now();
+        if (left > std::chrono::microseconds(200)) std::this_thread::sleep_for(left - std::chrono::microseconds(100));
+      }
+    }
+    if (window)
+      while (i - waited >= window) collect(waited++);
+    int rc;
+    for (;;) {  // an admission refusal under load waits for the oldest request, then retries
+      rc = ig_serve_submit(s, db, store, handles[i], shard_ids[i], seeds + (size_t)i * 32, bs + (size_t)i * ring_dim,
+                           ring_dim, mod_switch_target, a_out + (size_t)i * ring_dim, b_out + (size_t)i * ring_dim,
+                           &tickets[i]);
+      if (rc != IG_ERR_NOMEM || waited == i) break;
+      collect(waited++);
+    }
+    if (rc != IG_OK) {
+      for (; waited < i; waited++) collect(waited);
+      return rc;
+    }
+  }
+  for (; waited < count; waited++) collect(waited);
+  if (elapsed_s) *elapsed_s = std::chrono::duration<double>(clk::now() - t0).count();
+  return first_err;
+}
+
 int ig_serve_stats(ig_serve* s, ig_serve_stats_t* out, int reset) {
   if (!s || !out) return IG_ERR_ARG;
   std::lock_guard<std::mutex> lk(s->mu);

@@ -1,7 +1,7 @@
-"""Device-resident batches over several lanes (ig_ctx_set_lanes): consecutive batches
-rotate over streams and overlap on the device, and with more than one lane they run one
-CTA per query. Every batch's responses must equal the host-buffer respond_seeded_batch
-answers for the same queries, for one lane and for three."""
+"""Device-resident serving pieces: batches over several lanes (ig_ctx_set_lanes), whose
+responses must equal the host-buffer respond_seeded_batch answers for one lane and for
+three, and the device-side response wire (ig_response_encode_device), whose bytes must
+equal the host encoder's."""
 import numpy as np
 import pytest
 
@@ -61,3 +61,38 @@ def test_lanes_give_the_same_responses(pkg, oracle, batch):
         got_b = b.cpu().numpy().view(np.uint64)
         for j in range(nbatches):
             assert (got_a[j] == want[j][0]).all() and (got_b[j] == want[j][1]).all(), (lanes, j)
+
+
+def test_device_wire_matches_host_bytes(pkg, oracle):
+    """ig_response_encode_device builds the ServerResponse bytes next to the responses; they
+    equal the host encoder's (and so the reference's) bytes, unswitched and 36-bit."""
+    torch = pytest.importorskip("torch")
+    ctx = pkg.Context.default()
+    P = oracle.Params.d2048()
+    cell = oracle.Cell(P, 512, 0x3A7E)
+    crs = pkg.ServerCrs(pkg.InspireParams(ring_dim=P.n, p=P.p), cell.w_seed, cell.gamma)
+    cache = pkg.ServerInspiringCache.new(crs, ctx=ctx)
+    db = pkg.EncodedDatabase.from_columns(cache, [cell.columns(s) for s in range(cell.num_shards)])
+    db.precompute_packing_all()
+    store = pkg.ServerSessionStore.new(ctx)
+    h = store.register_server_side(pkg.ClientPackingKeys(cell.keys(), cell.gamma), cache)
+    n, count = P.n, 5
+    qs = [pkg.SeededBatchQuery(*cell.next_query(k * 1201 % (cell.num_shards * n))) for k in range(count)]
+    for ms in (0, pkg.MOD_SWITCH_TARGET_36BIT):
+        out = pkg.respond_seeded_batch(crs, db, pkg.SeededQueryBatch(pkg.PackingKeySource.Registered(h), qs), cache,
+                                       store, mod_switch_target=ms)
+        want = [r.to_binary() for r in out]
+        a = torch.from_numpy(np.stack([r.a for r in out]).view(np.int64)).cuda()
+        b = torch.from_numpy(np.stack([r.b for r in out]).view(np.int64)).cuda()
+        modulus = ms or P.q
+        length = ctx.response_wire_len(n, cell.gamma, modulus)
+        d_out = torch.zeros(count * length, dtype=torch.uint8, device="cuda")
+        st = torch.ones(count, dtype=torch.int32, device="cuda")
+        torch.cuda.synchronize()
+        assert ctx.response_wire_device(count, a.data_ptr(), b.data_ptr(), n, cell.gamma, modulus, d_out.data_ptr(),
+                                        st.data_ptr()) == length
+        torch.cuda.ExternalStream(ctx.stream).synchronize()
+        got = d_out.cpu().numpy().tobytes()
+        assert int(st.abs().sum().item()) == 0
+        for r in range(count):
+            assert got[r * length:(r + 1) * length] == want[r], (ms, r)

@@ -176,3 +176,30 @@ def test_admission_by_device_budget(pkg, ctx):
     assert e.value.code == 8
     with pkg.ServingLoop(ctx, slots=1, max_batch=4, hbm_budget_bytes=1 << 30) as loop:
         assert 0 < loop.stats()["device_bytes"] <= 1 << 30
+
+
+def test_native_replay_matches_alone(pkg, oracle, ctx, sets):
+    """ig_serve_replay drives the loop from native code, closed loop (a window of
+    outstanding requests) and open loop (arrival times); the responses equal the same
+    queries answered alone."""
+    store, exact, approx = sets
+    count = 40
+    rng = np.random.default_rng(11)
+    total = exact.cell.num_shards * exact.P.n
+    idx = [int(i) for i in rng.integers(0, total, count)]
+    qs = [exact.query(pkg, i) for i in idx]
+    alone = [exact.alone(pkg, store, q) for q in qs]
+    shard_ids = [q.shard_id for q in qs]
+    handles = [exact.handle] * count
+    seeds = np.stack([np.frombuffer(q.seed, dtype=np.uint8) for q in qs])
+    bs = np.stack([q.b for q in qs])
+    with pkg.ServingLoop(ctx, slots=2, max_batch=16) as loop:
+        a, b, lat, el = loop.replay(exact.db, store, shard_ids, handles, seeds, bs, window=24)
+        assert el > 0 and (lat > 0).all()
+        for k in range(count):
+            assert (a[k] == alone[k].a).all() and (b[k] == alone[k].b).all()
+        arrivals = np.cumsum(rng.exponential(50_000, count)).astype(np.uint64)  # ~20k/s offered
+        a, b, lat, el = loop.replay(exact.db, store, shard_ids, handles, seeds, bs, arrival_ns=arrivals)
+        assert el * 1e9 >= float(arrivals[-1])
+        for k in range(count):
+            assert (a[k] == alone[k].a).all() and (b[k] == alone[k].b).all()
