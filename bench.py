@@ -508,12 +508,14 @@ def run_sm(args, rank, world):
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     barrier(world)
     with ClockSampler(local) as clk:
+        torch.cuda.profiler.start()  # bounds an ncu --profile-from-start off capture
         with torch.cuda.stream(stream):
             ev0.record(stream)
             for i in range(args.warmup, total):
                 step(i)
             ev1.record(stream)
         torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
     barrier(world)
     if int(d_status.abs().sum().item()) != 0:
         raise RuntimeError("a special-modulus batch reported a device status")

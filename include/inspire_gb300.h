@@ -244,6 +244,12 @@ int ig_serve_create(ig_ctx* ctx, uint32_t slots, uint32_t max_batch, uint64_t hb
 int ig_serve_submit(ig_serve* s, uint64_t db, uint64_t store, uint64_t handle, uint32_t shard_id,
                     const uint8_t* seed, const uint64_t* b, uint32_t ring_dim, uint64_t mod_switch_target,
                     uint64_t* a_out, uint64_t* b_out, uint64_t* ticket_out);
+/* The same request answered as ServerResponse bytes (respond.rs:111-176) built on the GPU
+ * next to the batch's responses: wire_out receives *wire_len bytes (at most wire_cap;
+ * 10,446 at the 36-bit switch with gamma 256) when the ticket finishes. */
+int ig_serve_submit_wire(ig_serve* s, uint64_t db, uint64_t store, uint64_t handle, uint32_t shard_id,
+                         const uint8_t* seed, const uint64_t* b, uint32_t ring_dim, uint64_t mod_switch_target,
+                         uint8_t* wire_out, size_t wire_cap, size_t* wire_len, uint64_t* ticket_out);
 int ig_serve_wait(ig_serve* s, uint64_t ticket, int64_t timeout_ms, uint64_t* latency_ns, char* err, size_t err_len);
 int ig_serve_stats(ig_serve* s, ig_serve_stats_t* out, int reset);
 /* Native load driver for the loop: submits a trace of `count` requests (request i reads

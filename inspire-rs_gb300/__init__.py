@@ -120,6 +120,8 @@ def _load():
         "ig_debug_store_sums": (I, [P, U64, U32, P]),
         "ig_serve_create": (I, [P, U32, U32, U64, ctypes.POINTER(P)]),
         "ig_serve_submit": (I, [P, U64, U64, U64, U32, P, P, U32, U64, P, P, pu64]),
+        "ig_serve_submit_wire": (I, [P, U64, U64, U64, U32, P, P, U32, U64, P, ctypes.c_size_t,
+                                     ctypes.POINTER(ctypes.c_size_t), pu64]),
         "ig_serve_wait": (I, [P, U64, ctypes.c_int64, pu64, ctypes.c_char_p, ctypes.c_size_t]),
         "ig_serve_stats": (I, [P, ctypes.POINTER(ServeStats), I]),
         "ig_serve_destroy": (I, [P]),
@@ -608,9 +610,10 @@ def respond_seeded_inspiring(crs: ServerCrs, encoded_db: EncodedDatabase, query:
 class ServeTicket:
     """One submitted request of a ServingLoop; owns the buffers its result lands in."""
 
-    def __init__(self, loop, ticket, a_out, b_out, modulus, packed):
+    def __init__(self, loop, ticket, a_out, b_out, modulus, packed, wire=None):
         self.loop, self.ticket = loop, ticket
         self._a, self._b, self._modulus, self._packed = a_out, b_out, modulus, packed
+        self._wire = wire  # (buffer, length) for wire requests
         self.latency_us = None
         self.done = False
 
@@ -635,7 +638,10 @@ class ServingLoop:
         self.h = h
 
     def submit(self, crs: ServerCrs, encoded_db: EncodedDatabase, query: SeededBatchQuery,
-               session_store: ServerSessionStore, handle, mod_switch_target: int = 0) -> ServeTicket:
+               session_store: ServerSessionStore, handle, mod_switch_target: int = 0,
+               wire: bool = False) -> ServeTicket:
+        """Queues one query; with wire=True the ticket resolves to the ServerResponse bytes,
+        built on the GPU, instead of a ServerResponse."""
         if self.h is None:
             raise PirError("serving loop is closed")
         n = crs.params.ring_dim
@@ -646,9 +652,20 @@ class ServingLoop:
         ms = int(mod_switch_target or 0)
         if ms:
             check_mod_switch_noise_budget(crs.params, ms)
+        t = ctypes.c_uint64()
+        if wire:
+            cap = 78 + 2 * ((n * 64 + 7) // 8)
+            buf = np.zeros(cap, dtype=np.uint8)
+            length = ctypes.c_size_t()
+            self.ctx.check(self.ctx._lib.ig_serve_submit_wire(self.h, encoded_db.h, session_store.h, int(handle),
+                                                              int(query.shard_id), _ptr(seed), _ptr(b), n, ms,
+                                                              _ptr(buf), cap, ctypes.byref(length), ctypes.byref(t)))
+            ticket = ServeTicket(self, t.value, None, None, ms or crs.params.q, crs.inspiring_num_columns,
+                                 wire=(buf, length))
+            self._live[t.value] = ticket
+            return ticket
         a_out = np.zeros(n, dtype=np.uint64)
         b_out = np.zeros(n, dtype=np.uint64)
-        t = ctypes.c_uint64()
         self.ctx.check(self.ctx._lib.ig_serve_submit(self.h, encoded_db.h, session_store.h, int(handle),
                                                      int(query.shard_id), _ptr(seed), _ptr(b), n, ms, _ptr(a_out),
                                                      _ptr(b_out), ctypes.byref(t)))
@@ -669,6 +686,9 @@ class ServingLoop:
         if rc != 0:
             raise PirError(err.value.decode(errors="replace"), rc)
         ticket.latency_us = lat.value / 1e3
+        if ticket._wire is not None:
+            buf, length = ticket._wire
+            return buf[:length.value].tobytes()
         return ServerResponse(ticket._a, ticket._b, ticket._packed, ticket._modulus)
 
     def replay(self, encoded_db, session_store, shard_ids, handles, seeds, bs, mod_switch_target=0,

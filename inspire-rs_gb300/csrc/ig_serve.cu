@@ -38,6 +38,8 @@ typedef std::chrono::steady_clock clk;
 
 constexpr size_t kMaxN = 2048;      // largest ring the respond kernels serve
 constexpr size_t kMaxGamma = 2048;  // largest packing width (gamma <= n)
+// Largest ServerResponse wire: header and trailer (78 bytes) and two 60-bit tight blocks.
+constexpr size_t kMaxWire = 78 + 2 * ((kMaxN * 60 + 7) / 8);
 
 struct Req {
   u64 ticket = 0;
@@ -47,6 +49,9 @@ struct Req {
   std::vector<u64> b;
   u64* a_out = nullptr;
   u64* b_out = nullptr;
+  uint8_t* wire_out = nullptr;  // wire requests: the ServerResponse bytes instead of a, b
+  size_t wire_cap = 0;
+  size_t* wire_len = nullptr;
   clk::time_point t_submit;
   int status = -1;  // -1 while waiting or in flight
   u64 latency_ns = 0;
@@ -65,6 +70,9 @@ struct Slot {
   u64* d_a = nullptr;
   u64* d_b = nullptr;
   u32* d_status = nullptr;
+  uint8_t* d_wire = nullptr;
+  uint8_t* d_tmpl = nullptr;
+  u32* d_wstatus = nullptr;
   QueryDev* h_q = nullptr;
   ShardDev* h_table = nullptr;
   uint8_t* h_seeds = nullptr;
@@ -72,6 +80,11 @@ struct Slot {
   u64* h_a = nullptr;
   u64* h_b = nullptr;
   u32* h_status = nullptr;
+  uint8_t* h_wire = nullptr;
+  uint8_t* h_tmpl = nullptr;
+  u32* h_wstatus = nullptr;
+  size_t wire_len = 0;  // bytes per response of the batch in flight (0: no wire requests)
+  bool want_ab = false;
   std::vector<Req*> reqs;
   int launch_err = 0;
   u32 ctas = 0;  // CTAs of the batch in flight
@@ -102,7 +115,8 @@ struct ig_serve {
 namespace {
 
 size_t slot_device_bytes(u32 B) {
-  return (size_t)B * (sizeof(QueryDev) + sizeof(ShardDev) + 32 + kMaxN * 8 * 3 + kMaxGamma * 8 + 4);
+  return (size_t)B * (sizeof(QueryDev) + sizeof(ShardDev) + 32 + kMaxN * 8 * 3 + kMaxGamma * 8 + 8 + kMaxWire) +
+         kMaxWire;
 }
 
 int alloc_slot(ig_serve* s, Slot& sl) {
@@ -116,12 +130,16 @@ int alloc_slot(ig_serve* s, Slot& sl) {
   if ((rc = dev((void**)&sl.d_q, B * sizeof(QueryDev))) || (rc = dev((void**)&sl.d_table, B * sizeof(ShardDev))) ||
       (rc = dev((void**)&sl.d_seeds, B * 32)) || (rc = dev((void**)&sl.d_bs, B * kMaxN * 8)) ||
       (rc = dev((void**)&sl.d_fold, B * kMaxGamma * 8)) || (rc = dev((void**)&sl.d_a, B * kMaxN * 8)) ||
-      (rc = dev((void**)&sl.d_b, B * kMaxN * 8)) || (rc = dev((void**)&sl.d_status, B * 4)))
+      (rc = dev((void**)&sl.d_b, B * kMaxN * 8)) || (rc = dev((void**)&sl.d_status, B * 4)) ||
+      (rc = dev((void**)&sl.d_wire, B * kMaxWire)) || (rc = dev((void**)&sl.d_tmpl, kMaxWire)) ||
+      (rc = dev((void**)&sl.d_wstatus, B * 4)))
     return rc;
   if (cudaHostAlloc((void**)&sl.h_q, B * sizeof(QueryDev), 0) ||
       cudaHostAlloc((void**)&sl.h_table, B * sizeof(ShardDev), 0) || cudaHostAlloc((void**)&sl.h_seeds, B * 32, 0) ||
       cudaHostAlloc((void**)&sl.h_bs, B * kMaxN * 8, 0) || cudaHostAlloc((void**)&sl.h_a, B * kMaxN * 8, 0) ||
-      cudaHostAlloc((void**)&sl.h_b, B * kMaxN * 8, 0) || cudaHostAlloc((void**)&sl.h_status, B * 4, 0))
+      cudaHostAlloc((void**)&sl.h_b, B * kMaxN * 8, 0) || cudaHostAlloc((void**)&sl.h_status, B * 4, 0) ||
+      cudaHostAlloc((void**)&sl.h_wire, B * kMaxWire, 0) || cudaHostAlloc((void**)&sl.h_tmpl, kMaxWire, 0) ||
+      cudaHostAlloc((void**)&sl.h_wstatus, B * 4, 0))
     return igint::fail(s->ctx, IG_ERR_NOMEM, "serving loop: pinned host allocation of a slot failed");
   if (cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) ||
       cudaEventCreateWithFlags(&sl.ready, cudaEventDisableTiming) ||
@@ -141,8 +159,11 @@ void free_slot(ig_serve* s, Slot& sl) {
   igint::dfree(s->ctx, sl.d_a, B * kMaxN * 8);
   igint::dfree(s->ctx, sl.d_b, B * kMaxN * 8);
   igint::dfree(s->ctx, sl.d_status, B * 4);
+  igint::dfree(s->ctx, sl.d_wire, B * kMaxWire);
+  igint::dfree(s->ctx, sl.d_tmpl, kMaxWire);
+  igint::dfree(s->ctx, sl.d_wstatus, B * 4);
   for (void* h : {(void*)sl.h_q, (void*)sl.h_table, (void*)sl.h_seeds, (void*)sl.h_bs, (void*)sl.h_a, (void*)sl.h_b,
-                  (void*)sl.h_status})
+                  (void*)sl.h_status, (void*)sl.h_wire, (void*)sl.h_tmpl, (void*)sl.h_wstatus})
     if (h) cudaFreeHost(h);
   if (sl.ready) cudaEventDestroy(sl.ready);
   if (sl.done) cudaEventDestroy(sl.done);
@@ -302,8 +323,38 @@ void dispatch_loop(ig_serve* s) {
       igint::add_launches(s->ctx, 2);
       e = cudaMemcpyAsync(sl.h_status, sl.d_status, count * 4, cudaMemcpyDeviceToHost, st);
     }
-    if (e == cudaSuccess) e = cudaMemcpyAsync(sl.h_a, sl.d_a, (size_t)count * n * 8, cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(sl.h_b, sl.d_b, (size_t)count * n * 8, cudaMemcpyDeviceToHost, st);
+    // Outputs: the coefficient words for requests that want them, the wire bytes (built
+    // here from the words, tight codec) for requests that want those.
+    sl.want_ab = false;
+    sl.wire_len = 0;
+    bool want_wire = false;
+    for (const Req* r : sl.reqs) (r->wire_out ? want_wire : sl.want_ab) = true;
+    if (e == cudaSuccess && want_wire) {
+      const u64 modulus = ms ? ms : Q;
+      const unsigned bits = 64 - __builtin_clzll(modulus - 1);
+      const u32 a_bytes = (u32)(((u64)n * bits + 7) / 8), b_bytes = (u32)(((u64)crs.gamma * bits + 7) / 8);
+      std::vector<u64> zeros(n, 0);
+      size_t len = 0;
+      if (ig_response_encode(zeros.data(), zeros.data(), (u32)n, crs.gamma, modulus, sl.h_tmpl, kMaxWire, &len) ==
+              IG_OK &&
+          len <= kMaxWire) {
+        sl.wire_len = len;
+        e = cudaMemcpyAsync(sl.d_tmpl, sl.h_tmpl, len, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(sl.d_wstatus, 0, count * 4, st);
+        if (e == cudaSuccess)
+          e = igk::wire(sl.d_a, sl.d_b, count, (u32)n, crs.gamma, bits, modulus, sl.d_tmpl, (u32)len, 12, a_bytes,
+                        12 + a_bytes + 41 + 8, b_bytes, sl.d_wire, sl.d_wstatus, st);
+        if (e == cudaSuccess) {
+          igint::add_launches(s->ctx, 1);
+          e = cudaMemcpyAsync(sl.h_wire, sl.d_wire, (size_t)count * len, cudaMemcpyDeviceToHost, st);
+        }
+        if (e == cudaSuccess) e = cudaMemcpyAsync(sl.h_wstatus, sl.d_wstatus, count * 4, cudaMemcpyDeviceToHost, st);
+      }
+    }
+    if (e == cudaSuccess && sl.want_ab)
+      e = cudaMemcpyAsync(sl.h_a, sl.d_a, (size_t)count * n * 8, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && sl.want_ab)
+      e = cudaMemcpyAsync(sl.h_b, sl.d_b, (size_t)count * n * 8, cudaMemcpyDeviceToHost, st);
     cudaEventRecord(sl.done, st);
     {
       std::lock_guard<std::mutex> lk(s->mu);
@@ -349,6 +400,17 @@ void complete_loop(ig_serve* s) {
                  r->shard);
         } else if (sl.h_status[i]) {
           refuse(s, r, IG_ERR_DEVICE, "respond kernel status %u", sl.h_status[i]);
+        } else if (r->wire_out) {
+          if (sl.wire_len == 0 || sl.h_wstatus[i]) {
+            refuse(s, r, IG_ERR_SHAPE, "ServerResponse encode refused: coefficients must be canonical");
+          } else if (sl.wire_len > r->wire_cap) {
+            refuse(s, r, IG_ERR_ARG, "wire buffer of %zu bytes is smaller than the %zu-byte response", r->wire_cap,
+                   sl.wire_len);
+          } else {
+            memcpy(r->wire_out, sl.h_wire + i * sl.wire_len, sl.wire_len);
+            *r->wire_len = sl.wire_len;
+            finish(s, r, IG_OK);
+          }
         } else {
           memcpy(r->a_out, sl.h_a + i * r->n, (size_t)r->n * 8);
           memcpy(r->b_out, sl.h_b + i * r->n, (size_t)r->n * 8);
@@ -421,13 +483,13 @@ int ig_serve_destroy(ig_serve* s) {
   return IG_OK;
 }
 
-int ig_serve_submit(ig_serve* s, uint64_t db, uint64_t store, uint64_t handle, uint32_t shard_id,
-                    const uint8_t* seed, const uint64_t* b, uint32_t ring_dim, uint64_t mod_switch_target,
-                    uint64_t* a_out, uint64_t* b_out, uint64_t* ticket_out) {
-  if (!s) return IG_ERR_ARG;
-  if (!seed || !b || !a_out || !b_out || !ticket_out || ring_dim == 0 || ring_dim > kMaxN)
-    return igint::fail(s->ctx, IG_ERR_ARG, "ig_serve_submit: null buffer or ring_dim outside 1..2048");
+static int submit(ig_serve* s, uint64_t db, uint64_t store, uint64_t handle, uint32_t shard_id, const uint8_t* seed,
+                  const uint64_t* b, uint32_t ring_dim, uint64_t mod_switch_target, uint64_t* a_out, uint64_t* b_out,
+                  uint8_t* wire_out, size_t wire_cap, size_t* wire_len, uint64_t* ticket_out) {
   auto* r = new Req();
+  r->wire_out = wire_out;
+  r->wire_cap = wire_cap;
+  r->wire_len = wire_len;
   r->db = db;
   r->store = store;
   r->handle = handle;
@@ -454,6 +516,26 @@ int ig_serve_submit(ig_serve* s, uint64_t db, uint64_t store, uint64_t handle, u
   }
   s->cv_work.notify_one();
   return IG_OK;
+}
+
+int ig_serve_submit(ig_serve* s, uint64_t db, uint64_t store, uint64_t handle, uint32_t shard_id,
+                    const uint8_t* seed, const uint64_t* b, uint32_t ring_dim, uint64_t mod_switch_target,
+                    uint64_t* a_out, uint64_t* b_out, uint64_t* ticket_out) {
+  if (!s) return IG_ERR_ARG;
+  if (!seed || !b || !a_out || !b_out || !ticket_out || ring_dim == 0 || ring_dim > kMaxN)
+    return igint::fail(s->ctx, IG_ERR_ARG, "ig_serve_submit: null buffer or ring_dim outside 1..2048");
+  return submit(s, db, store, handle, shard_id, seed, b, ring_dim, mod_switch_target, a_out, b_out, nullptr, 0,
+                nullptr, ticket_out);
+}
+
+int ig_serve_submit_wire(ig_serve* s, uint64_t db, uint64_t store, uint64_t handle, uint32_t shard_id,
+                         const uint8_t* seed, const uint64_t* b, uint32_t ring_dim, uint64_t mod_switch_target,
+                         uint8_t* wire_out, size_t wire_cap, size_t* wire_len, uint64_t* ticket_out) {
+  if (!s) return IG_ERR_ARG;
+  if (!seed || !b || !wire_out || !wire_len || !ticket_out || ring_dim == 0 || ring_dim > kMaxN)
+    return igint::fail(s->ctx, IG_ERR_ARG, "ig_serve_submit_wire: null buffer or ring_dim outside 1..2048");
+  return submit(s, db, store, handle, shard_id, seed, b, ring_dim, mod_switch_target, nullptr, nullptr, wire_out,
+                wire_cap, wire_len, ticket_out);
 }
 
 int ig_serve_wait(ig_serve* s, uint64_t ticket, int64_t timeout_ms, uint64_t* latency_ns, char* err, size_t err_len) {

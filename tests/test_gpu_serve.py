@@ -203,3 +203,18 @@ def test_native_replay_matches_alone(pkg, oracle, ctx, sets):
         assert el * 1e9 >= float(arrivals[-1])
         for k in range(count):
             assert (a[k] == alone[k].a).all() and (b[k] == alone[k].b).all()
+
+
+def test_wire_requests_return_reference_bytes(pkg, oracle, ctx, sets):
+    """Requests submitted for wire bytes get the ServerResponse built on the GPU: the same
+    bytes as the host encoder's for the same query answered alone, mixed in one loop with
+    requests for coefficient words."""
+    store, exact, approx = sets
+    reqs = mixed_requests(pkg, sets, 18)
+    alone = [ps.alone(pkg, store, q, ms).to_binary() for ps, q, ms, _ in reqs]
+    with pkg.ServingLoop(ctx, slots=2, max_batch=8) as loop:
+        tickets = [loop.submit(ps.crs, ps.db, q, store, ps.handle, mod_switch_target=ms, wire=(k % 3 != 1))
+                   for k, (ps, q, ms, _) in enumerate(reqs)]
+        got = [loop.wait(t, WAIT_MS) for t in tickets]
+    for k, g in enumerate(got):
+        assert (g if isinstance(g, bytes) else g.to_binary()) == alone[k], k
