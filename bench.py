@@ -489,22 +489,28 @@ def run_sm(args, rank, world):
     bodies_h = rng.integers(0, 536_813_569, (total, B, 2048), dtype=np.uint32)
     d_seeds = torch.from_numpy(seeds_h).cuda()
     d_bodies = torch.from_numpy(bodies_h.view(np.int32)).cuda()
-    d_mask = torch.empty((B, 2048), dtype=torch.int32, device="cuda")
-    d_body = torch.empty((B, 492), dtype=torch.int32, device="cuda")
-    d_status = torch.zeros(B, dtype=torch.int32, device="cuda")
+    lanes = args.lanes
+    d_mask = torch.empty((lanes, B, 2048), dtype=torch.int32, device="cuda")
+    d_body = torch.empty((lanes, B, 492), dtype=torch.int32, device="cuda")
+    d_status = torch.zeros((lanes, B), dtype=torch.int32, device="cuda")
     torch.cuda.synchronize()
     lib = ctx._lib
 
     def step(i):
+        k = i % lanes
         ctx.check(lib.ig_sm_respond_batch_device(ctx.h, server.h, B, tsel[i].ctypes.data, ssel[i].ctypes.data,
-                                                  d_seeds[i].data_ptr(), d_bodies[i].data_ptr(), d_mask.data_ptr(),
-                                                  d_body.data_ptr(), d_status.data_ptr()))
+                                                  d_seeds[i].data_ptr(), d_bodies[i].data_ptr(), d_mask[k].data_ptr(),
+                                                  d_body[k].data_ptr(), d_status[k].data_ptr()))
 
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    ctx.set_lanes(lanes)
     for i in range(args.warmup):
         step(i)
+    ctx.join()
     torch.cuda.synchronize()
+    stream.synchronize()
+    ctx.set_lanes(lanes)
     launches0 = ctx.launch_count
-    stream = torch.cuda.ExternalStream(ctx.stream)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     barrier(world)
     with ClockSampler(local) as clk:
@@ -513,9 +519,12 @@ def run_sm(args, rank, world):
             ev0.record(stream)
             for i in range(args.warmup, total):
                 step(i)
+            ctx.join()
             ev1.record(stream)
         torch.cuda.synchronize()
+        stream.synchronize()
         torch.cuda.profiler.stop()
+    ctx.set_lanes(1)
     barrier(world)
     if int(d_status.abs().sum().item()) != 0:
         raise RuntimeError("a special-modulus batch reported a device status")
@@ -533,7 +542,7 @@ def run_sm(args, rank, world):
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u32 (exact mod q and p)",
         "data": "synthetic: uniform record bytes, uniform key and query words",
-        "config": dict(SM_CONFIG, shards=shards),
+        "config": dict(SM_CONFIG, shards=shards, lanes=lanes),
         "db_gbs": value * 2048 * 256 / 1e9,
         "e2e": {"value": e2e, "unit": "queries/s", "h2d_bytes_per_step": B * (32 + 2048 * 4),
                 "d2h_bytes_per_step": B * (2048 + 492) * 4},

@@ -283,6 +283,10 @@ int ig_response_encode_device(ig_ctx* ctx, uint32_t count, const uint64_t* d_a, 
                               size_t* len_out, uint32_t* d_status);
 
 /* ---- observability ------------------------------------------------------------------------
+ * With RAVEN_PROFILE_RESPOND set in the environment (read once per process, as
+ * respond.rs:1332-1345), every ig_respond_seeded_batch / ig_respond_batch call prints
+ * "RAVEN_PROFILE num_cols=... queries=... column_check_us=... pack_us=..." to stderr, the
+ * regions timed with CUDA events.
  * Per-region device timing of respond calls, the GPU form of the reference's
  * RAVEN_PROFILE_RESPOND regions (respond.rs:1295-1345): with profiling on, each kernel
  * launch is bracketed by CUDA events on the context stream. ig_profile_read synchronises,
@@ -302,6 +306,10 @@ uint64_t ig_launch_count(const ig_ctx* ctx);
  * Forces the word-by-word `a` expansion the kernel otherwise takes only after a rejected
  * ChaCha word, so tests can check that path against the vectorised one. */
 int ig_debug_force_serial_expand(ig_ctx* ctx, int on);
+/* Host-side fault injection: the k-th device allocation of this context from now (1 = the
+ * next) fails with IG_ERR_NOMEM, as a full GPU would make it; 0 disarms. The call that
+ * made it is refused and leaves no half-built object; the context stays usable. */
+int ig_debug_fail_alloc_at(ig_ctx* ctx, uint32_t k);
 /* Copies a shard's store sums (gamma x ring_dim, NTT form times 2^64 mod q, the
  * reference's Montgomery layout) to host memory. */
 int ig_debug_store_sums(ig_ctx* ctx, uint64_t db, uint32_t shard_id, uint64_t* out);

@@ -118,6 +118,7 @@ def _load():
         "ig_sm_respond_batch_device": (I, [P, U64, U32, P, P, P, P, P, P, P]),
         "ig_sm_response_encode": (I, [P, U32, P, U32, U64, P, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
         "ig_debug_store_sums": (I, [P, U64, U32, P]),
+        "ig_debug_fail_alloc_at": (I, [P, U32]),
         "ig_serve_create": (I, [P, U32, U32, U64, ctypes.POINTER(P)]),
         "ig_serve_submit": (I, [P, U64, U64, U64, U32, P, P, U32, U64, P, P, pu64]),
         "ig_serve_submit_wire": (I, [P, U64, U64, U64, U32, P, P, U32, U64, P, ctypes.c_size_t,

@@ -39,5 +39,14 @@ struct RequestView {
 };
 int resolve_request(ig_ctx* c, uint64_t db, uint64_t store, uint64_t handle, uint32_t shard, RequestView* out);
 int pair_threshold(ig_ctx* c);
+// Device-path lanes (ig_ctx_set_lanes), for callers holding the context lock:
+// lane_acquire picks the call's stream (the context stream when lanes == 1, lane -1) and
+// orders the context stream after the lane's previous batch, so the lane's scratch can be
+// rewritten; lane_enter, after the call's staging copies on the context stream, makes the
+// lane wait for them; lane_release marks the lane's work for the next acquire and join.
+int lanes(ig_ctx* c);
+int lane_acquire(ig_ctx* c, cudaStream_t* s, int* lane);
+int lane_enter(ig_ctx* c, int lane);
+int lane_release(ig_ctx* c, int lane);
 int sm_count(ig_ctx* c);
 }  // namespace igint

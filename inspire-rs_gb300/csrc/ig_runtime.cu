@@ -7,6 +7,7 @@
 #include <atomic>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <random>
@@ -185,6 +186,9 @@ struct ig_ctx {
   // rotate over that many streams, each with its own scratch, so batches overlap on the
   // device; ig_ctx_join orders the context stream after all of them.
   u32 lanes = 1, lane_next = 0, sms = 0;
+  // Host-side fault injection: the device allocation `fail_alloc_at` calls from now fails
+  // (1 = the next one; 0 = none).
+  std::atomic<u32> fail_alloc_at{0};
   cudaStream_t lane_stream[IG_MAX_LANES] = {};
   cudaEvent_t lane_in[IG_MAX_LANES] = {}, lane_done[IG_MAX_LANES] = {};
   bool lane_used[IG_MAX_LANES] = {};
@@ -237,6 +241,13 @@ int fail(ig_ctx* c, int code, const char* fmt, ...) {
   } while (0)
 
 int dalloc(ig_ctx* c, void** p, size_t bytes, size_t* counter) {
+  u32 at = c->fail_alloc_at.load();
+  while (at && !c->fail_alloc_at.compare_exchange_weak(at, at - 1)) {
+  }
+  if (at == 1) {
+    *p = nullptr;
+    return fail(c, IG_ERR_NOMEM, "device allocation of %zu bytes failed: injected failure", bytes);
+  }
   cudaError_t e = cudaMalloc(p, bytes);
   if (e != cudaSuccess) {
     *p = nullptr;
@@ -354,12 +365,21 @@ int build_store(ig_ctx* c, DbObj& db, CrsObj& o, u32 s) {
     return fail(c, IG_ERR_ARG, "shard %u: no columns uploaded; precompute_packing needs the shard's columns", s);
   const size_t n = o.n, g = o.gamma;
   if (!sl.sums) {
-    int rc = dalloc(c, (void**)&sl.sums, g * n * 8, &db.bytes);
-    if (rc) return rc;
-    rc = dalloc(c, (void**)&sl.tag_key, 2 * n * 8, &db.bytes);
-    if (rc) return rc;
-    rc = dalloc(c, (void**)&sl.tags, g * 8, &db.bytes);
-    if (rc) return rc;
+    // All three buffers or none: a shard counts as stored when `sums` is set.
+    u64 *sums = nullptr, *key = nullptr, *tags = nullptr;
+    size_t got = 0;
+    int rc = dalloc(c, (void**)&sums, g * n * 8, &got);
+    if (!rc) rc = dalloc(c, (void**)&key, 2 * n * 8, &got);
+    if (!rc) rc = dalloc(c, (void**)&tags, g * 8, &got);
+    if (rc) {
+      if (sums) dfree(c, sums, g * n * 8);
+      if (key) dfree(c, key, 2 * n * 8);
+      return rc;
+    }
+    db.bytes += got;
+    sl.sums = sums;
+    sl.tag_key = key;
+    sl.tags = tags;
   }
   // Tag key: two words per column word below 2^61 - 1, drawn from OS entropy and never
   // leaving the device (shard_store.rs:127-135).
@@ -422,6 +442,29 @@ int stage_h2d(ig_ctx* c, void* dst, const void* src, size_t bytes) { return ::st
 void add_launches(ig_ctx* c, unsigned n) { c->launches += n; }
 void*& sm_slot(ig_ctx* c) { return c->sm; }
 int pair_threshold(ig_ctx* c) { return (int)c->pair_threshold; }
+int lanes(ig_ctx* c) { return (int)c->lanes; }
+int lane_acquire(ig_ctx* c, cudaStream_t* s, int* lane) {
+  *lane = -1;
+  *s = c->stream;
+  if (c->lanes <= 1) return IG_OK;
+  const int k = (int)(c->lane_next++ % c->lanes);
+  if (c->lane_used[k]) IG_CUDA(c, cudaStreamWaitEvent(c->stream, c->lane_done[k], 0));
+  *lane = k;
+  *s = c->lane_stream[k];
+  return IG_OK;
+}
+int lane_enter(ig_ctx* c, int lane) {
+  if (lane < 0) return IG_OK;
+  IG_CUDA(c, cudaEventRecord(c->lane_in[lane], c->stream));
+  IG_CUDA(c, cudaStreamWaitEvent(c->lane_stream[lane], c->lane_in[lane], 0));
+  return IG_OK;
+}
+int lane_release(ig_ctx* c, int lane) {
+  if (lane < 0) return IG_OK;
+  IG_CUDA(c, cudaEventRecord(c->lane_done[lane], c->lane_stream[lane]));
+  c->lane_used[lane] = true;
+  return IG_OK;
+}
 int sm_count(ig_ctx* c) { return (int)c->sms; }
 void set_sm_destructor(ig_ctx* c, void (*fn)(ig_ctx*, void*)) { c->sm_destroy = fn; }
 }  // namespace igint
@@ -599,6 +642,7 @@ int ig_crs_create(ig_ctx* c, uint32_t n, uint64_t q, uint64_t p, uint64_t gadget
       (rc = upload(c, o, cpow, &d.cpow)) || (rc = upload(c, o, m_of_i, &d.m_of_i)) ||
       (rc = upload(c, o, pow_root_R, &d.pow_root_R))) {
     for (void* p2 : o.allocs) cudaFree(p2);
+    c->obj_bytes -= o.bytes;
     return rc;
   }
   d.ninv = invmod(n);
@@ -611,12 +655,15 @@ int ig_crs_create(ig_ctx* c, uint32_t n, uint64_t q, uint64_t p, uint64_t gadget
   d.ld_c0_R = mulmod(negq(inv), R_MOD_Q);
   d.ld_c1_R = mulmod(negq(mulmod(inv, 1ULL << 20)), R_MOD_Q);
   // Mask rows -> NTT, R-form.
-  void* mraw;
+  void* mraw = nullptr;
+  void* wm = nullptr;
   rc = scratch(c, "mask_raw", mask.size() * 8, &mraw);
-  if (rc) return rc;
-  void* wm;
-  rc = dalloc(c, &wm, mask.size() * 8, &o.bytes);
-  if (rc) return rc;
+  if (!rc) rc = dalloc(c, &wm, mask.size() * 8, &o.bytes);
+  if (rc) {
+    for (void* p2 : o.allocs) cudaFree(p2);
+    c->obj_bytes -= o.bytes;
+    return rc;
+  }
   o.allocs.push_back(wm);
   IG_CUDA(c, cudaMemcpyAsync(mraw, mask.data(), mask.size() * 8, cudaMemcpyHostToDevice, c->stream));
   IG_CUDA(c, igk::ntt_rows(d, (const u64*)mraw, (u64*)wm, o.rows, R_MOD_Q, shoup_companion(R_MOD_Q), c->stream));
@@ -686,6 +733,26 @@ int ig_db_destroy(ig_ctx* c, uint64_t dbh) {
   return IG_OK;
 }
 
+// A shard's u64 columns and their u16 copy, both or neither (a shard counts as uploaded
+// when `cols` is set).
+static int alloc_columns(ig_ctx* c, DbObj& db, ShardSlot& sl, size_t bytes) {
+  if (sl.cols && sl.cols16) return IG_OK;
+  u64* cols = sl.cols;
+  uint16_t* cols16 = sl.cols16;
+  size_t got = 0;
+  int rc = IG_OK;
+  if (!cols) rc = dalloc(c, (void**)&cols, bytes, &got);
+  if (!rc && !cols16) rc = dalloc(c, (void**)&cols16, bytes / 4, &got);
+  if (rc) {
+    if (cols && !sl.cols) dfree(c, cols, bytes);
+    return rc;
+  }
+  db.bytes += got;
+  sl.cols = cols;
+  sl.cols16 = cols16;
+  return IG_OK;
+}
+
 static int set_shard(ig_ctx* c, uint64_t dbh, uint32_t s, const uint64_t* cols, cudaMemcpyKind kind) {
   if (!c || !cols) return fail(c, IG_ERR_ARG, "ig_db_set_shard: null columns");
   std::lock_guard<std::mutex> lk(c->mu);
@@ -698,16 +765,10 @@ static int set_shard(ig_ctx* c, uint64_t dbh, uint32_t s, const uint64_t* cols, 
   CrsObj* o = get_crs(c, db->crs);
   const size_t bytes = (size_t)o->gamma * o->n * 8;
   ShardSlot& sl = db->shards[s];
-  if (!sl.cols) {
-    int rc = dalloc(c, (void**)&sl.cols, bytes, &db->bytes);
-    if (rc) return rc;
-  }
-  if (!sl.cols16) {
-    int rc = dalloc(c, (void**)&sl.cols16, bytes / 4, &db->bytes);
-    if (rc) return rc;
-  }
+  int rc = alloc_columns(c, *db, sl, bytes);
+  if (rc) return rc;
   void* wide;
-  int rc = scratch(c, "compact_flag", 4, &wide);
+  rc = scratch(c, "compact_flag", 4, &wide);
   if (rc) return rc;
   IG_CUDA(c, cudaMemcpyAsync(sl.cols, cols, bytes, kind, c->stream));
   // Shards whose words all fit 16 bits (encoded records always do) are scanned from a
@@ -753,12 +814,8 @@ int ig_db_encode_records(ig_ctx* c, uint64_t dbh, uint32_t first_shard, const ui
   for (size_t s = 0; s < shards; s++) {
     ShardSlot& sl = db->shards[first_shard + s];
     const size_t words = (size_t)g * n;
-    if (!sl.cols) {
-      int rc = dalloc(c, (void**)&sl.cols, words * 8, &db->bytes);
-      if (rc) return rc;
-    }
-    if (!sl.cols16) {
-      int rc = dalloc(c, (void**)&sl.cols16, words * 2, &db->bytes);
+    {
+      int rc = alloc_columns(c, *db, sl, words * 8);
       if (rc) return rc;
     }
     const size_t first = s * n;
@@ -999,6 +1056,12 @@ static int resolve_seat(ig_ctx* c, CrsObj& o, uint64_t st, uint64_t handle, cons
   return IG_OK;
 }
 
+// RAVEN_PROFILE_RESPOND is read once per process, as the reference does (respond.rs:1332-1345).
+static bool env_profile() {
+  static const bool on = getenv("RAVEN_PROFILE_RESPOND") != nullptr;
+  return on;
+}
+
 static int respond_host(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_t handle, const uint64_t* inline_y,
                         uint32_t inline_rows, uint32_t inline_ntp, uint32_t count, const uint32_t* shard_ids,
                         const uint8_t* seeds, const uint64_t* as, const uint64_t* bs, uint64_t ms_target,
@@ -1083,14 +1146,32 @@ static int respond_host(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_t handle, c
       (rc = stage_h2d(c, d_bs, bs, (size_t)count * n * 8)))
     return rc;
   IG_CUDA(c, cudaMemsetAsync(d_status, 0, count * 4, s));
+  // RAVEN_PROFILE_RESPOND (respond.rs:1295-1345): CUDA events around the two regions of the
+  // batch, printed to stderr in the reference's line format.
+  cudaEvent_t env_ev[3] = {};
+  const bool env_prof = env_profile();
+  if (env_prof)
+    for (auto& e : env_ev) cudaEventCreate(&e);
+  if (env_prof) cudaEventRecord(env_ev[0], s);
   long pk = prof_begin(c, REGION_SCAN);
   IG_CUDA(c, igk::shard_scan(o.dev, (const QueryDev*)d_q, (const ShardDev*)d_table, count, (u64*)d_fold,
                              (u32*)d_status, 0, nullptr, s));
   prof_end(c, pk);
+  if (env_prof) cudaEventRecord(env_ev[1], s);
   pk = prof_begin(c, REGION_RESPOND);
   IG_CUDA(c, igk::respond(o.dev, (const QueryDev*)d_q, (const ShardDev*)d_table, count, (const u64*)d_fold, ms_target,
                           (u64*)d_a, (u64*)d_b, (u32*)d_status, c->force_serial, count <= c->pair_threshold, s));
   prof_end(c, pk);
+  if (env_prof) {
+    cudaEventRecord(env_ev[2], s);
+    cudaEventSynchronize(env_ev[2]);
+    float scan_ms = 0, pack_ms = 0;
+    cudaEventElapsedTime(&scan_ms, env_ev[0], env_ev[1]);
+    cudaEventElapsedTime(&pack_ms, env_ev[1], env_ev[2]);
+    fprintf(stderr, "RAVEN_PROFILE num_cols=%u queries=%u column_check_us=%.0f pack_us=%.0f\n", (unsigned)g,
+            (unsigned)count, 1e3 * scan_ms, 1e3 * pack_ms);
+    for (auto& e : env_ev) cudaEventDestroy(e);
+  }
   std::vector<u32> status(count);
   IG_CUDA(c, cudaMemcpyAsync(status.data(), d_status, count * 4, cudaMemcpyDeviceToHost, s));
   IG_CUDA(c, cudaStreamSynchronize(s));
@@ -1153,11 +1234,7 @@ int ig_respond_seeded_batch_device(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_
   // only after the lane's previous batch has finished with it.
   int lane = -1;
   cudaStream_t s = c->stream;
-  if (c->lanes > 1) {
-    lane = (int)(c->lane_next++ % c->lanes);
-    s = c->lane_stream[lane];
-    if (c->lane_used[lane]) IG_CUDA(c, cudaStreamWaitEvent(c->stream, c->lane_done[lane], 0));
-  }
+  if ((rc = igint::lane_acquire(c, &s, &lane))) return rc;
   char qname[32], fname[32];
   snprintf(qname, sizeof qname, "dev_queries%d", lane);
   snprintf(fname, sizeof fname, "dev_fold%d", lane);
@@ -1174,10 +1251,7 @@ int ig_respond_seeded_batch_device(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_
     qs[i].seat_R = seat;
   }
   if ((rc = stage_h2d(c, d_q, qs.data(), count * sizeof(QueryDev)))) return rc;
-  if (lane >= 0) {
-    IG_CUDA(c, cudaEventRecord(c->lane_in[lane], c->stream));
-    IG_CUDA(c, cudaStreamWaitEvent(s, c->lane_in[lane], 0));
-  }
+  if ((rc = igint::lane_enter(c, lane))) return rc;
   IG_CUDA(c, cudaMemsetAsync(d_status, 0, count * 4, s));
   long pk = prof_begin(c, REGION_SCAN, s);
   IG_CUDA(c, igk::shard_scan(o.dev, (const QueryDev*)d_q, db->d_table, count, (u64*)d_fold, d_status, 0, nullptr, s));
@@ -1188,11 +1262,7 @@ int ig_respond_seeded_batch_device(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_
   IG_CUDA(c, igk::respond(o.dev, (const QueryDev*)d_q, db->d_table, count, (const u64*)d_fold, ms_target, d_a, d_b,
                           d_status, c->force_serial, pair, s));
   prof_end(c, pk, s);
-  if (lane >= 0) {
-    IG_CUDA(c, cudaEventRecord(c->lane_done[lane], s));
-    c->lane_used[lane] = true;
-  }
-  return IG_OK;
+  return igint::lane_release(c, lane);
 }
 
 int ig_ctx_set_lanes(ig_ctx* c, uint32_t lanes) {
@@ -1368,6 +1438,12 @@ int ig_butterfly_peak(ig_ctx* c, int blocks_per_sm, int iters, double* per_s) {
   cudaEventDestroy(e1);
   c->launches += 2;
   *per_s = (double)blocks * 256.0 * (double)iters * 8.0 / ((double)ms / 1e3);
+  return IG_OK;
+}
+
+int ig_debug_fail_alloc_at(ig_ctx* c, uint32_t k) {
+  if (!c) return IG_ERR_ARG;
+  c->fail_alloc_at.store(k);
   return IG_OK;
 }
 

@@ -3,6 +3,8 @@
 // the batched respond, with the refusal rules of src/special_modulus/server.rs.
 #include <cuda_runtime.h>
 
+#include <cstdio>
+
 #include <cstring>
 #include <unordered_map>
 #include <vector>
@@ -542,22 +544,30 @@ int ig_sm_respond_batch_device(ig_ctx* c, uint64_t server, uint32_t count, const
   int rc = sm_prepare(c, st, server, count, tables, seats, &o, qs);
   if (rc) return rc;
   const size_t d = o->n, nb = o->dev.nb;
+  // Lanes (ig_ctx_set_lanes) apply here as on the InspiRING device path: consecutive
+  // batches rotate over streams with their own scratch.
+  cudaStream_t s;
+  int lane;
+  if ((rc = igint::lane_acquire(c, &s, &lane))) return rc;
+  char qname[32], fname[32];
+  snprintf(qname, sizeof qname, "smd_q%d", lane);
+  snprintf(fname, sizeof fname, "smd_fold%d", lane);
   void *dq, *dfold;
-  if ((rc = igint::scratch(c, "smd_q", count * sizeof(SmQueryDev), &dq)) ||
-      (rc = igint::scratch(c, "smd_fold", count * nb * 8, &dfold)))
+  if ((rc = igint::scratch(c, qname, count * sizeof(SmQueryDev), &dq)) ||
+      (rc = igint::scratch(c, fname, count * nb * 8, &dfold)))
     return rc;
   for (u32 i = 0; i < count; i++) {
     qs[i].seed = (const u32*)(d_seeds + (size_t)i * 32);
     qs[i].body = d_bodies + (size_t)i * d;
   }
-  cudaStream_t s = igint::stream(c);
   if ((rc = igint::stage_h2d(c, dq, qs.data(), count * sizeof(SmQueryDev)))) return rc;
+  if ((rc = igint::lane_enter(c, lane))) return rc;
   SM_CUDA(c, cudaMemsetAsync(d_status, 0, count * 4, s));
   SM_CUDA(c, igsmk::body_fold(o->dev, (const SmQueryDev*)dq, count, (i64*)dfold, s));
   SM_CUDA(c, igsmk::respond(o->dev, (const SmQueryDev*)dq, count, (const i64*)dfold, d_mask_out, d_body_out, d_status,
                             s));
   igint::add_launches(c, 2);
-  return IG_OK;
+  return igint::lane_release(c, lane);
 }
 
 // Response::to_bytes (special_modulus/wire.rs:120-125): mask then body, each packed at q's
