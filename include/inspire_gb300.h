@@ -265,6 +265,21 @@ int ig_serve_replay(ig_serve* s, uint64_t db, uint64_t store, uint32_t count, co
                     uint64_t* b_out, uint64_t* latency_ns, double* elapsed_s);
 int ig_serve_destroy(ig_serve* s);
 
+/* ---- NoPacking respond -------------------------------------------------------------------
+ * respond / respond_seeded (respond.rs:614-643, 1229-1237), the unpacked variant: per query,
+ * one RLWE ciphertext (a h_j, b h_j) per column j of its shard (plaintext_multiply_columns,
+ * respond.rs:585-599) and their sum. Query i: shard_ids[i], a from seeds[32 i..] (seeded) or
+ * as[ring_dim i..] (pass seeds null), b from bs[ring_dim i..]. out receives count x
+ * (gamma + 1) ciphertexts of (a, b), ring_dim words each in coefficient form, the sum first.
+ * No store or seat is needed. All or nothing. */
+int ig_respond_nopacking_batch(ig_ctx* ctx, uint64_t db, uint32_t count, const uint32_t* shard_ids,
+                               const uint8_t* seeds, const uint64_t* as, const uint64_t* bs, uint64_t* out);
+/* The unpacked ServerResponse bytes (respond.rs:111-176): Full(ciphertext), the column
+ * ciphertexts, packing_mode None. cts: `count` ciphertexts of (a, b), the response
+ * ciphertext first. */
+int ig_response_encode_full(const uint64_t* cts, uint32_t count, uint32_t ring_dim, uint64_t modulus, uint8_t* out,
+                            size_t cap, size_t* len_out);
+
 /* ---- wire ------------------------------------------------------------------------------
  * ServerResponse bincode bytes of a packed response (respond.rs:111-176, tight codec
  * poly.rs:166-225): Packed{a, b_prefix (first `retained` b coefficients), retained}, no

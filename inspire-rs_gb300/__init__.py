@@ -30,6 +30,7 @@ __all__ = [
     "PirError", "InspireParams", "ServerCrs", "ShardData", "EncodedDatabase", "ServerInspiringCache",
     "ServerSessionStore", "ServerSessionHandle", "ClientPackingKeys", "SeededBatchQuery", "SeededClientQuery",
     "SeededQueryBatch", "PackingKeySource", "ServerResponse", "respond_seeded_inspiring", "respond_seeded_batch", "respond_inspiring",
+    "respond", "respond_seeded", "respond_nopacking_batch",
     "check_mod_switch_noise_budget", "ClientQuery", "Context", "DEFAULT_Q",
     "MOD_SWITCH_TARGET_36BIT", "MOD_SWITCH_TARGET_45BIT", "library_path", "special_modulus", "ServingLoop",
     "ServeTicket",
@@ -101,6 +102,8 @@ def _load():
         "ig_respond_seeded_batch_device": (I, [P, U64, U64, U64, U32, P, P, P, U64, P, P, P]),
         "ig_respond_batch": (I, [P, U64, U64, U64, P, U32, U32, U32, P, P, P, U64, P, P]),
         "ig_response_encode": (I, [P, P, U32, U32, U64, P, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
+        "ig_response_encode_full": (I, [P, U32, U32, U64, P, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
+        "ig_respond_nopacking_batch": (I, [P, U64, U32, P, P, P, P, P]),
         "ig_response_encode_device": (I, [P, U32, P, P, U32, U32, U64, P, ctypes.POINTER(ctypes.c_size_t), P]),
         "ig_debug_force_serial_expand": (I, [P, I]),
         "ig_profile_enable": (I, [P, I]),
@@ -499,15 +502,30 @@ class SeededQueryBatch:
 
 
 class ServerResponse:
-    """A packed InspiRING response: a, b (the first `packed_coefficients` b words cross
-    the wire) over `modulus` (respond.rs:27-41)."""
+    """ServerResponse (respond.rs:27-41). Packed (InspiRING): a, b, of which the first
+    `packed_coefficients` b words cross the wire, over `modulus`. Unpacked (NoPacking):
+    packed_coefficients None, (a, b) the sum of `column_ciphertexts`, a list of (a, b)."""
 
-    def __init__(self, a, b, packed_coefficients, modulus=DEFAULT_Q):
+    def __init__(self, a, b, packed_coefficients, modulus=DEFAULT_Q, column_ciphertexts=None):
         self.a, self.b = a, b
-        self.packed_coefficients, self.modulus = int(packed_coefficients), int(modulus)
+        self.packed_coefficients = None if packed_coefficients is None else int(packed_coefficients)
+        self.modulus = int(modulus)
+        self.column_ciphertexts = column_ciphertexts or []
+        self.packing_mode = None if packed_coefficients is None else "Inspiring"
 
     def to_binary(self) -> bytes:
         L = _load()
+        if self.packed_coefficients is None:
+            cts = np.ascontiguousarray(
+                np.stack([np.stack([self.a, self.b])] + [np.stack([ca, cb]) for ca, cb in self.column_ciphertexts]),
+                dtype=np.uint64)
+            n = ctypes.c_size_t()
+            count, _, ring = cts.shape
+            if L.ig_response_encode_full(_ptr(cts), count, ring, self.modulus, None, 0, ctypes.byref(n)):
+                raise PirError("ServerResponse encode refused: coefficients must be canonical")
+            out = np.zeros(n.value, dtype=np.uint8)
+            L.ig_response_encode_full(_ptr(cts), count, ring, self.modulus, _ptr(out), n.value, ctypes.byref(n))
+            return out.tobytes()
         a = np.ascontiguousarray(self.a, dtype=np.uint64)
         b = np.ascontiguousarray(self.b, dtype=np.uint64)
         n = ctypes.c_size_t()
@@ -734,6 +752,46 @@ class ServingLoop:
             self.close()
         except Exception:
             pass
+
+
+def _nopacking(crs, encoded_db, queries):
+    ctx = encoded_db.ctx
+    n, g = crs.params.ring_dim, crs.inspiring_num_columns
+    count = len(queries)
+    if count == 0:
+        raise PirError("empty batch")
+    unseeded = queries[0].seed is None
+    if any((q.seed is None) != unseeded for q in queries):
+        raise PirError("a batch is all seeded or all unseeded queries")
+    shard_ids = np.array([q.shard_id for q in queries], dtype=np.uint32)
+    if unseeded:
+        seeds, a_in = None, np.stack([_u64(q.a, (n,)) for q in queries])
+    else:
+        seeds, a_in = np.frombuffer(b"".join(q.seed for q in queries), dtype=np.uint8).copy(), None
+    bs = np.stack([_u64(q.b, (n,)) for q in queries])
+    out = np.zeros((count, g + 1, 2, n), dtype=np.uint64)
+    ctx.check(ctx._lib.ig_respond_nopacking_batch(ctx.h, encoded_db.h, count, _ptr(shard_ids), _ptr(seeds),
+                                                  _ptr(a_in), _ptr(bs), _ptr(out)))
+    return [ServerResponse(out[i, 0, 0], out[i, 0, 1], None, crs.params.q,
+                           column_ciphertexts=[(out[i, j, 0], out[i, j, 1]) for j in range(1, g + 1)])
+            for i in range(count)]
+
+
+def respond(crs: ServerCrs, encoded_db: EncodedDatabase, query: ClientQuery) -> ServerResponse:
+    """respond (respond.rs:614-643): the NoPacking variant, one ciphertext per column and
+    their sum, for an unseeded query."""
+    return _nopacking(crs, encoded_db, [query])[0]
+
+
+def respond_seeded(crs: ServerCrs, encoded_db: EncodedDatabase, query: SeededBatchQuery) -> ServerResponse:
+    """respond_seeded (respond.rs:1229-1237): the query's `a` expanded from its seed, then
+    respond."""
+    return _nopacking(crs, encoded_db, [query])[0]
+
+
+def respond_nopacking_batch(crs: ServerCrs, encoded_db: EncodedDatabase, queries) -> list:
+    """NoPacking responses of many queries in one launch sequence (seeded or unseeded)."""
+    return _nopacking(crs, encoded_db, list(queries))
 
 
 class _SpecialModulus:

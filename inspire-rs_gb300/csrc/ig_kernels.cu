@@ -588,6 +588,14 @@ __device__ __forceinline__ u64 finish_b(const CrsDev& c, u64 x, u32 t, u32 qi, c
 }
 
 // ------------------------------------------------------------------------------------
+// Shared-memory position of word e of the one-CTA kernel's per-link transform buffers
+// (8-byte words, 16 to a 128-byte bank row): bits 4 and 5 of e are XORed into bits 2 and 3,
+// which puts every half-warp of the small-stride radix-4 passes (t = 4, 16 in the inverse;
+// h = 4, 16 in the forward) on 16 distinct bank pairs. 2-word pairs stay contiguous and
+// 16-byte aligned, and each 16-word row maps onto itself.
+__device__ __forceinline__ int sw(int e) { return e ^ (((e >> 4) & 3) << 2); }
+
+// ------------------------------------------------------------------------------------
 // One CTA per query (batches that fill the GPU). Thread u owns slots 4u..4u+3 of every
 // NTT-domain vector (one transform unit). Each link of the recursion (i from gamma-2 down
 // to 0) holds R_{i+1} in NTT form (`cur`, in registers):
@@ -671,8 +679,8 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
       bf_inv(a2, a3, w1, w1p);
       bf_inv(a0, a2, w2, w2p);
       bf_inv(a1, a3, w2, w2p);
-      *reinterpret_cast<ulonglong2*>(X + l0) = make_ulonglong2(a0, a1);
-      *reinterpret_cast<ulonglong2*>(X + l0 + 2) = make_ulonglong2(a2, a3);
+      *reinterpret_cast<ulonglong2*>(X + sw(l0)) = make_ulonglong2(a0, a1);
+      *reinterpret_cast<ulonglong2*>(X + sw(l0 + 2)) = make_ulonglong2(a2, a3);
     }
     __syncthreads();
     // Inverse stages 2 .. logn-2 (radix-4 pairs, a radix-2 stage last when logn is even).
@@ -686,15 +694,15 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
       inv_twiddle(tw, twp, m + 2 * B, w0, w0p);
       inv_twiddle(tw, twp, m + 2 * B + 1, w1, w1p);
       inv_twiddle(tw, twp, (m >> 1) + B, w2, w2p);
-      u64 a0 = X[e0], a1 = X[e0 + t], a2 = X[e0 + 2 * t], a3 = X[e0 + 3 * t];
+      u64 a0 = X[sw(e0)], a1 = X[sw(e0 + t)], a2 = X[sw(e0 + 2 * t)], a3 = X[sw(e0 + 3 * t)];
       bf_inv(a0, a1, w0, w0p);
       bf_inv(a2, a3, w1, w1p);
       bf_inv(a0, a2, w2, w2p);
       bf_inv(a1, a3, w2, w2p);
-      X[e0] = a0;
-      X[e0 + t] = a1;
-      X[e0 + 2 * t] = a2;
-      X[e0 + 3 * t] = a3;
+      X[sw(e0)] = a0;
+      X[sw(e0 + t)] = a1;
+      X[sw(e0 + 2 * t)] = a2;
+      X[sw(e0 + 3 * t)] = a3;
       __syncthreads();
     }
     if (s == LOGN - 2) {
@@ -706,10 +714,10 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
         const int e = B * 2 * t + o;
         u64 w, wp;
         inv_twiddle(tw, twp, m + B, w, wp);
-        u64 a = X[e], b = X[e + t];
+        u64 a = X[sw(e)], b = X[sw(e + t)];
         bf_inv(a, b, w, wp);
-        X[e] = a;
-        X[e + t] = b;
+        X[sw(e)] = a;
+        X[sw(e + t)] = b;
       }
       __syncthreads();
     }
@@ -717,7 +725,7 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
 #pragma unroll
     for (int j = 0; j < 2; j++) {
       const int b = tid + j * NT;
-      u64 x0 = X[b], x1 = X[b + H];
+      u64 x0 = X[sw(b)], x1 = X[sw(b + H)];
       bf_inv(x0, x1, wi, wip);
       const u64 r0 = shoup(x0, c.ninv, c.ninvp), r1 = shoup(x1, c.ninv, c.ninvp);
       u64 p0, p1, q0, q1;  // digits 0 and 1 of coefficients b and b + N/2
@@ -734,10 +742,10 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
         q1 = rr1 >> 20;
       }
       const u64 t0 = shoup_lazy(q0, wf, wfp), t1 = shoup_lazy(q1, wf, wfp);
-      D[b] = p0 + t0;
-      D[b + H] = p0 + 2 * Q - t0;
-      D[N + b] = p1 + t1;
-      D[N + b + H] = p1 + 2 * Q - t1;
+      D[sw(b)] = p0 + t0;
+      D[sw(b + H)] = p0 + 2 * Q - t0;
+      D[N + sw(b)] = p1 + t1;
+      D[N + sw(b + H)] = p1 + 2 * Q - t1;
     }
     __syncthreads();
     // Forward stages 1 .. logn-3 (a radix-2 stage first when logn is even), both digits.
@@ -753,10 +761,10 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
 #pragma unroll
         for (int k = 0; k < 2; k++) {
           u64* x = D + k * N;
-          u64 a = x[e], b = x[e + t];
+          u64 a = x[sw(e)], b = x[sw(e + t)];
           bf_fwd(a, b, w, wp);
-          x[e] = a;
-          x[e + t] = b;
+          x[sw(e)] = a;
+          x[sw(e + t)] = b;
         }
       }
       __syncthreads();
@@ -770,10 +778,11 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
       const u64 wa = tw[m + ib], wap = twp[m + ib];
       const u64 wb = tw[2 * m + 2 * ib], wbp = twp[2 * m + 2 * ib];
       const u64 wc = tw[2 * m + 2 * ib + 1], wcp = twp[2 * m + 2 * ib + 1];
-      u64* x0 = D + e0;
-      u64* x1 = D + N + e0;
-      u64 a0 = x0[0], a1 = x0[h], a2 = x0[t], a3 = x0[t + h];
-      u64 c0 = x1[0], c1 = x1[h], c2 = x1[t], c3 = x1[t + h];
+      const int i0 = sw(e0), i1 = sw(e0 + h), i2 = sw(e0 + t), i3 = sw(e0 + t + h);
+      u64* x0 = D;
+      u64* x1 = D + N;
+      u64 a0 = x0[i0], a1 = x0[i1], a2 = x0[i2], a3 = x0[i3];
+      u64 c0 = x1[i0], c1 = x1[i1], c2 = x1[i2], c3 = x1[i3];
       bf_fwd(a0, a2, wa, wap);
       bf_fwd(c0, c2, wa, wap);
       bf_fwd(a1, a3, wa, wap);
@@ -782,14 +791,14 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
       bf_fwd(c0, c1, wb, wbp);
       bf_fwd(a2, a3, wc, wcp);
       bf_fwd(c2, c3, wc, wcp);
-      x0[0] = a0;
-      x0[h] = a1;
-      x0[t] = a2;
-      x0[t + h] = a3;
-      x1[0] = c0;
-      x1[h] = c1;
-      x1[t] = c2;
-      x1[t + h] = c3;
+      x0[i0] = a0;
+      x0[i1] = a1;
+      x0[i2] = a2;
+      x0[i3] = a3;
+      x1[i0] = c0;
+      x1[i1] = c1;
+      x1[i2] = c2;
+      x1[i3] = c3;
       __syncthreads();
     }
     // Forward stages logn-2, logn-1 of unit tid, both digits, in registers.
@@ -798,10 +807,10 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
       const u64 fa = tw[MF + tid], fap = twp[MF + tid];
       const u64 fb = tw[2 * MF + 2 * tid], fbp = twp[2 * MF + 2 * tid];
       const u64 fc = tw[2 * MF + 2 * tid + 1], fcp = twp[2 * MF + 2 * tid + 1];
-      const ulonglong2 v01 = *reinterpret_cast<const ulonglong2*>(D + l0);
-      const ulonglong2 v23 = *reinterpret_cast<const ulonglong2*>(D + l0 + 2);
-      const ulonglong2 g01 = *reinterpret_cast<const ulonglong2*>(D + N + l0);
-      const ulonglong2 g23 = *reinterpret_cast<const ulonglong2*>(D + N + l0 + 2);
+      const ulonglong2 v01 = *reinterpret_cast<const ulonglong2*>(D + sw(l0));
+      const ulonglong2 v23 = *reinterpret_cast<const ulonglong2*>(D + sw(l0 + 2));
+      const ulonglong2 g01 = *reinterpret_cast<const ulonglong2*>(D + N + sw(l0));
+      const ulonglong2 g23 = *reinterpret_cast<const ulonglong2*>(D + N + sw(l0 + 2));
       d0[0] = v01.x, d0[1] = v01.y, d0[2] = v23.x, d0[3] = v23.y;
       d1[0] = g01.x, d1[1] = g01.y, d1[2] = g23.x, d1[3] = g23.y;
       bf_fwd(d0[0], d0[2], fa, fap);
@@ -1156,6 +1165,93 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
 }
 
 // ------------------------------------------------------------------------------------
+// NoPacking respond (respond.rs:614-643): one RLWE ciphertext (a h_j, b h_j) per column j
+// (plaintext_multiply_columns, respond.rs:585-599) and their sum.
+//   nopack_prep: per query, NTT(a) and NTT(b) in R-form (a expanded from the seed);
+//   nopack_cols: per (query, column), NTT(h_j), the two products (one Montgomery product
+//                each against the R-form operands) and their inverse transforms, written
+//                as ciphertext 1 + j of the query;
+//   nopack_sum:  ciphertext 0 = the sum of the column ciphertexts mod q.
+template <int LOGN>
+__global__ void __launch_bounds__((1 << LOGN) / 4) k_nopack_prep(CrsDev c, const QueryDev* queries, u64 r_mod_q,
+                                                                 u64 r_mod_qp, u64* AB_R, u32* status) {
+  constexpr int N = 1 << LOGN, NT = N / 4;
+  extern __shared__ __align__(16) u64 sm[];
+  u64* xa = sm;
+  u64* xb = sm + N;
+  u64* tw = sm + 2 * N;
+  u64* twp = sm + 3 * N;
+  const u32 qi = blockIdx.x;
+  const QueryDev qd = queries[qi];
+  for (int k = threadIdx.x; k < N; k += NT) {
+    tw[k] = c.tw[k];
+    twp[k] = c.twp[k];
+    xb[k] = reduce128(qd.b[k]);
+  }
+  expand_a<N, NT>(qd, xa, status, qi, 0);  // ends with a barrier
+  {
+    u64* const bufs[2] = {xa, xb};
+    ntt_fwd_r4<LOGN, NT, 2>(bufs, tw, twp);
+  }
+  u64* o = AB_R + (size_t)qi * 2 * N;
+  for (int k = threadIdx.x; k < N; k += NT) {
+    o[k] = shoup(xa[k], r_mod_q, r_mod_qp);
+    o[N + k] = shoup(xb[k], r_mod_q, r_mod_qp);
+  }
+}
+
+template <int LOGN>
+__global__ void __launch_bounds__((1 << LOGN) / 4) k_nopack_cols(CrsDev c, const QueryDev* queries,
+                                                                 const ShardDev* shards, const u64* AB_R, u64* out) {
+  constexpr int N = 1 << LOGN, NT = N / 4;
+  extern __shared__ __align__(16) u64 sm[];
+  u64* x = sm;
+  u64* ya = sm + N;
+  u64* yb = sm + 2 * N;
+  u64* tw = sm + 3 * N;
+  u64* twp = sm + 4 * N;
+  const u32 j = blockIdx.x, qi = blockIdx.y;
+  const QueryDev qd = queries[qi];
+  const u64* col = shards[qd.shard].columns + (size_t)j * N;
+  for (int k = threadIdx.x; k < N; k += NT) {
+    tw[k] = c.tw[k];
+    twp[k] = c.twp[k];
+    x[k] = reduce128(col[k]);
+  }
+  __syncthreads();
+  {
+    u64* const bufs[1] = {x};
+    ntt_fwd_r4<LOGN, NT, 1>(bufs, tw, twp);
+  }
+  const u64* A = AB_R + (size_t)qi * 2 * N;
+  for (int k = threadIdx.x; k < N; k += NT) {
+    const u64 h = csub(csub2(x[k]));
+    ya[k] = mont(A[k], h);
+    yb[k] = mont(A[N + k], h);
+  }
+  __syncthreads();
+  {
+    u64* const bufs[2] = {ya, yb};
+    ntt_inv_r4<LOGN, NT, 2>(bufs, tw, twp);
+  }
+  u64* o = out + ((size_t)qi * (c.gamma + 1) + 1 + j) * 2 * N;
+  for (int k = threadIdx.x; k < N; k += NT) {
+    o[k] = shoup(ya[k], c.ninv, c.ninvp);
+    o[N + k] = shoup(yb[k], c.ninv, c.ninvp);
+  }
+}
+
+__global__ void k_nopack_sum(u32 n, u32 gamma, u64* out) {
+  const u32 qi = blockIdx.y;
+  const u32 k = blockIdx.x * blockDim.x + threadIdx.x;  // over 2n words of a ciphertext
+  if (k >= 2 * n) return;
+  u64* base = out + (size_t)qi * (gamma + 1) * 2 * n;
+  u64 acc = 0;
+  for (u32 j = 1; j <= gamma; j++) acc = addq(acc, base[(size_t)j * 2 * n + k]);
+  base[k] = acc;
+}
+
+// ------------------------------------------------------------------------------------
 // Integer roofline probe: lazy forward butterflies (one Shoup product, two 64-bit adds and
 // a conditional subtraction each, the transforms' unit of work) on values held in
 // registers, eight independent chains per thread, no memory traffic. Its rate is the
@@ -1254,6 +1350,30 @@ cudaError_t compact16(const u64* cols, size_t words, uint16_t* out, u32* wide, c
   const size_t groups = words / 8;
   const unsigned threads = 256;
   k_compact16<<<(unsigned)((groups + threads - 1) / threads), threads, 0, s>>>(cols, groups, out, wide);
+  return cudaGetLastError();
+}
+
+cudaError_t nopack(const CrsDev& c, const QueryDev* queries, const ShardDev* shards, u32 nq, u64 r_mod_q,
+                   u64* AB_R, u64* out, u32* status, cudaStream_t s) {
+  if (nq == 0) return cudaSuccess;
+  IG_DISPATCH_LOGN(c.logn, {
+    constexpr int N = 1 << L;
+    {
+      auto k = k_nopack_prep<L>;
+      const size_t smem = 4 * (size_t)N * 8;
+      cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+      k<<<nq, N / 4, smem, s>>>(c, queries, r_mod_q, shoup_companion(r_mod_q), AB_R, status);
+    }
+    {
+      auto k = k_nopack_cols<L>;
+      const size_t smem = 5 * (size_t)N * 8;
+      cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+      k<<<dim3(c.gamma, nq), N / 4, smem, s>>>(c, queries, shards, AB_R, out);
+    }
+    k_nopack_sum<<<dim3((2 * N + 255) / 256, nq), 256, 0, s>>>(N, c.gamma, out);
+  });
   return cudaGetLastError();
 }
 

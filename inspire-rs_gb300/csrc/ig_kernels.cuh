@@ -95,6 +95,12 @@ cudaError_t respond(const CrsDev& c, const QueryDev* queries, const ShardDev* sh
 
 size_t respond_smem_bytes(const CrsDev& c, bool pair);
 
+// NoPacking respond of `nq` queries: out[q] holds gamma + 1 ciphertexts of (a, b), n words
+// each in coefficient form, the column sum first (respond.rs:614-643). AB_R: nq x 2n words
+// of scratch. r_mod_q = 2^64 mod q.
+cudaError_t nopack(const CrsDev& c, const QueryDev* queries, const ShardDev* shards, u32 nq, u64 r_mod_q,
+                   u64* AB_R, u64* out, u32* status, cudaStream_t s);
+
 // Integer roofline probe: blocks x 256 threads x iters x 8 lazy butterflies in registers.
 cudaError_t butterfly_peak(u64* out, int blocks, int iters, cudaStream_t s);
 }  // namespace igk

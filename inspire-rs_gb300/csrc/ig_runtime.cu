@@ -1206,6 +1206,70 @@ int ig_respond_batch(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_t handle, cons
                       ms_target, a_out, b_out);
 }
 
+// ---- NoPacking respond -------------------------------------------------------------------
+int ig_respond_nopacking_batch(ig_ctx* c, uint64_t dbh, uint32_t count, const uint32_t* shard_ids,
+                               const uint8_t* seeds, const uint64_t* as, const uint64_t* bs, uint64_t* out) {
+  if (!c) return IG_ERR_ARG;
+  if (count == 0 || !shard_ids || (!seeds && !as) || !bs || !out)
+    return fail(c, IG_ERR_ARG, "respond: empty batch or null buffer");
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  DbObj* db = get_db(c, dbh);
+  if (!db) return fail(c, IG_ERR_HANDLE, "unknown database handle %llu", (unsigned long long)dbh);
+  CrsObj& o = *get_crs(c, db->crs);
+  const size_t n = o.n, g = o.gamma;
+  std::unordered_map<u32, u32> local;
+  std::vector<ShardDev> table;
+  for (u32 i = 0; i < count; i++) {
+    const u32 s = shard_ids[i];
+    if (s >= db->num_shards)
+      return fail(c, IG_ERR_ARG, "respond: shard %u not found at dense position %u; encoded database has %u shards", s,
+                  s, db->num_shards);
+    if (!db->shards[s].cols) return fail(c, IG_ERR_ARG, "respond: shard %u holds no columns", s);
+    if (!local.count(s)) {
+      local[s] = (u32)table.size();
+      table.push_back(db->shards[s].dev());
+    }
+  }
+  const size_t seed_bytes = as ? (size_t)count * n * 8 : (size_t)count * 32;
+  const size_t out_words = (size_t)count * (g + 1) * 2 * n;
+  void *d_table, *d_q, *d_seeds, *d_bs, *d_ab, *d_out, *d_status;
+  int rc;
+  if ((rc = scratch(c, "np_table", table.size() * sizeof(ShardDev), &d_table)) ||
+      (rc = scratch(c, "np_queries", count * sizeof(QueryDev), &d_q)) ||
+      (rc = scratch(c, "np_seeds", seed_bytes, &d_seeds)) || (rc = scratch(c, "np_bs", (size_t)count * n * 8, &d_bs)) ||
+      (rc = scratch(c, "np_ab", (size_t)count * 2 * n * 8, &d_ab)) || (rc = scratch(c, "np_out", out_words * 8, &d_out)) ||
+      (rc = scratch(c, "np_status", count * 4, &d_status)))
+    return rc;
+  std::vector<QueryDev> qs(count);
+  for (u32 i = 0; i < count; i++) {
+    qs[i].shard = local[shard_ids[i]];
+    qs[i].reserved = 0;
+    qs[i].seed = as ? nullptr : (const u32*)((const uint8_t*)d_seeds + (size_t)i * 32);
+    qs[i].a = as ? (const u64*)d_seeds + (size_t)i * n : nullptr;
+    qs[i].b = (const u64*)d_bs + (size_t)i * n;
+    qs[i].seat_R = nullptr;
+  }
+  cudaStream_t s = c->stream;
+  if ((rc = stage_h2d(c, d_table, table.data(), table.size() * sizeof(ShardDev))) ||
+      (rc = stage_h2d(c, d_q, qs.data(), count * sizeof(QueryDev))) ||
+      (rc = stage_h2d(c, d_seeds, as ? (const void*)as : (const void*)seeds, seed_bytes)) ||
+      (rc = stage_h2d(c, d_bs, bs, (size_t)count * n * 8)))
+    return rc;
+  IG_CUDA(c, cudaMemsetAsync(d_status, 0, count * 4, s));
+  IG_CUDA(c, igk::nopack(o.dev, (const QueryDev*)d_q, (const ShardDev*)d_table, count, R_MOD_Q, (u64*)d_ab,
+                         (u64*)d_out, (u32*)d_status, s));
+  c->launches += 3;
+  std::vector<u32> status(count);
+  IG_CUDA(c, cudaMemcpyAsync(status.data(), d_status, count * 4, cudaMemcpyDeviceToHost, s));
+  IG_CUDA(c, cudaStreamSynchronize(s));
+  for (u32 i = 0; i < count; i++)
+    if (status[i]) return fail(c, IG_ERR_DEVICE, "query %u: respond kernel status %u", i, status[i]);
+  IG_CUDA(c, cudaMemcpyAsync(out, d_out, out_words * 8, cudaMemcpyDeviceToHost, s));
+  IG_CUDA(c, cudaStreamSynchronize(s));
+  return IG_OK;
+}
+
 int ig_respond_seeded_batch_device(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_t handle, uint32_t count,
                                    const uint32_t* shard_ids, const uint8_t* d_seeds, const uint64_t* d_bs,
                                    uint64_t ms_target, uint64_t* d_a, uint64_t* d_b, uint32_t* d_status) {
@@ -1344,6 +1408,31 @@ int ig_response_encode_device(ig_ctx* c, uint32_t count, const uint64_t* d_a, co
   IG_CUDA(c, igk::wire(d_a, d_b, count, n, retained, bits, modulus, (const uint8_t*)d_t, (u32)len, a_off, a_bytes,
                        b_off, b_bytes, d_out, d_status, c->stream));
   c->launches++;
+  return IG_OK;
+}
+
+int ig_response_encode_full(const uint64_t* cts, uint32_t count, uint32_t n, uint64_t modulus, uint8_t* out,
+                            size_t cap, size_t* len_out) {
+  if (!cts || !len_out || n == 0 || modulus < 2 || count == 0) return IG_ERR_ARG;
+  std::vector<uint8_t> w;
+  auto poly = [&](const u64* c) {
+    if (!put_tight(w, c, n, modulus)) return false;
+    put_u64(w, 1);  // moduli
+    put_u64(w, modulus);
+    put_u64(w, modulus);  // q
+    put_u64(w, n);        // dim
+    put_u64(w, 0);        // crt_q0_inv_mod_q1
+    w.push_back(0);       // is_ntt
+    return true;
+  };
+  put_u32(w, 0);  // ResponseCiphertextWire::Full
+  if (!poly(cts) || !poly(cts + n)) return IG_ERR_SHAPE;
+  put_u64(w, count - 1);  // column_ciphertexts
+  for (u32 j = 1; j < count; j++)
+    if (!poly(cts + (size_t)2 * j * n) || !poly(cts + (size_t)(2 * j + 1) * n)) return IG_ERR_SHAPE;
+  w.push_back(0);  // packing_mode: None
+  *len_out = w.size();
+  if (out) memcpy(out, w.data(), w.size() < cap ? w.size() : cap);
   return IG_OK;
 }
 

@@ -1022,6 +1022,60 @@ u64 orc_response_bytes(const u64* a, const u64* b, u64 n, u64 retained, u64 modu
   return v.size();
 }
 
+// respond (respond.rs:614-643), the NoPacking variant: one RLWE ciphertext (a h_j, b h_j)
+// per column from plaintext_multiply_columns (respond.rs:585-599), and their sum as the
+// response ciphertext. out: (gamma + 1) ciphertexts of (a, b), n words each, the sum first.
+int orc_respond_nopacking(void* cv, const u64* columns, const u64* a, const u64* b, u64* out) {
+  auto* c = (OrcCache*)cv;
+  const size_t n = c->pp->P.n, gamma = c->pp->gamma;
+  const u64 q = c->pp->P.q;
+  try {
+    const Ntt& ntt = *c->pp->ntt;
+    auto cols = unpack_polys(columns, gamma, n);
+    Vec av(a, a + n), bv(b, b + n);
+    std::vector<Vec> ca(gamma), cb(gamma);
+#pragma omp parallel for
+    for (long j = 0; j < (long)gamma; j++) {
+      ca[j] = ntt.mul(av, cols[j]);
+      cb[j] = ntt.mul(bv, cols[j]);
+    }
+    Vec sa = ca[0], sb = cb[0];
+    for (size_t j = 1; j < gamma; j++)
+      for (size_t k = 0; k < n; k++) {
+        sa[k] = (sa[k] + ca[j][k]) % q;
+        sb[k] = (sb[k] + cb[j][k]) % q;
+      }
+    memcpy(out, sa.data(), n * 8);
+    memcpy(out + n, sb.data(), n * 8);
+    for (size_t j = 0; j < gamma; j++) {
+      memcpy(out + (2 + 2 * j) * n, ca[j].data(), n * 8);
+      memcpy(out + (3 + 2 * j) * n, cb[j].data(), n * 8);
+    }
+    return 0;
+  } catch (std::exception& e) {
+    g_err = e.what();
+    return -1;
+  }
+}
+
+// ServerResponse tight wire of an unpacked response (respond.rs:111-176): Full(ciphertext),
+// the column ciphertexts, packing_mode None. cts: `count` ciphertexts of (a, b), the
+// response ciphertext first, then count - 1 column ciphertexts.
+u64 orc_response_bytes_full(const u64* cts, u64 count, u64 n, u64 modulus, uint8_t* out, u64 cap) {
+  Bin w;
+  w.u32(0);
+  write_poly(w, Vec(cts, cts + n), modulus);
+  write_poly(w, Vec(cts + n, cts + 2 * n), modulus);
+  w.u64_(count - 1);
+  for (u64 j = 1; j < count; j++) {
+    write_poly(w, Vec(cts + 2 * j * n, cts + (2 * j + 1) * n), modulus);
+    write_poly(w, Vec(cts + (2 * j + 1) * n, cts + (2 * j + 2) * n), modulus);
+  }
+  w.u8(0);
+  if (out) memcpy(out, w.b.data(), std::min<u64>(cap, w.b.size()));
+  return w.b.size();
+}
+
 // -- KAT cells --------------------------------------------------------------------------
 void* orc_cell_build(u64 n, u64 q, u64 p, double sigma, u64 base, u64 glen, int approx, u64 entry_size, u64 seed,
                      u64 entries) {

@@ -47,6 +47,8 @@ def lib():
             "orc_cache_tables": (None, [V, P]),
             "orc_cache_w_all_ntt": (None, [V, P]),
             "orc_respond_per_query": (I, [V, P, P, P, P, P, P]),
+            "orc_respond_nopacking": (I, [V, P, P, P, P]),
+            "orc_response_bytes_full": (U64, [P, U64, U64, U64, P, U64]),
             "orc_store_build": (V, [V, P, U64]),
             "orc_store_free": (None, [V]),
             "orc_store_sums": (None, [V, V, P]),
@@ -143,6 +145,17 @@ class Cache:
             raise RuntimeError(lib().orc_last_error().decode())
         return ao, bo
 
+    def respond_nopacking(self, columns, a, b):
+        """respond (respond.rs:614-643): (gamma + 1) x 2 x n words, the column sum first."""
+        n, g = self.params.n, self.gamma
+        columns = np.ascontiguousarray(columns, dtype=np.uint64)
+        a = np.ascontiguousarray(a, dtype=np.uint64)
+        b = np.ascontiguousarray(b, dtype=np.uint64)
+        out = np.zeros((g + 1, 2, n), dtype=np.uint64)
+        if lib().orc_respond_nopacking(self.h, _p(columns), _p(a), _p(b), _p(out)):
+            raise RuntimeError(lib().orc_last_error().decode())
+        return out
+
 
 class Store:
     """ShardPackingStore restated: step-1 sums + tags over one shard's columns."""
@@ -224,6 +237,16 @@ def response_bytes(a, b, retained, modulus=DEFAULT_Q) -> bytes:
     L = lib().orc_response_bytes(_p(a), _p(b), len(a), retained, modulus, None, 0)
     out = np.zeros(L, dtype=np.uint8)
     lib().orc_response_bytes(_p(a), _p(b), len(a), retained, modulus, _p(out), L)
+    return out.tobytes()
+
+
+def response_bytes_full(cts, modulus=DEFAULT_Q) -> bytes:
+    """Unpacked ServerResponse bytes: cts is (count, 2, n), the response ciphertext first."""
+    cts = np.ascontiguousarray(cts, dtype=np.uint64)
+    count, _, n = cts.shape
+    L = lib().orc_response_bytes_full(_p(cts), count, n, modulus, None, 0)
+    out = np.zeros(L, dtype=np.uint8)
+    lib().orc_response_bytes_full(_p(cts), count, n, modulus, _p(out), L)
     return out.tobytes()
 
 

@@ -150,3 +150,23 @@ def test_special_modulus_pinned_wire_digests(oracle):
     assert oracle.fnv1a(qb) == int(pins["query"], 16)
     assert oracle.fnv1a(rb) == int(pins["response"], 16)
     assert client.decode(mask, rbody) == cells[1234 * 256:1234 * 256 + 246]
+
+
+def test_nopacking_restatement_decodes(oracle):
+    """The oracle's NoPacking respond (respond.rs:614-643) decodes, through the reference's
+    unpacked extract, to the requested record, and its sum ciphertext is the column sum."""
+    from nopacking_decode import extract
+    P = oracle.Params.d2048()
+    cell = oracle.Cell(P, 32, 0x52455300)
+    cache = oracle.Cache(P, cell.gamma, cell.w_seed)
+    secret = cell.secret()
+    for idx in [0, 1, P.n + 7]:
+        sid, seed, b = cell.next_query(idx)
+        out = cache.respond_nopacking(cell.columns(sid), oracle.expand_seed(seed, P.n), b)
+        assert (out[1:].astype(object).sum(axis=0) % P.q == out[0].astype(object)).all()
+        rec = extract([(out[j, 0], out[j, 1]) for j in range(1, cell.gamma + 1)], secret, P.q, P.p, 32)
+        assert rec == cell.record(idx), idx
+        wire = oracle.response_bytes_full(out)
+        bits = 60
+        poly = 8 + (P.n * bits + 7) // 8 + 41
+        assert len(wire) == 4 + 2 * poly + 8 + cell.gamma * 2 * poly + 1
