@@ -192,6 +192,17 @@ struct ig_ctx {
   cudaStream_t lane_stream[IG_MAX_LANES] = {};
   cudaEvent_t lane_in[IG_MAX_LANES] = {}, lane_done[IG_MAX_LANES] = {};
   bool lane_used[IG_MAX_LANES] = {};
+  // Host-buffer calls over lanes: a lane's mutex is held by one call from before its
+  // launches until its results have left the lane's pinned buffer, so several caller
+  // threads can have batches in flight while the context lock is held only to launch.
+  struct HostLane {
+    std::mutex mu;
+    void* pin = nullptr;  // pinned status, a and b of the call in flight
+    size_t pin_bytes = 0;
+    cudaEvent_t done = nullptr;
+  };
+  HostLane hlane[IG_MAX_LANES];
+  std::atomic<u32> hlane_next{0};
   // special_modulus objects (ig_sm_runtime.cu) and their destructor.
   void* sm = nullptr;
   void (*sm_destroy)(ig_ctx*, void*) = nullptr;
@@ -507,6 +518,8 @@ void ig_ctx_destroy(ig_ctx* c) {
       cudaEventDestroy(c->lane_in[k]);
       cudaEventDestroy(c->lane_done[k]);
     }
+    if (c->hlane[k].pin) cudaFreeHost(c->hlane[k].pin);
+    if (c->hlane[k].done) cudaEventDestroy(c->hlane[k].done);
   }
   if (c->sm && c->sm_destroy) c->sm_destroy(c, c->sm);
   for (auto& kv : c->crs)
@@ -1022,10 +1035,13 @@ int ig_session_contains(ig_ctx* c, uint64_t st, uint64_t handle, int* present) {
 
 // ---- respond ---------------------------------------------------------------------------
 static int resolve_seat(ig_ctx* c, CrsObj& o, uint64_t st, uint64_t handle, const uint64_t* inline_y,
-                        uint32_t inline_rows, uint32_t inline_ntp, const u64** seat_out) {
+                        uint32_t inline_rows, uint32_t inline_ntp, const u64** seat_out, u32 lane = 0) {
   if (inline_y) {
+    // An inline key's seat lives in its caller's lane, which no concurrent call shares.
+    char name[32];
+    snprintf(name, sizeof name, "inline_seat%u", lane);
     void* p;
-    int rc = scratch(c, "inline_seat", (size_t)o.rows * o.n * 8, &p);
+    int rc = scratch(c, name, (size_t)o.rows * o.n * 8, &p);
     if (rc) return rc;
     rc = make_seat(c, o, inline_y, inline_rows, inline_ntp, (u64*)p, false);
     if (rc) return rc;
@@ -1069,7 +1085,13 @@ static int respond_host(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_t handle, c
   if (!c) return IG_ERR_ARG;
   if (count == 0 || !shard_ids || (!seeds && !as) || !bs || !a_out || !b_out)
     return fail(c, IG_ERR_ARG, "respond: empty batch or null buffer");
-  std::lock_guard<std::mutex> lk(c->mu);
+  // The call's lane (lane 0 on the context stream when lanes == 1), held until its results
+  // are copied out; the context lock is held only while the call validates and launches.
+  const u32 lanes = c->lanes;
+  const u32 k = lanes > 1 ? c->hlane_next.fetch_add(1) % lanes : 0;
+  ig_ctx::HostLane& hl = c->hlane[k];
+  std::unique_lock<std::mutex> lane_lock(hl.mu);
+  std::unique_lock<std::mutex> lk(c->mu);
   cudaSetDevice(c->device);
   DbObj* db = get_db(c, dbh);
   if (!db) return fail(c, IG_ERR_HANDLE, "unknown database handle %llu", (unsigned long long)dbh);
@@ -1079,7 +1101,7 @@ static int respond_host(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_t handle, c
     return fail(c, IG_ERR_ARG, "mod-switch target_modulus %llu must be in [p, q) and 1 mod 2d",
                 (unsigned long long)ms_target);
   const u64* seat;
-  int rc = resolve_seat(c, o, st, handle, inline_y, inline_rows, inline_ntp, &seat);
+  int rc = resolve_seat(c, o, st, handle, inline_y, inline_rows, inline_ntp, &seat, k);
   if (rc) return rc;
   // checked_shard (respond.rs:601-611) for every query before any work.
   std::unordered_map<u32, u32> local;
@@ -1104,7 +1126,9 @@ static int respond_host(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_t handle, c
     if (!db->shards[s].sums) transient++;
   void* tsums = nullptr;
   if (transient) {
-    rc = scratch(c, "transient_sums", (size_t)transient * g * n * 8, &tsums);
+    char tname[32];
+    snprintf(tname, sizeof tname, "transient_sums%u", k);
+    rc = scratch(c, tname, (size_t)transient * g * n * 8, &tsums);
     if (rc) return rc;
   }
   u64* zkey;
@@ -1124,12 +1148,30 @@ static int respond_host(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_t handle, c
   }
   void *d_table, *d_q, *d_seeds, *d_bs, *d_a, *d_b, *d_fold, *d_status;
   const size_t seed_bytes = as ? (size_t)count * n * 8 : (size_t)count * 32;
-  if ((rc = scratch(c, "table", table.size() * sizeof(ShardDev), &d_table)) ||
-      (rc = scratch(c, "queries", count * sizeof(QueryDev), &d_q)) || (rc = scratch(c, "seeds", seed_bytes, &d_seeds)) ||
-      (rc = scratch(c, "bs", count * n * 8, &d_bs)) || (rc = scratch(c, "a_out", count * n * 8, &d_a)) ||
-      (rc = scratch(c, "b_out", count * n * 8, &d_b)) || (rc = scratch(c, "fold", count * g * 8, &d_fold)) ||
-      (rc = scratch(c, "status", count * 4, &d_status)))
+  auto lane_scratch = [&](const char* name, size_t bytes, void** out) {
+    char full[48];
+    snprintf(full, sizeof full, "%s%u", name, k);
+    return scratch(c, full, bytes, out);
+  };
+  if ((rc = lane_scratch("table", table.size() * sizeof(ShardDev), &d_table)) ||
+      (rc = lane_scratch("queries", count * sizeof(QueryDev), &d_q)) ||
+      (rc = lane_scratch("seeds", seed_bytes, &d_seeds)) || (rc = lane_scratch("bs", count * n * 8, &d_bs)) ||
+      (rc = lane_scratch("a_out", count * n * 8, &d_a)) || (rc = lane_scratch("b_out", count * n * 8, &d_b)) ||
+      (rc = lane_scratch("fold", count * g * 8, &d_fold)) || (rc = lane_scratch("status", count * 4, &d_status)))
     return rc;
+  // Pinned landing buffer of the lane: status words, then a, then b.
+  const size_t pin_need = (size_t)count * 4 + 2 * (size_t)count * n * 8 + 16;
+  if (hl.pin_bytes < pin_need) {
+    if (hl.pin) cudaFreeHost(hl.pin);
+    hl.pin = nullptr;
+    hl.pin_bytes = 0;
+    IG_CUDA(c, cudaHostAlloc(&hl.pin, pin_need, cudaHostAllocDefault));
+    hl.pin_bytes = pin_need;
+  }
+  if (!hl.done) IG_CUDA(c, cudaEventCreateWithFlags(&hl.done, cudaEventDisableTiming));
+  u32* h_status = (u32*)hl.pin;
+  u64* h_a = (u64*)((uint8_t*)hl.pin + (((size_t)count * 4 + 15) & ~(size_t)15));
+  u64* h_b = h_a + (size_t)count * n;
   std::vector<QueryDev> qs(count);
   for (u32 i = 0; i < count; i++) {
     qs[i].shard = local[shard_ids[i]];
@@ -1139,12 +1181,16 @@ static int respond_host(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_t handle, c
     qs[i].b = (const u64*)d_bs + (size_t)i * n;
     qs[i].seat_R = seat;
   }
-  cudaStream_t s = c->stream;
+  cudaStream_t s = lanes > 1 ? c->lane_stream[k] : c->stream;
   if ((rc = stage_h2d(c, d_table, table.data(), table.size() * sizeof(ShardDev))) ||
       (rc = stage_h2d(c, d_q, qs.data(), count * sizeof(QueryDev))) ||
       (rc = stage_h2d(c, d_seeds, as ? (const void*)as : (const void*)seeds, seed_bytes)) ||
       (rc = stage_h2d(c, d_bs, bs, (size_t)count * n * 8)))
     return rc;
+  if (lanes > 1) {
+    IG_CUDA(c, cudaEventRecord(c->lane_in[k], c->stream));
+    IG_CUDA(c, cudaStreamWaitEvent(s, c->lane_in[k], 0));
+  }
   IG_CUDA(c, cudaMemsetAsync(d_status, 0, count * 4, s));
   // RAVEN_PROFILE_RESPOND (respond.rs:1295-1345): CUDA events around the two regions of the
   // batch, printed to stderr in the reference's line format.
@@ -1153,15 +1199,16 @@ static int respond_host(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_t handle, c
   if (env_prof)
     for (auto& e : env_ev) cudaEventCreate(&e);
   if (env_prof) cudaEventRecord(env_ev[0], s);
-  long pk = prof_begin(c, REGION_SCAN);
+  long pk = prof_begin(c, REGION_SCAN, s);
   IG_CUDA(c, igk::shard_scan(o.dev, (const QueryDev*)d_q, (const ShardDev*)d_table, count, (u64*)d_fold,
                              (u32*)d_status, 0, nullptr, s));
-  prof_end(c, pk);
+  prof_end(c, pk, s);
   if (env_prof) cudaEventRecord(env_ev[1], s);
-  pk = prof_begin(c, REGION_RESPOND);
+  pk = prof_begin(c, REGION_RESPOND, s);
   IG_CUDA(c, igk::respond(o.dev, (const QueryDev*)d_q, (const ShardDev*)d_table, count, (const u64*)d_fold, ms_target,
-                          (u64*)d_a, (u64*)d_b, (u32*)d_status, c->force_serial, count <= c->pair_threshold, s));
-  prof_end(c, pk);
+                          (u64*)d_a, (u64*)d_b, (u32*)d_status, c->force_serial,
+                          (u64)count * lanes <= c->pair_threshold, s));
+  prof_end(c, pk, s);
   if (env_prof) {
     cudaEventRecord(env_ev[2], s);
     cudaEventSynchronize(env_ev[2]);
@@ -1172,20 +1219,26 @@ static int respond_host(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_t handle, c
             (unsigned)count, 1e3 * scan_ms, 1e3 * pack_ms);
     for (auto& e : env_ev) cudaEventDestroy(e);
   }
-  std::vector<u32> status(count);
-  IG_CUDA(c, cudaMemcpyAsync(status.data(), d_status, count * 4, cudaMemcpyDeviceToHost, s));
-  IG_CUDA(c, cudaStreamSynchronize(s));
+  IG_CUDA(c, cudaMemcpyAsync(h_status, d_status, count * 4, cudaMemcpyDeviceToHost, s));
+  IG_CUDA(c, cudaMemcpyAsync(h_a, d_a, (size_t)count * n * 8, cudaMemcpyDeviceToHost, s));
+  IG_CUDA(c, cudaMemcpyAsync(h_b, d_b, (size_t)count * n * 8, cudaMemcpyDeviceToHost, s));
+  IG_CUDA(c, cudaEventRecord(hl.done, s));
+  if (lanes > 1) {
+    IG_CUDA(c, cudaEventRecord(c->lane_done[k], s));
+    c->lane_used[k] = true;
+  }
+  lk.unlock();  // other callers launch while this batch runs
+  IG_CUDA(c, cudaEventSynchronize(hl.done));
   for (u32 i = 0; i < count; i++) {
-    if (status[i] & DEV_TAG_MISMATCH)
+    if (h_status[i] & DEV_TAG_MISMATCH)
       return fail(c, IG_ERR_STORE_REFUSED,
                   "shard %u: packing store refused: a column is not the column the store was built from. The shard "
                   "changed after the build; rebuild the store before serving it",
                   shard_ids[i]);
-    if (status[i]) return fail(c, IG_ERR_DEVICE, "query %u: respond kernel status %u", i, status[i]);
+    if (h_status[i]) return fail(c, IG_ERR_DEVICE, "query %u: respond kernel status %u", i, h_status[i]);
   }
-  IG_CUDA(c, cudaMemcpyAsync(a_out, d_a, (size_t)count * n * 8, cudaMemcpyDeviceToHost, s));
-  IG_CUDA(c, cudaMemcpyAsync(b_out, d_b, (size_t)count * n * 8, cudaMemcpyDeviceToHost, s));
-  IG_CUDA(c, cudaStreamSynchronize(s));
+  memcpy(a_out, h_a, (size_t)count * n * 8);
+  memcpy(b_out, h_b, (size_t)count * n * 8);
   return IG_OK;
 }
 

@@ -96,3 +96,49 @@ def test_device_wire_matches_host_bytes(pkg, oracle):
         assert int(st.abs().sum().item()) == 0
         for r in range(count):
             assert got[r * length:(r + 1) * length] == want[r], (ms, r)
+
+
+def test_concurrent_host_calls_over_lanes(pkg, oracle):
+    """respond_seeded_batch from three threads with three lanes: each call holds a lane
+    while its batch runs, the context lock only while it launches; every answer equals the
+    one-lane answer, including inline-key calls, whose seats live in their caller's lane."""
+    import threading
+    ctx = pkg.Context.default()
+    P = oracle.Params.d2048()
+    cell = oracle.Cell(P, 256, 0x7A4E)
+    crs = pkg.ServerCrs(pkg.InspireParams(ring_dim=P.n, p=P.p), cell.w_seed, cell.gamma)
+    cache = pkg.ServerInspiringCache.new(crs, ctx=ctx)
+    db = pkg.EncodedDatabase.from_columns(cache, [cell.columns(s) for s in range(cell.num_shards)])
+    db.precompute_packing_all()
+    store = pkg.ServerSessionStore.new(ctx)
+    keys = pkg.ClientPackingKeys(cell.keys(), cell.gamma)
+    other = pkg.ClientPackingKeys(np.random.default_rng(3).integers(0, pkg.DEFAULT_Q, cell.keys().shape,
+                                                                   dtype=np.uint64), cell.gamma)
+    h = store.register_server_side(keys, cache)
+    total = cell.num_shards * P.n
+    batches = []
+    for j in range(9):
+        qs = [pkg.SeededBatchQuery(*cell.next_query((j * 13 + k) * 577 % total)) for k in range(6)]
+        src = [pkg.PackingKeySource.Registered(h), pkg.PackingKeySource.Inline(keys),
+               pkg.PackingKeySource.Inline(other)][j % 3]
+        batches.append(pkg.SeededQueryBatch(src, qs))
+    want = [[r.to_binary() for r in pkg.respond_seeded_batch(crs, db, b, cache, store)] for b in batches]
+    got = [None] * len(batches)
+    errors = []
+    ctx.set_lanes(3)
+    try:
+        def caller(t):
+            try:
+                for j in range(t, len(batches), 3):
+                    got[j] = [r.to_binary() for r in pkg.respond_seeded_batch(crs, db, batches[j], cache, store)]
+            except Exception as e:
+                errors.append(e)
+        threads = [threading.Thread(target=caller, args=(t,)) for t in range(3)]
+        for th in threads:
+            th.start()
+        for th in threads:
+            th.join()
+    finally:
+        ctx.set_lanes(1)
+    assert not errors, errors
+    assert got == want
