@@ -880,15 +880,15 @@ __device__ __forceinline__ void inv_half_r4(u64* xh, int s, int rank, const u64*
     inv_twiddle(tw, twp, m + 2 * B, w0, w0p);
     inv_twiddle(tw, twp, m + 2 * B + 1, w1, w1p);
     inv_twiddle(tw, twp, (m >> 1) + B, w2, w2p);
-    u64 a0 = xh[e0], a1 = xh[e0 + t], a2 = xh[e0 + 2 * t], a3 = xh[e0 + 3 * t];
+    u64 a0 = xh[sw(e0)], a1 = xh[sw(e0 + t)], a2 = xh[sw(e0 + 2 * t)], a3 = xh[sw(e0 + 3 * t)];
     bf_inv(a0, a1, w0, w0p);
     bf_inv(a2, a3, w1, w1p);
     bf_inv(a0, a2, w2, w2p);
     bf_inv(a1, a3, w2, w2p);
-    xh[e0] = a0;
-    xh[e0 + t] = a1;
-    xh[e0 + 2 * t] = a2;
-    xh[e0 + 3 * t] = a3;
+    xh[sw(e0)] = a0;
+    xh[sw(e0 + t)] = a1;
+    xh[sw(e0 + 2 * t)] = a2;
+    xh[sw(e0 + 3 * t)] = a3;
   }
   __syncthreads();
 }
@@ -904,10 +904,10 @@ __device__ __forceinline__ void inv_half_r2(u64* xh, int s, int rank, const u64*
   const int e = B * 2 * t + o - rank * (N / 2);
   u64 w, wp;
   inv_twiddle(tw, twp, m + B, w, wp);
-  u64 a = xh[e], b = xh[e + t];
+  u64 a = xh[sw(e)], b = xh[sw(e + t)];
   bf_inv(a, b, w, wp);
-  xh[e] = a;
-  xh[e + t] = b;
+  xh[sw(e)] = a;
+  xh[sw(e + t)] = b;
   __syncthreads();
 }
 
@@ -926,15 +926,15 @@ __device__ __forceinline__ void fwd_half_r4(u64* D, int s, int rank, const u64* 
   const u64 wa = tw[m + i], wap = twp[m + i];
   const u64 wb = tw[2 * m + 2 * i], wbp = twp[2 * m + 2 * i];
   const u64 wc = tw[2 * m + 2 * i + 1], wcp = twp[2 * m + 2 * i + 1];
-  u64 a0 = x[e0], a1 = x[e0 + h], a2 = x[e0 + t], a3 = x[e0 + t + h];
+  u64 a0 = x[sw(e0)], a1 = x[sw(e0 + h)], a2 = x[sw(e0 + t)], a3 = x[sw(e0 + t + h)];
   bf_fwd(a0, a2, wa, wap);
   bf_fwd(a1, a3, wa, wap);
   bf_fwd(a0, a1, wb, wbp);
   bf_fwd(a2, a3, wc, wcp);
-  x[e0] = a0;
-  x[e0 + h] = a1;
-  x[e0 + t] = a2;
-  x[e0 + t + h] = a3;
+  x[sw(e0)] = a0;
+  x[sw(e0 + h)] = a1;
+  x[sw(e0 + t)] = a2;
+  x[sw(e0 + t + h)] = a3;
   __syncthreads();
 }
 
@@ -952,10 +952,10 @@ __device__ __forceinline__ void fwd_half_r2(u64* D, int s, int rank, const u64* 
 #pragma unroll
   for (int k = 0; k < 2; k++) {
     u64* x = D + k * (N / 2);
-    u64 a = x[e], b = x[e + t];
+    u64 a = x[sw(e)], b = x[sw(e + t)];
     bf_fwd(a, b, w, wp);
-    x[e] = a;
-    x[e + t] = b;
+    x[sw(e)] = a;
+    x[sw(e + t)] = b;
   }
   __syncthreads();
 }
@@ -1055,8 +1055,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
       const u64 recv = __shfl_xor_sync(0xffffffffu, dg == 0 ? q : p, 1);
       u64 x0 = dg == 0 ? p : recv, x1 = dg == 0 ? recv : q;  // (slot 4u, 4u+2) or (4u+1, 4u+3)
       bf_inv(x0, x1, wl2, wl2p);
-      xh[4 * u + dg] = x0;
-      xh[4 * u + dg + 2] = x1;
+      xh[sw(4 * u + dg)] = x0;
+      xh[sw(4 * u + dg + 2)] = x1;
     }
     __syncthreads();
     int s = 2;
@@ -1071,7 +1071,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
 #pragma unroll
       for (int j = 0; j < 2; j++) {
         const int b = tid + j * NT;
-        u64 x0 = lo[b], x1 = hi[b];
+        u64 x0 = lo[sw(b)], x1 = hi[sw(b)];
         bf_inv(x0, x1, wi, wip);
         const u64 r0 = shoup(x0, c.ninv, c.ninvp), r1 = shoup(x1, c.ninv, c.ninvp);
         u64 p0, p1, q0, q1;  // digits 0 and 1 of coefficients b and b + H
@@ -1089,8 +1089,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
         }
         // Forward cross stage: slot b gets p + w q, slot b + H gets p - w q.
         const u64 t0 = shoup_lazy(q0, wf, wfp), t1 = shoup_lazy(q1, wf, wfp);
-        D[b] = rank == 0 ? p0 + t0 : p0 + 2 * Q - t0;
-        D[H + b] = rank == 0 ? p1 + t1 : p1 + 2 * Q - t1;
+        D[sw(b)] = rank == 0 ? p0 + t0 : p0 + 2 * Q - t0;
+        D[H + sw(b)] = rank == 0 ? p1 + t1 : p1 + 2 * Q - t1;
       }
     }
     __syncthreads();
@@ -1105,9 +1105,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
     // digit at its own two slots from its partner.
     u64 d0[2], d1[2];
     {
-      const u64* x = D + dg * H + 4 * u;
-      const ulonglong2 v01 = *reinterpret_cast<const ulonglong2*>(x);
-      const ulonglong2 v23 = *reinterpret_cast<const ulonglong2*>(x + 2);
+      const u64* x = D + dg * H;
+      const ulonglong2 v01 = *reinterpret_cast<const ulonglong2*>(x + sw(4 * u));
+      const ulonglong2 v23 = *reinterpret_cast<const ulonglong2*>(x + sw(4 * u + 2));
       u64 a0 = v01.x, a1 = v01.y, a2 = v23.x, a3 = v23.y;
       bf_fwd(a0, a2, fa, fap);
       bf_fwd(a1, a3, fa, fap);
