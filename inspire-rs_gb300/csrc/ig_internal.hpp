@@ -45,6 +45,22 @@ int pair_threshold(ig_ctx* c);
 // rewritten; lane_enter, after the call's staging copies on the context stream, makes the
 // lane wait for them; lane_release marks the lane's work for the next acquire and join.
 int lanes(ig_ctx* c);
+// A host-buffer call over lanes. begin (before the context lock) picks the call's lane and
+// holds its mutex until the call ends; under the context lock, pinned() returns the lane's
+// pinned landing buffer (grown to `bytes`), stream() the stream to launch on (after the
+// call's staging copies: enter()), launched() marks the end of the call's device work; after
+// the context lock is released, wait() blocks until that work is done. With one lane the
+// call runs on the context stream.
+struct HostCall {
+  unsigned k = 0;
+  std::unique_lock<std::mutex> lane_lock;
+};
+void host_call_begin(ig_ctx* c, HostCall& hc);
+int host_call_pinned(ig_ctx* c, HostCall& hc, size_t bytes, void** pin);
+cudaStream_t host_call_stream(ig_ctx* c, HostCall& hc);
+int host_call_enter(ig_ctx* c, HostCall& hc);
+int host_call_launched(ig_ctx* c, HostCall& hc);
+int host_call_wait(ig_ctx* c, HostCall& hc);
 int lane_acquire(ig_ctx* c, cudaStream_t* s, int* lane);
 int lane_enter(ig_ctx* c, int lane);
 int lane_release(ig_ctx* c, int lane);

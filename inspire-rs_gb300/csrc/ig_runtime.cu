@@ -464,6 +464,43 @@ int lane_acquire(ig_ctx* c, cudaStream_t* s, int* lane) {
   *s = c->lane_stream[k];
   return IG_OK;
 }
+void host_call_begin(ig_ctx* c, HostCall& hc) {
+  hc.k = c->lanes > 1 ? c->hlane_next.fetch_add(1) % c->lanes : 0;
+  hc.lane_lock = std::unique_lock<std::mutex>(c->hlane[hc.k].mu);
+}
+int host_call_pinned(ig_ctx* c, HostCall& hc, size_t bytes, void** pin) {
+  ig_ctx::HostLane& hl = c->hlane[hc.k];
+  if (hl.pin_bytes < bytes) {
+    if (hl.pin) cudaFreeHost(hl.pin);
+    hl.pin = nullptr;
+    hl.pin_bytes = 0;
+    IG_CUDA(c, cudaHostAlloc(&hl.pin, bytes, cudaHostAllocDefault));
+    hl.pin_bytes = bytes;
+  }
+  if (!hl.done) IG_CUDA(c, cudaEventCreateWithFlags(&hl.done, cudaEventDisableTiming));
+  *pin = hl.pin;
+  return IG_OK;
+}
+cudaStream_t host_call_stream(ig_ctx* c, HostCall& hc) { return c->lanes > 1 ? c->lane_stream[hc.k] : c->stream; }
+int host_call_enter(ig_ctx* c, HostCall& hc) {
+  if (c->lanes <= 1) return IG_OK;
+  IG_CUDA(c, cudaEventRecord(c->lane_in[hc.k], c->stream));
+  IG_CUDA(c, cudaStreamWaitEvent(c->lane_stream[hc.k], c->lane_in[hc.k], 0));
+  return IG_OK;
+}
+int host_call_launched(ig_ctx* c, HostCall& hc) {
+  cudaStream_t s = host_call_stream(c, hc);
+  IG_CUDA(c, cudaEventRecord(c->hlane[hc.k].done, s));
+  if (c->lanes > 1) {
+    IG_CUDA(c, cudaEventRecord(c->lane_done[hc.k], s));
+    c->lane_used[hc.k] = true;
+  }
+  return IG_OK;
+}
+int host_call_wait(ig_ctx* c, HostCall& hc) {
+  IG_CUDA(c, cudaEventSynchronize(c->hlane[hc.k].done));
+  return IG_OK;
+}
 int lane_enter(ig_ctx* c, int lane) {
   if (lane < 0) return IG_OK;
   IG_CUDA(c, cudaEventRecord(c->lane_in[lane], c->stream));

@@ -487,7 +487,11 @@ int ig_sm_respond_batch(ig_ctx* c, uint64_t server, uint32_t count, const uint64
   if (!c) return IG_ERR_ARG;
   if (!count || !tables || !seats || !seeds || !bodies || !mask_out || !body_out)
     return fail(c, IG_ERR_ARG, "ig_sm_respond_batch: empty batch or null buffer");
-  std::lock_guard<std::mutex> lk(igint::mutex(c));
+  // Lanes (ig_ctx_set_lanes) let several caller threads have batches in flight: the call
+  // holds its lane until its results are copied out, the context lock only to launch.
+  igint::HostCall hc;
+  igint::host_call_begin(c, hc);
+  std::unique_lock<std::mutex> lk(igint::mutex(c));
   cudaSetDevice(igint::device(c));
   SmState& st = state(c);
   ServerObj* o;
@@ -498,35 +502,50 @@ int ig_sm_respond_batch(ig_ctx* c, uint64_t server, uint32_t count, const uint64
   for (size_t k = 0; k < (size_t)count * d; k++)
     if (bodies[k] >= o->q) return fail(c, IG_ERR_SHAPE, "query %zu does not fit the set", k / d);
   void *dq, *dseeds, *dbodies, *dfold, *dmask, *dbody, *dstatus;
-  if ((rc = igint::scratch(c, "sm_q", count * sizeof(SmQueryDev), &dq)) ||
-      (rc = igint::scratch(c, "sm_seeds", count * 32, &dseeds)) ||
-      (rc = igint::scratch(c, "sm_bodies", count * d * 4, &dbodies)) ||
-      (rc = igint::scratch(c, "sm_fold", count * nb * 8, &dfold)) ||
-      (rc = igint::scratch(c, "sm_mask", count * d * 4, &dmask)) ||
-      (rc = igint::scratch(c, "sm_body", count * nb * 4, &dbody)) ||
-      (rc = igint::scratch(c, "sm_status", count * 4, &dstatus)))
+  auto lane_scratch = [&](const char* name, size_t bytes, void** out) {
+    char full[48];
+    snprintf(full, sizeof full, "%s%u", name, hc.k);
+    return igint::scratch(c, full, bytes, out);
+  };
+  if ((rc = lane_scratch("sm_q", count * sizeof(SmQueryDev), &dq)) ||
+      (rc = lane_scratch("sm_seeds", count * 32, &dseeds)) ||
+      (rc = lane_scratch("sm_bodies", count * d * 4, &dbodies)) ||
+      (rc = lane_scratch("sm_fold", count * nb * 8, &dfold)) ||
+      (rc = lane_scratch("sm_mask", count * d * 4, &dmask)) ||
+      (rc = lane_scratch("sm_body", count * nb * 4, &dbody)) ||
+      (rc = lane_scratch("sm_status", count * 4, &dstatus)))
     return rc;
+  // Pinned landing buffer: status words, mask, body.
+  const size_t st_bytes = ((size_t)count * 4 + 15) & ~(size_t)15;
+  void* pin;
+  if ((rc = igint::host_call_pinned(c, hc, st_bytes + (size_t)count * (d + nb) * 4, &pin))) return rc;
+  u32* h_status = (u32*)pin;
+  u32* h_mask = (u32*)((uint8_t*)pin + st_bytes);
+  u32* h_body = h_mask + (size_t)count * d;
   for (u32 i = 0; i < count; i++) {
     qs[i].seed = (const u32*)((const uint8_t*)dseeds + (size_t)i * 32);
     qs[i].body = (const u32*)dbodies + (size_t)i * d;
   }
-  cudaStream_t s = igint::stream(c);
+  cudaStream_t s = igint::host_call_stream(c, hc);
   if ((rc = igint::stage_h2d(c, dq, qs.data(), count * sizeof(SmQueryDev))) ||
       (rc = igint::stage_h2d(c, dseeds, seeds, (size_t)count * 32)) ||
-      (rc = igint::stage_h2d(c, dbodies, bodies, (size_t)count * d * 4)))
+      (rc = igint::stage_h2d(c, dbodies, bodies, (size_t)count * d * 4)) || (rc = igint::host_call_enter(c, hc)))
     return rc;
   SM_CUDA(c, cudaMemsetAsync(dstatus, 0, count * 4, s));
   SM_CUDA(c, igsmk::body_fold(o->dev, (const SmQueryDev*)dq, count, (i64*)dfold, s));
   SM_CUDA(c, igsmk::respond(o->dev, (const SmQueryDev*)dq, count, (const i64*)dfold, (u32*)dmask, (u32*)dbody,
                             (u32*)dstatus, s));
   igint::add_launches(c, 2);
-  std::vector<u32> status(count);
-  SM_CUDA(c, cudaMemcpyAsync(status.data(), dstatus, count * 4, cudaMemcpyDeviceToHost, s));
-  SM_CUDA(c, cudaMemcpyAsync(mask_out, dmask, (size_t)count * d * 4, cudaMemcpyDeviceToHost, s));
-  SM_CUDA(c, cudaMemcpyAsync(body_out, dbody, (size_t)count * nb * 4, cudaMemcpyDeviceToHost, s));
-  SM_CUDA(c, cudaStreamSynchronize(s));
+  SM_CUDA(c, cudaMemcpyAsync(h_status, dstatus, count * 4, cudaMemcpyDeviceToHost, s));
+  SM_CUDA(c, cudaMemcpyAsync(h_mask, dmask, (size_t)count * d * 4, cudaMemcpyDeviceToHost, s));
+  SM_CUDA(c, cudaMemcpyAsync(h_body, dbody, (size_t)count * nb * 4, cudaMemcpyDeviceToHost, s));
+  if ((rc = igint::host_call_launched(c, hc))) return rc;
+  lk.unlock();
+  if ((rc = igint::host_call_wait(c, hc))) return rc;
   for (u32 i = 0; i < count; i++)
-    if (status[i]) return fail(c, IG_ERR_DEVICE, "query %u: respond kernel status %u", i, status[i]);
+    if (h_status[i]) return fail(c, IG_ERR_DEVICE, "query %u: respond kernel status %u", i, h_status[i]);
+  memcpy(mask_out, h_mask, (size_t)count * d * 4);
+  memcpy(body_out, h_body, (size_t)count * nb * 4);
   return IG_OK;
 }
 

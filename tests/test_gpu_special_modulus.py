@@ -90,3 +90,40 @@ def test_refusals(sm, oracle):
         server.respond(table, seat, sm.Query(bytes(32), body))
     with pytest.raises(load_package().PirError, match="ring dimension"):
         sm.Server(sm.Params(ring_dim=1024, gamma=256, cell_bytes=128, record_bytes=120))
+
+
+def test_concurrent_callers_over_lanes(oracle):
+    """Server::respond from three threads over three lanes equals the one-lane answers."""
+    import threading
+    pkg = load_package()
+    ctx = pkg.Context.default()
+    sm = pkg.special_modulus
+    server = sm.Server(ctx=ctx)
+    rng = np.random.default_rng(31)
+    cells = np.zeros((2048, 256), dtype=np.uint8)
+    cells[:, :246] = rng.integers(0, 256, (2048, 246), dtype=np.uint8)
+    table = server.table(cells.tobytes())
+    seat = server.seat(sm.PackingKey(rng.bytes(32), rng.integers(0, 536_813_569, 2048, dtype=np.uint32),
+                                     rng.integers(0, 2_147_389_441, 2048, dtype=np.uint32)))
+    batches = [[sm.Query(rng.bytes(32), rng.integers(0, 536_813_569, 2048, dtype=np.uint32)) for _ in range(4)]
+               for _ in range(6)]
+    want = [[r.to_bytes() for r in server.respond_batch([table] * 4, [seat] * 4, b)] for b in batches]
+    got = [None] * len(batches)
+    errors = []
+    ctx.set_lanes(3)
+    try:
+        def caller(t):
+            try:
+                for j in range(t, len(batches), 3):
+                    got[j] = [r.to_bytes() for r in server.respond_batch([table] * 4, [seat] * 4, batches[j])]
+            except Exception as e:
+                errors.append(e)
+        threads = [threading.Thread(target=caller, args=(t,)) for t in range(3)]
+        for th in threads:
+            th.start()
+        for th in threads:
+            th.join()
+    finally:
+        ctx.set_lanes(1)
+    assert not errors, errors
+    assert got == want
