@@ -450,7 +450,7 @@ def run_gb300(args, rank, world):
 
 
 # ------------------------------------------------------------------------------------
-# special_modulus workload (configs[2]): ring2048_cell256, 2^22 cells of 256 bytes
+# special_modulus workload: ring2048_cell256, 2^22 cells of 256 bytes
 # (2048 shards, 1 GiB), a ShardTable per shard, 8 seated keys, batches of 256 uniform rows.
 SM_METRIC = "special_modulus respond queries/s (batch 256, 2^22 x 256 B cells, 8 seated keys)"
 SM_CONFIG = {"workload": "special_modulus ring2048_cell256: 2^22 cells x 256 B (2048 shards), ShardTable per "

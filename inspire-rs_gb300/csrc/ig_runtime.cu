@@ -1124,10 +1124,9 @@ static int respond_host(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_t handle, c
     return fail(c, IG_ERR_ARG, "respond: empty batch or null buffer");
   // The call's lane (lane 0 on the context stream when lanes == 1), held until its results
   // are copied out; the context lock is held only while the call validates and launches.
-  const u32 lanes = c->lanes;
-  const u32 k = lanes > 1 ? c->hlane_next.fetch_add(1) % lanes : 0;
-  ig_ctx::HostLane& hl = c->hlane[k];
-  std::unique_lock<std::mutex> lane_lock(hl.mu);
+  igint::HostCall hc;
+  igint::host_call_begin(c, hc);
+  const u32 lanes = c->lanes, k = hc.k;
   std::unique_lock<std::mutex> lk(c->mu);
   cudaSetDevice(c->device);
   DbObj* db = get_db(c, dbh);
@@ -1197,17 +1196,11 @@ static int respond_host(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_t handle, c
       (rc = lane_scratch("fold", count * g * 8, &d_fold)) || (rc = lane_scratch("status", count * 4, &d_status)))
     return rc;
   // Pinned landing buffer of the lane: status words, then a, then b.
-  const size_t pin_need = (size_t)count * 4 + 2 * (size_t)count * n * 8 + 16;
-  if (hl.pin_bytes < pin_need) {
-    if (hl.pin) cudaFreeHost(hl.pin);
-    hl.pin = nullptr;
-    hl.pin_bytes = 0;
-    IG_CUDA(c, cudaHostAlloc(&hl.pin, pin_need, cudaHostAllocDefault));
-    hl.pin_bytes = pin_need;
-  }
-  if (!hl.done) IG_CUDA(c, cudaEventCreateWithFlags(&hl.done, cudaEventDisableTiming));
-  u32* h_status = (u32*)hl.pin;
-  u64* h_a = (u64*)((uint8_t*)hl.pin + (((size_t)count * 4 + 15) & ~(size_t)15));
+  const size_t st_bytes = ((size_t)count * 4 + 15) & ~(size_t)15;
+  void* pin;
+  if ((rc = igint::host_call_pinned(c, hc, st_bytes + 2 * (size_t)count * n * 8, &pin))) return rc;
+  u32* h_status = (u32*)pin;
+  u64* h_a = (u64*)((uint8_t*)pin + st_bytes);
   u64* h_b = h_a + (size_t)count * n;
   std::vector<QueryDev> qs(count);
   for (u32 i = 0; i < count; i++) {
@@ -1218,16 +1211,12 @@ static int respond_host(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_t handle, c
     qs[i].b = (const u64*)d_bs + (size_t)i * n;
     qs[i].seat_R = seat;
   }
-  cudaStream_t s = lanes > 1 ? c->lane_stream[k] : c->stream;
+  cudaStream_t s = igint::host_call_stream(c, hc);
   if ((rc = stage_h2d(c, d_table, table.data(), table.size() * sizeof(ShardDev))) ||
       (rc = stage_h2d(c, d_q, qs.data(), count * sizeof(QueryDev))) ||
       (rc = stage_h2d(c, d_seeds, as ? (const void*)as : (const void*)seeds, seed_bytes)) ||
-      (rc = stage_h2d(c, d_bs, bs, (size_t)count * n * 8)))
+      (rc = stage_h2d(c, d_bs, bs, (size_t)count * n * 8)) || (rc = igint::host_call_enter(c, hc)))
     return rc;
-  if (lanes > 1) {
-    IG_CUDA(c, cudaEventRecord(c->lane_in[k], c->stream));
-    IG_CUDA(c, cudaStreamWaitEvent(s, c->lane_in[k], 0));
-  }
   IG_CUDA(c, cudaMemsetAsync(d_status, 0, count * 4, s));
   // RAVEN_PROFILE_RESPOND (respond.rs:1295-1345): CUDA events around the two regions of the
   // batch, printed to stderr in the reference's line format.
@@ -1259,13 +1248,9 @@ static int respond_host(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_t handle, c
   IG_CUDA(c, cudaMemcpyAsync(h_status, d_status, count * 4, cudaMemcpyDeviceToHost, s));
   IG_CUDA(c, cudaMemcpyAsync(h_a, d_a, (size_t)count * n * 8, cudaMemcpyDeviceToHost, s));
   IG_CUDA(c, cudaMemcpyAsync(h_b, d_b, (size_t)count * n * 8, cudaMemcpyDeviceToHost, s));
-  IG_CUDA(c, cudaEventRecord(hl.done, s));
-  if (lanes > 1) {
-    IG_CUDA(c, cudaEventRecord(c->lane_done[k], s));
-    c->lane_used[k] = true;
-  }
+  if ((rc = igint::host_call_launched(c, hc))) return rc;
   lk.unlock();  // other callers launch while this batch runs
-  IG_CUDA(c, cudaEventSynchronize(hl.done));
+  if ((rc = igint::host_call_wait(c, hc))) return rc;
   for (u32 i = 0; i < count; i++) {
     if (h_status[i] & DEV_TAG_MISMATCH)
       return fail(c, IG_ERR_STORE_REFUSED,
