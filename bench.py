@@ -101,23 +101,29 @@ class ClockSampler:
 
     def __init__(self, device):
         self.device, self.proc, self.lines = device, None, []
+        self.first = threading.Event()
+        self.t_begin = self.t_end = None
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            self.first.wait(timeout=5.0)  # the sampler is live before the timed work starts
         except Exception:
             self.proc = None
+        self.t_begin = time.perf_counter()
         return self
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
+            self.first.set()
 
     def __exit__(self, *a):
+        self.t_end = time.perf_counter()
         if self.proc:
             self.proc.terminate()
             try:
@@ -128,7 +134,9 @@ class ClockSampler:
     def summary(self):
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        # Samples taken inside the sampled region; a line arrives just after its sample.
+        inside = [ln for t, ln in self.lines if self.t_begin is not None and self.t_begin <= t <= self.t_end + 0.05]
+        for ln in inside:
             f = [x.strip() for x in ln.split(",")]
             if len(f) < 9:
                 continue
@@ -141,7 +149,8 @@ class ClockSampler:
                 if v.lower() == "active":
                     reasons.add(nm)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "interval_ms": 50,
+                "region_s": None if self.t_end is None else round(self.t_end - self.t_begin, 3)}
 
 
 def dist_setup(n_gpus):
@@ -693,7 +702,9 @@ def run_cfg5(args, rank, world):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default: 300 for config 2 and 100 for config 3, a timed region of about "
+                         "half a second that the 50 ms clock sampler sees; 20 for the reference arm)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -707,6 +718,8 @@ def main():
                     help="shards in the database (smaller values only for profiling captures)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.steps is None:
+        args.steps = 20 if args.impl == "reference" else {2: 300, 3: 100, 5: 0}[args.config]
     rank, world = dist_setup(args.gpus)
     if args.impl == "reference":
         if rank != 0:

@@ -11,16 +11,25 @@ typedef uint64_t u64;
 typedef int64_t i64;
 
 // Prime32 (arith.rs:13-102): canonical words, mont(a, b) = a b 2^-32 mod m.
+// x - k where x >= k, else x, for any 32-bit x and k: when x < k the difference wraps
+// above x, so the smaller of the two is the answer.
+__host__ __device__ __forceinline__ u32 csub_by(u32 x, u32 k) {
+  const u32 d = x - k;
+  return d < x ? d : x;
+}
+
 struct Prime32 {
   u32 m, neg_minv;
-  __host__ __device__ __forceinline__ u32 csub(u32 x) const { return x >= m ? x - m : x; }
+  __host__ __device__ __forceinline__ u32 csub(u32 x) const { return csub_by(x, m); }
   __host__ __device__ __forceinline__ u32 add(u32 a, u32 b) const { return csub(a + b); }
   __host__ __device__ __forceinline__ u32 sub(u32 a, u32 b) const { return csub(a + m - b); }
-  __host__ __device__ __forceinline__ u32 mont(u32 a, u32 b) const {
+  // a b 2^-32 mod m in [0, 2m), for any 32-bit a and b < m: a b + k m < 2^33 m.
+  __host__ __device__ __forceinline__ u32 montl(u32 a, u32 b) const {
     const u64 t = (u64)a * b;
     const u32 k = (u32)t * neg_minv;
-    return csub((u32)((t + (u64)k * m) >> 32));
+    return (u32)((t + (u64)k * m) >> 32);
   }
+  __host__ __device__ __forceinline__ u32 mont(u32 a, u32 b) const { return csub(montl(a, b)); }
   __host__ __device__ __forceinline__ u32 small(i64 x) const { return (u32)x + (m & (u32)(x >> 63)); }
   __host__ __device__ __forceinline__ i64 centred(u32 x) const { return x > (m >> 1) ? (i64)x - (i64)m : (i64)x; }
 };

@@ -264,7 +264,14 @@ __device__ __forceinline__ u32 q_to_p(const SmDev& c, u32 x) {
 // INTT_p, and the last forward pass of NTT_q with the link's update. Each inverse's last
 // stage (t = n/2, carrying 1/n), the limb lift and the next forward's first stage (the
 // same index pairs) run as one pass in place.
-template <int LOGN>
+//
+// LAZY (q below 2^29, so 8q < 2^32): the q-limb passes skip most reductions. montl leaves
+// [0, 2q) for any 32-bit left operand, and the values between passes stay in [0, 4q)
+// through INTT_q and in [0, 6q) through NTT_q; every sum and every difference (offset by
+// 2q or 4q) stays below 8q. Values are brought to [0, q) where the arithmetic needs a
+// residue: before the lift to p and at the end of the chain. The p limb (near 2^31) has
+// no headroom and stays reduced.
+template <int LOGN, bool LAZY>
 __global__ void __launch_bounds__((1 << LOGN) / 4, 2)
     k_sm_respond(SmDev c, const SmQueryDev* queries, const i64* fold, u32* mask_out, u32* body_out, u32* status) {
   constexpr int N = 1 << LOGN, NT = N / 4, H = N / 2;
@@ -384,6 +391,69 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 2)
     x[2] = P.add(a2, v);
     x[3] = P.sub(a2, v);
   };
+  const u32 Q2 = 2 * PQ.m, Q4 = 4 * PQ.m, Q6 = 6 * PQ.m;
+  // Lazy INTT_q passes: inputs below 4q, outputs below 4q (three reductions per unit).
+  auto inv_unit_lazy = [&](u32 w0, u32 w1, u32 w2, u32& a0, u32& a1, u32& a2, u32& a3) {
+    const u32 d01 = PQ.montl(a0 + Q4 - a1, w0);
+    const u32 s01 = csub_by(a0 + a1, Q4);
+    const u32 d23 = PQ.montl(a2 + Q4 - a3, w1);
+    const u32 s23 = csub_by(a2 + a3, Q4);
+    a0 = csub_by(s01 + s23, Q4);
+    a2 = PQ.montl(s01 + Q4 - s23, w2);
+    a1 = d01 + d23;
+    a3 = PQ.montl(d01 + Q2 - d23, w2);
+  };
+  auto inv_first_lazy = [&](u32 a0, u32 a1, u32 a2, u32 a3) {
+    inv_unit_lazy(iq[H + 2 * tid], iq[H + 2 * tid + 1], iq[H / 2 + tid], a0, a1, a2, a3);
+    *reinterpret_cast<uint4*>(buf + l0) = make_uint4(a0, a1, a2, a3);
+  };
+  auto inv_middle_lazy = [&]() {
+#pragma unroll 1
+    for (int s = 2; s + 1 < LOGN; s += 2) {
+      const int t = 1 << s, m = N >> (s + 1);
+      const int B = tid >> s, o = tid & (t - 1);
+      const int e0 = B * 4 * t + o;
+      u32 a0 = buf[e0], a1 = buf[e0 + t], a2 = buf[e0 + 2 * t], a3 = buf[e0 + 3 * t];
+      inv_unit_lazy(iq[m + 2 * B], iq[m + 2 * B + 1], iq[(m >> 1) + B], a0, a1, a2, a3);
+      buf[e0] = a0;
+      buf[e0 + t] = a1;
+      buf[e0 + 2 * t] = a2;
+      buf[e0 + 3 * t] = a3;
+      __syncthreads();
+    }
+  };
+  // Lazy NTT_q passes: inputs below 6q, outputs below 6q (two reductions per unit).
+  auto fwd_unit_lazy = [&](u32 wa, u32 wb, u32 wc, u32& a0, u32& a1, u32& a2, u32& a3) {
+    u32 v = PQ.montl(a2, wa);
+    a2 = a0 + Q2 - v;  // below 8q
+    a0 = a0 + v;
+    v = PQ.montl(a3, wa);
+    a3 = a1 + Q2 - v;
+    a1 = a1 + v;
+    a0 = csub_by(a0, Q4);  // below 4q
+    v = PQ.montl(a1, wb);
+    a1 = a0 + Q2 - v;
+    a0 = a0 + v;
+    a2 = csub_by(a2, Q4);
+    v = PQ.montl(a3, wc);
+    a3 = a2 + Q2 - v;
+    a2 = a2 + v;
+  };
+  auto fwd_middle_lazy = [&]() {
+#pragma unroll 1
+    for (int s = 1; s < LOGN - 2; s += 2) {
+      const int t = N >> (s + 1), m = 1 << s, h = t >> 1;
+      const int i = tid / h, o = tid - i * h;
+      const int e0 = i * 2 * t + o;
+      u32 a0 = buf[e0], a1 = buf[e0 + h], a2 = buf[e0 + t], a3 = buf[e0 + t + h];
+      fwd_unit_lazy(fq[m + i], fq[2 * m + 2 * i], fq[2 * m + 2 * i + 1], a0, a1, a2, a3);
+      buf[e0] = a0;
+      buf[e0 + h] = a1;
+      buf[e0 + t] = a2;
+      buf[e0 + t + h] = a3;
+      __syncthreads();
+    }
+  };
 #pragma unroll 1
   for (int i = (int)c.gamma - 2; i >= 0; i--) {
     const uint4 sv4 = *reinterpret_cast<const uint4*>(qd.step1_R + (size_t)i * N + l0);
@@ -392,16 +462,23 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 2)
     const u32 gp = c.gpow[i];
 #pragma unroll
     for (int k = 0; k < 4; k++) tb[k] = s_tab[((gp * et[k]) & M2N) >> 1];
-    inv_first(PQ, iq, cur[0], cur[1], cur[2], cur[3]);
-    __syncthreads();
-    inv_middle(PQ, iq);
+    if constexpr (LAZY) {
+      inv_first_lazy(cur[0], cur[1], cur[2], cur[3]);
+      __syncthreads();
+      inv_middle_lazy();
+    } else {
+      inv_first(PQ, iq, cur[0], cur[1], cur[2], cur[3]);
+      __syncthreads();
+      inv_middle(PQ, iq);
+    }
     // INTT_q's last stage with 1/n, the lift to p, and NTT_p's first stage, pair (b, b + n/2).
+    // The lift takes residues, so both products are reduced fully here.
 #pragma unroll
     for (int r = 0; r < 2; r++) {
       const int b = tid + r * NT;
       const u32 u = buf[b], v = buf[b + H];
       const u32 y0 = q_to_p(c, PQ.mont(u + v, c.lq.n_inv));
-      const u32 y1 = q_to_p(c, PQ.mont(u + PQ.m - v, c.lq.last));
+      const u32 y1 = q_to_p(c, PQ.mont(u + (LAZY ? Q4 : PQ.m) - v, c.lq.last));
       const u32 z = PP.mont(y1, fp[1]);
       buf[b] = PP.add(y0, z);
       buf[b + H] = PP.sub(y0, z);
@@ -427,19 +504,48 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 2)
       const u32 u = buf[b], v = buf[b + H];
       const u32 y0 = p_to_q(c, PP.mont(u + v, c.lp.n_inv));
       const u32 y1 = p_to_q(c, PP.mont(u + PP.m - v, c.lp.last));
-      const u32 z = PQ.mont(y1, fq[1]);
-      buf[b] = PQ.add(y0, z);
-      buf[b + H] = PQ.sub(y0, z);
+      if constexpr (LAZY) {
+        const u32 z = PQ.montl(y1, fq[1]);
+        buf[b] = y0 + z;  // below 3q
+        buf[b + H] = y0 + Q2 - z;
+      } else {
+        const u32 z = PQ.mont(y1, fq[1]);
+        buf[b] = PQ.add(y0, z);
+        buf[b + H] = PQ.sub(y0, z);
+      }
     }
     __syncthreads();
-    fwd_middle(PQ, fq);
     u32 rq[4];
-    fwd_last(PQ, fq, rq);
+    if constexpr (LAZY) {
+      fwd_middle_lazy();
+      constexpr int MF = 1 << (LOGN - 2);
+      const uint4 v4 = *reinterpret_cast<const uint4*>(buf + l0);
+      rq[0] = v4.x, rq[1] = v4.y, rq[2] = v4.z, rq[3] = v4.w;
+      fwd_unit_lazy(fq[MF + tid], fq[2 * MF + 2 * tid], fq[2 * MF + 2 * tid + 1], rq[0], rq[1], rq[2], rq[3]);
+      // cur below 4q, rq below 6q: R_i = a S_i + (cur w_q - rq) / p lands below 4q, acc_q
+      // stays below 2q.
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        const u32 cq = PQ.montl(cur[k], wq[tb[k]]);
+        accq[k] = csub_by(accq[k] + PQ.montl(cur[k], kq[tb[k]]), Q2);
+        cur[k] = PQ.montl(a[tb[k]], sv[k]) + PQ.montl(cq + Q6 - rq[k], c.p_inv_R);
+      }
+    } else {
+      fwd_middle(PQ, fq);
+      fwd_last(PQ, fq, rq);
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        const u32 cq = PQ.mont(cur[k], wq[tb[k]]);
+        accq[k] = PQ.add(accq[k], PQ.mont(cur[k], kq[tb[k]]));
+        cur[k] = PQ.add(PQ.mont(a[tb[k]], sv[k]), PQ.mont(PQ.sub(cq, rq[k]), c.p_inv_R));
+      }
+    }
+  }
+  if constexpr (LAZY) {
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-      const u32 cq = PQ.mont(cur[k], wq[tb[k]]);
-      accq[k] = PQ.add(accq[k], PQ.mont(cur[k], kq[tb[k]]));
-      cur[k] = PQ.add(PQ.mont(a[tb[k]], sv[k]), PQ.mont(PQ.sub(cq, rq[k]), c.p_inv_R));
+      cur[k] = PQ.csub(csub_by(cur[k], Q2));
+      accq[k] = PQ.csub(accq[k]);
     }
   }
   // mask = INTT_q(R_0); body = mod_down(INTT_q(acc_q), INTT_p(acc_p)) + fold.
@@ -510,9 +616,12 @@ cudaError_t respond(const SmDev& c, const SmQueryDev* queries, u32 nq, const i64
   if (nq == 0) return cudaSuccess;
   if (c.logn != 11) return cudaErrorInvalidValue;
   const size_t smem = (10 * (size_t)c.n) * 4 + 2 * (size_t)c.n * 2;
-  cudaError_t e = cudaFuncSetAttribute(k_sm_respond<11>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  // The lazy q-limb passes need every value below 8q to fit 32 bits.
+  const bool lazy = (u64)c.lq.p.m * 8 <= (1ULL << 32);
+  auto kern = lazy ? k_sm_respond<11, true> : k_sm_respond<11, false>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  k_sm_respond<11><<<nq, 512, smem, s>>>(c, queries, fold, mask_out, body_out, status);
+  kern<<<nq, 512, smem, s>>>(c, queries, fold, mask_out, body_out, status);
   return cudaGetLastError();
 }
 

@@ -329,6 +329,7 @@ def _sm_lib():
         V, P, U64 = ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64
         sig = {
             "orc_sm_server_new": (V, []), "orc_sm_server_free": (None, [V]),
+            "orc_sm_server_new_q": (V, [U64]), "orc_sm_client_new_q": (V, [P, U64]),
             "orc_sm_client_new": (V, [P]), "orc_sm_client_free": (None, [V]),
             "orc_sm_client_key": (None, [V, P, P, P]), "orc_sm_client_key_bytes": (U64, [V, P, U64]),
             "orc_sm_client_query": (None, [V, U64, P, P]), "orc_sm_client_decode": (U64, [V, P, P, P]),
@@ -355,8 +356,9 @@ def _bytes_of(fn, *args):
 
 
 class SmServer:
-    def __init__(self):
-        self.h = _sm_lib().orc_sm_server_new()
+    def __init__(self, q=None):
+        """q: another ciphertext prime for the ring2048_cell256 set (default 536813569)."""
+        self.h = _sm_lib().orc_sm_server_new() if q is None else _sm_lib().orc_sm_server_new_q(q)
 
     def __del__(self):
         if getattr(self, "h", None):
@@ -407,9 +409,9 @@ class SmSeat:
 class SmClient:
     """Client::from_seed of the reference (special_modulus/client.rs:137-143)."""
 
-    def __init__(self, seed: bytes):
+    def __init__(self, seed: bytes, q=None):
         s = np.frombuffer(seed, dtype=np.uint8).copy()
-        self.h = _sm_lib().orc_sm_client_new(_p(s))
+        self.h = _sm_lib().orc_sm_client_new(_p(s)) if q is None else _sm_lib().orc_sm_client_new_q(_p(s), q)
 
     def __del__(self):
         if getattr(self, "h", None):

@@ -515,8 +515,19 @@ extern "C" {
 
 void* orc_sm_server_new() { return new Server(Params()); }
 void orc_sm_server_free(void* s) { delete (Server*)s; }
+// The same parameter set over another ciphertext prime q (Params::validate's rules).
+void* orc_sm_server_new_q(uint64_t q) {
+  Params P;
+  P.q = q;
+  return new Server(P);
+}
 
 void* orc_sm_client_new(const uint8_t* seed) { return new Client(Params(), seed); }
+void* orc_sm_client_new_q(const uint8_t* seed, uint64_t q) {
+  Params P;
+  P.q = q;
+  return new Client(P, seed);
+}
 void orc_sm_client_free(void* c) { delete (Client*)c; }
 
 // Key parts: mask_seed (32 B), q limb and p limb (d words each, coefficient form).

@@ -127,3 +127,27 @@ def test_concurrent_callers_over_lanes(oracle):
         ctx.set_lanes(1)
     assert not errors, errors
     assert got == want
+
+
+@pytest.mark.parametrize("q", [536_903_681, 1_073_750_017])
+def test_other_ciphertext_primes_match_oracle(oracle, q):
+    """Ciphertext primes at or above 2^29 leave no room for the kernel's unreduced q-limb
+    values (below 8q), so they take the fully reduced passes; the answers equal the oracle's
+    over the same prime and decode to the record."""
+    pkg = load_package()
+    sm = pkg.special_modulus
+    server = sm.Server(sm.Params(q=q))
+    oserver = oracle.SmServer(q=q)
+    rng = np.random.default_rng(q % 1000)
+    cells = np.zeros((2048, 256), dtype=np.uint8)
+    cells[:, :246] = rng.integers(0, 256, (2048, 246), dtype=np.uint8)
+    table, otable = server.table(cells.tobytes()), oserver.table(cells.tobytes())
+    client = oracle.SmClient(bytes([77] * 32), q=q)
+    seat, oseat = server.seat(sm.PackingKey(*client.key())), oserver.seat(client.key())
+    rows = [0, 1, 1000, 2047]
+    qs = [client.query(r) for r in rows]
+    out = server.respond_batch([table] * len(rows), [seat] * len(rows), [sm.Query(s, b) for s, b in qs])
+    for row, (seed, body), r in zip(rows, qs, out):
+        mask, obody = oserver.respond(otable, oseat, seed, body)
+        assert (r.mask == mask).all() and (r.body == obody).all(), row
+        assert client.decode(r.mask, r.body) == cells[row, :246].tobytes()
