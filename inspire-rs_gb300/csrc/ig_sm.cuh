@@ -1,5 +1,5 @@
 // special_modulus respond path (reference src/special_modulus/): 32-bit words, ciphertext
-// prime q < 2^29, special prime p < 2^31, Montgomery with R = 2^32 throughout.
+// prime q below the special prime p < 2^31, Montgomery with R = 2^32 throughout.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -10,7 +10,6 @@ typedef uint32_t u32;
 typedef uint64_t u64;
 typedef int64_t i64;
 
-// Prime32 (arith.rs:13-102): canonical words, mont(a, b) = a b 2^-32 mod m.
 // x - k where x >= k, else x, for any 32-bit x and k: when x < k the difference wraps
 // above x, so the smaller of the two is the answer.
 __host__ __device__ __forceinline__ u32 csub_by(u32 x, u32 k) {
@@ -18,6 +17,7 @@ __host__ __device__ __forceinline__ u32 csub_by(u32 x, u32 k) {
   return d < x ? d : x;
 }
 
+// Prime32 (arith.rs:13-102): canonical words, mont(a, b) = a b 2^-32 mod m.
 struct Prime32 {
   u32 m, neg_minv;
   __host__ __device__ __forceinline__ u32 csub(u32 x) const { return csub_by(x, m); }
@@ -54,6 +54,7 @@ struct SmDev {
   const u32* pow_root_R;     // w0^e * 2^32 mod q, e < 2n (store fold)
   u32 inv_gamma_RR;          // gamma^-1 * 2^64 mod q: mont(x, .) = x gamma^-1 2^32
   u32 p_over_q, neg_off, p_inv_R;  // lifts between the limbs and 1/p mod q (R-form)
+  u32 q_mu;                        // floor(2^32 / q), the Barrett factor of the lazy lift
 };
 
 struct SmQueryDev {

@@ -250,6 +250,13 @@ __device__ __forceinline__ u32 p_to_q(const SmDev& c, u32 r) {
   for (u32 k = 0; k < c.p_over_q; k++) base = Q.csub(base);
   return r > (c.lp.p.m >> 1) ? Q.add(base, c.neg_off) : base;
 }
+// The same lift left in [0, 3q) for the lazy q passes: one Barrett step (the quotient
+// estimate from floor(2^32 / q) is the true quotient or one less, r being below 2^32)
+// leaves r mod q plus at most q, and the centred offset adds less than q.
+__device__ __forceinline__ u32 p_to_q_lazy(const SmDev& c, u32 r) {
+  const u32 base = r - __umulhi(r, c.q_mu) * c.lq.p.m;
+  return r > (c.lp.p.m >> 1) ? base + c.neg_off : base;
+}
 __device__ __forceinline__ u32 q_to_p(const SmDev& c, u32 x) {
   return x > (c.lq.p.m >> 1) ? x + (c.lp.p.m - c.lq.p.m) : x;
 }
@@ -502,13 +509,14 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 2)
     for (int r = 0; r < 2; r++) {
       const int b = tid + r * NT;
       const u32 u = buf[b], v = buf[b + H];
-      const u32 y0 = p_to_q(c, PP.mont(u + v, c.lp.n_inv));
-      const u32 y1 = p_to_q(c, PP.mont(u + PP.m - v, c.lp.last));
+      const u32 xp0 = PP.mont(u + v, c.lp.n_inv), xp1 = PP.mont(u + PP.m - v, c.lp.last);
       if constexpr (LAZY) {
-        const u32 z = PQ.montl(y1, fq[1]);
-        buf[b] = y0 + z;  // below 3q
+        const u32 y0 = p_to_q_lazy(c, xp0);  // below 3q
+        const u32 z = PQ.montl(p_to_q_lazy(c, xp1), fq[1]);
+        buf[b] = y0 + z;  // below 5q
         buf[b + H] = y0 + Q2 - z;
       } else {
+        const u32 y0 = p_to_q(c, xp0), y1 = p_to_q(c, xp1);
         const u32 z = PQ.mont(y1, fq[1]);
         buf[b] = PQ.add(y0, z);
         buf[b + H] = PQ.sub(y0, z);

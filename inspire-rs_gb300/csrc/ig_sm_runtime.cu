@@ -313,6 +313,7 @@ int ig_sm_server_create(ig_ctx* c, uint32_t ring_dim, uint32_t gamma, uint64_t q
   dv.inv_gamma_RR = (u32)((u128)powm(gamma, q - 2, q) * (u64)(((u128)1 << 64) % q) % q);
   dv.p_over_q = (u32)(special_prime / q);
   dv.neg_off = (u32)((q - special_prime % q) % q);
+  dv.q_mu = (u32)((1ULL << 32) / q);
   dv.p_inv_R = (u32)(((u128)powm(special_prime % q, q - 2, q) << 32) % q);
   SmState& st = state(c);
   const u64 h = st.next++;
