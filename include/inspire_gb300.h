@@ -297,6 +297,38 @@ int ig_response_encode_device(ig_ctx* ctx, uint32_t count, const uint64_t* d_a, 
                               uint32_t ring_dim, uint32_t retained, uint64_t modulus, uint8_t* d_out,
                               size_t* len_out, uint32_t* d_status);
 
+/* ---- RIMS codec ----------------------------------------------------------------------------
+ * encode_response_packed / decode_response_packed (mod_switch.rs:254-521): the byte-aligned,
+ * self-describing frame "RIMS", version 2, target modulus (u64 LE), ring_dim (u32 LE),
+ * bytes per coefficient (ceil(bits(modulus - 1) / 8), at least 1), packing mode (0 none,
+ * 1 InspiRING, 2 tree), shape (u32 LE: the column count unpacked, the retained b count
+ * packed), then a, the retained b and each column ciphertext's a and b, every coefficient
+ * in that many little-endian bytes.
+ * packing_mode 0 takes retained == 0 (b is written whole) and `columns` ciphertexts of (a, b)
+ * in cts (columns x 2 x ring_dim words); modes 1 and 2 take retained in 1..ring_dim and no
+ * columns. A coefficient not below the modulus is refused (IG_ERR_SHAPE). */
+int ig_response_encode_rims(const uint64_t* a, const uint64_t* b, uint32_t ring_dim, uint32_t retained,
+                            uint32_t packing_mode, const uint64_t* cts, uint32_t columns, uint64_t modulus,
+                            uint8_t* out, size_t cap, size_t* len_out);
+/* Decodes a RIMS frame. With a, b and cts null it validates the whole frame and returns its
+ * header (*modulus_out, *ring_dim_out, *packing_mode_out, *retained_out: 0 when unpacked,
+ * *columns_out); with buffers (a: ring_dim words, b: ring_dim words, zero past the retained
+ * prefix, cts: columns x 2 x ring_dim words) it also writes the coefficients. Refusals carry
+ * the reference's message in err (when err_cap > 0): bad magic or truncated header,
+ * unsupported version, zero modulus or ring_dim, a width that does not match the modulus,
+ * an unknown packing mode, a retained count outside 1..ring_dim, a payload length
+ * mismatch, a coefficient not below the modulus. */
+int ig_response_decode_rims(const uint8_t* bytes, size_t len, uint64_t* modulus_out, uint32_t* ring_dim_out,
+                            uint32_t* packing_mode_out, uint32_t* retained_out, uint32_t* columns_out, uint64_t* a,
+                            uint64_t* b, uint64_t* cts, char* err, size_t err_cap);
+/* The RIMS frames of `count` device-resident packed InspiRING responses (mode 1), built on
+ * the context stream like ig_response_encode_device: d_out receives count x *len_out bytes,
+ * d_status[r] gets bit 1 when a coefficient is not below the modulus; with d_out null only
+ * *len_out is set. */
+int ig_response_encode_rims_device(ig_ctx* ctx, uint32_t count, const uint64_t* d_a, const uint64_t* d_b,
+                                   uint32_t ring_dim, uint32_t retained, uint64_t modulus, uint8_t* d_out,
+                                   size_t* len_out, uint32_t* d_status);
+
 /* ---- observability ------------------------------------------------------------------------
  * With RAVEN_PROFILE_RESPOND set in the environment (read once per process, as
  * respond.rs:1332-1345), every ig_respond_seeded_batch / ig_respond_batch call prints

@@ -105,6 +105,12 @@ def _load():
         "ig_response_encode_full": (I, [P, U32, U32, U64, P, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
         "ig_respond_nopacking_batch": (I, [P, U64, U32, P, P, P, P, P]),
         "ig_response_encode_device": (I, [P, U32, P, P, U32, U32, U64, P, ctypes.POINTER(ctypes.c_size_t), P]),
+        "ig_response_encode_rims": (I, [P, P, U32, U32, U32, P, U32, U64, P, ctypes.c_size_t,
+                                        ctypes.POINTER(ctypes.c_size_t)]),
+        "ig_response_decode_rims": (I, [P, ctypes.c_size_t, ctypes.POINTER(U64), ctypes.POINTER(U32),
+                                        ctypes.POINTER(U32), ctypes.POINTER(U32), ctypes.POINTER(U32), P, P, P,
+                                        ctypes.c_char_p, ctypes.c_size_t]),
+        "ig_response_encode_rims_device": (I, [P, U32, P, P, U32, U32, U64, P, ctypes.POINTER(ctypes.c_size_t), P]),
         "ig_debug_force_serial_expand": (I, [P, I]),
         "ig_profile_enable": (I, [P, I]),
         "ig_profile_read": (I, [P, P, P, I, I]),
@@ -206,6 +212,16 @@ class Context:
         self.check(self._lib.ig_response_encode_device(self.h, count, ctypes.c_void_p(d_a), ctypes.c_void_p(d_b),
                                                        ring_dim, retained, modulus, ctypes.c_void_p(d_out),
                                                        ctypes.byref(n), ctypes.c_void_p(d_status)))
+        return n.value
+
+    def response_rims_device(self, count, d_a, d_b, ring_dim, retained, modulus, d_out, d_status):
+        """RIMS frames (mod_switch.rs:254-345) of `count` device-resident InspiRING responses
+        into d_out on the context stream (ig_response_encode_rims_device); with d_out 0 it
+        only sizes one frame. Returns the bytes per frame."""
+        n = ctypes.c_size_t()
+        self.check(self._lib.ig_response_encode_rims_device(
+            self.h, count, ctypes.c_void_p(d_a), ctypes.c_void_p(d_b), ring_dim, retained, modulus,
+            ctypes.c_void_p(d_out) if d_out else None, ctypes.byref(n), ctypes.c_void_p(d_status)))
         return n.value
 
     def set_lanes(self, lanes):
@@ -537,6 +553,53 @@ class ServerResponse:
         L.ig_response_encode(_ptr(a), _ptr(b), len(a), self.packed_coefficients, self.modulus, _ptr(out), n.value,
                              ctypes.byref(n))
         return out.tobytes()
+
+    _RIMS_MODES = {None: 0, "Inspiring": 1, "Tree": 2}
+
+    def to_rims(self) -> bytes:
+        """encode_response_packed (mod_switch.rs:254-345): the self-describing RIMS frame,
+        every coefficient in ceil(bits / 8) little-endian bytes."""
+        L = _load()
+        a = np.ascontiguousarray(self.a, dtype=np.uint64)
+        b = np.ascontiguousarray(self.b, dtype=np.uint64)
+        mode = self._RIMS_MODES[self.packing_mode]
+        retained = 0 if mode == 0 else self.packed_coefficients
+        cts = None
+        if self.column_ciphertexts:
+            cts = np.ascontiguousarray(np.stack([np.stack([ca, cb]) for ca, cb in self.column_ciphertexts]),
+                                       dtype=np.uint64)
+        ncols = 0 if cts is None else len(cts)
+        n = ctypes.c_size_t()
+        args = (_ptr(a), _ptr(b), len(a), retained, mode, None if cts is None else _ptr(cts), ncols, self.modulus)
+        rc = L.ig_response_encode_rims(*args, None, 0, ctypes.byref(n))
+        if rc:
+            raise PirError(f"encode_response_packed refused (status {rc}): shape or non-canonical coefficient")
+        out = np.zeros(n.value, dtype=np.uint8)
+        L.ig_response_encode_rims(*args, _ptr(out), n.value, ctypes.byref(n))
+        return out.tobytes()
+
+    @staticmethod
+    def from_rims(data: bytes) -> "ServerResponse":
+        """decode_response_packed (mod_switch.rs:367-521)."""
+        L = _load()
+        buf = np.frombuffer(bytes(data), dtype=np.uint8).copy()
+        modulus, ring, mode, retained, ncols = (ctypes.c_uint64(), ctypes.c_uint32(), ctypes.c_uint32(),
+                                                ctypes.c_uint32(), ctypes.c_uint32())
+        err = ctypes.create_string_buffer(512)
+        hdr = [ctypes.byref(x) for x in (modulus, ring, mode, retained, ncols)]
+        if L.ig_response_decode_rims(_ptr(buf) if len(buf) else None, len(buf), *hdr, None, None, None, err,
+                                     len(err)):
+            raise PirError(err.value.decode())
+        n = ring.value
+        a = np.zeros(n, dtype=np.uint64)
+        b = np.zeros(n, dtype=np.uint64)
+        cts = np.zeros((max(ncols.value, 1), 2, n), dtype=np.uint64)
+        L.ig_response_decode_rims(_ptr(buf), len(buf), *hdr, _ptr(a), _ptr(b), _ptr(cts), err, len(err))
+        packing_mode = {0: None, 1: "Inspiring", 2: "Tree"}[mode.value]
+        r = ServerResponse(a, b, None if packing_mode is None else retained.value, modulus.value,
+                           [(cts[j, 0], cts[j, 1]) for j in range(ncols.value)])
+        r.packing_mode = packing_mode
+        return r
 
 
 def check_mod_switch_noise_budget(params: InspireParams, target_modulus: int):

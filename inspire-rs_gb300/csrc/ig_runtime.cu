@@ -1454,6 +1454,33 @@ static bool put_tight(std::vector<uint8_t>& w, const u64* c, size_t count, u64 m
   return true;
 }
 
+// RIMS frame (mod_switch.rs:254-345): header of 23 bytes, then coefficients at a whole
+// number of bytes each.
+static const size_t RIMS_HEADER = 23;
+static unsigned rims_width(u64 modulus) {
+  const unsigned bits = modulus <= 1 ? 1 : 64 - __builtin_clzll(modulus - 1);
+  return (bits + 7) / 8;
+}
+// Writes "decode_response_packed: <message>" into err (when given) and refuses.
+__attribute__((format(printf, 3, 4))) static int rims_refuse(char* err, size_t cap, const char* fmt, ...) {
+  if (err && cap) {
+    char msg[256];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(msg, sizeof msg, fmt, ap);
+    va_end(ap);
+    snprintf(err, cap, "decode_response_packed: %s", msg);
+  }
+  return IG_ERR_SHAPE;
+}
+static bool put_rims_poly(std::vector<uint8_t>& w, const u64* c, size_t count, u64 modulus, unsigned width) {
+  for (size_t i = 0; i < count; i++) {
+    if (c[i] >= modulus) return false;
+    for (unsigned k = 0; k < width; k++) w.push_back((uint8_t)(c[i] >> (8 * k)));
+  }
+  return true;
+}
+
 int ig_response_encode_device(ig_ctx* c, uint32_t count, const uint64_t* d_a, const uint64_t* d_b, uint32_t n,
                               uint32_t retained, uint64_t modulus, uint8_t* d_out, size_t* len_out,
                               uint32_t* d_status) {
@@ -1530,6 +1557,136 @@ int ig_response_encode(const uint64_t* a, const uint64_t* b, uint32_t n, uint32_
   put_u32(w, 0);   //   PackingMode::Inspiring)
   *len_out = w.size();
   if (out) memcpy(out, w.data(), w.size() < cap ? w.size() : cap);
+  return IG_OK;
+}
+
+int ig_response_encode_rims(const uint64_t* a, const uint64_t* b, uint32_t n, uint32_t retained,
+                            uint32_t packing_mode, const uint64_t* cts, uint32_t columns, uint64_t modulus,
+                            uint8_t* out, size_t cap, size_t* len_out) {
+  if (!a || !b || !len_out || n == 0 || modulus == 0 || packing_mode > 2) return IG_ERR_ARG;
+  // (None, None): b whole and the column ciphertexts; (Some, Some(retained)): a b prefix
+  // and no columns (mod_switch.rs:288-309).
+  if (packing_mode == 0 ? (retained != 0 || (columns && !cts)) : (retained == 0 || retained > n || columns != 0))
+    return IG_ERR_ARG;
+  const unsigned width = rims_width(modulus);
+  const u32 kept = packing_mode == 0 ? n : retained;
+  std::vector<uint8_t> w;
+  w.reserve(RIMS_HEADER + ((size_t)n + kept + 2 * (size_t)columns * n) * width);
+  w.insert(w.end(), {'R', 'I', 'M', 'S', 2});
+  put_u64(w, modulus);
+  put_u32(w, n);
+  w.push_back((uint8_t)width);
+  w.push_back((uint8_t)packing_mode);
+  put_u32(w, packing_mode == 0 ? columns : retained);
+  if (!put_rims_poly(w, a, n, modulus, width) || !put_rims_poly(w, b, kept, modulus, width)) return IG_ERR_SHAPE;
+  for (u32 j = 0; j < columns; j++)
+    if (!put_rims_poly(w, cts + (size_t)2 * j * n, 2 * (size_t)n, modulus, width)) return IG_ERR_SHAPE;
+  *len_out = w.size();
+  if (out) memcpy(out, w.data(), w.size() < cap ? w.size() : cap);
+  return IG_OK;
+}
+
+int ig_response_decode_rims(const uint8_t* bytes, size_t len, uint64_t* modulus_out, uint32_t* ring_dim_out,
+                            uint32_t* packing_mode_out, uint32_t* retained_out, uint32_t* columns_out, uint64_t* a,
+                            uint64_t* b, uint64_t* cts, char* err, size_t err_cap) {
+  if (!bytes && len) return IG_ERR_ARG;
+  auto le = [&](size_t off, int nb) {
+    u64 v = 0;
+    for (int k = 0; k < nb; k++) v |= (u64)bytes[off + k] << (8 * k);
+    return v;
+  };
+  // Each check in the order of mod_switch.rs:368-509.
+  if (len < RIMS_HEADER || memcmp(bytes, "RIMS", 4) != 0) return rims_refuse(err, err_cap, "bad magic / truncated header");
+  if (bytes[4] != 2) return rims_refuse(err, err_cap, "unsupported version %u", (unsigned)bytes[4]);
+  const u64 modulus = le(5, 8);
+  if (modulus == 0) return rims_refuse(err, err_cap, "target_modulus must be positive");
+  const u64 n = le(13, 4);
+  if (n == 0) return rims_refuse(err, err_cap, "ring_dim must be positive");
+  const unsigned width = bytes[17], expect = rims_width(modulus);
+  if (width != expect || width > 8)
+    return rims_refuse(err, err_cap, "bytes_per_coeff %u does not match modulus width %u", width, expect);
+  const unsigned mode = bytes[18];
+  if (mode > 2) return rims_refuse(err, err_cap, "unknown packing_mode byte %u", mode);
+  const u64 shape = le(19, 4);
+  u64 columns = 0, kept = n, retained = 0;
+  if (mode == 0) {
+    columns = shape;
+  } else {
+    if (shape == 0 || shape > n)
+      return rims_refuse(err, err_cap, "retained count %llu outside 1..=%llu", (unsigned long long)shape, (unsigned long long)n);
+    kept = retained = shape;
+  }
+  const u128 coeffs = (u128)n + kept + (u128)2 * columns * n;
+  const u128 expected = RIMS_HEADER + coeffs * width;
+  if (expected != (u128)len)
+    return rims_refuse(err, err_cap, "payload length mismatch (expected %llu, got %llu)", (unsigned long long)expected,
+                  (unsigned long long)len);
+  size_t cur = RIMS_HEADER;
+  auto read = [&](u64* dst, u64 count, u64 dim) -> bool {
+    for (u64 i = 0; i < count; i++, cur += width) {
+      const u64 v = le(cur, (int)width);
+      if (v >= modulus) return false;
+      if (dst) dst[i] = v;
+    }
+    if (dst)
+      for (u64 i = count; i < dim; i++) dst[i] = 0;
+    return true;
+  };
+  u64 bad = 0;
+  auto check = [&](u64* dst, u64 count, u64 dim) {
+    const size_t at = cur;
+    if (read(dst, count, dim)) return true;
+    // Find the offending word for the message.
+    for (size_t p = at; p < at + count * width; p += width)
+      if ((bad = le(p, (int)width)) >= modulus) break;
+    return false;
+  };
+  const bool fill = a && b && (columns == 0 || cts);
+  if (!check(fill ? a : nullptr, n, n) || !check(fill ? b : nullptr, kept, n))
+    return rims_refuse(err, err_cap, "coefficient %llu is not canonical for modulus %llu", (unsigned long long)bad,
+                  (unsigned long long)modulus);
+  for (u64 j = 0; j < columns; j++)
+    if (!check(fill ? cts + 2 * j * n : nullptr, n, n) || !check(fill ? cts + (2 * j + 1) * n : nullptr, n, n))
+      return rims_refuse(err, err_cap, "coefficient %llu is not canonical for modulus %llu", (unsigned long long)bad,
+                    (unsigned long long)modulus);
+  if (n > 0xffffffffull || columns > 0xffffffffull) return rims_refuse(err, err_cap, "ring_dim or column count exceeds u32");
+  if (modulus_out) *modulus_out = modulus;
+  if (ring_dim_out) *ring_dim_out = (u32)n;
+  if (packing_mode_out) *packing_mode_out = mode;
+  if (retained_out) *retained_out = (u32)retained;
+  if (columns_out) *columns_out = (u32)columns;
+  return IG_OK;
+}
+
+int ig_response_encode_rims_device(ig_ctx* c, uint32_t count, const uint64_t* d_a, const uint64_t* d_b, uint32_t n,
+                                   uint32_t retained, uint64_t modulus, uint8_t* d_out, size_t* len_out,
+                                   uint32_t* d_status) {
+  if (!c) return IG_ERR_ARG;
+  if (!len_out || n == 0 || modulus < 2 || retained == 0 || retained > n)
+    return fail(c, IG_ERR_ARG, "ig_response_encode_rims_device: ring_dim, retained or modulus out of range");
+  // The template: the frame of a zero response; the coefficients fill whole bytes, so the
+  // bit-packing wire kernel at 8 x width bits writes them.
+  std::vector<u64> za(n, 0), zb(retained, 0);
+  size_t len = 0;
+  int rc = ig_response_encode_rims(za.data(), zb.data(), n, retained, 1, nullptr, 0, modulus, nullptr, 0, &len);
+  if (rc) return fail(c, rc, "ig_response_encode_rims_device: template refused");
+  *len_out = len;
+  if (!d_out) return IG_OK;  // size query
+  if (count == 0 || !d_a || !d_b || !d_status)
+    return fail(c, IG_ERR_ARG, "ig_response_encode_rims_device: empty batch or null buffer");
+  std::vector<uint8_t> tmpl(len);
+  ig_response_encode_rims(za.data(), zb.data(), n, retained, 1, nullptr, 0, modulus, tmpl.data(), len, &len);
+  const u32 width = rims_width(modulus);
+  const u32 a_off = (u32)RIMS_HEADER, a_bytes = n * width, b_off = a_off + a_bytes, b_bytes = retained * width;
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  void* d_t;
+  if ((rc = scratch(c, "rims_template", len, &d_t))) return rc;
+  if ((rc = stage_h2d(c, d_t, tmpl.data(), len))) return rc;
+  IG_CUDA(c, cudaMemsetAsync(d_status, 0, (size_t)count * 4, c->stream));
+  IG_CUDA(c, igk::wire(d_a, d_b, count, n, retained, 8 * width, modulus, (const uint8_t*)d_t, (u32)len, a_off,
+                       a_bytes, b_off, b_bytes, d_out, d_status, c->stream));
+  c->launches++;
   return IG_OK;
 }
 

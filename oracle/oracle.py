@@ -250,6 +250,32 @@ def response_bytes_full(cts, modulus=DEFAULT_Q) -> bytes:
     return out.tobytes()
 
 
+def rims_bytes(a, b, modulus, retained=None, columns=(), mode=None) -> bytes:
+    """encode_response_packed (mod_switch.rs:254-345) restated: magic "RIMS", version 2,
+    target modulus u64 LE, ring_dim u32 LE, bytes per coefficient ceil(bits(modulus-1)/8)
+    (at least one), packing mode byte (0 none, 1 InspiRING, 2 tree), shape u32 LE (columns
+    unpacked, retained packed), then a, the retained b and each column's a and b, each
+    coefficient in that many little-endian bytes. mode defaults to 1 when retained is given."""
+    n = len(a)
+    if mode is None:
+        mode = 0 if retained is None else 1
+    width = (max(1, int(modulus - 1).bit_length()) + 7) // 8
+    out = bytearray(b"RIMS") + bytes([2]) + int(modulus).to_bytes(8, "little") + n.to_bytes(4, "little")
+    out += bytes([width, mode]) + (len(columns) if mode == 0 else retained).to_bytes(4, "little")
+
+    def poly(c, count):
+        for x in list(c)[:count]:
+            assert int(x) < modulus
+            out.extend(int(x).to_bytes(8, "little")[:width])
+
+    poly(a, n)
+    poly(b, n if mode == 0 else retained)
+    for ca, cb in columns:
+        poly(ca, n)
+        poly(cb, n)
+    return bytes(out)
+
+
 class Cell:
     """A KAT cell: database, setup, client session and the reproducible query stream of the
     reference's tests/packing_key_fixture/mod.rs:90-146."""

@@ -1,7 +1,7 @@
 """Device-resident serving pieces: batches over several lanes (ig_ctx_set_lanes), whose
 responses must equal the host-buffer respond_seeded_batch answers for one lane and for
-three, and the device-side response wire (ig_response_encode_device), whose bytes must
-equal the host encoder's."""
+three, and the device-side response wire (ig_response_encode_device) and RIMS frames
+(ig_response_encode_rims_device), whose bytes must equal the host encoders'."""
 import numpy as np
 import pytest
 
@@ -96,6 +96,18 @@ def test_device_wire_matches_host_bytes(pkg, oracle):
         assert int(st.abs().sum().item()) == 0
         for r in range(count):
             assert got[r * length:(r + 1) * length] == want[r], (ms, r)
+        # The RIMS frames (mod_switch.rs:254-345) of the same responses, built on the device.
+        rlen = ctx.response_rims_device(count, 0, 0, n, cell.gamma, modulus, 0, 0)
+        d_rims = torch.zeros(count * rlen, dtype=torch.uint8, device="cuda")
+        st.fill_(1)
+        torch.cuda.synchronize()
+        assert ctx.response_rims_device(count, a.data_ptr(), b.data_ptr(), n, cell.gamma, modulus, d_rims.data_ptr(),
+                                        st.data_ptr()) == rlen
+        torch.cuda.ExternalStream(ctx.stream).synchronize()
+        got = d_rims.cpu().numpy().tobytes()
+        assert int(st.abs().sum().item()) == 0
+        for r in range(count):
+            assert got[r * rlen:(r + 1) * rlen] == out[r].to_rims(), (ms, r)
 
 
 def test_concurrent_host_calls_over_lanes(pkg, oracle):
