@@ -7,7 +7,11 @@ uniform indices per step answered through respond_seeded_batch, responses mod-sw
 36 bits. Inputs are seeded synthetic data of those shapes: uniform 16-bit column words
 (the encoding of uniform random record bytes), uniform key and query words mod q.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--config 2|3|4|5]
+
+--config 3 times the special_modulus batch of 256, --config 4 six mixed parameter sets
+(32/512/2048 B records under both gadgets, batch sizes 1-512), --config 5 the serving loop
+over 2^25 records and 1000 seats.
 
 Prints one JSON line. `value` = queries/s over K device-resident batches (CUDA events on
 the library's stream); `e2e` = the same through the public API with host buffers;
@@ -613,6 +617,196 @@ def run_sm(args, rank, world):
 # records) encoded on the GPU, a store on every shard, 1000 registered seats, requests with
 # uniform index and seat through the continuous-batching loop, driven natively: a closed
 # loop to saturation, then Poisson arrivals at fractions of the saturation rate.
+# ------------------------------------------------------------------------------------
+# Mixed databases: 32 B x 2^22 (gamma 16, 2048 shards), 512 B x 2^20 (gamma 256, 512
+# shards), 2048 B x 2^18 (gamma 1024, 128 shards), each under the exact and the approximate
+# gadget (six parameter sets), 128 keys spread over the sets, batch sizes drawn from
+# {1, 7, 33, 128, 512}; responses unswitched.
+C4_DBS = [(32, 2048, 3), (512, 512, 4), (2048, 128, 5)]  # entry bytes, shards, seed
+C4_KEYS = 128
+C4_BATCHES = (1, 7, 33, 128, 512)
+C4_METRIC = ("mixed-database respond queries/s (32/512/2048 B records x exact/approximate gadget, 128 keys, "
+             "batch sizes 1-512)")
+
+
+def run_cfg4(args, rank, world):
+    import threading
+
+    import torch
+
+    from __graft_entry__ import _package
+    pkg = _package()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    ctx = pkg.Context(local)
+    rng = np.random.default_rng(4 + rank)
+    store = pkg.ServerSessionStore.new(ctx)
+    sets = []
+    t0 = time.perf_counter()
+    for entry, shards, seed in C4_DBS:
+        if args.shards != NUM_SHARDS:
+            shards = max(1, min(shards, args.shards))
+        gamma = (entry + 1) // 2
+        g = torch.Generator(device="cuda")
+        g.manual_seed(seed + rank)
+        rec = torch.randint(0, 256, (shards * N_RING * entry,), dtype=torch.uint8, device="cuda", generator=g)
+        torch.cuda.current_stream().synchronize()
+        for approx in (False, True):
+            params = pkg.InspireParams.d2048_approximate_gadget() if approx else pkg.InspireParams.d2048()
+            crs = pkg.ServerCrs(params, rng.integers(0, 256, 32, dtype=np.uint8).tobytes(), gamma)
+            cache = pkg.ServerInspiringCache.new(crs, ctx=ctx)
+            db = pkg.EncodedDatabase(cache, shards)
+            db.encode_records(None, entry, device_ptr=rec.data_ptr(), nbytes=rec.numel())
+            db.precompute_packing_all()
+            sets.append({"entry": entry, "gamma": gamma, "shards": shards, "approx": approx, "crs": crs,
+                         "cache": cache, "db": db, "rows": params.packing_key_rows(), "keys": []})
+        del rec
+        torch.cuda.empty_cache()
+    for k in range(C4_KEYS):
+        st = sets[k % len(sets)]
+        keys = pkg.ClientPackingKeys(rand_words(rng, (st["rows"], N_RING)), st["gamma"])
+        st["keys"].append((keys, store.register_server_side(keys, st["cache"])))
+    setup_s = time.perf_counter() - t0
+
+    total = args.warmup + args.steps
+    plan = []
+    for i in range(total):
+        si = int(rng.integers(0, len(sets)))
+        st = sets[si]
+        count = int(rng.choice(C4_BATCHES))
+        kh = st["keys"][int(rng.integers(0, len(st["keys"])))]
+        sids = np.ascontiguousarray(rng.integers(0, st["shards"], count), dtype=np.uint32)
+        seeds = rng.integers(0, 256, (count, 32), dtype=np.uint8)
+        bs = rand_words(rng, (count, N_RING))
+        plan.append((si, count, kh, sids, seeds, bs))
+    offs = np.cumsum([0] + [p[1] for p in plan])
+    d_seeds = torch.from_numpy(np.concatenate([p[4] for p in plan])).cuda()
+    d_bs = torch.from_numpy(np.concatenate([p[5] for p in plan]).view(np.int64)).cuda()
+    d_a = torch.empty((int(offs[-1]), N_RING), dtype=torch.int64, device="cuda")
+    d_b = torch.empty_like(d_a)
+    d_status = torch.zeros(int(offs[-1]), dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    lib = ctx._lib
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    lanes = args.lanes
+
+    def step(i):
+        si, count, (_, handle), sids, _, _ = plan[i]
+        o = int(offs[i])
+        ctx.check(lib.ig_respond_seeded_batch_device(
+            ctx.h, sets[si]["db"].h, store.h, int(handle), count, sids.ctypes.data, d_seeds[o].data_ptr(),
+            d_bs[o].data_ptr(), 0, d_a[o].data_ptr(), d_b[o].data_ptr(), d_status[o:].data_ptr()))
+
+    ctx.set_lanes(lanes)
+    for i in range(args.warmup):
+        step(i)
+    ctx.join()
+    stream.synchronize()
+    torch.cuda.synchronize()
+    ctx.set_lanes(lanes)
+    launches0 = ctx.launch_count
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier(world)
+    with ClockSampler(local) as clk:
+        with torch.cuda.stream(stream):
+            ev0.record(stream)
+            for i in range(args.warmup, total):
+                step(i)
+            ctx.join()
+            ev1.record(stream)
+        stream.synchronize()
+        torch.cuda.synchronize()
+    launches = ctx.launch_count - launches0
+    if int(d_status.abs().sum().item()) != 0:
+        raise RuntimeError("a batch was refused during the timed region")
+    timed_queries = int(offs[-1] - offs[args.warmup])
+    ms = max_over_ranks(ev0.elapsed_time(ev1), world)
+    value = world * timed_queries / (ms / 1e3)
+
+    # e2e: respond_seeded_batch with host buffers from `lanes` caller threads.
+    calls = []
+    for si, count, (keys, handle), sids, seeds, bs in plan:
+        st = sets[si]
+        qs = [pkg.SeededBatchQuery(int(sids[k]), seeds[k].tobytes(), bs[k]) for k in range(count)]
+        calls.append((st, pkg.SeededQueryBatch(pkg.PackingKeySource.Registered(handle), qs)))
+    errors = []
+
+    def caller(idx):
+        try:
+            for i in idx:
+                st, batch = calls[i]
+                pkg.respond_seeded_batch(st["crs"], st["db"], batch, st["cache"], store)
+        except Exception as e:  # reported below
+            errors.append(e)
+
+    def run_callers(indices):
+        threads = [threading.Thread(target=caller, args=(indices[t::lanes],)) for t in range(lanes)]
+        for th in threads:
+            th.start()
+        for th in threads:
+            th.join()
+
+    ctx.set_lanes(lanes)
+    run_callers(list(range(args.warmup)))
+    t0 = time.perf_counter()
+    run_callers(list(range(args.warmup, total)))
+    e2e = world * timed_queries / max_over_ranks(time.perf_counter() - t0, world)
+    ctx.set_lanes(1)
+    if errors:
+        raise errors[0]
+
+    # Per parameter set: batches of 128 on one set at a time, three lanes.
+    per_set = []
+    ps_seeds = torch.from_numpy(rng.integers(0, 256, (128, 32), dtype=np.uint8)).cuda()
+    ps_bs = torch.from_numpy(rand_words(rng, (128, N_RING)).view(np.int64)).cuda()
+    ps_a = torch.empty((128, N_RING), dtype=torch.int64, device="cuda")
+    ps_b = torch.empty_like(ps_a)
+    ps_status = torch.zeros(128, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    for si, st in enumerate(sets):
+        handle = st["keys"][0][1]
+        sids = np.ascontiguousarray(rng.integers(0, st["shards"], 128), dtype=np.uint32)
+        ctx.set_lanes(lanes)
+        reps = 6
+        for r in range(reps + 1):
+            if r == 1:
+                ctx.join()
+                stream.synchronize()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+            ctx.check(lib.ig_respond_seeded_batch_device(
+                ctx.h, st["db"].h, store.h, int(handle), 128, sids.ctypes.data, ps_seeds.data_ptr(),
+                ps_bs.data_ptr(), 0, ps_a.data_ptr(), ps_b.data_ptr(), ps_status.data_ptr()))
+        ctx.join()
+        e1.record(stream)
+        stream.synchronize()
+        ctx.set_lanes(1)
+        if int(ps_status.abs().sum().item()) != 0:
+            raise RuntimeError("a per-set batch was refused")
+        per_set.append({"entry": st["entry"], "gamma": st["gamma"], "gadget": "approximate" if st["approx"] else "exact",
+                        "queries_per_s": reps * 128 / (e0.elapsed_time(e1) / 1e3)})
+    mix = {str(b): sum(1 for p in plan[args.warmup:] if p[1] == b) for b in C4_BATCHES}
+    return {
+        "metric": C4_METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u64 (exact mod q = 2^60-2^14+1)",
+        "data": "synthetic: uniform record bytes encoded on the GPU, uniform key and query words",
+        "config": {"workload": "six parameter sets (32 B x 2^22 gamma 16, 512 B x 2^20 gamma 256, 2048 B x 2^18 "
+                               "gamma 1024; exact and approximate gadget), 128 keys, one batch per step of a "
+                               "size drawn from {1, 7, 33, 128, 512} on a random set and key, uniform shards",
+                   "shards": [st["shards"] for st in sets[::2]], "keys": C4_KEYS, "lanes": lanes,
+                   "queries": timed_queries, "batch_mix": mix, "mod_switch": None,
+                   "l2": "inputs larger than L2: the six sets hold about 22 GiB of columns and stores"},
+        "e2e": {"value": e2e, "unit": "queries/s", "h2d_bytes_per_step": int(timed_queries * (32 + N_RING * 8 + 4)
+                                                                            / args.steps),
+                "d2h_bytes_per_step": int(timed_queries * 2 * N_RING * 8 / args.steps), "callers": lanes,
+                "call": "respond_seeded_batch (one batch per call)"},
+        "per_set": per_set, "gpu_launches": int(launches), "setup_s": setup_s, "clocks": clk.summary(),
+        "device_bytes": ctx.device_bytes,
+    }
+
+
 C5_SHARDS = 16384
 C5_SEATS = 1000
 C5_METRIC = ("served queries/s at saturation (continuous batching, 2^25 x 512 B records, 16,384 shards, "
@@ -710,16 +904,16 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--lanes", type=int, default=3,
                     help="streams consecutive batches rotate over in the device-resident timed region")
-    ap.add_argument("--config", type=int, default=2, choices=[2, 3, 5],
+    ap.add_argument("--config", type=int, default=2, choices=[2, 3, 4, 5],
                     help="2: served InspiRING batch (the headline); 3: special_modulus batch; "
-                         "5: serving sweep over 16,384 shards and 1000 seats")
+                         "4: mixed databases and batch sizes; 5: serving sweep over 16,384 shards and 1000 seats")
     ap.add_argument("--requests", type=int, default=16384, help="trace length of the serving sweep (config 5)")
     ap.add_argument("--shards", type=int, default=NUM_SHARDS,
                     help="shards in the database (smaller values only for profiling captures)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.steps is None:
-        args.steps = 20 if args.impl == "reference" else {2: 300, 3: 100, 5: 0}[args.config]
+        args.steps = 20 if args.impl == "reference" else {2: 300, 3: 100, 4: 60, 5: 0}[args.config]
     rank, world = dist_setup(args.gpus)
     if args.impl == "reference":
         if rank != 0:
@@ -731,6 +925,11 @@ def main():
                 "impl": "reference", "cpu_baseline": cb,
                 "e2e": {"value": cb["value"], "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
+        return
+    if args.config == 4:
+        line = run_cfg4(args, rank, world)
+        if rank == 0:
+            print(json.dumps(line))
         return
     if args.config == 5:
         line = run_cfg5(args, rank, world)
