@@ -253,8 +253,10 @@ __global__ void __launch_bounds__(FOLD_THREADS) k_store_fold(CrsDev c, const u64
 // while loading the same positions of a column as one 16-byte word.
 //
 // Other shards take the exact 128-bit path over the u64 words.
-constexpr int SCAN_WARPS = 8;
-constexpr int SCAN_ROWS = 8;  // columns per warp: 64 per CTA, two CTAs resident per SM
+// 16 warps of 4 columns: 64 columns per CTA share one staged vector, and two CTAs per SM
+// (64 registers a thread) give 32 warps per SM to cover the column loads' latency.
+constexpr int SCAN_WARPS = 16;
+constexpr int SCAN_ROWS = 4;
 constexpr u64 TAG_PRIME = (1ULL << 61) - 1;
 
 __device__ __forceinline__ u128 shfl_xor_u128(u128 v, int m) {
