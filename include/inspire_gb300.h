@@ -280,6 +280,24 @@ int ig_respond_nopacking_batch(ig_ctx* ctx, uint64_t db, uint32_t count, const u
 int ig_response_encode_full(const uint64_t* cts, uint32_t count, uint32_t ring_dim, uint64_t modulus, uint8_t* out,
                             size_t cap, size_t* len_out);
 
+/* ---- OnePacking respond -------------------------------------------------------------------
+ * respond_one_packing / respond_seeded_packed (respond.rs:696-729, 1241-1249): the column
+ * products' coefficient-0 LWEs packed by the Galois-automorphism tree of
+ * inspiring/automorph_pack.rs into one RLWE holding column k at coefficient k, scaled by d.
+ * The CRS needs its Galois keys first: ig_crs_set_galois_keys takes ServerCrs::galois_keys,
+ * `count` = log2(ring_dim) keys (key i for t = ring_dim / 2^i + 1) of `rows` = 3 rows (a, b),
+ * ring_dim words each in coefficient form (keys[((i * rows + r) * 2 + {0 a, 1 b}) *
+ * ring_dim + k]), refused as require_galois_keys refuses (setup.rs:195-226). A second call
+ * replaces the keys. */
+int ig_crs_set_galois_keys(ig_ctx* ctx, uint64_t crs, uint32_t count, uint32_t rows, const uint64_t* keys);
+/* Query i: shard_ids[i], a from seeds[32 i..] (seeded) or as[ring_dim i..] (pass seeds null),
+ * b from bs[ring_dim i..]. a_out, b_out receive count x ring_dim coefficient-form words over
+ * q, or over mod_switch_target when nonzero; the response's packed_coefficients is gamma
+ * and its packing_mode Tree. No store or seat is needed. All or nothing. */
+int ig_respond_one_packing_batch(ig_ctx* ctx, uint64_t db, uint32_t count, const uint32_t* shard_ids,
+                                 const uint8_t* seeds, const uint64_t* as, const uint64_t* bs,
+                                 uint64_t mod_switch_target, uint64_t* a_out, uint64_t* b_out);
+
 /* ---- wire ------------------------------------------------------------------------------
  * ServerResponse bincode bytes of a packed response (respond.rs:111-176, tight codec
  * poly.rs:166-225): Packed{a, b_prefix (first `retained` b coefficients), retained}, no
@@ -287,6 +305,9 @@ int ig_response_encode_full(const uint64_t* cts, uint32_t count, uint32_t ring_d
  * (the mod-switch target after a switch). Writes at most cap bytes; *len_out = size. */
 int ig_response_encode(const uint64_t* a, const uint64_t* b, uint32_t ring_dim, uint32_t retained, uint64_t modulus,
                        uint8_t* out, size_t cap, size_t* len_out);
+/* The same bytes with packing_mode Some(PackingMode::Tree) (a OnePacking response). */
+int ig_response_encode_tree(const uint64_t* a, const uint64_t* b, uint32_t ring_dim, uint32_t retained,
+                            uint64_t modulus, uint8_t* out, size_t cap, size_t* len_out);
 /* The same bytes for `count` device-resident responses (d_a, d_b: count x ring_dim words)
  * into d_out (count x *len_out bytes, response r at r * *len_out), enqueued on the context
  * stream: the wire is built next to the responses, and only its bytes cross to the host

@@ -33,6 +33,7 @@ __all__ = [
     "respond", "respond_seeded", "respond_nopacking_batch",
     "check_mod_switch_noise_budget", "ClientQuery", "Context", "DEFAULT_Q",
     "MOD_SWITCH_TARGET_36BIT", "MOD_SWITCH_TARGET_45BIT", "library_path", "special_modulus", "ServingLoop",
+    "respond_one_packing", "respond_seeded_packed", "respond_one_packing_batch",
     "ServeTicket",
 ]
 
@@ -105,6 +106,9 @@ def _load():
         "ig_response_encode_full": (I, [P, U32, U32, U64, P, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
         "ig_respond_nopacking_batch": (I, [P, U64, U32, P, P, P, P, P]),
         "ig_response_encode_device": (I, [P, U32, P, P, U32, U32, U64, P, ctypes.POINTER(ctypes.c_size_t), P]),
+        "ig_response_encode_tree": (I, [P, P, U32, U32, U64, P, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
+        "ig_crs_set_galois_keys": (I, [P, U64, U32, U32, P]),
+        "ig_respond_one_packing_batch": (I, [P, U64, U32, P, P, P, P, U64, P, P]),
         "ig_response_encode_rims": (I, [P, P, U32, U32, U32, P, U32, U64, P, ctypes.c_size_t,
                                         ctypes.POINTER(ctypes.c_size_t)]),
         "ig_response_decode_rims": (I, [P, ctypes.c_size_t, ctypes.POINTER(U64), ctypes.POINTER(U32),
@@ -289,11 +293,15 @@ class InspireParams:
 class ServerCrs:
     """The public parameters a responder needs (setup.rs:75-96): params, w_seed, width."""
 
-    def __init__(self, params: InspireParams, inspiring_w_seed: bytes, inspiring_num_columns: int):
+    def __init__(self, params: InspireParams, inspiring_w_seed: bytes, inspiring_num_columns: int,
+                 galois_keys=None):
+        """galois_keys: the tree responder's keys (setup.rs:435-445), log2(ring_dim) x rows x
+        (a, b) x ring_dim coefficient-form words, or None (the published CRS strips them)."""
         if len(inspiring_w_seed) != 32:
             raise PirError("inspiring_w_seed must be 32 bytes")
         self.params, self.inspiring_w_seed = params, bytes(inspiring_w_seed)
         self.inspiring_num_columns = int(inspiring_num_columns)
+        self.galois_keys = None if galois_keys is None else np.ascontiguousarray(galois_keys, dtype=np.uint64)
 
     def ring_dim(self):
         return self.params.ring_dim
@@ -315,6 +323,15 @@ class ServerInspiringCache:
             self.ctx.h, p.ring_dim, p.q, p.p, p.gadget_base, p.packing_gadget_len,
             int(p.approximate_packing_gadget), crs.inspiring_num_columns, _ptr(seed), ctypes.byref(h)))
         self.h = h.value
+        if crs.galois_keys is not None:
+            self.set_galois_keys(crs.galois_keys)
+
+    def set_galois_keys(self, keys):
+        """Uploads ServerCrs::galois_keys (ig_crs_set_galois_keys) for the tree responder."""
+        k = np.ascontiguousarray(keys, dtype=np.uint64)
+        if k.ndim != 4 or k.shape[2] != 2 or k.shape[3] != self.crs.params.ring_dim:
+            raise PirError("galois keys must be (keys, rows, 2, ring_dim) coefficient-form words")
+        self.ctx.check(self.ctx._lib.ig_crs_set_galois_keys(self.ctx.h, self.h, k.shape[0], k.shape[1], _ptr(k)))
 
     @staticmethod
     def new(crs: ServerCrs, encoded_db=None, ctx: Context = None):
@@ -545,13 +562,12 @@ class ServerResponse:
         a = np.ascontiguousarray(self.a, dtype=np.uint64)
         b = np.ascontiguousarray(self.b, dtype=np.uint64)
         n = ctypes.c_size_t()
-        rc = L.ig_response_encode(_ptr(a), _ptr(b), len(a), self.packed_coefficients, self.modulus, None, 0,
-                                  ctypes.byref(n))
+        enc = L.ig_response_encode_tree if self.packing_mode == "Tree" else L.ig_response_encode
+        rc = enc(_ptr(a), _ptr(b), len(a), self.packed_coefficients, self.modulus, None, 0, ctypes.byref(n))
         if rc:
             raise PirError(f"ServerResponse encode refused (status {rc}): coefficients must be canonical")
         out = np.zeros(n.value, dtype=np.uint8)
-        L.ig_response_encode(_ptr(a), _ptr(b), len(a), self.packed_coefficients, self.modulus, _ptr(out), n.value,
-                             ctypes.byref(n))
+        enc(_ptr(a), _ptr(b), len(a), self.packed_coefficients, self.modulus, _ptr(out), n.value, ctypes.byref(n))
         return out.tobytes()
 
     _RIMS_MODES = {None: 0, "Inspiring": 1, "Tree": 2}
@@ -855,6 +871,55 @@ def respond_seeded(crs: ServerCrs, encoded_db: EncodedDatabase, query: SeededBat
 def respond_nopacking_batch(crs: ServerCrs, encoded_db: EncodedDatabase, queries) -> list:
     """NoPacking responses of many queries in one launch sequence (seeded or unseeded)."""
     return _nopacking(crs, encoded_db, list(queries))
+
+
+def _one_packing(crs, encoded_db, queries, mod_switch_target=0):
+    ctx = encoded_db.ctx
+    n, g = crs.params.ring_dim, crs.inspiring_num_columns
+    count = len(queries)
+    if count == 0:
+        raise PirError("empty batch")
+    unseeded = queries[0].seed is None
+    if any((q.seed is None) != unseeded for q in queries):
+        raise PirError("a batch is all seeded or all unseeded queries")
+    if mod_switch_target:
+        check_mod_switch_noise_budget(crs.params, mod_switch_target)
+    shard_ids = np.array([q.shard_id for q in queries], dtype=np.uint32)
+    if unseeded:
+        seeds, a_in = None, np.stack([_u64(q.a, (n,)) for q in queries])
+    else:
+        seeds, a_in = np.frombuffer(b"".join(q.seed for q in queries), dtype=np.uint8).copy(), None
+    bs = np.stack([_u64(q.b, (n,)) for q in queries])
+    a = np.zeros((count, n), dtype=np.uint64)
+    b = np.zeros((count, n), dtype=np.uint64)
+    ctx.check(ctx._lib.ig_respond_one_packing_batch(ctx.h, encoded_db.h, count, _ptr(shard_ids), _ptr(seeds),
+                                                    _ptr(a_in), _ptr(bs), int(mod_switch_target), _ptr(a), _ptr(b)))
+    out = []
+    for i in range(count):
+        r = ServerResponse(a[i], b[i], g, mod_switch_target or crs.params.q)
+        r.packing_mode = "Tree"
+        out.append(r)
+    return out
+
+
+def respond_one_packing(crs: ServerCrs, encoded_db: EncodedDatabase, query: ClientQuery,
+                        mod_switch_target: int = 0) -> ServerResponse:
+    """respond_one_packing (respond.rs:696-729): the column LWEs packed by the Galois-
+    automorphism tree into one ciphertext holding column k at coefficient k, scaled by d.
+    Needs the CRS's Galois keys."""
+    return _one_packing(crs, encoded_db, [query], mod_switch_target)[0]
+
+
+def respond_seeded_packed(crs: ServerCrs, encoded_db: EncodedDatabase, query: SeededBatchQuery,
+                          mod_switch_target: int = 0) -> ServerResponse:
+    """respond_seeded_packed (respond.rs:1241-1249): the seed expanded, then
+    respond_one_packing."""
+    return _one_packing(crs, encoded_db, [query], mod_switch_target)[0]
+
+
+def respond_one_packing_batch(crs: ServerCrs, encoded_db: EncodedDatabase, queries, mod_switch_target: int = 0):
+    """OnePacking responses of many queries in one launch (seeded or unseeded)."""
+    return _one_packing(crs, encoded_db, list(queries), mod_switch_target)
 
 
 class _SpecialModulus:

@@ -1254,6 +1254,224 @@ __global__ void k_nopack_sum(u32 n, u32 gamma, u64* out) {
 }
 
 // ------------------------------------------------------------------------------------
+// OnePacking: respond_one_packing (pir/respond.rs:696-729), the Galois-automorphism tree of
+// inspiring/automorph_pack.rs, one CTA per query. Leaf j (j < gamma) is the column product's
+// a part a h_j (b part zero) and b-value_j = coeff0(b h_j); leaves past gamma are the
+// padding's zero ciphertexts. Node (ell, start) = (E + y O) + keyswitch(tau_t(E - y O)) with
+// E, O its children (start, start + n/2^ell), y = X^(n >> ell), t = 2^ell + 1 and Galois key
+// log n - ell (pack_lwes_inner, automorph_pack.rs:96-163). Every node whose start is at or
+// past gamma is exactly zero, so only those below gamma are computed.
+//
+// Nodes live in the NTT domain: y O is a product by NTT(X^s), tau_t a slot permutation,
+// and only the key switch's digit split needs coefficients: a = INTT(tau_t(...).a), digits
+// 0 and 1 (base 2^20) transformed, digit 2's transform derived as base^-2 (a - D0 - base D1)
+// (the unsigned split of rgsw/external_product.rs:58-99 leaves a = D0 + base D1 + base^2 D2
+// exactly). Key rows are R-form NTT, so each sum of three products takes one reduction.
+//
+// The walk is the recursion's depth-first order: leaf k of the walk is start = bitrev(k),
+// and a binary-counter carry combines each finished node with its waiting sibling; the
+// waiting nodes sit in a per-query stack of log n node slots in global memory.
+template <int LOGN>
+__global__ void __launch_bounds__((1 << LOGN) / 4, 1)
+    k_tree(CrsDev c, const QueryDev* queries, const ShardDev* shards, u64 r_mod_q, u64 r_mod_qp, u64 ms_target,
+           u64* stack, u64* a_out, u64* b_out, u32* status) {
+  constexpr int N = 1 << LOGN, NT = N / 4;
+  constexpr u32 M2N = 2 * N - 1;
+  constexpr u64 DMASK = (1ULL << 20) - 1;
+  extern __shared__ __align__(16) u64 sm[];
+  u64* tw = sm;
+  u64* twp = tw + N;
+  u64* aR = twp + N;     // NTT(a) in R-form
+  u64* S1a = aR + N;     // E - y O, permuted by the automorphism
+  u64* S1b = S1a + N;
+  u64* X = S1b + N;      // the inverse in progress, then a leaf column
+  u64* D = X + N;        // digits 0 and 1
+  u64* bval = D + 2 * N; // b-values of the leaves (gamma <= n/2)
+  u64* red = bval + N / 2;  // per-warp partial sums
+  uint16_t* e_tab = reinterpret_cast<uint16_t*>(red + 32);
+  uint16_t* s_tab = e_tab + N;
+  const int tid = threadIdx.x;
+  const u32 qi = blockIdx.x;
+  const QueryDev qd = queries[qi];
+  const ShardDev sh = shards[qd.shard];
+  const u32 gamma = c.gamma;
+  u64* stk = stack + (size_t)qi * LOGN * 2 * N;
+
+  for (int k = tid; k < N; k += NT) {
+    tw[k] = c.tw[k];
+    twp[k] = c.twp[k];
+    e_tab[k] = c.slot_exp[k];
+    s_tab[k] = c.exp_slot[k];
+  }
+  expand_a<N, NT>(qd, aR, status, qi, 0);  // ends with a barrier
+  {
+    u64* const bufs[1] = {aR};
+    ntt_fwd_r4<LOGN, NT, 1>(bufs, tw, twp);
+  }
+  for (int k = tid; k < N; k += NT) aR[k] = shoup(aR[k], r_mod_q, r_mod_qp);
+  __syncthreads();
+
+  u64 ca[4], cb[4];  // the current node, slots tid + j NT
+  bool cur_zero = true;
+  // Leaf `start`: the column through the transform times NTT(a); its b-value on the side.
+  auto leaf = [&](u32 start) {
+    u128 acc = 0;
+    for (int j = 0; j < 4; j++) {
+      const int k = tid + j * NT;
+      const u64 h = sh.cols16 ? (u64)sh.cols16[(size_t)start * N + k] : reduce128(sh.columns[(size_t)start * N + k]);
+      const u64 br = k == 0 ? reduce128(qd.b[0]) : negq(reduce128(qd.b[N - k]));
+      acc += wide(h, br);
+      X[k] = h;
+    }
+    u64 v = reduce128(acc);
+#pragma unroll
+    for (int m = 16; m >= 1; m >>= 1) v = addq(v, __shfl_xor_sync(0xffffffffu, v, m));
+    if ((tid & 31) == 0) red[tid >> 5] = v;
+    __syncthreads();
+    if (tid == 0) {
+      u64 t = 0;
+      for (int w = 0; w < NT / 32; w++) t = addq(t, red[w]);
+      bval[start] = t;
+    }
+    {
+      u64* const bufs[1] = {X};
+      ntt_fwd_r4<LOGN, NT, 1>(bufs, tw, twp);  // ends with a barrier
+    }
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      const int k = tid + j * NT;
+      ca[j] = mont(csub(csub2(X[k])), aR[k]);
+      cb[j] = 0;
+    }
+    __syncthreads();  // X is rewritten next
+  };
+  // The current node becomes (E + y O) + keyswitch(tau_t(E - y O)) at level ell, E from the
+  // stack slot ell - 1; the current node is O (zero when odd_zero).
+  auto combine = [&](int ell, bool odd_zero) {
+    const u64* E = stk + (size_t)(ell - 1) * 2 * N;
+    const u32 sh_y = (u32)(N >> ell), t = (1u << ell) + 1;
+    const u64* key = c.galois_R + (size_t)(LOGN - ell) * 6 * N;
+    u64 s0a[4], s0b[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      const int k = tid + j * NT;
+      const u64 ea = E[k], eb = E[N + k];
+      u64 ya = 0, yb = 0;
+      if (!odd_zero) {
+        const u64 y = c.pow_root_R[(e_tab[k] * sh_y) & M2N];
+        ya = mont(ca[j], y);
+        yb = mont(cb[j], y);
+      }
+      s0a[j] = addq(ea, ya);
+      s0b[j] = addq(eb, yb);
+      S1a[k] = subq(ea, ya);
+      S1b[k] = subq(eb, yb);
+    }
+    __syncthreads();
+    u64 aa[4], ab[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      const int k = tid + j * NT;
+      const u32 src = s_tab[((t * e_tab[k]) & M2N) >> 1];
+      aa[j] = S1a[src];
+      ab[j] = S1b[src];
+      X[k] = aa[j];
+    }
+    __syncthreads();
+    {
+      u64* const bufs[1] = {X};
+      ntt_inv_r4<LOGN, NT, 1>(bufs, tw, twp);
+    }
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      const int k = tid + j * NT;
+      const u64 r = shoup(X[k], c.ninv, c.ninvp);
+      D[k] = r & DMASK;
+      D[N + k] = (r >> 20) & DMASK;
+    }
+    __syncthreads();
+    {
+      u64* const bufs[2] = {D, D + N};
+      ntt_fwd_r4<LOGN, NT, 2>(bufs, tw, twp);
+    }
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      const int k = tid + j * NT;
+      const u64 d0 = D[k], d1 = D[N + k];
+      const u64 d2 = redc(wide(aa[j], c.ld_inv_R) + wide(d0, c.ld_c0_R) + wide(d1, c.ld_c1_R));
+      const u64 na = redc(wide(d0, key[k]) + wide(d1, key[2 * N + k]) + wide(d2, key[4 * N + k]));
+      const u64 nb = redc(wide(d0, key[N + k]) + wide(d1, key[3 * N + k]) + wide(d2, key[5 * N + k]));
+      ca[j] = addq(s0a[j], na);
+      cb[j] = addq(s0b[j], addq(ab[j], nb));
+    }
+    __syncthreads();  // D and X are rewritten next
+  };
+
+  if (gamma == 1) {
+    // pack_lwes with one input returns it untouched: no tree and no d scaling.
+    leaf(0);
+    cur_zero = false;
+  } else {
+    u32 zero_slots = 0;  // bit L: the waiting node at level L is zero
+#pragma unroll 1
+    for (u32 k = 0; k < (u32)N; k++) {
+      const u32 start = __brev(k) >> (32 - LOGN);
+      cur_zero = start >= gamma;
+      if (!cur_zero) leaf(start);
+      int L = 0;
+      while ((k >> L) & 1) {
+        if ((zero_slots >> L) & 1) {
+          cur_zero = true;  // an even child at or past gamma makes its sibling zero too
+        } else {
+          combine(L + 1, cur_zero);
+          cur_zero = false;
+        }
+        L++;
+      }
+      if (L < LOGN) {
+        if (cur_zero) {
+          zero_slots |= 1u << L;
+        } else {
+          zero_slots &= ~(1u << L);
+          u64* slot = stk + (size_t)L * 2 * N;
+#pragma unroll
+          for (int j = 0; j < 4; j++) {
+            slot[tid + j * NT] = ca[j];
+            slot[N + tid + j * NT] = cb[j];
+          }
+        }
+      }
+    }
+  }
+  // The root to coefficients; b_z += n b-value_z for z < gamma (pack_lwes, automorph_pack.rs
+  // 327-338), except for a single input.
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    X[tid + j * NT] = ca[j];
+    D[tid + j * NT] = cb[j];
+  }
+  __syncthreads();
+  {
+    u64* const bufs[2] = {X, D};
+    ntt_inv_r4<LOGN, NT, 2>(bufs, tw, twp);
+  }
+  const u64 scale = gamma == 1 ? 1 : (u64)N;
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    const int k = tid + j * NT;
+    u64 av = shoup(X[k], c.ninv, c.ninvp);
+    u64 bv = gamma == 1 ? (k == 0 ? bval[0] : 0) : shoup(D[k], c.ninv, c.ninvp);
+    if (gamma > 1 && (u32)k < gamma) bv = addq(bv, reduce128(wide(bval[k], scale)));
+    if (ms_target) {
+      av = mod_switch_word(av, ms_target);
+      bv = mod_switch_word(bv, ms_target);
+    }
+    a_out[(size_t)qi * N + k] = av;
+    b_out[(size_t)qi * N + k] = bv;
+  }
+}
+
+// ------------------------------------------------------------------------------------
 // Integer roofline probe: lazy forward butterflies (one Shoup product, two 64-bit adds and
 // a conditional subtraction each, the transforms' unit of work) on values held in
 // registers, eight independent chains per thread, no memory traffic. Its rate is the
@@ -1375,6 +1593,23 @@ cudaError_t nopack(const CrsDev& c, const QueryDev* queries, const ShardDev* sha
       k<<<dim3(c.gamma, nq), N / 4, smem, s>>>(c, queries, shards, AB_R, out);
     }
     k_nopack_sum<<<dim3((2 * N + 255) / 256, nq), 256, 0, s>>>(N, c.gamma, out);
+  });
+  return cudaGetLastError();
+}
+
+size_t tree_smem_bytes(const CrsDev& c) { return ((size_t)8 * c.n + c.n / 2 + 32) * 8 + 2 * (size_t)c.n * 2; }
+
+cudaError_t tree(const CrsDev& c, const QueryDev* queries, const ShardDev* shards, u32 nq, u64 r_mod_q, u64 ms_target,
+                 u64* stack, u64* a_out, u64* b_out, u32* status, cudaStream_t s) {
+  if (nq == 0) return cudaSuccess;
+  if (!c.galois_R || c.gamma > c.n / 2) return cudaErrorInvalidValue;
+  const size_t smem = tree_smem_bytes(c);
+  IG_DISPATCH_LOGN(c.logn, {
+    auto k = k_tree<L>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k<<<nq, (1 << L) / 4, smem, s>>>(c, queries, shards, r_mod_q, shoup_companion(r_mod_q), ms_target, stack, a_out,
+                                      b_out, status);
   });
   return cudaGetLastError();
 }

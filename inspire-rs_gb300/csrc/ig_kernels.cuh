@@ -30,6 +30,9 @@ struct CrsDev {
   // NTT of the last exact-gadget digit from the others (base^-2 (R - D0 - base D1)):
   // the three constants in R-form, for one lazy Montgomery reduction.
   u64 ld_inv_R, ld_c0_R, ld_c1_R;
+  // Galois keys of the automorphism tree (OnePacking), null when the CRS carries none:
+  // key i (t = n / 2^i + 1) as 3 rows of (a, b), each n words, R-form NTT.
+  const u64* galois_R;
 };
 
 // One query of a launch.
@@ -100,6 +103,13 @@ size_t respond_smem_bytes(const CrsDev& c, bool pair);
 // of scratch. r_mod_q = 2^64 mod q.
 cudaError_t nopack(const CrsDev& c, const QueryDev* queries, const ShardDev* shards, u32 nq, u64 r_mod_q,
                    u64* AB_R, u64* out, u32* status, cudaStream_t s);
+
+// OnePacking (respond_one_packing): one CTA per query walks the automorphism tree; stack
+// holds nq x logn x 2n words of waiting nodes. Outputs coefficient-form (a, b), switched to
+// ms_target when nonzero.
+size_t tree_smem_bytes(const CrsDev& c);
+cudaError_t tree(const CrsDev& c, const QueryDev* queries, const ShardDev* shards, u32 nq, u64 r_mod_q, u64 ms_target,
+                 u64* stack, u64* a_out, u64* b_out, u32* status, cudaStream_t s);
 
 // Integer roofline probe: blocks x 256 threads x iters x 8 lazy butterflies in registers.
 cudaError_t butterfly_peak(u64* out, int blocks, int iters, cudaStream_t s);

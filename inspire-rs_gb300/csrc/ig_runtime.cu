@@ -1345,6 +1345,123 @@ int ig_respond_nopacking_batch(ig_ctx* c, uint64_t dbh, uint32_t count, const ui
   return IG_OK;
 }
 
+int ig_crs_set_galois_keys(ig_ctx* c, uint64_t crs, uint32_t count, uint32_t rows, const uint64_t* keys) {
+  if (!c) return IG_ERR_ARG;
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  CrsObj* o = get_crs(c, crs);
+  if (!o) return fail(c, IG_ERR_HANDLE, "unknown CRS handle %llu", (unsigned long long)crs);
+  // ServerCrs::require_galois_keys (pir/setup.rs:195-226).
+  if (count != o->logn)
+    return fail(c, IG_ERR_SHAPE,
+                "respond_one_packing: %u galois keys, but ring_dim %u packs through %u tree levels; this CRS cannot "
+                "drive automorphism packing",
+                count, o->n, o->logn);
+  if (rows != 3) return fail(c, IG_ERR_SHAPE, "respond_one_packing: galois key 0 carries %u rows for a 3-digit gadget", rows);
+  if (!keys) return fail(c, IG_ERR_ARG, "ig_crs_set_galois_keys: null keys");
+  const size_t words = (size_t)count * rows * 2 * o->n;
+  for (size_t i = 0; i < words; i++)
+    if (keys[i] >= Q)
+      return fail(c, IG_ERR_SHAPE, "respond_one_packing: galois key %zu holds a coefficient that is not a residue mod q",
+                  i / ((size_t)rows * 2 * o->n));
+  void* raw = nullptr;
+  void* dk = nullptr;
+  int rc = scratch(c, "galois_raw", words * 8, &raw);
+  if (!rc) rc = dalloc(c, &dk, words * 8, &o->bytes);
+  if (rc) return rc;
+  IG_CUDA(c, cudaMemcpyAsync(raw, keys, words * 8, cudaMemcpyHostToDevice, c->stream));
+  IG_CUDA(c, igk::ntt_rows(o->dev, (const u64*)raw, (u64*)dk, (u32)(words / o->n), R_MOD_Q, shoup_companion(R_MOD_Q),
+                           c->stream));
+  IG_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (o->dev.galois_R) {
+    for (auto it = o->allocs.begin(); it != o->allocs.end(); ++it)
+      if (*it == (void*)o->dev.galois_R) {
+        cudaFree(*it);
+        o->allocs.erase(it);
+        o->bytes -= words * 8;
+        c->obj_bytes -= words * 8;
+        break;
+      }
+  }
+  o->allocs.push_back(dk);
+  o->dev.galois_R = (const u64*)dk;
+  return IG_OK;
+}
+
+int ig_respond_one_packing_batch(ig_ctx* c, uint64_t dbh, uint32_t count, const uint32_t* shard_ids,
+                                 const uint8_t* seeds, const uint64_t* as, const uint64_t* bs, uint64_t ms_target,
+                                 uint64_t* a_out, uint64_t* b_out) {
+  if (!c) return IG_ERR_ARG;
+  if (count == 0 || !shard_ids || (!seeds && !as) || !bs || !a_out || !b_out)
+    return fail(c, IG_ERR_ARG, "respond_one_packing: empty batch or null buffer");
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  DbObj* db = get_db(c, dbh);
+  if (!db) return fail(c, IG_ERR_HANDLE, "unknown database handle %llu", (unsigned long long)dbh);
+  CrsObj& o = *get_crs(c, db->crs);
+  const size_t n = o.n;
+  if (!o.dev.galois_R)
+    return fail(c, IG_ERR_SHAPE,
+                "respond_one_packing: 0 galois keys, but ring_dim %u packs through %u tree levels; this CRS cannot "
+                "drive automorphism packing",
+                o.n, o.logn);
+  if (ms_target && (ms_target >= Q || ms_target < o.p || ms_target % (2 * n) != 1))
+    return fail(c, IG_ERR_ARG, "mod-switch target_modulus %llu must be in [p, q) and 1 mod 2d",
+                (unsigned long long)ms_target);
+  std::unordered_map<u32, u32> local;
+  std::vector<ShardDev> table;
+  for (u32 i = 0; i < count; i++) {
+    const u32 s = shard_ids[i];
+    if (s >= db->num_shards)
+      return fail(c, IG_ERR_ARG,
+                  "respond_one_packing: shard %u not found at dense position %u; encoded database has %u shards", s, s,
+                  db->num_shards);
+    if (!db->shards[s].cols) return fail(c, IG_ERR_ARG, "respond_one_packing: shard %u holds no columns", s);
+    if (!local.count(s)) {
+      local[s] = (u32)table.size();
+      table.push_back(db->shards[s].dev());
+    }
+  }
+  const size_t seed_bytes = as ? (size_t)count * n * 8 : (size_t)count * 32;
+  void *d_table, *d_q, *d_seeds, *d_bs, *d_stack, *d_a, *d_b, *d_status;
+  int rc;
+  if ((rc = scratch(c, "tr_table", table.size() * sizeof(ShardDev), &d_table)) ||
+      (rc = scratch(c, "tr_queries", count * sizeof(QueryDev), &d_q)) ||
+      (rc = scratch(c, "tr_seeds", seed_bytes, &d_seeds)) || (rc = scratch(c, "tr_bs", (size_t)count * n * 8, &d_bs)) ||
+      (rc = scratch(c, "tr_stack", (size_t)count * o.logn * 2 * n * 8, &d_stack)) ||
+      (rc = scratch(c, "tr_a", (size_t)count * n * 8, &d_a)) || (rc = scratch(c, "tr_b", (size_t)count * n * 8, &d_b)) ||
+      (rc = scratch(c, "tr_status", count * 4, &d_status)))
+    return rc;
+  std::vector<QueryDev> qs(count);
+  for (u32 i = 0; i < count; i++) {
+    qs[i].shard = local[shard_ids[i]];
+    qs[i].reserved = 0;
+    qs[i].seed = as ? nullptr : (const u32*)((const uint8_t*)d_seeds + (size_t)i * 32);
+    qs[i].a = as ? (const u64*)d_seeds + (size_t)i * n : nullptr;
+    qs[i].b = (const u64*)d_bs + (size_t)i * n;
+    qs[i].seat_R = nullptr;
+  }
+  cudaStream_t s = c->stream;
+  if ((rc = stage_h2d(c, d_table, table.data(), table.size() * sizeof(ShardDev))) ||
+      (rc = stage_h2d(c, d_q, qs.data(), count * sizeof(QueryDev))) ||
+      (rc = stage_h2d(c, d_seeds, as ? (const void*)as : (const void*)seeds, seed_bytes)) ||
+      (rc = stage_h2d(c, d_bs, bs, (size_t)count * n * 8)))
+    return rc;
+  IG_CUDA(c, cudaMemsetAsync(d_status, 0, count * 4, s));
+  IG_CUDA(c, igk::tree(o.dev, (const QueryDev*)d_q, (const ShardDev*)d_table, count, R_MOD_Q, ms_target,
+                       (u64*)d_stack, (u64*)d_a, (u64*)d_b, (u32*)d_status, s));
+  c->launches++;
+  std::vector<u32> status(count);
+  IG_CUDA(c, cudaMemcpyAsync(status.data(), d_status, count * 4, cudaMemcpyDeviceToHost, s));
+  IG_CUDA(c, cudaStreamSynchronize(s));
+  for (u32 i = 0; i < count; i++)
+    if (status[i]) return fail(c, IG_ERR_DEVICE, "query %u: tree kernel status %u", i, status[i]);
+  IG_CUDA(c, cudaMemcpyAsync(a_out, d_a, (size_t)count * n * 8, cudaMemcpyDeviceToHost, s));
+  IG_CUDA(c, cudaMemcpyAsync(b_out, d_b, (size_t)count * n * 8, cudaMemcpyDeviceToHost, s));
+  IG_CUDA(c, cudaStreamSynchronize(s));
+  return IG_OK;
+}
+
 int ig_respond_seeded_batch_device(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_t handle, uint32_t count,
                                    const uint32_t* shard_ids, const uint8_t* d_seeds, const uint64_t* d_bs,
                                    uint64_t ms_target, uint64_t* d_a, uint64_t* d_b, uint32_t* d_status) {
@@ -1557,6 +1674,20 @@ int ig_response_encode(const uint64_t* a, const uint64_t* b, uint32_t n, uint32_
   put_u32(w, 0);   //   PackingMode::Inspiring)
   *len_out = w.size();
   if (out) memcpy(out, w.data(), w.size() < cap ? w.size() : cap);
+  return IG_OK;
+}
+
+int ig_response_encode_tree(const uint64_t* a, const uint64_t* b, uint32_t n, uint32_t retained, uint64_t modulus,
+                            uint8_t* out, size_t cap, size_t* len_out) {
+  size_t len = 0;
+  const int rc = ig_response_encode(a, b, n, retained, modulus, nullptr, 0, &len);
+  if (rc) return rc;
+  *len_out = len;
+  if (!out) return IG_OK;
+  std::vector<uint8_t> w(len);
+  ig_response_encode(a, b, n, retained, modulus, w.data(), len, &len);
+  w[len - 4] = 1;  // Some(PackingMode::Tree): variant 1 of query.rs:20-26
+  memcpy(out, w.data(), len < cap ? len : cap);
   return IG_OK;
 }
 

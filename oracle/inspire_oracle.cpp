@@ -638,7 +638,9 @@ static void write_poly(Bin& w, const Vec& c, u64 modulus) {
 
 // ServerResponse tight wire (respond.rs:111-176): Packed{a, b_prefix, retained}, no
 // column ciphertexts, Some(PackingMode::Inspiring).
-static std::vector<uint8_t> response_bytes(const Vec& a, const Vec& b, size_t retained, u64 modulus) {
+// `variant`: the PackingMode index (query.rs:20-26), 0 Inspiring, 1 Tree.
+static std::vector<uint8_t> response_bytes(const Vec& a, const Vec& b, size_t retained, u64 modulus,
+                                           uint32_t variant = 0) {
   Bin w;
   w.u32(1);
   write_poly(w, a, modulus);
@@ -646,7 +648,7 @@ static std::vector<uint8_t> response_bytes(const Vec& a, const Vec& b, size_t re
   w.u32((uint32_t)retained);
   w.u64_(0);
   w.u8(1);
-  w.u32(0);
+  w.u32(variant);
   return w.b;
 }
 
@@ -817,6 +819,168 @@ static bool cell_decode(const Cell* c, u64 index, const u64* a, const u64* b, ui
     size_t off = col * 2;
     if (off < c->entry_size) entry[off] = (uint8_t)(vals[col] & 0xff);
     if (off + 1 < c->entry_size) entry[off + 1] = (uint8_t)((vals[col] >> 8) & 0xff);
+  }
+  memcpy(record_out, entry.data(), entry.size());
+  return memcmp(entry.data(), &c->db[index * c->entry_size], c->entry_size) == 0;
+}
+
+// ---------------------------------------------------------------------------------------
+// OnePacking: respond_one_packing (pir/respond.rs:696-729) over the Galois-automorphism tree
+// of inspiring/automorph_pack.rs.
+
+// One key-switching matrix (ks/setup.rs:12-20): a row (a, b) per gadget power, coefficient
+// form.
+struct KsMatrix {
+  std::vector<Vec> a, b;
+};
+
+// homomorphic_automorph (automorph_pack.rs:15-43): tau_t on both parts, then the a part's
+// base-2^20 digits times the key rows, each product through the transform.
+static void hom_automorph(const Params& P, const Ntt& ntt, const Vec& ca, const Vec& cb, u64 t, const KsMatrix& ks,
+                          Vec& ra, Vec& rb) {
+  const u64 q = P.q;
+  const Vec aa = automorphism_coeff(ca, t, q);
+  rb = automorphism_coeff(cb, t, q);
+  ra.assign(P.n, 0);
+  const auto digits = gadget_decompose(P, aa);
+  for (size_t i = 0; i < digits.size(); i++) {
+    if (i >= ks.a.size()) continue;
+    const Vec ta = ntt.mul(digits[i], ks.a[i]), tb = ntt.mul(digits[i], ks.b[i]);
+    for (size_t k = 0; k < P.n; k++) {
+      ra[k] = addmod(ra[k], ta[k], q);
+      rb[k] = addmod(rb[k], tb[k], q);
+    }
+  }
+}
+
+// pack_lwes_inner (automorph_pack.rs:96-163): the 2^ell ciphertexts reachable from `start`
+// (b parts zero at the leaves) combined as (even + y odd) + tau_t(even - y odd) with
+// y = X^(d >> ell), t = 2^ell + 1 and key index log d - ell. Leaves past the inputs are the
+// zero ciphertexts of the padding.
+static void pack_inner(const Params& P, const Ntt& ntt, size_t ell, size_t start, const std::vector<Vec>& leaf_a,
+                       const std::vector<KsMatrix>& keys, size_t log_n, Vec& ra, Vec& rb) {
+  const size_t d = P.n;
+  const u64 q = P.q;
+  if (ell == 0) {
+    ra = start < leaf_a.size() ? leaf_a[start] : Vec(d, 0);
+    rb.assign(d, 0);
+    return;
+  }
+  const size_t step = (size_t)1 << (log_n - ell);
+  Vec ea, eb, oa, ob;
+  pack_inner(P, ntt, ell - 1, start, leaf_a, keys, log_n, ea, eb);
+  pack_inner(P, ntt, ell - 1, start + step, leaf_a, keys, log_n, oa, ob);
+  Vec y(d, 0), ny(d, 0);  // YConstants (automorph_pack.rs:55-83), level ell - 1
+  y[d >> ell] = 1;
+  ny[d >> ell] = q - 1;
+  const Vec ya = ntt.mul(oa, y), yb = ntt.mul(ob, y), na = ntt.mul(oa, ny), nb = ntt.mul(ob, ny);
+  Vec s0a(d), s0b(d), s1a(d), s1b(d);
+  for (size_t k = 0; k < d; k++) {
+    s0a[k] = addmod(ea[k], ya[k], q);
+    s0b[k] = addmod(eb[k], yb[k], q);
+    s1a[k] = addmod(ea[k], na[k], q);
+    s1b[k] = addmod(eb[k], nb[k], q);
+  }
+  const u64 t = ((u64)1 << ell) + 1;
+  const size_t ks_idx = keys.size() - ell;
+  Vec ha, hb;
+  hom_automorph(P, ntt, s1a, s1b, t, keys[ks_idx], ha, hb);
+  ra.resize(d);
+  rb.resize(d);
+  for (size_t k = 0; k < d; k++) {
+    ra[k] = addmod(s0a[k], ha[k], q);
+    rb[k] = addmod(s0b[k], hb[k], q);
+  }
+}
+
+// respond_one_packing: the column products (plaintext_multiply_columns, respond.rs:585-599),
+// their coefficient-0 LWEs (rlwe/enc.rs:161-174), whose a vectors prep_pack_lwes turns back
+// into the products' a polynomials (automorph_pack.rs:238-268), then pack_lwes
+// (automorph_pack.rs:270-341): one input skips the tree and its scaling; otherwise the
+// tree over d padded leaves, and b_k += d b-value_k.
+static void respond_one_packing(const PackParams& pp, const std::vector<Vec>& columns, const Vec& a, const Vec& b,
+                                const std::vector<KsMatrix>& keys, Vec& out_a, Vec& out_b) {
+  const Params& P = pp.P;
+  const Ntt& ntt = *pp.ntt;
+  const size_t d = P.n, gamma = columns.size();
+  const u64 q = P.q;
+  std::vector<Vec> leaf_a(gamma);
+  Vec bvals(gamma);
+#pragma omp parallel for
+  for (long j = 0; j < (long)gamma; j++) {
+    leaf_a[j] = ntt.mul(a, columns[j]);
+    bvals[j] = ntt.mul(b, columns[j])[0];
+  }
+  if (gamma == 1) {
+    out_a = leaf_a[0];
+    out_b.assign(d, 0);
+    out_b[0] = bvals[0];
+    return;
+  }
+  size_t log_d = 0;
+  while (((size_t)1 << log_d) < d) log_d++;
+  pack_inner(P, ntt, log_d, 0, leaf_a, keys, log_d, out_a, out_b);
+  for (size_t z = 0; z < gamma; z++) out_b[z] = addmod(out_b[z], mulmod(bvals[z], d % q, q), q);
+}
+
+// Test-only Galois keys for secret s, in the shape setup_with_rng makes them
+// (pir/setup.rs:435-445, ks/setup.rs:101-153): key i switches tau_t(s) to s for
+// t = d / 2^i + 1, rows (a_r, -a_r s + e_r + tau_t(s) base^r). The reference draws a_r from
+// the OS entropy source, so its keys cannot be regenerated; here a_r is uniform from
+// ChaCha20(seed) on stream i * rows + r and e_r uniform in [-4, 4] from the same stream.
+static std::vector<KsMatrix> test_galois_keys(const Params& P, const Ntt& ntt, const Vec& sk, const uint8_t seed[32]) {
+  const size_t d = P.n;
+  const u64 q = P.q;
+  size_t log_d = 0;
+  while (((size_t)1 << log_d) < d) log_d++;
+  std::vector<KsMatrix> keys(log_d);
+  for (size_t i = 0; i < log_d; i++) {
+    const Vec sa = automorphism_coeff(sk, (d >> i) + 1, q);
+    for (size_t r = 0; r < P.gadget_len; r++) {
+      ChaCha20Rng rng = ChaCha20Rng::from_seed(seed);
+      rng.set_stream(i * P.gadget_len + r);
+      Vec a(d), e(d);
+      for (size_t k = 0; k < d; k++) a[k] = gen_range_u64(rng, 0, q);
+      for (size_t k = 0; k < d; k++) e[k] = from_signed((i64)(rng.next_u64() % 9) - 4, q);
+      const Vec as = ntt.mul(a, sk);
+      const u64 pw = gadget_power(P, r);
+      Vec bb(d);
+      for (size_t k = 0; k < d; k++) bb[k] = addmod(submod(e[k], as[k], q), mulmod(sa[k], pw, q), q);
+      keys[i].a.push_back(a);
+      keys[i].b.push_back(bb);
+    }
+  }
+  return keys;
+}
+
+static std::vector<KsMatrix> unpack_keys(const u64* keys, size_t count, size_t rows, size_t n) {
+  std::vector<KsMatrix> out(count);
+  for (size_t i = 0; i < count; i++)
+    for (size_t r = 0; r < rows; r++) {
+      const u64* row = keys + (i * rows + r) * 2 * n;
+      out[i].a.emplace_back(row, row + n);
+      out[i].b.emplace_back(row + n, row + 2 * n);
+    }
+  return out;
+}
+
+// extract_packed for a tree response (pir/extract.rs:184-226): decrypt, round by delta,
+// then multiply by d^-1 mod p.
+static bool cell_decode_tree(const Cell* c, u64 index, const u64* a, const u64* b, uint8_t* record_out) {
+  const Params& P = c->P;
+  const size_t n = P.n;
+  Vec av(a, a + n);
+  const Vec as = c->pp->ntt->mul(av, c->sk);
+  const u64 delta = P.delta();
+  const u64 d_inv = powmod(n % P.p, P.p - 2, P.p);
+  std::vector<uint8_t> entry(c->entry_size, 0);
+  for (size_t col = 0; col < c->gamma; col++) {
+    const u64 noisy = addmod(as[col], b[col], P.q);
+    const u64 m = (u64)(((u128)noisy + delta / 2) / delta) % P.p;
+    const u64 v = mulmod(m, d_inv, P.p);
+    const size_t off = col * 2;
+    if (off < c->entry_size) entry[off] = (uint8_t)(v & 0xff);
+    if (off + 1 < c->entry_size) entry[off + 1] = (uint8_t)((v >> 8) & 0xff);
   }
   memcpy(record_out, entry.data(), entry.size());
   return memcmp(entry.data(), &c->db[index * c->entry_size], c->entry_size) == 0;
@@ -1021,6 +1185,12 @@ u64 orc_response_bytes(const u64* a, const u64* b, u64 n, u64 retained, u64 modu
   if (out) memcpy(out, v.data(), std::min<u64>(cap, v.size()));
   return v.size();
 }
+// The same bytes for a tree-packed response (packing_mode Some(Tree)).
+u64 orc_response_bytes_tree(const u64* a, const u64* b, u64 n, u64 retained, u64 modulus, uint8_t* out, u64 cap) {
+  auto v = response_bytes(Vec(a, a + n), Vec(b, b + n), retained, modulus, 1);
+  if (out) memcpy(out, v.data(), std::min<u64>(cap, v.size()));
+  return v.size();
+}
 
 // respond (respond.rs:614-643), the NoPacking variant: one RLWE ciphertext (a h_j, b h_j)
 // per column from plaintext_multiply_columns (respond.rs:585-599), and their sum as the
@@ -1051,6 +1221,26 @@ int orc_respond_nopacking(void* cv, const u64* columns, const u64* a, const u64*
       memcpy(out + (2 + 2 * j) * n, ca[j].data(), n * 8);
       memcpy(out + (3 + 2 * j) * n, cb[j].data(), n * 8);
     }
+    return 0;
+  } catch (std::exception& e) {
+    g_err = e.what();
+    return -1;
+  }
+}
+
+// respond_one_packing for one query: columns gamma x n, a and b n words (coefficient form),
+// keys log d x rows x (a, b) x n words; writes the packed (a, b).
+int orc_respond_one_packing(void* cv, const u64* columns, const u64* a, const u64* b, const u64* keys, u64 nkeys,
+                            u64* out_a, u64* out_b) {
+  auto* c = (OrcCache*)cv;
+  const size_t n = c->pp->P.n, gamma = c->pp->gamma;
+  try {
+    auto cols = unpack_polys(columns, gamma, n);
+    const auto ks = unpack_keys(keys, nkeys, c->pp->P.gadget_len, n);
+    Vec av(a, a + n), bv(b, b + n), ra, rb;
+    respond_one_packing(*c->pp, cols, av, bv, ks, ra, rb);
+    memcpy(out_a, ra.data(), n * 8);
+    memcpy(out_b, rb.data(), n * 8);
     return 0;
   } catch (std::exception& e) {
     g_err = e.what();
@@ -1117,6 +1307,21 @@ void orc_cell_next_query(void* cv, u64 index, uint32_t* shard_id, uint8_t* seed,
 }
 int orc_cell_decode(void* cv, u64 index, const u64* a, const u64* b, uint8_t* record_out) {
   return cell_decode((const Cell*)cv, index, a, b, record_out) ? 1 : 0;
+}
+// Test Galois keys of the cell's secret: out = log d x rows x (a, b) x n words.
+void orc_cell_galois_keys(void* cv, const uint8_t* seed, u64* out) {
+  auto* c = (Cell*)cv;
+  const auto keys = test_galois_keys(c->P, *c->pp->ntt, c->sk, seed);
+  size_t k = 0;
+  for (auto& m : keys)
+    for (size_t r = 0; r < m.a.size(); r++) {
+      memcpy(out + k * c->P.n, m.a[r].data(), c->P.n * 8);
+      memcpy(out + (k + 1) * c->P.n, m.b[r].data(), c->P.n * 8);
+      k += 2;
+    }
+}
+int orc_cell_decode_tree(void* cv, u64 index, const u64* a, const u64* b, uint8_t* record_out) {
+  return cell_decode_tree((const Cell*)cv, index, a, b, record_out) ? 1 : 0;
 }
 void orc_cell_record(void* cv, u64 index, uint8_t* out) {
   auto* c = (Cell*)cv;

@@ -56,6 +56,10 @@ def lib():
             "orc_store_scan": (I, [V, V, P, P, P]),
             "orc_mod_switch": (None, [P, U64, U64, U64, P]),
             "orc_response_bytes": (U64, [P, P, U64, U64, U64, P, U64]),
+            "orc_response_bytes_tree": (U64, [P, P, U64, U64, U64, P, U64]),
+            "orc_respond_one_packing": (I, [V, P, P, P, P, U64, P, P]),
+            "orc_cell_galois_keys": (None, [V, P, P]),
+            "orc_cell_decode_tree": (I, [V, U64, P, P, P]),
             "orc_cell_build": (V, [U64, U64, U64, ctypes.c_double, U64, U64, I, U64, U64, U64]),
             "orc_cell_free": (None, [V]),
             "orc_cell_info": (None, [V, P, P, P, P]),
@@ -157,6 +161,21 @@ class Cache:
         return out
 
 
+    def respond_one_packing(self, columns, a, b, galois_keys):
+        """respond_one_packing (respond.rs:696-729): the Galois-automorphism tree over the
+        column LWEs; galois_keys is (log d, rows, 2, n) in coefficient form."""
+        n = self.params.n
+        columns = np.ascontiguousarray(columns, dtype=np.uint64)
+        a = np.ascontiguousarray(a, dtype=np.uint64)
+        b = np.ascontiguousarray(b, dtype=np.uint64)
+        keys = np.ascontiguousarray(galois_keys, dtype=np.uint64)
+        ao = np.zeros(n, dtype=np.uint64)
+        bo = np.zeros(n, dtype=np.uint64)
+        if lib().orc_respond_one_packing(self.h, _p(columns), _p(a), _p(b), _p(keys), keys.shape[0], _p(ao), _p(bo)):
+            raise RuntimeError(lib().orc_last_error().decode())
+        return ao, bo
+
+
 class Store:
     """ShardPackingStore restated: step-1 sums + tags over one shard's columns."""
 
@@ -237,6 +256,16 @@ def response_bytes(a, b, retained, modulus=DEFAULT_Q) -> bytes:
     L = lib().orc_response_bytes(_p(a), _p(b), len(a), retained, modulus, None, 0)
     out = np.zeros(L, dtype=np.uint8)
     lib().orc_response_bytes(_p(a), _p(b), len(a), retained, modulus, _p(out), L)
+    return out.tobytes()
+
+
+def response_bytes_tree(a, b, retained, modulus=DEFAULT_Q) -> bytes:
+    """ServerResponse bytes of a tree-packed response (packing_mode Some(Tree))."""
+    a = np.ascontiguousarray(a, dtype=np.uint64)
+    b = np.ascontiguousarray(b, dtype=np.uint64)
+    L = lib().orc_response_bytes_tree(_p(a), _p(b), len(a), retained, modulus, None, 0)
+    out = np.zeros(L, dtype=np.uint8)
+    lib().orc_response_bytes_tree(_p(a), _p(b), len(a), retained, modulus, _p(out), L)
     return out.tobytes()
 
 
@@ -335,6 +364,23 @@ class Cell:
         out = np.zeros(self.entry_size, dtype=np.uint8)
         lib().orc_cell_record(self.h, index, _p(out))
         return out.tobytes()
+
+    def galois_keys(self, seed: bytes):
+        """Test Galois keys of this cell's secret, (log d, rows, 2, n): a from ChaCha20(seed),
+        small errors (the reference draws its keys' a from OS entropy)."""
+        log_d = self.params.n.bit_length() - 1
+        out = np.zeros((log_d, self.params.gadget_len, 2, self.params.n), dtype=np.uint64)
+        s = np.frombuffer(seed, dtype=np.uint8).copy()
+        lib().orc_cell_galois_keys(self.h, _p(s), _p(out))
+        return out
+
+    def decode_tree(self, index, a, b):
+        """extract_packed for a tree response (extract.rs:184-226)."""
+        a = np.ascontiguousarray(a, dtype=np.uint64)
+        b = np.ascontiguousarray(b, dtype=np.uint64)
+        rec = np.zeros(self.entry_size, dtype=np.uint8)
+        ok = lib().orc_cell_decode_tree(self.h, index, _p(a), _p(b), _p(rec))
+        return bool(ok), rec.tobytes()
 
 
 def gaussian_stream_fnv(sigma, seed, count):

@@ -170,3 +170,23 @@ def test_nopacking_restatement_decodes(oracle):
         bits = 60
         poly = 8 + (P.n * bits + 7) // 8 + 41
         assert len(wire) == 4 + 2 * poly + 8 + cell.gamma * 2 * poly + 1
+
+
+def test_tree_restatement_decodes(oracle):
+    """The oracle's OnePacking respond (respond.rs:696-729, the automorphism tree of
+    automorph_pack.rs) under test Galois keys of the cell's secret decodes, through
+    extract_packed's d^-1 scaling (extract.rs:184-226), to the requested record; the tree
+    response's wire is the packed one with packing_mode Some(Tree)."""
+    P = oracle.Params(n=256)
+    cell = oracle.Cell(P, 16, 0x7EE0)
+    keys = cell.galois_keys(bytes(range(32)))
+    assert keys.shape == (8, 3, 2, P.n)
+    cache = oracle.Cache(P, cell.gamma, cell.w_seed)
+    for idx in [0, 5, P.n + 3]:
+        sid, seed, b = cell.next_query(idx)
+        ao, bo = cache.respond_one_packing(cell.columns(sid), oracle.expand_seed(seed, P.n), b, keys)
+        ok, rec = cell.decode_tree(idx, ao, bo)
+        assert ok and rec == cell.record(idx), idx
+        packed = oracle.response_bytes(ao, bo, cell.gamma)
+        tree = oracle.response_bytes_tree(ao, bo, cell.gamma)
+        assert tree[:-4] == packed[:-4] and packed[-4:] == bytes(4) and tree[-4:] == bytes([1, 0, 0, 0])
