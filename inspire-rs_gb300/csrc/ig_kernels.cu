@@ -1311,11 +1311,17 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
   for (int k = tid; k < N; k += NT) aR[k] = shoup(aR[k], r_mod_q, r_mod_qp);
   __syncthreads();
 
-  u64 ca[4], cb[4];  // the current node, slots tid + j NT
+  const int l0 = 4 * tid;
+  u64 ca[4], cb[4];  // the current node at slots l0..l0+3 (thread tid's transform unit)
   bool cur_zero = true;
+  u64 wi, wip;
+  inv_twiddle(tw, twp, 1, wi, wip);
+  const u64 wf = tw[1], wfp = twp[1];
+  constexpr int H = N / 2, MF = 1 << (LOGN - 2);
   // Leaf `start`: the column through the transform times NTT(a); its b-value on the side.
   auto leaf = [&](u32 start) {
     u128 acc = 0;
+#pragma unroll
     for (int j = 0; j < 4; j++) {
       const int k = tid + j * NT;
       const u64 h = sh.cols16 ? (u64)sh.cols16[(size_t)start * N + k] : reduce128(sh.columns[(size_t)start * N + k]);
@@ -1339,72 +1345,204 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
     }
 #pragma unroll
     for (int j = 0; j < 4; j++) {
-      const int k = tid + j * NT;
-      ca[j] = mont(csub(csub2(X[k])), aR[k]);
+      ca[j] = mont(csub(csub2(X[l0 + j])), aR[l0 + j]);
       cb[j] = 0;
     }
     __syncthreads();  // X is rewritten next
   };
   // The current node becomes (E + y O) + keyswitch(tau_t(E - y O)) at level ell, E from the
-  // stack slot ell - 1; the current node is O (zero when odd_zero).
+  // stack slot ell - 1; the current node is O (zero when odd_zero). The transforms follow
+  // k_respond's link: the inverse's first two stages in registers, its last stage fused with
+  // n^-1, the digit split and the forward's first stage, the forward's last two stages in
+  // registers, X and D under the sw() layout.
   auto combine = [&](int ell, bool odd_zero) {
-    const u64* E = stk + (size_t)(ell - 1) * 2 * N;
-    const u32 sh_y = (u32)(N >> ell), t = (1u << ell) + 1;
-    const u64* key = c.galois_R + (size_t)(LOGN - ell) * 6 * N;
-    u64 s0a[4], s0b[4];
+    const u64* E = stk + (size_t)(ell - 1) * 2 * N + l0;
+    const u32 sy = (u32)(N >> ell), t = (1u << ell) + 1;
+    const u64* key = c.galois_R + (size_t)(LOGN - ell) * 6 * N + l0;
+    u64 s0a[4], s0b[4], aa[4], ab[4];
+    {
+      const ulonglong2 e01 = *reinterpret_cast<const ulonglong2*>(E);
+      const ulonglong2 e23 = *reinterpret_cast<const ulonglong2*>(E + 2);
+      const ulonglong2 f01 = *reinterpret_cast<const ulonglong2*>(E + N);
+      const ulonglong2 f23 = *reinterpret_cast<const ulonglong2*>(E + N + 2);
+      const u64 ea[4] = {e01.x, e01.y, e23.x, e23.y}, eb[4] = {f01.x, f01.y, f23.x, f23.y};
+      u64 da[4], db[4];
 #pragma unroll
-    for (int j = 0; j < 4; j++) {
-      const int k = tid + j * NT;
-      const u64 ea = E[k], eb = E[N + k];
-      u64 ya = 0, yb = 0;
-      if (!odd_zero) {
-        const u64 y = c.pow_root_R[(e_tab[k] * sh_y) & M2N];
-        ya = mont(ca[j], y);
-        yb = mont(cb[j], y);
+      for (int j = 0; j < 4; j++) {
+        u64 ya = 0, yb = 0;
+        if (!odd_zero) {
+          const u64 y = c.pow_root_R[(e_tab[l0 + j] * sy) & M2N];
+          ya = mont(ca[j], y);
+          yb = mont(cb[j], y);
+        }
+        s0a[j] = addq(ea[j], ya);
+        s0b[j] = addq(eb[j], yb);
+        da[j] = subq(ea[j], ya);
+        db[j] = subq(eb[j], yb);
       }
-      s0a[j] = addq(ea, ya);
-      s0b[j] = addq(eb, yb);
-      S1a[k] = subq(ea, ya);
-      S1b[k] = subq(eb, yb);
+      *reinterpret_cast<ulonglong2*>(S1a + l0) = make_ulonglong2(da[0], da[1]);
+      *reinterpret_cast<ulonglong2*>(S1a + l0 + 2) = make_ulonglong2(da[2], da[3]);
+      *reinterpret_cast<ulonglong2*>(S1b + l0) = make_ulonglong2(db[0], db[1]);
+      *reinterpret_cast<ulonglong2*>(S1b + l0 + 2) = make_ulonglong2(db[2], db[3]);
     }
     __syncthreads();
-    u64 aa[4], ab[4];
 #pragma unroll
     for (int j = 0; j < 4; j++) {
-      const int k = tid + j * NT;
-      const u32 src = s_tab[((t * e_tab[k]) & M2N) >> 1];
+      const u32 src = s_tab[((t * e_tab[l0 + j]) & M2N) >> 1];
       aa[j] = S1a[src];
       ab[j] = S1b[src];
-      X[k] = aa[j];
+    }
+    {
+      // Inverse stages 0-1 of unit tid (block B = tid, m = N/2).
+      u64 w0, w0p, w1, w1p, w2, w2p;
+      inv_twiddle(tw, twp, H + 2 * tid, w0, w0p);
+      inv_twiddle(tw, twp, H + 2 * tid + 1, w1, w1p);
+      inv_twiddle(tw, twp, H / 2 + tid, w2, w2p);
+      u64 a0 = aa[0], a1 = aa[1], a2 = aa[2], a3 = aa[3];
+      bf_inv(a0, a1, w0, w0p);
+      bf_inv(a2, a3, w1, w1p);
+      bf_inv(a0, a2, w2, w2p);
+      bf_inv(a1, a3, w2, w2p);
+      *reinterpret_cast<ulonglong2*>(X + sw(l0)) = make_ulonglong2(a0, a1);
+      *reinterpret_cast<ulonglong2*>(X + sw(l0 + 2)) = make_ulonglong2(a2, a3);
     }
     __syncthreads();
+    // Inverse stages 2 .. logn-2 (radix-4 pairs, a radix-2 stage last when logn is even).
+    int s = 2;
+#pragma unroll 1
+    for (; s + 1 <= LOGN - 2; s += 2) {
+      const int tt = 1 << s, m = N >> (s + 1);
+      const int B = tid >> s, o = tid & (tt - 1);
+      const int e0 = B * 4 * tt + o;
+      u64 w0, w0p, w1, w1p, w2, w2p;
+      inv_twiddle(tw, twp, m + 2 * B, w0, w0p);
+      inv_twiddle(tw, twp, m + 2 * B + 1, w1, w1p);
+      inv_twiddle(tw, twp, (m >> 1) + B, w2, w2p);
+      u64 a0 = X[sw(e0)], a1 = X[sw(e0 + tt)], a2 = X[sw(e0 + 2 * tt)], a3 = X[sw(e0 + 3 * tt)];
+      bf_inv(a0, a1, w0, w0p);
+      bf_inv(a2, a3, w1, w1p);
+      bf_inv(a0, a2, w2, w2p);
+      bf_inv(a1, a3, w2, w2p);
+      X[sw(e0)] = a0;
+      X[sw(e0 + tt)] = a1;
+      X[sw(e0 + 2 * tt)] = a2;
+      X[sw(e0 + 3 * tt)] = a3;
+      __syncthreads();
+    }
+    if (s == LOGN - 2) {
+      const int tt = 1 << s, m = N >> (s + 1);
+#pragma unroll
+      for (int r = 0; r < 2; r++) {
+        const int v = tid + r * NT;
+        const int B = v >> s, o = v & (tt - 1);
+        const int e = B * 2 * tt + o;
+        u64 w, wp;
+        inv_twiddle(tw, twp, m + B, w, wp);
+        u64 a = X[sw(e)], b = X[sw(e + tt)];
+        bf_inv(a, b, w, wp);
+        X[sw(e)] = a;
+        X[sw(e + tt)] = b;
+      }
+      __syncthreads();
+    }
+    // Inverse stage logn-1, n^-1, digit split and forward stage 0, per pair (b, b + N/2).
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+      const int b = tid + j * NT;
+      u64 x0 = X[sw(b)], x1 = X[sw(b + H)];
+      bf_inv(x0, x1, wi, wip);
+      const u64 r0 = shoup(x0, c.ninv, c.ninvp), r1 = shoup(x1, c.ninv, c.ninvp);
+      const u64 p0 = r0 & DMASK, p1 = (r0 >> 20) & DMASK, q0 = r1 & DMASK, q1 = (r1 >> 20) & DMASK;
+      const u64 t0 = shoup_lazy(q0, wf, wfp), t1 = shoup_lazy(q1, wf, wfp);
+      D[sw(b)] = p0 + t0;
+      D[sw(b + H)] = p0 + 2 * Q - t0;
+      D[N + sw(b)] = p1 + t1;
+      D[N + sw(b + H)] = p1 + 2 * Q - t1;
+    }
+    __syncthreads();
+    // Forward stages 1 .. logn-3 (a radix-2 stage first when logn is even), both digits.
+    s = 1;
+    if (!(LOGN & 1)) {
+      const int lt = LOGN - 2, tt = 1 << lt;
+#pragma unroll
+      for (int r = 0; r < 2; r++) {
+        const int v = tid + r * NT;
+        const int ib = v >> lt, o = v & (tt - 1);
+        const int e = ib * 2 * tt + o;
+        const u64 w = tw[2 + ib], wp = twp[2 + ib];
+#pragma unroll
+        for (int k = 0; k < 2; k++) {
+          u64* x = D + k * N;
+          u64 a = x[sw(e)], b = x[sw(e + tt)];
+          bf_fwd(a, b, w, wp);
+          x[sw(e)] = a;
+          x[sw(e + tt)] = b;
+        }
+      }
+      __syncthreads();
+      s = 2;
+    }
+#pragma unroll 1
+    for (; s < LOGN - 2; s += 2) {
+      const int tt = N >> (s + 1), m = 1 << s, h = tt >> 1;
+      const int ib = tid / h, o = tid - ib * h;
+      const int e0 = ib * 2 * tt + o;
+      const u64 wa = tw[m + ib], wap = twp[m + ib];
+      const u64 wb = tw[2 * m + 2 * ib], wbp = twp[2 * m + 2 * ib];
+      const u64 wc = tw[2 * m + 2 * ib + 1], wcp = twp[2 * m + 2 * ib + 1];
+      const int i0 = sw(e0), i1 = sw(e0 + h), i2 = sw(e0 + tt), i3 = sw(e0 + tt + h);
+      u64* x0 = D;
+      u64* x1 = D + N;
+      u64 a0 = x0[i0], a1 = x0[i1], a2 = x0[i2], a3 = x0[i3];
+      u64 c0 = x1[i0], c1 = x1[i1], c2 = x1[i2], c3 = x1[i3];
+      bf_fwd(a0, a2, wa, wap);
+      bf_fwd(c0, c2, wa, wap);
+      bf_fwd(a1, a3, wa, wap);
+      bf_fwd(c1, c3, wa, wap);
+      bf_fwd(a0, a1, wb, wbp);
+      bf_fwd(c0, c1, wb, wbp);
+      bf_fwd(a2, a3, wc, wcp);
+      bf_fwd(c2, c3, wc, wcp);
+      x0[i0] = a0;
+      x0[i1] = a1;
+      x0[i2] = a2;
+      x0[i3] = a3;
+      x1[i0] = c0;
+      x1[i1] = c1;
+      x1[i2] = c2;
+      x1[i3] = c3;
+      __syncthreads();
+    }
+    // Forward stages logn-2, logn-1 of unit tid, both digits, in registers.
+    u64 d0[4], d1[4];
     {
-      u64* const bufs[1] = {X};
-      ntt_inv_r4<LOGN, NT, 1>(bufs, tw, twp);
+      const u64 fa = tw[MF + tid], fap = twp[MF + tid];
+      const u64 fb = tw[2 * MF + 2 * tid], fbp = twp[2 * MF + 2 * tid];
+      const u64 fc = tw[2 * MF + 2 * tid + 1], fcp = twp[2 * MF + 2 * tid + 1];
+      const ulonglong2 v01 = *reinterpret_cast<const ulonglong2*>(D + sw(l0));
+      const ulonglong2 v23 = *reinterpret_cast<const ulonglong2*>(D + sw(l0 + 2));
+      const ulonglong2 g01 = *reinterpret_cast<const ulonglong2*>(D + N + sw(l0));
+      const ulonglong2 g23 = *reinterpret_cast<const ulonglong2*>(D + N + sw(l0 + 2));
+      d0[0] = v01.x, d0[1] = v01.y, d0[2] = v23.x, d0[3] = v23.y;
+      d1[0] = g01.x, d1[1] = g01.y, d1[2] = g23.x, d1[3] = g23.y;
+      bf_fwd(d0[0], d0[2], fa, fap);
+      bf_fwd(d1[0], d1[2], fa, fap);
+      bf_fwd(d0[1], d0[3], fa, fap);
+      bf_fwd(d1[1], d1[3], fa, fap);
+      bf_fwd(d0[0], d0[1], fb, fbp);
+      bf_fwd(d1[0], d1[1], fb, fbp);
+      bf_fwd(d0[2], d0[3], fc, fcp);
+      bf_fwd(d1[2], d1[3], fc, fcp);
     }
 #pragma unroll
     for (int j = 0; j < 4; j++) {
-      const int k = tid + j * NT;
-      const u64 r = shoup(X[k], c.ninv, c.ninvp);
-      D[k] = r & DMASK;
-      D[N + k] = (r >> 20) & DMASK;
-    }
-    __syncthreads();
-    {
-      u64* const bufs[2] = {D, D + N};
-      ntt_fwd_r4<LOGN, NT, 2>(bufs, tw, twp);
-    }
-#pragma unroll
-    for (int j = 0; j < 4; j++) {
-      const int k = tid + j * NT;
-      const u64 d0 = D[k], d1 = D[N + k];
-      const u64 d2 = redc(wide(aa[j], c.ld_inv_R) + wide(d0, c.ld_c0_R) + wide(d1, c.ld_c1_R));
-      const u64 na = redc(wide(d0, key[k]) + wide(d1, key[2 * N + k]) + wide(d2, key[4 * N + k]));
-      const u64 nb = redc(wide(d0, key[N + k]) + wide(d1, key[3 * N + k]) + wide(d2, key[5 * N + k]));
+      const u64 d2 = redc(wide(aa[j], c.ld_inv_R) + wide(d0[j], c.ld_c0_R) + wide(d1[j], c.ld_c1_R));
+      const u64 na = redc(wide(d0[j], key[j]) + wide(d1[j], key[2 * N + j]) + wide(d2, key[4 * N + j]));
+      const u64 nb = redc(wide(d0[j], key[N + j]) + wide(d1[j], key[3 * N + j]) + wide(d2, key[5 * N + j]));
       ca[j] = addq(s0a[j], na);
       cb[j] = addq(s0b[j], addq(ab[j], nb));
     }
-    __syncthreads();  // D and X are rewritten next
+    __syncthreads();  // S1, X and D are rewritten next
   };
 
   if (gamma == 1) {
@@ -1433,12 +1571,11 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
           zero_slots |= 1u << L;
         } else {
           zero_slots &= ~(1u << L);
-          u64* slot = stk + (size_t)L * 2 * N;
-#pragma unroll
-          for (int j = 0; j < 4; j++) {
-            slot[tid + j * NT] = ca[j];
-            slot[N + tid + j * NT] = cb[j];
-          }
+          u64* slot = stk + (size_t)L * 2 * N + l0;
+          *reinterpret_cast<ulonglong2*>(slot) = make_ulonglong2(ca[0], ca[1]);
+          *reinterpret_cast<ulonglong2*>(slot + 2) = make_ulonglong2(ca[2], ca[3]);
+          *reinterpret_cast<ulonglong2*>(slot + N) = make_ulonglong2(cb[0], cb[1]);
+          *reinterpret_cast<ulonglong2*>(slot + N + 2) = make_ulonglong2(cb[2], cb[3]);
         }
       }
     }
@@ -1447,8 +1584,8 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
   // 327-338), except for a single input.
 #pragma unroll
   for (int j = 0; j < 4; j++) {
-    X[tid + j * NT] = ca[j];
-    D[tid + j * NT] = cb[j];
+    X[l0 + j] = ca[j];
+    D[l0 + j] = cb[j];
   }
   __syncthreads();
   {
