@@ -7,11 +7,12 @@ uniform indices per step answered through respond_seeded_batch, responses mod-sw
 36 bits. Inputs are seeded synthetic data of those shapes: uniform 16-bit column words
 (the encoding of uniform random record bytes), uniform key and query words mod q.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--config 2|3|4|5]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--workload served-batch|special-modulus|mixed|serving-sweep]
 
---config 3 times the special_modulus batch of 256, --config 4 six mixed parameter sets
-(32/512/2048 B records under both gadgets, batch sizes 1-512), --config 5 the serving loop
-over 2^25 records and 1000 seats.
+--workload special-modulus times the special_modulus batch of 256, mixed six parameter sets
+(32/512/2048 B records under both gadgets, batch sizes 1-512), serving-sweep the serving
+loop over 2^25 records and 1000 seats.
 
 Prints one JSON line. `value` = queries/s over K device-resident batches (CUDA events on
 the library's stream); `e2e` = the same through the public API with host buffers;
@@ -613,10 +614,69 @@ def run_sm(args, rank, world):
 
 
 # ------------------------------------------------------------------------------------
-# Serving sweep (the survey's config 5): 2^25 records of 512 B (16,384 shards, 16 GiB of
+# Serving sweep: 2^25 records of 512 B (16,384 shards, 16 GiB of
 # records) encoded on the GPU, a store on every shard, 1000 registered seats, requests with
 # uniform index and seat through the continuous-batching loop, driven natively: a closed
 # loop to saturation, then Poisson arrivals at fractions of the saturation rate.
+# ------------------------------------------------------------------------------------
+# OnePacking (the Galois-automorphism tree responder) over the served-batch database:
+# 2^20 records of 512 B (512 shards, gamma 256), batches of 152 seeded queries (one per SM)
+# through respond_one_packing_batch with host buffers. The Galois keys are uniform words:
+# the tree's work does not depend on their values.
+TREE_METRIC = "OnePacking respond queries/s (batch 152, d2048, 512 B records, 2^20 records)"
+
+
+def run_tree(args, rank, world):
+    import torch
+
+    from __graft_entry__ import _package
+    pkg = _package()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    ctx = pkg.Context(local)
+    g = torch.Generator(device="cuda")
+    g.manual_seed(1 + rank)
+    rng = np.random.default_rng(2000 + rank)
+    log_n = N_RING.bit_length() - 1
+    keys = rand_words(rng, (log_n, 3, 2, N_RING))
+    crs = pkg.ServerCrs(pkg.InspireParams.d2048(), rng.integers(0, 256, 32, dtype=np.uint8).tobytes(), GAMMA,
+                        galois_keys=keys)
+    cache = pkg.ServerInspiringCache.new(crs, ctx=ctx)
+    db = pkg.EncodedDatabase(cache, args.shards)
+    for s in range(args.shards):
+        cols = torch.randint(0, 1 << 16, (GAMMA, N_RING), generator=g, device="cuda", dtype=torch.int64)
+        torch.cuda.current_stream().synchronize()
+        db.set_shard_device(s, cols.data_ptr())
+    B = 152
+    total = args.warmup + args.steps
+    batches = [[pkg.SeededBatchQuery(int(rng.integers(0, args.shards)), rng.bytes(32), rand_words(rng, N_RING))
+                for _ in range(B)] for _ in range(total)]
+    for i in range(args.warmup):
+        pkg.respond_one_packing_batch(crs, db, batches[i])
+    launches0 = ctx.launch_count
+    barrier(world)
+    with ClockSampler(local) as clk:
+        torch.cuda.profiler.start()
+        t0 = time.perf_counter()
+        for i in range(args.warmup, total):
+            pkg.respond_one_packing_batch(crs, db, batches[i])
+        el = max_over_ranks(time.perf_counter() - t0, world)
+        torch.cuda.profiler.stop()
+    value = world * B * args.steps / el
+    return {
+        "metric": TREE_METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u64 (exact mod q = 2^60-2^14+1)",
+        "data": "synthetic: uniform 16-bit column words, uniform query words and Galois-key words",
+        "config": {"workload": "d2048 OnePacking, 512-byte records x 2^20 (512 shards, gamma 256), batch 152, "
+                               "unswitched", "shards": args.shards, "batch": B},
+        "e2e": {"value": value, "unit": "queries/s", "h2d_bytes_per_step": B * (32 + N_RING * 8 + 4),
+                "d2h_bytes_per_step": B * 2 * N_RING * 8,
+                "note": "host buffers in and out: one respond_one_packing_batch call per step"},
+        "gpu_launches": int(ctx.launch_count - launches0), "clocks": clk.summary(),
+    }
+
+
 # ------------------------------------------------------------------------------------
 # Mixed databases: 32 B x 2^22 (gamma 16, 2048 shards), 512 B x 2^20 (gamma 256, 512
 # shards), 2048 B x 2^18 (gamma 1024, 128 shards), each under the exact and the approximate
@@ -897,23 +957,28 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=None,
-                    help="timed steps (default: 300 for config 2 and 100 for config 3, a timed region of about "
+                    help="timed steps (default: 300 for the served batch and 100 for the special_modulus batch, a "
+                         "timed region of about "
                          "half a second that the 50 ms clock sampler sees; 20 for the reference arm)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--lanes", type=int, default=3,
                     help="streams consecutive batches rotate over in the device-resident timed region")
-    ap.add_argument("--config", type=int, default=2, choices=[2, 3, 4, 5],
-                    help="2: served InspiRING batch (the headline); 3: special_modulus batch; "
-                         "4: mixed databases and batch sizes; 5: serving sweep over 16,384 shards and 1000 seats")
-    ap.add_argument("--requests", type=int, default=16384, help="trace length of the serving sweep (config 5)")
+    ap.add_argument("--workload", default="served-batch",
+                    choices=["served-batch", "special-modulus", "mixed", "serving-sweep", "one-packing"],
+                    help="served-batch: the InspiRING batch of 64 over 2^20 records (the headline); special-modulus: "
+                         "the special_modulus batch of 256; mixed: six parameter sets and batch sizes 1-512; "
+                         "serving-sweep: the serving loop over 16,384 shards and 1000 seats; one-packing: the "
+                         "tree responder, batches of 152")
+    ap.add_argument("--requests", type=int, default=16384, help="trace length of the serving sweep")
     ap.add_argument("--shards", type=int, default=NUM_SHARDS,
                     help="shards in the database (smaller values only for profiling captures)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.steps is None:
-        args.steps = 20 if args.impl == "reference" else {2: 300, 3: 100, 4: 60, 5: 0}[args.config]
+        args.steps = 20 if args.impl == "reference" else {"served-batch": 300, "special-modulus": 100, "mixed": 60,
+                                                          "serving-sweep": 0, "one-packing": 20}[args.workload]
     rank, world = dist_setup(args.gpus)
     if args.impl == "reference":
         if rank != 0:
@@ -926,17 +991,22 @@ def main():
                 "e2e": {"value": cb["value"], "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
-    if args.config == 4:
+    if args.workload == "one-packing":
+        line = run_tree(args, rank, world)
+        if rank == 0:
+            print(json.dumps(line))
+        return
+    if args.workload == "mixed":
         line = run_cfg4(args, rank, world)
         if rank == 0:
             print(json.dumps(line))
         return
-    if args.config == 5:
+    if args.workload == "serving-sweep":
         line = run_cfg5(args, rank, world)
         if rank == 0:
             print(json.dumps(line))
         return
-    if args.config == 3:
+    if args.workload == "special-modulus":
         line = run_sm(args, rank, world)
         if rank == 0:
             if not args.no_cpu_baseline:
