@@ -298,6 +298,31 @@ int ig_respond_one_packing_batch(ig_ctx* ctx, uint64_t db, uint32_t count, const
                                  const uint8_t* seeds, const uint64_t* as, const uint64_t* bs,
                                  uint64_t mod_switch_target, uint64_t* a_out, uint64_t* b_out);
 
+/* ---- client side (load generation and decoding) --------------------------------------
+ * A ClientSession's query batch and record extraction on the GPU, for driving and checking
+ * the server at saturation. ig_client_create takes the session's RLWE secret (ring_dim
+ * words mod q, coefficient form) and its sampler's sigma. */
+int ig_client_create(ig_ctx* ctx, uint64_t crs, const uint64_t* secret, double sigma, uint64_t* client_out);
+int ig_client_destroy(ig_ctx* ctx, uint64_t client);
+/* ClientSession::query_batch (session.rs:377-434): query i is the seeded RGSW row of index
+ * indices[i] (SeededRgswCiphertext::encrypt_with_rng, rgsw/types.rs:345-388, one row of
+ * power 1), its `a` seed seeds[32 i..] (the reference draws them from the caller's rng), its
+ * error the next ring_dim samples of the session's Gaussian sampler (math/gaussian.rs:210-224)
+ * in query order. The sampler is its ChaCha20 key sampler_key and its position
+ * *sampler_word (32-bit keystream words consumed so far), advanced past the batch's draws.
+ * Writes shard_ids_out[i] and b_out[ring_dim i..] (coefficient form); the queries' `a`
+ * expand from the seeds on the server. */
+int ig_client_query_batch(ig_ctx* ctx, uint64_t client, uint32_t count, const uint64_t* indices,
+                          const uint8_t* seeds, const uint8_t* sampler_key, uint64_t* sampler_word,
+                          uint32_t* shard_ids_out, uint64_t* b_out);
+/* extract_inspiring / extract_packed / extract_inspiring_mod_switched (extract.rs:184-263,
+ * mod_switch.rs:573-640) for `count` packed responses (a, b: count x ring_dim words over
+ * `modulus`, 0 meaning q): decrypt, round by modulus / p, times d^-1 mod p when tree != 0,
+ * then the record bytes (records_out: count x entry_size). A switched modulus m is served
+ * when ring_dim * m * max|s| < q/2 (the 36-bit target is). */
+int ig_client_extract_batch(ig_ctx* ctx, uint64_t client, uint32_t count, const uint64_t* a, const uint64_t* b,
+                            uint64_t modulus, uint32_t entry_size, int tree, uint8_t* records_out);
+
 /* ---- wire ------------------------------------------------------------------------------
  * ServerResponse bincode bytes of a packed response (respond.rs:111-176, tight codec
  * poly.rs:166-225): Packed{a, b_prefix (first `retained` b coefficients), retained}, no

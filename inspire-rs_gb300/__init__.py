@@ -33,7 +33,7 @@ __all__ = [
     "respond", "respond_seeded", "respond_nopacking_batch",
     "check_mod_switch_noise_budget", "ClientQuery", "Context", "DEFAULT_Q",
     "MOD_SWITCH_TARGET_36BIT", "MOD_SWITCH_TARGET_45BIT", "library_path", "special_modulus", "ServingLoop",
-    "respond_one_packing", "respond_seeded_packed", "respond_one_packing_batch",
+    "respond_one_packing", "respond_seeded_packed", "respond_one_packing_batch", "DeviceClient",
     "ServeTicket",
 ]
 
@@ -108,6 +108,10 @@ def _load():
         "ig_response_encode_device": (I, [P, U32, P, P, U32, U32, U64, P, ctypes.POINTER(ctypes.c_size_t), P]),
         "ig_response_encode_tree": (I, [P, P, U32, U32, U64, P, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
         "ig_crs_set_galois_keys": (I, [P, U64, U32, U32, P]),
+        "ig_client_create": (I, [P, U64, P, ctypes.c_double, pu64]),
+        "ig_client_destroy": (I, [P, U64]),
+        "ig_client_query_batch": (I, [P, U64, U32, P, P, P, pu64, P, P]),
+        "ig_client_extract_batch": (I, [P, U64, U32, P, P, U64, U32, I, P]),
         "ig_respond_one_packing_batch": (I, [P, U64, U32, P, P, P, P, U64, P, P]),
         "ig_response_encode_rims": (I, [P, P, U32, U32, U32, P, U32, U64, P, ctypes.c_size_t,
                                         ctypes.POINTER(ctypes.c_size_t)]),
@@ -871,6 +875,60 @@ def respond_seeded(crs: ServerCrs, encoded_db: EncodedDatabase, query: SeededBat
 def respond_nopacking_batch(crs: ServerCrs, encoded_db: EncodedDatabase, queries) -> list:
     """NoPacking responses of many queries in one launch sequence (seeded or unseeded)."""
     return _nopacking(crs, encoded_db, list(queries))
+
+
+class DeviceClient:
+    """A ClientSession's query batch and record extraction on the GPU (session.rs:377-434,
+    extract.rs:184-263), for driving the server with real encrypted queries at saturation
+    and checking every answer. `secret` is the session's RLWE secret (ring_dim words mod q)."""
+
+    def __init__(self, cache: "ServerInspiringCache", secret, sigma: float = 6.4):
+        self.ctx, self.crs = cache.ctx, cache.crs
+        s = _u64(secret, (self.crs.params.ring_dim,))
+        h = ctypes.c_uint64()
+        self.ctx.check(self.ctx._lib.ig_client_create(self.ctx.h, cache.h, _ptr(s), float(sigma), ctypes.byref(h)))
+        self.h = h.value
+
+    def close(self):
+        if self.h:
+            self.ctx._lib.ig_client_destroy(self.ctx.h, self.h)
+            self.h = None
+
+    def query_batch(self, indices, seeds, sampler_key: bytes, sampler_word: int):
+        """Seeded queries for global `indices` with `a` seeds (32 bytes each) and errors from the
+        sampler (ChaCha20 key, 32-bit words consumed). Returns (SeededBatchQuery list, the
+        sampler's new word position)."""
+        n = self.crs.params.ring_dim
+        idx = np.ascontiguousarray(indices, dtype=np.uint64)
+        count = len(idx)
+        sd = np.frombuffer(b"".join(bytes(x) for x in seeds), dtype=np.uint8).copy()
+        if len(sd) != 32 * count or len(sampler_key) != 32:
+            raise PirError("query_batch needs one 32-byte seed per index and a 32-byte sampler key")
+        key = np.frombuffer(bytes(sampler_key), dtype=np.uint8).copy()
+        pos = ctypes.c_uint64(int(sampler_word))
+        sids = np.zeros(count, dtype=np.uint32)
+        b = np.zeros((count, n), dtype=np.uint64)
+        self.ctx.check(self.ctx._lib.ig_client_query_batch(self.ctx.h, self.h, count, _ptr(idx), _ptr(sd), _ptr(key),
+                                                           ctypes.byref(pos), _ptr(sids), _ptr(b)))
+        qs = [SeededBatchQuery(int(sids[i]), bytes(seeds[i]), b[i]) for i in range(count)]
+        return qs, pos.value
+
+    def extract_batch(self, responses, entry_size: int):
+        """Records of packed responses (InspiRING or tree, unswitched or switched)."""
+        n = self.crs.params.ring_dim
+        count = len(responses)
+        if count == 0:
+            return []
+        modulus = responses[0].modulus
+        tree = responses[0].packing_mode == "Tree"
+        if any(r.modulus != modulus or (r.packing_mode == "Tree") != tree for r in responses):
+            raise PirError("extract_batch takes responses of one modulus and one packing mode")
+        a = np.stack([_u64(r.a, (n,)) for r in responses])
+        b = np.stack([_u64(r.b, (n,)) for r in responses])
+        out = np.zeros((count, entry_size), dtype=np.uint8)
+        self.ctx.check(self.ctx._lib.ig_client_extract_batch(self.ctx.h, self.h, count, _ptr(a), _ptr(b),
+                                                             int(modulus), int(entry_size), int(tree), _ptr(out)))
+        return [out[i].tobytes() for i in range(count)]
 
 
 def _one_packing(crs, encoded_db, queries, mod_switch_target=0):

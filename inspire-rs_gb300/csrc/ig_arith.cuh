@@ -24,6 +24,7 @@ namespace ig {
 typedef uint64_t u64;
 typedef uint32_t u32;
 typedef unsigned __int128 u128;
+typedef int64_t i64;
 
 static constexpr u64 Q = 1152921504606830593ULL;  // 2^60 - 2^14 + 1
 // -q^-1 mod 2^64

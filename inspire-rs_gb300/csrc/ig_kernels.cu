@@ -1609,6 +1609,243 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
 }
 
 // ------------------------------------------------------------------------------------
+// Client side (ClientSession::query_batch, session.rs:377-434; extract_inspiring and
+// extract_packed, extract.rs:184-263): queries and record decoding for many queries at once.
+//
+// The query error comes from the session's Gaussian sampler (math/gaussian.rs:210-224),
+// one stream shared by the whole batch in order: each sample draws x uniform in
+// [-tailcut, tailcut] (rand's widening-multiply rejection: a 64-bit word whose low product
+// half exceeds the zone is skipped) and then u uniform in [0, 1) from one 64-bit word, and
+// keeps x when threshold(x) > bits(u). Read as a machine over the stream's 64-bit words it
+// has two states, A (next word is an x candidate) and B (next word is the u of an accepted
+// x), so the stream is parsed in parallel: each thread composes the state maps of a segment
+// of words, a scan gives every segment its start state, and a second walk counts and places
+// the samples.
+
+// Word i of the stream: u32 words base + 2i, base + 2i + 1 of the keystream buffer.
+__device__ __forceinline__ u64 ks_word(const u32* ks, u64 base, u64 i) {
+  return (u64)ks[base + 2 * i] | ((u64)ks[base + 2 * i + 1] << 32);
+}
+// x of candidate word w, or false when rand rejects it.
+__device__ __forceinline__ bool gauss_x(const GaussDev& g, u64 w, i64& x) {
+  const u128 m = (u128)w * g.range;
+  if ((u64)m > g.zone) return false;
+  x = -g.tailcut + (i64)(u64)(m >> 64);
+  return true;
+}
+// rand's f64 in [0, 1) from w (52 high bits as the mantissa of [1, 2), minus 1, exact), and
+// the acceptance of x: threshold bits above the bits of u.
+__device__ __forceinline__ bool gauss_keep(const GaussDev& g, i64 x, u64 w) {
+  const double v = __longlong_as_double((long long)((w >> 12) | 0x3FF0000000000000ULL)) - 1.0;
+  return g.accept[x + g.tailcut] > (u64)__double_as_longlong(v);
+}
+
+// The sampler's keystream: ChaCha20 blocks block0 .. block0 + nblocks - 1 of stream 0.
+__global__ void k_keystream(const u32* key, u64 block0, u64 nblocks, u32* ks) {
+  const u64 b = (u64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nblocks) return;
+  u32 k[8], out[16];
+#pragma unroll
+  for (int i = 0; i < 8; i++) k[i] = key[i];
+  chacha20_block(k, block0 + b, 0, out);
+#pragma unroll
+  for (int i = 0; i < 16; i++) ks[b * 16 + i] = out[i];
+}
+
+// Segment t (words [t seg, t seg + seg) of W): bit 0 = end state from A, bit 1 = from B.
+__global__ void k_gauss_maps(GaussDev g, const u32* ks, u64 base, u64 W, u32 seg, uint8_t* maps, u64 T) {
+  const u64 t = (u64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= T) return;
+  u32 sa = 0, sb = 1;
+  const u64 e = min(W, (t + 1) * seg);
+  for (u64 i = t * seg; i < e; i++) {
+    i64 x;
+    const u32 next_a = gauss_x(g, ks_word(ks, base, i), x) ? 1u : 0u;
+    sa = sa ? 0u : next_a;
+    sb = sb ? 0u : next_a;
+  }
+  maps[t] = (uint8_t)(sa | (sb << 1));
+}
+
+// One block: exclusive scan of T segment maps from state A (start states), or, with
+// counts, exclusive prefix sums of T counts (offsets) and their total.
+__global__ void __launch_bounds__(1024) k_gauss_scan(const uint8_t* maps, uint8_t* starts, const u32* counts,
+                                                     u64* offsets, u64* total, u64 T) {
+  __shared__ u64 part[1024];
+  const u64 per = (T + 1023) / 1024;
+  const u64 b = threadIdx.x * per, e = min(T, b + per);
+  if (maps) {
+    // Composite map of this thread's range, as the pair (image of A, image of B).
+    u32 fa = 0, fb = 1;
+    for (u64 i = b; i < e; i++) {
+      const u32 m = maps[i];
+      fa = (m >> fa) & 1;
+      fb = (m >> fb) & 1;
+    }
+    part[threadIdx.x] = fa | (fb << 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      u32 st = 0;
+      for (int c = 0; c < 1024; c++) {
+        const u32 m = (u32)part[c];
+        part[c] = st;
+        st = (m >> st) & 1;
+      }
+    }
+    __syncthreads();
+    u32 st = (u32)part[threadIdx.x];
+    for (u64 i = b; i < e; i++) {
+      starts[i] = (uint8_t)st;
+      st = (maps[i] >> st) & 1;
+    }
+  } else {
+    u64 sum = 0;
+    for (u64 i = b; i < e; i++) sum += counts[i];
+    part[threadIdx.x] = sum;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      u64 acc = 0;
+      for (int c = 0; c < 1024; c++) {
+        const u64 v = part[c];
+        part[c] = acc;
+        acc += v;
+      }
+      *total = acc;
+    }
+    __syncthreads();
+    u64 acc = part[threadIdx.x];
+    for (u64 i = b; i < e; i++) {
+      offsets[i] = acc;
+      acc += counts[i];
+    }
+  }
+}
+
+// Walk of segment t from its start state: counts its samples (offsets null), or writes
+// sample k to out[k] for k < S and, at the S-th, the word index after it to *end.
+__global__ void k_gauss_walk(GaussDev g, const u32* ks, u64 base, u64 W, u32 seg, const uint8_t* starts, u64 T,
+                             u32* counts, const u64* offsets, u64 S, i64* out, u64* end) {
+  const u64 t = (u64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= T) return;
+  u64 i = t * seg;
+  const u64 e = min(W, i + seg);
+  u32 st = starts[t];
+  i64 x = 0;
+  if (st == 1) gauss_x(g, ks_word(ks, base, i - 1), x);  // the pending x is the previous word's
+  u64 k = offsets ? offsets[t] : 0;
+  u32 n = 0;
+  for (; i < e; i++) {
+    const u64 w = ks_word(ks, base, i);
+    if (st == 0) {
+      st = gauss_x(g, w, x) ? 1u : 0u;
+    } else {
+      st = 0;
+      if (gauss_keep(g, x, w)) {
+        if (offsets) {
+          if (k < S) out[k] = x;
+          if (k == S - 1) *end = i + 1;
+          k++;
+        } else {
+          n++;
+        }
+      }
+    }
+  }
+  if (!offsets) counts[t] = n;
+}
+
+// One CTA per query: b = Delta X^-local - a s + e (SeededRgswCiphertext::encrypt_with_rng,
+// rgsw/types.rs:345-388, one gadget row of power 1), a from the query's seed.
+template <int LOGN>
+__global__ void __launch_bounds__((1 << LOGN) / 4) k_client_query(CrsDev c, const QueryDev* queries,
+                                                                  const u64* s_R, const u32* locals,
+                                                                  const i64* samples, u64 delta, u64* b_out,
+                                                                  u32* status) {
+  constexpr int N = 1 << LOGN, NT = N / 4;
+  extern __shared__ __align__(16) u64 sm[];
+  u64* x = sm;
+  u64* tw = sm + N;
+  u64* twp = tw + N;
+  const u32 qi = blockIdx.x;
+  const QueryDev qd = queries[qi];
+  for (int k = threadIdx.x; k < N; k += NT) {
+    tw[k] = c.tw[k];
+    twp[k] = c.twp[k];
+  }
+  expand_a<N, NT>(qd, x, status, qi, 0);  // ends with a barrier
+  {
+    u64* const bufs[1] = {x};
+    ntt_fwd_r4<LOGN, NT, 1>(bufs, tw, twp);
+  }
+  for (int k = threadIdx.x; k < N; k += NT) x[k] = mont(csub(csub2(x[k])), s_R[k]);
+  __syncthreads();
+  {
+    u64* const bufs[1] = {x};
+    ntt_inv_r4<LOGN, NT, 1>(bufs, tw, twp);
+  }
+  const u32 local = locals[qi];
+  const int pos = local == 0 ? 0 : N - (int)local;
+  const u64 mono = local == 0 ? delta : Q - delta;  // Delta X^-local (encode_db.rs:43-70)
+  for (int k = threadIdx.x; k < N; k += NT) {
+    const u64 as = shoup(x[k], c.ninv, c.ninvp);
+    const i64 ev = samples[(size_t)qi * N + k];
+    u64 b = addq(negq(as), ev < 0 ? Q - (u64)(-ev) : (u64)ev);
+    if (k == pos) b = addq(b, mono);
+    b_out[(size_t)qi * N + k] = b;
+  }
+}
+
+// One CTA per response: (a s + b) mod the response modulus, rounded by delta and taken mod p
+// (PlaintextRounding, rlwe/enc.rs:14-44); times d^-1 mod p for a tree response; the first
+// ceil(entry/2) values are the record's 16-bit columns (encode_db.rs:152-168). The product
+// is taken mod q: a switched modulus m keeps |a s| below n m max|s| < q/2, so the centred
+// residue is the integer product (the host checks the bound).
+template <int LOGN>
+__global__ void __launch_bounds__((1 << LOGN) / 4) k_client_extract(CrsDev c, const u64* s_R, const u64* a,
+                                                                    const u64* b, u64 modulus, u64 delta, u64 p,
+                                                                    u64 dinv, u32 entry_size, uint8_t* out) {
+  constexpr int N = 1 << LOGN, NT = N / 4;
+  extern __shared__ __align__(16) u64 sm[];
+  u64* x = sm;
+  u64* tw = sm + N;
+  u64* twp = tw + N;
+  const u32 qi = blockIdx.x;
+  for (int k = threadIdx.x; k < N; k += NT) {
+    tw[k] = c.tw[k];
+    twp[k] = c.twp[k];
+    x[k] = a[(size_t)qi * N + k];
+  }
+  __syncthreads();
+  {
+    u64* const bufs[1] = {x};
+    ntt_fwd_r4<LOGN, NT, 1>(bufs, tw, twp);
+  }
+  for (int k = threadIdx.x; k < N; k += NT) x[k] = mont(csub(csub2(x[k])), s_R[k]);
+  __syncthreads();
+  {
+    u64* const bufs[1] = {x};
+    ntt_inv_r4<LOGN, NT, 1>(bufs, tw, twp);
+  }
+  const u32 cols = (entry_size + 1) / 2;
+  for (u32 k = threadIdx.x; k < cols && k < (u32)N; k += NT) {
+    u64 as = shoup(x[k], c.ninv, c.ninvp);
+    if (modulus != Q) {
+      const bool neg = as > (Q >> 1);
+      const u64 mag = (neg ? Q - as : as) % modulus;
+      as = neg && mag ? modulus - mag : mag;
+    }
+    const u64 bv = b[(size_t)qi * N + k];
+    u64 noisy = as + bv;
+    if (noisy >= modulus) noisy -= modulus;
+    u64 m = ((noisy + delta / 2) / delta) % p;
+    if (dinv) m = (u64)((u128)m * dinv % p);
+    uint8_t* rec = out + (size_t)qi * entry_size;
+    rec[2 * k] = (uint8_t)(m & 0xff);
+    if (2 * k + 1 < entry_size) rec[2 * k + 1] = (uint8_t)((m >> 8) & 0xff);
+  }
+}
+
+// ------------------------------------------------------------------------------------
 // Integer roofline probe: lazy forward butterflies (one Shoup product, two 64-bit adds and
 // a conditional subtraction each, the transforms' unit of work) on values held in
 // registers, eight independent chains per thread, no memory traffic. Its rate is the
@@ -1730,6 +1967,50 @@ cudaError_t nopack(const CrsDev& c, const QueryDev* queries, const ShardDev* sha
       k<<<dim3(c.gamma, nq), N / 4, smem, s>>>(c, queries, shards, AB_R, out);
     }
     k_nopack_sum<<<dim3((2 * N + 255) / 256, nq), 256, 0, s>>>(N, c.gamma, out);
+  });
+  return cudaGetLastError();
+}
+
+cudaError_t keystream(const u32* key, u64 block0, u64 nblocks, u32* ks, cudaStream_t s) {
+  if (nblocks == 0) return cudaSuccess;
+  k_keystream<<<(unsigned)((nblocks + 255) / 256), 256, 0, s>>>(key, block0, nblocks, ks);
+  return cudaGetLastError();
+}
+
+cudaError_t gauss_parse(const GaussDev& g, const u32* ks, u64 base, u64 W, u32 seg, uint8_t* maps, uint8_t* starts,
+                        u32* counts, u64* offsets, u64* total, u64 S, i64* out, u64* end, cudaStream_t s) {
+  const u64 T = (W + seg - 1) / seg;
+  const unsigned blocks = (unsigned)((T + 255) / 256);
+  k_gauss_maps<<<blocks, 256, 0, s>>>(g, ks, base, W, seg, maps, T);
+  k_gauss_scan<<<1, 1024, 0, s>>>(maps, starts, nullptr, nullptr, nullptr, T);
+  k_gauss_walk<<<blocks, 256, 0, s>>>(g, ks, base, W, seg, starts, T, counts, nullptr, S, out, end);
+  k_gauss_scan<<<1, 1024, 0, s>>>(nullptr, nullptr, counts, offsets, total, T);
+  k_gauss_walk<<<blocks, 256, 0, s>>>(g, ks, base, W, seg, starts, T, nullptr, offsets, S, out, end);
+  return cudaGetLastError();
+}
+
+cudaError_t client_query(const CrsDev& c, const QueryDev* queries, u32 nq, const u64* s_R, const u32* locals,
+                         const i64* samples, u64 delta, u64* b_out, u32* status, cudaStream_t s) {
+  if (nq == 0) return cudaSuccess;
+  const size_t smem = 3 * (size_t)c.n * 8;
+  IG_DISPATCH_LOGN(c.logn, {
+    auto k = k_client_query<L>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k<<<nq, (1 << L) / 4, smem, s>>>(c, queries, s_R, locals, samples, delta, b_out, status);
+  });
+  return cudaGetLastError();
+}
+
+cudaError_t client_extract(const CrsDev& c, u32 count, const u64* s_R, const u64* a, const u64* b, u64 modulus,
+                           u64 delta, u64 p, u64 dinv, u32 entry_size, uint8_t* out, cudaStream_t s) {
+  if (count == 0) return cudaSuccess;
+  const size_t smem = 3 * (size_t)c.n * 8;
+  IG_DISPATCH_LOGN(c.logn, {
+    auto k = k_client_extract<L>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k<<<count, (1 << L) / 4, smem, s>>>(c, s_R, a, b, modulus, delta, p, dinv, entry_size, out);
   });
   return cudaGetLastError();
 }

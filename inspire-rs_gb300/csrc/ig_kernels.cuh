@@ -45,6 +45,14 @@ struct QueryDev {
   const u64* a;       // explicit coefficient-form `a` (unseeded query), or null
 };
 
+// The client's Gaussian sampler (math/gaussian.rs:95-224): acceptance thresholds (f64 bit
+// patterns of exp(-x^2 / 2 sigma^2), x = -tailcut .. tailcut) and rand's integer range.
+struct GaussDev {
+  const u64* accept;
+  i64 tailcut;
+  u64 range, zone;  // 2 tailcut + 1 and (range << clz(range)) - 1
+};
+
 struct ShardDev {
   const u64* columns;        // gamma x n raw column words
   const u64* sums_R;         // gamma x n step-1 sums, R-form NTT (the packing store)
@@ -108,6 +116,18 @@ cudaError_t nopack(const CrsDev& c, const QueryDev* queries, const ShardDev* sha
 // holds nq x logn x 2n words of waiting nodes. Outputs coefficient-form (a, b), switched to
 // ms_target when nonzero.
 size_t tree_smem_bytes(const CrsDev& c);
+
+// Client side: the sampler's keystream (ChaCha20 blocks of stream 0), the parallel parse of
+// W stream words from u32 offset `base` of ks into the first S samples (out) and the word
+// index after the S-th (*end; *total counts every sample in the window), the queries' b
+// and the records of responses.
+cudaError_t keystream(const u32* key, u64 block0, u64 nblocks, u32* ks, cudaStream_t s);
+cudaError_t gauss_parse(const GaussDev& g, const u32* ks, u64 base, u64 W, u32 seg, uint8_t* maps, uint8_t* starts,
+                        u32* counts, u64* offsets, u64* total, u64 S, i64* out, u64* end, cudaStream_t s);
+cudaError_t client_query(const CrsDev& c, const QueryDev* queries, u32 nq, const u64* s_R, const u32* locals,
+                         const i64* samples, u64 delta, u64* b_out, u32* status, cudaStream_t s);
+cudaError_t client_extract(const CrsDev& c, u32 count, const u64* s_R, const u64* a, const u64* b, u64 modulus,
+                           u64 delta, u64 p, u64 dinv, u32 entry_size, uint8_t* out, cudaStream_t s);
 cudaError_t tree(const CrsDev& c, const QueryDev* queries, const ShardDev* shards, u32 nq, u64 r_mod_q, u64 ms_target,
                  u64* stack, u64* a_out, u64* b_out, u32* status, cudaStream_t s);
 

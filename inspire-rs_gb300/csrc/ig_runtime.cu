@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <atomic>
 #include <cstdarg>
 #include <cstdio>
@@ -143,6 +144,18 @@ struct StoreObj {
   std::unordered_map<u64, SeatObj> seats;
 };
 
+// A client session on the device (ClientSession, session.rs): the secret's NTT in R-form
+// and the sampler's acceptance thresholds.
+struct ClientObj {
+  u64 crs = 0;
+  u64* s_R = nullptr;
+  u64* accept = nullptr;
+  GaussDev g{};
+  u64 max_abs_s = 0;  // largest |s_k| of the centred secret
+  std::vector<void*> allocs;
+  size_t bytes = 0;
+};
+
 std::atomic<u64> g_next_handle{0};  // process-global, monotonic (session.rs:715-738)
 std::atomic<u64> g_next_object{1};
 
@@ -159,6 +172,7 @@ struct ig_ctx {
   std::unordered_map<u64, CrsObj> crs;
   std::unordered_map<u64, DbObj> dbs;
   std::unordered_map<u64, StoreObj> stores;
+  std::unordered_map<u64, ClientObj> clients;
   std::unordered_map<std::string, DevBuf> scratch;
   u64* zero_key = nullptr;
   size_t zero_key_words = 0;
@@ -573,6 +587,8 @@ void ig_ctx_destroy(ig_ctx* c) {
   }
   for (auto& kv : c->stores)
     for (auto& s : kv.second.seats) cudaFree(s.second.yR);
+  for (auto& kv : c->clients)
+    for (void* p : kv.second.allocs) cudaFree(p);
   for (auto& kv : c->scratch) cudaFree(kv.second.p);
   for (auto& st : c->staging) {
     if (st.host) cudaFreeHost(st.host);
@@ -1341,6 +1357,214 @@ int ig_respond_nopacking_batch(ig_ctx* c, uint64_t dbh, uint32_t count, const ui
   for (u32 i = 0; i < count; i++)
     if (status[i]) return fail(c, IG_ERR_DEVICE, "query %u: respond kernel status %u", i, status[i]);
   IG_CUDA(c, cudaMemcpyAsync(out, d_out, out_words * 8, cudaMemcpyDeviceToHost, s));
+  IG_CUDA(c, cudaStreamSynchronize(s));
+  return IG_OK;
+}
+
+// ---- client side -------------------------------------------------------------------------
+int ig_client_create(ig_ctx* c, uint64_t crs, const uint64_t* secret, double sigma, uint64_t* client_out) {
+  if (!c || !secret || !client_out) return IG_ERR_ARG;
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  CrsObj* o = get_crs(c, crs);
+  if (!o) return fail(c, IG_ERR_HANDLE, "unknown CRS handle %llu", (unsigned long long)crs);
+  if (!(sigma > 0) || sigma > 1e6) return fail(c, IG_ERR_ARG, "sampler sigma %g is not served", sigma);
+  const size_t n = o->n;
+  ClientObj cl;
+  cl.crs = crs;
+  for (size_t k = 0; k < n; k++) {
+    if (secret[k] >= Q) return fail(c, IG_ERR_SHAPE, "secret coefficient %zu is not a residue mod q", k);
+    const u64 mag = secret[k] > Q / 2 ? Q - secret[k] : secret[k];
+    cl.max_abs_s = std::max(cl.max_abs_s, mag);
+  }
+  // GaussianSampler::new (math/gaussian.rs:95-117): tailcut ceil(6 sigma), thresholds the
+  // f64 bit patterns of exp(-x^2 / 2 sigma^2), a NaN as +0.0.
+  const i64 t = (i64)std::ceil(sigma * 6.0);
+  std::vector<u64> table;
+  const double two_s2 = 2.0 * sigma * sigma;
+  for (i64 x = -t; x <= t; x++) {
+    double prob = std::exp(-(double)(x * x) / two_s2);
+    if (std::isnan(prob)) prob = 0.0;
+    u64 bits;
+    memcpy(&bits, &prob, 8);
+    table.push_back(bits);
+  }
+  void *raw = nullptr, *sR = nullptr, *acc = nullptr;
+  int rc = scratch(c, "client_raw", n * 8, &raw);
+  if (!rc) rc = dalloc(c, &sR, n * 8, &cl.bytes);
+  if (!rc) {
+    cl.allocs.push_back(sR);
+    rc = dalloc(c, &acc, table.size() * 8, &cl.bytes);
+  }
+  if (rc) {
+    for (void* p2 : cl.allocs) cudaFree(p2);
+    c->obj_bytes -= cl.bytes;
+    return rc;
+  }
+  cl.allocs.push_back(acc);
+  IG_CUDA(c, cudaMemcpyAsync(raw, secret, n * 8, cudaMemcpyHostToDevice, c->stream));
+  IG_CUDA(c, cudaMemcpyAsync(acc, table.data(), table.size() * 8, cudaMemcpyHostToDevice, c->stream));
+  IG_CUDA(c, igk::ntt_rows(o->dev, (const u64*)raw, (u64*)sR, 1, R_MOD_Q, shoup_companion(R_MOD_Q), c->stream));
+  IG_CUDA(c, cudaStreamSynchronize(c->stream));
+  cl.s_R = (u64*)sR;
+  cl.accept = (u64*)acc;
+  cl.g.accept = cl.accept;
+  cl.g.tailcut = t;
+  cl.g.range = (u64)(2 * t + 1);
+  cl.g.zone = (cl.g.range << __builtin_clzll(cl.g.range)) - 1;
+  const u64 h = g_next_object++;
+  c->clients[h] = cl;
+  *client_out = h;
+  return IG_OK;
+}
+
+int ig_client_destroy(ig_ctx* c, uint64_t client) {
+  if (!c) return IG_ERR_ARG;
+  std::lock_guard<std::mutex> lk(c->mu);
+  auto it = c->clients.find(client);
+  if (it == c->clients.end()) return fail(c, IG_ERR_HANDLE, "unknown client handle %llu", (unsigned long long)client);
+  cudaStreamSynchronize(c->stream);
+  for (void* p : it->second.allocs) cudaFree(p);
+  c->obj_bytes -= it->second.bytes;
+  c->clients.erase(it);
+  return IG_OK;
+}
+
+int ig_client_query_batch(ig_ctx* c, uint64_t client, uint32_t count, const uint64_t* indices, const uint8_t* seeds,
+                          const uint8_t* sampler_key, uint64_t* sampler_word, uint32_t* shard_ids_out,
+                          uint64_t* b_out) {
+  if (!c) return IG_ERR_ARG;
+  if (count == 0 || !indices || !seeds || !sampler_key || !sampler_word || !shard_ids_out || !b_out)
+    return fail(c, IG_ERR_ARG, "query_batch: empty batch or null buffer");
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  auto it = c->clients.find(client);
+  if (it == c->clients.end()) return fail(c, IG_ERR_HANDLE, "unknown client handle %llu", (unsigned long long)client);
+  ClientObj& cl = it->second;
+  CrsObj* o = get_crs(c, cl.crs);
+  if (!o) return fail(c, IG_ERR_HANDLE, "the client's CRS is gone");
+  const size_t n = o->n;
+  const u64 S = (u64)count * n;
+  const u64 P = *sampler_word;
+  cudaStream_t s = c->stream;
+  u32 key[8];
+  for (int i = 0; i < 8; i++) memcpy(&key[i], sampler_key + 4 * i, 4);
+  void *d_key, *d_samples, *d_total, *d_end;
+  int rc;
+  if ((rc = scratch(c, "cl_key", 32, &d_key)) || (rc = scratch(c, "cl_samples", S * 8, &d_samples)) ||
+      (rc = scratch(c, "cl_total", 8, &d_total)) || (rc = scratch(c, "cl_end", 8, &d_end)))
+    return rc;
+  if ((rc = stage_h2d(c, d_key, key, 32))) return rc;
+  // About 13 stream words per sample at sigma 6.4 (an x candidate is kept with probability
+  // 0.62, a candidate x with about 0.2); the window doubles until it holds S samples.
+  constexpr u32 SEG = 16;
+  u64 W = 14 * S + 4096, total = 0, end = 0;
+  for (int tries = 0; tries < 8 && total < S; tries++, W *= 2) {
+    const u64 block0 = P / 16, base = P - 16 * block0;
+    const u64 nblocks = (base + 2 * W + 2 + 15) / 16;
+    const u64 T = (W + SEG - 1) / SEG;
+    void *d_ks, *d_maps, *d_starts, *d_counts, *d_offsets;
+    if ((rc = scratch(c, "cl_ks", nblocks * 64, &d_ks)) || (rc = scratch(c, "cl_maps", T, &d_maps)) ||
+        (rc = scratch(c, "cl_starts", T, &d_starts)) || (rc = scratch(c, "cl_counts", T * 4, &d_counts)) ||
+        (rc = scratch(c, "cl_offsets", T * 8, &d_offsets)))
+      return rc;
+    IG_CUDA(c, igk::keystream((const u32*)d_key, block0, nblocks, (u32*)d_ks, s));
+    IG_CUDA(c, igk::gauss_parse(cl.g, (const u32*)d_ks, base, W, SEG, (uint8_t*)d_maps, (uint8_t*)d_starts,
+                                (u32*)d_counts, (u64*)d_offsets, (u64*)d_total, S, (i64*)d_samples, (u64*)d_end, s));
+    c->launches += 6;
+    IG_CUDA(c, cudaMemcpyAsync(&total, d_total, 8, cudaMemcpyDeviceToHost, s));
+    IG_CUDA(c, cudaMemcpyAsync(&end, d_end, 8, cudaMemcpyDeviceToHost, s));
+    IG_CUDA(c, cudaStreamSynchronize(s));
+  }
+  if (total < S) return fail(c, IG_ERR_DEVICE, "query_batch: the sampler stream gave %llu of %llu samples",
+                             (unsigned long long)total, (unsigned long long)S);
+  // ShardConfig::index_to_shard (params.rs:1344-1385): ring_dim entries a shard.
+  std::vector<u32> locals(count);
+  for (u32 i = 0; i < count; i++) {
+    shard_ids_out[i] = (u32)(indices[i] / n);
+    locals[i] = (u32)(indices[i] % n);
+  }
+  void *d_q, *d_seeds, *d_locals, *d_b, *d_status;
+  if ((rc = scratch(c, "cl_queries", count * sizeof(QueryDev), &d_q)) ||
+      (rc = scratch(c, "cl_seeds", (size_t)count * 32, &d_seeds)) ||
+      (rc = scratch(c, "cl_locals", (size_t)count * 4, &d_locals)) ||
+      (rc = scratch(c, "cl_b", (size_t)count * n * 8, &d_b)) || (rc = scratch(c, "cl_status", count * 4, &d_status)))
+    return rc;
+  std::vector<QueryDev> qs(count);
+  for (u32 i = 0; i < count; i++) {
+    qs[i] = QueryDev{};
+    qs[i].seed = (const u32*)((const uint8_t*)d_seeds + (size_t)i * 32);
+  }
+  if ((rc = stage_h2d(c, d_q, qs.data(), count * sizeof(QueryDev))) ||
+      (rc = stage_h2d(c, d_seeds, seeds, (size_t)count * 32)) ||
+      (rc = stage_h2d(c, d_locals, locals.data(), (size_t)count * 4)))
+    return rc;
+  IG_CUDA(c, cudaMemsetAsync(d_status, 0, count * 4, s));
+  IG_CUDA(c, igk::client_query(o->dev, (const QueryDev*)d_q, count, cl.s_R, (const u32*)d_locals,
+                               (const i64*)d_samples, Q / o->p, (u64*)d_b, (u32*)d_status, s));
+  c->launches++;
+  std::vector<u32> status(count);
+  IG_CUDA(c, cudaMemcpyAsync(status.data(), d_status, count * 4, cudaMemcpyDeviceToHost, s));
+  IG_CUDA(c, cudaMemcpyAsync(b_out, d_b, (size_t)count * n * 8, cudaMemcpyDeviceToHost, s));
+  IG_CUDA(c, cudaStreamSynchronize(s));
+  for (u32 i = 0; i < count; i++)
+    if (status[i]) return fail(c, IG_ERR_DEVICE, "query %u: query kernel status %u", i, status[i]);
+  *sampler_word = P + 2 * end;
+  return IG_OK;
+}
+
+int ig_client_extract_batch(ig_ctx* c, uint64_t client, uint32_t count, const uint64_t* a, const uint64_t* b,
+                            uint64_t modulus, uint32_t entry_size, int tree, uint8_t* records_out) {
+  if (!c) return IG_ERR_ARG;
+  if (count == 0 || !a || !b || !records_out || entry_size == 0)
+    return fail(c, IG_ERR_ARG, "extract: empty batch, zero entry size or null buffer");
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  auto it = c->clients.find(client);
+  if (it == c->clients.end()) return fail(c, IG_ERR_HANDLE, "unknown client handle %llu", (unsigned long long)client);
+  ClientObj& cl = it->second;
+  CrsObj* o = get_crs(c, cl.crs);
+  if (!o) return fail(c, IG_ERR_HANDLE, "the client's CRS is gone");
+  const size_t n = o->n;
+  if (modulus == 0) modulus = Q;
+  if (modulus > Q || modulus < o->p)
+    return fail(c, IG_ERR_ARG, "response modulus %llu outside [p, q]", (unsigned long long)modulus);
+  if (modulus != Q && (u128)n * modulus * cl.max_abs_s >= (u128)(Q / 2))
+    return fail(c, IG_ERR_UNSUPPORTED,
+                "extract over modulus %llu is not served: the secret's product could wrap q (n * m * max|s| >= q/2)",
+                (unsigned long long)modulus);
+  if ((entry_size + 1) / 2 > n) return fail(c, IG_ERR_ARG, "entry of %u bytes needs more than ring_dim columns", entry_size);
+  const u64 delta = modulus / o->p;
+  if (delta == 0) return fail(c, IG_ERR_ARG, "delta = modulus / p = 0; cannot decrypt");
+  u64 dinv = 0;
+  if (tree) {
+    // extract_packed (extract.rs:184-226): d^-1 mod p, refused when gcd(d, p) != 1.
+    u64 inv = 0;
+    for (u64 x = 1; x < o->p; x++)
+      if ((u128)x * (n % o->p) % o->p == 1) {
+        inv = x;
+        break;
+      }
+    if (!inv) return fail(c, IG_ERR_ARG, "degree %zu is not invertible mod p = %llu", n, (unsigned long long)o->p);
+    dinv = inv;
+  }
+  const size_t words = (size_t)count * n;
+  for (size_t i = 0; i < words; i++)
+    if (a[i] >= modulus || b[i] >= modulus)
+      return fail(c, IG_ERR_SHAPE, "response %zu coefficient is not canonical for modulus %llu", i / n,
+                  (unsigned long long)modulus);
+  void *d_a, *d_b, *d_out;
+  int rc;
+  if ((rc = scratch(c, "cx_a", words * 8, &d_a)) || (rc = scratch(c, "cx_b", words * 8, &d_b)) ||
+      (rc = scratch(c, "cx_out", (size_t)count * entry_size, &d_out)))
+    return rc;
+  cudaStream_t s = c->stream;
+  if ((rc = stage_h2d(c, d_a, a, words * 8)) || (rc = stage_h2d(c, d_b, b, words * 8))) return rc;
+  IG_CUDA(c, cudaMemsetAsync(d_out, 0, (size_t)count * entry_size, s));
+  IG_CUDA(c, igk::client_extract(o->dev, count, cl.s_R, (const u64*)d_a, (const u64*)d_b, modulus, delta, o->p, dinv,
+                                 entry_size, (uint8_t*)d_out, s));
+  c->launches++;
+  IG_CUDA(c, cudaMemcpyAsync(records_out, d_out, (size_t)count * entry_size, cudaMemcpyDeviceToHost, s));
   IG_CUDA(c, cudaStreamSynchronize(s));
   return IG_OK;
 }

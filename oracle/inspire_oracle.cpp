@@ -1323,6 +1323,13 @@ void orc_cell_galois_keys(void* cv, const uint8_t* seed, u64* out) {
 int orc_cell_decode_tree(void* cv, u64 index, const u64* a, const u64* b, uint8_t* record_out) {
   return cell_decode_tree((const Cell*)cv, index, a, b, record_out) ? 1 : 0;
 }
+// The cell's Gaussian sampler stream: its ChaCha20 key and the 32-bit words consumed so far.
+void orc_cell_sampler_state(void* cv, uint8_t* key_out, u64* word_pos) {
+  auto* c = (Cell*)cv;
+  const ChaCha20Rng& r = c->sampler.rng;
+  memcpy(key_out, r.key, 32);
+  *word_pos = r.idx >= 64 ? r.block * 16 : (r.block - 4) * 16 + r.idx;
+}
 void orc_cell_record(void* cv, u64 index, uint8_t* out) {
   auto* c = (Cell*)cv;
   memcpy(out, &c->db[index * c->entry_size], c->entry_size);

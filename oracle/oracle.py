@@ -60,6 +60,7 @@ def lib():
             "orc_respond_one_packing": (I, [V, P, P, P, P, U64, P, P]),
             "orc_cell_galois_keys": (None, [V, P, P]),
             "orc_cell_decode_tree": (I, [V, U64, P, P, P]),
+            "orc_cell_sampler_state": (None, [V, P, P]),
             "orc_cell_build": (V, [U64, U64, U64, ctypes.c_double, U64, U64, I, U64, U64, U64]),
             "orc_cell_free": (None, [V]),
             "orc_cell_info": (None, [V, P, P, P, P]),
@@ -373,6 +374,13 @@ class Cell:
         s = np.frombuffer(seed, dtype=np.uint8).copy()
         lib().orc_cell_galois_keys(self.h, _p(s), _p(out))
         return out
+
+    def sampler_state(self):
+        """(ChaCha20 key bytes, 32-bit words consumed) of the session's Gaussian sampler."""
+        key = np.zeros(32, dtype=np.uint8)
+        pos = ctypes.c_uint64()
+        lib().orc_cell_sampler_state(self.h, _p(key), ctypes.byref(pos))
+        return key.tobytes(), pos.value
 
     def decode_tree(self, index, a, b):
         """extract_packed for a tree response (extract.rs:184-226)."""
