@@ -58,6 +58,13 @@ def peaks():
         return 6800.0, "fallback"
 
 
+# DRAM bytes (read + write) of one k_scan launch of this workload, from an ncu capture of
+# the timed region (dram__bytes_read.sum + dram__bytes_write.sum, two launches averaged:
+# 67.78 MB and 68.39 MB; the command is in profiles/k_scan_batch64_d2048_g256.md). It sits
+# just under the algorithmic bytes: the scan reads each byte once.
+SCAN_TRAFFIC_BYTES = 68_084_992
+
+
 def rand_words(rng, shape):
     return rng.integers(0, Q, size=shape, dtype=np.uint64)
 
@@ -442,7 +449,9 @@ def run_gb300(args, rank, world):
                 "d2h_bytes_per_step": BATCH * 2 * N_RING * 8,
                 "callers": lanes, "call": "respond_seeded_batch (one batch of 64 per call)"},
         "roofline": {"kernel": "shard_scan", "bound": "hbm", "achieved": achieved, "peak": hbm_peak,
-                     "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": None,
+                     "unit": "GB/s", "frac": achieved / hbm_peak,
+                     "traffic": SCAN_TRAFFIC_BYTES if args.shards == NUM_SHARDS else None,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, same workload",
                      "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
                      "avg_launch_ms": scan_avg, "algorithmic_bytes_per_launch": scan_bytes},
         "roofline_dominant": {"kernel": "respond (fused recursion + online gather)", "bound": "integer issue",
