@@ -137,7 +137,9 @@ int ig_session_contains(ig_ctx* ctx, uint64_t store, uint64_t handle, int* prese
  * seed of the one RGSW row) and bs[i*ring_dim..] (its b). Outputs: the packed ciphertext's
  * a (a_out[i*ring_dim..]) and b (b_out[i*ring_dim..], the first gamma coefficients are the
  * response's b prefix). mod_switch_target != 0 applies mod_switch_response_checked
- * (mod_switch.rs:178-186) to both, e.g. 68718428161 (MOD_SWITCH_TARGET_36BIT). */
+ * (mod_switch.rs:178-186) to both, e.g. 68718428161 (MOD_SWITCH_TARGET_36BIT). A call with
+ * count 0 resolves the packing key (refused as above) and answers nothing; its buffers may
+ * be NULL. */
 int ig_respond_seeded_batch(ig_ctx* ctx, uint64_t db, uint64_t store, uint64_t handle, const uint64_t* inline_y_body,
                             uint32_t inline_rows, uint32_t inline_num_to_pack, uint32_t count,
                             const uint32_t* shard_ids, const uint8_t* seeds, const uint64_t* bs,

@@ -647,17 +647,15 @@ def _batch(crs, encoded_db, queries, packing_key, session_store, mod_switch_targ
         raise PirError("cached pack params do not match CRS params")
     n = crs.params.ring_dim
     count = len(queries)
-    if count == 0:
-        raise PirError("empty batch")
     shard_ids = np.array([q.shard_id for q in queries], dtype=np.uint32)
-    unseeded = queries[0].seed is None
+    unseeded = count > 0 and queries[0].seed is None
     if any((q.seed is None) != unseeded for q in queries):
         raise PirError("a batch is all seeded or all unseeded queries")
     if unseeded:
         seeds = np.stack([_u64(q.a, (n,)) for q in queries])
     else:
         seeds = np.frombuffer(b"".join(q.seed for q in queries), dtype=np.uint8).copy()
-    bs = np.stack([_u64(q.b, (n,)) for q in queries])
+    bs = np.stack([_u64(q.b, (n,)) for q in queries]) if count else np.zeros((0, n), dtype=np.uint64)
     a_out = np.zeros((count, n), dtype=np.uint64)
     b_out = np.zeros((count, n), dtype=np.uint64)
     if packing_key.inline is not None:

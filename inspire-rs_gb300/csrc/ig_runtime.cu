@@ -1136,8 +1136,8 @@ static int respond_host(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_t handle, c
                         const uint8_t* seeds, const uint64_t* as, const uint64_t* bs, uint64_t ms_target,
                         uint64_t* a_out, uint64_t* b_out) {
   if (!c) return IG_ERR_ARG;
-  if (count == 0 || !shard_ids || (!seeds && !as) || !bs || !a_out || !b_out)
-    return fail(c, IG_ERR_ARG, "respond: empty batch or null buffer");
+  if (count && (!shard_ids || (!seeds && !as) || !bs || !a_out || !b_out))
+    return fail(c, IG_ERR_ARG, "respond: null buffer");
   // The call's lane (lane 0 on the context stream when lanes == 1), held until its results
   // are copied out; the context lock is held only while the call validates and launches.
   igint::HostCall hc;
@@ -1155,6 +1155,9 @@ static int respond_host(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_t handle, c
   const u64* seat;
   int rc = resolve_seat(c, o, st, handle, inline_y, inline_rows, inline_ntp, &seat, k);
   if (rc) return rc;
+  // respond_seeded_batch over no queries resolves the seat and answers nothing
+  // (respond.rs:1196-1201).
+  if (count == 0) return IG_OK;
   // checked_shard (respond.rs:601-611) for every query before any work.
   std::unordered_map<u32, u32> local;
   std::vector<u32> distinct;
@@ -1284,7 +1287,7 @@ int ig_respond_seeded_batch(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_t handl
                             uint32_t inline_rows, uint32_t inline_ntp, uint32_t count, const uint32_t* shard_ids,
                             const uint8_t* seeds, const uint64_t* bs, uint64_t ms_target, uint64_t* a_out,
                             uint64_t* b_out) {
-  if (!seeds && c) return fail(c, IG_ERR_ARG, "ig_respond_seeded_batch: null seeds");
+  if (!seeds && count && c) return fail(c, IG_ERR_ARG, "ig_respond_seeded_batch: null seeds");
   return respond_host(c, dbh, st, handle, inline_y, inline_rows, inline_ntp, count, shard_ids, seeds, nullptr, bs,
                       ms_target, a_out, b_out);
 }
@@ -1292,7 +1295,7 @@ int ig_respond_seeded_batch(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_t handl
 int ig_respond_batch(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_t handle, const uint64_t* inline_y,
                      uint32_t inline_rows, uint32_t inline_ntp, uint32_t count, const uint32_t* shard_ids,
                      const uint64_t* as, const uint64_t* bs, uint64_t ms_target, uint64_t* a_out, uint64_t* b_out) {
-  if (!as && c) return fail(c, IG_ERR_ARG, "ig_respond_batch: null a");
+  if (!as && count && c) return fail(c, IG_ERR_ARG, "ig_respond_batch: null a");
   return respond_host(c, dbh, st, handle, inline_y, inline_rows, inline_ntp, count, shard_ids, nullptr, as, bs,
                       ms_target, a_out, b_out);
 }

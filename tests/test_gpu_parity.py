@@ -256,3 +256,26 @@ def test_d256_single_prime_kat_lines_on_gpu(pkg, oracle, ctx, recorded_lines, la
             wire = r.to_binary()
             line = f"RESP d256-single-l3 entry={entry} seed={seed:#x} index={idx} len={len(wire)} fnv={oracle.fnv1a(wire):#018x}"
             assert line in rec, line
+
+
+def test_one_shard_and_repeated_queries(pkg, oracle, ctx, launch_shape):
+    """Collisions: a batch whose queries all name one shard, with the same query repeated,
+    answers each query exactly as a batch of one does. An empty batch resolves its key and
+    answers nothing, as respond_seeded_batch's map over no queries does (respond.rs:1196-1201):
+    an empty list under a registered key, a refusal under an unknown handle."""
+    P = oracle.Params.d2048()
+    cell, crs, cache, db, keys = gpu_cell(pkg, oracle, P, 256, 0xC011)
+    db.precompute_packing_all()
+    store = pkg.ServerSessionStore.new()
+    h = store.register_server_side(keys, cache)
+    src = pkg.PackingKeySource.Registered(h)
+    qs = [pkg.SeededBatchQuery(*cell.next_query(P.n + (k * 37) % P.n)) for k in range(12)]
+    batch = qs + [qs[3]] * 5 + qs[:3]
+    out = pkg.respond_seeded_batch(crs, db, pkg.SeededQueryBatch(src, batch), cache, store)
+    alone = {id(q): pkg.respond_seeded_batch(crs, db, pkg.SeededQueryBatch(src, [q]), cache, store)[0].to_binary()
+             for q in qs}
+    assert [r.to_binary() for r in out] == [alone[id(q)] for q in batch]
+    assert pkg.respond_seeded_batch(crs, db, pkg.SeededQueryBatch(src, []), cache, store) == []
+    with pytest.raises(pkg.PirError, match="no entry for session_handle"):
+        pkg.respond_seeded_batch(crs, db, pkg.SeededQueryBatch(pkg.PackingKeySource.Registered(1 << 60), []), cache,
+                                 store)
