@@ -925,20 +925,21 @@ def run_cfg5(args, rank, world):
            "config": {"workload": "d2048 TwoPacking, 512-byte records x 2^25 (16,384 shards), store on every "
                                   "shard, 1000 seats, uniform index and seat per request, 36-bit mod switch",
                       "shards": shards, "records": shards * N_RING, "seats": C5_SEATS, "requests": count,
-                      "slots": 3, "max_batch": BATCH},
+                      "slots": args.lanes, "max_batch": BATCH},
            "setup_s": {"encode_records": encode_s, "precompute_packing": store_s},
            "device_bytes": ctx.device_bytes}
-    with pkg.ServingLoop(ctx, slots=3, max_batch=BATCH) as loop:
+    slots = args.lanes
+    with pkg.ServingLoop(ctx, slots=slots, max_batch=BATCH) as loop:
         w = min(count, 512)
         loop.replay(db, store, shard_ids[:w], handles[:w], seeds[:w], bs[:w], MS_TARGET, window=256)  # warm-up
         with ClockSampler(local) as clk:
-            _, _, lat, el = loop.replay(db, store, shard_ids, handles, seeds, bs, MS_TARGET, window=4 * 3 * BATCH)
+            _, _, lat, el = loop.replay(db, store, shard_ids, handles, seeds, bs, MS_TARGET, window=4 * slots * BATCH)
         sat = count / el
         lat_ms = np.sort(lat) / 1e6
         out["value"] = sat
         out["saturation"] = {"queries_per_s": sat, "p50_ms": float(lat_ms[len(lat_ms) // 2]),
                              "p99_ms": float(lat_ms[int(0.99 * (len(lat_ms) - 1))]),
-                             "window": 4 * 3 * BATCH}
+                             "window": 4 * slots * BATCH}
         out["clocks"] = clk.summary()
         sweep = []
         for frac in (0.25, 0.5, 0.75, 0.9):
@@ -976,7 +977,7 @@ def main():
     ap.add_argument("--lanes", type=int, default=None,
                     help="streams consecutive batches rotate over in the device-resident timed region, and the "
                          "caller threads and serving slots of the host-buffer legs (default: 4 for the served "
-                         "batch of 64, 3 otherwise; the measured optimum of each)")
+                         "batch of 64 and the serving sweep, 3 otherwise; the measured optimum of each)")
     ap.add_argument("--workload", default="served-batch",
                     choices=["served-batch", "special-modulus", "mixed", "serving-sweep", "one-packing"],
                     help="served-batch: the InspiRING batch of 64 over 2^20 records (the headline); special-modulus: "
@@ -989,7 +990,7 @@ def main():
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.lanes is None:
-        args.lanes = 4 if args.workload == "served-batch" else 3
+        args.lanes = 4 if args.workload in ("served-batch", "serving-sweep") else 3
     if args.steps is None:
         args.steps = 20 if args.impl == "reference" else {"served-batch": 300, "special-modulus": 100, "mixed": 60,
                                                           "serving-sweep": 0, "one-packing": 20}[args.workload]
