@@ -911,6 +911,18 @@ class DeviceClient:
         qs = [SeededBatchQuery(int(sids[i]), bytes(seeds[i]), b[i]) for i in range(count)]
         return qs, pos.value
 
+    def extract_arrays(self, a, b, modulus: int, entry_size: int, tree: bool = False) -> np.ndarray:
+        """Records (count x entry_size bytes) of packed responses given as (count, n) arrays."""
+        n = self.crs.params.ring_dim
+        a = np.ascontiguousarray(a, dtype=np.uint64)
+        b = np.ascontiguousarray(b, dtype=np.uint64)
+        if a.ndim != 2 or a.shape != b.shape or a.shape[1] != n:
+            raise PirError(f"responses must be (count, {n}) arrays")
+        out = np.zeros((a.shape[0], entry_size), dtype=np.uint8)
+        self.ctx.check(self.ctx._lib.ig_client_extract_batch(self.ctx.h, self.h, a.shape[0], _ptr(a), _ptr(b),
+                                                             int(modulus), int(entry_size), int(tree), _ptr(out)))
+        return out
+
     def extract_batch(self, responses, entry_size: int):
         """Records of packed responses (InspiRING or tree, unswitched or switched)."""
         n = self.crs.params.ring_dim

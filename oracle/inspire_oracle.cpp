@@ -1330,6 +1330,12 @@ void orc_cell_sampler_state(void* cv, uint8_t* key_out, u64* word_pos) {
   memcpy(key_out, r.key, 32);
   *word_pos = r.idx >= 64 ? r.block * 16 : (r.block - 4) * 16 + r.idx;
 }
+// The cell's whole database (entries x entry_size bytes); returns its length.
+u64 orc_cell_db(void* cv, uint8_t* out, u64 cap) {
+  auto* c = (Cell*)cv;
+  if (out) memcpy(out, c->db.data(), std::min<u64>(cap, c->db.size()));
+  return c->db.size();
+}
 void orc_cell_record(void* cv, u64 index, uint8_t* out) {
   auto* c = (Cell*)cv;
   memcpy(out, &c->db[index * c->entry_size], c->entry_size);

@@ -61,6 +61,7 @@ def lib():
             "orc_cell_galois_keys": (None, [V, P, P]),
             "orc_cell_decode_tree": (I, [V, U64, P, P, P]),
             "orc_cell_sampler_state": (None, [V, P, P]),
+            "orc_cell_db": (U64, [V, P, U64]),
             "orc_cell_build": (V, [U64, U64, U64, ctypes.c_double, U64, U64, I, U64, U64, U64]),
             "orc_cell_free": (None, [V]),
             "orc_cell_info": (None, [V, P, P, P, P]),
@@ -374,6 +375,13 @@ class Cell:
         s = np.frombuffer(seed, dtype=np.uint8).copy()
         lib().orc_cell_galois_keys(self.h, _p(s), _p(out))
         return out
+
+    def database(self) -> bytes:
+        """The cell's records, concatenated (the fixture's database formula)."""
+        L = lib().orc_cell_db(self.h, None, 0)
+        out = np.zeros(L, dtype=np.uint8)
+        lib().orc_cell_db(self.h, _p(out), L)
+        return out.tobytes()
 
     def sampler_state(self):
         """(ChaCha20 key bytes, 32-bit words consumed) of the session's Gaussian sampler."""
