@@ -424,7 +424,7 @@ int build_store(ig_ctx* c, DbObj& db, CrsObj& o, u32 s) {
   }
   IG_CUDA(c, cudaMemcpyAsync(sl.tag_key, key.data(), key.size() * 8, cudaMemcpyHostToDevice, c->stream));
   // Tags through the scan kernel in build mode.
-  ShardDev sd{sl.cols, nullptr, sl.tag_key, nullptr};
+  ShardDev sd{sl.cols, nullptr, sl.tag_key, nullptr, nullptr};
   QueryDev qd{};
   qd.shard = 0;
   void *dq, *ds;
@@ -2245,7 +2245,7 @@ int ig_respond_seeded_batch_noalloc(ig_ctx* c, uint64_t dbh, uint64_t st, uint64
       return fail(c, IG_ERR_ARG, "shard %u has no packing store; the allocation-free respond serves stored shards",
                   s);
   }
-  unsigned char* base;
+  unsigned char* base = nullptr;
   if ((rc = noalloc_scratch(c, &base))) return rc;
   u64* d_fold = (u64*)base;
   QueryDev* d_q = (QueryDev*)(base + NOALLOC_QUERY_OFF);
