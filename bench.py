@@ -427,9 +427,11 @@ def run_gb300(args, rank, world):
     scan_bytes = BATCH * (GAMMA * N_RING * 2 + N_RING * 8 + N_RING * 8 + GAMMA * 8)
     hbm_peak, peak_kind = peaks()
     achieved = scan_bytes / (scan_avg / 1e3) / 1e9
-    # Recursion: 3 transforms of n/2 log n butterflies per link + 16 pointwise products.
+    # Recursion: 3 transforms of n/2 log n butterflies per link, and per slot 7 pointwise
+    # products (the folded gadget rows: 3 for the seat sum, 4 for the next R) and 2
+    # Montgomery reductions of 2 products each.
     links = GAMMA - 1
-    modmul_per_query = links * (3 * (N_RING // 2) * 11 + 16 * N_RING) + 3 * (N_RING // 2) * 11
+    modmul_per_query = links * (3 * (N_RING // 2) * 11 + 11 * N_RING) + 3 * (N_RING // 2) * 11
     resp_gmodmul = BATCH * modmul_per_query / (resp_avg / 1e3) / 1e9  # one launch alone
     timed_gmodmul = value / world * modmul_per_query / 1e9  # per GPU over the timed region
     # Integer ceiling, measured now on this GPU: register-resident lazy butterflies (one

@@ -513,8 +513,33 @@ __device__ __forceinline__ u64 mod_switch_word(u64 cv, u64 qn) {
   return quo % qn;
 }
 
+// Rows X_0, X_1, X_2 (R-form, `stride` words apart) of a 3-digit gadget key, folded for
+// digits whose third transform is derived, D_2 = base^-2 (R - D_0 - base D_1):
+//   sum_k X_k D_k = D_0 (X_0 - base^-2 X_2) + D_1 (X_1 - base^-1 X_2) + R base^-2 X_2.
+// The folded rows are R-form too; a consumer then needs neither D_2 nor its reduction.
+// Every read precedes every write, so src may equal dst.
+__device__ __forceinline__ void fold_gadget3(const CrsDev& c, const u64* src, u64* dst, int stride) {
+  const u64 x0 = src[0], x1 = src[stride], x2 = src[2 * stride];
+  const u64 f0 = addq(x0, mont(x2, c.ld_c0_R));
+  const u64 f1 = addq(x1, mont(x2, c.ld_c1_R));
+  const u64 f2 = mont(x2, c.ld_inv_R);
+  dst[0] = f0;
+  dst[stride] = f1;
+  dst[2 * stride] = f2;
+}
+
+// The Galois keys ([key][digit][part][n], R-form NTT) folded in place by fold_gadget3.
+__global__ void k_fold_gadget_keys(CrsDev c, u64* keys, u32 count) {
+  const u32 n = c.n;
+  const u32 i = blockIdx.x * blockDim.x + threadIdx.x;  // (key, part, coefficient)
+  if (i >= count * 2 * n) return;
+  const u32 key = i / (2 * n), r = i - key * 2 * n;
+  u64* x = keys + (size_t)key * 6 * n + r;
+  fold_gadget3(c, x, x, (int)(2 * n));
+}
+
 // Per-query constants into shared memory: forward ladder, slot tables, the mask rows and
-// the seat's key rows (both R-form NTT).
+// the seat's key rows (both R-form NTT; with the exact gadget, folded by fold_gadget3).
 template <int N, int NT>
 __device__ __forceinline__ void stage_constants(const CrsDev& c, const u64* yR, u64* tw, u64* twp, u64* Wm, u64* Y,
                                                 uint16_t* e_tab, uint16_t* s_tab) {
@@ -524,9 +549,16 @@ __device__ __forceinline__ void stage_constants(const CrsDev& c, const u64* yR, 
     e_tab[k] = c.slot_exp[k];
     s_tab[k] = c.exp_slot[k];
   }
-  for (u32 k = threadIdx.x; k < c.rows * N; k += NT) {
-    Wm[k] = c.wmask_R[k];
-    Y[k] = yR[k];
+  if (c.approx == 0) {
+    for (int k = threadIdx.x; k < N; k += NT) {
+      fold_gadget3(c, c.wmask_R + k, Wm + k, N);
+      fold_gadget3(c, yR + k, Y + k, N);
+    }
+  } else {
+    for (u32 k = threadIdx.x; k < c.rows * N; k += NT) {
+      Wm[k] = c.wmask_R[k];
+      Y[k] = yR[k];
+    }
   }
 }
 
@@ -830,10 +862,9 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
       const u32 tb = s_tab[((gp * et[k]) & M2N) >> 1];
       u128 nb = wide(d0[k], Y[tb]) + wide(d1[k], Y[N + tb]);
       u128 nc = wide(a_ntt[tb], sv[k]) + wide(d0[k], Wm[tb]) + wide(d1[k], Wm[N + tb]);
-      if (exact) {
-        const u64 d2 = redc(wide(cur[k], c.ld_inv_R) + wide(d0[k], c.ld_c0_R) + wide(d1[k], c.ld_c1_R));
-        nb += wide(d2, Y[2 * N + tb]);
-        nc += wide(d2, Wm[2 * N + tb]);
+      if (exact) {  // the rows are folded: R_{i+1} stands in for digit 2
+        nb += wide(cur[k], Y[2 * N + tb]);
+        nc += wide(cur[k], Wm[2 * N + tb]);
       }
       sb[k] = addq(sb[k], redc(nb));
       cur[k] = redc(nc);
@@ -1128,10 +1159,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
       const u32 tb = s_tab[((gp * et[k]) & M2N) >> 1];
       u128 nb = wide(d0[k], Y[tb]) + wide(d1[k], Y[N + tb]);
       u128 nc = wide(a_ntt[tb], k == 0 ? sv.x : sv.y) + wide(d0[k], Wm[tb]) + wide(d1[k], Wm[N + tb]);
-      if (exact) {
-        const u64 d2 = redc(wide(cur[k], c.ld_inv_R) + wide(d0[k], c.ld_c0_R) + wide(d1[k], c.ld_c1_R));
-        nb += wide(d2, Y[2 * N + tb]);
-        nc += wide(d2, Wm[2 * N + tb]);
+      if (exact) {  // the rows are folded: R_{i+1} stands in for digit 2
+        nb += wide(cur[k], Y[2 * N + tb]);
+        nc += wide(cur[k], Wm[2 * N + tb]);
       }
       sb[k] = addq(sb[k], redc(nb));
       cur[k] = redc(nc);
@@ -1536,9 +1566,9 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
     }
 #pragma unroll
     for (int j = 0; j < 4; j++) {
-      const u64 d2 = redc(wide(aa[j], c.ld_inv_R) + wide(d0[j], c.ld_c0_R) + wide(d1[j], c.ld_c1_R));
-      const u64 na = redc(wide(d0[j], key[j]) + wide(d1[j], key[2 * N + j]) + wide(d2, key[4 * N + j]));
-      const u64 nb = redc(wide(d0[j], key[N + j]) + wide(d1[j], key[3 * N + j]) + wide(d2, key[5 * N + j]));
+      // The keys' digit rows are folded (fold_gadget3): aa stands in for digit 2.
+      const u64 na = redc(wide(d0[j], key[j]) + wide(d1[j], key[2 * N + j]) + wide(aa[j], key[4 * N + j]));
+      const u64 nb = redc(wide(d0[j], key[N + j]) + wide(d1[j], key[3 * N + j]) + wide(aa[j], key[5 * N + j]));
       ca[j] = addq(s0a[j], na);
       cb[j] = addq(s0b[j], addq(ab[j], nb));
     }
@@ -1878,6 +1908,13 @@ __global__ void __launch_bounds__(256) k_butterfly_peak(u64* out, int iters, u64
     case 11: { constexpr int L = 11; __VA_ARGS__; } break; \
     default: return cudaErrorInvalidValue;                 \
   }
+
+cudaError_t fold_gadget_keys(const CrsDev& c, u64* keys, u32 count, cudaStream_t s) {
+  const u32 total = count * 2 * c.n;
+  if (total == 0) return cudaSuccess;
+  k_fold_gadget_keys<<<(total + 255) / 256, 256, 0, s>>>(c, keys, count);
+  return cudaGetLastError();
+}
 
 cudaError_t ntt_rows(const CrsDev& c, const u64* in, u64* out, u32 rows, u64 scale, u64 scalep, cudaStream_t s) {
   if (rows == 0) return cudaSuccess;

@@ -68,6 +68,9 @@ struct ShardDev {
 namespace igk {
 using namespace ig;
 
+// The Galois keys ([key][3 digits][2 parts][n], R-form NTT) folded in place for consumers
+// that take R in place of the derived third digit.
+cudaError_t fold_gadget_keys(const CrsDev& c, u64* keys, u32 count, cudaStream_t s);
 // Forward NTT of `rows` polynomials: out[r] = scale * NTT(in[r] mod q), scale given with
 // its Shoup companion (scale = 1 for standard form, 2^64 mod q for R-form).
 cudaError_t ntt_rows(const CrsDev& c, const u64* in, u64* out, u32 rows, u64 scale, u64 scalep,

@@ -1599,6 +1599,7 @@ int ig_crs_set_galois_keys(ig_ctx* c, uint64_t crs, uint32_t count, uint32_t row
   IG_CUDA(c, cudaMemcpyAsync(raw, keys, words * 8, cudaMemcpyHostToDevice, c->stream));
   IG_CUDA(c, igk::ntt_rows(o->dev, (const u64*)raw, (u64*)dk, (u32)(words / o->n), R_MOD_Q, shoup_companion(R_MOD_Q),
                            c->stream));
+  IG_CUDA(c, igk::fold_gadget_keys(o->dev, (u64*)dk, count, c->stream));
   IG_CUDA(c, cudaStreamSynchronize(c->stream));
   if (o->dev.galois_R) {
     for (auto it = o->allocs.begin(); it != o->allocs.end(); ++it)
