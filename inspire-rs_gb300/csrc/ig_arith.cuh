@@ -71,8 +71,29 @@ IG_HD u64 shoup_lazy(u64 a, u64 w, u64 wp) {
 // a * w mod q, w < q; any a < 2^64.
 IG_HD u64 shoup(u64 a, u64 w, u64 wp) { return csub(shoup_lazy(a, w, wp)); }
 
+IG_HD u32 mulhi32(u32 a, u32 b) {
+#ifdef __CUDA_ARCH__
+  return __umulhi(a, b);
+#else
+  return (u32)(((u64)a * b) >> 32);
+#endif
+}
+
+// a * w mod q up to three q: in [0, 4q) for any a < 2^64. The quotient estimate takes the
+// high word of a * w' from three of its four 32-bit partial products: the high one whole
+// and the high halves of the two middle ones; the low one is dropped. The three dropped
+// fractions are each below one unit, so the estimate undershoots floor(a w' / 2^64) by
+// at most 2, and a w - est q exceeds the exact Shoup remainder (below 2q) by at most 2q.
+IG_HD u64 shoup_lazy4(u64 a, u64 w, u64 wp) {
+  const u32 ah = (u32)(a >> 32), al = (u32)a, wh = (u32)(wp >> 32), wl = (u32)wp;
+  const u64 est = (u64)ah * wh + mulhi32(ah, wl) + mulhi32(al, wh);
+  return a * w - est * q_opaque();
+}
+
 // x - 2q when x >= 2q.
 IG_HD u64 csub2(u64 x) { return x >= 2 * Q ? x - 2 * Q : x; }
+// x - 4q when x >= 4q.
+IG_HD u64 csub4(u64 x) { return x >= 4 * Q ? x - 4 * Q : x; }
 
 // a * b * 2^-64 mod q for a, b < q.
 IG_HD u64 mont(u64 a, u64 b) {
@@ -90,6 +111,14 @@ IG_HD u64 redc(u128 x) {
   const u64 lo = (u64)x, hi = (u64)(x >> 64);
   const u64 m = lo * QINV_NEG;
   return csub(hi + mulhi(m, Q) + (lo != 0 ? 1 : 0));
+}
+
+// The same for x < 2q * 2^64 (sums of products whose factors run up to 8q, such as
+// transforms kept below 8q times words below q): the quotient lands below 3q.
+IG_HD u64 redc_wide(u128 x) {
+  const u64 lo = (u64)x, hi = (u64)(x >> 64);
+  const u64 m = lo * QINV_NEG;
+  return csub(csub2(hi + mulhi(m, Q) + (lo != 0 ? 1 : 0)));
 }
 
 IG_HD u128 wide(u64 a, u64 b) { return (u128)a * b; }

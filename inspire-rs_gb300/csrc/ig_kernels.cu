@@ -34,7 +34,9 @@ using namespace ig;
 // barriers against a stage-per-barrier radix-2 schedule. Odd log n adds one radix-2 stage
 // (first in the forward, last in the inverse). The butterflies are Harvey's lazy ones: the
 // forward keeps words in [0, 4q) and the inverse in [0, 2q) (inputs canonical), reducing
-// only where the bound requires; results agree with the reference transform mod q.
+// only where the bound requires; results agree with the reference transform mod q. The
+// recursion kernels' per-link transforms use bf_fwd8 / bf_inv4 instead, whose products
+// take one 32-bit multiply fewer and whose words stay below 8q and 4q.
 
 // Forward CT butterfly on lazy words: X, Y < 4q in, both outputs < 4q.
 __device__ __forceinline__ void bf_fwd(u64& X, u64& Y, u64 w, u64 wp) {
@@ -48,6 +50,20 @@ __device__ __forceinline__ void bf_fwd(u64& X, u64& Y, u64 w, u64 wp) {
 __device__ __forceinline__ void bf_inv(u64& X, u64& Y, u64 w, u64 wp) {
   const u64 u = csub2(X + Y);
   Y = shoup_lazy(X - Y + 2 * Q, w, wp);
+  X = u;
+}
+
+// The same butterflies on shoup_lazy4 (one 32-bit multiply fewer per product), with the
+// bounds doubled: the forward keeps words below 8q, the inverse below 4q.
+__device__ __forceinline__ void bf_fwd8(u64& X, u64& Y, u64 w, u64 wp) {
+  const u64 x = csub4(X);
+  const u64 t = shoup_lazy4(Y, w, wp);
+  X = x + t;
+  Y = x - t + 4 * Q;
+}
+__device__ __forceinline__ void bf_inv4(u64& X, u64& Y, u64 w, u64 wp) {
+  const u64 u = csub4(X + Y);
+  Y = shoup_lazy4(X - Y + 4 * Q, w, wp);
   X = u;
 }
 
@@ -709,10 +725,10 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
       inv_twiddle(tw, twp, H + 2 * tid + 1, w1, w1p);
       inv_twiddle(tw, twp, H / 2 + tid, w2, w2p);
       u64 a0 = cur[0], a1 = cur[1], a2 = cur[2], a3 = cur[3];
-      bf_inv(a0, a1, w0, w0p);
-      bf_inv(a2, a3, w1, w1p);
-      bf_inv(a0, a2, w2, w2p);
-      bf_inv(a1, a3, w2, w2p);
+      bf_inv4(a0, a1, w0, w0p);
+      bf_inv4(a2, a3, w1, w1p);
+      bf_inv4(a0, a2, w2, w2p);
+      bf_inv4(a1, a3, w2, w2p);
       *reinterpret_cast<ulonglong2*>(X + sw(l0)) = make_ulonglong2(a0, a1);
       *reinterpret_cast<ulonglong2*>(X + sw(l0 + 2)) = make_ulonglong2(a2, a3);
     }
@@ -729,10 +745,10 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
       inv_twiddle(tw, twp, m + 2 * B + 1, w1, w1p);
       inv_twiddle(tw, twp, (m >> 1) + B, w2, w2p);
       u64 a0 = X[sw(e0)], a1 = X[sw(e0 + t)], a2 = X[sw(e0 + 2 * t)], a3 = X[sw(e0 + 3 * t)];
-      bf_inv(a0, a1, w0, w0p);
-      bf_inv(a2, a3, w1, w1p);
-      bf_inv(a0, a2, w2, w2p);
-      bf_inv(a1, a3, w2, w2p);
+      bf_inv4(a0, a1, w0, w0p);
+      bf_inv4(a2, a3, w1, w1p);
+      bf_inv4(a0, a2, w2, w2p);
+      bf_inv4(a1, a3, w2, w2p);
       X[sw(e0)] = a0;
       X[sw(e0 + t)] = a1;
       X[sw(e0 + 2 * t)] = a2;
@@ -749,7 +765,7 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
         u64 w, wp;
         inv_twiddle(tw, twp, m + B, w, wp);
         u64 a = X[sw(e)], b = X[sw(e + t)];
-        bf_inv(a, b, w, wp);
+        bf_inv4(a, b, w, wp);
         X[sw(e)] = a;
         X[sw(e + t)] = b;
       }
@@ -760,7 +776,7 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
     for (int j = 0; j < 2; j++) {
       const int b = tid + j * NT;
       u64 x0 = X[sw(b)], x1 = X[sw(b + H)];
-      bf_inv(x0, x1, wi, wip);
+      bf_inv4(x0, x1, wi, wip);
       const u64 r0 = shoup(x0, c.ninv, c.ninvp), r1 = shoup(x1, c.ninv, c.ninvp);
       u64 p0, p1, q0, q1;  // digits 0 and 1 of coefficients b and b + N/2
       if (exact) {
@@ -775,11 +791,11 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
         q0 = rr1 & DMASK;
         q1 = rr1 >> 20;
       }
-      const u64 t0 = shoup_lazy(q0, wf, wfp), t1 = shoup_lazy(q1, wf, wfp);
+      const u64 t0 = shoup_lazy4(q0, wf, wfp), t1 = shoup_lazy4(q1, wf, wfp);
       D[sw(b)] = p0 + t0;
-      D[sw(b + H)] = p0 + 2 * Q - t0;
+      D[sw(b + H)] = p0 + 4 * Q - t0;
       D[N + sw(b)] = p1 + t1;
-      D[N + sw(b + H)] = p1 + 2 * Q - t1;
+      D[N + sw(b + H)] = p1 + 4 * Q - t1;
     }
     __syncthreads();
     // Forward stages 1 .. logn-3 (a radix-2 stage first when logn is even), both digits.
@@ -796,7 +812,7 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
         for (int k = 0; k < 2; k++) {
           u64* x = D + k * N;
           u64 a = x[sw(e)], b = x[sw(e + t)];
-          bf_fwd(a, b, w, wp);
+          bf_fwd8(a, b, w, wp);
           x[sw(e)] = a;
           x[sw(e + t)] = b;
         }
@@ -817,14 +833,14 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
       u64* x1 = D + N;
       u64 a0 = x0[i0], a1 = x0[i1], a2 = x0[i2], a3 = x0[i3];
       u64 c0 = x1[i0], c1 = x1[i1], c2 = x1[i2], c3 = x1[i3];
-      bf_fwd(a0, a2, wa, wap);
-      bf_fwd(c0, c2, wa, wap);
-      bf_fwd(a1, a3, wa, wap);
-      bf_fwd(c1, c3, wa, wap);
-      bf_fwd(a0, a1, wb, wbp);
-      bf_fwd(c0, c1, wb, wbp);
-      bf_fwd(a2, a3, wc, wcp);
-      bf_fwd(c2, c3, wc, wcp);
+      bf_fwd8(a0, a2, wa, wap);
+      bf_fwd8(c0, c2, wa, wap);
+      bf_fwd8(a1, a3, wa, wap);
+      bf_fwd8(c1, c3, wa, wap);
+      bf_fwd8(a0, a1, wb, wbp);
+      bf_fwd8(c0, c1, wb, wbp);
+      bf_fwd8(a2, a3, wc, wcp);
+      bf_fwd8(c2, c3, wc, wcp);
       x0[i0] = a0;
       x0[i1] = a1;
       x0[i2] = a2;
@@ -847,14 +863,14 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
       const ulonglong2 g23 = *reinterpret_cast<const ulonglong2*>(D + N + sw(l0 + 2));
       d0[0] = v01.x, d0[1] = v01.y, d0[2] = v23.x, d0[3] = v23.y;
       d1[0] = g01.x, d1[1] = g01.y, d1[2] = g23.x, d1[3] = g23.y;
-      bf_fwd(d0[0], d0[2], fa, fap);
-      bf_fwd(d1[0], d1[2], fa, fap);
-      bf_fwd(d0[1], d0[3], fa, fap);
-      bf_fwd(d1[1], d1[3], fa, fap);
-      bf_fwd(d0[0], d0[1], fb, fbp);
-      bf_fwd(d1[0], d1[1], fb, fbp);
-      bf_fwd(d0[2], d0[3], fc, fcp);
-      bf_fwd(d1[2], d1[3], fc, fcp);
+      bf_fwd8(d0[0], d0[2], fa, fap);
+      bf_fwd8(d1[0], d1[2], fa, fap);
+      bf_fwd8(d0[1], d0[3], fa, fap);
+      bf_fwd8(d1[1], d1[3], fa, fap);
+      bf_fwd8(d0[0], d0[1], fb, fbp);
+      bf_fwd8(d1[0], d1[1], fb, fbp);
+      bf_fwd8(d0[2], d0[3], fc, fcp);
+      bf_fwd8(d1[2], d1[3], fc, fcp);
     }
     const u64 sv[4] = {sv01.x, sv01.y, sv23.x, sv23.y};
 #pragma unroll
@@ -866,8 +882,8 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
         nb += wide(cur[k], Y[2 * N + tb]);
         nc += wide(cur[k], Wm[2 * N + tb]);
       }
-      sb[k] = addq(sb[k], redc(nb));
-      cur[k] = redc(nc);
+      sb[k] = addq(sb[k], redc_wide(nb));
+      cur[k] = redc_wide(nc);
     }
   }
   __syncthreads();  // every thread is past its last read of D
@@ -914,10 +930,10 @@ __device__ __forceinline__ void inv_half_r4(u64* xh, int s, int rank, const u64*
     inv_twiddle(tw, twp, m + 2 * B + 1, w1, w1p);
     inv_twiddle(tw, twp, (m >> 1) + B, w2, w2p);
     u64 a0 = xh[sw(e0)], a1 = xh[sw(e0 + t)], a2 = xh[sw(e0 + 2 * t)], a3 = xh[sw(e0 + 3 * t)];
-    bf_inv(a0, a1, w0, w0p);
-    bf_inv(a2, a3, w1, w1p);
-    bf_inv(a0, a2, w2, w2p);
-    bf_inv(a1, a3, w2, w2p);
+    bf_inv4(a0, a1, w0, w0p);
+    bf_inv4(a2, a3, w1, w1p);
+    bf_inv4(a0, a2, w2, w2p);
+    bf_inv4(a1, a3, w2, w2p);
     xh[sw(e0)] = a0;
     xh[sw(e0 + t)] = a1;
     xh[sw(e0 + 2 * t)] = a2;
@@ -938,7 +954,7 @@ __device__ __forceinline__ void inv_half_r2(u64* xh, int s, int rank, const u64*
   u64 w, wp;
   inv_twiddle(tw, twp, m + B, w, wp);
   u64 a = xh[sw(e)], b = xh[sw(e + t)];
-  bf_inv(a, b, w, wp);
+  bf_inv4(a, b, w, wp);
   xh[sw(e)] = a;
   xh[sw(e + t)] = b;
   __syncthreads();
@@ -960,10 +976,10 @@ __device__ __forceinline__ void fwd_half_r4(u64* D, int s, int rank, const u64* 
   const u64 wb = tw[2 * m + 2 * i], wbp = twp[2 * m + 2 * i];
   const u64 wc = tw[2 * m + 2 * i + 1], wcp = twp[2 * m + 2 * i + 1];
   u64 a0 = x[sw(e0)], a1 = x[sw(e0 + h)], a2 = x[sw(e0 + t)], a3 = x[sw(e0 + t + h)];
-  bf_fwd(a0, a2, wa, wap);
-  bf_fwd(a1, a3, wa, wap);
-  bf_fwd(a0, a1, wb, wbp);
-  bf_fwd(a2, a3, wc, wcp);
+  bf_fwd8(a0, a2, wa, wap);
+  bf_fwd8(a1, a3, wa, wap);
+  bf_fwd8(a0, a1, wb, wbp);
+  bf_fwd8(a2, a3, wc, wcp);
   x[sw(e0)] = a0;
   x[sw(e0 + h)] = a1;
   x[sw(e0 + t)] = a2;
@@ -986,7 +1002,7 @@ __device__ __forceinline__ void fwd_half_r2(u64* D, int s, int rank, const u64* 
   for (int k = 0; k < 2; k++) {
     u64* x = D + k * (N / 2);
     u64 a = x[sw(e)], b = x[sw(e + t)];
-    bf_fwd(a, b, w, wp);
+    bf_fwd8(a, b, w, wp);
     x[sw(e)] = a;
     x[sw(e + t)] = b;
   }
@@ -1084,10 +1100,10 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
     {
       // Inverse stages 0-1 of unit ug: lane dg holds slots 4u + 2dg, +1.
       u64 p = cur[0], q = cur[1];
-      bf_inv(p, q, wl1, wl1p);
+      bf_inv4(p, q, wl1, wl1p);
       const u64 recv = __shfl_xor_sync(0xffffffffu, dg == 0 ? q : p, 1);
       u64 x0 = dg == 0 ? p : recv, x1 = dg == 0 ? recv : q;  // (slot 4u, 4u+2) or (4u+1, 4u+3)
-      bf_inv(x0, x1, wl2, wl2p);
+      bf_inv4(x0, x1, wl2, wl2p);
       xh[sw(4 * u + dg)] = x0;
       xh[sw(4 * u + dg + 2)] = x1;
     }
@@ -1105,7 +1121,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
       for (int j = 0; j < 2; j++) {
         const int b = tid + j * NT;
         u64 x0 = lo[sw(b)], x1 = hi[sw(b)];
-        bf_inv(x0, x1, wi, wip);
+        bf_inv4(x0, x1, wi, wip);
         const u64 r0 = shoup(x0, c.ninv, c.ninvp), r1 = shoup(x1, c.ninv, c.ninvp);
         u64 p0, p1, q0, q1;  // digits 0 and 1 of coefficients b and b + H
         if (exact) {
@@ -1121,9 +1137,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
           q1 = rr1 >> 20;
         }
         // Forward cross stage: slot b gets p + w q, slot b + H gets p - w q.
-        const u64 t0 = shoup_lazy(q0, wf, wfp), t1 = shoup_lazy(q1, wf, wfp);
-        D[sw(b)] = rank == 0 ? p0 + t0 : p0 + 2 * Q - t0;
-        D[H + sw(b)] = rank == 0 ? p1 + t1 : p1 + 2 * Q - t1;
+        const u64 t0 = shoup_lazy4(q0, wf, wfp), t1 = shoup_lazy4(q1, wf, wfp);
+        D[sw(b)] = rank == 0 ? p0 + t0 : p0 + 4 * Q - t0;
+        D[H + sw(b)] = rank == 0 ? p1 + t1 : p1 + 4 * Q - t1;
       }
     }
     __syncthreads();
@@ -1142,10 +1158,10 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
       const ulonglong2 v01 = *reinterpret_cast<const ulonglong2*>(x + sw(4 * u));
       const ulonglong2 v23 = *reinterpret_cast<const ulonglong2*>(x + sw(4 * u + 2));
       u64 a0 = v01.x, a1 = v01.y, a2 = v23.x, a3 = v23.y;
-      bf_fwd(a0, a2, fa, fap);
-      bf_fwd(a1, a3, fa, fap);
-      bf_fwd(a0, a1, fb, fbp);
-      bf_fwd(a2, a3, fc, fcp);
+      bf_fwd8(a0, a2, fa, fap);
+      bf_fwd8(a1, a3, fa, fap);
+      bf_fwd8(a0, a1, fb, fbp);
+      bf_fwd8(a2, a3, fc, fcp);
       const u64 g0 = __shfl_xor_sync(0xffffffffu, dg == 0 ? a2 : a0, 1);
       const u64 g1 = __shfl_xor_sync(0xffffffffu, dg == 0 ? a3 : a1, 1);
       const u64 m0 = dg == 0 ? a0 : a2, m1 = dg == 0 ? a1 : a3;
@@ -1163,8 +1179,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
         nb += wide(cur[k], Y[2 * N + tb]);
         nc += wide(cur[k], Wm[2 * N + tb]);
       }
-      sb[k] = addq(sb[k], redc(nb));
-      cur[k] = redc(nc);
+      sb[k] = addq(sb[k], redc_wide(nb));
+      cur[k] = redc_wide(nc);
     }
   }
   // Final transforms: rank 0 assembles R_0 (-> a), rank 1 the online sum (-> b), each
@@ -1876,10 +1892,10 @@ __global__ void __launch_bounds__((1 << LOGN) / 4) k_client_extract(CrsDev c, co
 }
 
 // ------------------------------------------------------------------------------------
-// Integer roofline probe: lazy forward butterflies (one Shoup product, two 64-bit adds and
-// a conditional subtraction each, the transforms' unit of work) on values held in
-// registers, eight independent chains per thread, no memory traffic. Its rate is the
-// ceiling the respond kernels' butterflies are measured against.
+// Integer roofline probe: the recursion kernels' lazy forward butterflies (bf_fwd8: one
+// Shoup product, two 64-bit adds and a conditional subtraction each, the transforms' unit
+// of work) on values held in registers, eight independent chains per thread, no memory
+// traffic. Its rate is the ceiling the respond kernels' butterflies are measured against.
 __global__ void __launch_bounds__(256) k_butterfly_peak(u64* out, int iters, u64 w, u64 wp) {
   u64 x[8];
 #pragma unroll
@@ -1887,9 +1903,9 @@ __global__ void __launch_bounds__(256) k_butterfly_peak(u64* out, int iters, u64
 #pragma unroll 1
   for (int it = 0; it < iters; it++) {
 #pragma unroll
-    for (int k = 0; k < 8; k += 2) bf_fwd(x[k], x[k + 1], w, wp);
+    for (int k = 0; k < 8; k += 2) bf_fwd8(x[k], x[k + 1], w, wp);
 #pragma unroll
-    for (int k = 0; k < 4; k++) bf_fwd(x[k], x[k + 4], w, wp);
+    for (int k = 0; k < 4; k++) bf_fwd8(x[k], x[k + 4], w, wp);
   }
   u64 acc = 0;
 #pragma unroll
