@@ -1445,10 +1445,10 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
       inv_twiddle(tw, twp, H + 2 * tid + 1, w1, w1p);
       inv_twiddle(tw, twp, H / 2 + tid, w2, w2p);
       u64 a0 = aa[0], a1 = aa[1], a2 = aa[2], a3 = aa[3];
-      bf_inv(a0, a1, w0, w0p);
-      bf_inv(a2, a3, w1, w1p);
-      bf_inv(a0, a2, w2, w2p);
-      bf_inv(a1, a3, w2, w2p);
+      bf_inv4(a0, a1, w0, w0p);
+      bf_inv4(a2, a3, w1, w1p);
+      bf_inv4(a0, a2, w2, w2p);
+      bf_inv4(a1, a3, w2, w2p);
       *reinterpret_cast<ulonglong2*>(X + sw(l0)) = make_ulonglong2(a0, a1);
       *reinterpret_cast<ulonglong2*>(X + sw(l0 + 2)) = make_ulonglong2(a2, a3);
     }
@@ -1465,10 +1465,10 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
       inv_twiddle(tw, twp, m + 2 * B + 1, w1, w1p);
       inv_twiddle(tw, twp, (m >> 1) + B, w2, w2p);
       u64 a0 = X[sw(e0)], a1 = X[sw(e0 + tt)], a2 = X[sw(e0 + 2 * tt)], a3 = X[sw(e0 + 3 * tt)];
-      bf_inv(a0, a1, w0, w0p);
-      bf_inv(a2, a3, w1, w1p);
-      bf_inv(a0, a2, w2, w2p);
-      bf_inv(a1, a3, w2, w2p);
+      bf_inv4(a0, a1, w0, w0p);
+      bf_inv4(a2, a3, w1, w1p);
+      bf_inv4(a0, a2, w2, w2p);
+      bf_inv4(a1, a3, w2, w2p);
       X[sw(e0)] = a0;
       X[sw(e0 + tt)] = a1;
       X[sw(e0 + 2 * tt)] = a2;
@@ -1485,7 +1485,7 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
         u64 w, wp;
         inv_twiddle(tw, twp, m + B, w, wp);
         u64 a = X[sw(e)], b = X[sw(e + tt)];
-        bf_inv(a, b, w, wp);
+        bf_inv4(a, b, w, wp);
         X[sw(e)] = a;
         X[sw(e + tt)] = b;
       }
@@ -1496,14 +1496,14 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
     for (int j = 0; j < 2; j++) {
       const int b = tid + j * NT;
       u64 x0 = X[sw(b)], x1 = X[sw(b + H)];
-      bf_inv(x0, x1, wi, wip);
+      bf_inv4(x0, x1, wi, wip);
       const u64 r0 = shoup(x0, c.ninv, c.ninvp), r1 = shoup(x1, c.ninv, c.ninvp);
       const u64 p0 = r0 & DMASK, p1 = (r0 >> 20) & DMASK, q0 = r1 & DMASK, q1 = (r1 >> 20) & DMASK;
-      const u64 t0 = shoup_lazy(q0, wf, wfp), t1 = shoup_lazy(q1, wf, wfp);
+      const u64 t0 = shoup_lazy4(q0, wf, wfp), t1 = shoup_lazy4(q1, wf, wfp);
       D[sw(b)] = p0 + t0;
-      D[sw(b + H)] = p0 + 2 * Q - t0;
+      D[sw(b + H)] = p0 + 4 * Q - t0;
       D[N + sw(b)] = p1 + t1;
-      D[N + sw(b + H)] = p1 + 2 * Q - t1;
+      D[N + sw(b + H)] = p1 + 4 * Q - t1;
     }
     __syncthreads();
     // Forward stages 1 .. logn-3 (a radix-2 stage first when logn is even), both digits.
@@ -1520,7 +1520,7 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
         for (int k = 0; k < 2; k++) {
           u64* x = D + k * N;
           u64 a = x[sw(e)], b = x[sw(e + tt)];
-          bf_fwd(a, b, w, wp);
+          bf_fwd8(a, b, w, wp);
           x[sw(e)] = a;
           x[sw(e + tt)] = b;
         }
@@ -1541,14 +1541,14 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
       u64* x1 = D + N;
       u64 a0 = x0[i0], a1 = x0[i1], a2 = x0[i2], a3 = x0[i3];
       u64 c0 = x1[i0], c1 = x1[i1], c2 = x1[i2], c3 = x1[i3];
-      bf_fwd(a0, a2, wa, wap);
-      bf_fwd(c0, c2, wa, wap);
-      bf_fwd(a1, a3, wa, wap);
-      bf_fwd(c1, c3, wa, wap);
-      bf_fwd(a0, a1, wb, wbp);
-      bf_fwd(c0, c1, wb, wbp);
-      bf_fwd(a2, a3, wc, wcp);
-      bf_fwd(c2, c3, wc, wcp);
+      bf_fwd8(a0, a2, wa, wap);
+      bf_fwd8(c0, c2, wa, wap);
+      bf_fwd8(a1, a3, wa, wap);
+      bf_fwd8(c1, c3, wa, wap);
+      bf_fwd8(a0, a1, wb, wbp);
+      bf_fwd8(c0, c1, wb, wbp);
+      bf_fwd8(a2, a3, wc, wcp);
+      bf_fwd8(c2, c3, wc, wcp);
       x0[i0] = a0;
       x0[i1] = a1;
       x0[i2] = a2;
@@ -1571,20 +1571,20 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
       const ulonglong2 g23 = *reinterpret_cast<const ulonglong2*>(D + N + sw(l0 + 2));
       d0[0] = v01.x, d0[1] = v01.y, d0[2] = v23.x, d0[3] = v23.y;
       d1[0] = g01.x, d1[1] = g01.y, d1[2] = g23.x, d1[3] = g23.y;
-      bf_fwd(d0[0], d0[2], fa, fap);
-      bf_fwd(d1[0], d1[2], fa, fap);
-      bf_fwd(d0[1], d0[3], fa, fap);
-      bf_fwd(d1[1], d1[3], fa, fap);
-      bf_fwd(d0[0], d0[1], fb, fbp);
-      bf_fwd(d1[0], d1[1], fb, fbp);
-      bf_fwd(d0[2], d0[3], fc, fcp);
-      bf_fwd(d1[2], d1[3], fc, fcp);
+      bf_fwd8(d0[0], d0[2], fa, fap);
+      bf_fwd8(d1[0], d1[2], fa, fap);
+      bf_fwd8(d0[1], d0[3], fa, fap);
+      bf_fwd8(d1[1], d1[3], fa, fap);
+      bf_fwd8(d0[0], d0[1], fb, fbp);
+      bf_fwd8(d1[0], d1[1], fb, fbp);
+      bf_fwd8(d0[2], d0[3], fc, fcp);
+      bf_fwd8(d1[2], d1[3], fc, fcp);
     }
 #pragma unroll
     for (int j = 0; j < 4; j++) {
       // The keys' digit rows are folded (fold_gadget3): aa stands in for digit 2.
-      const u64 na = redc(wide(d0[j], key[j]) + wide(d1[j], key[2 * N + j]) + wide(aa[j], key[4 * N + j]));
-      const u64 nb = redc(wide(d0[j], key[N + j]) + wide(d1[j], key[3 * N + j]) + wide(aa[j], key[5 * N + j]));
+      const u64 na = redc_wide(wide(d0[j], key[j]) + wide(d1[j], key[2 * N + j]) + wide(aa[j], key[4 * N + j]));
+      const u64 nb = redc_wide(wide(d0[j], key[N + j]) + wide(d1[j], key[3 * N + j]) + wide(aa[j], key[5 * N + j]));
       ca[j] = addq(s0a[j], na);
       cb[j] = addq(s0b[j], addq(ab[j], nb));
     }
