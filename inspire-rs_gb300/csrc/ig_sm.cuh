@@ -30,6 +30,17 @@ struct Prime32 {
     return (u32)((t + (u64)k * m) >> 32);
   }
   __host__ __device__ __forceinline__ u32 mont(u32 a, u32 b) const { return csub(montl(a, b)); }
+  // a w mod m in [0, 2m) for any 32-bit a and w < m, with w' = floor(w 2^32 / m) (Shoup):
+  // one high and two low 32-bit multiplies, where montl takes two wide ones and a low one.
+  __host__ __device__ __forceinline__ u32 shoupl(u32 a, u32 w, u32 wp) const {
+#ifdef __CUDA_ARCH__
+    const u32 est = __umulhi(a, wp);
+#else
+    const u32 est = (u32)(((u64)a * wp) >> 32);
+#endif
+    return a * w - est * m;
+  }
+  __host__ __device__ __forceinline__ u32 shoup(u32 a, u32 w, u32 wp) const { return csub(shoupl(a, w, wp)); }
   __host__ __device__ __forceinline__ u32 small(i64 x) const { return (u32)x + (m & (u32)(x >> 63)); }
   __host__ __device__ __forceinline__ i64 centred(u32 x) const { return x > (m >> 1) ? (i64)x - (i64)m : (i64)x; }
 };
@@ -40,6 +51,7 @@ struct Ntt32Dev {
   Prime32 p;
   const u32* fwd;
   const u32* inv;
+  const uint2* fwd_sh;  // the forward ladder in standard form with Shoup companions (w, w')
   u32 n_inv, last;
 };
 

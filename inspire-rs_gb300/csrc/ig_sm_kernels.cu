@@ -195,6 +195,16 @@ __global__ void __launch_bounds__(512) k_sm_body_fold(SmDev c, const SmQueryDev*
   fold[(size_t)blockIdx.x * c.nb + k] = acc;
 }
 
+// Inverse twiddle m of a ladder (Gentleman-Sande, psi^-brv(m)) from the forward ladder's
+// Shoup pairs: for 2^s <= m < 2^(s+1), brv(3 2^s - 1 - m) = n - brv(m), so
+// psi^-brv(m) = -psi^brv(3 2^s - 1 - m); and the companion of pm - w is the complement of
+// w's (w != 0, pm prime above w).
+__device__ __forceinline__ uint2 inv_tw(const uint2* fs, u32 pm, int m) {
+  const int s = 31 - __clz(m);
+  const uint2 f = fs[3 * (1 << s) - 1 - m];
+  return make_uint2(pm - f.x, ~f.y);
+}
+
 // ------------------------------------------------------------------------------------
 // expand_uniform (mod.rs:225-237) on the query seed's stream 0: accept u < floor(2^64/q) q,
 // take u mod q. Word w of the stream is keystream words 2w, 2w+1. A rejection (probability
@@ -272,8 +282,12 @@ __device__ __forceinline__ u32 q_to_p(const SmDev& c, u32 x) {
 // stage (t = n/2, carrying 1/n), the limb lift and the next forward's first stage (the
 // same index pairs) run as one pass in place.
 //
-// LAZY (q below 2^29, so 8q < 2^32): the q-limb passes skip most reductions. montl leaves
-// [0, 2q) for any 32-bit left operand, and the values between passes stay in [0, 4q)
+// Twiddle products are Shoup products against the forward ladders' (w, w') pairs (the
+// inverse ladders derived from them by inv_tw); products by R-form operands are
+// Montgomery products.
+//
+// LAZY (q below 2^29, so 8q < 2^32): the q-limb passes skip most reductions. montl and
+// shoupl leave [0, 2q) for any 32-bit left operand, and the values between passes stay in [0, 4q)
 // through INTT_q and in [0, 6q) through NTT_q; every sum and every difference (offset by
 // 2q or 4q) stays below 8q. Values are brought to [0, q) where the arithmetic needs a
 // residue: before the lift to p and at the end of the chain. The p limb (near 2^31) has
@@ -290,10 +304,8 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 2)
   u32* kp = smw + 3 * N;
   u32* wq = smw + 4 * N;
   u32* wp = smw + 5 * N;
-  u32* fq = smw + 6 * N;
-  u32* iq = smw + 7 * N;
-  u32* fp = smw + 8 * N;
-  u32* ip = smw + 9 * N;
+  uint2* fqs = reinterpret_cast<uint2*>(smw + 6 * N);  // forward ladders with Shoup companions
+  uint2* fps = reinterpret_cast<uint2*>(smw + 8 * N);
   uint16_t* e_tab = reinterpret_cast<uint16_t*>(smw + 10 * N);
   uint16_t* s_tab = e_tab + N;
   const int tid = threadIdx.x;
@@ -305,15 +317,13 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 2)
     kp[k] = qd.seat[N + k];
     wq[k] = qd.seat[2 * N + k];
     wp[k] = qd.seat[3 * N + k];
-    fq[k] = c.lq.fwd[k];
-    iq[k] = c.lq.inv[k];
-    fp[k] = c.lp.fwd[k];
-    ip[k] = c.lp.inv[k];
+    fqs[k] = c.lq.fwd_sh[k];
+    fps[k] = c.lp.fwd_sh[k];
     e_tab[k] = c.slot_exp[k];
     s_tab[k] = c.exp_slot[k];
   }
   sm_expand<N, NT>(qd, PQ.m, a, status, qi);
-  fwd32<LOGN>(a, c.lq, fq);
+  fwd32<LOGN>(a, c.lq, c.lq.fwd);
 
   const int l0 = 4 * tid;
   u32 cur[4], accq[4], accp[4], et[4];
@@ -326,92 +336,95 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 2)
     accp[k] = 0;
   }
   // Inverse stages 0-1 of unit tid (t = 1, block tid), in registers, to buf[l0..l0+3].
-  auto inv_first = [&](const Prime32& P, const u32* itw, u32 a0, u32 a1, u32 a2, u32 a3) {
-    const u32 w0 = itw[H + 2 * tid], w1 = itw[H + 2 * tid + 1], w2 = itw[H / 2 + tid];
-    const u32 d01 = P.mont(a0 + P.m - a1, w0);
+  auto inv_first = [&](const Prime32& P, const uint2* fs, u32 a0, u32 a1, u32 a2, u32 a3) {
+    const uint2 w0 = inv_tw(fs, P.m, H + 2 * tid), w1 = inv_tw(fs, P.m, H + 2 * tid + 1),
+                w2 = inv_tw(fs, P.m, H / 2 + tid);
+    const u32 d01 = P.shoup(a0 + P.m - a1, w0.x, w0.y);
     a0 = P.add(a0, a1);
-    const u32 d23 = P.mont(a2 + P.m - a3, w1);
+    const u32 d23 = P.shoup(a2 + P.m - a3, w1.x, w1.y);
     a2 = P.add(a2, a3);
-    *reinterpret_cast<uint4*>(buf + l0) =
-        make_uint4(P.add(a0, a2), P.add(d01, d23), P.mont(a0 + P.m - a2, w2), P.mont(d01 + P.m - d23, w2));
+    *reinterpret_cast<uint4*>(buf + l0) = make_uint4(P.add(a0, a2), P.add(d01, d23), P.shoup(a0 + P.m - a2, w2.x, w2.y),
+                                                     P.shoup(d01 + P.m - d23, w2.x, w2.y));
   };
   // Inverse stages 2 .. logn-2 over buf (radix-4 pairs; logn is odd).
-  auto inv_middle = [&](const Prime32& P, const u32* itw) {
+  auto inv_middle = [&](const Prime32& P, const uint2* fs) {
 #pragma unroll 1
     for (int s = 2; s + 1 < LOGN; s += 2) {
       const int t = 1 << s, m = N >> (s + 1);
       const int B = tid >> s, o = tid & (t - 1);
       const int e0 = B * 4 * t + o;
-      const u32 w0 = itw[m + 2 * B], w1 = itw[m + 2 * B + 1], w2 = itw[(m >> 1) + B];
+      const uint2 w0 = inv_tw(fs, P.m, m + 2 * B), w1 = inv_tw(fs, P.m, m + 2 * B + 1),
+                  w2 = inv_tw(fs, P.m, (m >> 1) + B);
       u32 a0 = buf[e0], a1 = buf[e0 + t], a2 = buf[e0 + 2 * t], a3 = buf[e0 + 3 * t];
-      const u32 d01 = P.mont(a0 + P.m - a1, w0);
+      const u32 d01 = P.shoup(a0 + P.m - a1, w0.x, w0.y);
       a0 = P.add(a0, a1);
-      const u32 d23 = P.mont(a2 + P.m - a3, w1);
+      const u32 d23 = P.shoup(a2 + P.m - a3, w1.x, w1.y);
       a2 = P.add(a2, a3);
       buf[e0] = P.add(a0, a2);
-      buf[e0 + 2 * t] = P.mont(a0 + P.m - a2, w2);
+      buf[e0 + 2 * t] = P.shoup(a0 + P.m - a2, w2.x, w2.y);
       buf[e0 + t] = P.add(d01, d23);
-      buf[e0 + 3 * t] = P.mont(d01 + P.m - d23, w2);
+      buf[e0 + 3 * t] = P.shoup(d01 + P.m - d23, w2.x, w2.y);
       __syncthreads();
     }
   };
   // Forward stages 1 .. logn-3 over buf.
-  auto fwd_middle = [&](const Prime32& P, const u32* tw) {
+  auto fwd_middle = [&](const Prime32& P, const uint2* fs) {
 #pragma unroll 1
     for (int s = 1; s < LOGN - 2; s += 2) {
       const int t = N >> (s + 1), m = 1 << s, h = t >> 1;
       const int i = tid / h, o = tid - i * h;
       const int e0 = i * 2 * t + o;
-      const u32 wa = tw[m + i], wb = tw[2 * m + 2 * i], wc = tw[2 * m + 2 * i + 1];
+      const uint2 wa = fs[m + i], wb = fs[2 * m + 2 * i], wc = fs[2 * m + 2 * i + 1];
       u32 a0 = buf[e0], a1 = buf[e0 + h], a2 = buf[e0 + t], a3 = buf[e0 + t + h];
-      u32 v = P.mont(a2, wa);
+      u32 v = P.shoup(a2, wa.x, wa.y);
       a2 = P.sub(a0, v);
       a0 = P.add(a0, v);
-      v = P.mont(a3, wa);
+      v = P.shoup(a3, wa.x, wa.y);
       a3 = P.sub(a1, v);
       a1 = P.add(a1, v);
-      v = P.mont(a1, wb);
+      v = P.shoup(a1, wb.x, wb.y);
       buf[e0] = P.add(a0, v);
       buf[e0 + h] = P.sub(a0, v);
-      v = P.mont(a3, wc);
+      v = P.shoup(a3, wc.x, wc.y);
       buf[e0 + t] = P.add(a2, v);
       buf[e0 + t + h] = P.sub(a2, v);
       __syncthreads();
     }
   };
   // Forward stages logn-2, logn-1 of unit tid, in registers, from buf[l0..l0+3].
-  auto fwd_last = [&](const Prime32& P, const u32* tw, u32 (&x)[4]) {
+  auto fwd_last = [&](const Prime32& P, const uint2* fs, u32 (&x)[4]) {
     constexpr int MF = 1 << (LOGN - 2);
-    const u32 wa = tw[MF + tid], wb = tw[2 * MF + 2 * tid], wc = tw[2 * MF + 2 * tid + 1];
+    const uint2 wa = fs[MF + tid], wb = fs[2 * MF + 2 * tid], wc = fs[2 * MF + 2 * tid + 1];
     const uint4 v4 = *reinterpret_cast<const uint4*>(buf + l0);
     u32 a0 = v4.x, a1 = v4.y, a2 = v4.z, a3 = v4.w;
-    u32 v = P.mont(a2, wa);
+    u32 v = P.shoup(a2, wa.x, wa.y);
     a2 = P.sub(a0, v);
     a0 = P.add(a0, v);
-    v = P.mont(a3, wa);
+    v = P.shoup(a3, wa.x, wa.y);
     a3 = P.sub(a1, v);
     a1 = P.add(a1, v);
-    v = P.mont(a1, wb);
+    v = P.shoup(a1, wb.x, wb.y);
     x[0] = P.add(a0, v);
     x[1] = P.sub(a0, v);
-    v = P.mont(a3, wc);
+    v = P.shoup(a3, wc.x, wc.y);
     x[2] = P.add(a2, v);
     x[3] = P.sub(a2, v);
   };
   const u32 Q2 = 2 * PQ.m, Q4 = 4 * PQ.m, Q6 = 6 * PQ.m;
   // Lazy INTT_q passes: inputs below 4q, outputs below 4q (three reductions per unit).
-  auto inv_unit_lazy = [&](u32 w0, u32 w1, u32 w2, u32& a0, u32& a1, u32& a2, u32& a3) {
-    const u32 d01 = PQ.montl(a0 + Q4 - a1, w0);
+  auto inv_unit_lazy = [&](uint2 w0, uint2 w1, uint2 w2, u32& a0, u32& a1, u32& a2, u32& a3) {
+    const u32 d01 = PQ.shoupl(a0 + Q4 - a1, w0.x, w0.y);
     const u32 s01 = csub_by(a0 + a1, Q4);
-    const u32 d23 = PQ.montl(a2 + Q4 - a3, w1);
+    const u32 d23 = PQ.shoupl(a2 + Q4 - a3, w1.x, w1.y);
     const u32 s23 = csub_by(a2 + a3, Q4);
     a0 = csub_by(s01 + s23, Q4);
-    a2 = PQ.montl(s01 + Q4 - s23, w2);
+    a2 = PQ.shoupl(s01 + Q4 - s23, w2.x, w2.y);
     a1 = d01 + d23;
-    a3 = PQ.montl(d01 + Q2 - d23, w2);
+    a3 = PQ.shoupl(d01 + Q2 - d23, w2.x, w2.y);
   };
   auto inv_first_lazy = [&](u32 a0, u32 a1, u32 a2, u32 a3) {
-    inv_unit_lazy(iq[H + 2 * tid], iq[H + 2 * tid + 1], iq[H / 2 + tid], a0, a1, a2, a3);
+    inv_unit_lazy(inv_tw(fqs, PQ.m, H + 2 * tid), inv_tw(fqs, PQ.m, H + 2 * tid + 1), inv_tw(fqs, PQ.m, H / 2 + tid), a0,
+                  a1, a2, a3);
     *reinterpret_cast<uint4*>(buf + l0) = make_uint4(a0, a1, a2, a3);
   };
   auto inv_middle_lazy = [&]() {
@@ -421,7 +434,8 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 2)
       const int B = tid >> s, o = tid & (t - 1);
       const int e0 = B * 4 * t + o;
       u32 a0 = buf[e0], a1 = buf[e0 + t], a2 = buf[e0 + 2 * t], a3 = buf[e0 + 3 * t];
-      inv_unit_lazy(iq[m + 2 * B], iq[m + 2 * B + 1], iq[(m >> 1) + B], a0, a1, a2, a3);
+      inv_unit_lazy(inv_tw(fqs, PQ.m, m + 2 * B), inv_tw(fqs, PQ.m, m + 2 * B + 1), inv_tw(fqs, PQ.m, (m >> 1) + B), a0,
+                    a1, a2, a3);
       buf[e0] = a0;
       buf[e0 + t] = a1;
       buf[e0 + 2 * t] = a2;
@@ -430,19 +444,19 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 2)
     }
   };
   // Lazy NTT_q passes: inputs below 6q, outputs below 6q (two reductions per unit).
-  auto fwd_unit_lazy = [&](u32 wa, u32 wb, u32 wc, u32& a0, u32& a1, u32& a2, u32& a3) {
-    u32 v = PQ.montl(a2, wa);
+  auto fwd_unit_lazy = [&](uint2 wa, uint2 wb, uint2 wc, u32& a0, u32& a1, u32& a2, u32& a3) {
+    u32 v = PQ.shoupl(a2, wa.x, wa.y);
     a2 = a0 + Q2 - v;  // below 8q
     a0 = a0 + v;
-    v = PQ.montl(a3, wa);
+    v = PQ.shoupl(a3, wa.x, wa.y);
     a3 = a1 + Q2 - v;
     a1 = a1 + v;
     a0 = csub_by(a0, Q4);  // below 4q
-    v = PQ.montl(a1, wb);
+    v = PQ.shoupl(a1, wb.x, wb.y);
     a1 = a0 + Q2 - v;
     a0 = a0 + v;
     a2 = csub_by(a2, Q4);
-    v = PQ.montl(a3, wc);
+    v = PQ.shoupl(a3, wc.x, wc.y);
     a3 = a2 + Q2 - v;
     a2 = a2 + v;
   };
@@ -453,7 +467,7 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 2)
       const int i = tid / h, o = tid - i * h;
       const int e0 = i * 2 * t + o;
       u32 a0 = buf[e0], a1 = buf[e0 + h], a2 = buf[e0 + t], a3 = buf[e0 + t + h];
-      fwd_unit_lazy(fq[m + i], fq[2 * m + 2 * i], fq[2 * m + 2 * i + 1], a0, a1, a2, a3);
+      fwd_unit_lazy(fqs[m + i], fqs[2 * m + 2 * i], fqs[2 * m + 2 * i + 1], a0, a1, a2, a3);
       buf[e0] = a0;
       buf[e0 + h] = a1;
       buf[e0 + t] = a2;
@@ -474,9 +488,9 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 2)
       __syncthreads();
       inv_middle_lazy();
     } else {
-      inv_first(PQ, iq, cur[0], cur[1], cur[2], cur[3]);
+      inv_first(PQ, fqs, cur[0], cur[1], cur[2], cur[3]);
       __syncthreads();
-      inv_middle(PQ, iq);
+      inv_middle(PQ, fqs);
     }
     // INTT_q's last stage with 1/n, the lift to p, and NTT_p's first stage, pair (b, b + n/2).
     // The lift takes residues, so both products are reduced fully here.
@@ -486,24 +500,24 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 2)
       const u32 u = buf[b], v = buf[b + H];
       const u32 y0 = q_to_p(c, PQ.mont(u + v, c.lq.n_inv));
       const u32 y1 = q_to_p(c, PQ.mont(u + (LAZY ? Q4 : PQ.m) - v, c.lq.last));
-      const u32 z = PP.mont(y1, fp[1]);
+      const u32 z = PP.shoup(y1, fps[1].x, fps[1].y);
       buf[b] = PP.add(y0, z);
       buf[b + H] = PP.sub(y0, z);
     }
     __syncthreads();
-    fwd_middle(PP, fp);
+    fwd_middle(PP, fps);
     {
       u32 tp[4], y[4];
-      fwd_last(PP, fp, tp);
+      fwd_last(PP, fps, tp);
 #pragma unroll
       for (int k = 0; k < 4; k++) {
         accp[k] = PP.add(accp[k], PP.mont(tp[k], kp[tb[k]]));
         y[k] = PP.mont(tp[k], wp[tb[k]]);
       }
-      inv_first(PP, ip, y[0], y[1], y[2], y[3]);
+      inv_first(PP, fps, y[0], y[1], y[2], y[3]);
     }
     __syncthreads();
-    inv_middle(PP, ip);
+    inv_middle(PP, fps);
     // INTT_p's last stage with 1/n, the lift to q, and NTT_q's first stage.
 #pragma unroll
     for (int r = 0; r < 2; r++) {
@@ -512,12 +526,12 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 2)
       const u32 xp0 = PP.mont(u + v, c.lp.n_inv), xp1 = PP.mont(u + PP.m - v, c.lp.last);
       if constexpr (LAZY) {
         const u32 y0 = p_to_q_lazy(c, xp0);  // below 3q
-        const u32 z = PQ.montl(p_to_q_lazy(c, xp1), fq[1]);
+        const u32 z = PQ.shoupl(p_to_q_lazy(c, xp1), fqs[1].x, fqs[1].y);
         buf[b] = y0 + z;  // below 5q
         buf[b + H] = y0 + Q2 - z;
       } else {
         const u32 y0 = p_to_q(c, xp0), y1 = p_to_q(c, xp1);
-        const u32 z = PQ.mont(y1, fq[1]);
+        const u32 z = PQ.shoup(y1, fqs[1].x, fqs[1].y);
         buf[b] = PQ.add(y0, z);
         buf[b + H] = PQ.sub(y0, z);
       }
@@ -529,7 +543,7 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 2)
       constexpr int MF = 1 << (LOGN - 2);
       const uint4 v4 = *reinterpret_cast<const uint4*>(buf + l0);
       rq[0] = v4.x, rq[1] = v4.y, rq[2] = v4.z, rq[3] = v4.w;
-      fwd_unit_lazy(fq[MF + tid], fq[2 * MF + 2 * tid], fq[2 * MF + 2 * tid + 1], rq[0], rq[1], rq[2], rq[3]);
+      fwd_unit_lazy(fqs[MF + tid], fqs[2 * MF + 2 * tid], fqs[2 * MF + 2 * tid + 1], rq[0], rq[1], rq[2], rq[3]);
       // cur below 4q, rq below 6q: R_i = a S_i + (cur w_q - rq) / p lands below 4q, acc_q
       // stays below 2q.
 #pragma unroll
@@ -539,8 +553,8 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 2)
         cur[k] = PQ.montl(a[tb[k]], sv[k]) + PQ.montl(cq + Q6 - rq[k], c.p_inv_R);
       }
     } else {
-      fwd_middle(PQ, fq);
-      fwd_last(PQ, fq, rq);
+      fwd_middle(PQ, fqs);
+      fwd_last(PQ, fqs, rq);
 #pragma unroll
       for (int k = 0; k < 4; k++) {
         const u32 cq = PQ.mont(cur[k], wq[tb[k]]);
@@ -561,14 +575,14 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 2)
 #pragma unroll
   for (int k = 0; k < 4; k++) buf[l0 + k] = cur[k];
   __syncthreads();
-  inv32<LOGN>(buf, c.lq, iq);
+  inv32<LOGN>(buf, c.lq, c.lq.inv);
 #pragma unroll
   for (int k = 0; k < 4; k++) mask_out[(size_t)qi * N + tid + k * NT] = buf[tid + k * NT];
   __syncthreads();
 #pragma unroll
   for (int k = 0; k < 4; k++) buf[l0 + k] = accq[k];
   __syncthreads();
-  inv32<LOGN>(buf, c.lq, iq);
+  inv32<LOGN>(buf, c.lq, c.lq.inv);
   u32 xq[4];
 #pragma unroll
   for (int k = 0; k < 4; k++) xq[k] = buf[tid + k * NT];
@@ -576,7 +590,7 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 2)
 #pragma unroll
   for (int k = 0; k < 4; k++) buf[l0 + k] = accp[k];
   __syncthreads();
-  inv32<LOGN>(buf, c.lp, ip);
+  inv32<LOGN>(buf, c.lp, c.lp.inv);
 #pragma unroll
   for (int k = 0; k < 4; k++) {
     const int t = tid + k * NT;

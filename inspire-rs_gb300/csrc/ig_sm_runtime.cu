@@ -302,14 +302,29 @@ int ig_sm_server_create(ig_ctx* c, uint32_t ring_dim, uint32_t gamma, uint64_t q
   // last = mont(inv[1], n_inv) = inv[1] n_inv 2^-32
   dv.lq.last = dv.lq.p.mont(hq.inv[1], hq.n_inv);
   dv.lp.last = dv.lp.p.mont(hp.inv[1], hp.n_inv);
+  // The forward ladders as (w, floor(w 2^32 / m)) pairs for Shoup products.
+  auto shoup_ladder = [](const HostNtt32& T) {
+    std::vector<u32> v(2 * T.n);
+    for (size_t k = 0; k < T.n; k++) {
+      v[2 * k] = T.fwd_std[k];
+      v[2 * k + 1] = (u32)(((u64)T.fwd_std[k] << 32) / T.m);
+    }
+    return v;
+  };
+  const std::vector<u32> shq = shoup_ladder(hq), shp = shoup_ladder(hp);
+  const u32* shq_dev = nullptr;
+  const u32* shp_dev = nullptr;
   int rc;
   if ((rc = up(c, o, hq.fwd, &dv.lq.fwd)) || (rc = up(c, o, hq.inv, &dv.lq.inv)) || (rc = up(c, o, hp.fwd, &dv.lp.fwd)) ||
-      (rc = up(c, o, hp.inv, &dv.lp.inv)) || (rc = up(c, o, se, &dv.slot_exp)) || (rc = up(c, o, es, &dv.exp_slot)) ||
+      (rc = up(c, o, hp.inv, &dv.lp.inv)) || (rc = up(c, o, shq, &shq_dev)) || (rc = up(c, o, shp, &shp_dev)) ||
+      (rc = up(c, o, se, &dv.slot_exp)) || (rc = up(c, o, es, &dv.exp_slot)) ||
       (rc = up(c, o, gpow, &dv.gpow)) || (rc = up(c, o, cpow, &dv.cpow)) || (rc = up(c, o, mi, &dv.m_of_i)) ||
       (rc = up(c, o, pw, &dv.pow_root_R))) {
     for (auto& a2 : o.allocs) igint::dfree(c, a2.first, a2.second);
     return rc;
   }
+  dv.lq.fwd_sh = reinterpret_cast<const uint2*>(shq_dev);
+  dv.lp.fwd_sh = reinterpret_cast<const uint2*>(shp_dev);
   dv.inv_gamma_RR = (u32)((u128)powm(gamma, q - 2, q) * (u64)(((u128)1 << 64) % q) % q);
   dv.p_over_q = (u32)(special_prime / q);
   dv.neg_off = (u32)((q - special_prime % q) % q);
