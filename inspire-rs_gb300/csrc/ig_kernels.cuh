@@ -27,11 +27,12 @@ struct CrsDev {
   const u64* pow_root_R;     // w0^e * 2^64 mod q for e < 2n (w0 = slot 0's root)
   u64 inv_gamma_R, inv_gamma_Rp;  // gamma^-1 * 2^64 mod q, Shoup
   const u64* wmask_R;        // rows x n: NTT of the kept mask rows, R-form
-  // NTT of the last exact-gadget digit from the others (base^-2 (R - D0 - base D1)):
-  // the three constants in R-form, for one lazy Montgomery reduction.
+  // The last exact-gadget digit's factors (D2 = base^-2 (R - D0 - base D1)) in R-form:
+  // base^-2, -base^-2 and -base^-1, by which the key rows are folded (fold_gadget3).
   u64 ld_inv_R, ld_c0_R, ld_c1_R;
   // Galois keys of the automorphism tree (OnePacking), null when the CRS carries none:
-  // key i (t = n / 2^i + 1) as 3 rows of (a, b), each n words, R-form NTT.
+  // key i (t = n / 2^i + 1) as 3 rows of (a, b), each n words, R-form NTT, folded at
+  // upload (fold_gadget_keys) so the node stands in for the third digit.
   const u64* galois_R;
 };
 

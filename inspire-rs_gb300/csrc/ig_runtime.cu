@@ -715,7 +715,8 @@ int ig_crs_create(ig_ctx* c, uint32_t n, uint64_t q, uint64_t p, uint64_t gadget
   d.ninvp = shoup_companion(d.ninv);
   d.inv_gamma_R = mulmod(invmod(gamma), R_MOD_Q);
   d.inv_gamma_Rp = shoup_companion(d.inv_gamma_R);
-  // Last exact digit: base^-2 (R - D0 - base D1) (inspiring2.rs:1094-1161).
+  // Last exact digit: base^-2 (R - D0 - base D1) (inspiring2.rs:1094-1161). The kernels
+  // fold these three factors into the key rows (fold_gadget3) rather than form the digit.
   const u64 inv = invmod(1ULL << 40);
   d.ld_inv_R = mulmod(inv, R_MOD_Q);
   d.ld_c0_R = mulmod(negq(inv), R_MOD_Q);
