@@ -457,7 +457,7 @@ def run_gb300(args, rank, world):
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, same workload",
                      "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
                      "avg_launch_ms": scan_avg, "algorithmic_bytes_per_launch": scan_bytes},
-        "roofline_dominant": {"kernel": "respond (fused recursion + online gather)", "bound": "integer issue",
+        "roofline_dominant": {"kernel": "respond (fused recursion + online gather)", "bound": "integer multiply pipe",
                               "achieved": timed_gmodmul, "unit": "G modmul/s", "peak": peak_gmodmul,
                               "frac": timed_gmodmul / peak_gmodmul,
                               "peak_source": "measured in this run: lazy mod-q butterflies in registers "
