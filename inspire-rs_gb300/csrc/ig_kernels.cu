@@ -709,8 +709,6 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
     }
   }
   constexpr int MF = 1 << (LOGN - 2);
-  u64 wi, wip;
-  inv_twiddle(tw, twp, 1, wi, wip);
   const u64 wf = tw[1], wfp = twp[1];
 #pragma unroll 1
   for (int i = (int)gamma - 2; i >= 0; i--) {
@@ -775,9 +773,10 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
 #pragma unroll
     for (int j = 0; j < 2; j++) {
       const int b = tid + j * NT;
-      u64 x0 = X[sw(b)], x1 = X[sw(b + H)];
-      bf_inv4(x0, x1, wi, wip);
-      const u64 r0 = shoup(x0, c.ninv, c.ninvp), r1 = shoup(x1, c.ninv, c.ninvp);
+      const u64 x0 = X[sw(b)], x1 = X[sw(b + H)];
+      // The inverse's last stage and n^-1 as one product per output: n^-1 on the sum,
+      // n^-1 times the stage's twiddle on the difference.
+      const u64 r0 = shoup(x0 + x1, c.ninv, c.ninvp), r1 = shoup(x0 - x1 + 4 * Q, c.nlast, c.nlastp);
       u64 p0, p1, q0, q1;  // digits 0 and 1 of coefficients b and b + N/2
       if (exact) {
         p0 = r0 & DMASK;
@@ -1087,8 +1086,6 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
   const u64 fa = tw[MF + ug], fap = twp[MF + ug];
   const u64 fb = tw[2 * MF + 2 * ug], fbp = twp[2 * MF + 2 * ug];
   const u64 fc = tw[2 * MF + 2 * ug + 1], fcp = twp[2 * MF + 2 * ug + 1];
-  u64 wi, wip;
-  inv_twiddle(tw, twp, 1, wi, wip);
   const u64 wf = tw[1], wfp = twp[1];
 #pragma unroll 1
   for (int i = (int)gamma - 2; i >= 0; i--) {
@@ -1120,9 +1117,10 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
 #pragma unroll
       for (int j = 0; j < 2; j++) {
         const int b = tid + j * NT;
-        u64 x0 = lo[sw(b)], x1 = hi[sw(b)];
-        bf_inv4(x0, x1, wi, wip);
-        const u64 r0 = shoup(x0, c.ninv, c.ninvp), r1 = shoup(x1, c.ninv, c.ninvp);
+        const u64 x0 = lo[sw(b)], x1 = hi[sw(b)];
+        // The inverse's last stage and n^-1 as one product per output: n^-1 on the sum,
+        // n^-1 times the stage's twiddle on the difference.
+        const u64 r0 = shoup(x0 + x1, c.ninv, c.ninvp), r1 = shoup(x0 - x1 + 4 * Q, c.nlast, c.nlastp);
         u64 p0, p1, q0, q1;  // digits 0 and 1 of coefficients b and b + H
         if (exact) {
           p0 = r0 & DMASK;
@@ -1360,8 +1358,6 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
   const int l0 = 4 * tid;
   u64 ca[4], cb[4];  // the current node at slots l0..l0+3 (thread tid's transform unit)
   bool cur_zero = true;
-  u64 wi, wip;
-  inv_twiddle(tw, twp, 1, wi, wip);
   const u64 wf = tw[1], wfp = twp[1];
   constexpr int H = N / 2, MF = 1 << (LOGN - 2);
   // Leaf `start`: the column through the transform times NTT(a); its b-value on the side.
@@ -1495,9 +1491,10 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
 #pragma unroll
     for (int j = 0; j < 2; j++) {
       const int b = tid + j * NT;
-      u64 x0 = X[sw(b)], x1 = X[sw(b + H)];
-      bf_inv4(x0, x1, wi, wip);
-      const u64 r0 = shoup(x0, c.ninv, c.ninvp), r1 = shoup(x1, c.ninv, c.ninvp);
+      const u64 x0 = X[sw(b)], x1 = X[sw(b + H)];
+      // The inverse's last stage and n^-1 as one product per output: n^-1 on the sum,
+      // n^-1 times the stage's twiddle on the difference.
+      const u64 r0 = shoup(x0 + x1, c.ninv, c.ninvp), r1 = shoup(x0 - x1 + 4 * Q, c.nlast, c.nlastp);
       const u64 p0 = r0 & DMASK, p1 = (r0 >> 20) & DMASK, q0 = r1 & DMASK, q1 = (r1 >> 20) & DMASK;
       const u64 t0 = shoup_lazy4(q0, wf, wfp), t1 = shoup_lazy4(q1, wf, wfp);
       D[sw(b)] = p0 + t0;

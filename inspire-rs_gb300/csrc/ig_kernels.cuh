@@ -19,6 +19,7 @@ struct CrsDev {
   u32 n, logn, gamma, rows, approx;
   const u64 *tw, *twp;    // forward ladder psi^brv(m), Shoup companions (index m in [1, n))
   u64 ninv, ninvp;        // n^-1 mod q, Shoup
+  u64 nlast, nlastp;      // n^-1 times the inverse's last twiddle (q - tw[1]), Shoup
   const uint16_t* slot_exp;  // odd exponent e_t of slot t's root relative to slot 0's
   const uint16_t* exp_slot;  // slot holding exponent e, indexed e/2
   const u32* gpow;           // g^i mod 2n, i < gamma

@@ -713,6 +713,8 @@ int ig_crs_create(ig_ctx* c, uint32_t n, uint64_t q, uint64_t p, uint64_t gadget
   }
   d.ninv = invmod(n);
   d.ninvp = shoup_companion(d.ninv);
+  d.nlast = mulmod(d.ninv, negq(tw[1]));
+  d.nlastp = shoup_companion(d.nlast);
   d.inv_gamma_R = mulmod(invmod(gamma), R_MOD_Q);
   d.inv_gamma_Rp = shoup_companion(d.inv_gamma_R);
   // Last exact digit: base^-2 (R - D0 - base D1) (inspiring2.rs:1094-1161). The kernels
