@@ -658,8 +658,9 @@ __device__ __forceinline__ int sw(int e) { return e ^ (((e >> 4) & 3) << 2); }
 // The inverse's first two stages and the forward's last two act within each thread's unit
 // and run in registers; the inverse's last stage, n^-1, the digit split and the forward's
 // first stage fuse into one pass. Digits 0 and 1 are transformed; with the exact gadget
-// digit 2's transform comes from them, D_2 = base^-2 (R_{i+1} - D_0 - base D_1)
-// (inspiring2.rs:1094-1161).
+// digit 2's transform is D_2 = base^-2 (R_{i+1} - D_0 - base D_1) (inspiring2.rs:1094-1161),
+// a fixed linear combination, so the key rows are folded at staging (fold_gadget3) and
+// R_{i+1} takes digit 2's place in the sums.
 template <int LOGN>
 __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
     k_respond(CrsDev c, const QueryDev* queries, const ShardDev* shards, const u64* b_fold, u64 ms_target,
@@ -1308,9 +1309,10 @@ __global__ void k_nopack_sum(u32 n, u32 gamma, u64* out) {
 //
 // Nodes live in the NTT domain: y O is a product by NTT(X^s), tau_t a slot permutation,
 // and only the key switch's digit split needs coefficients: a = INTT(tau_t(...).a), digits
-// 0 and 1 (base 2^20) transformed, digit 2's transform derived as base^-2 (a - D0 - base D1)
-// (the unsigned split of rgsw/external_product.rs:58-99 leaves a = D0 + base D1 + base^2 D2
-// exactly). Key rows are R-form NTT, so each sum of three products takes one reduction.
+// 0 and 1 (base 2^20) transformed, digit 2's transform base^-2 (a - D0 - base D1) (the
+// unsigned split of rgsw/external_product.rs:58-99 leaves a = D0 + base D1 + base^2 D2
+// exactly), which the keys' folded rows (fold_gadget_keys) take from a itself. Key rows
+// are R-form NTT, so each sum of three products takes one reduction.
 //
 // The walk is the recursion's depth-first order: leaf k of the walk is start = bitrev(k),
 // and a binary-counter carry combines each finished node with its waiting sibling; the
