@@ -52,7 +52,8 @@ struct Ntt32Dev {
   const u32* fwd;
   const u32* inv;
   const uint2* fwd_sh;  // the forward ladder in standard form with Shoup companions (w, w')
-  u32 n_inv, last;
+  u32 n_inv, last;      // Montgomery form: 1/n, and 1/n times the inverse's last twiddle
+  u32 n_inv_s, n_inv_sp, last_s, last_sp;  // the same two in standard form with companions
 };
 
 struct SmDev {

@@ -498,8 +498,8 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 2)
     for (int r = 0; r < 2; r++) {
       const int b = tid + r * NT;
       const u32 u = buf[b], v = buf[b + H];
-      const u32 y0 = q_to_p(c, PQ.mont(u + v, c.lq.n_inv));
-      const u32 y1 = q_to_p(c, PQ.mont(u + (LAZY ? Q4 : PQ.m) - v, c.lq.last));
+      const u32 y0 = q_to_p(c, PQ.shoup(u + v, c.lq.n_inv_s, c.lq.n_inv_sp));
+      const u32 y1 = q_to_p(c, PQ.shoup(u + (LAZY ? Q4 : PQ.m) - v, c.lq.last_s, c.lq.last_sp));
       const u32 z = PP.shoup(y1, fps[1].x, fps[1].y);
       buf[b] = PP.add(y0, z);
       buf[b + H] = PP.sub(y0, z);
@@ -523,7 +523,8 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 2)
     for (int r = 0; r < 2; r++) {
       const int b = tid + r * NT;
       const u32 u = buf[b], v = buf[b + H];
-      const u32 xp0 = PP.mont(u + v, c.lp.n_inv), xp1 = PP.mont(u + PP.m - v, c.lp.last);
+      const u32 xp0 = PP.shoup(u + v, c.lp.n_inv_s, c.lp.n_inv_sp);
+      const u32 xp1 = PP.shoup(u + PP.m - v, c.lp.last_s, c.lp.last_sp);
       if constexpr (LAZY) {
         const u32 y0 = p_to_q_lazy(c, xp0);  // below 3q
         const u32 z = PQ.shoupl(p_to_q_lazy(c, xp1), fqs[1].x, fqs[1].y);

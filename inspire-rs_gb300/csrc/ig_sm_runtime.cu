@@ -302,6 +302,18 @@ int ig_sm_server_create(ig_ctx* c, uint32_t ring_dim, uint32_t gamma, uint64_t q
   // last = mont(inv[1], n_inv) = inv[1] n_inv 2^-32
   dv.lq.last = dv.lq.p.mont(hq.inv[1], hq.n_inv);
   dv.lp.last = dv.lp.p.mont(hp.inv[1], hp.n_inv);
+  // Standard-form Shoup pairs of the same: 1/n, and 1/n (m - fwd[1]) (the inverse's last
+  // twiddle is the negated second forward one).
+  for (Ntt32Dev* T : {&dv.lq, &dv.lp}) {
+    const HostNtt32& H = T == &dv.lq ? hq : hp;
+    const u64 m = H.m;
+    const u64 ninv = powm(H.n % m, m - 2, m);
+    const u64 last = ninv * ((m - H.fwd_std[1]) % m) % m;
+    T->n_inv_s = (u32)ninv;
+    T->n_inv_sp = (u32)((ninv << 32) / m);
+    T->last_s = (u32)last;
+    T->last_sp = (u32)((last << 32) / m);
+  }
   // The forward ladders as (w, floor(w 2^32 / m)) pairs for Shoup products.
   auto shoup_ladder = [](const HostNtt32& T) {
     std::vector<u32> v(2 * T.n);
