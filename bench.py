@@ -690,6 +690,92 @@ def run_tree(args, rank, world):
 
 
 # ------------------------------------------------------------------------------------
+# NoPacking (respond / respond_seeded, respond.rs:614-643, 1229-1237): the served-batch
+# database, batches of 16 seeded queries through the C ABI with host buffers. A response
+# is gamma + 1 ciphertexts (8.4 MB at gamma 256), so the batch is small.
+NOPACK_METRIC = "NoPacking respond queries/s (batch 16, d2048, 512 B records, 2^20 records)"
+
+
+def run_nopack(args, rank, world):
+    import threading
+
+    import torch
+
+    from __graft_entry__ import _package
+    pkg = _package()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    ctx = pkg.Context(local)
+    g = torch.Generator(device="cuda")
+    g.manual_seed(1 + rank)
+    rng = np.random.default_rng(3000 + rank)
+    crs = pkg.ServerCrs(pkg.InspireParams.d2048(), rng.integers(0, 256, 32, dtype=np.uint8).tobytes(), GAMMA)
+    cache = pkg.ServerInspiringCache.new(crs, ctx=ctx)
+    db = pkg.EncodedDatabase(cache, args.shards)
+    for s in range(args.shards):
+        cols = torch.randint(0, 1 << 16, (GAMMA, N_RING), generator=g, device="cuda", dtype=torch.int64)
+        torch.cuda.current_stream().synchronize()
+        db.set_shard_device(s, cols.data_ptr())
+    B = 16
+    total = args.warmup + args.steps
+    sids = [np.ascontiguousarray(rng.integers(0, args.shards, B), dtype=np.uint32) for _ in range(total)]
+    seeds = [np.frombuffer(rng.bytes(32 * B), dtype=np.uint8).copy() for _ in range(total)]
+    bs = [rand_words(rng, (B, N_RING)) for _ in range(total)]
+    # Caller threads over as many lanes, as a server's worker pool would issue the calls;
+    # each lands its responses in its own pinned host buffer.
+    T = max(1, args.lanes)
+    ctx.set_lanes(T)
+    outs = [torch.empty((B, GAMMA + 1, 2, N_RING), dtype=torch.int64, pin_memory=True) for _ in range(T)]
+    lib = ctx._lib
+
+    def step(i, t):
+        ctx.check(lib.ig_respond_nopacking_batch(ctx.h, db.h, B, sids[i].ctypes.data, seeds[i].ctypes.data, None,
+                                                 bs[i].ctypes.data, outs[t].data_ptr()))
+
+    def run(lo, hi):
+        errors = []
+
+        def caller(t):
+            try:
+                for i in range(lo + t, hi, T):
+                    step(i, t)
+            except Exception as e:
+                errors.append(e)
+        threads = [threading.Thread(target=caller, args=(t,)) for t in range(T)]
+        for th in threads:
+            th.start()
+        for th in threads:
+            th.join()
+        if errors:
+            raise errors[0]
+
+    run(0, args.warmup)
+    launches0 = ctx.launch_count
+    barrier(world)
+    with ClockSampler(local) as clk:
+        torch.cuda.profiler.start()
+        t0 = time.perf_counter()
+        run(args.warmup, total)
+        el = max_over_ranks(time.perf_counter() - t0, world)
+        torch.cuda.profiler.stop()
+    ctx.set_lanes(1)
+    value = world * B * args.steps / el
+    return {
+        "metric": NOPACK_METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u64 (exact mod q = 2^60-2^14+1)",
+        "data": "synthetic: uniform 16-bit column words, uniform query words",
+        "config": {"workload": "d2048 NoPacking, 512-byte records x 2^20 (512 shards, gamma 256), batch 16, "
+                               "seeded queries", "shards": args.shards, "batch": B, "callers": T, "lanes": T},
+        "e2e": {"value": value, "unit": "queries/s", "h2d_bytes_per_step": B * (32 + N_RING * 8 + 4),
+                "d2h_bytes_per_step": B * (GAMMA + 1) * 2 * N_RING * 8,
+                "note": "host buffers in and out (responses into pinned memory): one ig_respond_nopacking_batch "
+                        "call per step, from the caller threads"},
+        "gpu_launches": int(ctx.launch_count - launches0), "clocks": clk.summary(),
+    }
+
+
+# ------------------------------------------------------------------------------------
 # Mixed databases: 32 B x 2^22 (gamma 16, 2048 shards), 512 B x 2^20 (gamma 256, 512
 # shards), 2048 B x 2^18 (gamma 1024, 128 shards), each under the exact and the approximate
 # gadget (six parameter sets), 128 keys spread over the sets, batch sizes drawn from
@@ -981,11 +1067,11 @@ def main():
                          "caller threads and serving slots of the host-buffer legs (default: 4 for the served "
                          "batch of 64 and the serving sweep, 3 otherwise; the measured optimum of each)")
     ap.add_argument("--workload", default="served-batch",
-                    choices=["served-batch", "special-modulus", "mixed", "serving-sweep", "one-packing"],
+                    choices=["served-batch", "special-modulus", "mixed", "serving-sweep", "one-packing", "no-packing"],
                     help="served-batch: the InspiRING batch of 64 over 2^20 records (the headline); special-modulus: "
                          "the special_modulus batch of 256; mixed: six parameter sets and batch sizes 1-512; "
                          "serving-sweep: the serving loop over 16,384 shards and 1000 seats; one-packing: the "
-                         "tree responder, batches of 152")
+                         "tree responder, batches of 152; no-packing: the NoPacking responder, batches of 16")
     ap.add_argument("--requests", type=int, default=16384, help="trace length of the serving sweep")
     ap.add_argument("--shards", type=int, default=NUM_SHARDS,
                     help="shards in the database (smaller values only for profiling captures)")
@@ -995,7 +1081,8 @@ def main():
         args.lanes = 4 if args.workload in ("served-batch", "serving-sweep") else 3
     if args.steps is None:
         args.steps = 20 if args.impl == "reference" else {"served-batch": 300, "special-modulus": 100, "mixed": 60,
-                                                          "serving-sweep": 0, "one-packing": 20}[args.workload]
+                                                          "serving-sweep": 0, "one-packing": 20,
+                                                          "no-packing": 300}[args.workload]
     rank, world = dist_setup(args.gpus)
     if args.impl == "reference":
         if rank != 0:
@@ -1010,6 +1097,11 @@ def main():
         return
     if args.workload == "one-packing":
         line = run_tree(args, rank, world)
+        if rank == 0:
+            print(json.dumps(line))
+        return
+    if args.workload == "no-packing":
+        line = run_nopack(args, rank, world)
         if rank == 0:
             print(json.dumps(line))
         return

@@ -60,3 +60,34 @@ def test_nopacking_single_column_ring256(pkg, oracle):
     assert r.to_binary() == oracle.response_bytes_full(want)
     assert len(r.column_ciphertexts) == 1
     assert (r.a == r.column_ciphertexts[0][0]).all() and (r.b == r.column_ciphertexts[0][1]).all()
+
+
+def test_nopacking_concurrent_callers_over_lanes(pkg, oracle):
+    """Three caller threads over three lanes (each call holds a lane and copies its
+    ciphertexts out after releasing the context lock) give the one-lane answers."""
+    import threading
+    P = oracle.Params.d2048()
+    ctx = pkg.Context.default()
+    cell, crs, db, _ = setup(pkg, oracle, P, 64, 0x4E52)
+    batches = [[pkg.SeededBatchQuery(*cell.next_query((7 * j + 3 * i) % (2 * P.n))) for i in range(3)]
+               for j in range(6)]
+    want = [[r.to_binary() for r in pkg.respond_nopacking_batch(crs, db, b)] for b in batches]
+    got = [None] * len(batches)
+    errors = []
+    ctx.set_lanes(3)
+    try:
+        def caller(t):
+            try:
+                for j in range(t, len(batches), 3):
+                    got[j] = [r.to_binary() for r in pkg.respond_nopacking_batch(crs, db, batches[j])]
+            except Exception as e:
+                errors.append(e)
+        threads = [threading.Thread(target=caller, args=(t,)) for t in range(3)]
+        for th in threads:
+            th.start()
+        for th in threads:
+            th.join()
+    finally:
+        ctx.set_lanes(1)
+    assert not errors, errors
+    assert got == want
