@@ -639,6 +639,8 @@ TREE_METRIC = "OnePacking respond queries/s (batch 152, d2048, 512 B records, 2^
 
 
 def run_tree(args, rank, world):
+    import threading
+
     import torch
 
     from __graft_entry__ import _package
@@ -663,17 +665,37 @@ def run_tree(args, rank, world):
     total = args.warmup + args.steps
     batches = [[pkg.SeededBatchQuery(int(rng.integers(0, args.shards)), rng.bytes(32), rand_words(rng, N_RING))
                 for _ in range(B)] for _ in range(total)]
-    for i in range(args.warmup):
-        pkg.respond_one_packing_batch(crs, db, batches[i])
+    # Caller threads over as many lanes, as a server's worker pool would issue the calls.
+    T = max(1, args.lanes)
+    ctx.set_lanes(T)
+
+    def run(lo, hi):
+        errors = []
+
+        def caller(t):
+            try:
+                for i in range(lo + t, hi, T):
+                    pkg.respond_one_packing_batch(crs, db, batches[i])
+            except Exception as e:
+                errors.append(e)
+        threads = [threading.Thread(target=caller, args=(t,)) for t in range(T)]
+        for th in threads:
+            th.start()
+        for th in threads:
+            th.join()
+        if errors:
+            raise errors[0]
+
+    run(0, args.warmup)
     launches0 = ctx.launch_count
     barrier(world)
     with ClockSampler(local) as clk:
         torch.cuda.profiler.start()
         t0 = time.perf_counter()
-        for i in range(args.warmup, total):
-            pkg.respond_one_packing_batch(crs, db, batches[i])
+        run(args.warmup, total)
         el = max_over_ranks(time.perf_counter() - t0, world)
         torch.cuda.profiler.stop()
+    ctx.set_lanes(1)
     value = world * B * args.steps / el
     return {
         "metric": TREE_METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
@@ -681,10 +703,11 @@ def run_tree(args, rank, world):
         "vs_baseline": None, "dtype": "u64 (exact mod q = 2^60-2^14+1)",
         "data": "synthetic: uniform 16-bit column words, uniform query words and Galois-key words",
         "config": {"workload": "d2048 OnePacking, 512-byte records x 2^20 (512 shards, gamma 256), batch 152, "
-                               "unswitched", "shards": args.shards, "batch": B},
+                               "unswitched", "shards": args.shards, "batch": B, "callers": T, "lanes": T},
         "e2e": {"value": value, "unit": "queries/s", "h2d_bytes_per_step": B * (32 + N_RING * 8 + 4),
                 "d2h_bytes_per_step": B * 2 * N_RING * 8,
-                "note": "host buffers in and out: one respond_one_packing_batch call per step"},
+                "note": "host buffers in and out: one respond_one_packing_batch call per step, from the caller "
+                        "threads"},
         "gpu_launches": int(ctx.launch_count - launches0), "clocks": clk.summary(),
     }
 

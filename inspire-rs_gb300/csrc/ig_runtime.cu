@@ -1643,7 +1643,13 @@ int ig_respond_one_packing_batch(ig_ctx* c, uint64_t dbh, uint32_t count, const 
   if (!c) return IG_ERR_ARG;
   if (count == 0 || !shard_ids || (!seeds && !as) || !bs || !a_out || !b_out)
     return fail(c, IG_ERR_ARG, "respond_one_packing: empty batch or null buffer");
-  std::lock_guard<std::mutex> lk(c->mu);
+  // As respond_seeded_batch: the call holds one lane (stream and scratch, the node stacks
+  // included) while its batch runs, takes the context lock only to validate and launch, and
+  // copies the responses to the caller's buffers after releasing it.
+  igint::HostCall hc;
+  igint::host_call_begin(c, hc);
+  const u32 k = hc.k;
+  std::unique_lock<std::mutex> lk(c->mu);
   cudaSetDevice(c->device);
   DbObj* db = get_db(c, dbh);
   if (!db) return fail(c, IG_ERR_HANDLE, "unknown database handle %llu", (unsigned long long)dbh);
@@ -1673,14 +1679,23 @@ int ig_respond_one_packing_batch(ig_ctx* c, uint64_t dbh, uint32_t count, const 
   }
   const size_t seed_bytes = as ? (size_t)count * n * 8 : (size_t)count * 32;
   void *d_table, *d_q, *d_seeds, *d_bs, *d_stack, *d_a, *d_b, *d_status;
+  auto lane_scratch = [&](const char* name, size_t bytes, void** p) {
+    char full[48];
+    snprintf(full, sizeof full, "%s%u", name, k);
+    return scratch(c, full, bytes, p);
+  };
   int rc;
-  if ((rc = scratch(c, "tr_table", table.size() * sizeof(ShardDev), &d_table)) ||
-      (rc = scratch(c, "tr_queries", count * sizeof(QueryDev), &d_q)) ||
-      (rc = scratch(c, "tr_seeds", seed_bytes, &d_seeds)) || (rc = scratch(c, "tr_bs", (size_t)count * n * 8, &d_bs)) ||
-      (rc = scratch(c, "tr_stack", (size_t)count * o.logn * 2 * n * 8, &d_stack)) ||
-      (rc = scratch(c, "tr_a", (size_t)count * n * 8, &d_a)) || (rc = scratch(c, "tr_b", (size_t)count * n * 8, &d_b)) ||
-      (rc = scratch(c, "tr_status", count * 4, &d_status)))
+  if ((rc = lane_scratch("tr_table", table.size() * sizeof(ShardDev), &d_table)) ||
+      (rc = lane_scratch("tr_queries", count * sizeof(QueryDev), &d_q)) ||
+      (rc = lane_scratch("tr_seeds", seed_bytes, &d_seeds)) ||
+      (rc = lane_scratch("tr_bs", (size_t)count * n * 8, &d_bs)) ||
+      (rc = lane_scratch("tr_stack", (size_t)count * o.logn * 2 * n * 8, &d_stack)) ||
+      (rc = lane_scratch("tr_a", (size_t)count * n * 8, &d_a)) ||
+      (rc = lane_scratch("tr_b", (size_t)count * n * 8, &d_b)) || (rc = lane_scratch("tr_status", count * 4, &d_status)))
     return rc;
+  void* pin;
+  if ((rc = igint::host_call_pinned(c, hc, (size_t)count * 4, &pin))) return rc;
+  const u32* h_status = (const u32*)pin;
   std::vector<QueryDev> qs(count);
   for (u32 i = 0; i < count; i++) {
     qs[i].shard = local[shard_ids[i]];
@@ -1690,24 +1705,27 @@ int ig_respond_one_packing_batch(ig_ctx* c, uint64_t dbh, uint32_t count, const 
     qs[i].b = (const u64*)d_bs + (size_t)i * n;
     qs[i].seat_R = nullptr;
   }
-  cudaStream_t s = c->stream;
   if ((rc = stage_h2d(c, d_table, table.data(), table.size() * sizeof(ShardDev))) ||
       (rc = stage_h2d(c, d_q, qs.data(), count * sizeof(QueryDev))) ||
       (rc = stage_h2d(c, d_seeds, as ? (const void*)as : (const void*)seeds, seed_bytes)) ||
-      (rc = stage_h2d(c, d_bs, bs, (size_t)count * n * 8)))
+      (rc = stage_h2d(c, d_bs, bs, (size_t)count * n * 8)) || (rc = igint::host_call_enter(c, hc)))
     return rc;
+  cudaStream_t s = igint::host_call_stream(c, hc);
   IG_CUDA(c, cudaMemsetAsync(d_status, 0, count * 4, s));
   IG_CUDA(c, igk::tree(o.dev, (const QueryDev*)d_q, (const ShardDev*)d_table, count, R_MOD_Q, ms_target,
                        (u64*)d_stack, (u64*)d_a, (u64*)d_b, (u32*)d_status, s));
   c->launches++;
-  std::vector<u32> status(count);
-  IG_CUDA(c, cudaMemcpyAsync(status.data(), d_status, count * 4, cudaMemcpyDeviceToHost, s));
-  IG_CUDA(c, cudaStreamSynchronize(s));
+  IG_CUDA(c, cudaMemcpyAsync((void*)h_status, d_status, count * 4, cudaMemcpyDeviceToHost, s));
+  if ((rc = igint::host_call_launched(c, hc))) return rc;
+  lk.unlock();  // other callers launch while this batch runs and copies out
+  // The lane's stream and scratch stay this call's until it returns (the lane lock).
+  cudaError_t e = cudaMemcpyAsync(a_out, d_a, (size_t)count * n * 8, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(b_out, d_b, (size_t)count * n * 8, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess)
+    return fail(c, IG_ERR_CUDA, "respond_one_packing: copy of the responses failed: %s", cudaGetErrorString(e));
   for (u32 i = 0; i < count; i++)
-    if (status[i]) return fail(c, IG_ERR_DEVICE, "query %u: tree kernel status %u", i, status[i]);
-  IG_CUDA(c, cudaMemcpyAsync(a_out, d_a, (size_t)count * n * 8, cudaMemcpyDeviceToHost, s));
-  IG_CUDA(c, cudaMemcpyAsync(b_out, d_b, (size_t)count * n * 8, cudaMemcpyDeviceToHost, s));
-  IG_CUDA(c, cudaStreamSynchronize(s));
+    if (h_status[i]) return fail(c, IG_ERR_DEVICE, "query %u: tree kernel status %u", i, h_status[i]);
   return IG_OK;
 }
 

@@ -90,3 +90,35 @@ def test_refusals(pkg, oracle):
     cache.set_galois_keys(keys)
     r = pkg.respond_seeded_packed(crs, db, pkg.SeededBatchQuery(sid, seed, b))
     assert cell.decode_tree(0, r.a, r.b)[0]
+
+
+def test_concurrent_callers_over_lanes(pkg, oracle):
+    """Three caller threads over three lanes (each call holds a lane with its node stacks
+    and copies its responses out after releasing the context lock) give the one-lane
+    answers."""
+    import threading
+    P = oracle.Params(n=256)
+    ctx = pkg.Context.default()
+    cell, keys, crs, db, _ = setup(pkg, oracle, P, 64, 0x7EE5)
+    batches = [[pkg.SeededBatchQuery(*cell.next_query((11 * j + 5 * i) % (2 * P.n))) for i in range(4)]
+               for j in range(6)]
+    want = [[r.to_binary() for r in pkg.respond_one_packing_batch(crs, db, b)] for b in batches]
+    got = [None] * len(batches)
+    errors = []
+    ctx.set_lanes(3)
+    try:
+        def caller(t):
+            try:
+                for j in range(t, len(batches), 3):
+                    got[j] = [r.to_binary() for r in pkg.respond_one_packing_batch(crs, db, batches[j])]
+            except Exception as e:
+                errors.append(e)
+        threads = [threading.Thread(target=caller, args=(t,)) for t in range(3)]
+        for th in threads:
+            th.start()
+        for th in threads:
+            th.join()
+    finally:
+        ctx.set_lanes(1)
+    assert not errors, errors
+    assert got == want
