@@ -61,7 +61,11 @@ int ig_ctx_set_pair_threshold(ig_ctx* ctx, uint32_t max_queries);
  * scratch, so a batch's scan and recursion overlap the batches before it and batches of
  * fewer queries than SMs still fill the GPU. Each call's work starts after everything
  * queued on the context stream before it; call ig_ctx_join before reading a lane's
- * outputs on the context stream. Responses are identical for any lane count. */
+ * outputs on the context stream. The host-buffer calls (ig_respond_seeded_batch,
+ * ig_respond_one_packing_batch, ig_respond_nopacking_batch, ig_sm_respond_batch) each hold
+ * one lane while their batch runs and take the context lock only to validate and launch,
+ * so calls from several threads overlap on the device. Responses are identical for any
+ * lane count. */
 int ig_ctx_set_lanes(ig_ctx* ctx, uint32_t lanes);
 /* Orders the context stream after all work queued on the lanes. */
 int ig_ctx_join(ig_ctx* ctx);
