@@ -456,7 +456,11 @@ def run_gb300(args, rank, world):
                      "traffic": SCAN_TRAFFIC_BYTES if args.shards == NUM_SHARDS else None,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, same workload",
                      "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
-                     "avg_launch_ms": scan_avg, "algorithmic_bytes_per_launch": scan_bytes},
+                     "avg_launch_ms": scan_avg, "algorithmic_bytes_per_launch": scan_bytes,
+                     "note": "the HBM-facing kernel, 1.3% of the device time; its rate is set by its multiply "
+                             "pipe (four 32x32->64 products per 16-bit word against the 61-bit tag key and "
+                             "60-bit b) and, at 64 queries a launch, by a fixed cost of about 13 us; the "
+                             "dominant kernel is in roofline_dominant"},
         "roofline_dominant": {"kernel": "respond (fused recursion + online gather)", "bound": "integer multiply pipe",
                               "achieved": timed_gmodmul, "unit": "G modmul/s", "peak": peak_gmodmul,
                               "frac": timed_gmodmul / peak_gmodmul,
