@@ -167,18 +167,21 @@ int ig_respond_seeded_batch_device(ig_ctx* ctx, uint64_t db, uint64_t store, uin
 
 /* Allocation-free form of ig_respond_seeded_batch_device, with no counterpart in the
  * reference. For callers that must not have the library allocate device memory while
- * serving: servers that size every device buffer at start-up, processes that record their
- * launches into a CUDA graph, GPUs shared under a memory cap. The call's scratch (fold of
- * b, query descriptors, status words) lives in one fixed device array of 527,104 bytes
- * that every GPU loading the library holds until the process exits; the call makes no
- * cudaMalloc/cudaFree and no other allocating call. Limits: at most 64 queries per call,
- * gamma at most 1024, a registered seat (handle) and packing stores on the queried
- * shards; larger batches are refused with IG_ERR_ARG. The first call on a device resolves
- * the array's device address (cudaGetSymbolAddress) and should come before any stream
- * capture. All calls share the array, so calls that overlap on the GPU (from different
- * contexts of one device) race and must be serialised by the caller. Inputs and outputs
- * are device pointers as in ig_respond_seeded_batch_device; the call returns after the
- * batch completes, with a refused batch reported as in ig_respond_seeded_batch. */
+ * serving: servers that size every device buffer at start-up and refuse growth later,
+ * and processes sharing a GPU under a memory cap, where an allocation on the request path
+ * can fail or evict a neighbour. The call's scratch (fold of b, query descriptors, status
+ * words) lives in one fixed device array of 527,104 bytes that every GPU loading the
+ * library holds until the process exits; the call makes no cudaMalloc/cudaFree and no
+ * other allocating call. Limits: at most 64 queries per call, gamma at most 1024, a
+ * registered seat (handle) and packing stores on the queried shards; larger batches are
+ * refused with IG_ERR_ARG before any work. The first call on a device resolves the
+ * array's device address (cudaGetSymbolAddress); make that first call before any stream
+ * capture. All calls share the array, and it keeps the last call's contents: calls that
+ * overlap on the GPU (from different contexts of one device) race and must be serialised
+ * by the caller. Inputs and outputs are device pointers as in
+ * ig_respond_seeded_batch_device. The call blocks: it synchronises the context stream,
+ * reads the batch's status words back and returns after the batch completes, with a
+ * refused batch reported as in ig_respond_seeded_batch. */
 int ig_respond_seeded_batch_noalloc(ig_ctx* ctx, uint64_t db, uint64_t store, uint64_t handle, uint32_t count,
                                     const uint32_t* shard_ids, const uint8_t* d_seeds, const uint64_t* d_bs,
                                     uint64_t mod_switch_target, uint64_t* d_a_out, uint64_t* d_b_out);

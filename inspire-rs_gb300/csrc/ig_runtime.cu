@@ -2218,11 +2218,12 @@ extern "C" {
 
 // ---- allocation-free respond --------------------------------------------------------------
 // Some embedders cannot let a library allocate device memory on a request path: servers
-// that pre-size every device buffer at start-up and refuse growth afterwards, processes
-// that capture their launch sequence into a graph, and memory-capped GPU partitions shared
-// with other jobs. For them the batch respond has a variant whose scratch (the per-query
-// fold of b, the query descriptors and the status words) lives in one file-scope device
-// array of fixed size. Every GPU that loads the library holds this array until exit.
+// that pre-size every device buffer at start-up and refuse growth afterwards, and
+// memory-capped GPU partitions shared with other jobs, where a late allocation can fail.
+// For them the batch respond has a variant whose scratch (the per-query fold of b, the
+// query descriptors and the status words) lives in one file-scope device array of fixed
+// size. Every GPU that loads the library holds this array until exit. The call blocks
+// until its batch completes (it reads the status words back).
 enum : u32 { NOALLOC_MAX_QUERIES = 64, NOALLOC_MAX_GAMMA = 1024 };
 static constexpr size_t NOALLOC_FOLD_BYTES = (size_t)NOALLOC_MAX_QUERIES * NOALLOC_MAX_GAMMA * 8;
 static constexpr size_t NOALLOC_QUERY_OFF = NOALLOC_FOLD_BYTES;
@@ -2303,8 +2304,9 @@ int ig_respond_seeded_batch_noalloc(ig_ctx* c, uint64_t dbh, uint64_t st, uint64
   IG_CUDA(c, cudaMemcpyAsync(d_q, qs, count * sizeof(QueryDev), cudaMemcpyHostToDevice, s));
   IG_CUDA(c, cudaMemsetAsync(d_status, 0, count * 4, s));
   IG_CUDA(c, igk::shard_scan(o.dev, d_q, db->d_table, count, d_fold, d_status, 0, nullptr, s));
+  // The launch shape of ig_respond_seeded_batch_device for the same batch and lane count.
   IG_CUDA(c, igk::respond(o.dev, d_q, db->d_table, count, d_fold, ms_target, d_a, d_b, d_status, c->force_serial,
-                          count <= c->pair_threshold, s));
+                          (u64)count * c->lanes <= c->pair_threshold, s));
   c->launches += 2;
   u32 status[NOALLOC_MAX_QUERIES];
   IG_CUDA(c, cudaMemcpyAsync(status, d_status, count * 4, cudaMemcpyDeviceToHost, s));

@@ -1,13 +1,14 @@
 """The allocation-free respond entry point, checked against the allocating one.
 
 ig_respond_seeded_batch_noalloc exists for embedders that cannot let a library allocate
-device memory while it serves: servers that size every device buffer once at start-up,
-processes that record their launch sequence into a CUDA graph, and GPUs shared with other
-jobs under a memory cap. Its scratch is one fixed device array inside the library. This
-test calls it through the C ABI twice in a row (the array keeps the previous call's
-contents between calls) and requires the bytes of ig_respond_seeded_batch_device, exactly:
-the arithmetic is integer mod q, so the tolerance is zero. It lives in its own file so that
-pytest collects it last.
+device memory while it serves: servers that size every device buffer once at start-up and
+refuse growth later, and GPUs shared with other jobs under a memory cap, where a late
+allocation can fail. Its scratch is one fixed device array inside the library. This test
+calls it through the C ABI twice in a row (the array keeps the previous call's contents
+between calls) and requires the bytes of ig_respond_seeded_batch_device, exactly: the
+arithmetic is integer mod q, so the tolerance is zero. Around each call the context's
+allocation injector is armed, so any device allocation the call made would refuse it. It
+lives in its own file so that pytest collects it last.
 """
 import ctypes
 
@@ -62,15 +63,35 @@ def test_noalloc_matches_allocating_entry_point_on_two_calls():
             ctx.h, db.h, store.h, int(handle), count, shard_ids.ctypes.data, seeds.data_ptr(), bs.data_ptr(), ms,
             a_ref.data_ptr(), b_ref.data_ptr(), status.data_ptr()))
         torch.cuda.synchronize()
-        ctx.check(noalloc(ctx.h, db.h, store.h, int(handle), count, shard_ids.ctypes.data, seeds.data_ptr(),
-                          bs.data_ptr(), ms, a_new.data_ptr(), b_new.data_ptr()))
+        # The next device allocation of this context fails: the call must not make one.
+        ctx.check(ctx._lib.ig_debug_fail_alloc_at(ctx.h, 1))
+        try:
+            ctx.check(noalloc(ctx.h, db.h, store.h, int(handle), count, shard_ids.ctypes.data, seeds.data_ptr(),
+                              bs.data_ptr(), ms, a_new.data_ptr(), b_new.data_ptr()))
+        finally:
+            ctx.check(ctx._lib.ig_debug_fail_alloc_at(ctx.h, 0))
         torch.cuda.synchronize()
         assert int(status.abs().sum()) == 0
         assert torch.equal(a_new, a_ref), f"call {call}: a differs"
         assert torch.equal(b_new, b_ref), f"call {call}: b differs"
+    # With the injector disarmed, the allocating path still serves (it grows a new scratch).
+    more = np.ascontiguousarray(rng.integers(0, 4, 80), dtype=np.uint32)
+    seeds = torch.from_numpy(rng.integers(0, 256, (80, 32), dtype=np.uint8)).cuda()
+    bs = torch.from_numpy(rng.integers(0, Q, (80, N), dtype=np.uint64).view(np.int64)).cuda()
+    a_big = torch.empty((80, N), dtype=torch.int64, device="cuda")
+    b_big = torch.empty_like(a_big)
+    status = torch.zeros(80, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    ctx.check(ctx._lib.ig_respond_seeded_batch_device(
+        ctx.h, db.h, store.h, int(handle), 80, more.ctypes.data, seeds.data_ptr(), bs.data_ptr(), 0,
+        a_big.data_ptr(), b_big.data_ptr(), status.data_ptr()))
+    torch.cuda.synchronize()
+    assert int(status.abs().sum()) == 0
 
 
 def test_noalloc_refuses_batches_beyond_its_fixed_scratch():
+    import torch
+
     pkg = load_package()
     ctx = pkg.Context.default()
     noalloc = _bind(ctx._lib)
@@ -83,8 +104,16 @@ def test_noalloc_refuses_batches_beyond_its_fixed_scratch():
     store = pkg.ServerSessionStore.new(ctx)
     handle = store.register_server_side(pkg.ClientPackingKeys(np.zeros((3, N), dtype=np.uint64), 16), cache)
     shard_ids = np.zeros(65, dtype=np.uint32)
-    dummy = ctypes.c_void_p(1 << 20)  # never dereferenced: the size check refuses first
-    rc = noalloc(ctx.h, db.h, store.h, int(handle), 65, shard_ids.ctypes.data, dummy, dummy, 0, dummy, dummy)
+    # Real device buffers sized for the 65 queries: should the size check ever stop refusing,
+    # the call computes into them instead of touching memory it does not own.
+    seeds = torch.zeros((65, 32), dtype=torch.uint8, device="cuda")
+    bs = torch.zeros((65, N), dtype=torch.int64, device="cuda")
+    a_out = torch.zeros((65, N), dtype=torch.int64, device="cuda")
+    b_out = torch.zeros((65, N), dtype=torch.int64, device="cuda")
+    torch.cuda.synchronize()
+    rc = noalloc(ctx.h, db.h, store.h, int(handle), 65, shard_ids.ctypes.data, seeds.data_ptr(), bs.data_ptr(), 0,
+                 a_out.data_ptr(), b_out.data_ptr())
+    torch.cuda.synchronize()
     assert rc == 1
     with pytest.raises(pkg.PirError, match="at most 64 queries"):
         ctx.check(rc)
