@@ -2,10 +2,12 @@
 
 Workload (the reference's headline serving configuration): InspireParams::d2048, 512-byte
 records (gamma = 256 columns per shard), 2^20 records = 512 shards, a packing store folded
-on every shard, one session key registered by handle, one batch of 64 queries with
-uniform indices per step answered through respond_seeded_batch, responses mod-switched to
-36 bits. Inputs are seeded synthetic data of those shapes: uniform 16-bit column words
-(the encoding of uniform random record bytes), uniform key and query words mod q.
+on every shard, one session key registered by handle, batches of 64 queries with uniform
+indices answered through respond_seeded_batch, responses mod-switched to 36 bits; a step is
+16 such batches. Inputs are seeded synthetic data of those shapes: uniform 16-bit column
+words (the encoding of uniform random record bytes), uniform key and query words mod q.
+After the timed region, sampled responses of it are recomputed by the CPU oracle and must
+match byte for byte (`parity_checked`).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
                     [--workload served-batch|special-modulus|mixed|serving-sweep]
@@ -14,10 +16,11 @@ uniform indices per step answered through respond_seeded_batch, responses mod-sw
 (32/512/2048 B records under both gadgets, batch sizes 1-512), serving-sweep the serving
 loop over 2^25 records and 1000 seats.
 
-Prints one JSON line. `value` = queries/s over K device-resident batches (CUDA events on
+Prints one JSON line. `value` = queries/s over K device-resident steps (CUDA events on
 the library's stream); `e2e` = the same through the public API with host buffers;
 `cpu_baseline` = the CPU oracle (a port of the reference's respond path) on a bounded
-sample on this host's cores. `--impl reference` times that CPU port alone.
+sample on this host's cores. `--impl reference` times that CPU port alone on the whole
+configuration (every shard stored, one batch of 64 per step).
 """
 import argparse
 import json
@@ -38,15 +41,17 @@ GAMMA = 256
 ENTRY_BYTES = 512
 NUM_SHARDS = 512  # 2^20 records / 2048 per shard
 BATCH = 64
+BATCHES_PER_STEP = 16  # a step answers 16 batches of 64 (1024 queries), about 17 ms on one GB300
+SERVE_REQUESTS = 16384  # requests of each serving-loop leg past its warm-up, whatever --steps is
 Q = 1152921504606830593
 MS_TARGET = 68_718_428_161
 SHARD_DB_BYTES = N_RING * ENTRY_BYTES  # the queried shard's records: 1 MiB
 METRIC = "respond queries/s (served batch of 64, d2048, 512 B records, 2^20 records, 36-bit mod switch)"
 CONFIG = {"workload": "d2048 TwoPacking, 512-byte records x 2^20 (512 shards, gamma 256), packing store on "
-                      "every shard, batch 64 under one registered key, uniform indices, 36-bit mod switch",
+                      "every shard, batches of 64 under one registered key, uniform indices, 36-bit mod switch",
           "ring_dim": N_RING, "gamma": GAMMA, "records": 1 << 20, "shards": NUM_SHARDS, "batch": BATCH,
-          "mod_switch_bits": 36, "l2": "inputs larger than L2: each step reads 64 random shards' columns and "
-                                       "stores (8 MiB per query, 512 MiB per step)"}
+          "mod_switch_bits": 36, "l2": "inputs larger than L2: each batch reads 64 random shards' columns and "
+                                       "stores (8 MiB per query, 512 MiB per batch)"}
 
 
 def peaks():
@@ -58,11 +63,21 @@ def peaks():
         return 6800.0, "fallback"
 
 
-# DRAM bytes (read + write) of one k_scan launch of this workload, from an ncu capture of
-# the timed region (dram__bytes_read.sum + dram__bytes_write.sum, two launches averaged:
-# 67.78 MB and 68.39 MB; the command is in profiles/k_scan_batch64_d2048_g256.md). It sits
-# just under the algorithmic bytes: the scan reads each byte once.
-SCAN_TRAFFIC_BYTES = 68_084_992
+# DRAM bytes (read + write) of one k_scan launch of this workload, from an ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum per launch; the command is in
+# profiles/k_scan_batch64_d2048_g256.md), or None until one is recorded for this kernel.
+SCAN_TRAFFIC_BYTES = None
+
+
+def shard_seed(rank, s):
+    """Seed of shard s's synthetic columns, so a shard can be regenerated for the oracle."""
+    return (1 + rank) * 1_000_003 + s
+
+
+def shard_columns_device(torch, rank, s):
+    g = torch.Generator(device="cuda")
+    g.manual_seed(shard_seed(rank, s))
+    return torch.randint(0, 1 << 16, (GAMMA, N_RING), generator=g, device="cuda", dtype=torch.int64)
 
 
 def rand_words(rng, shape):
@@ -72,35 +87,67 @@ def rand_words(rng, shape):
 # ------------------------------------------------------------------------------------
 # CPU oracle leg (the reference's algorithm restated; test infrastructure only here as
 # the timed CPU baseline).
-def cpu_sample(steps, warmup, queries_per_step=8, shards=4, seed=11):
+def cpu_sample(batches, warmup_batches=0, build_all=False, shards=NUM_SHARDS, seed=11):
+    """The workload on the host's cores through the oracle's store path (the reference's
+    respond_seeded_batch restated: seed expansion, column check and b fold, store gather,
+    recursion, online gather, 36-bit switch; OpenMP at the reference's rayon sites): batches
+    of 64 queries with uniform indices over a database of `shards` shards of gamma 256,
+    answered one query after another as respond_seeded_batch answers them. The shards'
+    stores are built offline (untimed): all of them with build_all, else the shards the
+    sample touches. Timing follows the reference's bench method
+    (benches/shard_packing_store_bench.rs:1-60): every sample listed, median/p90/p99."""
     from oracle import oracle as O
 
     O.build()
     cores = O.lib().orc_max_threads()
     rng = np.random.default_rng(seed)
     P = O.Params.d2048()
-    w_seed = rng.integers(0, 256, 32, dtype=np.uint8).tobytes()
-    cache = O.Cache(P, GAMMA, w_seed)
-    cols = [rng.integers(0, 1 << 16, size=(GAMMA, N_RING), dtype=np.uint64) for _ in range(shards)]
-    stores = [O.Store(cache, c) for c in cols]
+    cache = O.Cache(P, GAMMA, rng.bytes(32))
     y = rand_words(rng, (3, N_RING))
-    times = []
-    for step in range(warmup + steps):
-        t0 = time.perf_counter()
-        for k in range(queries_per_step):
-            s = k % shards
-            seed_b = rng.integers(0, 256, 32, dtype=np.uint8).tobytes()
-            a = O.expand_seed(seed_b, N_RING)
-            b = rand_words(rng, N_RING)
-            ao, bo = stores[s].respond(cols[s], a, b, y)
+    cols, stores = {}, {}
+
+    def shard(s):
+        if s not in stores:
+            c = np.random.default_rng((seed, s)).integers(0, 1 << 16, (GAMMA, N_RING), dtype=np.uint64)
+            cols[s], stores[s] = c, O.Store(cache, c)
+        return cols[s], stores[s]
+
+    t0 = time.perf_counter()
+    if build_all:
+        for s in range(shards):
+            shard(s)
+    setup_s = time.perf_counter() - t0
+    lat, batch_s = [], []
+    for bi in range(warmup_batches + batches):
+        sids = rng.integers(0, shards * N_RING, BATCH) // N_RING
+        queries = [(int(sid), rng.bytes(32), rand_words(rng, N_RING)) for sid in sids]
+        for sid, _, _ in queries:
+            shard(sid)  # offline precompute_packing, outside the timing
+        t_batch = time.perf_counter()
+        for sid, seed_b, b in queries:
+            tq = time.perf_counter()
+            c, st = shard(sid)
+            ao, bo = st.respond(c, O.expand_seed(seed_b, N_RING), b, y)
             O.mod_switch(ao, Q, MS_TARGET)
             O.mod_switch(bo, Q, MS_TARGET)
-        if step >= warmup:
-            times.append(time.perf_counter() - t0)
-    qps = queries_per_step * len(times) / sum(times)
+            if bi >= warmup_batches:
+                lat.append(time.perf_counter() - tq)
+        if bi >= warmup_batches:
+            batch_s.append(time.perf_counter() - t_batch)
+    qps = BATCH * len(batch_s) / sum(batch_s)
+    lat_ms = np.sort(np.array(lat)) * 1e3
+
+    def pct(p):
+        return float(lat_ms[min(len(lat_ms) - 1, int(p * len(lat_ms)))])
+
     return {"value": qps, "unit": "queries/s", "cores": int(cores), "kind": "port",
-            "sample": f"{queries_per_step} queries per step over {shards} stored shards, {steps} steps "
-                      "(oracle store path + 36-bit switch, OpenMP over the reference's rayon sites)"}
+            "sample": f"{batches} batch(es) of 64 queries with uniform indices over {shards} shards of gamma 256 "
+                      f"(512-byte records), {len(stores)} stores built ({'every shard' if build_all else 'the shards the sample touches'}); "
+                      "oracle store path + 36-bit switch, one query after another, OpenMP over the reference's "
+                      "rayon sites",
+            "queries": len(lat), "setup_s": setup_s,
+            "batch_s": [round(x, 4) for x in batch_s],
+            "query_ms": {"median": pct(0.5), "p90": pct(0.9), "p99": pct(0.99)}}
 
 
 # ------------------------------------------------------------------------------------
@@ -194,63 +241,62 @@ def barrier(world):
 
 
 # ------------------------------------------------------------------------------------
-def serve_leg(pkg, ctx, crs, db, store, handle, queries, ms, slots=3, max_batch=BATCH):
-    """The continuous-batching loop (ig_serve_*) under two arrival patterns, with host
-    buffers: a closed loop keeping 4 x slots x max_batch requests outstanding (saturation
-    throughput), and Poisson arrivals at half that rate from a submitting thread (latency
-    under load). Latency runs from submit to result in the caller's buffer."""
-    import threading
+def oracle_check(O, cache_o, y, cols_of, cases):
+    """Each case (shard, seed, b, gpu_a, gpu_b) recomputed by the oracle's store path with the
+    36-bit switch; raises on the first response whose wire bytes differ. Returns the count."""
+    stores = {}
+    for sid, seed_b, b, ga, gb in cases:
+        if sid not in stores:
+            c = cols_of(sid)
+            stores[sid] = (c, O.Store(cache_o, c))
+        c, st = stores[sid]
+        ao, bo = st.respond(c, O.expand_seed(seed_b, N_RING), b, y)
+        want = O.response_bytes(O.mod_switch(ao, Q, MS_TARGET), O.mod_switch(bo, Q, MS_TARGET), GAMMA, MS_TARGET)
+        got = O.response_bytes(np.asarray(ga, dtype=np.uint64), np.asarray(gb, dtype=np.uint64), GAMMA, MS_TARGET)
+        if got != want:
+            raise RuntimeError(f"GPU response differs from the oracle's (shard {sid})")
+    return len(cases)
 
-    out = {"slots": slots, "max_batch": max_batch, "requests": len(queries)}
+
+def serve_leg(pkg, ctx, db, store, handle, shards, rng, ms, slots, max_batch=BATCH, requests=SERVE_REQUESTS):
+    """The continuous-batching loop (ig_serve_*) with host buffers, driven by the native load
+    driver (ig_serve_replay) so the client side is not the bottleneck: a closed loop keeping
+    4 x slots x max_batch requests outstanding (saturation), then Poisson arrivals at half
+    that rate (latency under load). Each leg runs `requests` requests past a warm-up of its
+    own; latency runs from submit to the result in the caller's buffer. Returns the stats and
+    a few (shard, seed, b, a, b) responses for the oracle check."""
+    warm = 4 * slots * max_batch
+    total = warm + requests
+    sids = (rng.integers(0, shards * N_RING, total) // N_RING).astype(np.uint32)
+    handles = np.full(total, int(handle), dtype=np.uint64)
+    seeds = rng.integers(0, 256, (total, 32), dtype=np.uint8)
+    bs = rand_words(rng, (total, N_RING))
+    out = {"slots": slots, "max_batch": max_batch, "requests": requests, "driver": "ig_serve_replay (native)"}
+    window = 4 * slots * max_batch
     with pkg.ServingLoop(ctx, slots=slots, max_batch=max_batch) as loop:
-        for q in queries[:2 * max_batch]:  # warm-up
-            loop.wait(loop.submit(crs, db, q, store, handle, mod_switch_target=ms))
+        loop.replay(db, store, sids[:warm], handles[:warm], seeds[:warm], bs[:warm], ms, window=window)
         loop.stats(reset=True)
-        window = 4 * slots * max_batch  # outstanding requests, below the loop's admission limit
-        t0 = time.perf_counter()
-        pending = []
-        for q in queries:
-            if len(pending) == window:
-                loop.wait(pending.pop(0))
-            pending.append(loop.submit(crs, db, q, store, handle, mod_switch_target=ms))
-        for t in pending:
-            loop.wait(t)
-        sat_s = time.perf_counter() - t0
+        a, b, lat, el = loop.replay(db, store, sids[warm:], handles[warm:], seeds[warm:], bs[warm:], ms,
+                                    window=window)
         st = loop.stats(reset=True)
-        sat_qps = len(queries) / sat_s
-        out["saturation"] = {"queries_per_s": sat_qps, "p50_ms": st["p50_us"] / 1e3, "p99_ms": st["p99_us"] / 1e3,
-                             "mean_batch": st["mean_batch"]}
-        rate = 0.5 * sat_qps
-        gaps = np.random.default_rng(7).exponential(1.0 / rate, size=len(queries))
-        tickets = [None] * len(queries)
-        dropped = [0]
-
-        def submitter():
-            t_next = time.perf_counter()
-            for i, q in enumerate(queries):
-                t_next += gaps[i]
-                while time.perf_counter() < t_next:
-                    pass
-                try:
-                    tickets[i] = loop.submit(crs, db, q, store, handle, mod_switch_target=ms)
-                except pkg.PirError as e:
-                    if e.code != 8:  # only an admission refusal is an expected outcome
-                        raise
-                    dropped[0] += 1
-
-        th = threading.Thread(target=submitter)
-        t0 = time.perf_counter()
-        th.start()
-        th.join()
-        for t in tickets:
-            if t is not None:
-                loop.wait(t)
-        open_s = time.perf_counter() - t0
+        sat = requests / el
+        lat_ms = np.sort(lat) / 1e6
+        out["saturation"] = {"queries_per_s": sat, "p50_ms": float(lat_ms[len(lat_ms) // 2]),
+                             "p99_ms": float(lat_ms[int(0.99 * (len(lat_ms) - 1))]), "mean_batch": st["mean_batch"],
+                             "window": window}
+        picks = [warm + int(i) for i in rng.choice(requests, 2, replace=False)]
+        cases = [(int(sids[i]), seeds[i].tobytes(), bs[i], a[i - warm], b[i - warm]) for i in picks]
+        rate = 0.5 * sat
+        arr = np.cumsum(rng.exponential(1e9 / rate, requests)).astype(np.uint64)
+        a, b, lat, el = loop.replay(db, store, sids[warm:], handles[warm:], seeds[warm:], bs[warm:], ms,
+                                    arrival_ns=arr)
         st = loop.stats(reset=True)
-        out["poisson_half_load"] = {"offered_per_s": rate, "queries_per_s": len(queries) / open_s,
-                                    "p50_ms": st["p50_us"] / 1e3, "p99_ms": st["p99_us"] / 1e3,
-                                    "mean_batch": st["mean_batch"], "admission_refused": dropped[0]}
-    return out
+        lat_ms = np.sort(lat) / 1e6
+        out["poisson_half_load"] = {"offered_per_s": rate, "queries_per_s": requests / el,
+                                    "p50_ms": float(lat_ms[len(lat_ms) // 2]),
+                                    "p99_ms": float(lat_ms[int(0.99 * (len(lat_ms) - 1))]),
+                                    "mean_batch": st["mean_batch"]}
+    return out, cases
 
 
 def plain_leg(pkg, crs, db, keys, queries, ms):
@@ -280,8 +326,6 @@ def run_gb300(args, rank, world):
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     ctx = pkg.Context(local)
-    g = torch.Generator(device="cuda")
-    g.manual_seed(1 + rank)
     rng = np.random.default_rng(1000 + rank)
 
     params = pkg.InspireParams.d2048()
@@ -291,18 +335,21 @@ def run_gb300(args, rank, world):
     db = pkg.EncodedDatabase(cache, args.shards)
     t_setup = time.perf_counter()
     for s in range(args.shards):
-        cols = torch.randint(0, 1 << 16, (GAMMA, N_RING), generator=g, device="cuda", dtype=torch.int64)
+        cols = shard_columns_device(torch, rank, s)
         torch.cuda.current_stream().synchronize()
         db.set_shard_device(s, cols.data_ptr())
     db.precompute_packing_all()
     setup_s = time.perf_counter() - t_setup
     store = pkg.ServerSessionStore.new(ctx)
-    keys = pkg.ClientPackingKeys(rand_words(rng, (3, N_RING)), GAMMA)
+    y_body = rand_words(rng, (3, N_RING))
+    keys = pkg.ClientPackingKeys(y_body, GAMMA)
     handle = store.register_server_side(keys, cache)
 
-    total = args.warmup + args.steps
-    shard_ids = [rng.integers(0, args.shards * N_RING, size=BATCH) // N_RING for _ in range(total)]
-    shard_ids = [np.ascontiguousarray(x, dtype=np.uint32) for x in shard_ids]
+    bps = args.batches_per_step
+    total = (args.warmup + args.steps) * bps  # batches
+    first_timed = args.warmup * bps
+    shard_ids = [np.ascontiguousarray(rng.integers(0, args.shards * N_RING, size=BATCH) // N_RING, dtype=np.uint32)
+                 for _ in range(total)]
     seeds_h = rng.integers(0, 256, size=(total, BATCH, 32), dtype=np.uint8)
     bs_h = rand_words(rng, (total, BATCH, N_RING))
     d_seeds = torch.from_numpy(seeds_h).cuda()
@@ -320,15 +367,15 @@ def run_gb300(args, rank, world):
     pair_default = 76
     shape = "pair (2 CTAs per query)" if BATCH * lanes <= pair_default else "single (1 CTA per query)"
 
-    def step(i):
+    def batch(i):
         k = i % lanes
         ctx.check(lib.ig_respond_seeded_batch_device(
             ctx.h, db.h, store.h, int(handle), BATCH, shard_ids[i].ctypes.data, d_seeds[i].data_ptr(),
             d_bs[i].data_ptr(), MS_TARGET, d_a[k].data_ptr(), d_b[k].data_ptr(), d_status[k].data_ptr()))
 
     ctx.set_lanes(lanes)
-    for i in range(args.warmup):
-        step(i)
+    for i in range(first_timed):
+        batch(i)
     ctx.join()
     torch.cuda.synchronize()
     stream.synchronize()
@@ -342,8 +389,8 @@ def run_gb300(args, rank, world):
         torch.cuda.profiler.start()  # bounds an ncu --profile-from-start off capture
         with torch.cuda.stream(stream):
             ev0.record(stream)
-            for i in range(args.warmup, total):
-                step(i)
+            for i in range(first_timed, total):
+                batch(i)
             ctx.join()
             ev1.record(stream)
         torch.cuda.synchronize()
@@ -355,7 +402,27 @@ def run_gb300(args, rank, world):
     if int(d_status.abs().sum().item()) != 0:
         raise RuntimeError("a batch was refused during the timed region")
     ms_max = max_over_ranks(ms_total, world)
-    value = world * BATCH * args.steps / (ms_max / 1e3)
+    timed_queries = BATCH * (total - first_timed)
+    value = world * timed_queries / (ms_max / 1e3)
+
+    # Byte check of what was timed, outside the timing: the last two batches' outputs are
+    # still in their lanes; two queries of each (first and last of the batch) against the
+    # oracle's store path on the same shards, key and queries.
+    from oracle import oracle as O
+    O.build()
+    cache_o = O.Cache(O.Params.d2048(), GAMMA, w_seed)
+    a_h = d_a.cpu().numpy().view(np.uint64)
+    b_h = d_b.cpu().numpy().view(np.uint64)
+    cases = []
+    for i in (total - 1, total - 2):
+        for k in (0, BATCH - 1):
+            cases.append((int(shard_ids[i][k]), seeds_h[i, k].tobytes(), bs_h[i, k], a_h[i % lanes, k],
+                          b_h[i % lanes, k]))
+
+    def cols_of(sid):
+        return shard_columns_device(torch, rank, sid).cpu().numpy().view(np.uint64)
+
+    checked = oracle_check(O, cache_o, y_body, cols_of, cases)
 
     # Kernel rooflines: the same batches one at a time (one lane, the launch shape of the
     # timed region), each kernel bracketed by CUDA events on the stream it runs on.
@@ -363,12 +430,12 @@ def run_gb300(args, rank, world):
     if lanes > 1:
         ctx.set_pair_threshold(0)
     ctx.profile(True)
-    prof_steps = min(args.steps, 20)
-    for i in range(args.warmup):
-        step(i)
+    prof_batches = min(total - first_timed, 20)
+    for i in range(3):
+        batch(i)
     ctx.profile_read(reset=True)
-    for i in range(args.warmup, args.warmup + prof_steps):
-        step(i)
+    for i in range(first_timed, first_timed + prof_batches):
+        batch(i)
     prof = ctx.profile_read(reset=True)
     ctx.profile(False)
     ctx.set_pair_threshold(pair_default)
@@ -384,12 +451,15 @@ def run_gb300(args, rank, world):
     ctx.set_lanes(lanes)
     served = [0] * lanes
     errors = []
+    last_out = {}
 
     def caller(t, idx):
         try:
             for i in idx:
                 out = pkg.respond_seeded_batch(crs, db, batches[i], cache, store, mod_switch_target=MS_TARGET)
                 served[t] += len(out)
+                if i == total - 1:
+                    last_out[i] = out
         except Exception as e:  # reported below
             errors.append(e)
 
@@ -400,21 +470,27 @@ def run_gb300(args, rank, world):
         for th in threads:
             th.join()
 
-    run_callers(list(range(args.warmup)))
+    run_callers(list(range(first_timed)))
     served = [0] * lanes
     barrier(world)
     t0 = time.perf_counter()
-    run_callers(list(range(args.warmup, total)))
+    run_callers(list(range(first_timed, total)))
     e2e_s = max_over_ranks(time.perf_counter() - t0, world)
     ctx.set_lanes(1)
     if errors:
         raise errors[0]
-    assert sum(served) == BATCH * args.steps
-    e2e_value = world * BATCH * args.steps / e2e_s
+    assert sum(served) == timed_queries
+    e2e_value = world * timed_queries / e2e_s
+    # The host-buffer path's last batch: the same bytes as the device path's.
+    for k in (0, BATCH - 1):
+        r = last_out[total - 1][k]
+        if not (np.array_equal(np.asarray(r.a, dtype=np.uint64), a_h[(total - 1) % lanes, k]) and
+                np.array_equal(np.asarray(r.b, dtype=np.uint64)[:GAMMA], b_h[(total - 1) % lanes, k][:GAMMA])):
+            raise RuntimeError("respond_seeded_batch differs from the device path on the same batch")
 
-    serving = serve_leg(pkg, ctx, crs, db, store, handle, [q for qs in e2e_queries for q in qs], MS_TARGET,
-                        slots=lanes)
-    plain = plain_leg(pkg, crs, db, keys, [q for qs in e2e_queries for q in qs][:64], MS_TARGET)
+    serving, serve_cases = serve_leg(pkg, ctx, db, store, handle, args.shards, rng, MS_TARGET, slots=lanes)
+    checked += oracle_check(O, cache_o, y_body, cols_of, serve_cases)
+    plain = plain_leg(pkg, crs, db, keys, [q for qs in e2e_queries[:1] for q in qs], MS_TARGET)
 
     scan_ms, scan_n = prof["scan"]
     resp_ms, resp_n = prof["respond"]
@@ -422,9 +498,8 @@ def run_gb300(args, rank, world):
     resp_avg = resp_ms / max(resp_n, 1)
     # Algorithmic bytes of one scan launch. The shards hold 16-bit record words, which the
     # library keeps as a u16 copy for the scan: per query the gamma columns at 2 bytes a
-    # word, the even tag-key words (the odd ones multiply the high halves, all zero), the
-    # query's b (n words), and gamma folded words out.
-    scan_bytes = BATCH * (GAMMA * N_RING * 2 + N_RING * 8 + N_RING * 8 + GAMMA * 8)
+    # word, the query's b (n words) and gamma folded words out.
+    scan_bytes = BATCH * (GAMMA * N_RING * 2 + N_RING * 8 + GAMMA * 8)
     hbm_peak, peak_kind = peaks()
     achieved = scan_bytes / (scan_avg / 1e3) / 1e9
     # Recursion: 3 transforms of n/2 log n butterflies per link, and per slot 7 pointwise
@@ -442,14 +517,20 @@ def run_gb300(args, rank, world):
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u64 (exact mod q = 2^60-2^14+1)",
         "data": "synthetic: uniform 16-bit column words (uniform record bytes), uniform key/query words mod q",
-        "config": dict(CONFIG, parallelism=f"replicas x{world}" if world > 1 else "single GPU",
-                       lanes=lanes, launch_shape=shape,
-                       **({"shards": args.shards, "records": args.shards * N_RING} if args.shards != NUM_SHARDS
-                          else {})),
+        "config": dict(CONFIG, **({"shards": args.shards, "records": args.shards * N_RING}
+                                  if args.shards != NUM_SHARDS else {})),
+        "step": f"{bps} batches of {BATCH} queries, each one respond_seeded_batch_device call "
+                f"({bps * BATCH} queries a step)",
+        "execution": {"parallelism": f"replicas x{world}" if world > 1 else "single GPU", "lanes": lanes,
+                      "launch_shape": shape},
+        "parity_checked": checked,
+        "parity_note": "outside the timing: 4 responses of the timed region's last two batches (first and last "
+                       "query of each) and 2 served by the serving loop, recomputed by the oracle's store path "
+                       "on the same 2^20-record database, key and queries, 36-bit switch: wire bytes equal",
         "db_gbs": value * SHARD_DB_BYTES / 1e9,
         "e2e": {"value": e2e_value, "unit": "queries/s",
-                "h2d_bytes_per_step": BATCH * (32 + N_RING * 8 + 4),
-                "d2h_bytes_per_step": BATCH * 2 * N_RING * 8,
+                "h2d_bytes_per_step": bps * BATCH * (32 + N_RING * 8 + 4),
+                "d2h_bytes_per_step": bps * BATCH * 2 * N_RING * 8,
                 "callers": lanes, "call": "respond_seeded_batch (one batch of 64 per call)"},
         "roofline": {"kernel": "shard_scan", "bound": "hbm", "achieved": achieved, "peak": hbm_peak,
                      "unit": "GB/s", "frac": achieved / hbm_peak,
@@ -457,10 +538,8 @@ def run_gb300(args, rank, world):
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, same workload",
                      "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
                      "avg_launch_ms": scan_avg, "algorithmic_bytes_per_launch": scan_bytes,
-                     "note": "the HBM-facing kernel, 1.3% of the device time; its rate is set by its multiply "
-                             "pipe (four 32x32->64 products per 16-bit word against the 61-bit tag key and "
-                             "60-bit b) and, at 64 queries a launch, by a fixed cost of about 13 us; the "
-                             "dominant kernel is in roofline_dominant"},
+                     "timing": "one batch of 64 at a time on one lane, CUDA events around each scan launch",
+                     "note": "the HBM-facing kernel; the dominant kernel is in roofline_dominant"},
         "roofline_dominant": {"kernel": "respond (fused recursion + online gather)", "bound": "integer multiply pipe",
                               "achieved": timed_gmodmul, "unit": "G modmul/s", "peak": peak_gmodmul,
                               "frac": timed_gmodmul / peak_gmodmul,
@@ -1083,9 +1162,11 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=None,
-                    help="timed steps (default: 300 for the served batch and 100 for the special_modulus batch, a "
-                         "timed region of about "
-                         "half a second that the 50 ms clock sampler sees; 20 for the reference arm)")
+                    help="timed steps (default: 20 for the served batch, a step being 16 batches of 64, and 100 for "
+                         "the special_modulus batch: a timed region of about a third of a second that the 50 ms "
+                         "clock sampler sees; 20 for the reference arm, a step being one batch of 64)")
+    ap.add_argument("--batches-per-step", type=int, default=BATCHES_PER_STEP,
+                    help="batches of 64 in one step of the served-batch workload")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -1107,17 +1188,22 @@ def main():
     if args.lanes is None:
         args.lanes = 4 if args.workload in ("served-batch", "serving-sweep") else 3
     if args.steps is None:
-        args.steps = 20 if args.impl == "reference" else {"served-batch": 300, "special-modulus": 100, "mixed": 60,
+        args.steps = 20 if args.impl == "reference" else {"served-batch": 20, "special-modulus": 100, "mixed": 60,
                                                           "serving-sweep": 0, "one-packing": 20,
                                                           "no-packing": 300}[args.workload]
     rank, world = dist_setup(args.gpus)
     if args.impl == "reference":
         if rank != 0:
             return
-        cb = cpu_sample(args.steps, args.warmup)
+        # The whole configuration on the host's cores: all 512 shards with their stores, each
+        # step one batch of 64 queries with uniform indices, answered one after another.
+        cb = cpu_sample(batches=args.steps, warmup_batches=args.warmup, build_all=True)
         line = {"metric": METRIC, "value": cb["value"], "unit": "queries/s", "n_gpus": world, "steps": args.steps,
-                "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(cb["batch_s"])),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "u64 (exact mod q)", "data": "synthetic, same shapes", "config": CONFIG,
+                "step": f"one batch of {BATCH} queries (a bounded sample of the workload per step)",
+                "execution": {"parallelism": f"CPU, {cb['cores']} threads"},
                 "impl": "reference", "cpu_baseline": cb,
                 "e2e": {"value": cb["value"], "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
@@ -1152,7 +1238,9 @@ def main():
     line = run_gb300(args, rank, world)
     if rank == 0:
         if not args.no_cpu_baseline:
-            line["cpu_baseline"] = cpu_sample(steps=3, warmup=1)
+            # Two batches of 64 over the same 512-shard shape (about 10 s of CPU work); the
+            # stores of the touched shards, over 100 of them, exceed the host's last-level cache.
+            line["cpu_baseline"] = cpu_sample(batches=2)
         print(json.dumps(line))
 
 

@@ -90,7 +90,11 @@ int ig_crs_key_rows(ig_ctx* ctx, uint64_t crs, uint32_t* rows_out);
 int ig_db_create(ig_ctx* ctx, uint64_t crs, uint32_t num_shards, uint64_t* db_out);
 int ig_db_destroy(ig_ctx* ctx, uint64_t db);
 /* Uploads (or replaces) shard `shard_id`'s gamma x ring_dim columns. Replacing columns
- * keeps any store, which the next respond then refuses (shard_store.rs:247-257). */
+ * keeps any store. The new columns' keyed tags are checked against the store's at once
+ * (the check ShardPackingStore::check_columns_and_fold_b makes at every respond,
+ * shard_store.rs:197-264, made here once per change because the library writes every
+ * column word itself): when they differ, every respond on the shard is refused
+ * (IG_ERR_STORE_REFUSED, shard_store.rs:247-257) until its store is rebuilt. */
 int ig_db_set_shard(ig_ctx* ctx, uint64_t db, uint32_t shard_id, const uint64_t* columns);
 /* Same, from a device pointer (columns already in HBM). */
 int ig_db_set_shard_device(ig_ctx* ctx, uint64_t db, uint32_t shard_id, const uint64_t* d_columns);
@@ -165,12 +169,34 @@ int ig_respond_seeded_batch_device(ig_ctx* ctx, uint64_t db, uint64_t store, uin
                                    uint64_t mod_switch_target, uint64_t* d_a_out, uint64_t* d_b_out,
                                    uint32_t* d_status);
 
+/* Queries of several databases, parameter sets (record widths, exact or approximate gadget),
+ * seats and mod-switch targets answered in one scan and one respond launch: a fused form of
+ * one respond_seeded_batch call (respond.rs:1189-1202) per (key, database) group. Query i
+ * reads shard shard_ids[i] of database dbs[i] under seat handles[i] of session store
+ * stores[i], with seeds[32 i..] and bs[ring_dim i..], switched to ms_targets[i] (0: none;
+ * ms_targets may be NULL for no switch at all); its response is a_out[ring_dim i..] and
+ * b_out[ring_dim i..], the bytes ig_respond_seeded_batch gives for the same query. Every
+ * database must share one ring_dim, and every queried shard must hold a packing store. The
+ * launch runs the queries with the longest recursion (largest gamma) first. All or nothing,
+ * refused whole on the first error. */
+int ig_respond_mixed_batch(ig_ctx* ctx, uint32_t count, const uint64_t* dbs, const uint64_t* stores,
+                           const uint64_t* handles, const uint32_t* shard_ids, const uint8_t* seeds, const uint64_t* bs,
+                           const uint64_t* ms_targets, uint64_t* a_out, uint64_t* b_out);
+/* Same with the seeds, b, a, b and status words in device memory (shard_ids, dbs, stores,
+ * handles and ms_targets stay host arrays); enqueues on the context's lanes like
+ * ig_respond_seeded_batch_device and returns, status words in d_status[i] (0 = served,
+ * 1 = the shard's store refused its columns). */
+int ig_respond_mixed_batch_device(ig_ctx* ctx, uint32_t count, const uint64_t* dbs, const uint64_t* stores,
+                                  const uint64_t* handles, const uint32_t* shard_ids, const uint8_t* d_seeds,
+                                  const uint64_t* d_bs, const uint64_t* ms_targets, uint64_t* d_a_out,
+                                  uint64_t* d_b_out, uint32_t* d_status);
+
 /* Allocation-free form of ig_respond_seeded_batch_device, with no counterpart in the
  * reference. For callers that must not have the library allocate device memory while
  * serving: servers that size every device buffer at start-up and refuse growth later,
  * and processes sharing a GPU under a memory cap, where an allocation on the request path
  * can fail or evict a neighbour. The call's scratch (fold of b, query descriptors, status
- * words) lives in one fixed device array of 527,104 bytes that every GPU loading the
+ * words) lives in one fixed device array of 528,640 bytes that every GPU loading the
  * library holds until the process exits; the call makes no cudaMalloc/cudaFree and no
  * other allocating call. Limits: at most 64 queries per call, gamma at most 1024, a
  * registered seat (handle) and packing stores on the queried shards; larger batches are
@@ -229,25 +255,36 @@ int ig_sm_response_encode(const uint32_t* mask, uint32_t n, const uint32_t* body
  * No single counterpart in the reference, whose server answers one respond_seeded_batch call
  * at a time (respond.rs:1189-1202); this loop batches individually arriving queries instead.
  * Each request is one seeded query under a seat registered in `store`, on a shard whose
- * packing store was built. A dispatcher thread forms batches of waiting requests that share a
- * parameter set and mod-switch target (databases, shards and seats may differ) and launches
- * each on one of `slots` streams, so batches overlap on the device; device and pinned buffers
- * for every slot are allocated at create time, and create refuses (IG_ERR_NOMEM) when they
- * exceed hbm_budget_bytes (0 = no budget). A request's result equals ig_respond_seeded_batch's
- * for the same query. Databases, shards and seats named by a request must stay alive until
- * the request's ticket is finished.
+ * packing store was built. A dispatcher thread forms batches from the oldest waiting requests
+ * on one ring: databases, parameter sets (record widths, exact or approximate gadget),
+ * shards, seats and mod-switch targets may differ within a batch. Each batch runs on one of
+ * `slots` streams, so batches overlap on the device.
+ *
+ * Admission is by memory: hbm_budget_bytes (0: room for every slot full of max_batch of the
+ * largest requests) is allocated once at create as a device ring (with a pinned host
+ * mirror), and a request joins a batch only while the bytes of its buffers (descriptor,
+ * seed, b, b fold, a, b, status, wire) and of its key (its seat, counted once while any
+ * request on it is in flight) fit what the batches in flight leave free; the others wait in
+ * arrival order, and a request that could not fit even alone is refused (IG_ERR_NOMEM).
+ * create refuses (IG_ERR_NOMEM) when the budget cannot be allocated. A request's result
+ * equals ig_respond_seeded_batch's for the same query. Databases, shards and seats named by a
+ * request must stay alive until the request's ticket is finished.
  *
  * ig_serve_submit copies seed (32 B) and b (ring_dim words) and returns a ticket; a_out and
- * b_out (ring_dim words each) are written before the ticket finishes. Admission is refused
+ * b_out (ring_dim words each) are written before the ticket finishes. Submission is refused
  * (IG_ERR_NOMEM) while 8 x slots x max_batch requests are waiting.
  * ig_serve_wait blocks up to timeout_ms (< 0: no limit) and returns the request's status
  * (IG_ERR_PENDING on timeout, the ticket stays valid); err receives the refusal message.
- * ig_serve_stats reports counts and latency percentiles from submit to result; reset != 0
- * clears them. ig_serve_destroy finishes every submitted request, then frees the slots. */
+ * ig_serve_stats reports counts, latency percentiles from submit to result and the memory
+ * admitted; reset != 0 clears them. ig_serve_destroy finishes every submitted request, then
+ * frees the loop. */
 typedef struct ig_serve ig_serve;
 typedef struct ig_serve_stats_t {
   uint64_t served, refused, batches, waiting, device_bytes;
   double mean_batch, p50_us, p99_us, max_us;
+  /* Memory admission: the budget, the bytes (keys and buffers) of the requests in flight
+   * now, and their peak since create or the last reset. */
+  uint64_t budget_bytes, inflight_bytes, peak_inflight_bytes;
 } ig_serve_stats_t;
 int ig_serve_create(ig_ctx* ctx, uint32_t slots, uint32_t max_batch, uint64_t hbm_budget_bytes, ig_serve** out);
 int ig_serve_submit(ig_serve* s, uint64_t db, uint64_t store, uint64_t handle, uint32_t shard_id,

@@ -64,7 +64,9 @@ def library_path():
 class ServeStats(ctypes.Structure):
     _fields_ = [("served", ctypes.c_uint64), ("refused", ctypes.c_uint64), ("batches", ctypes.c_uint64),
                 ("waiting", ctypes.c_uint64), ("device_bytes", ctypes.c_uint64), ("mean_batch", ctypes.c_double),
-                ("p50_us", ctypes.c_double), ("p99_us", ctypes.c_double), ("max_us", ctypes.c_double)]
+                ("p50_us", ctypes.c_double), ("p99_us", ctypes.c_double), ("max_us", ctypes.c_double),
+                ("budget_bytes", ctypes.c_uint64), ("inflight_bytes", ctypes.c_uint64),
+                ("peak_inflight_bytes", ctypes.c_uint64)]
 
 
 def _load():
@@ -101,6 +103,8 @@ def _load():
         "ig_session_contains": (I, [P, U64, U64, ctypes.POINTER(I)]),
         "ig_respond_seeded_batch": (I, [P, U64, U64, U64, P, U32, U32, U32, P, P, P, U64, P, P]),
         "ig_respond_seeded_batch_device": (I, [P, U64, U64, U64, U32, P, P, P, U64, P, P, P]),
+        "ig_respond_mixed_batch": (I, [P, U32, P, P, P, P, P, P, P, P, P]),
+        "ig_respond_mixed_batch_device": (I, [P, U32, P, P, P, P, P, P, P, P, P, P]),
         "ig_respond_batch": (I, [P, U64, U64, U64, P, U32, U32, U32, P, P, P, U64, P, P]),
         "ig_response_encode": (I, [P, P, U32, U32, U64, P, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
         "ig_response_encode_full": (I, [P, U32, U32, U64, P, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
@@ -707,6 +711,47 @@ def respond_seeded_inspiring(crs: ServerCrs, encoded_db: EncodedDatabase, query:
     return _batch(crs, encoded_db, [query], src, session_store, mod_switch_target)[0]
 
 
+class MixedQuery:
+    """One query of a mixed launch: a seeded query on `encoded_db` under seat `handle` of
+    `session_store`, its response switched to mod_switch_target (0: none)."""
+
+    def __init__(self, encoded_db, session_store, handle, query: SeededBatchQuery, mod_switch_target: int = 0):
+        self.db, self.store, self.handle = encoded_db, session_store, int(handle)
+        self.query, self.mod_switch_target = query, int(mod_switch_target or 0)
+
+
+def respond_mixed_batch(queries) -> list:
+    """Queries of several databases, parameter sets, seats and switch targets in one launch:
+    the responses respond_seeded_batch gives each query under its own key and database
+    (respond.rs:1189-1202), in order; refused whole on the first error. Every database must
+    share one ring and one context."""
+    count = len(queries)
+    if count == 0:
+        return []
+    ctx = queries[0].db.ctx
+    n = queries[0].db.ring_dim
+    if any(q.db.ctx is not ctx for q in queries):
+        raise PirError("a mixed launch runs on one context")
+    for q in queries:
+        if q.query.seed is None or len(q.query.seed) != 32:
+            raise PirError("mixed launches take seeded queries (32-byte seed)")
+        if q.mod_switch_target:
+            check_mod_switch_noise_budget(q.db.cache.crs.params, q.mod_switch_target)
+    dbs = np.array([q.db.h for q in queries], dtype=np.uint64)
+    stores = np.array([q.store.h for q in queries], dtype=np.uint64)
+    handles = np.array([q.handle for q in queries], dtype=np.uint64)
+    sids = np.array([q.query.shard_id for q in queries], dtype=np.uint32)
+    ms = np.array([q.mod_switch_target for q in queries], dtype=np.uint64)
+    seeds = np.frombuffer(b"".join(bytes(q.query.seed) for q in queries), dtype=np.uint8).copy()
+    bs = np.stack([_u64(q.query.b, (n,)) for q in queries])
+    a_out = np.zeros((count, n), dtype=np.uint64)
+    b_out = np.zeros((count, n), dtype=np.uint64)
+    ctx.check(ctx._lib.ig_respond_mixed_batch(ctx.h, count, _ptr(dbs), _ptr(stores), _ptr(handles), _ptr(sids),
+                                              _ptr(seeds), _ptr(bs), _ptr(ms), _ptr(a_out), _ptr(b_out)))
+    return [ServerResponse(a_out[i], b_out[i], q.db.num_columns, q.mod_switch_target or q.db.cache.crs.params.q)
+            for i, q in enumerate(queries)]
+
+
 class ServeTicket:
     """One submitted request of a ServingLoop; owns the buffers its result lands in."""
 
@@ -723,10 +768,12 @@ class ServingLoop:
 
     The reference's server answers one respond_seeded_batch call at a time
     (respond.rs:1189-1202); here requests are submitted one by one, a dispatcher thread
-    groups waiting requests that share a parameter set and mod-switch target into batches,
-    and `slots` batches run concurrently on their own streams. Every slot's buffers are
-    allocated up front; `hbm_budget_bytes` (0 = none) refuses a loop that would exceed it.
-    A request's response equals respond_seeded_batch's for the same query."""
+    batches the oldest waiting requests on one ring (parameter sets, record widths, seats and
+    mod-switch targets may differ within a batch), and `slots` batches run concurrently on
+    their own streams. Admission is by memory: a request joins a batch while the bytes of its
+    key and buffers fit in `hbm_budget_bytes` (0: room for every slot full of the largest
+    requests) next to the batches in flight. A request's response equals
+    respond_seeded_batch's for the same query."""
 
     def __init__(self, ctx: Context = None, slots=2, max_batch=64, hbm_budget_bytes=0):
         self.ctx = ctx or Context.default()

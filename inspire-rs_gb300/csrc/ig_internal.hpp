@@ -30,8 +30,10 @@ void set_sm_destructor(ig_ctx* c, void (*fn)(ig_ctx*, void*));
 // reference's message.
 struct RequestView {
   ig::CrsDev crs;
+  const ig::CrsDev* crs_dev;  // device copy of crs, for launches that mix parameter sets
   ig::ShardDev shard;
   const uint64_t* seat;
+  uint32_t seat_rows;         // key rows of the seat (its bytes: seat_rows x n x 8)
   uint64_t crs_handle;
   uint64_t p;
   bool has_store;

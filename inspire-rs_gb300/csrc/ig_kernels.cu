@@ -255,24 +255,41 @@ __global__ void __launch_bounds__(FOLD_THREADS) k_store_fold(CrsDev c, const u64
 }
 
 // ------------------------------------------------------------------------------------
-// Shard scan (shard_store.rs:197-264). Per word w_k of column j:
-//   tag  += lo32(w_k) key[2k] + hi32(w_k) key[2k+1]            (mod 2^61 - 1 at the end)
-//   fold += w_k * b_rev[k],  b_rev[0] = b_0, b_rev[k] = -b_{n-k}  (mod q at the end)
-// Each warp takes SCAN_ROWS consecutive columns of one query.
+// Shard scan (shard_store.rs:197-264), split in two.
 //
-// Compact shards (every word below 2^16, kept as a u16 copy, so hi32(w) = 0): the tag and
-// fold are a matrix-vector product of the column words with (key[2k], b_rev[k]). Each
-// vector word is split into 32-bit limbs and staged once per CTA in shared memory; every
-// product w * limb is below 2^48, so a lane's 64-bit accumulators hold 2^16 products
-// exactly, and the limbs recombine into 128-bit sums at the end. The vector layout
-// V[k & 7][k >> 3] lets lane l read positions 8m..8m+7 (m = l + 32 it) conflict-free
-// while loading the same positions of a column as one 16-byte word.
+// Column tags (k_column_tags). Per word w_k of column j:
+//   tag = sum_k lo32(w_k) key[2k] + hi32(w_k) key[2k+1]   (mod 2^61 - 1)
+// The reference recomputes the tags from the caller's columns at every respond and refuses
+// a shard whose columns no longer give the stored tags. Here the columns live in device
+// memory the library owns and change only through its own calls (a shard upload or an
+// encode), so the tags are recomputed once, at each such change, and compared with the
+// stored ones: a mismatch marks the shard stale, and every later respond on it is refused
+// with the reference's message until the store is rebuilt. The refusal stays at respond
+// time; the tag check leaves the per-query scan.
 //
-// Other shards take the exact 128-bit path over the u64 words.
-// 16 warps of 4 columns: 64 columns per CTA share one staged vector, and two CTAs per SM
-// (64 registers a thread) give 32 warps per SM to cover the column loads' latency.
+// b fold (k_scan), per query and column j of its shard:
+//   fold_j = sum_k w_k * b_rev[k],  b_rev[0] = b_0, b_rev[k] = -b_{n-k}   (mod q)
+// = coeff0(b * h_j). Compact shards (every word below 2^16, kept as a u16 copy): the fold
+// is a matrix-vector product of the column words with b_rev, whose words are split into
+// two 32-bit limbs and staged once per CTA in shared memory. Every product w * limb is
+// below 2^48, so a lane's 64-bit accumulators hold its 64 products per column exactly, and
+// the limbs recombine into a 128-bit sum at the end: two 32x32->64 multiply-adds per
+// 16-bit word. The vector layout V[k & 7][k >> 3] lets lane l read positions 8m..8m+7
+// (m = l + 32 it) conflict-free while it reads the same positions of a column as one
+// 16-byte word. Other shards take an exact 128-bit path over the u64 words.
+//
+// Work items: a cluster of scan_split(n) CTAs takes SCAN_COLS consecutive columns of one
+// query (SCAN_ROWS per warp), each CTA one slice of 512 of the n words: it stages only its
+// slice of b_rev and copies its whole share of the columns (4 KiB a warp) into shared memory
+// at once, so a CTA is short and keeps its loads in flight together. The slices' partial
+// folds meet in the cluster's rank 0 through distributed shared memory. Items are
+// query << 12 | chunk from a per-launch list, so queries of different widths share a
+// launch; without a list item b is query b / chunks, chunk b % chunks.
 constexpr int SCAN_WARPS = 16;
 constexpr int SCAN_ROWS = 4;
+constexpr int SCAN_COLS = SCAN_WARPS * SCAN_ROWS;
+constexpr int SCAN_SLICE = 512;  // words of a column per CTA (the whole column below n = 512)
+__host__ __device__ constexpr int scan_split(int n) { return n > SCAN_SLICE ? n / SCAN_SLICE : 1; }
 constexpr u64 TAG_PRIME = (1ULL << 61) - 1;
 
 __device__ __forceinline__ u128 shfl_xor_u128(u128 v, int m) {
@@ -282,164 +299,207 @@ __device__ __forceinline__ u128 shfl_xor_u128(u128 v, int m) {
   return ((u128)hi << 64) | lo;
 }
 
-// Lane 0's end of a column: the tag check (or the tag itself in build mode) and the fold.
-__device__ __forceinline__ void scan_finish(const CrsDev& c, const ShardDev& sh, u32 qi, u32 j, u128 tag, u128 fold,
-                                            u64* b_fold, u32* status, int build, u64* tags_out) {
-  u128 t = tag;
-  t = (t & TAG_PRIME) + (t >> 61);
-  t = (t & TAG_PRIME) + (t >> 61);
-  u64 tv = (u64)t;
-  while (tv >= TAG_PRIME) tv -= TAG_PRIME;
-  if (build) {
-    tags_out[j] = tv;
-  } else {
-    if (sh.tags && tv != sh.tags[j]) atomicOr(status + qi, (u32)DEV_TAG_MISMATCH);
-    b_fold[(size_t)qi * c.gamma + j] = reduce128(fold);
+// Tags of `gamma` columns: one warp per column. With `expect` set, a tag that differs sets
+// *mismatch instead of being written.
+template <int LOGN>
+__global__ void __launch_bounds__(256) k_column_tags(u32 gamma, const u64* cols, const u64* key, u64* tags_out,
+                                                     const u64* expect, u32* mismatch) {
+  constexpr int N = 1 << LOGN;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const u32 j = blockIdx.x * (blockDim.x >> 5) + warp;
+  if (j >= gamma) return;
+  const u64* col = cols + (size_t)j * N;
+  u128 tag = 0;
+#pragma unroll 4
+  for (int k = lane; k < N; k += 32) {
+    const u64 w = col[k];
+    const ulonglong2 kk = *reinterpret_cast<const ulonglong2*>(key + 2 * k);
+    tag += (u128)(w & 0xffffffffULL) * kk.x + (u128)(w >> 32) * kk.y;
+  }
+#pragma unroll
+  for (int m = 16; m >= 1; m >>= 1) tag += shfl_xor_u128(tag, m);
+  if (lane == 0) {
+    u128 t = (tag & TAG_PRIME) + (tag >> 61);
+    t = (t & TAG_PRIME) + (t >> 61);
+    u64 tv = (u64)t;
+    while (tv >= TAG_PRIME) tv -= TAG_PRIME;
+    if (expect) {
+      if (tv != expect[j]) atomicOr(mismatch, 1u);
+    } else {
+      tags_out[j] = tv;
+    }
   }
 }
 
-// Shared memory of the compact path: the vector V, then per warp a two-stage ring of the
-// column chunks its lanes copy ahead (cp.async), so the next step's loads are in flight
-// while the current step's products run.
-constexpr int SCAN_STAGES = 2;
+// Shared memory of a scan CTA: its slice of the vector V, the columns' slice (every warp's
+// rows, copied ahead with cp.async), and the partial folds of its SCAN_COLS columns.
+__host__ __device__ constexpr size_t scan_slice(int n) { return (size_t)n / scan_split(n); }
 __host__ __device__ constexpr size_t scan_smem_bytes(int n) {
-  return (size_t)n * 16 + (size_t)SCAN_WARPS * SCAN_STAGES * SCAN_ROWS * 32 * 16;
+  return scan_slice(n) * 8 + (size_t)SCAN_COLS * scan_slice(n) * 2 + (size_t)SCAN_COLS * 8;
 }
 
 __device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
   const unsigned addr = (unsigned)__cvta_generic_to_shared(smem_dst);
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(addr), "l"(gmem_src) : "memory");
 }
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
+// Sums eight per-lane values over the warp in nine 64-bit exchanges instead of forty:
+// each step halves the values a lane keeps and doubles the lanes summed into them. On
+// return, lane l holds the warp total of value ((l >> 4) & 1) * 4 + ((l >> 3) & 1) * 2 +
+// ((l >> 2) & 1) in v[0].
+__device__ __forceinline__ void warp_reduce8(u64 (&v)[8], int lane) {
+  {
+    const bool up = lane & 16;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const u64 send = up ? v[k] : v[k + 4];
+      const u64 got = __shfl_xor_sync(0xffffffffu, send, 16);
+      v[k] = (up ? v[k + 4] : v[k]) + got;
+    }
+  }
+  {
+    const bool up = lane & 8;
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+      const u64 send = up ? v[k] : v[k + 2];
+      const u64 got = __shfl_xor_sync(0xffffffffu, send, 8);
+      v[k] = (up ? v[k + 2] : v[k]) + got;
+    }
+  }
+  {
+    const bool up = lane & 4;
+    const u64 send = up ? v[0] : v[1];
+    const u64 got = __shfl_xor_sync(0xffffffffu, send, 4);
+    v[0] = (up ? v[1] : v[0]) + got;
+  }
+  v[0] += __shfl_xor_sync(0xffffffffu, v[0], 2);
+  v[0] += __shfl_xor_sync(0xffffffffu, v[0], 1);
+}
 
 template <int LOGN>
 __global__ void __launch_bounds__(SCAN_WARPS * 32, 2) k_scan(CrsDev c, const QueryDev* queries, const ShardDev* shards,
-                                                          u64* b_fold, u32* status, int build, u64* tags_out) {
-  constexpr int N = 1 << LOGN, M = N / 8, ITER = M / 32;
+                                                          const u32* work, u32 chunks, u64* b_fold, u32* status) {
+  namespace cg = cooperative_groups;
+  constexpr int N = 1 << LOGN, SPLIT = scan_split(N), KS = N / SPLIT, MS = KS / 8;
+  constexpr int ITER = (MS + 31) / 32;
   extern __shared__ __align__(16) uint4 scan_sm[];
-  uint4* V = scan_sm;  // [8][M]: key[2k] lo, hi, b_rev[k] lo, hi
-  const u32 qi = blockIdx.y;
+  uint2* V = reinterpret_cast<uint2*>(scan_sm);                    // [8][MS]: b_rev[K0 + k] lo, hi
+  uint4* ring = scan_sm + KS / 2;                                   // [warp][it][row][lane]
+  u64* part = reinterpret_cast<u64*>(ring + (size_t)SCAN_WARPS * ITER * SCAN_ROWS * 32);  // [SCAN_COLS]
+  cg::cluster_group cluster = cg::this_cluster();
+  const int split = SPLIT > 1 ? (int)cluster.block_rank() : 0;
+  const u32 item = blockIdx.x / SPLIT;
+  u32 qi, chunk;
+  if (work) {
+    const u32 w = work[item];
+    qi = w >> 12;
+    chunk = w & 0xfff;
+  } else {
+    qi = item / chunks;
+    chunk = item - qi * chunks;
+  }
   const QueryDev qd = queries[qi];
   const ShardDev sh = shards[qd.shard];
+  const u32 gamma = qd.crs ? qd.crs->gamma : c.gamma;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const u32 j0 = (blockIdx.x * SCAN_WARPS + warp) * SCAN_ROWS;
-  const u64* key = sh.tag_key;
+  const u32 c0 = chunk * SCAN_COLS;                 // the item's first column
+  const u32 j0 = c0 + warp * SCAN_ROWS;             // this warp's first row
+  const int K0 = split * KS;                        // this CTA's slice of each column
   const u64* b = qd.b;
+  if (chunk == 0 && split == 0 && threadIdx.x == 0 && sh.stale) atomicOr(status + qd.row, (u32)DEV_TAG_MISMATCH);
+  const int rows = j0 < gamma ? min(SCAN_ROWS, (int)(gamma - j0)) : 0;
 
-  if (sh.cols16 && b && !build) {
-    const int rows = j0 < c.gamma ? min(SCAN_ROWS, (int)(c.gamma - j0)) : 0;
-    const uint16_t* col = sh.cols16 + (size_t)j0 * N;
-    uint4* ring = scan_sm + N + (size_t)warp * SCAN_STAGES * SCAN_ROWS * 32;
-    // Lane l copies, for step it, the 16-byte chunk at positions 8m..8m+7 (m = l + 32 it)
-    // of each of the warp's rows into its own ring slots.
-    auto issue = [&](int it) {
-      if (it < ITER) {
-        uint4* dst = ring + (it % SCAN_STAGES) * SCAN_ROWS * 32 + lane;
-        const int m = lane + 32 * it;
-        for (int r = 0; r < rows; r++) cp_async16(dst + r * 32, col + (size_t)r * N + 8 * m);
-      }
-      cp_async_commit();
-    };
-    issue(0);
+  u64 acc[8];  // acc[2r] = low-limb sum of row r, acc[2r + 1] = high-limb sum
 #pragma unroll
-    for (int k = threadIdx.x; k < N; k += SCAN_WARPS * 32) {
-      const u64 kv = key[2 * k];
-      const u64 bv = k == 0 ? reduce128(b[0]) : negq(reduce128(b[N - k]));
-      V[(k & 7) * M + (k >> 3)] = make_uint4((u32)kv, (u32)(kv >> 32), (u32)bv, (u32)(bv >> 32));
-    }
-    __syncthreads();
-    if (rows == 0) {
-      asm volatile("cp.async.wait_all;\n" ::: "memory");
-      return;
-    }
-    u64 tl[SCAN_ROWS], th[SCAN_ROWS], fl[SCAN_ROWS], fh[SCAN_ROWS];
+  for (int k = 0; k < 8; k++) acc[k] = 0;
+  if (sh.cols16) {
+    const uint16_t* col = sh.cols16 + (size_t)j0 * N + K0;
+    uint4* wring = ring + (size_t)warp * ITER * SCAN_ROWS * 32;
+    // Every chunk of the warp's rows in flight at once: lane l copies, for step it, the
+    // 16-byte chunk at positions 8m..8m+7 (m = l + 32 it) of each row.
 #pragma unroll
-    for (int r = 0; r < SCAN_ROWS; r++) tl[r] = th[r] = fl[r] = fh[r] = 0;
-#pragma unroll 1
     for (int it = 0; it < ITER; it++) {
-      issue(it + 1);
-      cp_async_wait_one();  // step it's copies have landed (only step it+1's may be pending)
       const int m = lane + 32 * it;
-      const uint4* src = ring + (it % SCAN_STAGES) * SCAN_ROWS * 32 + lane;
-      uint4 w[SCAN_ROWS];
-#pragma unroll
-      for (int r = 0; r < SCAN_ROWS; r++) w[r] = r < rows ? src[r * 32] : make_uint4(0, 0, 0, 0);
-#pragma unroll
-      for (int p = 0; p < 8; p++) {
-        const uint4 v = V[p * M + m];
-#pragma unroll
-        for (int r = 0; r < SCAN_ROWS; r++) {
-          const u32 word = p & 1 ? (((&w[r].x)[p >> 1]) >> 16) : (((&w[r].x)[p >> 1]) & 0xffffu);
-          tl[r] += (u64)word * v.x;
-          th[r] += (u64)word * v.y;
-          fl[r] += (u64)word * v.z;
-          fh[r] += (u64)word * v.w;
-        }
-      }
+      if (m < MS)
+        for (int r = 0; r < rows; r++) cp_async16(wring + (it * SCAN_ROWS + r) * 32 + lane, col + (size_t)r * N + 8 * m);
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+    for (int k = threadIdx.x; k < KS; k += SCAN_WARPS * 32) {
+      const int kk = K0 + k;
+      const u64 bv = kk == 0 ? reduce128(b[0]) : negq(reduce128(b[N - kk]));
+      V[(k & 7) * MS + (k >> 3)] = make_uint2((u32)bv, (u32)(bv >> 32));
     }
     asm volatile("cp.async.wait_all;\n" ::: "memory");
+    __syncthreads();
+    if (rows) {
 #pragma unroll
-    for (int r = 0; r < SCAN_ROWS; r++) {
+      for (int it = 0; it < ITER; it++) {
+        const int m = lane + 32 * it;
+        if (m >= MS) break;
+        uint4 w[SCAN_ROWS];
 #pragma unroll
-      for (int s = 16; s >= 1; s >>= 1) {
-        tl[r] += __shfl_xor_sync(0xffffffffu, tl[r], s);
-        th[r] += __shfl_xor_sync(0xffffffffu, th[r], s);
-        fl[r] += __shfl_xor_sync(0xffffffffu, fl[r], s);
-        fh[r] += __shfl_xor_sync(0xffffffffu, fh[r], s);
+        for (int r = 0; r < SCAN_ROWS; r++) w[r] = r < rows ? wring[(it * SCAN_ROWS + r) * 32 + lane] : make_uint4(0, 0, 0, 0);
+#pragma unroll
+        for (int p = 0; p < 8; p++) {
+          const uint2 v = V[p * MS + m];
+#pragma unroll
+          for (int r = 0; r < SCAN_ROWS; r++) {
+            const u32 word = p & 1 ? (((&w[r].x)[p >> 1]) >> 16) : (((&w[r].x)[p >> 1]) & 0xffffu);
+            acc[2 * r] += (u64)word * v.x;
+            acc[2 * r + 1] += (u64)word * v.y;
+          }
+        }
       }
     }
-    if (lane < rows) {
-      u64 a = tl[0], bh = th[0], f0 = fl[0], f1 = fh[0];
-#pragma unroll
-      for (int r = 1; r < SCAN_ROWS; r++)
-        if (lane == r) {
-          a = tl[r];
-          bh = th[r];
-          f0 = fl[r];
-          f1 = fh[r];
+  } else {
+    // u64 words: exact 128-bit products w * b_rev[k], their low and high words summed
+    // apart (a lane's KS / 32 of them stay below 2^68 in each 128-bit sum).
+    if (rows) {
+      for (int r = 0; r < rows; r++) {
+        const u64* cw = sh.columns + (size_t)(j0 + r) * N + K0;
+        u128 flo = 0, fhi = 0;
+        for (int k = lane; k < KS; k += 32) {
+          const int kk = K0 + k;
+          const u64 rv = kk == 0 ? reduce128(b[0]) : negq(reduce128(b[N - kk]));
+          const u128 pr = (u128)cw[k] * rv;
+          flo += (u64)pr;
+          fhi += (u64)(pr >> 64);
         }
-      const u128 tag = (u128)a + ((u128)bh << 32);
-      const u128 fold = (u128)f0 + ((u128)f1 << 32);
-      scan_finish(c, sh, qi, j0 + lane, tag, fold, b_fold, status, build, tags_out);
+#pragma unroll
+        for (int m = 16; m >= 1; m >>= 1) {
+          flo += shfl_xor_u128(flo, m);
+          fhi += shfl_xor_u128(fhi, m);
+        }
+        if (lane == 0) {
+          const u64 r64 = (u64)((((u128)1) << 64) % Q);
+          part[warp * SCAN_ROWS + r] = reduce128((u128)reduce128(fhi) * r64 + reduce128(flo));
+        }
+      }
     }
+  }
+  if (sh.cols16 && rows) {
+    warp_reduce8(acc, lane);
+    // Lane l holds value index x = ((l >> 4) & 1) 4 + ((l >> 3) & 1) 2 + ((l >> 2) & 1):
+    // row x / 2, limb x & 1; the high limb of the row sits four lanes up.
+    const u64 hi = __shfl_down_sync(0xffffffffu, acc[0], 4);
+    const int r = ((lane >> 4) & 1) * 2 + ((lane >> 3) & 1);
+    if ((lane & 7) == 0 && r < rows) part[warp * SCAN_ROWS + r] = reduce128((u128)acc[0] + ((u128)hi << 32));
+  }
+  u64* fold_out = b_fold + qd.fold_off;
+  const int ncols = c0 < gamma ? min(SCAN_COLS, (int)(gamma - c0)) : 0;
+  if (SPLIT == 1) {
+    __syncthreads();
+    if ((int)threadIdx.x < ncols) fold_out[c0 + threadIdx.x] = part[threadIdx.x];
     return;
   }
-
-#pragma unroll 1
-  for (int r = 0; r < SCAN_ROWS; r++) {
-    const u32 j = j0 + r;
-    if (j >= c.gamma) return;
-    const u64* col = sh.columns + (size_t)j * N;
-    u128 tag = 0, flo = 0, fhi = 0;
-#pragma unroll 4
-    for (int k0 = lane * 2; k0 < N; k0 += 64) {
-      const ulonglong2 w = *reinterpret_cast<const ulonglong2*>(col + k0);
-      const ulonglong2 ka = *reinterpret_cast<const ulonglong2*>(key + 2 * k0);
-      const ulonglong2 kb = *reinterpret_cast<const ulonglong2*>(key + 2 * k0 + 2);
-      tag += (u128)(w.x & 0xffffffffULL) * ka.x + (u128)(w.x >> 32) * ka.y;
-      tag += (u128)(w.y & 0xffffffffULL) * kb.x + (u128)(w.y >> 32) * kb.y;
-      if (b) {
-        const u64 r0 = k0 == 0 ? reduce128(b[0]) : negq(reduce128(b[N - k0]));
-        const u64 r1 = negq(reduce128(b[N - k0 - 1]));
-        const u128 p0 = (u128)w.x * r0, p1 = (u128)w.y * r1;
-        flo += (u128)(u64)p0 + (u64)p1;
-        fhi += (p0 >> 64) + (p1 >> 64);
-      }
-    }
+  cluster.sync();  // every slice's partial folds are in its shared memory
+  if (split == 0 && (int)threadIdx.x < ncols) {
+    u64 f = part[threadIdx.x];
 #pragma unroll
-    for (int m = 16; m >= 1; m >>= 1) {
-      tag += shfl_xor_u128(tag, m);
-      flo += shfl_xor_u128(flo, m);
-      fhi += shfl_xor_u128(fhi, m);
-    }
-    if (lane == 0) {
-      // fold = fhi * 2^64 + flo (mod q)
-      const u64 r64 = (u64)((((u128)1) << 64) % Q);
-      const u64 hq = reduce128(fhi), lq = reduce128(flo);
-      scan_finish(c, sh, qi, j, tag, (u128)hq * r64 + lq, b_fold, status, build, tags_out);
-    }
+    for (int r = 1; r < SPLIT; r++) f = addq(f, cluster.map_shared_rank(part, r)[threadIdx.x]);
+    fold_out[c0 + threadIdx.x] = f;
   }
+  cluster.sync();  // each CTA's shared memory stays alive until rank 0 has read it
 }
 
 // ServerResponse wire on the device (respond.rs:111-176, tight codec poly.rs:166-225):
@@ -534,11 +594,12 @@ __device__ __forceinline__ u64 mod_switch_word(u64 cv, u64 qn) {
 //   sum_k X_k D_k = D_0 (X_0 - base^-2 X_2) + D_1 (X_1 - base^-1 X_2) + R base^-2 X_2.
 // The folded rows are R-form too; a consumer then needs neither D_2 nor its reduction.
 // Every read precedes every write, so src may equal dst.
-__device__ __forceinline__ void fold_gadget3(const CrsDev& c, const u64* src, u64* dst, int stride) {
+__device__ __forceinline__ void fold_gadget3(u64 ld_inv_R, u64 ld_c0_R, u64 ld_c1_R, const u64* src, u64* dst,
+                                             int stride) {
   const u64 x0 = src[0], x1 = src[stride], x2 = src[2 * stride];
-  const u64 f0 = addq(x0, mont(x2, c.ld_c0_R));
-  const u64 f1 = addq(x1, mont(x2, c.ld_c1_R));
-  const u64 f2 = mont(x2, c.ld_inv_R);
+  const u64 f0 = addq(x0, mont(x2, ld_c0_R));
+  const u64 f1 = addq(x1, mont(x2, ld_c1_R));
+  const u64 f2 = mont(x2, ld_inv_R);
   dst[0] = f0;
   dst[stride] = f1;
   dst[2 * stride] = f2;
@@ -551,28 +612,29 @@ __global__ void k_fold_gadget_keys(CrsDev c, u64* keys, u32 count) {
   if (i >= count * 2 * n) return;
   const u32 key = i / (2 * n), r = i - key * 2 * n;
   u64* x = keys + (size_t)key * 6 * n + r;
-  fold_gadget3(c, x, x, (int)(2 * n));
+  fold_gadget3(c.ld_inv_R, c.ld_c0_R, c.ld_c1_R, x, x, (int)(2 * n));
 }
 
-// Per-query constants into shared memory: forward ladder, slot tables, the mask rows and
-// the seat's key rows (both R-form NTT; with the exact gadget, folded by fold_gadget3).
+// Per-query constants into shared memory: forward ladder and slot tables of the ring (c),
+// the mask rows of the query's parameter set (v) and the seat's key rows (both R-form NTT;
+// with the exact gadget, folded by fold_gadget3).
 template <int N, int NT>
-__device__ __forceinline__ void stage_constants(const CrsDev& c, const u64* yR, u64* tw, u64* twp, u64* Wm, u64* Y,
-                                                uint16_t* e_tab, uint16_t* s_tab) {
+__device__ __forceinline__ void stage_constants(const CrsDev& c, const SetView& v, const u64* yR, u64* tw, u64* twp,
+                                                u64* Wm, u64* Y, uint16_t* e_tab, uint16_t* s_tab) {
   for (int k = threadIdx.x; k < N; k += NT) {
     tw[k] = c.tw[k];
     twp[k] = c.twp[k];
     e_tab[k] = c.slot_exp[k];
     s_tab[k] = c.exp_slot[k];
   }
-  if (c.approx == 0) {
+  if (v.approx == 0) {
     for (int k = threadIdx.x; k < N; k += NT) {
-      fold_gadget3(c, c.wmask_R + k, Wm + k, N);
-      fold_gadget3(c, yR + k, Y + k, N);
+      fold_gadget3(v.ld_inv_R, v.ld_c0_R, v.ld_c1_R, v.wmask_R + k, Wm + k, N);
+      fold_gadget3(v.ld_inv_R, v.ld_c0_R, v.ld_c1_R, yR + k, Y + k, N);
     }
   } else {
-    for (u32 k = threadIdx.x; k < c.rows * N; k += NT) {
-      Wm[k] = c.wmask_R[k];
+    for (u32 k = threadIdx.x; k < v.rows * N; k += NT) {
+      Wm[k] = v.wmask_R[k];
       Y[k] = yR[k];
     }
   }
@@ -631,9 +693,9 @@ __device__ __forceinline__ u64 finish_a(const CrsDev& c, u64 x, u64 ms) {
   const u64 v = shoup(x, c.ninv, c.ninvp);
   return ms ? mod_switch_word(v, ms) : v;
 }
-__device__ __forceinline__ u64 finish_b(const CrsDev& c, u64 x, u32 t, u32 qi, const u64* b_fold, u64 ms) {
+__device__ __forceinline__ u64 finish_b(const CrsDev& c, u64 x, u32 t, u32 gamma, const u64* fold, u64 ms) {
   u64 v = shoup(x, c.ninv, c.ninvp);
-  if (t < c.gamma) v = addq(v, b_fold[(size_t)qi * c.gamma + t]);
+  if (t < gamma) v = addq(v, fold[t]);
   return ms ? mod_switch_word(v, ms) : v;
 }
 
@@ -663,8 +725,8 @@ __device__ __forceinline__ int sw(int e) { return e ^ (((e >> 4) & 3) << 2); }
 // R_{i+1} takes digit 2's place in the sums.
 template <int LOGN>
 __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
-    k_respond(CrsDev c, const QueryDev* queries, const ShardDev* shards, const u64* b_fold, u64 ms_target,
-              u64* a_out, u64* b_out, u32* status, int force_serial) {
+    k_respond(CrsDev c, const QueryDev* queries, const ShardDev* shards, const u64* b_fold, u64* a_out, u64* b_out,
+              u32* status, int force_serial) {
   constexpr int N = 1 << LOGN, NT = N / 4, H = N / 2;
   constexpr u32 M2N = 2 * N - 1;
   constexpr u64 DMASK = (1ULL << 20) - 1;
@@ -674,21 +736,23 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
   u64* a_ntt = D + 2 * N;
   u64* tw = a_ntt + N;
   u64* twp = tw + N;
-  const u32 rows = c.rows;
+  // Room for three key rows whatever the query's gadget, so queries of different sets
+  // share a launch.
   u64* Wm = twp + N;
-  u64* Y = Wm + rows * N;
-  uint16_t* e_tab = reinterpret_cast<uint16_t*>(Y + rows * N);
+  u64* Y = Wm + 3 * N;
+  uint16_t* e_tab = reinterpret_cast<uint16_t*>(Y + 3 * N);
   uint16_t* s_tab = e_tab + N;
 
   const int tid = threadIdx.x;
-  const u32 qi = blockIdx.x;
-  const QueryDev qd = queries[qi];
+  const QueryDev qd = queries[blockIdx.x];
+  const u32 qi = qd.row;  // output and status row
   const ShardDev sh = shards[qd.shard];
-  const u32 gamma = c.gamma;
-  const bool exact = c.approx == 0;
+  const SetView ps = set_view(c, qd.crs);
+  const u32 gamma = ps.gamma;
+  const bool exact = ps.approx == 0;
   const int l0 = 4 * tid;
 
-  stage_constants<N, NT>(c, qd.seat_R, tw, twp, Wm, Y, e_tab, s_tab);
+  stage_constants<N, NT>(c, ps, qd.seat_R, tw, twp, Wm, Y, e_tab, s_tab);
   expand_a<N, NT>(qd, a_ntt, status, qi, force_serial);
   {
     u64* const bufs[1] = {a_ntt};
@@ -700,7 +764,7 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
 #pragma unroll
   for (int k = 0; k < 4; k++) et[k] = e_tab[l0 + k];
   {
-    const u32 gp = c.gpow[gamma - 1];
+    const u32 gp = ps.gpow[gamma - 1];
     const u64* Srow = sh.sums_R + (size_t)(gamma - 1) * N;
 #pragma unroll
     for (int k = 0; k < 4; k++) {
@@ -716,7 +780,7 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
     const u64* Srow = sh.sums_R + (size_t)i * N + l0;
     const ulonglong2 sv01 = *reinterpret_cast<const ulonglong2*>(Srow);
     const ulonglong2 sv23 = *reinterpret_cast<const ulonglong2*>(Srow + 2);
-    const u32 gp = c.gpow[i];
+    const u32 gp = ps.gpow[i];
     {
       // Inverse stages 0-1 of unit tid (block B = tid, m = N/2).
       u64 w0, w0p, w1, w1p, w2, w2p;
@@ -900,8 +964,8 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
 #pragma unroll
   for (int k = 0; k < 4; k++) {
     const int t = tid + k * NT;
-    a_out[(size_t)qi * N + t] = finish_a(c, D[t], ms_target);
-    b_out[(size_t)qi * N + t] = finish_b(c, D[N + t], t, qi, b_fold, ms_target);
+    a_out[(size_t)qi * N + t] = finish_a(c, D[t], qd.ms);
+    b_out[(size_t)qi * N + t] = finish_b(c, D[N + t], t, gamma, b_fold + qd.fold_off, qd.ms);
   }
 }
 
@@ -1026,8 +1090,8 @@ __device__ __forceinline__ void fwd_half_r2(u64* D, int s, int rank, const u64* 
 // (inspiring2.rs:1094-1161).
 template <int LOGN>
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
-    k_respond_pair(CrsDev c, const QueryDev* queries, const ShardDev* shards, const u64* b_fold, u64 ms_target,
-                   u64* a_out, u64* b_out, u32* status, int force_serial) {
+    k_respond_pair(CrsDev c, const QueryDev* queries, const ShardDev* shards, const u64* b_fold, u64* a_out,
+                   u64* b_out, u32* status, int force_serial) {
   namespace cg = cooperative_groups;
   constexpr int N = 1 << LOGN, NT = N / 4, H = N / 2, HU = N / 8;
   constexpr u32 M2N = 2 * N - 1;
@@ -1038,27 +1102,27 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
   u64* a_ntt = D + N;
   u64* tw = a_ntt + N;
   u64* twp = tw + N;
-  const u32 rows = c.rows;
-  u64* Wm = twp + N;
-  u64* Y = Wm + rows * N;
-  uint16_t* e_tab = reinterpret_cast<uint16_t*>(Y + rows * N);
+  u64* Wm = twp + N;  // room for three key rows, as in k_respond
+  u64* Y = Wm + 3 * N;
+  uint16_t* e_tab = reinterpret_cast<uint16_t*>(Y + 3 * N);
   uint16_t* s_tab = e_tab + N;
 
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = (int)cluster.block_rank();
   const u64* peerX = cluster.map_shared_rank(X, rank ^ 1);
   const int tid = threadIdx.x;
-  const u32 qi = blockIdx.x >> 1;
-  const QueryDev qd = queries[qi];
+  const QueryDev qd = queries[blockIdx.x >> 1];
+  const u32 qi = qd.row;  // output and status row
   const ShardDev sh = shards[qd.shard];
-  const u32 gamma = c.gamma;
-  const bool exact = c.approx == 0;
+  const SetView ps = set_view(c, qd.crs);
+  const u32 gamma = ps.gamma;
+  const bool exact = ps.approx == 0;
   const int own = rank * H, other = (rank ^ 1) * H;
   const int u = tid >> 1, dg = tid & 1;
   const int ls = 4 * u + 2 * dg;  // local slots ls, ls + 1
   const int ug = rank * HU + u;   // global unit index of slots 4u..4u+3
 
-  stage_constants<N, NT>(c, qd.seat_R, tw, twp, Wm, Y, e_tab, s_tab);
+  stage_constants<N, NT>(c, ps, qd.seat_R, tw, twp, Wm, Y, e_tab, s_tab);
   expand_a<N, NT>(qd, a_ntt, status, qi, force_serial);
   {
     u64* const bufs[1] = {a_ntt};
@@ -1069,7 +1133,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
 #pragma unroll
   for (int k = 0; k < 2; k++) et[k] = e_tab[own + ls + k];
   {
-    const u32 gp = c.gpow[gamma - 1];
+    const u32 gp = ps.gpow[gamma - 1];
     const u64* Srow = sh.sums_R + (size_t)(gamma - 1) * N;
 #pragma unroll
     for (int k = 0; k < 2; k++) {
@@ -1092,7 +1156,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
   for (int i = (int)gamma - 2; i >= 0; i--) {
     const u64* Srow = sh.sums_R + (size_t)i * N;
     const ulonglong2 sv = *reinterpret_cast<const ulonglong2*>(Srow + own + ls);
-    const u32 gp = c.gpow[i];
+    const u32 gp = ps.gpow[i];
     const int par = (i & 1) * H;
     u64* xh = X + par;
     {
@@ -1205,9 +1269,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
   for (int k = 0; k < 4; k++) {
     const int t = tid + k * NT;
     if (rank == 0)
-      a_out[(size_t)qi * N + t] = finish_a(c, D[t], ms_target);
+      a_out[(size_t)qi * N + t] = finish_a(c, D[t], qd.ms);
     else
-      b_out[(size_t)qi * N + t] = finish_b(c, D[t], t, qi, b_fold, ms_target);
+      b_out[(size_t)qi * N + t] = finish_b(c, D[t], t, gamma, b_fold + qd.fold_off, qd.ms);
   }
 }
 
@@ -1959,17 +2023,45 @@ cudaError_t store_fold(const CrsDev& c, const u64* H, u64* sums_R, cudaStream_t 
   return cudaGetLastError();
 }
 
-cudaError_t shard_scan(const CrsDev& c, const QueryDev* queries, const ShardDev* shards, u32 nq, u64* b_fold,
-                       u32* status, int mode_build, u64* tags_out, cudaStream_t s) {
+u32 scan_chunks(u32 gamma) { return (gamma + SCAN_COLS - 1) / SCAN_COLS; }
+
+cudaError_t shard_scan(const CrsDev& c, const QueryDev* queries, const ShardDev* shards, u32 nq, const u32* work,
+                       u32 nwork, u64* b_fold, u32* status, cudaStream_t s) {
   if (nq == 0) return cudaSuccess;
-  constexpr u32 per_cta = SCAN_WARPS * SCAN_ROWS;
-  dim3 grid((c.gamma + per_cta - 1) / per_cta, nq);
+  const u32 chunks = scan_chunks(c.gamma);
+  const u32 items = work ? nwork : nq * chunks;
+  if (items == 0) return cudaSuccess;
   const size_t smem = scan_smem_bytes((int)c.n);
+  const u32 split = (u32)scan_split((int)c.n);
   IG_DISPATCH_LOGN(c.logn, {
     auto k = k_scan<L>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k<<<grid, SCAN_WARPS * 32, smem, s>>>(c, queries, shards, b_fold, status, mode_build, tags_out);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(items * split);
+    cfg.blockDim = dim3(SCAN_WARPS * 32);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = split;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    e = cudaLaunchKernelEx(&cfg, k, c, queries, shards, work, chunks, b_fold, status);
+    if (e != cudaSuccess) return e;
+  });
+  return cudaGetLastError();
+}
+
+cudaError_t column_tags(const CrsDev& c, const u64* cols, const u64* key, u64* tags_out, const u64* expect,
+                        u32* mismatch, cudaStream_t s) {
+  if (c.gamma == 0) return cudaSuccess;
+  constexpr u32 per_cta = 8;  // warps of 256 threads, one column each
+  IG_DISPATCH_LOGN(c.logn, {
+    k_column_tags<L><<<(c.gamma + per_cta - 1) / per_cta, per_cta * 32, 0, s>>>(c.gamma, cols, key, tags_out,
+                                                                              expect, mismatch);
   });
   return cudaGetLastError();
 }
@@ -2092,11 +2184,11 @@ cudaError_t butterfly_peak(u64* out, int blocks, int iters, cudaStream_t s) {
 
 size_t respond_smem_bytes(const CrsDev& c, bool pair) {
   const size_t words = pair ? (size_t)(5 * c.n) : (size_t)(6 * c.n);
-  return (words + 2 * (size_t)c.rows * c.n) * 8 + 2 * (size_t)c.n * 2;
+  return (words + 2 * (size_t)3 * c.n) * 8 + 2 * (size_t)c.n * 2;  // three key rows
 }
 
 cudaError_t respond(const CrsDev& c, const QueryDev* queries, const ShardDev* shards, u32 nq,
-                    const u64* b_fold, u64 ms_target, u64* a_out, u64* b_out, u32* status,
+                    const u64* b_fold, u64* a_out, u64* b_out, u32* status,
                     int force_serial_expand, bool pair, cudaStream_t s) {
   if (nq == 0) return cudaSuccess;
   const size_t smem = respond_smem_bytes(c, pair);
@@ -2105,14 +2197,12 @@ cudaError_t respond(const CrsDev& c, const QueryDev* queries, const ShardDev* sh
       auto k = k_respond_pair<L>;
       cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return e;
-      k<<<2 * nq, (1 << L) / 4, smem, s>>>(c, queries, shards, b_fold, ms_target, a_out, b_out, status,
-                                           force_serial_expand);
+      k<<<2 * nq, (1 << L) / 4, smem, s>>>(c, queries, shards, b_fold, a_out, b_out, status, force_serial_expand);
     } else {
       auto k = k_respond<L>;
       cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return e;
-      k<<<nq, (1 << L) / 4, smem, s>>>(c, queries, shards, b_fold, ms_target, a_out, b_out, status,
-                                       force_serial_expand);
+      k<<<nq, (1 << L) / 4, smem, s>>>(c, queries, shards, b_fold, a_out, b_out, status, force_serial_expand);
     }
   });
   return cudaGetLastError();

@@ -40,12 +40,34 @@ struct CrsDev {
 // One query of a launch.
 struct QueryDev {
   u32 shard;          // index into the launch's shard table
-  u32 reserved;
+  u32 fold_off;       // first of the query's gamma words in the launch's b_fold
   const u32* seed;    // 8 ChaCha20 key words of the query's `a` seed
   const u64* b;       // coefficient-form b of the query (n words)
   const u64* seat_R;  // rows x n key body in R-form NTT (the packing-key seat)
   const u64* a;       // explicit coefficient-form `a` (unseeded query), or null
+  // The query's parameter set (a device copy of its CrsDev), or null for the launch's. Every
+  // set of one launch shares the ring: n, q, the transform ladders and the slot tables;
+  // gamma, the gadget, the key rows and the mask may differ per query.
+  const CrsDev* crs;
+  u64 ms;             // mod-switch target of the response (0: none)
+  u32 row;            // the query's row of the launch's outputs and status words
+  u32 pad;
 };
+
+// The parts of a parameter set that may differ between the queries of one respond launch.
+struct SetView {
+  u32 gamma, rows, approx;
+  const u32* gpow;
+  const u64* wmask_R;
+  u64 ld_inv_R, ld_c0_R, ld_c1_R;
+};
+
+__device__ __forceinline__ SetView set_view(const CrsDev& c, const CrsDev* own) {
+  if (own)
+    return SetView{own->gamma, own->rows, own->approx, own->gpow, own->wmask_R, own->ld_inv_R, own->ld_c0_R,
+                   own->ld_c1_R};
+  return SetView{c.gamma, c.rows, c.approx, c.gpow, c.wmask_R, c.ld_inv_R, c.ld_c0_R, c.ld_c1_R};
+}
 
 // The client's Gaussian sampler (math/gaussian.rs:95-224): acceptance thresholds (f64 bit
 // patterns of exp(-x^2 / 2 sigma^2), x = -tailcut .. tailcut) and rand's integer range.
@@ -61,6 +83,10 @@ struct ShardDev {
   const u64* tag_key;        // 2n key words
   const u64* tags;           // gamma column tags
   const uint16_t* cols16;    // the same words as u16 when all are below 2^16, else null
+  // 1 when the columns no longer give the store's tags (checked whenever the columns
+  // change): a respond on the shard is refused with DEV_TAG_MISMATCH.
+  u32 stale;
+  u32 pad;
 };
 
 }  // namespace ig
@@ -78,11 +104,19 @@ cudaError_t fold_gadget_keys(const CrsDev& c, u64* keys, u32 count, cudaStream_t
 cudaError_t ntt_rows(const CrsDev& c, const u64* in, u64* out, u32 rows, u64 scale, u64 scalep,
                      cudaStream_t s);
 
-// Shard scan over `nq` queries: for query q and column j, recomputes the column's tag and
-// b_fold[q][j] = coeff0(b_q * column_j). mode_build = 1 writes the tags of shard 0 of the
-// table into `tags_out` instead of checking.
-cudaError_t shard_scan(const CrsDev& c, const QueryDev* queries, const ShardDev* shards, u32 nq,
-                       u64* b_fold, u32* status, int mode_build, u64* tags_out, cudaStream_t s);
+// Shard scan over `nq` queries: for query q and column j < gamma_q,
+// b_fold[fold_off_q + j] = coeff0(b_q * column_j); a query on a stale shard gets
+// DEV_TAG_MISMATCH. The work list (nwork entries, query << 12 | chunk, chunk < scan_chunks
+// of the query's gamma) lets queries of different widths share a launch; without one, every
+// query has c's gamma.
+u32 scan_chunks(u32 gamma);
+cudaError_t shard_scan(const CrsDev& c, const QueryDev* queries, const ShardDev* shards, u32 nq, const u32* work,
+                       u32 nwork, u64* b_fold, u32* status, cudaStream_t s);
+
+// Keyed tags of a shard's gamma columns (u64 words, key: 2n words below 2^61 - 1) into
+// tags_out; with `expect` set, *mismatch gets 1 when a tag differs from expect instead.
+cudaError_t column_tags(const CrsDev& c, const u64* cols, const u64* key, u64* tags_out, const u64* expect,
+                        u32* mismatch, cudaStream_t s);
 
 // One shard's columns from its records (entries of entry_size bytes, at most n of them):
 // the gamma x n u64 words and their u16 copy.
@@ -103,11 +137,12 @@ cudaError_t compact16(const u64* cols, size_t words, uint16_t* out, u32* wide, c
 cudaError_t store_fold(const CrsDev& c, const u64* H, u64* sums_R, cudaStream_t s);
 
 // Fused per-query respond: expansion of `a`, store gather, backward recursion with the
-// online gather, final transforms, optional mod switch. One CTA per query.
-// `pair` selects two CTAs per query (a cluster of 2), for batches of at most half the SMs.
+// online gather, final transforms, the mod switch to each query's target (QueryDev::ms).
+// One CTA per query; `pair` selects two CTAs per query (a cluster of 2), for batches of at
+// most half the SMs. Queries may carry their own parameter set (QueryDev::crs) on c's ring.
 cudaError_t respond(const CrsDev& c, const QueryDev* queries, const ShardDev* shards,
-                    u32 nq, const u64* b_fold, u64 ms_target,
-                    u64* a_out, u64* b_out, u32* status, int force_serial_expand, bool pair, cudaStream_t s);
+                    u32 nq, const u64* b_fold, u64* a_out, u64* b_out, u32* status, int force_serial_expand,
+                    bool pair, cudaStream_t s);
 
 size_t respond_smem_bytes(const CrsDev& c, bool pair);
 

@@ -10,6 +10,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <random>
 #include <string>
@@ -111,6 +112,7 @@ struct CrsObj {
   u32 n = 0, logn = 0, gamma = 0, rows = 0, approx = 0;
   u64 p = 0;
   CrsDev dev{};
+  CrsDev* d_self = nullptr;  // device copy of `dev`, named by the queries of mixed launches
   std::vector<void*> allocs;
   size_t bytes = 0;
 };
@@ -122,8 +124,11 @@ struct ShardSlot {
   u64* tags = nullptr;
   uint16_t* cols16 = nullptr;  // u16 copy of the columns; valid when `compact`
   bool compact = false;
+  // The columns changed after the store was built and no longer give its tags
+  // (shard_store.rs:247-257): responds on the shard are refused until the store is rebuilt.
+  bool stale = false;
   // The device table entry of this shard.
-  ShardDev dev() const { return ShardDev{cols, sums, tag_key, tags, compact ? cols16 : nullptr}; }
+  ShardDev dev() const { return ShardDev{cols, sums, tag_key, tags, compact ? cols16 : nullptr, stale ? 1u : 0u, 0}; }
 };
 
 struct DbObj {
@@ -363,6 +368,20 @@ DbObj* get_db(ig_ctx* c, u64 h) {
   return it == c->dbs.end() ? nullptr : &it->second;
 }
 
+// The CRS's device copy of its constants (allocated once, rewritten when they change).
+int sync_crs_self(ig_ctx* c, CrsObj& o) {
+  if (!o.d_self) {
+    void* p = nullptr;
+    int rc = dalloc(c, &p, sizeof(CrsDev), &o.bytes);
+    if (rc) return rc;
+    o.allocs.push_back(p);
+    o.d_self = (CrsDev*)p;
+  }
+  IG_CUDA(c, cudaMemcpyAsync(o.d_self, &o.dev, sizeof(CrsDev), cudaMemcpyHostToDevice, c->stream));
+  IG_CUDA(c, cudaStreamSynchronize(c->stream));
+  return IG_OK;
+}
+
 int sync_table_entry(ig_ctx* c, DbObj& db, u32 s) {
   const ShardDev d = db.shards[s].dev();
   IG_CUDA(c, cudaMemcpyAsync(db.d_table + s, &d, sizeof d, cudaMemcpyHostToDevice, c->stream));
@@ -423,23 +442,35 @@ int build_store(ig_ctx* c, DbObj& db, CrsObj& o, u32 s) {
     k = cand;
   }
   IG_CUDA(c, cudaMemcpyAsync(sl.tag_key, key.data(), key.size() * 8, cudaMemcpyHostToDevice, c->stream));
-  // Tags through the scan kernel in build mode.
-  ShardDev sd{sl.cols, nullptr, sl.tag_key, nullptr, nullptr};
-  QueryDev qd{};
-  qd.shard = 0;
-  void *dq, *ds;
-  int rc = scratch(c, "build_q", sizeof(QueryDev), &dq);
+  IG_CUDA(c, igk::column_tags(o.dev, sl.cols, sl.tag_key, sl.tags, nullptr, nullptr, c->stream));
+  int rc = fold_store(c, o, sl.cols, sl.sums);
   if (rc) return rc;
-  rc = scratch(c, "build_s", sizeof(ShardDev), &ds);
-  if (rc) return rc;
-  IG_CUDA(c, cudaMemcpyAsync(dq, &qd, sizeof qd, cudaMemcpyHostToDevice, c->stream));
-  IG_CUDA(c, cudaMemcpyAsync(ds, &sd, sizeof sd, cudaMemcpyHostToDevice, c->stream));
-  IG_CUDA(c, igk::shard_scan(o.dev, (const QueryDev*)dq, (const ShardDev*)ds, 1, nullptr, nullptr, 1, sl.tags,
-                             c->stream));
-  rc = fold_store(c, o, sl.cols, sl.sums);
-  if (rc) return rc;
+  c->launches++;
   IG_CUDA(c, cudaStreamSynchronize(c->stream));
+  sl.stale = false;
   return sync_table_entry(c, db, s);
+}
+
+// After new columns land in a shard that holds a store: the columns' tags against the
+// store's (the check shard_store.rs:197-264 makes at every respond, made here once per
+// change, since the library writes every column word itself). A mismatch marks the shard
+// stale; columns equal to the stored ones keep it served.
+int check_store_tags(ig_ctx* c, CrsObj& o, ShardSlot& sl) {
+  if (!sl.sums) {
+    sl.stale = false;
+    return IG_OK;
+  }
+  void* flag;
+  int rc = scratch(c, "tag_mismatch", 4, &flag);
+  if (rc) return rc;
+  IG_CUDA(c, cudaMemsetAsync(flag, 0, 4, c->stream));
+  IG_CUDA(c, igk::column_tags(o.dev, sl.cols, sl.tag_key, nullptr, sl.tags, (u32*)flag, c->stream));
+  c->launches++;
+  u32 mismatch = 1;
+  IG_CUDA(c, cudaMemcpyAsync(&mismatch, flag, 4, cudaMemcpyDeviceToHost, c->stream));
+  IG_CUDA(c, cudaStreamSynchronize(c->stream));
+  sl.stale = mismatch != 0;
+  return IG_OK;
 }
 
 }  // namespace
@@ -738,6 +769,11 @@ int ig_crs_create(ig_ctx* c, uint32_t n, uint64_t q, uint64_t p, uint64_t gadget
   IG_CUDA(c, igk::ntt_rows(d, (const u64*)mraw, (u64*)wm, o.rows, R_MOD_Q, shoup_companion(R_MOD_Q), c->stream));
   IG_CUDA(c, cudaStreamSynchronize(c->stream));
   d.wmask_R = (const u64*)wm;
+  if ((rc = sync_crs_self(c, o))) {
+    for (void* p2 : o.allocs) cudaFree(p2);
+    c->obj_bytes -= o.bytes;
+    return rc;
+  }
   const u64 h = g_next_object++;
   c->crs[h] = o;
   *crs_out = h;
@@ -849,6 +885,8 @@ static int set_shard(ig_ctx* c, uint64_t dbh, uint32_t s, const uint64_t* cols, 
   IG_CUDA(c, cudaMemcpyAsync(&wide_h, wide, 4, cudaMemcpyDeviceToHost, c->stream));
   IG_CUDA(c, cudaStreamSynchronize(c->stream));
   sl.compact = wide_h == 0;
+  rc = check_store_tags(c, *o, sl);
+  if (rc) return rc;
   return sync_table_entry(c, *db, s);
 }
 
@@ -900,7 +938,9 @@ int ig_db_encode_records(ig_ctx* c, uint64_t dbh, uint32_t first_shard, const ui
     sl.compact = true;
     // The staging buffer is reused by the next shard only after this encode has read it.
     if (!on_device) IG_CUDA(c, cudaStreamSynchronize(c->stream));
-    int rc = sync_table_entry(c, *db, first_shard + (u32)s);
+    int rc = check_store_tags(c, o, sl);
+    if (rc) return rc;
+    rc = sync_table_entry(c, *db, first_shard + (u32)s);
     if (rc) return rc;
   }
   return IG_OK;
@@ -956,6 +996,7 @@ int ig_db_drop_packing_store(ig_ctx* c, uint64_t dbh, uint32_t s) {
     c->obj_bytes -= freed;
     sl.sums = sl.tag_key = sl.tags = nullptr;
   }
+  sl.stale = false;
   return sync_table_entry(c, *db, s);
 }
 
@@ -1226,12 +1267,15 @@ static int respond_host(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_t handle, c
   u64* h_b = h_a + (size_t)count * n;
   std::vector<QueryDev> qs(count);
   for (u32 i = 0; i < count; i++) {
+    qs[i] = QueryDev{};
     qs[i].shard = local[shard_ids[i]];
-    qs[i].reserved = 0;
+    qs[i].fold_off = i * (u32)g;
     qs[i].seed = as ? nullptr : (const u32*)((const uint8_t*)d_seeds + (size_t)i * 32);
     qs[i].a = as ? (const u64*)d_seeds + (size_t)i * n : nullptr;
     qs[i].b = (const u64*)d_bs + (size_t)i * n;
     qs[i].seat_R = seat;
+    qs[i].ms = ms_target;
+    qs[i].row = i;
   }
   cudaStream_t s = igint::host_call_stream(c, hc);
   if ((rc = stage_h2d(c, d_table, table.data(), table.size() * sizeof(ShardDev))) ||
@@ -1248,12 +1292,12 @@ static int respond_host(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_t handle, c
     for (auto& e : env_ev) cudaEventCreate(&e);
   if (env_prof) cudaEventRecord(env_ev[0], s);
   long pk = prof_begin(c, REGION_SCAN, s);
-  IG_CUDA(c, igk::shard_scan(o.dev, (const QueryDev*)d_q, (const ShardDev*)d_table, count, (u64*)d_fold,
-                             (u32*)d_status, 0, nullptr, s));
+  IG_CUDA(c, igk::shard_scan(o.dev, (const QueryDev*)d_q, (const ShardDev*)d_table, count, nullptr, 0, (u64*)d_fold,
+                             (u32*)d_status, s));
   prof_end(c, pk, s);
   if (env_prof) cudaEventRecord(env_ev[1], s);
   pk = prof_begin(c, REGION_RESPOND, s);
-  IG_CUDA(c, igk::respond(o.dev, (const QueryDev*)d_q, (const ShardDev*)d_table, count, (const u64*)d_fold, ms_target,
+  IG_CUDA(c, igk::respond(o.dev, (const QueryDev*)d_q, (const ShardDev*)d_table, count, (const u64*)d_fold,
                           (u64*)d_a, (u64*)d_b, (u32*)d_status, c->force_serial,
                           (u64)count * lanes <= c->pair_threshold, s));
   prof_end(c, pk, s);
@@ -1356,8 +1400,8 @@ int ig_respond_nopacking_batch(ig_ctx* c, uint64_t dbh, uint32_t count, const ui
   const u32* h_status = (const u32*)pin;
   std::vector<QueryDev> qs(count);
   for (u32 i = 0; i < count; i++) {
+    qs[i] = QueryDev{};
     qs[i].shard = local[shard_ids[i]];
-    qs[i].reserved = 0;
     qs[i].seed = as ? nullptr : (const u32*)((const uint8_t*)d_seeds + (size_t)i * 32);
     qs[i].a = as ? (const u64*)d_seeds + (size_t)i * n : nullptr;
     qs[i].b = (const u64*)d_bs + (size_t)i * n;
@@ -1634,7 +1678,7 @@ int ig_crs_set_galois_keys(ig_ctx* c, uint64_t crs, uint32_t count, uint32_t row
   }
   o->allocs.push_back(dk);
   o->dev.galois_R = (const u64*)dk;
-  return IG_OK;
+  return sync_crs_self(c, *o);
 }
 
 int ig_respond_one_packing_batch(ig_ctx* c, uint64_t dbh, uint32_t count, const uint32_t* shard_ids,
@@ -1698,8 +1742,8 @@ int ig_respond_one_packing_batch(ig_ctx* c, uint64_t dbh, uint32_t count, const 
   const u32* h_status = (const u32*)pin;
   std::vector<QueryDev> qs(count);
   for (u32 i = 0; i < count; i++) {
+    qs[i] = QueryDev{};
     qs[i].shard = local[shard_ids[i]];
-    qs[i].reserved = 0;
     qs[i].seed = as ? nullptr : (const u32*)((const uint8_t*)d_seeds + (size_t)i * 32);
     qs[i].a = as ? (const u64*)d_seeds + (size_t)i * n : nullptr;
     qs[i].b = (const u64*)d_bs + (size_t)i * n;
@@ -1766,26 +1810,230 @@ int ig_respond_seeded_batch_device(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_
     return rc;
   std::vector<QueryDev> qs(count);
   for (u32 i = 0; i < count; i++) {
+    qs[i] = QueryDev{};
     qs[i].shard = shard_ids[i];
-    qs[i].reserved = 0;
+    qs[i].fold_off = i * (u32)g;
     qs[i].seed = (const u32*)(d_seeds + (size_t)i * 32);
-    qs[i].a = nullptr;
     qs[i].b = d_bs + (size_t)i * n;
     qs[i].seat_R = seat;
+    qs[i].ms = ms_target;
+    qs[i].row = i;
   }
   if ((rc = stage_h2d(c, d_q, qs.data(), count * sizeof(QueryDev)))) return rc;
   if ((rc = igint::lane_enter(c, lane))) return rc;
   IG_CUDA(c, cudaMemsetAsync(d_status, 0, count * 4, s));
   long pk = prof_begin(c, REGION_SCAN, s);
-  IG_CUDA(c, igk::shard_scan(o.dev, (const QueryDev*)d_q, db->d_table, count, (u64*)d_fold, d_status, 0, nullptr, s));
+  IG_CUDA(c, igk::shard_scan(o.dev, (const QueryDev*)d_q, db->d_table, count, nullptr, 0, (u64*)d_fold, d_status, s));
   prof_end(c, pk, s);
   // Two CTAs per query only while every lane's batch still leaves SMs for them.
   const bool pair = (u64)count * c->lanes <= c->pair_threshold;
   pk = prof_begin(c, REGION_RESPOND, s);
-  IG_CUDA(c, igk::respond(o.dev, (const QueryDev*)d_q, db->d_table, count, (const u64*)d_fold, ms_target, d_a, d_b,
-                          d_status, c->force_serial, pair, s));
+  IG_CUDA(c, igk::respond(o.dev, (const QueryDev*)d_q, db->d_table, count, (const u64*)d_fold, d_a, d_b, d_status,
+                          c->force_serial, pair, s));
   prof_end(c, pk, s);
   return igint::lane_release(c, lane);
+}
+
+// ---- mixed launches ------------------------------------------------------------------------
+// Queries of several databases, parameter sets, seats and mod-switch targets in one launch
+// (the reference answers one respond_seeded_batch call per key and database,
+// respond.rs:1189-1202; here the calls of a server's queue share one scan and one respond
+// launch). All sets must share the ring: n, q and with them the transform ladders and slot
+// tables the kernels take from the launch's constants; gamma, the gadget and the mask rows
+// come from each query's own set.
+struct MixedPlan {
+  CrsDev ring{};                 // the first query's set: the launch's ring constants
+  std::vector<ShardDev> table;   // distinct (database, shard) pairs of the launch
+  std::vector<QueryDev> qs;      // launch order: longest recursion (gamma) first
+  std::vector<u32> work;         // scan work items, position << 12 | chunk
+  size_t fold_words = 0;
+};
+
+// Resolves and checks every query (the caller holds the context lock). The whole batch is
+// refused on the first error, with the reference's message where it has one. Seeds and b
+// are left for the caller to point at its copies (query row r at row r of its arrays).
+static int plan_mixed(ig_ctx* c, u32 count, const uint64_t* dbs, const uint64_t* stores, const uint64_t* handles,
+                      const uint32_t* shard_ids, const uint64_t* ms_targets, MixedPlan& P) {
+  std::map<std::pair<u64, u32>, u32> local;
+  std::vector<std::pair<u32, u32>> order;  // (gamma, row)
+  u32 n = 0;
+  P.qs.resize(count);
+  for (u32 i = 0; i < count; i++) {
+    DbObj* db = get_db(c, dbs[i]);
+    if (!db) return fail(c, IG_ERR_HANDLE, "query %u: unknown database handle %llu", i, (unsigned long long)dbs[i]);
+    CrsObj& o = *get_crs(c, db->crs);
+    if (i == 0) {
+      n = o.n;
+      P.ring = o.dev;
+    } else if (o.n != n) {
+      return fail(c, IG_ERR_SHAPE, "query %u: ring_dim %u differs from the launch's ring_dim %u; one launch serves one ring",
+                  i, o.n, n);
+    }
+    const u64 ms = ms_targets ? ms_targets[i] : 0;
+    if (ms && (ms >= Q || ms < o.p || ms % (2ULL * n) != 1))
+      return fail(c, IG_ERR_ARG, "query %u: mod-switch target_modulus %llu must be in [p, q) and 1 mod 2d", i,
+                  (unsigned long long)ms);
+    const u64* seat;
+    int rc = resolve_seat(c, o, stores[i], handles[i], nullptr, 0, 0, &seat);
+    if (rc) return rc;
+    const u32 s = shard_ids[i];
+    if (s >= db->num_shards)
+      return fail(c, IG_ERR_ARG, "query %u: shard %u not found at dense position %u; encoded database has %u shards", i,
+                  s, s, db->num_shards);
+    if (!db->shards[s].sums)
+      return fail(c, IG_ERR_ARG, "query %u: shard %u has no packing store; mixed launches serve stored shards", i, s);
+    auto key = std::make_pair(dbs[i], s);
+    auto it = local.find(key);
+    if (it == local.end()) {
+      it = local.emplace(key, (u32)P.table.size()).first;
+      P.table.push_back(db->shards[s].dev());
+    }
+    QueryDev& q = P.qs[i];
+    q = QueryDev{};
+    q.shard = it->second;
+    q.seat_R = seat;
+    q.crs = o.d_self;
+    q.ms = ms;
+    q.row = i;
+    order.emplace_back(o.gamma, i);
+  }
+  // Longest recursion first, so the launch's tail is its shortest queries.
+  std::stable_sort(order.begin(), order.end(), [](const std::pair<u32, u32>& x, const std::pair<u32, u32>& y) {
+    return x.first > y.first;
+  });
+  std::vector<QueryDev> sorted(count);
+  for (u32 p = 0; p < count; p++) {
+    sorted[p] = P.qs[order[p].second];
+    sorted[p].fold_off = (u32)P.fold_words;
+    const u32 gamma = order[p].first;
+    for (u32 ch = 0; ch < igk::scan_chunks(gamma); ch++) P.work.push_back((p << 12) | ch);
+    P.fold_words += gamma;
+  }
+  P.qs.swap(sorted);
+  return IG_OK;
+}
+
+int ig_respond_mixed_batch_device(ig_ctx* c, uint32_t count, const uint64_t* dbs, const uint64_t* stores,
+                                  const uint64_t* handles, const uint32_t* shard_ids, const uint8_t* d_seeds,
+                                  const uint64_t* d_bs, const uint64_t* ms_targets, uint64_t* d_a, uint64_t* d_b,
+                                  uint32_t* d_status) {
+  if (!c) return IG_ERR_ARG;
+  if (count == 0 || !dbs || !stores || !handles || !shard_ids || !d_seeds || !d_bs || !d_a || !d_b || !d_status)
+    return fail(c, IG_ERR_ARG, "ig_respond_mixed_batch_device: empty batch or null buffer");
+  if (count >= (1u << 20)) return fail(c, IG_ERR_ARG, "ig_respond_mixed_batch_device: at most 2^20 - 1 queries a launch");
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  MixedPlan P;
+  int rc = plan_mixed(c, count, dbs, stores, handles, shard_ids, ms_targets, P);
+  if (rc) return rc;
+  const size_t n = P.ring.n;
+  for (QueryDev& q : P.qs) {
+    q.seed = (const u32*)(d_seeds + (size_t)q.row * 32);
+    q.b = d_bs + (size_t)q.row * n;
+  }
+  int lane = -1;
+  cudaStream_t s = c->stream;
+  if ((rc = igint::lane_acquire(c, &s, &lane))) return rc;
+  char nq[32], nt[32], nw[32], nf[32];
+  snprintf(nq, sizeof nq, "mix_queries%d", lane);
+  snprintf(nt, sizeof nt, "mix_table%d", lane);
+  snprintf(nw, sizeof nw, "mix_work%d", lane);
+  snprintf(nf, sizeof nf, "mix_fold%d", lane);
+  void *dq, *dt, *dw, *df;
+  if ((rc = scratch(c, nq, count * sizeof(QueryDev), &dq)) ||
+      (rc = scratch(c, nt, P.table.size() * sizeof(ShardDev), &dt)) ||
+      (rc = scratch(c, nw, P.work.size() * 4, &dw)) || (rc = scratch(c, nf, P.fold_words * 8, &df)))
+    return rc;
+  if ((rc = stage_h2d(c, dq, P.qs.data(), count * sizeof(QueryDev))) ||
+      (rc = stage_h2d(c, dt, P.table.data(), P.table.size() * sizeof(ShardDev))) ||
+      (rc = stage_h2d(c, dw, P.work.data(), P.work.size() * 4)) || (rc = igint::lane_enter(c, lane)))
+    return rc;
+  IG_CUDA(c, cudaMemsetAsync(d_status, 0, count * 4, s));
+  long pk = prof_begin(c, REGION_SCAN, s);
+  IG_CUDA(c, igk::shard_scan(P.ring, (const QueryDev*)dq, (const ShardDev*)dt, count, (const u32*)dw,
+                             (u32)P.work.size(), (u64*)df, d_status, s));
+  prof_end(c, pk, s);
+  const bool pair = (u64)count * c->lanes <= c->pair_threshold;
+  pk = prof_begin(c, REGION_RESPOND, s);
+  IG_CUDA(c, igk::respond(P.ring, (const QueryDev*)dq, (const ShardDev*)dt, count, (const u64*)df, d_a, d_b, d_status,
+                          c->force_serial, pair, s));
+  prof_end(c, pk, s);
+  c->launches += 2;
+  return igint::lane_release(c, lane);
+}
+
+int ig_respond_mixed_batch(ig_ctx* c, uint32_t count, const uint64_t* dbs, const uint64_t* stores,
+                           const uint64_t* handles, const uint32_t* shard_ids, const uint8_t* seeds, const uint64_t* bs,
+                           const uint64_t* ms_targets, uint64_t* a_out, uint64_t* b_out) {
+  if (!c) return IG_ERR_ARG;
+  if (count == 0 || !dbs || !stores || !handles || !shard_ids || !seeds || !bs || !a_out || !b_out)
+    return fail(c, IG_ERR_ARG, "ig_respond_mixed_batch: empty batch or null buffer");
+  if (count >= (1u << 20)) return fail(c, IG_ERR_ARG, "ig_respond_mixed_batch: at most 2^20 - 1 queries a call");
+  igint::HostCall hc;
+  igint::host_call_begin(c, hc);
+  const u32 k = hc.k;
+  std::unique_lock<std::mutex> lk(c->mu);
+  cudaSetDevice(c->device);
+  MixedPlan P;
+  int rc = plan_mixed(c, count, dbs, stores, handles, shard_ids, ms_targets, P);
+  if (rc) return rc;
+  const size_t n = P.ring.n;
+  void *dq, *dt, *dw, *df, *dseeds, *dbs_, *da, *db_, *dst;
+  auto lane_scratch = [&](const char* name, size_t bytes, void** out) {
+    char full[48];
+    snprintf(full, sizeof full, "%s%u", name, k);
+    return scratch(c, full, bytes, out);
+  };
+  if ((rc = lane_scratch("hmix_queries", count * sizeof(QueryDev), &dq)) ||
+      (rc = lane_scratch("hmix_table", P.table.size() * sizeof(ShardDev), &dt)) ||
+      (rc = lane_scratch("hmix_work", P.work.size() * 4, &dw)) ||
+      (rc = lane_scratch("hmix_fold", P.fold_words * 8, &df)) ||
+      (rc = lane_scratch("hmix_seeds", (size_t)count * 32, &dseeds)) ||
+      (rc = lane_scratch("hmix_bs", (size_t)count * n * 8, &dbs_)) ||
+      (rc = lane_scratch("hmix_a", (size_t)count * n * 8, &da)) ||
+      (rc = lane_scratch("hmix_b", (size_t)count * n * 8, &db_)) ||
+      (rc = lane_scratch("hmix_status", (size_t)count * 4, &dst)))
+    return rc;
+  for (QueryDev& q : P.qs) {
+    q.seed = (const u32*)((const uint8_t*)dseeds + (size_t)q.row * 32);
+    q.b = (const u64*)dbs_ + (size_t)q.row * n;
+  }
+  const size_t st_bytes = ((size_t)count * 4 + 15) & ~(size_t)15;
+  void* pin;
+  if ((rc = igint::host_call_pinned(c, hc, st_bytes + 2 * (size_t)count * n * 8, &pin))) return rc;
+  u32* h_status = (u32*)pin;
+  u64* h_a = (u64*)((uint8_t*)pin + st_bytes);
+  u64* h_b = h_a + (size_t)count * n;
+  cudaStream_t s = igint::host_call_stream(c, hc);
+  if ((rc = stage_h2d(c, dq, P.qs.data(), count * sizeof(QueryDev))) ||
+      (rc = stage_h2d(c, dt, P.table.data(), P.table.size() * sizeof(ShardDev))) ||
+      (rc = stage_h2d(c, dw, P.work.data(), P.work.size() * 4)) ||
+      (rc = stage_h2d(c, dseeds, seeds, (size_t)count * 32)) ||
+      (rc = stage_h2d(c, dbs_, bs, (size_t)count * n * 8)) || (rc = igint::host_call_enter(c, hc)))
+    return rc;
+  IG_CUDA(c, cudaMemsetAsync(dst, 0, count * 4, s));
+  IG_CUDA(c, igk::shard_scan(P.ring, (const QueryDev*)dq, (const ShardDev*)dt, count, (const u32*)dw,
+                             (u32)P.work.size(), (u64*)df, (u32*)dst, s));
+  IG_CUDA(c, igk::respond(P.ring, (const QueryDev*)dq, (const ShardDev*)dt, count, (const u64*)df, (u64*)da, (u64*)db_,
+                          (u32*)dst, c->force_serial, (u64)count * c->lanes <= c->pair_threshold, s));
+  c->launches += 2;
+  IG_CUDA(c, cudaMemcpyAsync(h_status, dst, count * 4, cudaMemcpyDeviceToHost, s));
+  IG_CUDA(c, cudaMemcpyAsync(h_a, da, (size_t)count * n * 8, cudaMemcpyDeviceToHost, s));
+  IG_CUDA(c, cudaMemcpyAsync(h_b, db_, (size_t)count * n * 8, cudaMemcpyDeviceToHost, s));
+  if ((rc = igint::host_call_launched(c, hc))) return rc;
+  lk.unlock();  // other callers launch while this batch runs
+  if ((rc = igint::host_call_wait(c, hc))) return rc;
+  for (u32 i = 0; i < count; i++) {
+    if (h_status[i] & DEV_TAG_MISMATCH)
+      return fail(c, IG_ERR_STORE_REFUSED,
+                  "shard %u: packing store refused: a column is not the column the store was built from. The shard "
+                  "changed after the build; rebuild the store before serving it",
+                  shard_ids[i]);
+    if (h_status[i]) return fail(c, IG_ERR_DEVICE, "query %u: respond kernel status %u", i, h_status[i]);
+  }
+  memcpy(a_out, h_a, (size_t)count * n * 8);
+  memcpy(b_out, h_b, (size_t)count * n * 8);
+  return IG_OK;
 }
 
 int ig_ctx_set_lanes(ig_ctx* c, uint32_t lanes) {
@@ -2194,8 +2442,10 @@ static int resolve_request_locked(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_t
   const ShardSlot& sl = db->shards[shard];
   if (!sl.cols) return fail(c, IG_ERR_ARG, "shard %u holds no columns", shard);
   out->crs = o.dev;
+  out->crs_dev = o.d_self;
   out->shard = sl.dev();
   out->seat = seat;
+  out->seat_rows = o.rows;
   out->crs_handle = db->crs;
   out->p = o.p;
   out->has_store = sl.sums != nullptr;
@@ -2230,7 +2480,7 @@ static constexpr size_t NOALLOC_QUERY_OFF = NOALLOC_FOLD_BYTES;
 static constexpr size_t NOALLOC_STATUS_OFF =
     NOALLOC_QUERY_OFF + ((NOALLOC_MAX_QUERIES * sizeof(QueryDev) + 255) / 256) * 256;
 static constexpr size_t NOALLOC_BYTES = NOALLOC_STATUS_OFF + 256;
-static_assert(NOALLOC_BYTES == 527104, "the header states this size");
+static_assert(NOALLOC_BYTES == 528640, "the header states this size");
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
 
 // Device address of g_noalloc_scratch on `device` (the current device). In host code the
@@ -2293,19 +2543,21 @@ int ig_respond_seeded_batch_noalloc(ig_ctx* c, uint64_t dbh, uint64_t st, uint64
   u32* d_status = (u32*)(base + NOALLOC_STATUS_OFF);
   QueryDev qs[NOALLOC_MAX_QUERIES];
   for (u32 i = 0; i < count; i++) {
+    qs[i] = QueryDev{};
     qs[i].shard = shard_ids[i];
-    qs[i].reserved = 0;
+    qs[i].fold_off = i * (u32)g;
     qs[i].seed = (const u32*)(d_seeds + (size_t)i * 32);
-    qs[i].a = nullptr;
     qs[i].b = d_bs + (size_t)i * n;
     qs[i].seat_R = seat;
+    qs[i].ms = ms_target;
+    qs[i].row = i;
   }
   cudaStream_t s = c->stream;
   IG_CUDA(c, cudaMemcpyAsync(d_q, qs, count * sizeof(QueryDev), cudaMemcpyHostToDevice, s));
   IG_CUDA(c, cudaMemsetAsync(d_status, 0, count * 4, s));
-  IG_CUDA(c, igk::shard_scan(o.dev, d_q, db->d_table, count, d_fold, d_status, 0, nullptr, s));
+  IG_CUDA(c, igk::shard_scan(o.dev, d_q, db->d_table, count, nullptr, 0, d_fold, d_status, s));
   // The launch shape of ig_respond_seeded_batch_device for the same batch and lane count.
-  IG_CUDA(c, igk::respond(o.dev, d_q, db->d_table, count, d_fold, ms_target, d_a, d_b, d_status, c->force_serial,
+  IG_CUDA(c, igk::respond(o.dev, d_q, db->d_table, count, d_fold, d_a, d_b, d_status, c->force_serial,
                           (u64)count * c->lanes <= c->pair_threshold, s));
   c->launches += 2;
   u32 status[NOALLOC_MAX_QUERIES];

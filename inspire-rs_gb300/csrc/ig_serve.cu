@@ -1,16 +1,20 @@
 // The serving loop: continuous batching of individually submitted respond requests.
 //
 // Requests (one seeded query each, under a registered seat) enter a queue. A dispatcher
-// thread takes the oldest request and every other waiting request that can share its
-// launch: the same parameter set and mod-switch target. Databases, shards and seats may
-// differ per query, because each launch carries its own shard table. The batch goes to a
-// free slot. Each slot owns a CUDA stream and device and pinned buffers sized when the loop
-// is created, so admission is bounded by memory fixed up front and a batch never allocates.
-// Batches on different slots overlap on the device, and requests that arrive while others
-// run are admitted as soon as a slot frees. A completion thread finishes slots in launch
-// order, copies each request's result to its caller's buffers and records its latency from
-// submission. A request's result is the one ig_respond_seeded_batch gives for the same
-// query, whatever batch it lands in.
+// thread forms a batch from the oldest waiting requests on one ring: databases, parameter
+// sets (record widths, exact or approximate gadget), shards, seats and mod-switch targets
+// may all differ within a batch, because every query of a launch carries its own set,
+// shard entry and target. Admission is by memory. The loop holds a budget of device bytes;
+// a request joins a batch only while the bytes its key and its buffers need fit in what the
+// batches in flight leave free. Its buffers (query descriptor, shard entry, scan work items,
+// seed, b, b fold, a and b out, status, wire bytes) are carved per batch from a device ring
+// of the budget's size and returned in launch order; its key (the seat, 49,152 B or
+// 32,768 B at ring 2048) counts once while any request on it is in flight. Each batch runs
+// on one of `slots` streams, so batches overlap on the device, and requests that arrive
+// while others run are admitted as slots and memory free up. A completion thread finishes
+// batches in launch order, copies each request's result to its caller's buffers and records
+// its latency from submission. A request's result is the one ig_respond_seeded_batch gives
+// for the same query, whatever batch it lands in.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -20,9 +24,11 @@
 #include <cstdio>
 #include <cstring>
 #include <deque>
+#include <map>
 #include <mutex>
 #include <string>
 #include <thread>
+#include <tuple>
 #include <unordered_map>
 #include <vector>
 
@@ -37,9 +43,13 @@ namespace {
 typedef std::chrono::steady_clock clk;
 
 constexpr size_t kMaxN = 2048;      // largest ring the respond kernels serve
-constexpr size_t kMaxGamma = 2048;  // largest packing width (gamma <= n)
+constexpr size_t kMaxGamma = 1024;  // largest packing width at that ring (gamma <= n/2)
 // Largest ServerResponse wire: header and trailer (78 bytes) and two 60-bit tight blocks.
 constexpr size_t kMaxWire = 78 + 2 * ((kMaxN * 60 + 7) / 8);
+constexpr size_t kAlign = 256;
+constexpr size_t kParts = 12;  // sub-buffers of a batch's region, each kAlign-aligned
+
+size_t up(size_t x) { return (x + kAlign - 1) & ~(kAlign - 1); }
 
 struct Req {
   u64 ticket = 0;
@@ -56,39 +66,99 @@ struct Req {
   int status = -1;  // -1 while waiting or in flight
   u64 latency_ns = 0;
   std::string err;
+  // Resolved when the request joins a batch.
+  igint::RequestView v{};
+  size_t wire_bytes = 0;  // its ServerResponse length (wire requests)
+};
+
+// Offsets of a batch's buffers within its region of the ring (device and pinned host
+// mirror alike). [q, fold) is staged to the device as one copy.
+struct Layout {
+  size_t q = 0, table = 0, work = 0, seeds = 0, bs = 0, fold = 0, a = 0, b = 0, status = 0, wire = 0, wstatus = 0,
+         tmpl = 0, total = 0;
+};
+
+Layout layout(size_t count, size_t n, size_t work, size_t fold, size_t wire, size_t tmpl) {
+  Layout L;
+  size_t o = 0;
+  auto put = [&](size_t bytes) {
+    const size_t at = o;
+    o += up(bytes);
+    return at;
+  };
+  L.q = put(count * sizeof(QueryDev));
+  L.table = put(count * sizeof(ShardDev));
+  L.work = put(work * 4);
+  L.seeds = put(count * 32);
+  L.bs = put(count * n * 8);
+  L.fold = put(fold * 8);
+  L.a = put(count * n * 8);
+  L.b = put(count * n * 8);
+  L.status = put(count * 4);
+  L.wire = put(wire);
+  L.wstatus = put(count * 4);
+  L.tmpl = put(tmpl);
+  L.total = o;
+  return L;
+}
+
+// Bytes one request adds to a batch's region (its share of every sub-buffer; the batch adds
+// kParts x kAlign of rounding once, and a template per (gamma, modulus) group of wire
+// requests).
+size_t request_bytes(size_t n, u32 gamma, size_t wire) {
+  return sizeof(QueryDev) + sizeof(ShardDev) + 4 * (size_t)igk::scan_chunks(gamma) + 32 + n * 8 + (size_t)gamma * 8 +
+         2 * n * 8 + 4 + wire + 4;
+}
+
+// One (gamma, modulus) group of wire requests in a batch: consecutive rows, one template.
+struct WireGroup {
+  u32 first = 0, count = 0, gamma = 0;
+  u64 modulus = 0;
+  size_t len = 0, tmpl_off = 0, out_off = 0;
 };
 
 struct Slot {
   cudaStream_t stream = nullptr;
   cudaEvent_t ready = nullptr;  // context work the batch depends on
   cudaEvent_t done = nullptr;
-  QueryDev* d_q = nullptr;
-  ShardDev* d_table = nullptr;
-  uint8_t* d_seeds = nullptr;
-  u64* d_bs = nullptr;
-  u64* d_fold = nullptr;
-  u64* d_a = nullptr;
-  u64* d_b = nullptr;
-  u32* d_status = nullptr;
-  uint8_t* d_wire = nullptr;
-  uint8_t* d_tmpl = nullptr;
-  u32* d_wstatus = nullptr;
-  QueryDev* h_q = nullptr;
-  ShardDev* h_table = nullptr;
-  uint8_t* h_seeds = nullptr;
-  u64* h_bs = nullptr;
-  u64* h_a = nullptr;
-  u64* h_b = nullptr;
-  u32* h_status = nullptr;
-  uint8_t* h_wire = nullptr;
-  uint8_t* h_tmpl = nullptr;
-  u32* h_wstatus = nullptr;
-  size_t wire_len = 0;  // bytes per response of the batch in flight (0: no wire requests)
+  std::vector<Req*> reqs;  // rows, in launch order
+  std::vector<WireGroup> groups;
+  size_t off = 0;  // the batch's region in the ring
+  Layout L;
+  u32 work_items = 0;
   bool want_ab = false;
-  std::vector<Req*> reqs;
   int launch_err = 0;
   u32 ctas = 0;  // CTAs of the batch in flight
   bool busy = false;
+};
+
+// A ring over [0, cap) whose regions are returned in the order they were carved.
+struct Ring {
+  size_t cap = 0, head = 0, tail = 0, used = 0;
+  std::deque<std::pair<size_t, size_t>> live;  // (offset, bytes), oldest first
+
+  bool wrapped() const { return head < tail || (head == tail && !live.empty()); }
+  bool fits(size_t bytes) const {
+    if (live.empty()) return bytes <= cap;
+    if (wrapped()) return tail - head >= bytes;
+    return cap - head >= bytes || tail >= bytes;
+  }
+  size_t take(size_t bytes) {  // the caller checked fits()
+    if (live.empty()) head = tail = 0;
+    const size_t off = (!wrapped() && cap - head < bytes) ? 0 : head;  // wrap: [head, cap) idles
+    head = off + bytes;
+    live.emplace_back(off, bytes);
+    used += bytes;
+    return off;
+  }
+  void give_oldest() {
+    used -= live.front().second;
+    live.pop_front();
+    if (live.empty())
+      head = tail = 0;
+    else
+      tail = live.front().first;
+  }
 };
 
 }  // namespace
@@ -109,66 +179,21 @@ struct ig_serve {
   u64 served = 0, refused = 0, batches = 0, batched_queries = 0;
   u32 inflight_ctas = 0;  // CTAs of all batches in flight
   std::vector<u64> latencies;
+  // Memory admission: the ring of request buffers (device, and its pinned host mirror) and
+  // the keys pinned by requests in flight, both counted against `budget`.
+  size_t budget = 0;
+  Ring ring;
+  uint8_t* d_arena = nullptr;
+  uint8_t* h_arena = nullptr;
+  std::unordered_map<const u64*, u32> seat_refs;  // seat -> requests in flight on it
+  size_t seat_bytes = 0;                          // bytes of the seats in seat_refs
+  size_t peak_bytes = 0;
+  // ServerResponse templates (zero coefficients) by (ring, gamma, modulus).
+  std::map<std::tuple<u32, u32, u64>, std::vector<uint8_t>> templates;
   size_t device_bytes = 0;
 };
 
 namespace {
-
-size_t slot_device_bytes(u32 B) {
-  return (size_t)B * (sizeof(QueryDev) + sizeof(ShardDev) + 32 + kMaxN * 8 * 3 + kMaxGamma * 8 + 8 + kMaxWire) +
-         kMaxWire;
-}
-
-int alloc_slot(ig_serve* s, Slot& sl) {
-  const size_t B = s->max_batch;
-  auto dev = [&](void** p, size_t bytes) -> int {
-    const int rc = igint::dalloc(s->ctx, p, bytes);
-    if (!rc) s->device_bytes += bytes;
-    return rc;
-  };
-  int rc;
-  if ((rc = dev((void**)&sl.d_q, B * sizeof(QueryDev))) || (rc = dev((void**)&sl.d_table, B * sizeof(ShardDev))) ||
-      (rc = dev((void**)&sl.d_seeds, B * 32)) || (rc = dev((void**)&sl.d_bs, B * kMaxN * 8)) ||
-      (rc = dev((void**)&sl.d_fold, B * kMaxGamma * 8)) || (rc = dev((void**)&sl.d_a, B * kMaxN * 8)) ||
-      (rc = dev((void**)&sl.d_b, B * kMaxN * 8)) || (rc = dev((void**)&sl.d_status, B * 4)) ||
-      (rc = dev((void**)&sl.d_wire, B * kMaxWire)) || (rc = dev((void**)&sl.d_tmpl, kMaxWire)) ||
-      (rc = dev((void**)&sl.d_wstatus, B * 4)))
-    return rc;
-  if (cudaHostAlloc((void**)&sl.h_q, B * sizeof(QueryDev), 0) ||
-      cudaHostAlloc((void**)&sl.h_table, B * sizeof(ShardDev), 0) || cudaHostAlloc((void**)&sl.h_seeds, B * 32, 0) ||
-      cudaHostAlloc((void**)&sl.h_bs, B * kMaxN * 8, 0) || cudaHostAlloc((void**)&sl.h_a, B * kMaxN * 8, 0) ||
-      cudaHostAlloc((void**)&sl.h_b, B * kMaxN * 8, 0) || cudaHostAlloc((void**)&sl.h_status, B * 4, 0) ||
-      cudaHostAlloc((void**)&sl.h_wire, B * kMaxWire, 0) || cudaHostAlloc((void**)&sl.h_tmpl, kMaxWire, 0) ||
-      cudaHostAlloc((void**)&sl.h_wstatus, B * 4, 0))
-    return igint::fail(s->ctx, IG_ERR_NOMEM, "serving loop: pinned host allocation of a slot failed");
-  if (cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) ||
-      cudaEventCreateWithFlags(&sl.ready, cudaEventDisableTiming) ||
-      cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming))
-    return igint::fail(s->ctx, IG_ERR_CUDA, "serving loop: stream or event creation failed");
-  return IG_OK;
-}
-
-void free_slot(ig_serve* s, Slot& sl) {
-  if (sl.stream) cudaStreamSynchronize(sl.stream);
-  const size_t B = s->max_batch;
-  igint::dfree(s->ctx, sl.d_q, B * sizeof(QueryDev));
-  igint::dfree(s->ctx, sl.d_table, B * sizeof(ShardDev));
-  igint::dfree(s->ctx, sl.d_seeds, B * 32);
-  igint::dfree(s->ctx, sl.d_bs, B * kMaxN * 8);
-  igint::dfree(s->ctx, sl.d_fold, B * kMaxGamma * 8);
-  igint::dfree(s->ctx, sl.d_a, B * kMaxN * 8);
-  igint::dfree(s->ctx, sl.d_b, B * kMaxN * 8);
-  igint::dfree(s->ctx, sl.d_status, B * 4);
-  igint::dfree(s->ctx, sl.d_wire, B * kMaxWire);
-  igint::dfree(s->ctx, sl.d_tmpl, kMaxWire);
-  igint::dfree(s->ctx, sl.d_wstatus, B * 4);
-  for (void* h : {(void*)sl.h_q, (void*)sl.h_table, (void*)sl.h_seeds, (void*)sl.h_bs, (void*)sl.h_a, (void*)sl.h_b,
-                  (void*)sl.h_status, (void*)sl.h_wire, (void*)sl.h_tmpl, (void*)sl.h_wstatus})
-    if (h) cudaFreeHost(h);
-  if (sl.ready) cudaEventDestroy(sl.ready);
-  if (sl.done) cudaEventDestroy(sl.done);
-  if (sl.stream) cudaStreamDestroy(sl.stream);
-}
 
 // Caller holds s->mu.
 void finish(ig_serve* s, Req* r, int status) {
@@ -193,12 +218,30 @@ void refuse(ig_serve* s, Req* r, int code, const char* fmt, ...) {
   finish(s, r, code);
 }
 
-// Forms one batch on a free slot: the oldest waiting request and every later one with the
-// same parameter set and mod-switch target, up to max_batch, in arrival order. Requests the
+// The zero-coefficient ServerResponse of (n, gamma, modulus), whose length is the wire's.
+// Caller holds s->mu.
+const std::vector<uint8_t>* wire_template(ig_serve* s, u32 n, u32 gamma, u64 modulus) {
+  auto key = std::make_tuple(n, gamma, modulus);
+  auto it = s->templates.find(key);
+  if (it != s->templates.end()) return &it->second;
+  std::vector<u64> zeros(n, 0);
+  std::vector<uint8_t> t(kMaxWire);
+  size_t len = 0;
+  if (ig_response_encode(zeros.data(), zeros.data(), n, gamma, modulus, t.data(), t.size(), &len) != IG_OK ||
+      len > kMaxWire)
+    return nullptr;
+  t.resize(len);
+  return &s->templates.emplace(key, std::move(t)).first->second;
+}
+
+// Forms one batch on a free slot from the oldest waiting requests on the head's ring, while
+// max_batch and memory allow: a request joins while the batch's region still fits the ring
+// and the ring's bytes, the pinned keys' bytes and the batch's stay within the budget
+// together. A request that could not fit even alone is refused (IG_ERR_NOMEM); requests the
 // context refuses finish here with the refusal. Returns the slot index, or -1 when nothing
 // was batched. Caller holds s->mu and has seen a free slot (the context lock is taken
 // inside, after s->mu).
-int form_batch(ig_serve* s, CrsDev* crs_out, u64* ms_out) {
+int form_batch(ig_serve* s, CrsDev* ring_out) {
   int slot = -1;
   for (u32 k = 0; k < s->nslots; k++)
     if (!s->slots[k].busy) {
@@ -208,11 +251,14 @@ int form_batch(ig_serve* s, CrsDev* crs_out, u64* ms_out) {
   if (slot < 0) return -1;
   Slot& sl = s->slots[slot];
   sl.reqs.clear();
-  bool have_head = false;
-  u64 crs = 0, ms = 0;
+  sl.groups.clear();
+  u32 n = 0;
+  size_t req_sum = 0, work = 0, fold = 0, wire = 0, tmpl = 0, new_seats = 0;
+  std::vector<const u64*> batch_seats;
+  std::vector<std::pair<u32, u64>> batch_groups;  // (gamma, modulus) of the batch's templates
   for (auto it = s->waiting.begin(); it != s->waiting.end() && sl.reqs.size() < s->max_batch;) {
     Req* r = *it;
-    igint::RequestView v;
+    igint::RequestView& v = r->v;
     const int rc = igint::resolve_request(s->ctx, r->db, r->store, r->handle, r->shard, &v);
     if (rc != IG_OK) {
       r->err = v.err;
@@ -239,30 +285,125 @@ int form_batch(ig_serve* s, CrsDev* crs_out, u64* ms_out) {
       it = s->waiting.erase(it);
       continue;
     }
-    if (!have_head) {
-      have_head = true;
-      crs = v.crs_handle;
-      ms = r->ms;
-      *crs_out = v.crs;
-      *ms_out = ms;
-    }
-    if (v.crs_handle != crs || r->ms != ms) {
+    if (sl.reqs.empty()) n = r->n;
+    if (r->n != n) {  // another ring waits for a later batch
       ++it;
       continue;
     }
-    const u32 i = (u32)sl.reqs.size();
-    sl.h_table[i] = v.shard;
-    QueryDev& q = sl.h_q[i];
-    q.shard = i;
-    q.reserved = 0;
-    q.seed = (const u32*)(sl.d_seeds + (size_t)i * 32);
-    q.b = sl.d_bs + (size_t)i * r->n;
-    q.seat_R = v.seat;
-    q.a = nullptr;
+    const u32 gamma = v.crs.gamma;
+    const u64 modulus = r->ms ? r->ms : Q;
+    size_t add_tmpl = 0;
+    r->wire_bytes = 0;
+    if (r->wire_out) {
+      const std::vector<uint8_t>* t = wire_template(s, n, gamma, modulus);
+      if (!t) {
+        refuse(s, r, IG_ERR_SHAPE, "ServerResponse encode refused for gamma %u over modulus %llu", gamma,
+               (unsigned long long)modulus);
+        it = s->waiting.erase(it);
+        continue;
+      }
+      r->wire_bytes = t->size();
+      if (std::find(batch_groups.begin(), batch_groups.end(), std::make_pair(gamma, modulus)) == batch_groups.end())
+        add_tmpl = t->size();
+    }
+    const bool seat_new = s->seat_refs.find(v.seat) == s->seat_refs.end() &&
+                          std::find(batch_seats.begin(), batch_seats.end(), v.seat) == batch_seats.end();
+    const size_t key_bytes = seat_new ? (size_t)v.seat_rows * n * 8 : 0;
+    const size_t mine = request_bytes(n, gamma, r->wire_bytes);
+    const size_t region = req_sum + mine + tmpl + add_tmpl + kParts * kAlign;
+    const size_t charged = s->ring.used + s->seat_bytes + new_seats + key_bytes + region;
+    if (!s->ring.fits(region) || charged > s->budget) {
+      const size_t alone = mine + r->wire_bytes + kParts * kAlign + (size_t)v.seat_rows * n * 8;
+      if (alone > s->budget) {
+        refuse(s, r, IG_ERR_NOMEM,
+               "admission refused: the request needs %zu device bytes (its key and buffers), the serving loop's "
+               "budget is %zu",
+               alone, s->budget);
+        it = s->waiting.erase(it);
+        continue;
+      }
+      break;  // waits, in arrival order, for batches in flight to return their memory
+    }
+    req_sum += mine;
+    work += igk::scan_chunks(gamma);
+    fold += gamma;
+    wire += r->wire_bytes;
+    if (add_tmpl) {
+      batch_groups.emplace_back(gamma, modulus);
+      tmpl += add_tmpl;
+    }
+    if (key_bytes) {
+      batch_seats.push_back(v.seat);
+      new_seats += key_bytes;
+    }
     sl.reqs.push_back(r);
     it = s->waiting.erase(it);
   }
   if (sl.reqs.empty()) return -1;
+  // Rows: longest recursion first (the launch's tail is its shortest queries), then by
+  // switch target and wire, so each (gamma, modulus) group of wire requests is consecutive.
+  std::stable_sort(sl.reqs.begin(), sl.reqs.end(), [](const Req* x, const Req* y) {
+    if (x->v.crs.gamma != y->v.crs.gamma) return x->v.crs.gamma > y->v.crs.gamma;
+    if (x->ms != y->ms) return x->ms < y->ms;
+    return (x->wire_out != nullptr) < (y->wire_out != nullptr);
+  });
+  const u32 count = (u32)sl.reqs.size();
+  sl.L = layout(count, n, work, fold, wire, tmpl);
+  sl.off = s->ring.take(sl.L.total);
+  for (Req* r : sl.reqs) s->seat_refs[r->v.seat]++;
+  s->seat_bytes += new_seats;
+  s->peak_bytes = std::max(s->peak_bytes, s->ring.used + s->seat_bytes);
+  // Host side of the region: descriptors, shard entries, work items, seeds, b, templates.
+  uint8_t* h = s->h_arena + sl.off;
+  uint8_t* d = s->d_arena + sl.off;
+  QueryDev* hq = (QueryDev*)(h + sl.L.q);
+  ShardDev* ht = (ShardDev*)(h + sl.L.table);
+  u32* hw = (u32*)(h + sl.L.work);
+  size_t fold_off = 0, wire_off = 0, tmpl_off = 0;
+  u32 work_n = 0;
+  sl.want_ab = false;
+  for (u32 i = 0; i < count; i++) {
+    Req* r = sl.reqs[i];
+    const u32 gamma = r->v.crs.gamma;
+    ht[i] = r->v.shard;
+    QueryDev& q = hq[i];
+    q = QueryDev{};
+    q.shard = i;
+    q.fold_off = (u32)fold_off;
+    q.seed = (const u32*)(d + sl.L.seeds + (size_t)i * 32);
+    q.b = (const u64*)(d + sl.L.bs) + (size_t)i * n;
+    q.seat_R = r->v.seat;
+    q.crs = r->v.crs_dev;
+    q.ms = r->ms;
+    q.row = i;
+    for (u32 ch = 0; ch < igk::scan_chunks(gamma); ch++) hw[work_n++] = (i << 12) | ch;
+    fold_off += gamma;
+    memcpy(h + sl.L.seeds + (size_t)i * 32, r->seed, 32);
+    memcpy(h + sl.L.bs + (size_t)i * n * 8, r->b.data(), (size_t)n * 8);
+    if (!r->wire_out) {
+      sl.want_ab = true;
+      continue;
+    }
+    const u64 modulus = r->ms ? r->ms : Q;
+    if (sl.groups.empty() || sl.groups.back().gamma != gamma || sl.groups.back().modulus != modulus) {
+      // Rows are sorted by (gamma, modulus), so each pair forms one group with one template.
+      WireGroup g;
+      g.first = i;
+      g.gamma = gamma;
+      g.modulus = modulus;
+      g.len = r->wire_bytes;
+      g.out_off = wire_off;
+      g.tmpl_off = tmpl_off;
+      const std::vector<uint8_t>* t = wire_template(s, n, gamma, modulus);
+      memcpy(h + sl.L.tmpl + tmpl_off, t->data(), t->size());
+      tmpl_off += t->size();
+      sl.groups.push_back(g);
+    }
+    sl.groups.back().count++;
+    wire_off += r->wire_bytes;
+  }
+  sl.work_items = work_n;
+  *ring_out = sl.reqs[0]->v.crs;
   sl.busy = true;
   return slot;
 }
@@ -270,8 +411,7 @@ int form_batch(ig_serve* s, CrsDev* crs_out, u64* ms_out) {
 void dispatch_loop(ig_serve* s) {
   cudaSetDevice(igint::device(s->ctx));
   for (;;) {
-    CrsDev crs{};
-    u64 ms = 0;
+    CrsDev ring{};
     int k;
     {
       std::unique_lock<std::mutex> lk(s->mu);
@@ -283,15 +423,19 @@ void dispatch_loop(ig_serve* s) {
             if (!x.busy) return true;
           return false;
         });
-        k = form_batch(s, &crs, &ms);
+        k = form_batch(s, &ring);
         if (k >= 0) break;
         s->cv_done.notify_all();  // requests refused while forming
+        // Nothing fit: wait until a batch in flight returns its memory.
+        const u64 done_before = s->batches - s->launched.size();
+        if (!s->waiting.empty() && !s->launched.empty())
+          s->cv_slot.wait(lk, [&] { return s->stop || s->batches - s->launched.size() != done_before; });
       }
     }
     s->cv_done.notify_all();
     Slot& sl = s->slots[k];
     const u32 count = (u32)sl.reqs.size();
-    const size_t n = crs.n;
+    const size_t n = ring.n;
     // Two CTAs per query only while the SMs left by the batches in flight hold them; with
     // other batches running, one CTA per query does the same work on fewer SMs.
     bool pair;
@@ -302,59 +446,44 @@ void dispatch_loop(ig_serve* s) {
       sl.ctas = pair ? 2 * count : count;
       s->inflight_ctas += sl.ctas;
     }
-    for (u32 i = 0; i < count; i++) {
-      memcpy(sl.h_seeds + (size_t)i * 32, sl.reqs[i]->seed, 32);
-      memcpy(sl.h_bs + i * n, sl.reqs[i]->b.data(), n * 8);
-    }
+    uint8_t* h = s->h_arena + sl.off;
+    uint8_t* d = s->d_arena + sl.off;
+    const Layout& L = sl.L;
     cudaStream_t st = sl.stream;
     // Ordered after every context call made before this batch formed (shard uploads, stores).
     cudaError_t e = cudaEventRecord(sl.ready, igint::stream(s->ctx));
     if (e == cudaSuccess) e = cudaStreamWaitEvent(st, sl.ready, 0);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(sl.d_q, sl.h_q, count * sizeof(QueryDev), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d + L.q, h + L.q, L.fold - L.q, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d + L.status, 0, count * 4, st);
     if (e == cudaSuccess)
-      e = cudaMemcpyAsync(sl.d_table, sl.h_table, count * sizeof(ShardDev), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(sl.d_seeds, sl.h_seeds, (size_t)count * 32, cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(sl.d_bs, sl.h_bs, (size_t)count * n * 8, cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(sl.d_status, 0, count * 4, st);
-    if (e == cudaSuccess) e = igk::shard_scan(crs, sl.d_q, sl.d_table, count, sl.d_fold, sl.d_status, 0, nullptr, st);
+      e = igk::shard_scan(ring, (const QueryDev*)(d + L.q), (const ShardDev*)(d + L.table), count,
+                          (const u32*)(d + L.work), sl.work_items, (u64*)(d + L.fold), (u32*)(d + L.status), st);
     if (e == cudaSuccess)
-      e = igk::respond(crs, sl.d_q, sl.d_table, count, sl.d_fold, ms, sl.d_a, sl.d_b, sl.d_status, 0, pair, st);
+      e = igk::respond(ring, (const QueryDev*)(d + L.q), (const ShardDev*)(d + L.table), count,
+                       (const u64*)(d + L.fold), (u64*)(d + L.a), (u64*)(d + L.b), (u32*)(d + L.status), 0, pair, st);
     if (e == cudaSuccess) {
       igint::add_launches(s->ctx, 2);
-      e = cudaMemcpyAsync(sl.h_status, sl.d_status, count * 4, cudaMemcpyDeviceToHost, st);
+      e = cudaMemcpyAsync(h + L.status, d + L.status, count * 4, cudaMemcpyDeviceToHost, st);
     }
-    // Outputs: the coefficient words for requests that want them, the wire bytes (built
-    // here from the words, tight codec) for requests that want those.
-    sl.want_ab = false;
-    sl.wire_len = 0;
-    bool want_wire = false;
-    for (const Req* r : sl.reqs) (r->wire_out ? want_wire : sl.want_ab) = true;
-    if (e == cudaSuccess && want_wire) {
-      const u64 modulus = ms ? ms : Q;
-      const unsigned bits = 64 - __builtin_clzll(modulus - 1);
-      const u32 a_bytes = (u32)(((u64)n * bits + 7) / 8), b_bytes = (u32)(((u64)crs.gamma * bits + 7) / 8);
-      std::vector<u64> zeros(n, 0);
-      size_t len = 0;
-      if (ig_response_encode(zeros.data(), zeros.data(), (u32)n, crs.gamma, modulus, sl.h_tmpl, kMaxWire, &len) ==
-              IG_OK &&
-          len <= kMaxWire) {
-        sl.wire_len = len;
-        e = cudaMemcpyAsync(sl.d_tmpl, sl.h_tmpl, len, cudaMemcpyHostToDevice, st);
-        if (e == cudaSuccess) e = cudaMemsetAsync(sl.d_wstatus, 0, count * 4, st);
-        if (e == cudaSuccess)
-          e = igk::wire(sl.d_a, sl.d_b, count, (u32)n, crs.gamma, bits, modulus, sl.d_tmpl, (u32)len, 12, a_bytes,
-                        12 + a_bytes + 41 + 8, b_bytes, sl.d_wire, sl.d_wstatus, st);
-        if (e == cudaSuccess) {
-          igint::add_launches(s->ctx, 1);
-          e = cudaMemcpyAsync(sl.h_wire, sl.d_wire, (size_t)count * len, cudaMemcpyDeviceToHost, st);
-        }
-        if (e == cudaSuccess) e = cudaMemcpyAsync(sl.h_wstatus, sl.d_wstatus, count * 4, cudaMemcpyDeviceToHost, st);
+    // Wire requests: the ServerResponse bytes (tight codec) built next to the words, one
+    // wire launch per (gamma, modulus) group of consecutive rows.
+    if (e == cudaSuccess && !sl.groups.empty()) {
+      e = cudaMemcpyAsync(d + L.tmpl, h + L.tmpl, L.total - L.tmpl, cudaMemcpyHostToDevice, st);
+      if (e == cudaSuccess) e = cudaMemsetAsync(d + L.wstatus, 0, count * 4, st);
+      for (const WireGroup& g : sl.groups) {
+        if (e != cudaSuccess) break;
+        const unsigned bits = 64 - __builtin_clzll(g.modulus - 1);
+        const u32 a_bytes = (u32)(((u64)n * bits + 7) / 8), b_bytes = (u32)(((u64)g.gamma * bits + 7) / 8);
+        e = igk::wire((const u64*)(d + L.a) + (size_t)g.first * n, (const u64*)(d + L.b) + (size_t)g.first * n,
+                      g.count, (u32)n, g.gamma, bits, g.modulus, d + L.tmpl + g.tmpl_off, (u32)g.len, 12, a_bytes,
+                      12 + a_bytes + 41 + 8, b_bytes, d + L.wire + g.out_off, (u32*)(d + L.wstatus) + g.first, st);
+        if (e == cudaSuccess) igint::add_launches(s->ctx, 1);
       }
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(h + L.wire, d + L.wire, L.wstatus + count * 4 - L.wire, cudaMemcpyDeviceToHost, st);
     }
     if (e == cudaSuccess && sl.want_ab)
-      e = cudaMemcpyAsync(sl.h_a, sl.d_a, (size_t)count * n * 8, cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess && sl.want_ab)
-      e = cudaMemcpyAsync(sl.h_b, sl.d_b, (size_t)count * n * 8, cudaMemcpyDeviceToHost, st);
+      e = cudaMemcpyAsync(h + L.a, d + L.a, L.status - L.a, cudaMemcpyDeviceToHost, st);
     cudaEventRecord(sl.done, st);
     {
       std::lock_guard<std::mutex> lk(s->mu);
@@ -382,41 +511,57 @@ void complete_loop(ig_serve* s) {
       });
       if (s->launched.empty()) return;
       k = s->launched.front();
-      s->launched.pop_front();
     }
     Slot& sl = s->slots[k];
     const cudaError_t e = cudaEventSynchronize(sl.done);
     {
       std::lock_guard<std::mutex> lk(s->mu);
+      s->launched.pop_front();
+      const uint8_t* h = s->h_arena + sl.off;
+      const Layout& L = sl.L;
+      const u32* h_status = (const u32*)(h + L.status);
+      const u32* h_wstatus = (const u32*)(h + L.wstatus);
+      size_t wire_off = 0;
       for (size_t i = 0; i < sl.reqs.size(); i++) {
         Req* r = sl.reqs[i];
+        const size_t n = r->n;
         if (sl.launch_err || e != cudaSuccess) {
           refuse(s, r, IG_ERR_CUDA, "serving launch failed: %s",
                  cudaGetErrorString(sl.launch_err ? (cudaError_t)sl.launch_err : e));
-        } else if (sl.h_status[i] & DEV_TAG_MISMATCH) {
+        } else if (h_status[i] & DEV_TAG_MISMATCH) {
           refuse(s, r, IG_ERR_STORE_REFUSED,
                  "shard %u: packing store refused: a column is not the column the store was built from. The shard "
                  "changed after the build; rebuild the store before serving it",
                  r->shard);
-        } else if (sl.h_status[i]) {
-          refuse(s, r, IG_ERR_DEVICE, "respond kernel status %u", sl.h_status[i]);
+        } else if (h_status[i]) {
+          refuse(s, r, IG_ERR_DEVICE, "respond kernel status %u", h_status[i]);
         } else if (r->wire_out) {
-          if (sl.wire_len == 0 || sl.h_wstatus[i]) {
+          if (h_wstatus[i]) {
             refuse(s, r, IG_ERR_SHAPE, "ServerResponse encode refused: coefficients must be canonical");
-          } else if (sl.wire_len > r->wire_cap) {
+          } else if (r->wire_bytes > r->wire_cap) {
             refuse(s, r, IG_ERR_ARG, "wire buffer of %zu bytes is smaller than the %zu-byte response", r->wire_cap,
-                   sl.wire_len);
+                   r->wire_bytes);
           } else {
-            memcpy(r->wire_out, sl.h_wire + i * sl.wire_len, sl.wire_len);
-            *r->wire_len = sl.wire_len;
+            memcpy(r->wire_out, h + L.wire + wire_off, r->wire_bytes);
+            *r->wire_len = r->wire_bytes;
             finish(s, r, IG_OK);
           }
         } else {
-          memcpy(r->a_out, sl.h_a + i * r->n, (size_t)r->n * 8);
-          memcpy(r->b_out, sl.h_b + i * r->n, (size_t)r->n * 8);
+          memcpy(r->a_out, h + L.a + i * n * 8, n * 8);
+          memcpy(r->b_out, h + L.b + i * n * 8, n * 8);
           finish(s, r, IG_OK);
         }
+        wire_off += r->wire_bytes;
       }
+      // The batch's memory returns: its region (the oldest in the ring) and its keys.
+      for (Req* r : sl.reqs) {
+        auto it = s->seat_refs.find(r->v.seat);
+        if (it != s->seat_refs.end() && --it->second == 0) {
+          s->seat_bytes -= (size_t)r->v.seat_rows * r->n * 8;
+          s->seat_refs.erase(it);
+        }
+      }
+      s->ring.give_oldest();
       sl.reqs.clear();
       sl.busy = false;
       s->inflight_ctas -= sl.ctas;
@@ -427,6 +572,17 @@ void complete_loop(ig_serve* s) {
   }
 }
 
+void free_loop(ig_serve* s) {
+  for (auto& sl : s->slots) {
+    if (sl.stream) cudaStreamSynchronize(sl.stream);
+    if (sl.ready) cudaEventDestroy(sl.ready);
+    if (sl.done) cudaEventDestroy(sl.done);
+    if (sl.stream) cudaStreamDestroy(sl.stream);
+  }
+  if (s->d_arena) igint::dfree(s->ctx, s->d_arena, s->budget);
+  if (s->h_arena) cudaFreeHost(s->h_arena);
+}
+
 }  // namespace
 
 extern "C" {
@@ -435,11 +591,11 @@ int ig_serve_create(ig_ctx* ctx, uint32_t slots, uint32_t max_batch, uint64_t hb
   if (!ctx) return IG_ERR_ARG;
   if (!out || slots == 0 || max_batch == 0 || slots > 64 || max_batch > 4096)
     return igint::fail(ctx, IG_ERR_ARG, "ig_serve_create: need 1..64 slots of 1..4096 queries and an out pointer");
-  const u64 need = (u64)slot_device_bytes(max_batch) * slots;
-  if (hbm_budget_bytes && need > hbm_budget_bytes)
-    return igint::fail(ctx, IG_ERR_NOMEM,
-                       "serving loop refused: %u slots of %u queries need %llu device bytes, the budget is %llu",
-                       slots, max_batch, (unsigned long long)need, (unsigned long long)hbm_budget_bytes);
+  // Default budget: every slot full of the largest requests (gamma 1024 at ring 2048, wire
+  // bytes, a key of three rows each).
+  const size_t largest = request_bytes(kMaxN, (u32)kMaxGamma, kMaxWire) + kMaxWire + 3 * kMaxN * 8;
+  const size_t budget =
+      hbm_budget_bytes ? (size_t)hbm_budget_bytes : (size_t)slots * ((size_t)max_batch * largest + kParts * kAlign);
   cudaSetDevice(igint::device(ctx));
   auto* s = new ig_serve();
   s->ctx = ctx;
@@ -447,16 +603,33 @@ int ig_serve_create(ig_ctx* ctx, uint32_t slots, uint32_t max_batch, uint64_t hb
   s->nslots = slots;
   s->max_waiting = (u64)slots * max_batch * 8;
   s->slots.resize(slots);
+  s->budget = budget;
+  s->ring.cap = budget;
   {
     std::lock_guard<std::mutex> lk(igint::mutex(ctx));
-    for (auto& sl : s->slots) {
-      const int rc = alloc_slot(s, sl);
-      if (rc) {
-        for (auto& x : s->slots) free_slot(s, x);
-        delete s;
-        return rc;
-      }
+    if (igint::dalloc(ctx, (void**)&s->d_arena, budget) != IG_OK) {
+      char why[256];
+      ig_last_error(ctx, why, sizeof why);
+      s->d_arena = nullptr;
+      delete s;
+      return igint::fail(ctx, IG_ERR_NOMEM, "serving loop refused: its %zu-byte device budget cannot be allocated (%s)",
+                         budget, why);
     }
+    s->device_bytes = budget;
+    if (cudaHostAlloc((void**)&s->h_arena, budget, 0) != cudaSuccess) {
+      s->h_arena = nullptr;
+      free_loop(s);
+      delete s;
+      return igint::fail(ctx, IG_ERR_NOMEM, "serving loop: pinned host allocation of %zu bytes failed", budget);
+    }
+    for (auto& sl : s->slots)
+      if (cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) ||
+          cudaEventCreateWithFlags(&sl.ready, cudaEventDisableTiming) ||
+          cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming)) {
+        free_loop(s);
+        delete s;
+        return igint::fail(ctx, IG_ERR_CUDA, "serving loop: stream or event creation failed");
+      }
   }
   s->dispatcher = std::thread(dispatch_loop, s);
   s->completer = std::thread(complete_loop, s);
@@ -471,12 +644,13 @@ int ig_serve_destroy(ig_serve* s) {
     s->stop = true;
   }
   s->cv_work.notify_all();
+  s->cv_slot.notify_all();
   s->dispatcher.join();
   s->cv_launched.notify_all();
   s->completer.join();
   {
     std::lock_guard<std::mutex> lk(igint::mutex(s->ctx));
-    for (auto& sl : s->slots) free_slot(s, sl);
+    free_loop(s);
   }
   for (auto& kv : s->tickets) delete kv.second;
   delete s;
@@ -630,9 +804,13 @@ int ig_serve_stats(ig_serve* s, ig_serve_stats_t* out, int reset) {
   out->p50_us = pct(0.50);
   out->p99_us = pct(0.99);
   out->max_us = v.empty() ? 0.0 : (double)v.back() / 1e3;
+  out->budget_bytes = s->budget;
+  out->inflight_bytes = s->ring.used + s->seat_bytes;
+  out->peak_inflight_bytes = s->peak_bytes;
   if (reset) {
     s->latencies.clear();
     s->served = s->refused = s->batches = s->batched_queries = 0;
+    s->peak_bytes = s->ring.used + s->seat_bytes;
   }
   return IG_OK;
 }

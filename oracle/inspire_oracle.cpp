@@ -723,20 +723,14 @@ struct Cell {
 
 static size_t num_columns(size_t entry) { return entry == 0 ? 1 : (entry + 1) / 2; }
 
-static Cell* cell_build(const Params& P, size_t entry_size, u64 seed, size_t entries) {
-  auto* c = new Cell();
-  c->P = P;
-  c->entry_size = entry_size;
+// setup_with_rng (pir/setup.rs:408-495) draws, once the cell's records, sampler and rng are
+// in place: the setup secret key, then one error polynomial per Galois-key row (their `a`
+// come from OS entropy and never reach a response), then the two public seeds. Returns the
+// setup secret.
+static Vec cell_setup_draws(Cell* c) {
+  const Params& P = c->P;
   size_t n = P.n;
-  // tests/packing_key_fixture/mod.rs:65-69 database formula.
-  c->db.resize(entries * entry_size);
-  for (size_t i = 0; i < c->db.size(); i++) c->db[i] = (uint8_t)(((u64)i * 0x9E3779B9ull + seed) >> 7);
-  c->sampler = GaussianSampler::with_seed(P.sigma, seed);
-  c->rng = ChaCha20Rng::seed_from_u64(seed ^ 0x5eed);
-  // setup_with_rng (pir/setup.rs:408-495): secret key, then one error polynomial per
-  // Galois-key row (their `a` come from OS entropy and never reach a response), then the
-  // two public seeds.
-  c->sk = sample_gaussian_poly(c->sampler, n, P.q);
+  Vec sk = sample_gaussian_poly(c->sampler, n, P.q);
   size_t log_d = 0;
   while ((size_t(1) << (log_d + 1)) <= n) log_d++;
   for (size_t i = 0; i < log_d; i++)
@@ -745,10 +739,19 @@ static Cell* cell_build(const Params& P, size_t entry_size, u64 seed, size_t ent
   c->rng.fill_bytes(c->w_seed, 32);
   uint8_t v_seed[32];
   c->rng.fill_bytes(v_seed, 32);
+  return sk;
+}
+
+// The rest of a cell once its secret c->sk is set: pack params, offline keys,
+// encode_database (encode_db.rs:74-134: one record per coefficient, 16-bit columns) and the
+// session's packing keys, ClientPackingKeys::generate_once (inspiring2.rs:764-791) and
+// generate_ksk_body (893-929), errors from the sampler.
+static void cell_finish(Cell* c) {
+  const Params& P = c->P;
+  size_t n = P.n, entry_size = c->entry_size;
   c->gamma = num_columns(entry_size);
   c->pp = make_pack_params(P, c->gamma);
   c->keys = make_offline_keys(*c->pp, c->w_seed);
-  // encode_database (encode_db.rs:74-134): one record per coefficient, 16-bit columns.
   size_t total = c->db.size() / entry_size;
   c->num_shards = (total + n - 1) / n;
   for (size_t s = 0; s < c->num_shards; s++) {
@@ -766,8 +769,6 @@ static Cell* cell_build(const Params& P, size_t entry_size, u64 seed, size_t ent
       }
     c->shards.push_back(cols);
   }
-  // ClientSession::new -> ClientPackingKeys::generate_once (inspiring2.rs:764-791) and
-  // generate_ksk_body (893-929).
   const Ntt& ntt = *c->pp->ntt;
   u64 gen = c->pp->generator % (2 * n);
   Vec tau_s = automorphism_coeff(c->sk, gen, P.q);
@@ -779,9 +780,51 @@ static Cell* cell_build(const Params& P, size_t entry_size, u64 seed, size_t ent
     for (size_t i = 0; i < n; i++) y[i] = addmod(addmod(mulmod(tau_s[i], gp, P.q), (P.q - s_w[i]) % P.q, P.q), e[i], P.q);
     c->y_body.push_back(y);
   }
+  c->stores.resize(c->num_shards);
+}
+
+// The KAT cell of tests/packing_key_fixture/mod.rs:65-146: the fixture's database formula,
+// the session built on the setup secret (ClientSession::new), and the probe query the
+// fixture makes before its recorded ones.
+static Cell* cell_build(const Params& P, size_t entry_size, u64 seed, size_t entries) {
+  auto* c = new Cell();
+  c->P = P;
+  c->entry_size = entry_size;
+  size_t n = P.n;
+  // tests/packing_key_fixture/mod.rs:65-69 database formula.
+  c->db.resize(entries * entry_size);
+  for (size_t i = 0; i < c->db.size(); i++) c->db[i] = (uint8_t)(((u64)i * 0x9E3779B9ull + seed) >> 7);
+  c->sampler = GaussianSampler::with_seed(P.sigma, seed);
+  c->rng = ChaCha20Rng::seed_from_u64(seed ^ 0x5eed);
+  c->sk = cell_setup_draws(c);
+  cell_finish(c);
   // The probe query_seeded(0): its `a` seed is OS entropy, its error draws n samples.
   for (size_t k = 0; k < n; k++) c->sampler.sample();
-  c->stores.resize(c->num_shards);
+  return c;
+}
+
+// The plain method as the reference's public API runs it: `entries` records of entry_size
+// uniform bytes from ChaCha20Rng::seed_from_u64(seed).fill_bytes; setup_with_rng under
+// GaussianSampler::with_seed(sigma, seed) and ChaCha20Rng::seed_from_u64(seed); then
+// ClientSession::with_seeded_secret (pir/session.rs:141-145), which draws the session's own
+// secret (RlweSecretKey::generate, rlwe/enc.rs:48-51) and its packing-key errors from the
+// same sampler. Queries follow with cell_next_query: the index and the `a` seed (OS entropy
+// in the reference, here the next 32 bytes of setup's rng) from the rng, the error from
+// the sampler.
+static Cell* cell_build_seeded(const Params& P, size_t entry_size, u64 seed, size_t entries) {
+  auto* c = new Cell();
+  c->P = P;
+  c->entry_size = entry_size;
+  c->db.resize(entries * entry_size);
+  {
+    ChaCha20Rng records = ChaCha20Rng::seed_from_u64(seed);
+    records.fill_bytes(c->db.data(), c->db.size());
+  }
+  c->sampler = GaussianSampler::with_seed(P.sigma, seed);
+  c->rng = ChaCha20Rng::seed_from_u64(seed);
+  (void)cell_setup_draws(c);  // the setup secret stays the server's; the session draws its own
+  c->sk = sample_gaussian_poly(c->sampler, P.n, P.q);
+  cell_finish(c);
   return c;
 }
 
@@ -1276,6 +1319,17 @@ void* orc_cell_build(u64 n, u64 q, u64 p, double sigma, u64 base, u64 glen, int 
     return nullptr;
   }
 }
+void* orc_cell_build_seeded(u64 n, u64 q, u64 p, double sigma, u64 base, u64 glen, int approx, u64 entry_size,
+                            u64 seed, u64 entries) {
+  try {
+    return cell_build_seeded(make_params(n, q, p, sigma, base, glen, approx), entry_size, seed, entries);
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return nullptr;
+  }
+}
+// rand's gen_range(0..bound) on the cell's rng (the query index of the plain method).
+u64 orc_cell_draw_index(void* cv, u64 bound) { return gen_range_u64(((Cell*)cv)->rng, 0, bound); }
 void orc_cell_free(void* c) { delete (Cell*)c; }
 void orc_cell_info(void* cv, u64* gamma, u64* num_shards, u64* key_rows, uint8_t* w_seed) {
   auto* c = (Cell*)cv;

@@ -63,6 +63,8 @@ def lib():
             "orc_cell_sampler_state": (None, [V, P, P]),
             "orc_cell_db": (U64, [V, P, U64]),
             "orc_cell_build": (V, [U64, U64, U64, ctypes.c_double, U64, U64, I, U64, U64, U64]),
+            "orc_cell_build_seeded": (V, [U64, U64, U64, ctypes.c_double, U64, U64, I, U64, U64, U64]),
+            "orc_cell_draw_index": (U64, [V, U64]),
             "orc_cell_free": (None, [V]),
             "orc_cell_info": (None, [V, P, P, P, P]),
             "orc_cell_columns": (None, [V, U64, P]),
@@ -311,10 +313,15 @@ class Cell:
     """A KAT cell: database, setup, client session and the reproducible query stream of the
     reference's tests/packing_key_fixture/mod.rs:90-146."""
 
-    def __init__(self, params: Params, entry_size: int, seed: int, entries=None):
+    def __init__(self, params: Params, entry_size: int, seed: int, entries=None, plain=False):
+        """plain=True: the plain method as the reference's public API runs it instead of the
+        fixture: records of uniform bytes from ChaCha20Rng::seed_from_u64(seed), setup_with_rng
+        and ClientSession::with_seeded_secret on GaussianSampler::with_seed(sigma, seed) and
+        ChaCha20Rng::seed_from_u64(seed); draw_index gives a query index from that rng."""
         self.params, self.entry_size, self.seed = params, entry_size, seed
         entries = 3 * params.n if entries is None else entries
-        self.h = lib().orc_cell_build(*params.args(), entry_size, seed, entries)
+        build = lib().orc_cell_build_seeded if plain else lib().orc_cell_build
+        self.h = build(*params.args(), entry_size, seed, entries)
         if not self.h:
             raise RuntimeError(lib().orc_last_error().decode())
         g, ns, kr = (ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64())
@@ -347,6 +354,10 @@ class Cell:
         out = np.zeros(L, dtype=np.uint8)
         lib().orc_cell_key_bytes(self.h, _p(out), L)
         return out.tobytes()
+
+    def draw_index(self, bound):
+        """rand's gen_range(0..bound) on the cell's rng."""
+        return int(lib().orc_cell_draw_index(self.h, bound))
 
     def next_query(self, index):
         sid = ctypes.c_uint32()

@@ -52,7 +52,7 @@ def test_injected_allocation_failures(pkg, oracle):
     lib.ig_debug_fail_alloc_at(ctx.h, 0)
     assert len(store) == 0
     h = store.register_server_side(keys, cache)
-    lib.ig_debug_fail_alloc_at(ctx.h, 3)
+    lib.ig_debug_fail_alloc_at(ctx.h, 1)  # the loop's one device allocation: its budget ring
     with pytest.raises(pkg.PirError, match="injected"):
         pkg.ServingLoop(ctx, slots=2, max_batch=8)
     lib.ig_debug_fail_alloc_at(ctx.h, 0)

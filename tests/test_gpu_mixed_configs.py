@@ -103,3 +103,84 @@ def test_serving_loop_across_all_sets(pkg, oracle, ctx, world):
         st = loop.stats()
     assert got == alone
     assert st["served"] == len(reqs) and st["batches"] >= len(sets)
+
+
+@pytest.mark.parametrize("threshold", [1 << 20, 0])
+def test_one_launch_across_all_sets(pkg, oracle, ctx, world, threshold):
+    """One scan and one respond launch over queries of all six sets, both seats of each and
+    two switch targets: every response is the one its query gets alone, under both launch
+    shapes (the launch orders its queries by gamma, so rows must come back in place)."""
+    store, sets = world
+    items = []
+    for k, s in enumerate(sets):
+        idx, qs = s.queries(pkg, 5, salt=4001 + 13 * k)
+        for j, q in enumerate(qs):
+            ms = pkg.MOD_SWITCH_TARGET_36BIT if (j + k) % 2 else 0
+            items.append((s, q, s.h_real if j % 2 == 0 else s.h_other, ms))
+    order = np.random.default_rng(11).permutation(len(items))
+    items = [items[i] for i in order]
+    alone = [pkg.respond_seeded_batch(s.crs, s.db, pkg.SeededQueryBatch(pkg.PackingKeySource.Registered(h), [q]),
+                                      s.cache, store, mod_switch_target=ms)[0].to_binary() for s, q, h, ms in items]
+    ctx.set_pair_threshold(threshold)
+    try:
+        got = pkg.respond_mixed_batch([pkg.MixedQuery(s.db, store, h, q, ms) for s, q, h, ms in items])
+    finally:
+        ctx.set_pair_threshold(76)
+    assert [r.to_binary() for r in got] == alone
+    # The first query of the mix against the oracle directly.
+    s, q, h, ms = items[0]
+    want = s.oracle_bytes(oracle, q, s.keys if h == s.h_real else s.other_keys)
+    if not ms:
+        assert got[0].to_binary() == want
+
+
+def test_mixed_launch_device_buffers_and_refusals(pkg, oracle, ctx, world):
+    import torch
+
+    store, sets = world
+    items = []
+    for k, s in enumerate(sets):
+        _, qs = s.queries(pkg, 3, salt=5003 + k)
+        items += [(s, q, s.h_real) for q in qs]
+    n = 2048
+    count = len(items)
+    dbs = np.array([s.db.h for s, _, _ in items], dtype=np.uint64)
+    stores = np.full(count, store.h, dtype=np.uint64)
+    handles = np.array([int(h) for _, _, h in items], dtype=np.uint64)
+    sids = np.array([q.shard_id for _, q, _ in items], dtype=np.uint32)
+    ms = np.zeros(count, dtype=np.uint64)
+    seeds = torch.from_numpy(np.stack([np.frombuffer(q.seed, dtype=np.uint8) for _, q, _ in items]).copy()).cuda()
+    bs = torch.from_numpy(np.stack([np.asarray(q.b, dtype=np.uint64) for _, q, _ in items]).view(np.int64)).cuda()
+    a = torch.zeros((count, n), dtype=torch.int64, device="cuda")
+    b = torch.zeros_like(a)
+    status = torch.full((count,), 7, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    ctx.check(ctx._lib.ig_respond_mixed_batch_device(
+        ctx.h, count, dbs.ctypes.data, stores.ctypes.data, handles.ctypes.data, sids.ctypes.data, seeds.data_ptr(),
+        bs.data_ptr(), ms.ctypes.data, a.data_ptr(), b.data_ptr(), status.data_ptr()))
+    ctx.join()
+    torch.cuda.synchronize()
+    assert int(status.abs().sum()) == 0
+    host = pkg.respond_mixed_batch([pkg.MixedQuery(s.db, store, h, q) for s, q, h in items])
+    a_h, b_h = a.cpu().numpy().view(np.uint64), b.cpu().numpy().view(np.uint64)
+    for i, r in enumerate(host):
+        assert np.array_equal(a_h[i], r.a) and np.array_equal(b_h[i], r.b)
+    # An unknown seat refuses the whole launch.
+    bad = [pkg.MixedQuery(s.db, store, h, q) for s, q, h in items]
+    bad[4] = pkg.MixedQuery(bad[4].db, store, 1 << 60, bad[4].query)
+    with pytest.raises(pkg.PirError, match="no entry for session_handle"):
+        pkg.respond_mixed_batch(bad)
+    # A shard whose columns changed after its store was built refuses the whole launch.
+    s0 = sets[0]
+    edited = s0.cell.columns(0)
+    edited[0, 0] ^= 1
+    s0.db.set_shard(0, edited)
+    try:
+        q_edit = pkg.SeededBatchQuery(*s0.cell.next_query(3))
+        mix = [pkg.MixedQuery(s.db, store, h, q) for s, q, h in items[-4:]] + [
+            pkg.MixedQuery(s0.db, store, s0.h_real, q_edit)]
+        with pytest.raises(pkg.PirError, match="packing store refused") as e:
+            pkg.respond_mixed_batch(mix)
+        assert e.value.code == 5
+    finally:
+        s0.db.set_shard(0, s0.cell.columns(0))  # the original words: the store serves again

@@ -170,6 +170,44 @@ def test_store_refuses_edited_columns_whole_batch(pkg, oracle, ctx):
     assert len(pkg.respond_seeded_batch(crs, db, batch, cache)) == 2
 
 
+def test_store_tags_follow_every_column_change(pkg, oracle, ctx):
+    """The tag check runs where the columns change (host upload, device upload, encode):
+    the same columns again keep the store served with the oracle's bytes, any edit refuses
+    the shard until its store is rebuilt."""
+    import torch
+
+    P = oracle.Params.d2048()
+    cell, crs, cache, db, keys = gpu_cell(pkg, oracle, P, 32, 0x7A65)
+    db.precompute_packing_all()
+    sid, seed, b = cell.next_query(2048 + 3)
+    q = pkg.SeededClientQuery(sid, seed, b, inspiring_packing_keys=keys)
+    want = oracle_bytes(oracle, cell, P, sid, seed, b)
+    assert pkg.respond_seeded_inspiring(crs, db, q).to_binary() == want
+    cols = cell.columns(1)
+    db.set_shard(1, cols)  # the same words: the tags still match
+    assert pkg.respond_seeded_inspiring(crs, db, q).to_binary() == want
+    edited = cols.copy()
+    edited[3, 2047] ^= 1 << 7
+    d_cols = torch.from_numpy(edited.view(np.int64)).cuda()
+    torch.cuda.synchronize()
+    db.set_shard_device(1, d_cols.data_ptr())
+    with pytest.raises(pkg.PirError, match="packing store refused") as e:
+        pkg.respond_seeded_inspiring(crs, db, q)
+    assert e.value.code == 5
+    d_cols = torch.from_numpy(cols.view(np.int64)).cuda()  # the original words restore the tags
+    torch.cuda.synchronize()
+    db.set_shard_device(1, d_cols.data_ptr())
+    assert pkg.respond_seeded_inspiring(crs, db, q).to_binary() == want
+    # Records encoded over the stored shard: other bytes refuse it, a rebuild serves them.
+    rec = bytearray(cell.database()[2048 * 32:2 * 2048 * 32])
+    rec[5] ^= 0xFF
+    db.encode_records(bytes(rec), 32, first_shard=1)
+    with pytest.raises(pkg.PirError, match="packing store refused"):
+        pkg.respond_seeded_inspiring(crs, db, q)
+    db.shards[1].precompute_packing()
+    assert len(pkg.respond_seeded_inspiring(crs, db, q).to_binary()) == len(want)
+
+
 def test_non_canonical_column_words_read_as_residues(pkg, oracle, ctx):
     """Words >= q are served as their residue on both branches (shard_store tests 204-257)."""
     P = oracle.Params.d2048()

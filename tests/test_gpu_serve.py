@@ -170,12 +170,33 @@ def test_refusals_finish_alone(pkg, oracle, ctx, sets):
     assert st["served"] == 3 and st["refused"] == 3
 
 
-def test_admission_by_device_budget(pkg, ctx):
-    with pytest.raises(pkg.PirError, match="serving loop refused") as e:
-        pkg.ServingLoop(ctx, slots=4, max_batch=64, hbm_budget_bytes=1 << 20)
+def test_admission_by_request_memory(pkg, ctx, sets):
+    """A budget that holds only a few requests' keys and buffers: every request is served with
+    its alone bytes, the bytes in flight never pass the budget, and batches stay small; a
+    budget below one request's key and buffers refuses that request (IG_ERR_NOMEM)."""
+    store, exact, approx = sets
+    # One gamma-256 request at ring 2048: about 51 KB of buffers, 48 KiB for its key.
+    budget = 400_000
+    reqs = [(exact, exact.query(pkg, (k * 104729 + 5) % (exact.cell.num_shards * 2048)),
+             pkg.MOD_SWITCH_TARGET_36BIT if k % 2 else 0) for k in range(24)]
+    alone = [ps.alone(pkg, store, q, ms).to_binary() for ps, q, ms in reqs]
+    with pkg.ServingLoop(ctx, slots=3, max_batch=64, hbm_budget_bytes=budget) as loop:
+        tickets = [loop.submit(ps.crs, ps.db, q, store, ps.handle, mod_switch_target=ms) for ps, q, ms in reqs]
+        got = [loop.wait(t, WAIT_MS).to_binary() for t in tickets]
+        st = loop.stats()
+    assert got == alone
+    assert st["budget_bytes"] == budget and st["device_bytes"] == budget
+    assert 0 < st["peak_inflight_bytes"] <= budget
+    assert st["mean_batch"] <= 7  # 64 would fit the slots; memory holds a batch to a handful
+    assert st["inflight_bytes"] == 0
+    with pkg.ServingLoop(ctx, slots=1, max_batch=4, hbm_budget_bytes=60_000) as loop:
+        t = loop.submit(exact.crs, exact.db, reqs[0][1], store, exact.handle)
+        with pytest.raises(pkg.PirError, match="admission refused") as e:
+            loop.wait(t, WAIT_MS)
+        assert e.value.code == 8
+    with pytest.raises(pkg.PirError, match="cannot be allocated") as e:
+        pkg.ServingLoop(ctx, slots=1, max_batch=4, hbm_budget_bytes=1 << 50)
     assert e.value.code == 8
-    with pkg.ServingLoop(ctx, slots=1, max_batch=4, hbm_budget_bytes=1 << 30) as loop:
-        assert 0 < loop.stats()["device_bytes"] <= 1 << 30
 
 
 def test_native_replay_matches_alone(pkg, oracle, ctx, sets):

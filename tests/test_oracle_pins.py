@@ -190,3 +190,21 @@ def test_tree_restatement_decodes(oracle):
         packed = oracle.response_bytes(ao, bo, cell.gamma)
         tree = oracle.response_bytes_tree(ao, bo, cell.gamma)
         assert tree[:-4] == packed[:-4] and packed[-4:] == bytes(4) and tree[-4:] == bytes([1, 0, 0, 0])
+
+
+def test_plain_method_cell_round_trips(oracle):
+    """The plain method's inputs (2048 uniform records of 32 bytes from seed 0, the seeded
+    setup and session, a uniform index) through the oracle's uncached respond: extract
+    returns the record."""
+    P = oracle.Params.d2048()
+    cell = oracle.Cell(P, 32, 0, entries=2048, plain=True)
+    assert (cell.gamma, cell.num_shards) == (16, 1)
+    index = cell.draw_index(2048)
+    assert 0 <= index < 2048
+    sid, seed, b = cell.next_query(index)
+    assert sid == 0
+    ao, bo = oracle.Cache(P, cell.gamma, cell.w_seed).respond_per_query(
+        cell.columns(0), oracle.expand_seed(seed, P.n), b, cell.keys())
+    ok, record = cell.decode(index, ao, bo)
+    assert ok and record == cell.record(index)
+    assert len(set(cell.database())) > 200  # uniform bytes, not the fixture's formula
