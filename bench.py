@@ -882,15 +882,24 @@ def run_nopack(args, rank, world):
 
 
 # ------------------------------------------------------------------------------------
-# Mixed databases: 32 B x 2^22 (gamma 16, 2048 shards), 512 B x 2^20 (gamma 256, 512
-# shards), 2048 B x 2^18 (gamma 1024, 128 shards), each under the exact and the approximate
-# gadget (six parameter sets), 128 keys spread over the sets, batch sizes drawn from
-# {1, 7, 33, 128, 512}; responses unswitched.
+# Uneven batching over three resident databases: 32 B x 2^22 (gamma 16, 2048 shards), 512 B
+# x 2^20 (gamma 256, 512 shards), 2048 B x 2^18 (gamma 1024, 128 shards), records of uniform
+# bytes from seeds 3, 4 and 5 encoded on the GPU. 128 keys, half under d2048 and half under
+# d2048_approximate_gadget, each registered under one (database width, gadget) set; a
+# database serves both gadgets' seats from one store. Every launch carries a batch of a size
+# drawn from {1, 7, 33, 128, 512} whose members each draw a key (so they span all three
+# databases and both gadgets) and a uniform shard; responses unswitched.
 C4_DBS = [(32, 2048, 3), (512, 512, 4), (2048, 128, 5)]  # entry bytes, shards, seed
 C4_KEYS = 128
 C4_BATCHES = (1, 7, 33, 128, 512)
-C4_METRIC = ("mixed-database respond queries/s (32/512/2048 B records x exact/approximate gadget, 128 keys, "
-             "batch sizes 1-512)")
+C4_METRIC = ("uneven-batch respond queries/s (members across 32/512/2048 B record databases and both gadgets, "
+             "128 keys, batch sizes 1-512)")
+
+
+def c4_records(torch, entry, shards, seed, rank):
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed + 1000 * rank)
+    return torch.randint(0, 256, (shards * N_RING * entry,), dtype=torch.uint8, device="cuda", generator=g)
 
 
 def run_cfg4(args, rank, world):
@@ -905,101 +914,184 @@ def run_cfg4(args, rank, world):
     ctx = pkg.Context(local)
     rng = np.random.default_rng(4 + rank)
     store = pkg.ServerSessionStore.new(ctx)
-    sets = []
+    dbs = []
     t0 = time.perf_counter()
     for entry, shards, seed in C4_DBS:
         if args.shards != NUM_SHARDS:
             shards = max(1, min(shards, args.shards))
         gamma = (entry + 1) // 2
-        g = torch.Generator(device="cuda")
-        g.manual_seed(seed + rank)
-        rec = torch.randint(0, 256, (shards * N_RING * entry,), dtype=torch.uint8, device="cuda", generator=g)
+        rec = c4_records(torch, entry, shards, seed, rank)
         torch.cuda.current_stream().synchronize()
-        for approx in (False, True):
-            params = pkg.InspireParams.d2048_approximate_gadget() if approx else pkg.InspireParams.d2048()
-            crs = pkg.ServerCrs(params, rng.integers(0, 256, 32, dtype=np.uint8).tobytes(), gamma)
-            cache = pkg.ServerInspiringCache.new(crs, ctx=ctx)
-            db = pkg.EncodedDatabase(cache, shards)
-            db.encode_records(None, entry, device_ptr=rec.data_ptr(), nbytes=rec.numel())
-            db.precompute_packing_all()
-            sets.append({"entry": entry, "gamma": gamma, "shards": shards, "approx": approx, "crs": crs,
-                         "cache": cache, "db": db, "rows": params.packing_key_rows(), "keys": []})
+        crs = pkg.ServerCrs(pkg.InspireParams.d2048(), rng.integers(0, 256, 32, dtype=np.uint8).tobytes(), gamma)
+        cache = pkg.ServerInspiringCache.new(crs, ctx=ctx)
+        db = pkg.EncodedDatabase(cache, shards)
+        db.encode_records(None, entry, device_ptr=rec.data_ptr(), nbytes=rec.numel())
+        db.precompute_packing_all()
         del rec
         torch.cuda.empty_cache()
+        # The approximate gadget's set of the same width: its seats run on this database.
+        crs_a = pkg.ServerCrs(pkg.InspireParams.d2048_approximate_gadget(),
+                              rng.integers(0, 256, 32, dtype=np.uint8).tobytes(), gamma)
+        cache_a = pkg.ServerInspiringCache.new(crs_a, ctx=ctx)
+        dbs.append({"entry": entry, "gamma": gamma, "shards": shards, "seed": seed, "db": db,
+                    "sets": [(crs, cache), (crs_a, cache_a)]})
+    keys = []  # (database index, gadget index, y_body, handle)
     for k in range(C4_KEYS):
-        st = sets[k % len(sets)]
-        keys = pkg.ClientPackingKeys(rand_words(rng, (st["rows"], N_RING)), st["gamma"])
-        st["keys"].append((keys, store.register_server_side(keys, st["cache"])))
+        di, gi = k % len(dbs), (k // len(dbs)) % 2
+        d = dbs[di]
+        rows = 2 if gi else 3
+        y = rand_words(rng, (rows, N_RING))
+        h = store.register_server_side(pkg.ClientPackingKeys(y, d["gamma"]), d["sets"][gi][1])
+        keys.append((di, gi, y, int(h)))
     setup_s = time.perf_counter() - t0
 
     total = args.warmup + args.steps
-    plan = []
+    plan = []  # per launch: key indices, shard ids
     for i in range(total):
-        si = int(rng.integers(0, len(sets)))
-        st = sets[si]
         count = int(rng.choice(C4_BATCHES))
-        kh = st["keys"][int(rng.integers(0, len(st["keys"])))]
-        sids = np.ascontiguousarray(rng.integers(0, st["shards"], count), dtype=np.uint32)
-        seeds = rng.integers(0, 256, (count, 32), dtype=np.uint8)
-        bs = rand_words(rng, (count, N_RING))
-        plan.append((si, count, kh, sids, seeds, bs))
-    offs = np.cumsum([0] + [p[1] for p in plan])
-    d_seeds = torch.from_numpy(np.concatenate([p[4] for p in plan])).cuda()
-    d_bs = torch.from_numpy(np.concatenate([p[5] for p in plan]).view(np.int64)).cuda()
-    d_a = torch.empty((int(offs[-1]), N_RING), dtype=torch.int64, device="cuda")
+        kidx = rng.integers(0, C4_KEYS, count)
+        sids = np.array([int(rng.integers(0, dbs[keys[k][0]]["shards"])) for k in kidx], dtype=np.uint32)
+        plan.append((count, kidx, sids))
+    offs = np.cumsum([0] + [p[0] for p in plan])
+    nq = int(offs[-1])
+    seeds_h = rng.integers(0, 256, (nq, 32), dtype=np.uint8)
+    bs_h = rand_words(rng, (nq, N_RING))
+    d_seeds = torch.from_numpy(seeds_h).cuda()
+    d_bs = torch.from_numpy(bs_h.view(np.int64)).cuda()
+    d_a = torch.empty((nq, N_RING), dtype=torch.int64, device="cuda")
     d_b = torch.empty_like(d_a)
-    d_status = torch.zeros(int(offs[-1]), dtype=torch.int32, device="cuda")
+    d_status = torch.zeros(nq, dtype=torch.int32, device="cuda")
+    arrays = []
+    for count, kidx, sids in plan:
+        arrays.append((np.array([dbs[keys[k][0]]["db"].h for k in kidx], dtype=np.uint64),
+                       np.full(count, store.h, dtype=np.uint64),
+                       np.array([keys[k][3] for k in kidx], dtype=np.uint64), sids,
+                       np.zeros(count, dtype=np.uint64)))
     torch.cuda.synchronize()
     lib = ctx._lib
     stream = torch.cuda.ExternalStream(ctx.stream)
     lanes = args.lanes
 
-    def step(i):
-        si, count, (_, handle), sids, _, _ = plan[i]
-        o = int(offs[i])
-        ctx.check(lib.ig_respond_seeded_batch_device(
-            ctx.h, sets[si]["db"].h, store.h, int(handle), count, sids.ctypes.data, d_seeds[o].data_ptr(),
-            d_bs[o].data_ptr(), 0, d_a[o].data_ptr(), d_b[o].data_ptr(), d_status[o:].data_ptr()))
+    def ctx_sms():
+        return torch.cuda.get_device_properties(local).multi_processor_count
 
-    ctx.set_lanes(lanes)
-    for i in range(args.warmup):
-        step(i)
-    ctx.join()
-    stream.synchronize()
-    torch.cuda.synchronize()
-    ctx.set_lanes(lanes)
-    launches0 = ctx.launch_count
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    barrier(world)
-    with ClockSampler(local) as clk:
-        with torch.cuda.stream(stream):
-            ev0.record(stream)
-            for i in range(args.warmup, total):
-                step(i)
-            ctx.join()
-            ev1.record(stream)
+    def launch(i):
+        count = plan[i][0]
+        dbh, sth, hh, sids, ms = arrays[i]
+        o = int(offs[i])
+        ctx.check(lib.ig_respond_mixed_batch_device(
+            ctx.h, count, dbh.ctypes.data, sth.ctypes.data, hh.ctypes.data, sids.ctypes.data, d_seeds[o].data_ptr(),
+            d_bs[o].data_ptr(), ms.ctypes.data, d_a[o].data_ptr(), d_b[o].data_ptr(), d_status[o:].data_ptr()))
+
+    def timed_region():
+        ctx.set_lanes(lanes)
+        for i in range(args.warmup):
+            launch(i)
+        ctx.join()
         stream.synchronize()
         torch.cuda.synchronize()
-    launches = ctx.launch_count - launches0
-    if int(d_status.abs().sum().item()) != 0:
-        raise RuntimeError("a batch was refused during the timed region")
-    timed_queries = int(offs[-1] - offs[args.warmup])
-    ms = max_over_ranks(ev0.elapsed_time(ev1), world)
-    value = world * timed_queries / (ms / 1e3)
+        ctx.set_lanes(lanes)
+        launches0 = ctx.launch_count
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        barrier(world)
+        with ClockSampler(local) as clk:
+            with torch.cuda.stream(stream):
+                ev0.record(stream)
+                for i in range(args.warmup, total):
+                    launch(i)
+                ctx.join()
+                ev1.record(stream)
+            stream.synchronize()
+            torch.cuda.synchronize()
+        ctx.set_lanes(1)
+        if int(d_status.abs().sum().item()) != 0:
+            raise RuntimeError("a launch was refused during the timed region")
+        return max_over_ranks(ev0.elapsed_time(ev1), world), ctx.launch_count - launches0, clk
 
-    # e2e: respond_seeded_batch with host buffers from `lanes` caller threads.
+    timed_queries = int(offs[-1] - offs[args.warmup])
+    # The fixed rule first (no table: two CTAs per query while count x lanes <= SMs / 2), then
+    # the launch-shape tuner's table for the three widths, then the same launches tuned.
+    ms_fixed, _, _ = timed_region()
+    t0 = time.perf_counter()
+    tuned = ctx.tune_launch_shapes([d["gamma"] for d in dbs], reps=2)
+    tune_s = time.perf_counter() - t0
+    ms_t, launches, clk = timed_region()
+    value = world * timed_queries / (ms_t / 1e3)
+    fixed_value = world * timed_queries / (ms_fixed / 1e3)
+
+    # Byte check outside the timing: the last launch's members from each database against
+    # the oracle's store path under the member's own key and set.
+    from oracle import oracle as O
+    O.build()
+    a_h = d_a.cpu().numpy().view(np.uint64)
+    b_h = d_b.cpu().numpy().view(np.uint64)
+    checked, seen = 0, set()
+    i_last = total - 1
+    while len(seen) < len(dbs) and i_last >= args.warmup:
+        count, kidx, sids = plan[i_last]
+        for j in range(count):
+            di, gi, y, _ = keys[kidx[j]]
+            if di in seen:
+                continue
+            seen.add(di)
+            d = dbs[di]
+            crs_j = d["sets"][gi][0]
+            P = O.Params.d2048_approximate_gadget() if gi else O.Params.d2048()
+            rec = c4_records(torch, d["entry"], d["shards"], d["seed"], rank)
+            s0 = int(sids[j]) * N_RING * d["entry"]
+            shard_bytes = rec[s0:s0 + N_RING * d["entry"]].cpu().numpy()
+            cols = np.ascontiguousarray(shard_bytes.view("<u2").reshape(N_RING, d["gamma"]).T, dtype=np.uint64)
+            st = O.Store(O.Cache(P, d["gamma"], crs_j.inspiring_w_seed), cols)
+            row = int(offs[i_last]) + j
+            ao, bo = st.respond(cols, O.expand_seed(seeds_h[row].tobytes(), N_RING), bs_h[row], y)
+            if O.response_bytes(ao, bo, d["gamma"]) != O.response_bytes(a_h[row], b_h[row], d["gamma"]):
+                raise RuntimeError(f"mixed launch differs from the oracle (database {di}, row {row})")
+            checked += 1
+            del rec
+        i_last -= 1
+    torch.cuda.empty_cache()
+
+    # Latency of small batches under each shape: batches of 1 and 7 on the 512-byte and the
+    # 2048-byte database (gamma 256 and 1024), one synchronous host-buffer call at a time.
+    latency = {}
+    for di in (1, 2):
+        d = dbs[di]
+        hk = next(k for k in keys if k[0] == di and k[1] == 0)[3]
+        cell = {}
+        for count in (1, 7):
+            qs_all = [pkg.MixedQuery(d["db"], store, hk,
+                                     pkg.SeededBatchQuery(int(rng.integers(0, d["shards"])), rng.bytes(32),
+                                                          rand_words(rng, N_RING)))
+                      for _ in range(count)]
+            row = {"tuned_choice": ctx.launch_shape_for(d["gamma"], count, ctx_sms())}
+            for shape in (1, 2, 4):
+                ctx.set_launch_shape(shape)
+                lat = []
+                for r in range(43):
+                    t = time.perf_counter()
+                    pkg.respond_mixed_batch(qs_all)
+                    if r >= 3:
+                        lat.append(time.perf_counter() - t)
+                lat_ms = np.sort(np.array(lat)) * 1e3
+                row[str(shape)] = {"p50_ms": float(lat_ms[len(lat_ms) // 2]),
+                                   "p99_ms": float(lat_ms[int(0.99 * (len(lat_ms) - 1))])}
+            ctx.set_launch_shape(0)
+            cell[f"batch{count}"] = row
+        latency[f"gamma{d['gamma']}"] = cell
+
+    # e2e: respond_mixed_batch with host buffers, one call per launch, from `lanes` threads.
     calls = []
-    for si, count, (keys, handle), sids, seeds, bs in plan:
-        st = sets[si]
-        qs = [pkg.SeededBatchQuery(int(sids[k]), seeds[k].tobytes(), bs[k]) for k in range(count)]
-        calls.append((st, pkg.SeededQueryBatch(pkg.PackingKeySource.Registered(handle), qs)))
+    for i, (count, kidx, sids) in enumerate(plan):
+        o = int(offs[i])
+        calls.append([pkg.MixedQuery(dbs[keys[k][0]]["db"], store, keys[k][3],
+                                     pkg.SeededBatchQuery(int(sids[j]), seeds_h[o + j].tobytes(), bs_h[o + j]))
+                      for j, k in enumerate(kidx)])
     errors = []
 
     def caller(idx):
         try:
             for i in idx:
-                st, batch = calls[i]
-                pkg.respond_seeded_batch(st["crs"], st["db"], batch, st["cache"], store)
+                pkg.respond_mixed_batch(calls[i])
         except Exception as e:  # reported below
             errors.append(e)
 
@@ -1019,54 +1111,41 @@ def run_cfg4(args, rank, world):
     if errors:
         raise errors[0]
 
-    # Per parameter set: batches of 128 on one set at a time, three lanes.
-    per_set = []
-    ps_seeds = torch.from_numpy(rng.integers(0, 256, (128, 32), dtype=np.uint8)).cuda()
-    ps_bs = torch.from_numpy(rand_words(rng, (128, N_RING)).view(np.int64)).cuda()
-    ps_a = torch.empty((128, N_RING), dtype=torch.int64, device="cuda")
-    ps_b = torch.empty_like(ps_a)
-    ps_status = torch.zeros(128, dtype=torch.int32, device="cuda")
-    torch.cuda.synchronize()
-    for si, st in enumerate(sets):
-        handle = st["keys"][0][1]
-        sids = np.ascontiguousarray(rng.integers(0, st["shards"], 128), dtype=np.uint32)
-        ctx.set_lanes(lanes)
-        reps = 6
-        for r in range(reps + 1):
-            if r == 1:
-                ctx.join()
-                stream.synchronize()
-                e0 = torch.cuda.Event(enable_timing=True)
-                e1 = torch.cuda.Event(enable_timing=True)
-                e0.record(stream)
-            ctx.check(lib.ig_respond_seeded_batch_device(
-                ctx.h, st["db"].h, store.h, int(handle), 128, sids.ctypes.data, ps_seeds.data_ptr(),
-                ps_bs.data_ptr(), 0, ps_a.data_ptr(), ps_b.data_ptr(), ps_status.data_ptr()))
-        ctx.join()
-        e1.record(stream)
-        stream.synchronize()
-        ctx.set_lanes(1)
-        if int(ps_status.abs().sum().item()) != 0:
-            raise RuntimeError("a per-set batch was refused")
-        per_set.append({"entry": st["entry"], "gamma": st["gamma"], "gadget": "approximate" if st["approx"] else "exact",
-                        "queries_per_s": reps * 128 / (e0.elapsed_time(e1) / 1e3)})
-    mix = {str(b): sum(1 for p in plan[args.warmup:] if p[1] == b) for b in C4_BATCHES}
+    # The plain per-query GPU path on the same members: one call per query under its own
+    # key, database and set (host buffers), over the first 512 timed members.
+    flat = [q for c in calls[args.warmup:] for q in c][:512]
+    t0 = time.perf_counter()
+    for q in flat:
+        pkg.respond_mixed_batch([q])
+    plain_qps = len(flat) / (time.perf_counter() - t0)
+    mix = {str(b): sum(1 for p in plan[args.warmup:] if p[0] == b) for b in C4_BATCHES}
     return {
         "metric": C4_METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "warmup": args.warmup, "ms_per_step": ms_t / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u64 (exact mod q = 2^60-2^14+1)",
         "data": "synthetic: uniform record bytes encoded on the GPU, uniform key and query words",
-        "config": {"workload": "six parameter sets (32 B x 2^22 gamma 16, 512 B x 2^20 gamma 256, 2048 B x 2^18 "
-                               "gamma 1024; exact and approximate gadget), 128 keys, one batch per step of a "
-                               "size drawn from {1, 7, 33, 128, 512} on a random set and key, uniform shards",
-                   "shards": [st["shards"] for st in sets[::2]], "keys": C4_KEYS, "lanes": lanes,
+        "config": {"workload": "three resident databases (32 B x 2^22 gamma 16, 512 B x 2^20 gamma 256, 2048 B x "
+                               "2^18 gamma 1024; seeds 3/4/5), 128 keys half exact and half approximate gadget, "
+                               "each launch a batch of a size drawn from {1, 7, 33, 128, 512} whose members draw "
+                               "a key and a uniform shard, so they span all three databases and both gadgets",
+                   "shards": [d["shards"] for d in dbs], "keys": C4_KEYS, "lanes": lanes,
                    "queries": timed_queries, "batch_mix": mix, "mod_switch": None,
-                   "l2": "inputs larger than L2: the six sets hold about 22 GiB of columns and stores"},
+                   "l2": "inputs larger than L2: the three databases hold about 10 GiB of columns and stores"},
+        "step": "one mixed launch (ig_respond_mixed_batch_device: one scan and one respond launch)",
+        "parity_checked": checked,
         "e2e": {"value": e2e, "unit": "queries/s", "h2d_bytes_per_step": int(timed_queries * (32 + N_RING * 8 + 4)
                                                                             / args.steps),
                 "d2h_bytes_per_step": int(timed_queries * 2 * N_RING * 8 / args.steps), "callers": lanes,
-                "call": "respond_seeded_batch (one batch per call)"},
-        "per_set": per_set, "gpu_launches": int(launches), "setup_s": setup_s, "clocks": clk.summary(),
+                "call": "respond_mixed_batch (one launch per call)"},
+        "fixed_rule": {"value": fixed_value, "unit": "queries/s",
+                       "rule": "two CTAs per query while count x lanes <= SMs / 2, else one"},
+        "launch_shapes": {"tuned_ms_per_wave": {str(g): {"1": t[0], "2": t[1], "4": t[2]} for g, t in tuned.items()},
+                          "tune_s": tune_s,
+                          "rule": "per launch the shape with the least ceil(count x ctas / (SMs / lanes)) x wave time"},
+        "latency": latency,
+        "plain_per_query": {"queries_per_s": plain_qps, "queries": len(flat),
+                            "call": "one respond_mixed_batch call per query (host buffers)"},
+        "gpu_launches": int(launches), "setup_s": setup_s, "clocks": clk.summary(),
         "device_bytes": ctx.device_bytes,
     }
 
@@ -1074,7 +1153,14 @@ def run_cfg4(args, rank, world):
 C5_SHARDS = 16384
 C5_SEATS = 1000
 C5_METRIC = ("served queries/s at saturation (continuous batching, 2^25 x 512 B records, 16,384 shards, "
-             "1000 seats, 36-bit mod switch)")
+             "1000 seats of 3- and 2-row gadgets, 36-bit mod switch)")
+C5_CHUNK = 512  # shards per piece of records generated on the device (512 MiB), seeded per piece
+
+
+def c5_records(torch, s0, k, rank):
+    g = torch.Generator(device="cuda")
+    g.manual_seed(6 + 1000 * rank + s0 // C5_CHUNK)
+    return torch.randint(0, 256, (k * N_RING * ENTRY_BYTES,), dtype=torch.uint8, device="cuda", generator=g)
 
 
 def run_cfg5(args, rank, world):
@@ -1089,14 +1175,15 @@ def run_cfg5(args, rank, world):
     rng = np.random.default_rng(6 + rank)
     crs = pkg.ServerCrs(pkg.InspireParams.d2048(), rng.integers(0, 256, 32, dtype=np.uint8).tobytes(), GAMMA)
     cache = pkg.ServerInspiringCache.new(crs, ctx=ctx)
+    # The approximate gadget's set of the same width: its 2-row seats run on the same store.
+    crs_a = pkg.ServerCrs(pkg.InspireParams.d2048_approximate_gadget(),
+                          rng.integers(0, 256, 32, dtype=np.uint8).tobytes(), GAMMA)
+    cache_a = pkg.ServerInspiringCache.new(crs_a, ctx=ctx)
     db = pkg.EncodedDatabase(cache, shards)
-    g = torch.Generator(device="cuda")
-    g.manual_seed(6 + rank)
     t0 = time.perf_counter()
-    chunk = 512  # shards per piece of records generated on the device (512 MiB)
-    for s0 in range(0, shards, chunk):
-        k = min(chunk, shards - s0)
-        rec = torch.randint(0, 256, (k * N_RING * ENTRY_BYTES,), dtype=torch.uint8, device="cuda", generator=g)
+    for s0 in range(0, shards, C5_CHUNK):
+        k = min(C5_CHUNK, shards - s0)
+        rec = c5_records(torch, s0, k, rank)
         torch.cuda.current_stream().synchronize()
         db.encode_records(None, ENTRY_BYTES, device_ptr=rec.data_ptr(), nbytes=rec.numel(), first_shard=s0)
         del rec
@@ -1106,8 +1193,13 @@ def run_cfg5(args, rank, world):
     store_s = time.perf_counter() - t0
     torch.cuda.empty_cache()
     store = pkg.ServerSessionStore.new(ctx)
-    seats = [store.register_server_side(pkg.ClientPackingKeys(rand_words(rng, (3, N_RING)), GAMMA), cache)
-             for _ in range(C5_SEATS)]
+    seat_keys = []  # (handle, gadget, y_body): even seats 3-row exact, odd seats 2-row approximate
+    for i in range(C5_SEATS):
+        gi = i % 2
+        y = rand_words(rng, (2 if gi else 3, N_RING))
+        seat_keys.append((int(store.register_server_side(pkg.ClientPackingKeys(y, GAMMA), cache_a if gi else cache)),
+                          gi, y))
+    seats = [h for h, _, _ in seat_keys]
     count = args.requests
     shard_ids = rng.integers(0, shards, count).astype(np.uint32)
     handles = np.array([int(seats[i]) for i in rng.integers(0, C5_SEATS, count)], dtype=np.uint64)
@@ -1117,7 +1209,9 @@ def run_cfg5(args, rank, world):
            "vs_baseline": None, "dtype": "u64 (exact mod q = 2^60-2^14+1)",
            "data": "synthetic: uniform record bytes encoded on the GPU, uniform key and query words",
            "config": {"workload": "d2048 TwoPacking, 512-byte records x 2^25 (16,384 shards), store on every "
-                                  "shard, 1000 seats, uniform index and seat per request, 36-bit mod switch",
+                                  "shard, 1000 seats (500 of 3 rows under d2048, 500 of 2 rows under "
+                                  "d2048_approximate_gadget, one store serving both), uniform index and seat per "
+                                  "request, 36-bit mod switch",
                       "shards": shards, "records": shards * N_RING, "seats": C5_SEATS, "requests": count,
                       "slots": args.lanes, "max_batch": BATCH},
            "setup_s": {"encode_records": encode_s, "precompute_packing": store_s},
@@ -1127,8 +1221,34 @@ def run_cfg5(args, rank, world):
         w = min(count, 512)
         loop.replay(db, store, shard_ids[:w], handles[:w], seeds[:w], bs[:w], MS_TARGET, window=256)  # warm-up
         with ClockSampler(local) as clk:
-            _, _, lat, el = loop.replay(db, store, shard_ids, handles, seeds, bs, MS_TARGET, window=4 * slots * BATCH)
+            a_out, b_out, lat, el = loop.replay(db, store, shard_ids, handles, seeds, bs, MS_TARGET,
+                                                window=4 * slots * BATCH)
         sat = count / el
+        # Byte check outside the timing: one response under each gadget against the oracle.
+        from oracle import oracle as O
+        O.build()
+        gadget_of = {h: (gi, y) for h, gi, y in seat_keys}
+        checked = 0
+        for want_gi in (0, 1):
+            i = next(j for j in range(count) if gadget_of[int(handles[j])][0] == want_gi)
+            gi, y = gadget_of[int(handles[i])]
+            sid = int(shard_ids[i])
+            s0 = sid - sid % C5_CHUNK
+            rec = c5_records(torch, s0, min(C5_CHUNK, shards - s0), rank)
+            off = (sid - s0) * N_RING * ENTRY_BYTES
+            shard_bytes = rec[off:off + N_RING * ENTRY_BYTES].cpu().numpy()
+            del rec
+            cols = np.ascontiguousarray(shard_bytes.view("<u2").reshape(N_RING, GAMMA).T, dtype=np.uint64)
+            P = O.Params.d2048_approximate_gadget() if gi else O.Params.d2048()
+            w = (crs_a if gi else crs).inspiring_w_seed
+            ao, bo = O.Store(O.Cache(P, GAMMA, w), cols).respond(cols, O.expand_seed(seeds[i].tobytes(), N_RING),
+                                                                 bs[i], y)
+            want = O.response_bytes(O.mod_switch(ao, Q, MS_TARGET), O.mod_switch(bo, Q, MS_TARGET), GAMMA, MS_TARGET)
+            if O.response_bytes(a_out[i], b_out[i], GAMMA, MS_TARGET) != want:
+                raise RuntimeError(f"served response differs from the oracle (request {i})")
+            checked += 1
+        torch.cuda.empty_cache()
+        out["parity_checked"] = checked
         lat_ms = np.sort(lat) / 1e6
         out["value"] = sat
         out["saturation"] = {"queries_per_s": sat, "p50_ms": float(lat_ms[len(lat_ms) // 2]),

@@ -128,6 +128,12 @@ def _load():
         "ig_profile_read": (I, [P, P, P, I, I]),
         "ig_launch_count": (U64, [P]),
         "ig_ctx_set_pair_threshold": (I, [P, U32]),
+        "ig_ctx_set_launch_shape": (I, [P, U32]),
+        "ig_tune_launch_shapes": (I, [P, U32, P, U32, U32]),
+        "ig_tune_get": (I, [P, U32, U32, P]),
+        "ig_tune_choose": (I, [P, U32, U32, U32, U32, ctypes.POINTER(U32)]),
+        "ig_tune_save": (I, [P, ctypes.c_char_p]),
+        "ig_tune_load": (I, [P, ctypes.c_char_p]),
         "ig_sm_server_create": (I, [P, U32, U32, U64, U64, U32, U32, U32, pu64]),
         "ig_sm_server_destroy": (I, [P, U64]),
         "ig_sm_seat": (I, [P, U64, P, P, P, pu64]),
@@ -205,6 +211,35 @@ class Context:
     @property
     def device_bytes(self):
         return self._lib.ig_ctx_device_bytes(self.h)
+
+    def set_launch_shape(self, ctas):
+        """CTAs per query of every later respond launch: 1, 2 or 4; 0 lets each launch choose."""
+        self.check(self._lib.ig_ctx_set_launch_shape(self.h, int(ctas)))
+
+    def tune_launch_shapes(self, gammas, ring_dim=2048, reps=3):
+        """Measures one full wave of queries under 1, 2 and 4 CTAs per query for each width;
+        returns {gamma: (ms_1, ms_2, ms_4)} and keeps the table for later launches."""
+        g = np.ascontiguousarray(gammas, dtype=np.uint32)
+        self.check(self._lib.ig_tune_launch_shapes(self.h, int(ring_dim), _ptr(g), len(g), int(reps)))
+        return {int(x): self.tuned(int(x), ring_dim) for x in g}
+
+    def tuned(self, gamma, ring_dim=2048):
+        ms = np.zeros(3, dtype=np.float64)
+        self.check(self._lib.ig_tune_get(self.h, int(ring_dim), int(gamma), _ptr(ms)))
+        return tuple(float(x) for x in ms)
+
+    def launch_shape_for(self, gamma, count, free_sms, ring_dim=2048):
+        """CTAs per query a launch of `count` queries of width gamma would take with free_sms free."""
+        out = ctypes.c_uint32()
+        self.check(self._lib.ig_tune_choose(self.h, int(ring_dim), int(gamma), int(count), int(free_sms),
+                                            ctypes.byref(out)))
+        return out.value
+
+    def save_tuning(self, path):
+        self.check(self._lib.ig_tune_save(self.h, str(path).encode()))
+
+    def load_tuning(self, path):
+        self.check(self._lib.ig_tune_load(self.h, str(path).encode()))
 
     def set_pair_threshold(self, max_queries):
         """Batches of at most max_queries run two CTAs per query (0: never)."""

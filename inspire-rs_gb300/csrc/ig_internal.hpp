@@ -25,8 +25,9 @@ void*& sm_slot(ig_ctx* c);
 void set_sm_destructor(ig_ctx* c, void (*fn)(ig_ctx*, void*));
 
 // One served request resolved against the context's objects (takes the context lock):
-// the parameter set's device constants, the shard's device pointers, the seat's device
-// words, and the shard's store state. Returns an IG_* status; on refusal `err` holds the
+// the parameter set's device constants (the seat's own set when it shares the database's
+// ring and width), the shard's device pointers, the seat's device words, and the shard's
+// store state. Returns an IG_* status; on refusal `err` holds the
 // reference's message.
 struct RequestView {
   ig::CrsDev crs;
@@ -34,13 +35,16 @@ struct RequestView {
   ig::ShardDev shard;
   const uint64_t* seat;
   uint32_t seat_rows;         // key rows of the seat (its bytes: seat_rows x n x 8)
-  uint64_t crs_handle;
   uint64_t p;
   bool has_store;
   char err[512];
 };
 int resolve_request(ig_ctx* c, uint64_t db, uint64_t store, uint64_t handle, uint32_t shard, RequestView* out);
 int pair_threshold(ig_ctx* c);
+// CTAs per query (1, 2 or 4) for a respond launch of `count` queries of width `gamma` on
+// ring n that can expect `free_sms` SMs: the forced shape, else the tuned estimate, else
+// the fixed rule's answer (fixed_rule_pair: the pair form, otherwise one CTA a query).
+int launch_ctas(ig_ctx* c, uint32_t n, uint32_t gamma, uint32_t count, uint32_t free_sms, bool fixed_rule_pair);
 // Device-path lanes (ig_ctx_set_lanes), for callers holding the context lock:
 // lane_acquire picks the call's stream (the context stream when lanes == 1, lane -1) and
 // orders the context stream after the lane's previous batch, so the lane's scratch can be

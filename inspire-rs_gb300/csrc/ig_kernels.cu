@@ -278,18 +278,13 @@ __global__ void __launch_bounds__(FOLD_THREADS) k_store_fold(CrsDev c, const u64
 // (m = l + 32 it) conflict-free while it reads the same positions of a column as one
 // 16-byte word. Other shards take an exact 128-bit path over the u64 words.
 //
-// Work items: a cluster of scan_split(n) CTAs takes SCAN_COLS consecutive columns of one
-// query (SCAN_ROWS per warp), each CTA one slice of 512 of the n words: it stages only its
-// slice of b_rev and copies its whole share of the columns (4 KiB a warp) into shared memory
-// at once, so a CTA is short and keeps its loads in flight together. The slices' partial
-// folds meet in the cluster's rank 0 through distributed shared memory. Items are
-// query << 12 | chunk from a per-launch list, so queries of different widths share a
-// launch; without a list item b is query b / chunks, chunk b % chunks.
+// Work items: a CTA takes SCAN_COLS consecutive columns of one query (SCAN_ROWS per warp),
+// item = query << 12 | chunk from a per-launch list, so queries of different widths share
+// a launch; without a list CTA b takes query b / chunks, chunk b % chunks.
 constexpr int SCAN_WARPS = 16;
 constexpr int SCAN_ROWS = 4;
 constexpr int SCAN_COLS = SCAN_WARPS * SCAN_ROWS;
-constexpr int SCAN_SLICE = 512;  // words of a column per CTA (the whole column below n = 512)
-__host__ __device__ constexpr int scan_split(int n) { return n > SCAN_SLICE ? n / SCAN_SLICE : 1; }
+constexpr int SCAN_STAGES = 2;
 constexpr u64 TAG_PRIME = (1ULL << 61) - 1;
 
 __device__ __forceinline__ u128 shfl_xor_u128(u128 v, int m) {
@@ -331,16 +326,21 @@ __global__ void __launch_bounds__(256) k_column_tags(u32 gamma, const u64* cols,
   }
 }
 
-// Shared memory of a scan CTA: its slice of the vector V, the columns' slice (every warp's
-// rows, copied ahead with cp.async), and the partial folds of its SCAN_COLS columns.
-__host__ __device__ constexpr size_t scan_slice(int n) { return (size_t)n / scan_split(n); }
+// Shared memory of the compact path: the vector V, then per warp a ring of SCAN_STAGES
+// steps of column chunks its lanes copy ahead (cp.async), so the next steps' loads are in
+// flight while the current step's products run.
 __host__ __device__ constexpr size_t scan_smem_bytes(int n) {
-  return scan_slice(n) * 8 + (size_t)SCAN_COLS * scan_slice(n) * 2 + (size_t)SCAN_COLS * 8;
+  return (size_t)n * 8 + (size_t)SCAN_WARPS * SCAN_STAGES * SCAN_ROWS * 32 * 16;
 }
 
 __device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
   const unsigned addr = (unsigned)__cvta_generic_to_shared(smem_dst);
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(addr), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int PENDING>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(PENDING) : "memory");
 }
 
 // Sums eight per-lane values over the warp in nine 64-bit exchanges instead of forty:
@@ -379,127 +379,111 @@ __device__ __forceinline__ void warp_reduce8(u64 (&v)[8], int lane) {
 template <int LOGN>
 __global__ void __launch_bounds__(SCAN_WARPS * 32, 2) k_scan(CrsDev c, const QueryDev* queries, const ShardDev* shards,
                                                           const u32* work, u32 chunks, u64* b_fold, u32* status) {
-  namespace cg = cooperative_groups;
-  constexpr int N = 1 << LOGN, SPLIT = scan_split(N), KS = N / SPLIT, MS = KS / 8;
-  constexpr int ITER = (MS + 31) / 32;
+  constexpr int N = 1 << LOGN, M = N / 8, ITER = M / 32;
   extern __shared__ __align__(16) uint4 scan_sm[];
-  uint2* V = reinterpret_cast<uint2*>(scan_sm);                    // [8][MS]: b_rev[K0 + k] lo, hi
-  uint4* ring = scan_sm + KS / 2;                                   // [warp][it][row][lane]
-  u64* part = reinterpret_cast<u64*>(ring + (size_t)SCAN_WARPS * ITER * SCAN_ROWS * 32);  // [SCAN_COLS]
-  cg::cluster_group cluster = cg::this_cluster();
-  const int split = SPLIT > 1 ? (int)cluster.block_rank() : 0;
-  const u32 item = blockIdx.x / SPLIT;
+  uint2* V = reinterpret_cast<uint2*>(scan_sm);  // [8][M]: b_rev[k] lo, hi
   u32 qi, chunk;
   if (work) {
-    const u32 w = work[item];
+    const u32 w = work[blockIdx.x];
     qi = w >> 12;
     chunk = w & 0xfff;
   } else {
-    qi = item / chunks;
-    chunk = item - qi * chunks;
+    qi = blockIdx.x / chunks;
+    chunk = blockIdx.x - qi * chunks;
   }
   const QueryDev qd = queries[qi];
   const ShardDev sh = shards[qd.shard];
   const u32 gamma = qd.crs ? qd.crs->gamma : c.gamma;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const u32 c0 = chunk * SCAN_COLS;                 // the item's first column
-  const u32 j0 = c0 + warp * SCAN_ROWS;             // this warp's first row
-  const int K0 = split * KS;                        // this CTA's slice of each column
+  const u32 j0 = chunk * SCAN_COLS + warp * SCAN_ROWS;
   const u64* b = qd.b;
-  if (chunk == 0 && split == 0 && threadIdx.x == 0 && sh.stale) atomicOr(status + qd.row, (u32)DEV_TAG_MISMATCH);
+  u64* fold_out = b_fold + qd.fold_off;
+  if (chunk == 0 && threadIdx.x == 0 && sh.stale) atomicOr(status + qd.row, (u32)DEV_TAG_MISMATCH);
   const int rows = j0 < gamma ? min(SCAN_ROWS, (int)(gamma - j0)) : 0;
 
-  u64 acc[8];  // acc[2r] = low-limb sum of row r, acc[2r + 1] = high-limb sum
-#pragma unroll
-  for (int k = 0; k < 8; k++) acc[k] = 0;
   if (sh.cols16) {
-    const uint16_t* col = sh.cols16 + (size_t)j0 * N + K0;
-    uint4* wring = ring + (size_t)warp * ITER * SCAN_ROWS * 32;
-    // Every chunk of the warp's rows in flight at once: lane l copies, for step it, the
-    // 16-byte chunk at positions 8m..8m+7 (m = l + 32 it) of each row.
+    const uint16_t* col = sh.cols16 + (size_t)j0 * N;
+    uint4* ring = scan_sm + N / 2 + (size_t)warp * SCAN_STAGES * SCAN_ROWS * 32;
+    // Lane l copies, for step it, the 16-byte chunk at positions 8m..8m+7 (m = l + 32 it)
+    // of each of the warp's rows into its own ring slots.
+    auto issue = [&](int it) {
+      if (it < ITER) {
+        uint4* dst = ring + (it % SCAN_STAGES) * SCAN_ROWS * 32 + lane;
+        const int m = lane + 32 * it;
+        for (int r = 0; r < rows; r++) cp_async16(dst + r * 32, col + (size_t)r * N + 8 * m);
+      }
+      cp_async_commit();
+    };
 #pragma unroll
-    for (int it = 0; it < ITER; it++) {
-      const int m = lane + 32 * it;
-      if (m < MS)
-        for (int r = 0; r < rows; r++) cp_async16(wring + (it * SCAN_ROWS + r) * 32 + lane, col + (size_t)r * N + 8 * m);
+    for (int it = 0; it < SCAN_STAGES - 1; it++) issue(it);
+    for (int k = threadIdx.x; k < N; k += SCAN_WARPS * 32) {
+      const u64 bv = k == 0 ? reduce128(b[0]) : negq(reduce128(b[N - k]));
+      V[(k & 7) * M + (k >> 3)] = make_uint2((u32)bv, (u32)(bv >> 32));
     }
-    asm volatile("cp.async.commit_group;\n" ::: "memory");
-    for (int k = threadIdx.x; k < KS; k += SCAN_WARPS * 32) {
-      const int kk = K0 + k;
-      const u64 bv = kk == 0 ? reduce128(b[0]) : negq(reduce128(b[N - kk]));
-      V[(k & 7) * MS + (k >> 3)] = make_uint2((u32)bv, (u32)(bv >> 32));
+    __syncthreads();
+    if (rows == 0) {
+      asm volatile("cp.async.wait_all;\n" ::: "memory");
+      return;
+    }
+    u64 acc[8];  // acc[2r] = low-limb sum of row r, acc[2r + 1] = high-limb sum
+#pragma unroll
+    for (int k = 0; k < 8; k++) acc[k] = 0;
+#pragma unroll 1
+    for (int it = 0; it < ITER; it++) {
+      issue(it + SCAN_STAGES - 1);
+      cp_async_wait<SCAN_STAGES - 1>();  // step it's copies have landed
+      const int m = lane + 32 * it;
+      const uint4* src = ring + (it % SCAN_STAGES) * SCAN_ROWS * 32 + lane;
+      uint4 w[SCAN_ROWS];
+#pragma unroll
+      for (int r = 0; r < SCAN_ROWS; r++) w[r] = r < rows ? src[r * 32] : make_uint4(0, 0, 0, 0);
+#pragma unroll
+      for (int p = 0; p < 8; p++) {
+        const uint2 v = V[p * M + m];
+#pragma unroll
+        for (int r = 0; r < SCAN_ROWS; r++) {
+          const u32 word = p & 1 ? (((&w[r].x)[p >> 1]) >> 16) : (((&w[r].x)[p >> 1]) & 0xffffu);
+          acc[2 * r] += (u64)word * v.x;
+          acc[2 * r + 1] += (u64)word * v.y;
+        }
+      }
     }
     asm volatile("cp.async.wait_all;\n" ::: "memory");
-    __syncthreads();
-    if (rows) {
-#pragma unroll
-      for (int it = 0; it < ITER; it++) {
-        const int m = lane + 32 * it;
-        if (m >= MS) break;
-        uint4 w[SCAN_ROWS];
-#pragma unroll
-        for (int r = 0; r < SCAN_ROWS; r++) w[r] = r < rows ? wring[(it * SCAN_ROWS + r) * 32 + lane] : make_uint4(0, 0, 0, 0);
-#pragma unroll
-        for (int p = 0; p < 8; p++) {
-          const uint2 v = V[p * MS + m];
-#pragma unroll
-          for (int r = 0; r < SCAN_ROWS; r++) {
-            const u32 word = p & 1 ? (((&w[r].x)[p >> 1]) >> 16) : (((&w[r].x)[p >> 1]) & 0xffffu);
-            acc[2 * r] += (u64)word * v.x;
-            acc[2 * r + 1] += (u64)word * v.y;
-          }
-        }
-      }
-    }
-  } else {
-    // u64 words: exact 128-bit products w * b_rev[k], their low and high words summed
-    // apart (a lane's KS / 32 of them stay below 2^68 in each 128-bit sum).
-    if (rows) {
-      for (int r = 0; r < rows; r++) {
-        const u64* cw = sh.columns + (size_t)(j0 + r) * N + K0;
-        u128 flo = 0, fhi = 0;
-        for (int k = lane; k < KS; k += 32) {
-          const int kk = K0 + k;
-          const u64 rv = kk == 0 ? reduce128(b[0]) : negq(reduce128(b[N - kk]));
-          const u128 pr = (u128)cw[k] * rv;
-          flo += (u64)pr;
-          fhi += (u64)(pr >> 64);
-        }
-#pragma unroll
-        for (int m = 16; m >= 1; m >>= 1) {
-          flo += shfl_xor_u128(flo, m);
-          fhi += shfl_xor_u128(fhi, m);
-        }
-        if (lane == 0) {
-          const u64 r64 = (u64)((((u128)1) << 64) % Q);
-          part[warp * SCAN_ROWS + r] = reduce128((u128)reduce128(fhi) * r64 + reduce128(flo));
-        }
-      }
-    }
-  }
-  if (sh.cols16 && rows) {
     warp_reduce8(acc, lane);
-    // Lane l holds value index x = ((l >> 4) & 1) 4 + ((l >> 3) & 1) 2 + ((l >> 2) & 1):
-    // row x / 2, limb x & 1; the high limb of the row sits four lanes up.
+    // Lane l holds value x = ((l >> 4) & 1) 4 + ((l >> 3) & 1) 2 + ((l >> 2) & 1): row x / 2,
+    // limb x & 1; a row's high limb sits four lanes above its low limb.
     const u64 hi = __shfl_down_sync(0xffffffffu, acc[0], 4);
     const int r = ((lane >> 4) & 1) * 2 + ((lane >> 3) & 1);
-    if ((lane & 7) == 0 && r < rows) part[warp * SCAN_ROWS + r] = reduce128((u128)acc[0] + ((u128)hi << 32));
-  }
-  u64* fold_out = b_fold + qd.fold_off;
-  const int ncols = c0 < gamma ? min(SCAN_COLS, (int)(gamma - c0)) : 0;
-  if (SPLIT == 1) {
-    __syncthreads();
-    if ((int)threadIdx.x < ncols) fold_out[c0 + threadIdx.x] = part[threadIdx.x];
+    if ((lane & 7) == 0 && r < rows) fold_out[j0 + r] = reduce128((u128)acc[0] + ((u128)hi << 32));
     return;
   }
-  cluster.sync();  // every slice's partial folds are in its shared memory
-  if (split == 0 && (int)threadIdx.x < ncols) {
-    u64 f = part[threadIdx.x];
+
+#pragma unroll 1
+  for (int r = 0; r < rows; r++) {
+    const u32 j = j0 + r;
+    const u64* col = sh.columns + (size_t)j * N;
+    u128 flo = 0, fhi = 0;
+#pragma unroll 4
+    for (int k0 = lane * 2; k0 < N; k0 += 64) {
+      const ulonglong2 w = *reinterpret_cast<const ulonglong2*>(col + k0);
+      const u64 r0 = k0 == 0 ? reduce128(b[0]) : negq(reduce128(b[N - k0]));
+      const u64 r1 = negq(reduce128(b[N - k0 - 1]));
+      const u128 p0 = (u128)w.x * r0, p1 = (u128)w.y * r1;
+      flo += (u128)(u64)p0 + (u64)p1;
+      fhi += (p0 >> 64) + (p1 >> 64);
+    }
 #pragma unroll
-    for (int r = 1; r < SPLIT; r++) f = addq(f, cluster.map_shared_rank(part, r)[threadIdx.x]);
-    fold_out[c0 + threadIdx.x] = f;
+    for (int m = 16; m >= 1; m >>= 1) {
+      flo += shfl_xor_u128(flo, m);
+      fhi += shfl_xor_u128(fhi, m);
+    }
+    if (lane == 0) {
+      // fold = fhi * 2^64 + flo (mod q)
+      const u64 r64 = (u64)((((u128)1) << 64) % Q);
+      const u64 hq = reduce128(fhi), lq = reduce128(flo);
+      fold_out[j] = reduce128((u128)hq * r64 + lq);
+    }
   }
-  cluster.sync();  // each CTA's shared memory stays alive until rank 0 has read it
 }
 
 // ServerResponse wire on the device (respond.rs:111-176, tight codec poly.rs:166-225):
@@ -978,97 +962,107 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
 // two cross stages run once per link, fused with the digit split. Unit and butterfly
 // numbering is the full transform's, so the twiddles are the full transform's.
 
-// Inverse radix-4 pass (stages s, s+1) over this CTA's half xh (N/2 words, local index);
-// threads below N/8 carry one unit each. Ends with a barrier.
-template <int LOGN>
-__device__ __forceinline__ void inv_half_r4(u64* xh, int s, int rank, const u64* tw, const u64* twp) {
-  constexpr int N = 1 << LOGN, HU = N / 8;
+// The same split holds for R parts of N/R words: the inverse's stages 0 .. logn-1-log R and
+// the forward's stages log R .. logn-1 stay inside a part. The helpers below run a local
+// pass on the part of rank `rank` of a cluster of R CTAs (R = 2 or 4).
+
+// Inverse radix-4 pass (stages s, s+1) over this CTA's part xp (N/R words, local index);
+// threads below N/(4R) carry one unit each. Ends with a barrier.
+template <int LOGN, int R>
+__device__ __forceinline__ void inv_part_r4(u64* xp, int s, int rank, const u64* tw, const u64* twp) {
+  constexpr int N = 1 << LOGN, P = N / R, PU = P / 4;
   const int tid = threadIdx.x;
-  if (tid < HU) {
-    const int u = rank * HU + tid;
+  if (tid < PU) {
+    const int u = rank * PU + tid;
     const int t = 1 << s, m = N >> (s + 1);
     const int B = u >> s, o = u & (t - 1);
-    const int e0 = B * 4 * t + o - rank * (N / 2);
+    const int e0 = B * 4 * t + o - rank * P;
     u64 w0, w0p, w1, w1p, w2, w2p;
     inv_twiddle(tw, twp, m + 2 * B, w0, w0p);
     inv_twiddle(tw, twp, m + 2 * B + 1, w1, w1p);
     inv_twiddle(tw, twp, (m >> 1) + B, w2, w2p);
-    u64 a0 = xh[sw(e0)], a1 = xh[sw(e0 + t)], a2 = xh[sw(e0 + 2 * t)], a3 = xh[sw(e0 + 3 * t)];
+    u64 a0 = xp[sw(e0)], a1 = xp[sw(e0 + t)], a2 = xp[sw(e0 + 2 * t)], a3 = xp[sw(e0 + 3 * t)];
     bf_inv4(a0, a1, w0, w0p);
     bf_inv4(a2, a3, w1, w1p);
     bf_inv4(a0, a2, w2, w2p);
     bf_inv4(a1, a3, w2, w2p);
-    xh[sw(e0)] = a0;
-    xh[sw(e0 + t)] = a1;
-    xh[sw(e0 + 2 * t)] = a2;
-    xh[sw(e0 + 3 * t)] = a3;
+    xp[sw(e0)] = a0;
+    xp[sw(e0 + t)] = a1;
+    xp[sw(e0 + 2 * t)] = a2;
+    xp[sw(e0 + 3 * t)] = a3;
   }
   __syncthreads();
 }
 
-// Inverse radix-2 stage s over this CTA's half (even logn: the last local stage); one
-// butterfly per thread. Ends with a barrier.
-template <int LOGN>
-__device__ __forceinline__ void inv_half_r2(u64* xh, int s, int rank, const u64* tw, const u64* twp) {
-  constexpr int N = 1 << LOGN;
-  const int v = rank * (N / 4) + (int)threadIdx.x;
-  const int t = 1 << s, m = N >> (s + 1);
-  const int B = v >> s, o = v & (t - 1);
-  const int e = B * 2 * t + o - rank * (N / 2);
-  u64 w, wp;
-  inv_twiddle(tw, twp, m + B, w, wp);
-  u64 a = xh[sw(e)], b = xh[sw(e + t)];
-  bf_inv4(a, b, w, wp);
-  xh[sw(e)] = a;
-  xh[sw(e + t)] = b;
+// Inverse radix-2 stage s over this CTA's part (the last local stage when their count is
+// odd); one butterfly per thread below N/(2R). Ends with a barrier.
+template <int LOGN, int R>
+__device__ __forceinline__ void inv_part_r2(u64* xp, int s, int rank, const u64* tw, const u64* twp) {
+  constexpr int N = 1 << LOGN, P = N / R;
+  if ((int)threadIdx.x < P / 2) {
+    const int v = rank * (P / 2) + (int)threadIdx.x;
+    const int t = 1 << s, m = N >> (s + 1);
+    const int B = v >> s, o = v & (t - 1);
+    const int e = B * 2 * t + o - rank * P;
+    u64 w, wp;
+    inv_twiddle(tw, twp, m + B, w, wp);
+    u64 a = xp[sw(e)], b = xp[sw(e + t)];
+    bf_inv4(a, b, w, wp);
+    xp[sw(e)] = a;
+    xp[sw(e + t)] = b;
+  }
   __syncthreads();
 }
 
-// Forward radix-4 pass (stages s, s+1; s >= 1) over this CTA's half of two buffers
-// D[0..N/2) and D[N/2..N); one unit per thread. Ends with a barrier.
-template <int LOGN>
-__device__ __forceinline__ void fwd_half_r4(u64* D, int s, int rank, const u64* tw, const u64* twp) {
-  constexpr int N = 1 << LOGN, HU = N / 8;
+// Forward radix-4 pass (stages s, s+1; s >= log R) over this CTA's part of two buffers
+// D[0..P) and D[P..2P), P = N/R; one unit per thread below N/(2R). Ends with a barrier.
+template <int LOGN, int R>
+__device__ __forceinline__ void fwd_part_r4(u64* D, int s, int rank, const u64* tw, const u64* twp) {
+  constexpr int N = 1 << LOGN, P = N / R, PU = P / 4;
   const int tid = threadIdx.x;
-  u64* x = D + (tid >= HU ? N / 2 : 0);
-  const int u = rank * HU + (tid & (HU - 1));
-  const int lt = LOGN - s - 1;  // log2 t
-  const int t = 1 << lt, m = 1 << s, h = t >> 1;
-  const int i = u >> (lt - 1), o = u & (h - 1);
-  const int e0 = i * 2 * t + o - rank * (N / 2);
-  const u64 wa = tw[m + i], wap = twp[m + i];
-  const u64 wb = tw[2 * m + 2 * i], wbp = twp[2 * m + 2 * i];
-  const u64 wc = tw[2 * m + 2 * i + 1], wcp = twp[2 * m + 2 * i + 1];
-  u64 a0 = x[sw(e0)], a1 = x[sw(e0 + h)], a2 = x[sw(e0 + t)], a3 = x[sw(e0 + t + h)];
-  bf_fwd8(a0, a2, wa, wap);
-  bf_fwd8(a1, a3, wa, wap);
-  bf_fwd8(a0, a1, wb, wbp);
-  bf_fwd8(a2, a3, wc, wcp);
-  x[sw(e0)] = a0;
-  x[sw(e0 + h)] = a1;
-  x[sw(e0 + t)] = a2;
-  x[sw(e0 + t + h)] = a3;
+  if (tid < 2 * PU) {
+    u64* x = D + (tid >= PU ? P : 0);
+    const int u = rank * PU + (tid & (PU - 1));
+    const int lt = LOGN - s - 1;  // log2 t
+    const int t = 1 << lt, m = 1 << s, h = t >> 1;
+    const int i = u >> (lt - 1), o = u & (h - 1);
+    const int e0 = i * 2 * t + o - rank * P;
+    const u64 wa = tw[m + i], wap = twp[m + i];
+    const u64 wb = tw[2 * m + 2 * i], wbp = twp[2 * m + 2 * i];
+    const u64 wc = tw[2 * m + 2 * i + 1], wcp = twp[2 * m + 2 * i + 1];
+    u64 a0 = x[sw(e0)], a1 = x[sw(e0 + h)], a2 = x[sw(e0 + t)], a3 = x[sw(e0 + t + h)];
+    bf_fwd8(a0, a2, wa, wap);
+    bf_fwd8(a1, a3, wa, wap);
+    bf_fwd8(a0, a1, wb, wbp);
+    bf_fwd8(a2, a3, wc, wcp);
+    x[sw(e0)] = a0;
+    x[sw(e0 + h)] = a1;
+    x[sw(e0 + t)] = a2;
+    x[sw(e0 + t + h)] = a3;
+  }
   __syncthreads();
 }
 
-// Forward radix-2 stage s (even logn: s = 1) over this CTA's half of both buffers; one
-// butterfly per buffer per thread. Ends with a barrier.
-template <int LOGN>
-__device__ __forceinline__ void fwd_half_r2(u64* D, int s, int rank, const u64* tw, const u64* twp) {
-  constexpr int N = 1 << LOGN;
-  const int v = rank * (N / 4) + (int)threadIdx.x;
-  const int lt = LOGN - s - 1;
-  const int t = 1 << lt, m = 1 << s;
-  const int i = v >> lt, o = v & (t - 1);
-  const int e = i * 2 * t + o - rank * (N / 2);
-  const u64 w = tw[m + i], wp = twp[m + i];
+// Forward radix-2 stage s over this CTA's part of both buffers (when the local stages are
+// odd in number); one butterfly per buffer per thread below N/(2R). Ends with a barrier.
+template <int LOGN, int R>
+__device__ __forceinline__ void fwd_part_r2(u64* D, int s, int rank, const u64* tw, const u64* twp) {
+  constexpr int N = 1 << LOGN, P = N / R;
+  if ((int)threadIdx.x < P / 2) {
+    const int v = rank * (P / 2) + (int)threadIdx.x;
+    const int lt = LOGN - s - 1;
+    const int t = 1 << lt, m = 1 << s;
+    const int i = v >> lt, o = v & (t - 1);
+    const int e = i * 2 * t + o - rank * P;
+    const u64 w = tw[m + i], wp = twp[m + i];
 #pragma unroll
-  for (int k = 0; k < 2; k++) {
-    u64* x = D + k * (N / 2);
-    u64 a = x[sw(e)], b = x[sw(e + t)];
-    bf_fwd8(a, b, w, wp);
-    x[sw(e)] = a;
-    x[sw(e + t)] = b;
+    for (int k = 0; k < 2; k++) {
+      u64* x = D + k * P;
+      u64 a = x[sw(e)], b = x[sw(e + t)];
+      bf_fwd8(a, b, w, wp);
+      x[sw(e)] = a;
+      x[sw(e + t)] = b;
+    }
   }
   __syncthreads();
 }
@@ -1172,8 +1166,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
     __syncthreads();
     int s = 2;
 #pragma unroll 1
-    for (; s + 1 <= LOGN - 2; s += 2) inv_half_r4<LOGN>(xh, s, rank, tw, twp);
-    if (s == LOGN - 2) inv_half_r2<LOGN>(xh, s, rank, tw, twp);
+    for (; s + 1 <= LOGN - 2; s += 2) inv_part_r4<LOGN, 2>(xh, s, rank, tw, twp);
+    if (s == LOGN - 2) inv_part_r2<LOGN, 2>(xh, s, rank, tw, twp);
     cluster.sync();
     {
       // Elements [0, H) of the inverse live in rank 0's X, elements [H, N) in rank 1's.
@@ -1208,11 +1202,11 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
     __syncthreads();
     s = 1;
     if (!(LOGN & 1)) {
-      fwd_half_r2<LOGN>(D, 1, rank, tw, twp);
+      fwd_part_r2<LOGN, 2>(D, 1, rank, tw, twp);
       s = 2;
     }
 #pragma unroll 1
-    for (; s < LOGN - 2; s += 2) fwd_half_r4<LOGN>(D, s, rank, tw, twp);
+    for (; s < LOGN - 2; s += 2) fwd_part_r4<LOGN, 2>(D, s, rank, tw, twp);
     // Forward stages logn-2, logn-1 of unit ug for digit dg, then each lane takes the other
     // digit at its own two slots from its partner.
     u64 d0[2], d1[2];
@@ -1261,6 +1255,174 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
 #pragma unroll
   for (int k = 0; k < 2; k++) D[other + tid + k * NT] = pf[tid + k * NT];
   cluster.sync();  // each CTA's X stays alive until its peer has read it
+  {
+    u64* const bufs[1] = {D};
+    ntt_inv_r4<LOGN, NT, 1>(bufs, tw, twp);
+  }
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const int t = tid + k * NT;
+    if (rank == 0)
+      a_out[(size_t)qi * N + t] = finish_a(c, D[t], qd.ms);
+    else
+      b_out[(size_t)qi * N + t] = finish_b(c, D[t], t, gamma, b_fold + qd.fold_off, qd.ms);
+  }
+}
+
+// ------------------------------------------------------------------------------------
+// Four CTAs per query (a cluster of 4), for small batches whose latency sets the tail: a
+// query's recursion spread over four SMs. CTA r owns quarter r, slots [r N/4, (r+1) N/4), of
+// every NTT-domain vector, one slot per thread. The inverse's stages 0 .. logn-3 and the
+// forward's stages 2 .. logn-1 stay inside a quarter (the part helpers above); the two
+// stages on each side that mix quarters combine the four elements b, b + N/4, b + N/2,
+// b + 3N/4 of each b < N/4, so they run as one radix-4 cross pass per link: thread b reads
+// its four elements (three through distributed shared memory), takes the inverse's last two
+// stages with n^-1 folded into the last (n^-1 on the sum, n^-1 times the stage's twiddle on
+// the difference), splits the four coefficients into digits and runs the forward's first
+// two stages, of which it keeps its own quarter's output (three products a digit). One
+// cluster barrier per link: the inverse's exchange buffer alternates between two quarters
+// by link parity, so a CTA rewrites what its peers read at link i only at link i-2, after
+// all passed the barrier of link i-1. With the exact gadget the third digit's transform
+// comes from the other two (inspiring2.rs:1094-1161), folded into the key rows as in
+// k_respond.
+template <int LOGN>
+__global__ void __cluster_dims__(4, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
+    k_respond_quad(CrsDev c, const QueryDev* queries, const ShardDev* shards, const u64* b_fold, u64* a_out,
+                   u64* b_out, u32* status, int force_serial) {
+  namespace cg = cooperative_groups;
+  constexpr int N = 1 << LOGN, NT = N / 4, P = N / 4;
+  constexpr u32 M2N = 2 * N - 1;
+  constexpr u64 DMASK = (1ULL << 20) - 1;
+  extern __shared__ __align__(16) u64 sm[];
+  u64* X = sm;          // [2][P] own quarter of the inverse, by link parity
+  u64* D = sm + 2 * P;  // [2][P] own quarter of digits 0 and 1; N words for the last transform
+  u64* a_ntt = D + N;
+  u64* tw = a_ntt + N;
+  u64* twp = tw + N;
+  u64* Wm = twp + N;  // room for three key rows, as in k_respond
+  u64* Y = Wm + 3 * N;
+  uint16_t* e_tab = reinterpret_cast<uint16_t*>(Y + 3 * N);
+  uint16_t* s_tab = e_tab + N;
+
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  const u64* peer[4];
+#pragma unroll
+  for (int k = 0; k < 4; k++) peer[k] = cluster.map_shared_rank(X, k);
+  const int tid = threadIdx.x;
+  const QueryDev qd = queries[blockIdx.x >> 2];
+  const u32 qi = qd.row;  // output and status row
+  const ShardDev sh = shards[qd.shard];
+  const SetView ps = set_view(c, qd.crs);
+  const u32 gamma = ps.gamma;
+  const bool exact = ps.approx == 0;
+  const int slot = rank * P + tid;  // this thread's slot
+
+  stage_constants<N, NT>(c, ps, qd.seat_R, tw, twp, Wm, Y, e_tab, s_tab);
+  expand_a<N, NT>(qd, a_ntt, status, qi, force_serial);
+  {
+    u64* const bufs[1] = {a_ntt};
+    ntt_fwd_r4<LOGN, NT, 1>(bufs, tw, twp);
+  }
+  const u32 et = e_tab[slot];
+  u64 cur, sb = 0;
+  {
+    const u32 gp = ps.gpow[gamma - 1];
+    const u32 tb = s_tab[((gp * et) & M2N) >> 1];
+    cur = mont(a_ntt[tb], sh.sums_R[(size_t)(gamma - 1) * N + slot]);
+  }
+  // Twiddles of the cross pass: the inverse's stage logn-2 (indices 2 and 3), the forward's
+  // stage 0 (index 1) and stage 1 (index 2 for the first half, 3 for the second).
+  u64 wi2, wi2p, wi3, wi3p;
+  inv_twiddle(tw, twp, 2, wi2, wi2p);
+  inv_twiddle(tw, twp, 3, wi3, wi3p);
+  const u64 wf1 = tw[1], wf1p = twp[1];
+  const u64 wfs = tw[2 + (rank >> 1)], wfsp = twp[2 + (rank >> 1)];
+#pragma unroll 1
+  for (int i = (int)gamma - 2; i >= 0; i--) {
+    const u64 sv = sh.sums_R[(size_t)i * N + slot];
+    const u32 gp = ps.gpow[i];
+    const int par = (i & 1) * P;
+    u64* xq = X + par;
+    xq[sw(tid)] = cur;
+    __syncthreads();
+    int s = 0;
+#pragma unroll 1
+    for (; s + 1 <= LOGN - 3; s += 2) inv_part_r4<LOGN, 4>(xq, s, rank, tw, twp);
+    if (s == LOGN - 3) inv_part_r2<LOGN, 4>(xq, s, rank, tw, twp);
+    cluster.sync();
+    {
+      u64 x0 = peer[0][par + sw(tid)], x1 = peer[1][par + sw(tid)];
+      u64 x2 = peer[2][par + sw(tid)], x3 = peer[3][par + sw(tid)];
+      bf_inv4(x0, x1, wi2, wi2p);  // (b, b + N/4), block 0 of stage logn-2
+      bf_inv4(x2, x3, wi3, wi3p);  // (b + N/2, b + 3N/4), block 1
+      u64 cf[4];                   // coefficients b, b + N/4, b + N/2, b + 3N/4
+      cf[0] = shoup(x0 + x2, c.ninv, c.ninvp);
+      cf[2] = shoup(x0 - x2 + 4 * Q, c.nlast, c.nlastp);
+      cf[1] = shoup(x1 + x3, c.ninv, c.ninvp);
+      cf[3] = shoup(x1 - x3 + 4 * Q, c.nlast, c.nlastp);
+      u64 g0[4], g1[4];  // digits 0 and 1
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        if (exact) {
+          g0[k] = cf[k] & DMASK;
+          g1[k] = (cf[k] >> 20) & DMASK;
+        } else {
+          const u64 rr = (cf[k] + (1ULL << 19)) >> 20;
+          g0[k] = rr & DMASK;
+          g1[k] = rr >> 20;
+        }
+      }
+      // Forward stage 0 (b with b + N/2, b + N/4 with b + 3N/4), then stage 1 on this
+      // quarter's half: a bf_fwd8 whose output r & 1 is the quarter's word.
+      auto fwd = [&](const u64(&g)[4]) -> u64 {
+        const u64 t2 = shoup_lazy4(g[2], wf1, wf1p), t3 = shoup_lazy4(g[3], wf1, wf1p);
+        u64 lo, hi;
+        if (rank < 2) {
+          lo = g[0] + t2;
+          hi = g[1] + t3;
+        } else {
+          lo = g[0] + 4 * Q - t2;
+          hi = g[1] + 4 * Q - t3;
+        }
+        bf_fwd8(lo, hi, wfs, wfsp);
+        return (rank & 1) ? hi : lo;
+      };
+      D[sw(tid)] = fwd(g0);
+      D[P + sw(tid)] = fwd(g1);
+    }
+    __syncthreads();
+    s = 2;
+    if ((LOGN - 2) & 1) {
+      fwd_part_r2<LOGN, 4>(D, 2, rank, tw, twp);
+      s = 3;
+    }
+#pragma unroll 1
+    for (; s < LOGN; s += 2) fwd_part_r4<LOGN, 4>(D, s, rank, tw, twp);
+    const u64 d0 = D[sw(tid)], d1 = D[P + sw(tid)];
+    const u32 tb = s_tab[((gp * et) & M2N) >> 1];
+    u128 nb = wide(d0, Y[tb]) + wide(d1, Y[N + tb]);
+    u128 nc = wide(a_ntt[tb], sv) + wide(d0, Wm[tb]) + wide(d1, Wm[N + tb]);
+    if (exact) {  // the rows are folded: R_{i+1} stands in for digit 2
+      nb += wide(cur, Y[2 * N + tb]);
+      nc += wide(cur, Wm[2 * N + tb]);
+    }
+    sb = addq(sb, redc_wide(nb));
+    cur = redc_wide(nc);
+  }
+  // Final transforms: rank 0 assembles R_0 (-> a), rank 1 the online sum (-> b), each from
+  // the four quarters exchanged through X once every peer is past its last cross-pass read.
+  cluster.sync();
+  X[tid] = cur;
+  X[P + tid] = sb;
+  cluster.sync();
+  if (rank < 2) {
+#pragma unroll
+    for (int k = 0; k < 4; k++) D[k * P + tid] = peer[k][rank * P + tid];
+  }
+  cluster.sync();  // each CTA's X stays alive until ranks 0 and 1 have read it
+  if (rank >= 2) return;
+  __syncthreads();
   {
     u64* const bufs[1] = {D};
     ntt_inv_r4<LOGN, NT, 1>(bufs, tw, twp);
@@ -2029,28 +2191,14 @@ cudaError_t shard_scan(const CrsDev& c, const QueryDev* queries, const ShardDev*
                        u32 nwork, u64* b_fold, u32* status, cudaStream_t s) {
   if (nq == 0) return cudaSuccess;
   const u32 chunks = scan_chunks(c.gamma);
-  const u32 items = work ? nwork : nq * chunks;
-  if (items == 0) return cudaSuccess;
+  const u32 blocks = work ? nwork : nq * chunks;
+  if (blocks == 0) return cudaSuccess;
   const size_t smem = scan_smem_bytes((int)c.n);
-  const u32 split = (u32)scan_split((int)c.n);
   IG_DISPATCH_LOGN(c.logn, {
     auto k = k_scan<L>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(items * split);
-    cfg.blockDim = dim3(SCAN_WARPS * 32);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = s;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = split;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    e = cudaLaunchKernelEx(&cfg, k, c, queries, shards, work, chunks, b_fold, status);
-    if (e != cudaSuccess) return e;
+    k<<<blocks, SCAN_WARPS * 32, smem, s>>>(c, queries, shards, work, chunks, b_fold, status);
   });
   return cudaGetLastError();
 }
@@ -2182,18 +2330,26 @@ cudaError_t butterfly_peak(u64* out, int blocks, int iters, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-size_t respond_smem_bytes(const CrsDev& c, bool pair) {
-  const size_t words = pair ? (size_t)(5 * c.n) : (size_t)(6 * c.n);
-  return (words + 2 * (size_t)3 * c.n) * 8 + 2 * (size_t)c.n * 2;  // three key rows
+size_t respond_smem_bytes(const CrsDev& c, int ctas) {
+  // X, D and a_ntt, the two ladders, three key rows of W and Y, two u16 slot tables.
+  const size_t n = c.n;
+  const size_t words = ctas == 4 ? n / 2 + 4 * n : ctas == 2 ? 5 * n : 6 * n;
+  return (words + 2 * (size_t)3 * n) * 8 + 2 * n * 2;
 }
 
 cudaError_t respond(const CrsDev& c, const QueryDev* queries, const ShardDev* shards, u32 nq,
                     const u64* b_fold, u64* a_out, u64* b_out, u32* status,
-                    int force_serial_expand, bool pair, cudaStream_t s) {
+                    int force_serial_expand, int ctas, cudaStream_t s) {
   if (nq == 0) return cudaSuccess;
-  const size_t smem = respond_smem_bytes(c, pair);
+  if (ctas != 1 && ctas != 2 && ctas != 4) return cudaErrorInvalidValue;
+  const size_t smem = respond_smem_bytes(c, ctas);
   IG_DISPATCH_LOGN(c.logn, {
-    if (pair) {
+    if (ctas == 4) {
+      auto k = k_respond_quad<L>;
+      cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+      k<<<4 * nq, (1 << L) / 4, smem, s>>>(c, queries, shards, b_fold, a_out, b_out, status, force_serial_expand);
+    } else if (ctas == 2) {
       auto k = k_respond_pair<L>;
       cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return e;

@@ -138,13 +138,14 @@ cudaError_t store_fold(const CrsDev& c, const u64* H, u64* sums_R, cudaStream_t 
 
 // Fused per-query respond: expansion of `a`, store gather, backward recursion with the
 // online gather, final transforms, the mod switch to each query's target (QueryDev::ms).
-// One CTA per query; `pair` selects two CTAs per query (a cluster of 2), for batches of at
-// most half the SMs. Queries may carry their own parameter set (QueryDev::crs) on c's ring.
+// `ctas` CTAs per query: 1, or a cluster of 2 or 4 that splits each query's transforms
+// over as many SMs (shorter latency, more SM time). Queries may carry their own parameter
+// set (QueryDev::crs) on c's ring.
 cudaError_t respond(const CrsDev& c, const QueryDev* queries, const ShardDev* shards,
                     u32 nq, const u64* b_fold, u64* a_out, u64* b_out, u32* status, int force_serial_expand,
-                    bool pair, cudaStream_t s);
+                    int ctas, cudaStream_t s);
 
-size_t respond_smem_bytes(const CrsDev& c, bool pair);
+size_t respond_smem_bytes(const CrsDev& c, int ctas);
 
 // NoPacking respond of `nq` queries: out[q] holds gamma + 1 ciphertexts of (a, b), n words
 // each in coefficient form, the column sum first (respond.rs:614-643). AB_R: nq x 2n words

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <atomic>
 #include <cstdarg>
@@ -208,6 +209,12 @@ struct ig_ctx {
   // Host-side fault injection: the device allocation `fail_alloc_at` calls from now fails
   // (1 = the next one; 0 = none).
   std::atomic<u32> fail_alloc_at{0};
+  // Launch shape of respond launches (CTAs per query). force_ctas != 0 fixes it; otherwise,
+  // with a tuned entry for the launch's (ring, gamma), the shape with the least estimated
+  // completion time is taken, else the fixed pair_threshold rule. tune[(n, gamma)] holds the
+  // measured milliseconds of one full wave (SMs / ctas queries) under 1, 2 and 4 CTAs.
+  u32 force_ctas = 0;
+  std::map<std::pair<u32, u32>, std::array<double, 3>> tune;
   cudaStream_t lane_stream[IG_MAX_LANES] = {};
   cudaEvent_t lane_in[IG_MAX_LANES] = {}, lane_done[IG_MAX_LANES] = {};
   bool lane_used[IG_MAX_LANES] = {};
@@ -498,6 +505,35 @@ int stage_h2d(ig_ctx* c, void* dst, const void* src, size_t bytes) { return ::st
 void add_launches(ig_ctx* c, unsigned n) { c->launches += n; }
 void*& sm_slot(ig_ctx* c) { return c->sm; }
 int pair_threshold(ig_ctx* c) { return (int)c->pair_threshold; }
+int launch_ctas(ig_ctx* c, u32 n, u32 gamma, u32 count, u32 free_sms, bool fixed_rule_pair) {
+  if (c->force_ctas) return (int)c->force_ctas;
+  auto it = c->tune.find({n, gamma});
+  if (it == c->tune.end()) {
+    // The nearest tuned width of the ring, if any.
+    for (auto jt = c->tune.begin(); jt != c->tune.end(); ++jt)
+      if (jt->first.first == n &&
+          (it == c->tune.end() || (jt->first.second > gamma ? jt->first.second - gamma : gamma - jt->first.second) <
+                                      (it->first.second > gamma ? it->first.second - gamma : gamma - it->first.second)))
+        it = jt;
+  }
+  if (it == c->tune.end()) return fixed_rule_pair ? 2 : 1;
+  // Waves of this launch on the SMs it can expect, times a wave's measured duration.
+  const u32 freeq = free_sms ? free_sms : 1;
+  int best = 1;
+  double best_ms = 0;
+  const int shapes[3] = {1, 2, 4};
+  for (int k = 0; k < 3; k++) {
+    const double t = it->second[k];
+    if (!(t > 0)) continue;
+    const u64 waves = ((u64)count * shapes[k] + freeq - 1) / freeq;
+    const double ms = (double)waves * t;
+    if (best_ms == 0 || ms < best_ms * 0.999) {
+      best = shapes[k];
+      best_ms = ms;
+    }
+  }
+  return best;
+}
 int lanes(ig_ctx* c) { return (int)c->lanes; }
 int lane_acquire(ig_ctx* c, cudaStream_t* s, int* lane) {
   *lane = -1;
@@ -1169,6 +1205,32 @@ static int resolve_seat(ig_ctx* c, CrsObj& o, uint64_t st, uint64_t handle, cons
   return IG_OK;
 }
 
+// The seat `handle` of `st` for a query on a database whose parameter set is `db_set`, and
+// the parameter set the query runs under. The reference passes the CRS and its cache to
+// respond_seeded_batch apart from the EncodedDatabase (respond.rs:1189-1202), and a shard's
+// packing store depends only on the ring and the width (shard_store.rs:86-156), so a
+// database serves every parameter set of its ring_dim and gamma: a seat registered under
+// another such set (the other gadget, another mask seed) runs under its own set. Otherwise
+// the seat must fit the database's set, with resolve_seat's refusals.
+static int resolve_seat_for_db(ig_ctx* c, CrsObj& db_set, uint64_t st, uint64_t handle, const u64** seat_out,
+                               CrsObj** set_out) {
+  auto it = c->stores.find(st);
+  if (it != c->stores.end()) {
+    auto sit = it->second.seats.find(handle);
+    if (sit != it->second.seats.end()) {
+      CrsObj* own = get_crs(c, sit->second.crs);
+      if (own && own != &db_set && own->n == db_set.n && own->gamma == db_set.gamma &&
+          sit->second.rows == own->rows && sit->second.num_to_pack == own->gamma) {
+        *seat_out = sit->second.yR;
+        *set_out = own;
+        return IG_OK;
+      }
+    }
+  }
+  *set_out = &db_set;
+  return resolve_seat(c, db_set, st, handle, nullptr, 0, 0, seat_out);
+}
+
 // RAVEN_PROFILE_RESPOND is read once per process, as the reference does (respond.rs:1332-1345).
 static bool env_profile() {
   static const bool on = getenv("RAVEN_PROFILE_RESPOND") != nullptr;
@@ -1299,7 +1361,9 @@ static int respond_host(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_t handle, c
   pk = prof_begin(c, REGION_RESPOND, s);
   IG_CUDA(c, igk::respond(o.dev, (const QueryDev*)d_q, (const ShardDev*)d_table, count, (const u64*)d_fold,
                           (u64*)d_a, (u64*)d_b, (u32*)d_status, c->force_serial,
-                          (u64)count * lanes <= c->pair_threshold, s));
+                          igint::launch_ctas(c, (u32)n, (u32)g, count, c->sms / lanes,
+                                             (u64)count * lanes <= c->pair_threshold),
+                          s));
   prof_end(c, pk, s);
   if (env_prof) {
     cudaEventRecord(env_ev[2], s);
@@ -1825,11 +1889,12 @@ int ig_respond_seeded_batch_device(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_
   long pk = prof_begin(c, REGION_SCAN, s);
   IG_CUDA(c, igk::shard_scan(o.dev, (const QueryDev*)d_q, db->d_table, count, nullptr, 0, (u64*)d_fold, d_status, s));
   prof_end(c, pk, s);
-  // Two CTAs per query only while every lane's batch still leaves SMs for them.
-  const bool pair = (u64)count * c->lanes <= c->pair_threshold;
+  // Several CTAs per query only while every lane's batch still leaves SMs for them.
+  const int ctas = igint::launch_ctas(c, (u32)n, (u32)g, count, c->sms / c->lanes,
+                                      (u64)count * c->lanes <= c->pair_threshold);
   pk = prof_begin(c, REGION_RESPOND, s);
   IG_CUDA(c, igk::respond(o.dev, (const QueryDev*)d_q, db->d_table, count, (const u64*)d_fold, d_a, d_b, d_status,
-                          c->force_serial, pair, s));
+                          c->force_serial, ctas, s));
   prof_end(c, pk, s);
   return igint::lane_release(c, lane);
 }
@@ -1847,6 +1912,7 @@ struct MixedPlan {
   std::vector<QueryDev> qs;      // launch order: longest recursion (gamma) first
   std::vector<u32> work;         // scan work items, position << 12 | chunk
   size_t fold_words = 0;
+  u32 max_gamma = 0;             // the longest recursion of the launch
 };
 
 // Resolves and checks every query (the caller holds the context lock). The whole batch is
@@ -1861,7 +1927,11 @@ static int plan_mixed(ig_ctx* c, u32 count, const uint64_t* dbs, const uint64_t*
   for (u32 i = 0; i < count; i++) {
     DbObj* db = get_db(c, dbs[i]);
     if (!db) return fail(c, IG_ERR_HANDLE, "query %u: unknown database handle %llu", i, (unsigned long long)dbs[i]);
-    CrsObj& o = *get_crs(c, db->crs);
+    const u64* seat;
+    CrsObj* set;
+    int rc = resolve_seat_for_db(c, *get_crs(c, db->crs), stores[i], handles[i], &seat, &set);
+    if (rc) return rc;
+    CrsObj& o = *set;
     if (i == 0) {
       n = o.n;
       P.ring = o.dev;
@@ -1873,9 +1943,6 @@ static int plan_mixed(ig_ctx* c, u32 count, const uint64_t* dbs, const uint64_t*
     if (ms && (ms >= Q || ms < o.p || ms % (2ULL * n) != 1))
       return fail(c, IG_ERR_ARG, "query %u: mod-switch target_modulus %llu must be in [p, q) and 1 mod 2d", i,
                   (unsigned long long)ms);
-    const u64* seat;
-    int rc = resolve_seat(c, o, stores[i], handles[i], nullptr, 0, 0, &seat);
-    if (rc) return rc;
     const u32 s = shard_ids[i];
     if (s >= db->num_shards)
       return fail(c, IG_ERR_ARG, "query %u: shard %u not found at dense position %u; encoded database has %u shards", i,
@@ -1908,6 +1975,7 @@ static int plan_mixed(ig_ctx* c, u32 count, const uint64_t* dbs, const uint64_t*
     const u32 gamma = order[p].first;
     for (u32 ch = 0; ch < igk::scan_chunks(gamma); ch++) P.work.push_back((p << 12) | ch);
     P.fold_words += gamma;
+    P.max_gamma = std::max(P.max_gamma, gamma);
   }
   P.qs.swap(sorted);
   return IG_OK;
@@ -1953,10 +2021,11 @@ int ig_respond_mixed_batch_device(ig_ctx* c, uint32_t count, const uint64_t* dbs
   IG_CUDA(c, igk::shard_scan(P.ring, (const QueryDev*)dq, (const ShardDev*)dt, count, (const u32*)dw,
                              (u32)P.work.size(), (u64*)df, d_status, s));
   prof_end(c, pk, s);
-  const bool pair = (u64)count * c->lanes <= c->pair_threshold;
+  const int ctas = igint::launch_ctas(c, (u32)n, P.max_gamma, count, c->sms / c->lanes,
+                                      (u64)count * c->lanes <= c->pair_threshold);
   pk = prof_begin(c, REGION_RESPOND, s);
   IG_CUDA(c, igk::respond(P.ring, (const QueryDev*)dq, (const ShardDev*)dt, count, (const u64*)df, d_a, d_b, d_status,
-                          c->force_serial, pair, s));
+                          c->force_serial, ctas, s));
   prof_end(c, pk, s);
   c->launches += 2;
   return igint::lane_release(c, lane);
@@ -2015,7 +2084,10 @@ int ig_respond_mixed_batch(ig_ctx* c, uint32_t count, const uint64_t* dbs, const
   IG_CUDA(c, igk::shard_scan(P.ring, (const QueryDev*)dq, (const ShardDev*)dt, count, (const u32*)dw,
                              (u32)P.work.size(), (u64*)df, (u32*)dst, s));
   IG_CUDA(c, igk::respond(P.ring, (const QueryDev*)dq, (const ShardDev*)dt, count, (const u64*)df, (u64*)da, (u64*)db_,
-                          (u32*)dst, c->force_serial, (u64)count * c->lanes <= c->pair_threshold, s));
+                          (u32*)dst, c->force_serial,
+                          igint::launch_ctas(c, (u32)n, P.max_gamma, count, c->sms / c->lanes,
+                                             (u64)count * c->lanes <= c->pair_threshold),
+                          s));
   c->launches += 2;
   IG_CUDA(c, cudaMemcpyAsync(h_status, dst, count * 4, cudaMemcpyDeviceToHost, s));
   IG_CUDA(c, cudaMemcpyAsync(h_a, da, (size_t)count * n * 8, cudaMemcpyDeviceToHost, s));
@@ -2336,6 +2408,189 @@ int ig_response_encode_rims_device(ig_ctx* c, uint32_t count, const uint64_t* d_
   return IG_OK;
 }
 
+int ig_ctx_set_launch_shape(ig_ctx* c, uint32_t ctas) {
+  if (!c) return IG_ERR_ARG;
+  if (ctas != 0 && ctas != 1 && ctas != 2 && ctas != 4)
+    return fail(c, IG_ERR_ARG, "ig_ctx_set_launch_shape: 0 (chosen per launch), 1, 2 or 4 CTAs per query");
+  std::lock_guard<std::mutex> lk(c->mu);
+  c->force_ctas = ctas;
+  return IG_OK;
+}
+
+// The launch-shape tuner: per width, one full wave of queries (SMs / ctas of them) under each
+// shape, on a synthetic database, seat and queries built here and freed after; the same
+// respond path as serving (scan and respond launches, device buffers), timed with CUDA events
+// on the context stream.
+int ig_tune_launch_shapes(ig_ctx* c, uint32_t ring_dim, const uint32_t* gammas, uint32_t count, uint32_t reps) {
+  if (!c) return IG_ERR_ARG;
+  if (!gammas || count == 0 || reps == 0 || reps > 1000)
+    return fail(c, IG_ERR_ARG, "ig_tune_launch_shapes: need 1.. widths and 1..1000 repetitions");
+  u32 lanes0, force0;
+  {
+    std::lock_guard<std::mutex> lk(c->mu);
+    lanes0 = c->lanes;
+    force0 = c->force_ctas;
+  }
+  int rc = ig_ctx_set_lanes(c, 1);
+  if (rc) return rc;
+  const u32 n = ring_dim, sms = c->sms ? c->sms : 1;
+  const u32 shards = 8;
+  std::mt19937_64 rng(0x7u);
+  u64 *d_bs = nullptr, *d_a = nullptr, *d_b = nullptr;
+  uint8_t* d_seeds = nullptr;
+  u32* d_status = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  auto cleanup = [&]() {
+    if (d_bs) dfree(c, d_bs, (size_t)sms * n * 8);
+    if (d_a) dfree(c, d_a, (size_t)sms * n * 8);
+    if (d_b) dfree(c, d_b, (size_t)sms * n * 8);
+    if (d_seeds) dfree(c, d_seeds, (size_t)sms * 32);
+    if (d_status) dfree(c, d_status, (size_t)sms * 4);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    {
+      std::lock_guard<std::mutex> lk(c->mu);
+      c->force_ctas = force0;
+    }
+    ig_ctx_set_lanes(c, lanes0);
+  };
+  {
+    std::lock_guard<std::mutex> lk(c->mu);
+    cudaSetDevice(c->device);
+    if ((rc = dalloc(c, (void**)&d_bs, (size_t)sms * n * 8, nullptr)) ||
+        (rc = dalloc(c, (void**)&d_a, (size_t)sms * n * 8, nullptr)) ||
+        (rc = dalloc(c, (void**)&d_b, (size_t)sms * n * 8, nullptr)) ||
+        (rc = dalloc(c, (void**)&d_seeds, (size_t)sms * 32, nullptr)) ||
+        (rc = dalloc(c, (void**)&d_status, (size_t)sms * 4, nullptr))) {
+      cleanup();
+      return rc;
+    }
+    std::vector<u64> hb((size_t)sms * n);
+    for (auto& x : hb) x = rng() % Q;
+    std::vector<uint8_t> hs((size_t)sms * 32);
+    for (auto& x : hs) x = (uint8_t)rng();
+    cudaMemcpy(d_bs, hb.data(), hb.size() * 8, cudaMemcpyHostToDevice);
+    cudaMemcpy(d_seeds, hs.data(), hs.size(), cudaMemcpyHostToDevice);
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+      cleanup();
+      return fail(c, IG_ERR_CUDA, "ig_tune_launch_shapes: event creation failed");
+    }
+  }
+  for (u32 gi = 0; gi < count; gi++) {
+    const u32 gamma = gammas[gi];
+    uint8_t w_seed[32] = {0};
+    u64 crs = 0, db = 0, store = 0, handle = 0;
+    auto drop = [&]() {
+      if (store) ig_session_store_destroy(c, store);
+      if (db) ig_db_destroy(c, db);
+      if (crs) ig_crs_destroy(c, crs);
+    };
+    if ((rc = ig_crs_create(c, n, Q, 65537, 1ULL << 20, 3, 0, gamma, w_seed, &crs)) ||
+        (rc = ig_db_create(c, crs, shards, &db))) {
+      drop();
+      cleanup();
+      return rc;
+    }
+    std::vector<u64> cols((size_t)gamma * n);
+    for (auto& x : cols) x = rng() & 0xffff;
+    for (u32 sh = 0; sh < shards && !rc; sh++) rc = ig_db_set_shard(c, db, sh, cols.data());
+    if (!rc) rc = ig_db_precompute_packing_all(c, db);
+    if (!rc) rc = ig_session_store_create(c, &store);
+    std::vector<u64> y((size_t)3 * n);
+    for (auto& x : y) x = rng() % Q;
+    if (!rc) rc = ig_session_register(c, store, crs, y.data(), 3, gamma, &handle);
+    if (rc) {
+      drop();
+      cleanup();
+      return rc;
+    }
+    std::array<double, 3> ms{};
+    const u32 shapes[3] = {1, 2, 4};
+    for (int k = 0; k < 3 && !rc; k++) {
+      const u32 batch = std::max(1u, sms / shapes[k]);
+      std::vector<u32> sids(batch);
+      for (u32 q = 0; q < batch; q++) sids[q] = q % shards;
+      {
+        std::lock_guard<std::mutex> lk(c->mu);
+        c->force_ctas = shapes[k];
+      }
+      for (u32 r = 0; r <= reps && !rc; r++) {
+        if (r == 1) cudaEventRecord(e0, c->stream);  // after one untimed warm-up launch
+        rc = ig_respond_seeded_batch_device(c, db, store, handle, batch, sids.data(), d_seeds, d_bs, 0, d_a, d_b,
+                                            d_status);
+      }
+      cudaEventRecord(e1, c->stream);
+      if (cudaEventSynchronize(e1) != cudaSuccess && !rc) rc = fail(c, IG_ERR_CUDA, "ig_tune_launch_shapes: launch failed");
+      float el = 0;
+      cudaEventElapsedTime(&el, e0, e1);
+      ms[k] = el / reps;
+    }
+    drop();
+    if (rc) {
+      cleanup();
+      return rc;
+    }
+    std::lock_guard<std::mutex> lk(c->mu);
+    c->tune[{n, gamma}] = ms;
+  }
+  cleanup();
+  return IG_OK;
+}
+
+int ig_tune_get(ig_ctx* c, uint32_t ring_dim, uint32_t gamma, double* ms_out) {
+  if (!c || !ms_out) return IG_ERR_ARG;
+  std::lock_guard<std::mutex> lk(c->mu);
+  auto it = c->tune.find({ring_dim, gamma});
+  if (it == c->tune.end())
+    return fail(c, IG_ERR_HANDLE, "no launch-shape entry for ring_dim %u, gamma %u", ring_dim, gamma);
+  for (int k = 0; k < 3; k++) ms_out[k] = it->second[k];
+  return IG_OK;
+}
+
+int ig_tune_choose(ig_ctx* c, uint32_t ring_dim, uint32_t gamma, uint32_t count, uint32_t free_sms, uint32_t* ctas) {
+  if (!c || !ctas) return IG_ERR_ARG;
+  std::lock_guard<std::mutex> lk(c->mu);
+  *ctas = (u32)igint::launch_ctas(c, ring_dim, gamma, count, free_sms, (u64)count <= c->pair_threshold);
+  return IG_OK;
+}
+
+int ig_tune_save(ig_ctx* c, const char* path) {
+  if (!c || !path) return IG_ERR_ARG;
+  std::lock_guard<std::mutex> lk(c->mu);
+  FILE* f = fopen(path, "w");
+  if (!f) return fail(c, IG_ERR_ARG, "ig_tune_save: cannot write %s", path);
+  fprintf(f, "inspire_gb300 launch shapes 1\nsms %u\n", c->sms);
+  for (const auto& kv : c->tune)
+    fprintf(f, "%u %u %.6f %.6f %.6f\n", kv.first.first, kv.first.second, kv.second[0], kv.second[1], kv.second[2]);
+  const bool ok = fclose(f) == 0;
+  return ok ? IG_OK : fail(c, IG_ERR_ARG, "ig_tune_save: writing %s failed", path);
+}
+
+int ig_tune_load(ig_ctx* c, const char* path) {
+  if (!c || !path) return IG_ERR_ARG;
+  FILE* f = fopen(path, "r");
+  if (!f) return fail(c, IG_ERR_ARG, "ig_tune_load: cannot read %s", path);
+  unsigned version = 0, sms = 0;
+  std::map<std::pair<u32, u32>, std::array<double, 3>> table;
+  int rc = IG_OK;
+  if (fscanf(f, "inspire_gb300 launch shapes %u sms %u", &version, &sms) != 2 || version != 1) {
+    rc = fail(c, IG_ERR_ARG, "ig_tune_load: %s is not a launch-shape table", path);
+  } else if (sms != c->sms) {
+    rc = fail(c, IG_ERR_ARG, "ig_tune_load: %s was measured on %u SMs, this device has %u", path, sms, c->sms);
+  } else {
+    unsigned n, g;
+    double a, b, d;
+    int got;
+    while ((got = fscanf(f, "%u %u %lf %lf %lf", &n, &g, &a, &b, &d)) == 5) table[{n, g}] = {a, b, d};
+    if (got != EOF) rc = fail(c, IG_ERR_ARG, "ig_tune_load: %s holds a malformed line", path);
+  }
+  fclose(f);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lk(c->mu);
+  for (const auto& kv : table) c->tune[kv.first] = kv.second;
+  return IG_OK;
+}
+
 int ig_ctx_set_pair_threshold(ig_ctx* c, uint32_t max_queries) {
   if (!c) return IG_ERR_ARG;
   std::lock_guard<std::mutex> lk(c->mu);
@@ -2432,10 +2687,11 @@ static int resolve_request_locked(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_t
                                   RequestView* out) {
   DbObj* db = get_db(c, dbh);
   if (!db) return fail(c, IG_ERR_HANDLE, "unknown database handle %llu", (unsigned long long)dbh);
-  CrsObj& o = *get_crs(c, db->crs);
   const u64* seat;
-  int rc = resolve_seat(c, o, st, handle, nullptr, 0, 0, &seat);
+  CrsObj* set;
+  int rc = resolve_seat_for_db(c, *get_crs(c, db->crs), st, handle, &seat, &set);
   if (rc) return rc;
+  CrsObj& o = *set;
   if (shard >= db->num_shards)
     return fail(c, IG_ERR_ARG, "shard %u not found at dense position %u; encoded database has %u shards", shard,
                 shard, db->num_shards);
@@ -2446,7 +2702,6 @@ static int resolve_request_locked(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_t
   out->shard = sl.dev();
   out->seat = seat;
   out->seat_rows = o.rows;
-  out->crs_handle = db->crs;
   out->p = o.p;
   out->has_store = sl.sums != nullptr;
   return IG_OK;
@@ -2558,7 +2813,9 @@ int ig_respond_seeded_batch_noalloc(ig_ctx* c, uint64_t dbh, uint64_t st, uint64
   IG_CUDA(c, igk::shard_scan(o.dev, d_q, db->d_table, count, nullptr, 0, d_fold, d_status, s));
   // The launch shape of ig_respond_seeded_batch_device for the same batch and lane count.
   IG_CUDA(c, igk::respond(o.dev, d_q, db->d_table, count, d_fold, d_a, d_b, d_status, c->force_serial,
-                          (u64)count * c->lanes <= c->pair_threshold, s));
+                          igint::launch_ctas(c, (u32)n, (u32)g, count, c->sms / c->lanes,
+                                             (u64)count * c->lanes <= c->pair_threshold),
+                          s));
   c->launches += 2;
   u32 status[NOALLOC_MAX_QUERIES];
   IG_CUDA(c, cudaMemcpyAsync(status, d_status, count * 4, cudaMemcpyDeviceToHost, s));

@@ -353,7 +353,8 @@ int form_batch(ig_serve* s, CrsDev* ring_out) {
   for (Req* r : sl.reqs) s->seat_refs[r->v.seat]++;
   s->seat_bytes += new_seats;
   s->peak_bytes = std::max(s->peak_bytes, s->ring.used + s->seat_bytes);
-  // Host side of the region: descriptors, shard entries, work items, seeds, b, templates.
+  // Host side of the region: descriptors, shard entries, work items and templates (the
+  // seeds and b are copied in by the dispatcher after it releases the loop's lock).
   uint8_t* h = s->h_arena + sl.off;
   uint8_t* d = s->d_arena + sl.off;
   QueryDev* hq = (QueryDev*)(h + sl.L.q);
@@ -378,8 +379,6 @@ int form_batch(ig_serve* s, CrsDev* ring_out) {
     q.row = i;
     for (u32 ch = 0; ch < igk::scan_chunks(gamma); ch++) hw[work_n++] = (i << 12) | ch;
     fold_off += gamma;
-    memcpy(h + sl.L.seeds + (size_t)i * 32, r->seed, 32);
-    memcpy(h + sl.L.bs + (size_t)i * n * 8, r->b.data(), (size_t)n * 8);
     if (!r->wire_out) {
       sl.want_ab = true;
       continue;
@@ -436,19 +435,27 @@ void dispatch_loop(ig_serve* s) {
     Slot& sl = s->slots[k];
     const u32 count = (u32)sl.reqs.size();
     const size_t n = ring.n;
-    // Two CTAs per query only while the SMs left by the batches in flight hold them; with
+    // Several CTAs per query only while the SMs left by the batches in flight hold them; with
     // other batches running, one CTA per query does the same work on fewer SMs.
-    bool pair;
+    int ctas;
     {
       std::lock_guard<std::mutex> lk(s->mu);
-      pair = (int)count <= igint::pair_threshold(s->ctx) &&
-             s->inflight_ctas + 2 * count <= (u32)igint::sm_count(s->ctx);
-      sl.ctas = pair ? 2 * count : count;
+      const u32 sms = (u32)igint::sm_count(s->ctx);
+      const u32 free_sms = s->inflight_ctas < sms ? sms - s->inflight_ctas : 1;
+      ctas = igint::launch_ctas(s->ctx, (u32)n, sl.reqs[0]->v.crs.gamma, count, free_sms,
+                                (int)count <= igint::pair_threshold(s->ctx) && s->inflight_ctas + 2 * count <= sms);
+      sl.ctas = (u32)ctas * count;
       s->inflight_ctas += sl.ctas;
     }
     uint8_t* h = s->h_arena + sl.off;
     uint8_t* d = s->d_arena + sl.off;
     const Layout& L = sl.L;
+    // The batch's requests belong to this slot until it completes: their inputs are copied
+    // into the pinned region without the loop's lock.
+    for (u32 i = 0; i < count; i++) {
+      memcpy(h + L.seeds + (size_t)i * 32, sl.reqs[i]->seed, 32);
+      memcpy(h + L.bs + (size_t)i * n * 8, sl.reqs[i]->b.data(), n * 8);
+    }
     cudaStream_t st = sl.stream;
     // Ordered after every context call made before this batch formed (shard uploads, stores).
     cudaError_t e = cudaEventRecord(sl.ready, igint::stream(s->ctx));
@@ -460,7 +467,7 @@ void dispatch_loop(ig_serve* s) {
                           (const u32*)(d + L.work), sl.work_items, (u64*)(d + L.fold), (u32*)(d + L.status), st);
     if (e == cudaSuccess)
       e = igk::respond(ring, (const QueryDev*)(d + L.q), (const ShardDev*)(d + L.table), count,
-                       (const u64*)(d + L.fold), (u64*)(d + L.a), (u64*)(d + L.b), (u32*)(d + L.status), 0, pair, st);
+                       (const u64*)(d + L.fold), (u64*)(d + L.a), (u64*)(d + L.b), (u32*)(d + L.status), 0, ctas, st);
     if (e == cudaSuccess) {
       igint::add_launches(s->ctx, 2);
       e = cudaMemcpyAsync(h + L.status, d + L.status, count * 4, cudaMemcpyDeviceToHost, st);
@@ -514,44 +521,71 @@ void complete_loop(ig_serve* s) {
     }
     Slot& sl = s->slots[k];
     const cudaError_t e = cudaEventSynchronize(sl.done);
+    // Outcomes and result copies without the loop's lock (the batch's requests belong to
+    // this slot until they finish); then, under it, the requests finish and the memory returns.
+    const uint8_t* h = s->h_arena + sl.off;
+    const Layout& L = sl.L;
+    const u32* h_status = (const u32*)(h + L.status);
+    const u32* h_wstatus = (const u32*)(h + L.wstatus);
+    enum Outcome { SERVED, LAUNCH, TAG, DEVICE, WIRE_SHAPE, WIRE_CAP };
+    std::vector<Outcome> outcome(sl.reqs.size());
+    size_t wire_off = 0;
+    for (size_t i = 0; i < sl.reqs.size(); i++) {
+      Req* r = sl.reqs[i];
+      const size_t n = r->n;
+      Outcome o = SERVED;
+      if (sl.launch_err || e != cudaSuccess) {
+        o = LAUNCH;
+      } else if (h_status[i] & DEV_TAG_MISMATCH) {
+        o = TAG;
+      } else if (h_status[i]) {
+        o = DEVICE;
+      } else if (r->wire_out) {
+        if (h_wstatus[i]) {
+          o = WIRE_SHAPE;
+        } else if (r->wire_bytes > r->wire_cap) {
+          o = WIRE_CAP;
+        } else {
+          memcpy(r->wire_out, h + L.wire + wire_off, r->wire_bytes);
+          *r->wire_len = r->wire_bytes;
+        }
+      } else {
+        memcpy(r->a_out, h + L.a + i * n * 8, n * 8);
+        memcpy(r->b_out, h + L.b + i * n * 8, n * 8);
+      }
+      outcome[i] = o;
+      wire_off += r->wire_bytes;
+    }
     {
       std::lock_guard<std::mutex> lk(s->mu);
       s->launched.pop_front();
-      const uint8_t* h = s->h_arena + sl.off;
-      const Layout& L = sl.L;
-      const u32* h_status = (const u32*)(h + L.status);
-      const u32* h_wstatus = (const u32*)(h + L.wstatus);
-      size_t wire_off = 0;
       for (size_t i = 0; i < sl.reqs.size(); i++) {
         Req* r = sl.reqs[i];
-        const size_t n = r->n;
-        if (sl.launch_err || e != cudaSuccess) {
-          refuse(s, r, IG_ERR_CUDA, "serving launch failed: %s",
-                 cudaGetErrorString(sl.launch_err ? (cudaError_t)sl.launch_err : e));
-        } else if (h_status[i] & DEV_TAG_MISMATCH) {
-          refuse(s, r, IG_ERR_STORE_REFUSED,
-                 "shard %u: packing store refused: a column is not the column the store was built from. The shard "
-                 "changed after the build; rebuild the store before serving it",
-                 r->shard);
-        } else if (h_status[i]) {
-          refuse(s, r, IG_ERR_DEVICE, "respond kernel status %u", h_status[i]);
-        } else if (r->wire_out) {
-          if (h_wstatus[i]) {
+        switch (outcome[i]) {
+          case SERVED:
+            finish(s, r, IG_OK);
+            break;
+          case LAUNCH:
+            refuse(s, r, IG_ERR_CUDA, "serving launch failed: %s",
+                   cudaGetErrorString(sl.launch_err ? (cudaError_t)sl.launch_err : e));
+            break;
+          case TAG:
+            refuse(s, r, IG_ERR_STORE_REFUSED,
+                   "shard %u: packing store refused: a column is not the column the store was built from. The "
+                   "shard changed after the build; rebuild the store before serving it",
+                   r->shard);
+            break;
+          case DEVICE:
+            refuse(s, r, IG_ERR_DEVICE, "respond kernel status %u", h_status[i]);
+            break;
+          case WIRE_SHAPE:
             refuse(s, r, IG_ERR_SHAPE, "ServerResponse encode refused: coefficients must be canonical");
-          } else if (r->wire_bytes > r->wire_cap) {
+            break;
+          case WIRE_CAP:
             refuse(s, r, IG_ERR_ARG, "wire buffer of %zu bytes is smaller than the %zu-byte response", r->wire_cap,
                    r->wire_bytes);
-          } else {
-            memcpy(r->wire_out, h + L.wire + wire_off, r->wire_bytes);
-            *r->wire_len = r->wire_bytes;
-            finish(s, r, IG_OK);
-          }
-        } else {
-          memcpy(r->a_out, h + L.a + i * n * 8, n * 8);
-          memcpy(r->b_out, h + L.b + i * n * 8, n * 8);
-          finish(s, r, IG_OK);
+            break;
         }
-        wire_off += r->wire_bytes;
       }
       // The batch's memory returns: its region (the oldest in the ring) and its keys.
       for (Req* r : sl.reqs) {

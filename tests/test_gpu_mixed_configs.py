@@ -102,11 +102,13 @@ def test_serving_loop_across_all_sets(pkg, oracle, ctx, world):
         got = [loop.wait(t, WAIT_MS).to_binary() for t in tickets]
         st = loop.stats()
     assert got == alone
-    assert st["served"] == len(reqs) and st["batches"] >= len(sets)
+    # Batches span parameter sets (one launch serves several), so 72 requests of up to 32 a
+    # batch take at least three batches, and may take fewer than the six sets.
+    assert st["served"] == len(reqs) and st["batches"] >= 3
 
 
-@pytest.mark.parametrize("threshold", [1 << 20, 0])
-def test_one_launch_across_all_sets(pkg, oracle, ctx, world, threshold):
+@pytest.mark.parametrize("shape", ["pair", "single", "quad"])
+def test_one_launch_across_all_sets(pkg, oracle, ctx, world, shape):
     """One scan and one respond launch over queries of all six sets, both seats of each and
     two switch targets: every response is the one its query gets alone, under both launch
     shapes (the launch orders its queries by gamma, so rows must come back in place)."""
@@ -121,11 +123,11 @@ def test_one_launch_across_all_sets(pkg, oracle, ctx, world, threshold):
     items = [items[i] for i in order]
     alone = [pkg.respond_seeded_batch(s.crs, s.db, pkg.SeededQueryBatch(pkg.PackingKeySource.Registered(h), [q]),
                                       s.cache, store, mod_switch_target=ms)[0].to_binary() for s, q, h, ms in items]
-    ctx.set_pair_threshold(threshold)
+    ctx.set_launch_shape({"pair": 2, "single": 1, "quad": 4}[shape])
     try:
         got = pkg.respond_mixed_batch([pkg.MixedQuery(s.db, store, h, q, ms) for s, q, h, ms in items])
     finally:
-        ctx.set_pair_threshold(76)
+        ctx.set_launch_shape(0)
     assert [r.to_binary() for r in got] == alone
     # The first query of the mix against the oracle directly.
     s, q, h, ms = items[0]
@@ -184,3 +186,46 @@ def test_mixed_launch_device_buffers_and_refusals(pkg, oracle, ctx, world):
         assert e.value.code == 5
     finally:
         s0.db.set_shard(0, s0.cell.columns(0))  # the original words: the store serves again
+
+
+def test_seats_of_either_gadget_share_one_database(pkg, oracle, ctx):
+    """A packing store depends only on the ring and the width, so one resident database
+    serves seats of the exact and the approximate gadget side by side (the reference takes
+    the CRS apart from the EncodedDatabase, respond.rs:1189-1202): a mixed launch and the
+    serving loop answer approximate-gadget seats on an exact-gadget database with the bytes
+    the approximate set's own database gives, and the single-set batch call still refuses
+    the foreign seat as the reference does."""
+    Pe, Pa = oracle.Params.d2048(), oracle.Params.d2048_approximate_gadget()
+    ce, ca = oracle.Cell(Pe, 64, 0x6A11), oracle.Cell(Pa, 64, 0x6A11)
+    assert all((ce.columns(s) == ca.columns(s)).all() for s in range(ce.num_shards))
+    sets = []
+    for cell, P, approx in ((ce, Pe, False), (ca, Pa, True)):
+        crs = pkg.ServerCrs(pkg.InspireParams(ring_dim=P.n, p=P.p, approximate_packing_gadget=approx), cell.w_seed,
+                            cell.gamma)
+        cache = pkg.ServerInspiringCache.new(crs, ctx=ctx)
+        db = pkg.EncodedDatabase.from_columns(cache, [cell.columns(s) for s in range(cell.num_shards)])
+        db.precompute_packing_all()
+        sets.append((crs, cache, db))
+    (crs_e, cache_e, db_e), (crs_a, cache_a, db_a) = sets
+    store = pkg.ServerSessionStore.new(ctx)
+    h_e = store.register_server_side(pkg.ClientPackingKeys(ce.keys(), ce.gamma), cache_e)
+    h_a = store.register_server_side(pkg.ClientPackingKeys(ca.keys(), ca.gamma), cache_a)
+    idx_a, idx_e = [5, 2048 + 7, 2 * 2048 + 100], [9, 4000]
+    qa = [pkg.SeededBatchQuery(*ca.next_query(i)) for i in idx_a]
+    qe = [pkg.SeededBatchQuery(*ce.next_query(i)) for i in idx_e]
+    alone_a = pkg.respond_seeded_batch(crs_a, db_a, pkg.SeededQueryBatch(pkg.PackingKeySource.Registered(h_a), qa),
+                                       cache_a, store)
+    alone_e = pkg.respond_seeded_batch(crs_e, db_e, pkg.SeededQueryBatch(pkg.PackingKeySource.Registered(h_e), qe),
+                                       cache_e, store)
+    mix = pkg.respond_mixed_batch([pkg.MixedQuery(db_e, store, h_a, q) for q in qa] +
+                                  [pkg.MixedQuery(db_e, store, h_e, q) for q in qe])
+    assert [r.to_binary() for r in mix] == [r.to_binary() for r in alone_a + alone_e]
+    for i, r in zip(idx_a, mix[:3]):
+        assert ca.decode(i, r.a, r.b)[0]
+    with pkg.ServingLoop(ctx, slots=2, max_batch=8) as loop:
+        tickets = [loop.submit(crs_a, db_e, q, store, h_a) for q in qa]
+        served = [loop.wait(t, WAIT_MS).to_binary() for t in tickets]
+    assert served == [r.to_binary() for r in alone_a]
+    with pytest.raises(pkg.PirError, match="another ring or gadget"):
+        pkg.respond_seeded_batch(crs_e, db_e, pkg.SeededQueryBatch(pkg.PackingKeySource.Registered(h_a), qa[:1]),
+                                 cache_e, store)

@@ -63,11 +63,16 @@ def test_d256_fixture_on_gpu(pkg, oracle, ctx):
     assert (db.store_sums(0) == ost.sums()).all()
 
 
-@pytest.fixture(params=["pair", "single"])
+@pytest.fixture(params=["pair", "single", "quad"])
 def launch_shape(request, ctx):
-    """Both respond kernels: two CTAs per query (small batches) and one CTA per query."""
-    ctx.set_pair_threshold(1 << 20 if request.param == "pair" else 0)
+    """The three respond kernels: two CTAs per query and four (clusters, for small batches),
+    and one CTA per query."""
+    if request.param == "quad":
+        ctx.set_launch_shape(4)
+    else:
+        ctx.set_pair_threshold(1 << 20 if request.param == "pair" else 0)
     yield request.param
+    ctx.set_launch_shape(0)
     ctx.set_pair_threshold(76)
 
 
