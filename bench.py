@@ -605,21 +605,26 @@ def run_sm(args, rank, world):
     server = sm.Server(ctx=ctx)
     shards = args.shards if args.shards != NUM_SHARDS else 2048
     t_setup = time.perf_counter()
-    tables = []
-    for s in range(shards):
+
+    def shard_cells(s):  # regenerable per shard, for the oracle check
         cells = np.zeros((2048, 256), dtype=np.uint8)
-        cells[:, :246] = rng.integers(0, 256, (2048, 246), dtype=np.uint8)
-        tables.append(server.table(cells.tobytes()))
-    seats = []
+        cells[:, :246] = np.random.default_rng((2 + rank, s)).integers(0, 256, (2048, 246), dtype=np.uint8)
+        return cells.tobytes()
+
+    tables = [server.table(shard_cells(s)) for s in range(shards)]
+    seats, keys = [], []
     for k in range(8):
-        key = sm.PackingKey(rng.bytes(32), rng.integers(0, 536_813_569, 2048, dtype=np.uint32),
-                            rng.integers(0, 2_147_389_441, 2048, dtype=np.uint32))
-        seats.append(server.seat(key))
+        key = (rng.bytes(32), rng.integers(0, 536_813_569, 2048, dtype=np.uint32),
+               rng.integers(0, 2_147_389_441, 2048, dtype=np.uint32))
+        keys.append(key)
+        seats.append(server.seat(sm.PackingKey(*key)))
     setup_s = time.perf_counter() - t_setup
     B = 256
     total = args.warmup + args.steps
-    tsel = [np.array([tables[i] for i in rng.integers(0, shards, B)], dtype=np.uint64) for _ in range(total)]
-    ssel = [np.array([seats[i] for i in rng.integers(0, 8, B)], dtype=np.uint64) for _ in range(total)]
+    tidx = [rng.integers(0, shards, B) for _ in range(total)]
+    sidx = [rng.integers(0, 8, B) for _ in range(total)]
+    tsel = [np.array([tables[i] for i in t], dtype=np.uint64) for t in tidx]
+    ssel = [np.array([seats[i] for i in t], dtype=np.uint64) for t in sidx]
     seeds_h = rng.integers(0, 256, (total, B, 32), dtype=np.uint8)
     bodies_h = rng.integers(0, 536_813_569, (total, B, 2048), dtype=np.uint32)
     d_seeds = torch.from_numpy(seeds_h).cuda()
@@ -664,6 +669,23 @@ def run_sm(args, rank, world):
     barrier(world)
     if int(d_status.abs().sum().item()) != 0:
         raise RuntimeError("a special-modulus batch reported a device status")
+    # Byte check outside the timing: the last batch's first and last queries (its outputs
+    # are still in their lane) against the oracle's Server::respond on the same table, key
+    # and query.
+    from oracle import oracle as O
+    O.build()
+    oserver = O.SmServer()
+    last = total - 1
+    mask_h = d_mask[last % lanes].cpu().numpy().view(np.uint32)
+    body_h = d_body[last % lanes].cpu().numpy().view(np.uint32)
+    checked = 0
+    for k in (0, B - 1):
+        otable = oserver.table(shard_cells(int(tidx[last][k])))
+        oseat = oserver.seat(keys[int(sidx[last][k])])
+        m_o, b_o = oserver.respond(otable, oseat, seeds_h[last, k].tobytes(), bodies_h[last, k])
+        if not (np.array_equal(m_o, mask_h[k]) and np.array_equal(b_o, body_h[k])):
+            raise RuntimeError(f"special_modulus response differs from the oracle (query {k} of the last batch)")
+        checked += 1
     ms = max_over_ranks(ev0.elapsed_time(ev1), world)
     value = world * B * args.steps / (ms / 1e3)
     # e2e: Server::respond for each batch with host buffers, from `lanes` caller threads
@@ -701,6 +723,7 @@ def run_sm(args, rank, world):
         "vs_baseline": None, "dtype": "u32 (exact mod q and p)",
         "data": "synthetic: uniform record bytes, uniform key and query words",
         "config": dict(SM_CONFIG, shards=shards, lanes=lanes),
+        "parity_checked": checked,
         "db_gbs": value * 2048 * 256 / 1e9,
         "e2e": {"value": e2e, "unit": "queries/s", "h2d_bytes_per_step": B * (32 + 2048 * 4),
                 "d2h_bytes_per_step": B * (2048 + 492) * 4, "callers": lanes},
@@ -972,9 +995,6 @@ def run_cfg4(args, rank, world):
     stream = torch.cuda.ExternalStream(ctx.stream)
     lanes = args.lanes
 
-    def ctx_sms():
-        return torch.cuda.get_device_properties(local).multi_processor_count
-
     def launch(i):
         count = plan[i][0]
         dbh, sth, hh, sids, ms = arrays[i]
@@ -1063,7 +1083,7 @@ def run_cfg4(args, rank, world):
                                      pkg.SeededBatchQuery(int(rng.integers(0, d["shards"])), rng.bytes(32),
                                                           rand_words(rng, N_RING)))
                       for _ in range(count)]
-            row = {"tuned_choice": ctx.launch_shape_for(d["gamma"], count, ctx_sms())}
+            row = {"tuned_choice": ctx.launch_shape_for(d["gamma"], count)}
             for shape in (1, 2, 4):
                 ctx.set_launch_shape(shape)
                 lat = []
@@ -1139,9 +1159,10 @@ def run_cfg4(args, rank, world):
                 "call": "respond_mixed_batch (one launch per call)"},
         "fixed_rule": {"value": fixed_value, "unit": "queries/s",
                        "rule": "two CTAs per query while count x lanes <= SMs / 2, else one"},
-        "launch_shapes": {"tuned_ms_per_wave": {str(g): {"1": t[0], "2": t[1], "4": t[2]} for g, t in tuned.items()},
+        "launch_shapes": {"tuned_ms_per_launch": {str(g): {str(b): {"1": t[0], "2": t[1], "4": t[2]}
+                                                           for b, t in rows.items()} for g, rows in tuned.items()},
                           "tune_s": tune_s,
-                          "rule": "per launch the shape with the least ceil(count x ctas / (SMs / lanes)) x wave time"},
+                          "rule": "per launch the shape the table times fastest at count x lanes queries in flight"},
         "latency": latency,
         "plain_per_query": {"queries_per_s": plain_qps, "queries": len(flat),
                             "call": "one respond_mixed_batch call per query (host buffers)"},

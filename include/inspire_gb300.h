@@ -57,28 +57,30 @@ uint64_t ig_ctx_device_bytes(const ig_ctx* ctx);
  * Responses are identical either way. */
 int ig_ctx_set_pair_threshold(ig_ctx* ctx, uint32_t max_queries);
 /* Launch shapes and their tuner. A respond launch runs 1, 2 or 4 CTAs per query: one CTA
- * per SM is the most work per SM-second, a cluster of 2 or 4 splits each query's
+ * per SM is the most work per SM-second; a cluster of 2 or 4 splits each query's
  * transforms over as many SMs and answers a small batch sooner. No counterpart in the
  * reference (its respond is CPU code).
  * ig_ctx_set_launch_shape fixes the shape of every later respond launch (1, 2 or 4), or
  * with 0 lets each launch choose: from the tuned table when it holds the launch's ring (the
- * nearest tuned gamma of it), else by the pair-threshold rule above.
+ * tuned gamma nearest the launch's), else by the pair-threshold rule above.
  * ig_tune_launch_shapes measures the table for `count` packing widths on ring_dim: for each
- * width and shape, the milliseconds of one full wave (SMs / ctas queries) on a synthetic
- * database of 8 shards, a synthetic seat and queries (built and freed inside), each the mean
- * of `reps` launches after one warm-up. A launch of q queries that can expect f free SMs
- * then takes the shape with the least ceil(q x ctas / f) x wave time; the device path counts
- * SMs / lanes as free, the serving loop the SMs its batches in flight leave. Responses are
- * identical under every shape.
- * ig_tune_get copies the entry of (ring_dim, gamma) (ms_out[0..2]: 1, 2, 4 CTAs);
- * ig_tune_save writes the table to a text file with the device's SM count, and
- * ig_tune_load merges a saved table, refusing one measured on another SM count. */
+ * width, each batch size of the grid 1, 4, 16, 32, 64, 128, 256 and each shape, the mean
+ * milliseconds of `reps` launches (after one warm-up) on a synthetic database of 8 shards,
+ * a synthetic seat and queries, built and freed inside. A launch then takes the shape whose
+ * time is least (by at least 2% for more CTAs) in the table's row for the queries expected
+ * in flight with it: the smallest tuned batch size at or above that number, the largest
+ * beyond the grid. The device path expects count x lanes queries in flight, the serving
+ * loop its batch and the CTAs of its batches in flight. Responses are identical under
+ * every shape.
+ * ig_tune_get copies the row of (ring_dim, gamma) for `queries` in flight (ms_out[0..2]: 1,
+ * 2, 4 CTAs per query); ig_tune_choose gives the shape a launch of `count` queries with
+ * `in_flight` queries expected would take. ig_tune_save writes the table to a text file
+ * with the device's SM count, and ig_tune_load merges a saved table, refusing one measured
+ * on another SM count. */
 int ig_ctx_set_launch_shape(ig_ctx* ctx, uint32_t ctas);
 int ig_tune_launch_shapes(ig_ctx* ctx, uint32_t ring_dim, const uint32_t* gammas, uint32_t count, uint32_t reps);
-int ig_tune_get(ig_ctx* ctx, uint32_t ring_dim, uint32_t gamma, double* ms_out);
-/* The shape a launch of `count` queries of width gamma on ring_dim would take with free_sms
- * SMs free (*ctas: 1, 2 or 4). */
-int ig_tune_choose(ig_ctx* ctx, uint32_t ring_dim, uint32_t gamma, uint32_t count, uint32_t free_sms,
+int ig_tune_get(ig_ctx* ctx, uint32_t ring_dim, uint32_t gamma, uint32_t queries, double* ms_out);
+int ig_tune_choose(ig_ctx* ctx, uint32_t ring_dim, uint32_t gamma, uint32_t count, uint32_t in_flight,
                    uint32_t* ctas);
 int ig_tune_save(ig_ctx* ctx, const char* path);
 int ig_tune_load(ig_ctx* ctx, const char* path);

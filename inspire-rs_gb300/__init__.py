@@ -39,6 +39,7 @@ __all__ = [
 
 DEFAULT_Q = 1152921504606830593
 MOD_SWITCH_TARGET_36BIT = 68_718_428_161
+TUNE_BATCHES = (1, 4, 16, 32, 64, 128, 256)  # batch sizes the launch-shape tuner measures
 MOD_SWITCH_TARGET_45BIT = 35_184_372_060_161
 
 IG_OK = 0
@@ -130,7 +131,7 @@ def _load():
         "ig_ctx_set_pair_threshold": (I, [P, U32]),
         "ig_ctx_set_launch_shape": (I, [P, U32]),
         "ig_tune_launch_shapes": (I, [P, U32, P, U32, U32]),
-        "ig_tune_get": (I, [P, U32, U32, P]),
+        "ig_tune_get": (I, [P, U32, U32, U32, P]),
         "ig_tune_choose": (I, [P, U32, U32, U32, U32, ctypes.POINTER(U32)]),
         "ig_tune_save": (I, [P, ctypes.c_char_p]),
         "ig_tune_load": (I, [P, ctypes.c_char_p]),
@@ -217,22 +218,25 @@ class Context:
         self.check(self._lib.ig_ctx_set_launch_shape(self.h, int(ctas)))
 
     def tune_launch_shapes(self, gammas, ring_dim=2048, reps=3):
-        """Measures one full wave of queries under 1, 2 and 4 CTAs per query for each width;
-        returns {gamma: (ms_1, ms_2, ms_4)} and keeps the table for later launches."""
+        """Measures launches of 1 .. 256 queries under 1, 2 and 4 CTAs per query for each
+        width; returns {gamma: {batch: (ms_1, ms_2, ms_4)}} and keeps the table for later
+        launches."""
         g = np.ascontiguousarray(gammas, dtype=np.uint32)
         self.check(self._lib.ig_tune_launch_shapes(self.h, int(ring_dim), _ptr(g), len(g), int(reps)))
-        return {int(x): self.tuned(int(x), ring_dim) for x in g}
+        return {int(x): {b: self.tuned(int(x), b, ring_dim) for b in TUNE_BATCHES} for x in g}
 
-    def tuned(self, gamma, ring_dim=2048):
+    def tuned(self, gamma, queries=1, ring_dim=2048):
+        """The tuned row (ms under 1, 2, 4 CTAs per query) for `queries` in flight."""
         ms = np.zeros(3, dtype=np.float64)
-        self.check(self._lib.ig_tune_get(self.h, int(ring_dim), int(gamma), _ptr(ms)))
+        self.check(self._lib.ig_tune_get(self.h, int(ring_dim), int(gamma), int(queries), _ptr(ms)))
         return tuple(float(x) for x in ms)
 
-    def launch_shape_for(self, gamma, count, free_sms, ring_dim=2048):
-        """CTAs per query a launch of `count` queries of width gamma would take with free_sms free."""
+    def launch_shape_for(self, gamma, count, in_flight=None, ring_dim=2048):
+        """CTAs per query a launch of `count` queries would take with `in_flight` queries
+        expected on the device (default: the launch alone)."""
         out = ctypes.c_uint32()
-        self.check(self._lib.ig_tune_choose(self.h, int(ring_dim), int(gamma), int(count), int(free_sms),
-                                            ctypes.byref(out)))
+        self.check(self._lib.ig_tune_choose(self.h, int(ring_dim), int(gamma), int(count),
+                                            int(count if in_flight is None else in_flight), ctypes.byref(out)))
         return out.value
 
     def save_tuning(self, path):

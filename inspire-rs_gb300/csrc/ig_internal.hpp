@@ -42,9 +42,10 @@ struct RequestView {
 int resolve_request(ig_ctx* c, uint64_t db, uint64_t store, uint64_t handle, uint32_t shard, RequestView* out);
 int pair_threshold(ig_ctx* c);
 // CTAs per query (1, 2 or 4) for a respond launch of `count` queries of width `gamma` on
-// ring n that can expect `free_sms` SMs: the forced shape, else the tuned estimate, else
-// the fixed rule's answer (fixed_rule_pair: the pair form, otherwise one CTA a query).
-int launch_ctas(ig_ctx* c, uint32_t n, uint32_t gamma, uint32_t count, uint32_t free_sms, bool fixed_rule_pair);
+// ring n with `in_flight` queries expected on the device with it (its own included): the
+// forced shape, else the shape the tuned table times fastest at that many queries, else the
+// fixed rule's answer (fixed_rule_pair: the pair form, otherwise one CTA a query).
+int launch_ctas(ig_ctx* c, uint32_t n, uint32_t gamma, uint32_t count, uint32_t in_flight, bool fixed_rule_pair);
 // Device-path lanes (ig_ctx_set_lanes), for callers holding the context lock:
 // lane_acquire picks the call's stream (the context stream when lanes == 1, lane -1) and
 // orders the context stream after the lane's previous batch, so the lane's scratch can be

@@ -210,11 +210,12 @@ struct ig_ctx {
   // (1 = the next one; 0 = none).
   std::atomic<u32> fail_alloc_at{0};
   // Launch shape of respond launches (CTAs per query). force_ctas != 0 fixes it; otherwise,
-  // with a tuned entry for the launch's (ring, gamma), the shape with the least estimated
-  // completion time is taken, else the fixed pair_threshold rule. tune[(n, gamma)] holds the
-  // measured milliseconds of one full wave (SMs / ctas queries) under 1, 2 and 4 CTAs.
+  // with a tuned entry for the launch's (ring, gamma), the shape whose measured launch time
+  // is least at the number of queries expected in flight, else the fixed pair_threshold
+  // rule. tune[(n, gamma)] maps a batch size to the measured milliseconds of one launch of
+  // that many queries under 1, 2 and 4 CTAs per query.
   u32 force_ctas = 0;
-  std::map<std::pair<u32, u32>, std::array<double, 3>> tune;
+  std::map<std::pair<u32, u32>, std::map<u32, std::array<double, 3>>> tune;
   cudaStream_t lane_stream[IG_MAX_LANES] = {};
   cudaEvent_t lane_in[IG_MAX_LANES] = {}, lane_done[IG_MAX_LANES] = {};
   bool lane_used[IG_MAX_LANES] = {};
@@ -505,31 +506,38 @@ int stage_h2d(ig_ctx* c, void* dst, const void* src, size_t bytes) { return ::st
 void add_launches(ig_ctx* c, unsigned n) { c->launches += n; }
 void*& sm_slot(ig_ctx* c) { return c->sm; }
 int pair_threshold(ig_ctx* c) { return (int)c->pair_threshold; }
-int launch_ctas(ig_ctx* c, u32 n, u32 gamma, u32 count, u32 free_sms, bool fixed_rule_pair) {
-  if (c->force_ctas) return (int)c->force_ctas;
+// The tuned row for `queries` in flight: the smallest measured batch size at or above it
+// (the largest measured one beyond the grid), of the tuned width nearest gamma on ring n.
+static const std::array<double, 3>* tuned_row(ig_ctx* c, u32 n, u32 gamma, u32 queries) {
   auto it = c->tune.find({n, gamma});
   if (it == c->tune.end()) {
-    // The nearest tuned width of the ring, if any.
-    for (auto jt = c->tune.begin(); jt != c->tune.end(); ++jt)
-      if (jt->first.first == n &&
-          (it == c->tune.end() || (jt->first.second > gamma ? jt->first.second - gamma : gamma - jt->first.second) <
-                                      (it->first.second > gamma ? it->first.second - gamma : gamma - it->first.second)))
-        it = jt;
+    for (auto jt = c->tune.begin(); jt != c->tune.end(); ++jt) {
+      if (jt->first.first != n) continue;
+      const u32 dj = jt->first.second > gamma ? jt->first.second - gamma : gamma - jt->first.second;
+      const u32 di = it == c->tune.end() ? ~0u
+                                         : (it->first.second > gamma ? it->first.second - gamma : gamma - it->first.second);
+      if (dj < di) it = jt;
+    }
   }
-  if (it == c->tune.end()) return fixed_rule_pair ? 2 : 1;
-  // Waves of this launch on the SMs it can expect, times a wave's measured duration.
-  const u32 freeq = free_sms ? free_sms : 1;
+  if (it == c->tune.end() || it->second.empty()) return nullptr;
+  auto row = it->second.lower_bound(queries);
+  if (row == it->second.end()) --row;
+  return &row->second;
+}
+
+int launch_ctas(ig_ctx* c, u32 n, u32 gamma, u32 count, u32 in_flight, bool fixed_rule_pair) {
+  if (c->force_ctas) return (int)c->force_ctas;
+  const std::array<double, 3>* row = tuned_row(c, n, gamma, std::max(count, in_flight));
+  if (!row) return fixed_rule_pair ? 2 : 1;
+  const int shapes[3] = {1, 2, 4};
   int best = 1;
   double best_ms = 0;
-  const int shapes[3] = {1, 2, 4};
   for (int k = 0; k < 3; k++) {
-    const double t = it->second[k];
+    const double t = (*row)[k];
     if (!(t > 0)) continue;
-    const u64 waves = ((u64)count * shapes[k] + freeq - 1) / freeq;
-    const double ms = (double)waves * t;
-    if (best_ms == 0 || ms < best_ms * 0.999) {
+    if (best_ms == 0 || t < best_ms * 0.98) {  // a shape must be 2% faster to take more SMs
       best = shapes[k];
-      best_ms = ms;
+      best_ms = t;
     }
   }
   return best;
@@ -1361,7 +1369,7 @@ static int respond_host(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_t handle, c
   pk = prof_begin(c, REGION_RESPOND, s);
   IG_CUDA(c, igk::respond(o.dev, (const QueryDev*)d_q, (const ShardDev*)d_table, count, (const u64*)d_fold,
                           (u64*)d_a, (u64*)d_b, (u32*)d_status, c->force_serial,
-                          igint::launch_ctas(c, (u32)n, (u32)g, count, c->sms / lanes,
+                          igint::launch_ctas(c, (u32)n, (u32)g, count, count * lanes,
                                              (u64)count * lanes <= c->pair_threshold),
                           s));
   prof_end(c, pk, s);
@@ -1890,7 +1898,7 @@ int ig_respond_seeded_batch_device(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_
   IG_CUDA(c, igk::shard_scan(o.dev, (const QueryDev*)d_q, db->d_table, count, nullptr, 0, (u64*)d_fold, d_status, s));
   prof_end(c, pk, s);
   // Several CTAs per query only while every lane's batch still leaves SMs for them.
-  const int ctas = igint::launch_ctas(c, (u32)n, (u32)g, count, c->sms / c->lanes,
+  const int ctas = igint::launch_ctas(c, (u32)n, (u32)g, count, count * c->lanes,
                                       (u64)count * c->lanes <= c->pair_threshold);
   pk = prof_begin(c, REGION_RESPOND, s);
   IG_CUDA(c, igk::respond(o.dev, (const QueryDev*)d_q, db->d_table, count, (const u64*)d_fold, d_a, d_b, d_status,
@@ -2021,7 +2029,7 @@ int ig_respond_mixed_batch_device(ig_ctx* c, uint32_t count, const uint64_t* dbs
   IG_CUDA(c, igk::shard_scan(P.ring, (const QueryDev*)dq, (const ShardDev*)dt, count, (const u32*)dw,
                              (u32)P.work.size(), (u64*)df, d_status, s));
   prof_end(c, pk, s);
-  const int ctas = igint::launch_ctas(c, (u32)n, P.max_gamma, count, c->sms / c->lanes,
+  const int ctas = igint::launch_ctas(c, (u32)n, P.max_gamma, count, count * c->lanes,
                                       (u64)count * c->lanes <= c->pair_threshold);
   pk = prof_begin(c, REGION_RESPOND, s);
   IG_CUDA(c, igk::respond(P.ring, (const QueryDev*)dq, (const ShardDev*)dt, count, (const u64*)df, d_a, d_b, d_status,
@@ -2085,7 +2093,7 @@ int ig_respond_mixed_batch(ig_ctx* c, uint32_t count, const uint64_t* dbs, const
                              (u32)P.work.size(), (u64*)df, (u32*)dst, s));
   IG_CUDA(c, igk::respond(P.ring, (const QueryDev*)dq, (const ShardDev*)dt, count, (const u64*)df, (u64*)da, (u64*)db_,
                           (u32*)dst, c->force_serial,
-                          igint::launch_ctas(c, (u32)n, P.max_gamma, count, c->sms / c->lanes,
+                          igint::launch_ctas(c, (u32)n, P.max_gamma, count, count * c->lanes,
                                              (u64)count * c->lanes <= c->pair_threshold),
                           s));
   c->launches += 2;
@@ -2417,10 +2425,11 @@ int ig_ctx_set_launch_shape(ig_ctx* c, uint32_t ctas) {
   return IG_OK;
 }
 
-// The launch-shape tuner: per width, one full wave of queries (SMs / ctas of them) under each
-// shape, on a synthetic database, seat and queries built here and freed after; the same
-// respond path as serving (scan and respond launches, device buffers), timed with CUDA events
-// on the context stream.
+// The launch-shape tuner: per width, launches of kTuneBatches queries under each shape, on a
+// synthetic database, seat and queries built here and freed after; the same respond path as
+// serving (scan and respond launches, device buffers), timed with CUDA events on the context
+// stream.
+static const u32 kTuneBatches[] = {1, 4, 16, 32, 64, 128, 256};
 int ig_tune_launch_shapes(ig_ctx* c, uint32_t ring_dim, const uint32_t* gammas, uint32_t count, uint32_t reps) {
   if (!c) return IG_ERR_ARG;
   if (!gammas || count == 0 || reps == 0 || reps > 1000)
@@ -2433,7 +2442,7 @@ int ig_tune_launch_shapes(ig_ctx* c, uint32_t ring_dim, const uint32_t* gammas, 
   }
   int rc = ig_ctx_set_lanes(c, 1);
   if (rc) return rc;
-  const u32 n = ring_dim, sms = c->sms ? c->sms : 1;
+  const u32 n = ring_dim, maxq = kTuneBatches[sizeof kTuneBatches / sizeof kTuneBatches[0] - 1];
   const u32 shards = 8;
   std::mt19937_64 rng(0x7u);
   u64 *d_bs = nullptr, *d_a = nullptr, *d_b = nullptr;
@@ -2441,11 +2450,11 @@ int ig_tune_launch_shapes(ig_ctx* c, uint32_t ring_dim, const uint32_t* gammas, 
   u32* d_status = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   auto cleanup = [&]() {
-    if (d_bs) dfree(c, d_bs, (size_t)sms * n * 8);
-    if (d_a) dfree(c, d_a, (size_t)sms * n * 8);
-    if (d_b) dfree(c, d_b, (size_t)sms * n * 8);
-    if (d_seeds) dfree(c, d_seeds, (size_t)sms * 32);
-    if (d_status) dfree(c, d_status, (size_t)sms * 4);
+    if (d_bs) dfree(c, d_bs, (size_t)maxq * n * 8);
+    if (d_a) dfree(c, d_a, (size_t)maxq * n * 8);
+    if (d_b) dfree(c, d_b, (size_t)maxq * n * 8);
+    if (d_seeds) dfree(c, d_seeds, (size_t)maxq * 32);
+    if (d_status) dfree(c, d_status, (size_t)maxq * 4);
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
     {
@@ -2457,17 +2466,17 @@ int ig_tune_launch_shapes(ig_ctx* c, uint32_t ring_dim, const uint32_t* gammas, 
   {
     std::lock_guard<std::mutex> lk(c->mu);
     cudaSetDevice(c->device);
-    if ((rc = dalloc(c, (void**)&d_bs, (size_t)sms * n * 8, nullptr)) ||
-        (rc = dalloc(c, (void**)&d_a, (size_t)sms * n * 8, nullptr)) ||
-        (rc = dalloc(c, (void**)&d_b, (size_t)sms * n * 8, nullptr)) ||
-        (rc = dalloc(c, (void**)&d_seeds, (size_t)sms * 32, nullptr)) ||
-        (rc = dalloc(c, (void**)&d_status, (size_t)sms * 4, nullptr))) {
+    if ((rc = dalloc(c, (void**)&d_bs, (size_t)maxq * n * 8, nullptr)) ||
+        (rc = dalloc(c, (void**)&d_a, (size_t)maxq * n * 8, nullptr)) ||
+        (rc = dalloc(c, (void**)&d_b, (size_t)maxq * n * 8, nullptr)) ||
+        (rc = dalloc(c, (void**)&d_seeds, (size_t)maxq * 32, nullptr)) ||
+        (rc = dalloc(c, (void**)&d_status, (size_t)maxq * 4, nullptr))) {
       cleanup();
       return rc;
     }
-    std::vector<u64> hb((size_t)sms * n);
+    std::vector<u64> hb((size_t)maxq * n);
     for (auto& x : hb) x = rng() % Q;
-    std::vector<uint8_t> hs((size_t)sms * 32);
+    std::vector<uint8_t> hs((size_t)maxq * 32);
     for (auto& x : hs) x = (uint8_t)rng();
     cudaMemcpy(d_bs, hb.data(), hb.size() * 8, cudaMemcpyHostToDevice);
     cudaMemcpy(d_seeds, hs.data(), hs.size(), cudaMemcpyHostToDevice);
@@ -2504,26 +2513,30 @@ int ig_tune_launch_shapes(ig_ctx* c, uint32_t ring_dim, const uint32_t* gammas, 
       cleanup();
       return rc;
     }
-    std::array<double, 3> ms{};
+    std::map<u32, std::array<double, 3>> rows;
     const u32 shapes[3] = {1, 2, 4};
-    for (int k = 0; k < 3 && !rc; k++) {
-      const u32 batch = std::max(1u, sms / shapes[k]);
+    for (u32 batch : kTuneBatches) {
+      std::array<double, 3> ms{};
       std::vector<u32> sids(batch);
       for (u32 q = 0; q < batch; q++) sids[q] = q % shards;
-      {
-        std::lock_guard<std::mutex> lk(c->mu);
-        c->force_ctas = shapes[k];
+      for (int k = 0; k < 3 && !rc; k++) {
+        {
+          std::lock_guard<std::mutex> lk(c->mu);
+          c->force_ctas = shapes[k];
+        }
+        for (u32 r = 0; r <= reps && !rc; r++) {
+          if (r == 1) cudaEventRecord(e0, c->stream);  // after one untimed warm-up launch
+          rc = ig_respond_seeded_batch_device(c, db, store, handle, batch, sids.data(), d_seeds, d_bs, 0, d_a, d_b,
+                                              d_status);
+        }
+        cudaEventRecord(e1, c->stream);
+        if (cudaEventSynchronize(e1) != cudaSuccess && !rc)
+          rc = fail(c, IG_ERR_CUDA, "ig_tune_launch_shapes: launch failed");
+        float el = 0;
+        cudaEventElapsedTime(&el, e0, e1);
+        ms[k] = el / reps;
       }
-      for (u32 r = 0; r <= reps && !rc; r++) {
-        if (r == 1) cudaEventRecord(e0, c->stream);  // after one untimed warm-up launch
-        rc = ig_respond_seeded_batch_device(c, db, store, handle, batch, sids.data(), d_seeds, d_bs, 0, d_a, d_b,
-                                            d_status);
-      }
-      cudaEventRecord(e1, c->stream);
-      if (cudaEventSynchronize(e1) != cudaSuccess && !rc) rc = fail(c, IG_ERR_CUDA, "ig_tune_launch_shapes: launch failed");
-      float el = 0;
-      cudaEventElapsedTime(&el, e0, e1);
-      ms[k] = el / reps;
+      rows[batch] = ms;
     }
     drop();
     if (rc) {
@@ -2531,26 +2544,27 @@ int ig_tune_launch_shapes(ig_ctx* c, uint32_t ring_dim, const uint32_t* gammas, 
       return rc;
     }
     std::lock_guard<std::mutex> lk(c->mu);
-    c->tune[{n, gamma}] = ms;
+    c->tune[{n, gamma}] = rows;
   }
   cleanup();
   return IG_OK;
 }
 
-int ig_tune_get(ig_ctx* c, uint32_t ring_dim, uint32_t gamma, double* ms_out) {
+int ig_tune_get(ig_ctx* c, uint32_t ring_dim, uint32_t gamma, uint32_t queries, double* ms_out) {
   if (!c || !ms_out) return IG_ERR_ARG;
   std::lock_guard<std::mutex> lk(c->mu);
   auto it = c->tune.find({ring_dim, gamma});
-  if (it == c->tune.end())
+  if (it == c->tune.end() || it->second.empty())
     return fail(c, IG_ERR_HANDLE, "no launch-shape entry for ring_dim %u, gamma %u", ring_dim, gamma);
-  for (int k = 0; k < 3; k++) ms_out[k] = it->second[k];
+  const std::array<double, 3>* row = igint::tuned_row(c, ring_dim, gamma, queries);
+  for (int k = 0; k < 3; k++) ms_out[k] = (*row)[k];
   return IG_OK;
 }
 
-int ig_tune_choose(ig_ctx* c, uint32_t ring_dim, uint32_t gamma, uint32_t count, uint32_t free_sms, uint32_t* ctas) {
+int ig_tune_choose(ig_ctx* c, uint32_t ring_dim, uint32_t gamma, uint32_t count, uint32_t in_flight, uint32_t* ctas) {
   if (!c || !ctas) return IG_ERR_ARG;
   std::lock_guard<std::mutex> lk(c->mu);
-  *ctas = (u32)igint::launch_ctas(c, ring_dim, gamma, count, free_sms, (u64)count <= c->pair_threshold);
+  *ctas = (u32)igint::launch_ctas(c, ring_dim, gamma, count, in_flight, (u64)std::max(count, in_flight) <= c->pair_threshold);
   return IG_OK;
 }
 
@@ -2559,9 +2573,11 @@ int ig_tune_save(ig_ctx* c, const char* path) {
   std::lock_guard<std::mutex> lk(c->mu);
   FILE* f = fopen(path, "w");
   if (!f) return fail(c, IG_ERR_ARG, "ig_tune_save: cannot write %s", path);
-  fprintf(f, "inspire_gb300 launch shapes 1\nsms %u\n", c->sms);
+  fprintf(f, "inspire_gb300 launch shapes 2\nsms %u\n", c->sms);
   for (const auto& kv : c->tune)
-    fprintf(f, "%u %u %.6f %.6f %.6f\n", kv.first.first, kv.first.second, kv.second[0], kv.second[1], kv.second[2]);
+    for (const auto& row : kv.second)
+      fprintf(f, "%u %u %u %.6f %.6f %.6f\n", kv.first.first, kv.first.second, row.first, row.second[0],
+              row.second[1], row.second[2]);
   const bool ok = fclose(f) == 0;
   return ok ? IG_OK : fail(c, IG_ERR_ARG, "ig_tune_save: writing %s failed", path);
 }
@@ -2571,17 +2587,17 @@ int ig_tune_load(ig_ctx* c, const char* path) {
   FILE* f = fopen(path, "r");
   if (!f) return fail(c, IG_ERR_ARG, "ig_tune_load: cannot read %s", path);
   unsigned version = 0, sms = 0;
-  std::map<std::pair<u32, u32>, std::array<double, 3>> table;
+  std::map<std::pair<u32, u32>, std::map<u32, std::array<double, 3>>> table;
   int rc = IG_OK;
-  if (fscanf(f, "inspire_gb300 launch shapes %u sms %u", &version, &sms) != 2 || version != 1) {
+  if (fscanf(f, "inspire_gb300 launch shapes %u sms %u", &version, &sms) != 2 || version != 2) {
     rc = fail(c, IG_ERR_ARG, "ig_tune_load: %s is not a launch-shape table", path);
   } else if (sms != c->sms) {
     rc = fail(c, IG_ERR_ARG, "ig_tune_load: %s was measured on %u SMs, this device has %u", path, sms, c->sms);
   } else {
-    unsigned n, g;
+    unsigned n, g, q;
     double a, b, d;
     int got;
-    while ((got = fscanf(f, "%u %u %lf %lf %lf", &n, &g, &a, &b, &d)) == 5) table[{n, g}] = {a, b, d};
+    while ((got = fscanf(f, "%u %u %u %lf %lf %lf", &n, &g, &q, &a, &b, &d)) == 6) table[{n, g}][q] = {a, b, d};
     if (got != EOF) rc = fail(c, IG_ERR_ARG, "ig_tune_load: %s holds a malformed line", path);
   }
   fclose(f);
@@ -2813,7 +2829,7 @@ int ig_respond_seeded_batch_noalloc(ig_ctx* c, uint64_t dbh, uint64_t st, uint64
   IG_CUDA(c, igk::shard_scan(o.dev, d_q, db->d_table, count, nullptr, 0, d_fold, d_status, s));
   // The launch shape of ig_respond_seeded_batch_device for the same batch and lane count.
   IG_CUDA(c, igk::respond(o.dev, d_q, db->d_table, count, d_fold, d_a, d_b, d_status, c->force_serial,
-                          igint::launch_ctas(c, (u32)n, (u32)g, count, c->sms / c->lanes,
+                          igint::launch_ctas(c, (u32)n, (u32)g, count, count * c->lanes,
                                              (u64)count * c->lanes <= c->pair_threshold),
                           s));
   c->launches += 2;

@@ -441,8 +441,7 @@ void dispatch_loop(ig_serve* s) {
     {
       std::lock_guard<std::mutex> lk(s->mu);
       const u32 sms = (u32)igint::sm_count(s->ctx);
-      const u32 free_sms = s->inflight_ctas < sms ? sms - s->inflight_ctas : 1;
-      ctas = igint::launch_ctas(s->ctx, (u32)n, sl.reqs[0]->v.crs.gamma, count, free_sms,
+      ctas = igint::launch_ctas(s->ctx, (u32)n, sl.reqs[0]->v.crs.gamma, count, count + s->inflight_ctas,
                                 (int)count <= igint::pair_threshold(s->ctx) && s->inflight_ctas + 2 * count <= sms);
       sl.ctas = (u32)ctas * count;
       s->inflight_ctas += sl.ctas;

@@ -15,21 +15,33 @@ def test_tune_save_load_choose(oracle, tmp_path):
     pkg = load_package()
     ctx = pkg.Context(0)
     table = ctx.tune_launch_shapes([16, 256], reps=1)
-    for g, ms in table.items():
-        assert len(ms) == 3 and all(x > 0 for x in ms), (g, ms)
+    for g, rows in table.items():
+        assert sorted(rows) == list(pkg.TUNE_BATCHES)
+        for b, ms in rows.items():
+            assert len(ms) == 3 and all(x > 0 for x in ms), (g, b, ms)
     path = tmp_path / "shapes.txt"
     ctx.save_tuning(path)
     other = pkg.Context(0)
     with pytest.raises(pkg.PirError, match="no launch-shape entry"):
         other.tuned(256)
     other.load_tuning(path)
-    assert other.tuned(256) == pytest.approx(table[256], rel=1e-5)
-    # A lone query spreads over the most SMs the table finds worth it; a batch that fills
-    # the GPU several times over runs one CTA per query.
-    t1, t2, t4 = table[256]
-    lone = other.launch_shape_for(256, 1, 152)
-    assert lone == min((1, 2, 4), key=lambda s: ({1: t1, 2: t2, 4: t4}[s], s))
-    assert other.launch_shape_for(256, 4096, 152) == 1
+    for b in pkg.TUNE_BATCHES:
+        assert other.tuned(256, b) == pytest.approx(table[256][b], rel=1e-5)
+
+    def pick(ms):  # the fastest shape, more CTAs only when at least 2% faster
+        best = 0
+        for k in (1, 2):
+            if ms[k] < ms[best] * 0.98:
+                best = k
+        return (1, 2, 4)[best]
+
+    # A lone query takes the row of one query in flight; between grid points the next row
+    # up; beyond the grid the last row.
+    assert other.launch_shape_for(256, 1) == pick(table[256][1])
+    assert other.launch_shape_for(256, 3) == pick(table[256][4])
+    assert other.launch_shape_for(256, 64, in_flight=4096) == pick(table[256][256])
+    # Many queries in flight fill the GPU several times over: one CTA per query.
+    assert pick(table[256][256]) == 1
     # A table measured on another SM count is refused.
     text = path.read_text().splitlines()
     text[1] = "sms 7"
