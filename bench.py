@@ -63,10 +63,18 @@ def peaks():
         return 6800.0, "fallback"
 
 
-# DRAM bytes (read + write) of one k_scan launch of this workload, from an ncu capture
-# (dram__bytes_read.sum + dram__bytes_write.sum per launch; the command is in
-# profiles/k_scan_batch64_d2048_g256.md), or None until one is recorded for this kernel.
-SCAN_TRAFFIC_BYTES = None
+# DRAM bytes (read + write) of one k_scan launch of this workload, from an ncu capture of a
+# batch of 64 queries of gamma 256 on a 512-shard database with L2 flushed before the launch
+# (dram__bytes_read.sum + dram__bytes_write.sum: 66,102,528 + 508,416; the command is in
+# profiles/k_scan_batch64_d2048_g256.md). It sits just under the algorithmic bytes: each
+# byte is read once.
+SCAN_TRAFFIC_BYTES = 66_610_944
+# Heavy integer pipe (IMAD, IMAD.WIDE, IMAD.HI) busy cycles of k_respond per query, summed
+# over the four sub-partitions of each SM: sm__pipe_fmaheavy_cycles_active.sum of one
+# 64-query launch of this workload's timed region (1,043,445,848) / 64, from the ncu
+# capture in profiles/k_respond_single_batch64_d2048_g256.md. The pipe offers four such
+# cycles per SM per clock.
+RESPOND_HEAVY_CYCLES_PER_QUERY = 16_303_841
 
 
 def shard_seed(rank, s):
@@ -502,15 +510,20 @@ def run_gb300(args, rank, world):
     scan_bytes = BATCH * (GAMMA * N_RING * 2 + N_RING * 8 + GAMMA * 8)
     hbm_peak, peak_kind = peaks()
     achieved = scan_bytes / (scan_avg / 1e3) / 1e9
-    # Recursion: 3 transforms of n/2 log n butterflies per link, and per slot 7 pointwise
-    # products (the folded gadget rows: 3 for the seat sum, 4 for the next R) and 2
-    # Montgomery reductions of 2 products each.
+    # The respond kernel is bound by the heavy integer pipe: its roofline counts that pipe's
+    # busy cycles (ncu's per-query count, RESPOND_HEAVY_CYCLES_PER_QUERY) against the cycles
+    # the pipe offers, four per SM per clock at the SM clock sampled during the timed region.
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    clk_sum = clk.summary()
+    mhz = clk_sum["sm_mhz"] or 2070.0
+    heavy_achieved = value / world * RESPOND_HEAVY_CYCLES_PER_QUERY / 1e9  # G pipe-cycles/s per GPU
+    heavy_peak = sms * 4 * mhz * 1e6 / 1e9
+    # Cross-check: modular products per second against a register-only butterfly loop (3
+    # transforms of n/2 log n butterflies per link; per slot 7 pointwise products and 2
+    # Montgomery reductions of 2 products each).
     links = GAMMA - 1
     modmul_per_query = links * (3 * (N_RING // 2) * 11 + 11 * N_RING) + 3 * (N_RING // 2) * 11
-    resp_gmodmul = BATCH * modmul_per_query / (resp_avg / 1e3) / 1e9  # one launch alone
-    timed_gmodmul = value / world * modmul_per_query / 1e9  # per GPU over the timed region
-    # Integer ceiling, measured now on this GPU: register-resident lazy butterflies (one
-    # Shoup product mod q each) with eight independent chains per thread.
+    timed_gmodmul = value / world * modmul_per_query / 1e9
     peak_gmodmul = ctx.butterfly_peak() / 1e9
     return {
         "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
@@ -540,19 +553,23 @@ def run_gb300(args, rank, world):
                      "avg_launch_ms": scan_avg, "algorithmic_bytes_per_launch": scan_bytes,
                      "timing": "one batch of 64 at a time on one lane, CUDA events around each scan launch",
                      "note": "the HBM-facing kernel; the dominant kernel is in roofline_dominant"},
-        "roofline_dominant": {"kernel": "respond (fused recursion + online gather)", "bound": "integer multiply pipe",
-                              "achieved": timed_gmodmul, "unit": "G modmul/s", "peak": peak_gmodmul,
-                              "frac": timed_gmodmul / peak_gmodmul,
-                              "peak_source": "measured in this run: lazy mod-q butterflies in registers "
-                                             "(ig_butterfly_peak)",
-                              "achieved_note": "modular products per second over the timed region "
-                                               "(queries/s x products per query)",
-                              "avg_launch_ms": resp_avg, "isolated_launch_gmodmul": resp_gmodmul,
-                              "modmul_per_query": modmul_per_query, "launch_shape": shape,
-                              "queries_per_launch": BATCH},
+        "roofline_dominant": {"kernel": "respond (fused recursion + online gather, one CTA per query)",
+                              "bound": "heavy integer multiply pipe (IMAD/IMAD.WIDE/IMAD.HI)",
+                              "achieved": heavy_achieved, "peak": heavy_peak,
+                              "unit": "G heavy-pipe sub-partition cycles/s",
+                              "frac": heavy_achieved / heavy_peak,
+                              "achieved_note": "queries/s over the timed region x the pipe's busy cycles per query "
+                                               "(ncu, RESPOND_HEAVY_CYCLES_PER_QUERY)",
+                              "peak_source": f"{sms} SMs x 4 sub-partitions x the sampled SM clock ({mhz:.0f} MHz)",
+                              "avg_launch_ms": resp_avg, "heavy_cycles_per_query": RESPOND_HEAVY_CYCLES_PER_QUERY,
+                              "cross_check": {"unit": "G modmul/s", "achieved": timed_gmodmul,
+                                              "butterfly_probe": peak_gmodmul,
+                                              "frac_of_probe": timed_gmodmul / peak_gmodmul,
+                                              "modmul_per_query": modmul_per_query},
+                              "launch_shape": shape, "queries_per_launch": BATCH},
         "gpu_launches": int(launches),
         "setup_s": setup_s,
-        "clocks": clk.summary(),
+        "clocks": clk_sum,
         "serving": serving,
         "plain": plain,
     }

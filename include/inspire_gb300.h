@@ -313,6 +313,9 @@ typedef struct ig_serve_stats_t {
   /* Memory admission: the budget, the bytes (keys and buffers) of the requests in flight
    * now, and their peak since create or the last reset. */
   uint64_t budget_bytes, inflight_bytes, peak_inflight_bytes;
+  /* Where a served request's time went: from submission to its batch's launch, and from the
+   * launch to its result in the caller's buffer (percentiles in microseconds). */
+  double queue_p50_us, queue_p99_us, exec_p50_us, exec_p99_us;
 } ig_serve_stats_t;
 int ig_serve_create(ig_ctx* ctx, uint32_t slots, uint32_t max_batch, uint64_t hbm_budget_bytes, ig_serve** out);
 int ig_serve_submit(ig_serve* s, uint64_t db, uint64_t store, uint64_t handle, uint32_t shard_id,

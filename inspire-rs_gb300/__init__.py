@@ -67,7 +67,9 @@ class ServeStats(ctypes.Structure):
                 ("waiting", ctypes.c_uint64), ("device_bytes", ctypes.c_uint64), ("mean_batch", ctypes.c_double),
                 ("p50_us", ctypes.c_double), ("p99_us", ctypes.c_double), ("max_us", ctypes.c_double),
                 ("budget_bytes", ctypes.c_uint64), ("inflight_bytes", ctypes.c_uint64),
-                ("peak_inflight_bytes", ctypes.c_uint64)]
+                ("peak_inflight_bytes", ctypes.c_uint64), ("queue_p50_us", ctypes.c_double),
+                ("queue_p99_us", ctypes.c_double), ("exec_p50_us", ctypes.c_double),
+                ("exec_p99_us", ctypes.c_double)]
 
 
 def _load():

@@ -416,8 +416,19 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32, 2) k_scan(CrsDev c, const Que
     };
 #pragma unroll
     for (int it = 0; it < SCAN_STAGES - 1; it++) issue(it);
-    for (int k = threadIdx.x; k < N; k += SCAN_WARPS * 32) {
-      const u64 bv = k == 0 ? reduce128(b[0]) : negq(reduce128(b[N - k]));
+    // b_rev in 32-bit limbs: every thread's loads of b issued together, then reduced.
+    constexpr int PER = (N + SCAN_WARPS * 32 - 1) / (SCAN_WARPS * 32);
+    u64 braw[PER];
+#pragma unroll
+    for (int j = 0; j < PER; j++) {
+      const int k = threadIdx.x + j * SCAN_WARPS * 32;
+      if (k < N) braw[j] = b[k == 0 ? 0 : N - k];
+    }
+#pragma unroll
+    for (int j = 0; j < PER; j++) {
+      const int k = threadIdx.x + j * SCAN_WARPS * 32;
+      if (k >= N) break;
+      const u64 bv = k == 0 ? reduce128(braw[j]) : negq(reduce128(braw[j]));
       V[(k & 7) * M + (k >> 3)] = make_uint2((u32)bv, (u32)(bv >> 32));
     }
     __syncthreads();

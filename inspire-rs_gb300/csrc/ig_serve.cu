@@ -62,7 +62,7 @@ struct Req {
   uint8_t* wire_out = nullptr;  // wire requests: the ServerResponse bytes instead of a, b
   size_t wire_cap = 0;
   size_t* wire_len = nullptr;
-  clk::time_point t_submit;
+  clk::time_point t_submit, t_launch;  // submission, and its batch's launch
   int status = -1;  // -1 while waiting or in flight
   u64 latency_ns = 0;
   std::string err;
@@ -179,6 +179,7 @@ struct ig_serve {
   u64 served = 0, refused = 0, batches = 0, batched_queries = 0;
   u32 inflight_ctas = 0;  // CTAs of all batches in flight
   std::vector<u64> latencies;
+  std::vector<u64> queue_ns, exec_ns;  // per served request: submit -> launch, launch -> result
   // Memory admission: the ring of request buffers (device, and its pinned host mirror) and
   // the keys pinned by requests in flight, both counted against `budget`.
   size_t budget = 0;
@@ -198,10 +199,13 @@ namespace {
 // Caller holds s->mu.
 void finish(ig_serve* s, Req* r, int status) {
   r->status = status;
-  r->latency_ns = (u64)std::chrono::duration_cast<std::chrono::nanoseconds>(clk::now() - r->t_submit).count();
+  const clk::time_point now = clk::now();
+  r->latency_ns = (u64)std::chrono::duration_cast<std::chrono::nanoseconds>(now - r->t_submit).count();
   if (status == IG_OK) {
     s->served++;
     s->latencies.push_back(r->latency_ns);
+    s->queue_ns.push_back((u64)std::chrono::duration_cast<std::chrono::nanoseconds>(r->t_launch - r->t_submit).count());
+    s->exec_ns.push_back((u64)std::chrono::duration_cast<std::chrono::nanoseconds>(now - r->t_launch).count());
   } else {
     s->refused++;
   }
@@ -491,6 +495,8 @@ void dispatch_loop(ig_serve* s) {
     if (e == cudaSuccess && sl.want_ab)
       e = cudaMemcpyAsync(h + L.a, d + L.a, L.status - L.a, cudaMemcpyDeviceToHost, st);
     cudaEventRecord(sl.done, st);
+    const clk::time_point t_launch = clk::now();
+    for (Req* r : sl.reqs) r->t_launch = t_launch;
     {
       std::lock_guard<std::mutex> lk(s->mu);
       sl.launch_err = (int)e;
@@ -820,14 +826,17 @@ int ig_serve_replay(ig_serve* s, uint64_t db, uint64_t store, uint32_t count, co
 int ig_serve_stats(ig_serve* s, ig_serve_stats_t* out, int reset) {
   if (!s || !out) return IG_ERR_ARG;
   std::lock_guard<std::mutex> lk(s->mu);
-  std::vector<u64> v = s->latencies;
+  std::vector<u64> v = s->latencies, vq = s->queue_ns, ve = s->exec_ns;
   std::sort(v.begin(), v.end());
-  auto pct = [&](double p) -> double {
-    if (v.empty()) return 0.0;
-    size_t i = (size_t)(p * (double)v.size());
-    if (i >= v.size()) i = v.size() - 1;
-    return (double)v[i] / 1e3;
+  std::sort(vq.begin(), vq.end());
+  std::sort(ve.begin(), ve.end());
+  auto pct_of = [](const std::vector<u64>& x, double p) -> double {
+    if (x.empty()) return 0.0;
+    size_t i = (size_t)(p * (double)x.size());
+    if (i >= x.size()) i = x.size() - 1;
+    return (double)x[i] / 1e3;
   };
+  auto pct = [&](double p) { return pct_of(v, p); };
   out->served = s->served;
   out->refused = s->refused;
   out->batches = s->batches;
@@ -840,8 +849,14 @@ int ig_serve_stats(ig_serve* s, ig_serve_stats_t* out, int reset) {
   out->budget_bytes = s->budget;
   out->inflight_bytes = s->ring.used + s->seat_bytes;
   out->peak_inflight_bytes = s->peak_bytes;
+  out->queue_p50_us = pct_of(vq, 0.50);
+  out->queue_p99_us = pct_of(vq, 0.99);
+  out->exec_p50_us = pct_of(ve, 0.50);
+  out->exec_p99_us = pct_of(ve, 0.99);
   if (reset) {
     s->latencies.clear();
+    s->queue_ns.clear();
+    s->exec_ns.clear();
     s->served = s->refused = s->batches = s->batched_queries = 0;
     s->peak_bytes = s->ring.used + s->seat_bytes;
   }
