@@ -46,6 +46,8 @@ int pair_threshold(ig_ctx* c);
 // forced shape, else the shape the tuned table times fastest at that many queries, else the
 // fixed rule's answer (fixed_rule_pair: the pair form, otherwise one CTA a query).
 int launch_ctas(ig_ctx* c, uint32_t n, uint32_t gamma, uint32_t count, uint32_t in_flight, bool fixed_rule_pair);
+// The launch shape set by ig_ctx_set_launch_shape (0 when the context chooses).
+int forced_ctas(ig_ctx* c);
 // Device-path lanes (ig_ctx_set_lanes), for callers holding the context lock:
 // lane_acquire picks the call's stream (the context stream when lanes == 1, lane -1) and
 // orders the context stream after the lane's previous batch, so the lane's scratch can be

@@ -542,6 +542,7 @@ int launch_ctas(ig_ctx* c, u32 n, u32 gamma, u32 count, u32 in_flight, bool fixe
   }
   return best;
 }
+int forced_ctas(ig_ctx* c) { return (int)c->force_ctas; }
 int lanes(ig_ctx* c) { return (int)c->lanes; }
 int lane_acquire(ig_ctx* c, cudaStream_t* s, int* lane) {
   *lane = -1;

@@ -426,6 +426,16 @@ void dispatch_loop(ig_serve* s) {
             if (!x.busy) return true;
           return false;
         });
+        // A batch launched into SMs the batches in flight still hold would wait on the device
+        // behind them, half-started; held here until it fits the free SMs (one CTA a query),
+        // it waits as long and more arrivals join it. A full batch's worth of waiting requests
+        // launches at once, so the device stays fed at saturation.
+        const u32 sms = (u32)igint::sm_count(s->ctx);
+        s->cv_slot.wait(lk, [&] {
+          const size_t next = std::min<size_t>(s->waiting.size(), s->max_batch);
+          return s->stop || s->launched.empty() || s->waiting.size() >= s->max_batch ||
+                 s->inflight_ctas + next <= sms;
+        });
         k = form_batch(s, &ring);
         if (k >= 0) break;
         s->cv_done.notify_all();  // requests refused while forming
@@ -439,14 +449,16 @@ void dispatch_loop(ig_serve* s) {
     Slot& sl = s->slots[k];
     const u32 count = (u32)sl.reqs.size();
     const size_t n = ring.n;
-    // Several CTAs per query only while the SMs left by the batches in flight hold them; with
-    // other batches running, one CTA per query does the same work on fewer SMs.
+    // Several CTAs per query (a cluster) only onto an idle device: a cluster needs its SMs free
+    // together within one GPC, and batches of single CTAs scattered over the GPCs leave it
+    // waiting on the device behind them although enough SMs are free in all. With other
+    // batches running, one CTA per query does the same work on fewer SMs.
     int ctas;
     {
       std::lock_guard<std::mutex> lk(s->mu);
-      const u32 sms = (u32)igint::sm_count(s->ctx);
       ctas = igint::launch_ctas(s->ctx, (u32)n, sl.reqs[0]->v.crs.gamma, count, count + s->inflight_ctas,
-                                (int)count <= igint::pair_threshold(s->ctx) && s->inflight_ctas + 2 * count <= sms);
+                                (int)count <= igint::pair_threshold(s->ctx));
+      if (s->inflight_ctas != 0 && ctas > 1 && !igint::forced_ctas(s->ctx)) ctas = 1;
       sl.ctas = (u32)ctas * count;
       s->inflight_ctas += sl.ctas;
     }
@@ -714,6 +726,7 @@ static int submit(ig_serve* s, uint64_t db, uint64_t store, uint64_t handle, uin
   r->a_out = a_out;
   r->b_out = b_out;
   r->t_submit = clk::now();
+  bool full = false;
   {
     std::lock_guard<std::mutex> lk(s->mu);
     if (s->stop || s->waiting.size() >= s->max_waiting) {
@@ -726,8 +739,10 @@ static int submit(ig_serve* s, uint64_t db, uint64_t store, uint64_t handle, uin
     s->tickets[r->ticket] = r;
     s->waiting.push_back(r);
     *ticket_out = r->ticket;
+    full = s->waiting.size() >= s->max_batch;
   }
   s->cv_work.notify_one();
+  if (full) s->cv_slot.notify_all();  // a held dispatcher launches a full batch at once
   return IG_OK;
 }
 
