@@ -326,6 +326,34 @@ def plain_leg(pkg, crs, db, keys, queries, ms):
             "p99_ms": 1e3 * lat[min(len(lat) - 1, int(0.99 * len(lat)))]}
 
 
+def small_batch_leg(pkg, ctx, crs, db, cache, store, handle, shards, rng, ms, calls=20):
+    """Latency of small batches under each launch shape: batches of 7 and 1 through
+    respond_seeded_batch (host buffers, one synchronous call at a time), at one, two and four
+    CTAs per query, and the shape the context picks for that batch alone. Inside a profiler
+    range, so an ncu --profile-from-start off capture with -k regex:k_respond_quad -c 1 takes
+    the first four-CTA launch of 7 queries."""
+    out = {}
+    for count in (7, 1):
+        qs = [pkg.SeededBatchQuery(int(rng.integers(0, shards)), rng.bytes(32), rand_words(rng, N_RING))
+              for _ in range(count)]
+        batch = pkg.SeededQueryBatch(pkg.PackingKeySource.Registered(handle), qs)
+        row = {"auto_shape": ctx.launch_shape_for(GAMMA, count)}
+        for shape in (4, 2, 1):
+            ctx.set_launch_shape(shape)
+            lat = []
+            for r in range(3 + calls):
+                t = time.perf_counter()
+                pkg.respond_seeded_batch(crs, db, batch, cache, store, mod_switch_target=ms)
+                if r >= 3:
+                    lat.append(time.perf_counter() - t)
+            lat.sort()
+            row[f"ctas{shape}"] = {"p50_ms": 1e3 * lat[len(lat) // 2], "max_ms": 1e3 * lat[-1]}
+        ctx.set_launch_shape(0)
+        out[f"batch{count}"] = row
+    out["call"] = f"respond_seeded_batch, host buffers, {calls} timed calls after 3 untimed"
+    return out
+
+
 def run_gb300(args, rank, world):
     import torch
 
@@ -499,6 +527,9 @@ def run_gb300(args, rank, world):
     serving, serve_cases = serve_leg(pkg, ctx, db, store, handle, args.shards, rng, MS_TARGET, slots=lanes)
     checked += oracle_check(O, cache_o, y_body, cols_of, serve_cases)
     plain = plain_leg(pkg, crs, db, keys, [q for qs in e2e_queries[:1] for q in qs], MS_TARGET)
+    torch.cuda.profiler.start()
+    small = small_batch_leg(pkg, ctx, crs, db, cache, store, handle, args.shards, rng, MS_TARGET)
+    torch.cuda.profiler.stop()
 
     scan_ms, scan_n = prof["scan"]
     resp_ms, resp_n = prof["respond"]
@@ -572,6 +603,7 @@ def run_gb300(args, rank, world):
         "clocks": clk_sum,
         "serving": serving,
         "plain": plain,
+        "small_batches": small,
     }
 
 

@@ -890,8 +890,12 @@ class ServingLoop:
         bs = np.ascontiguousarray(bs, dtype=np.uint64)
         count, n = bs.shape
         arr = None if arrival_ns is None else np.ascontiguousarray(arrival_ns, dtype=np.uint64)
-        a = np.zeros((count, n), dtype=np.uint64)
-        b = np.zeros((count, n), dtype=np.uint64)
+        # Written once here, so the first-touch page faults of the result arrays (hundreds of
+        # MB for a long trace) are taken before the trace starts, not by the loop's completer.
+        a = np.empty((count, n), dtype=np.uint64)
+        b = np.empty((count, n), dtype=np.uint64)
+        a.fill(0)
+        b.fill(0)
         lat = np.zeros(count, dtype=np.uint64)
         el = ctypes.c_double()
         self.ctx.check(self.ctx._lib.ig_serve_replay(
