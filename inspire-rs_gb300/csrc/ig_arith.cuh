@@ -90,6 +90,15 @@ IG_HD u64 shoup_lazy4(u64 a, u64 w, u64 wp) {
   return a * w - est * q_opaque();
 }
 
+// a * w mod q up to three q for a below 2^32 (a gadget digit). The quotient estimate is
+// floor(a wh / 2^32), wh the high word of w'; the exact floor(a w' / 2^64) adds a wl / 2^64
+// (below one unit, wl the low word) to a wh / 2^32, so the estimate undershoots it by at
+// most 1 and a w - est q lies in [0, 3q).
+IG_HD u64 shoup_digit(u32 a, u64 w, u64 wp) {
+  const u64 est = mulhi32(a, (u32)(wp >> 32));
+  return (u64)a * w - est * q_opaque();
+}
+
 // x - 2q when x >= 2q.
 IG_HD u64 csub2(u64 x) { return x >= 2 * Q ? x - 2 * Q : x; }
 // x - 4q when x >= 4q.

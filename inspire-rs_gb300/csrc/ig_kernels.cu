@@ -850,7 +850,7 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
         q0 = rr1 & DMASK;
         q1 = rr1 >> 20;
       }
-      const u64 t0 = shoup_lazy4(q0, wf, wfp), t1 = shoup_lazy4(q1, wf, wfp);
+      const u64 t0 = shoup_digit((u32)q0, wf, wfp), t1 = shoup_digit((u32)q1, wf, wfp);
       D[sw(b)] = p0 + t0;
       D[sw(b + H)] = p0 + 4 * Q - t0;
       D[N + sw(b)] = p1 + t1;
@@ -1205,7 +1205,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
           q1 = rr1 >> 20;
         }
         // Forward cross stage: slot b gets p + w q, slot b + H gets p - w q.
-        const u64 t0 = shoup_lazy4(q0, wf, wfp), t1 = shoup_lazy4(q1, wf, wfp);
+        const u64 t0 = shoup_digit((u32)q0, wf, wfp), t1 = shoup_digit((u32)q1, wf, wfp);
         D[sw(b)] = rank == 0 ? p0 + t0 : p0 + 4 * Q - t0;
         D[H + sw(b)] = rank == 0 ? p1 + t1 : p1 + 4 * Q - t1;
       }
@@ -1387,7 +1387,7 @@ __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
       // Forward stage 0 (b with b + N/2, b + N/4 with b + 3N/4), then stage 1 on this
       // quarter's half: a bf_fwd8 whose output r & 1 is the quarter's word.
       auto fwd = [&](const u64(&g)[4]) -> u64 {
-        const u64 t2 = shoup_lazy4(g[2], wf1, wf1p), t3 = shoup_lazy4(g[3], wf1, wf1p);
+        const u64 t2 = shoup_digit((u32)g[2], wf1, wf1p), t3 = shoup_digit((u32)g[3], wf1, wf1p);
         u64 lo, hi;
         if (rank < 2) {
           lo = g[0] + t2;
@@ -1735,7 +1735,7 @@ __global__ void __launch_bounds__((1 << LOGN) / 4, 1)
       // n^-1 times the stage's twiddle on the difference.
       const u64 r0 = shoup(x0 + x1, c.ninv, c.ninvp), r1 = shoup(x0 - x1 + 4 * Q, c.nlast, c.nlastp);
       const u64 p0 = r0 & DMASK, p1 = (r0 >> 20) & DMASK, q0 = r1 & DMASK, q1 = (r1 >> 20) & DMASK;
-      const u64 t0 = shoup_lazy4(q0, wf, wfp), t1 = shoup_lazy4(q1, wf, wfp);
+      const u64 t0 = shoup_digit((u32)q0, wf, wfp), t1 = shoup_digit((u32)q1, wf, wfp);
       D[sw(b)] = p0 + t0;
       D[sw(b + H)] = p0 + 4 * Q - t0;
       D[N + sw(b)] = p1 + t1;

@@ -1,6 +1,7 @@
 // Host check of the lazy bounds the recursion kernels rely on, against exact 128-bit
 // arithmetic (compiled and run by test_arith_cpu.py):
 //   shoup_lazy4(a, w, w')  in [0, 4q) and = a w mod q, for any a < 2^64, w < q;
+//   shoup_digit(a, w, w')  in [0, 3q) and = a w mod q, for any a < 2^32, w < q;
 //   the butterflies built on it keep the forward's words below 8q and the inverse's
 //   below 4q, and stay congruent to the exact butterflies;
 //   redc_wide(x)           canonical and = x 2^-64 mod q, for x < 2q 2^64;
@@ -43,6 +44,11 @@ int main(int argc, char** argv) {
     const u64 a = i < 9 ? edges[i] : (i & 1 ? next() : next() % (8 * Q));
     const u64 v = shoup_lazy4(a, w, wp);
     if (v >= 4 * Q || v % Q != mulmod(a % Q, w)) fail("shoup_lazy4", a, w);
+    // Digits: below 2^20 (exact gadget), below 2^24 (rounded), and any 32-bit word.
+    const u32 dg = i < 4 ? (u32)(i == 0 ? 0 : i == 1 ? 0xFFFFFu : i == 2 ? 0xFFFFFFu : 0xFFFFFFFFu)
+                         : (u32)(next() >> (i % 3 == 0 ? 44 : i % 3 == 1 ? 40 : 32));
+    const u64 vd = shoup_digit(dg, w, wp);
+    if (vd >= 3 * Q || vd % Q != mulmod(dg, w)) fail("shoup_digit", dg, w);
 
     // Forward butterfly on words below 8q (bf_fwd8), inverse on words below 4q (bf_inv4).
     const u64 X = next() % (8 * Q), Y = next() % (8 * Q);
