@@ -401,7 +401,9 @@ def run_gb300(args, rank, world):
     # recursion overlap the ones before it; with more than one lane the batches run one CTA
     # per query (64 x lanes CTAs in flight), with one lane two CTAs per query.
     pair_default = 76
-    shape = "pair (2 CTAs per query)" if BATCH * lanes <= pair_default else "single (1 CTA per query)"
+    q_in_flight = BATCH * lanes
+    shape = ("quad (4 CTAs per query)" if 2 * q_in_flight <= pair_default else
+             "pair (2 CTAs per query)" if q_in_flight <= pair_default else "single (1 CTA per query)")
 
     def batch(i):
         k = i % lanes
@@ -1078,7 +1080,8 @@ def run_cfg4(args, rank, world):
         return max_over_ranks(ev0.elapsed_time(ev1), world), ctx.launch_count - launches0, clk
 
     timed_queries = int(offs[-1] - offs[args.warmup])
-    # The fixed rule first (no table: two CTAs per query while count x lanes <= SMs / 2), then
+    # The fixed rule first (no table: four CTAs per query while 2 x count x lanes <= SMs / 2, two
+    # while count x lanes <= SMs / 2, else one), then
     # the launch-shape tuner's table for the three widths, then the same launches tuned.
     ms_fixed, _, _ = timed_region()
     t0 = time.perf_counter()
@@ -1207,7 +1210,8 @@ def run_cfg4(args, rank, world):
                 "d2h_bytes_per_step": int(timed_queries * 2 * N_RING * 8 / args.steps), "callers": lanes,
                 "call": "respond_mixed_batch (one launch per call)"},
         "fixed_rule": {"value": fixed_value, "unit": "queries/s",
-                       "rule": "two CTAs per query while count x lanes <= SMs / 2, else one"},
+                       "rule": "four CTAs per query while 2 x count x lanes <= SMs / 2, two while "
+                               "count x lanes <= SMs / 2, else one"},
         "launch_shapes": {"tuned_ms_per_launch": {str(g): {str(b): {"1": t[0], "2": t[1], "4": t[2]}
                                                            for b, t in rows.items()} for g, rows in tuned.items()},
                           "tune_s": tune_s,

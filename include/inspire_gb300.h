@@ -51,10 +51,12 @@ int ig_last_error(const ig_ctx* ctx, char* buf, size_t len);
 void* ig_ctx_stream(ig_ctx* ctx);
 /* Device bytes held by this context's objects (stores, shards, seats, scratch). */
 uint64_t ig_ctx_device_bytes(const ig_ctx* ctx);
-/* Launch-shape knob: respond batches of at most max_queries queries run two CTAs per
- * query (a thread-block cluster) so small batches still occupy most SMs; larger batches
- * run one CTA per query. Default: half the device's SM count; 0 disables the pair form.
- * Responses are identical either way. */
+/* Launch-shape knob of the fixed rule, used when the context holds no tuned table for the
+ * launch's width (ig_tune_launch_shapes): with q the queries expected on the device (the
+ * batch times the lanes, or the queries in flight), a launch runs four CTAs per query (a
+ * thread-block cluster) while 2q <= max_queries, two while q <= max_queries, else one, so
+ * small batches still occupy most SMs. Default: half the device's SM count; 0 runs one CTA
+ * per query always. Responses are identical under every shape. */
 int ig_ctx_set_pair_threshold(ig_ctx* ctx, uint32_t max_queries);
 /* Launch shapes and their tuner. A respond launch runs 1, 2 or 4 CTAs per query: one CTA
  * per SM is the most work per SM-second; a cluster of 2 or 4 splits each query's

@@ -248,7 +248,9 @@ class Context:
         self.check(self._lib.ig_tune_load(self.h, str(path).encode()))
 
     def set_pair_threshold(self, max_queries):
-        """Batches of at most max_queries run two CTAs per query (0: never)."""
+        """The fixed launch rule (no tuned table): four CTAs per query while twice the
+        queries expected in flight fit max_queries, two while they fit it, else one
+        (0: one CTA per query always)."""
         self.check(self._lib.ig_ctx_set_pair_threshold(self.h, int(max_queries)))
 
     def response_wire_len(self, ring_dim, retained, modulus):

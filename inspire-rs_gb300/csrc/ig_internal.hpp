@@ -44,8 +44,9 @@ int pair_threshold(ig_ctx* c);
 // CTAs per query (1, 2 or 4) for a respond launch of `count` queries of width `gamma` on
 // ring n with `in_flight` queries expected on the device with it (its own included): the
 // forced shape, else the shape the tuned table times fastest at that many queries, else the
-// fixed rule's answer (fixed_rule_pair: the pair form, otherwise one CTA a query).
-int launch_ctas(ig_ctx* c, uint32_t n, uint32_t gamma, uint32_t count, uint32_t in_flight, bool fixed_rule_pair);
+// fixed rule: four CTAs while twice the queries fit the pair threshold, two while they fit
+// it, else one.
+int launch_ctas(ig_ctx* c, uint32_t n, uint32_t gamma, uint32_t count, uint32_t in_flight);
 // The launch shape set by ig_ctx_set_launch_shape (0 when the context chooses).
 int forced_ctas(ig_ctx* c);
 // Device-path lanes (ig_ctx_set_lanes), for callers holding the context lock:

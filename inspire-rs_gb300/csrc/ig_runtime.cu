@@ -211,8 +211,8 @@ struct ig_ctx {
   std::atomic<u32> fail_alloc_at{0};
   // Launch shape of respond launches (CTAs per query). force_ctas != 0 fixes it; otherwise,
   // with a tuned entry for the launch's (ring, gamma), the shape whose measured launch time
-  // is least at the number of queries expected in flight, else the fixed pair_threshold
-  // rule. tune[(n, gamma)] maps a batch size to the measured milliseconds of one launch of
+  // is least at the number of queries expected in flight, else the fixed rule on
+  // pair_threshold (four CTAs up to half of it, two up to it). tune[(n, gamma)] maps a batch size to the measured milliseconds of one launch of
   // that many queries under 1, 2 and 4 CTAs per query.
   u32 force_ctas = 0;
   std::map<std::pair<u32, u32>, std::map<u32, std::array<double, 3>>> tune;
@@ -525,10 +525,14 @@ static const std::array<double, 3>* tuned_row(ig_ctx* c, u32 n, u32 gamma, u32 q
   return &row->second;
 }
 
-int launch_ctas(ig_ctx* c, u32 n, u32 gamma, u32 count, u32 in_flight, bool fixed_rule_pair) {
+int launch_ctas(ig_ctx* c, u32 n, u32 gamma, u32 count, u32 in_flight) {
   if (c->force_ctas) return (int)c->force_ctas;
-  const std::array<double, 3>* row = tuned_row(c, n, gamma, std::max(count, in_flight));
-  if (!row) return fixed_rule_pair ? 2 : 1;
+  const u32 queries = std::max(count, in_flight);
+  const std::array<double, 3>* row = tuned_row(c, n, gamma, queries);
+  if (!row) {  // the fixed rule: as many CTAs per query as the threshold leaves room for
+    const u64 t = c->pair_threshold;
+    return 2 * (u64)queries <= t ? 4 : (u64)queries <= t ? 2 : 1;
+  }
   const int shapes[3] = {1, 2, 4};
   int best = 1;
   double best_ms = 0;
@@ -1370,8 +1374,7 @@ static int respond_host(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_t handle, c
   pk = prof_begin(c, REGION_RESPOND, s);
   IG_CUDA(c, igk::respond(o.dev, (const QueryDev*)d_q, (const ShardDev*)d_table, count, (const u64*)d_fold,
                           (u64*)d_a, (u64*)d_b, (u32*)d_status, c->force_serial,
-                          igint::launch_ctas(c, (u32)n, (u32)g, count, count * lanes,
-                                             (u64)count * lanes <= c->pair_threshold),
+                          igint::launch_ctas(c, (u32)n, (u32)g, count, count * lanes),
                           s));
   prof_end(c, pk, s);
   if (env_prof) {
@@ -1899,8 +1902,7 @@ int ig_respond_seeded_batch_device(ig_ctx* c, uint64_t dbh, uint64_t st, uint64_
   IG_CUDA(c, igk::shard_scan(o.dev, (const QueryDev*)d_q, db->d_table, count, nullptr, 0, (u64*)d_fold, d_status, s));
   prof_end(c, pk, s);
   // Several CTAs per query only while every lane's batch still leaves SMs for them.
-  const int ctas = igint::launch_ctas(c, (u32)n, (u32)g, count, count * c->lanes,
-                                      (u64)count * c->lanes <= c->pair_threshold);
+  const int ctas = igint::launch_ctas(c, (u32)n, (u32)g, count, count * c->lanes);
   pk = prof_begin(c, REGION_RESPOND, s);
   IG_CUDA(c, igk::respond(o.dev, (const QueryDev*)d_q, db->d_table, count, (const u64*)d_fold, d_a, d_b, d_status,
                           c->force_serial, ctas, s));
@@ -2030,8 +2032,7 @@ int ig_respond_mixed_batch_device(ig_ctx* c, uint32_t count, const uint64_t* dbs
   IG_CUDA(c, igk::shard_scan(P.ring, (const QueryDev*)dq, (const ShardDev*)dt, count, (const u32*)dw,
                              (u32)P.work.size(), (u64*)df, d_status, s));
   prof_end(c, pk, s);
-  const int ctas = igint::launch_ctas(c, (u32)n, P.max_gamma, count, count * c->lanes,
-                                      (u64)count * c->lanes <= c->pair_threshold);
+  const int ctas = igint::launch_ctas(c, (u32)n, P.max_gamma, count, count * c->lanes);
   pk = prof_begin(c, REGION_RESPOND, s);
   IG_CUDA(c, igk::respond(P.ring, (const QueryDev*)dq, (const ShardDev*)dt, count, (const u64*)df, d_a, d_b, d_status,
                           c->force_serial, ctas, s));
@@ -2094,8 +2095,7 @@ int ig_respond_mixed_batch(ig_ctx* c, uint32_t count, const uint64_t* dbs, const
                              (u32)P.work.size(), (u64*)df, (u32*)dst, s));
   IG_CUDA(c, igk::respond(P.ring, (const QueryDev*)dq, (const ShardDev*)dt, count, (const u64*)df, (u64*)da, (u64*)db_,
                           (u32*)dst, c->force_serial,
-                          igint::launch_ctas(c, (u32)n, P.max_gamma, count, count * c->lanes,
-                                             (u64)count * c->lanes <= c->pair_threshold),
+                          igint::launch_ctas(c, (u32)n, P.max_gamma, count, count * c->lanes),
                           s));
   c->launches += 2;
   IG_CUDA(c, cudaMemcpyAsync(h_status, dst, count * 4, cudaMemcpyDeviceToHost, s));
@@ -2565,7 +2565,7 @@ int ig_tune_get(ig_ctx* c, uint32_t ring_dim, uint32_t gamma, uint32_t queries, 
 int ig_tune_choose(ig_ctx* c, uint32_t ring_dim, uint32_t gamma, uint32_t count, uint32_t in_flight, uint32_t* ctas) {
   if (!c || !ctas) return IG_ERR_ARG;
   std::lock_guard<std::mutex> lk(c->mu);
-  *ctas = (u32)igint::launch_ctas(c, ring_dim, gamma, count, in_flight, (u64)std::max(count, in_flight) <= c->pair_threshold);
+  *ctas = (u32)igint::launch_ctas(c, ring_dim, gamma, count, in_flight);
   return IG_OK;
 }
 
@@ -2830,8 +2830,7 @@ int ig_respond_seeded_batch_noalloc(ig_ctx* c, uint64_t dbh, uint64_t st, uint64
   IG_CUDA(c, igk::shard_scan(o.dev, d_q, db->d_table, count, nullptr, 0, d_fold, d_status, s));
   // The launch shape of ig_respond_seeded_batch_device for the same batch and lane count.
   IG_CUDA(c, igk::respond(o.dev, d_q, db->d_table, count, d_fold, d_a, d_b, d_status, c->force_serial,
-                          igint::launch_ctas(c, (u32)n, (u32)g, count, count * c->lanes,
-                                             (u64)count * c->lanes <= c->pair_threshold),
+                          igint::launch_ctas(c, (u32)n, (u32)g, count, count * c->lanes),
                           s));
   c->launches += 2;
   u32 status[NOALLOC_MAX_QUERIES];

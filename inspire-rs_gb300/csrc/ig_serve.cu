@@ -456,8 +456,7 @@ void dispatch_loop(ig_serve* s) {
     int ctas;
     {
       std::lock_guard<std::mutex> lk(s->mu);
-      ctas = igint::launch_ctas(s->ctx, (u32)n, sl.reqs[0]->v.crs.gamma, count, count + s->inflight_ctas,
-                                (int)count <= igint::pair_threshold(s->ctx));
+      ctas = igint::launch_ctas(s->ctx, (u32)n, sl.reqs[0]->v.crs.gamma, count, count + s->inflight_ctas);
       if (s->inflight_ctas != 0 && ctas > 1 && !igint::forced_ctas(s->ctx)) ctas = 1;
       sl.ctas = (u32)ctas * count;
       s->inflight_ctas += sl.ctas;

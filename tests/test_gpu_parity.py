@@ -67,13 +67,9 @@ def test_d256_fixture_on_gpu(pkg, oracle, ctx):
 def launch_shape(request, ctx):
     """The three respond kernels: two CTAs per query and four (clusters, for small batches),
     and one CTA per query."""
-    if request.param == "quad":
-        ctx.set_launch_shape(4)
-    else:
-        ctx.set_pair_threshold(1 << 20 if request.param == "pair" else 0)
+    ctx.set_launch_shape({"single": 1, "pair": 2, "quad": 4}[request.param])
     yield request.param
     ctx.set_launch_shape(0)
-    ctx.set_pair_threshold(76)
 
 
 @pytest.mark.parametrize("entry,seed", D2048_CELLS)
