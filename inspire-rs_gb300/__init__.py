@@ -773,22 +773,39 @@ def respond_mixed_batch(queries) -> list:
         return []
     ctx = queries[0].db.ctx
     n = queries[0].db.ring_dim
-    if any(q.db.ctx is not ctx for q in queries):
-        raise PirError("a mixed launch runs on one context")
-    for q in queries:
-        if q.query.seed is None or len(q.query.seed) != 32:
+    # One pass over the queries: the checks, and the per-query fields as lists.
+    dbs, stores, handles, sids, ms, seeds = [], [], [], [], [], []
+    bs = np.empty((count, n), dtype=np.uint64)
+    budget_checked = set()
+    for i, q in enumerate(queries):
+        db, query = q.db, q.query
+        if db.ctx is not ctx:
+            raise PirError("a mixed launch runs on one context")
+        if query.seed is None or len(query.seed) != 32:
             raise PirError("mixed launches take seeded queries (32-byte seed)")
-        if q.mod_switch_target:
-            check_mod_switch_noise_budget(q.db.cache.crs.params, q.mod_switch_target)
-    dbs = np.array([q.db.h for q in queries], dtype=np.uint64)
-    stores = np.array([q.store.h for q in queries], dtype=np.uint64)
-    handles = np.array([q.handle for q in queries], dtype=np.uint64)
-    sids = np.array([q.query.shard_id for q in queries], dtype=np.uint32)
-    ms = np.array([q.mod_switch_target for q in queries], dtype=np.uint64)
-    seeds = np.frombuffer(b"".join(bytes(q.query.seed) for q in queries), dtype=np.uint8).copy()
-    bs = np.stack([_u64(q.query.b, (n,)) for q in queries])
-    a_out = np.zeros((count, n), dtype=np.uint64)
-    b_out = np.zeros((count, n), dtype=np.uint64)
+        target = q.mod_switch_target
+        if target:
+            params = db.cache.crs.params
+            if (id(params), target) not in budget_checked:
+                check_mod_switch_noise_budget(params, target)
+                budget_checked.add((id(params), target))
+        if query.b.shape != (n,):
+            raise PirError(f"wire shape refused: expected an array of shape {(n,)}, got {query.b.shape}")
+        bs[i] = query.b
+        dbs.append(db.h)
+        stores.append(q.store.h)
+        handles.append(q.handle)
+        sids.append(query.shard_id)
+        ms.append(target)
+        seeds.append(query.seed)
+    dbs = np.array(dbs, dtype=np.uint64)
+    stores = np.array(stores, dtype=np.uint64)
+    handles = np.array(handles, dtype=np.uint64)
+    sids = np.array(sids, dtype=np.uint32)
+    ms = np.array(ms, dtype=np.uint64)
+    seeds = np.frombuffer(b"".join(seeds), dtype=np.uint8).copy()
+    a_out = np.empty((count, n), dtype=np.uint64)
+    b_out = np.empty((count, n), dtype=np.uint64)
     ctx.check(ctx._lib.ig_respond_mixed_batch(ctx.h, count, _ptr(dbs), _ptr(stores), _ptr(handles), _ptr(sids),
                                               _ptr(seeds), _ptr(bs), _ptr(ms), _ptr(a_out), _ptr(b_out)))
     return [ServerResponse(a_out[i], b_out[i], q.db.num_columns, q.mod_switch_target or q.db.cache.crs.params.q)

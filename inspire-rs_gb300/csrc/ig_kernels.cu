@@ -392,6 +392,14 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32, 2) k_scan(CrsDev c, const Que
     chunk = blockIdx.x - qi * chunks;
   }
   const QueryDev qd = queries[qi];
+  // b_rev in 32-bit limbs: every thread's loads of b issued first, beside the shard entry's.
+  constexpr int PER = (N + SCAN_WARPS * 32 - 1) / (SCAN_WARPS * 32);
+  u64 braw[PER];
+#pragma unroll
+  for (int j = 0; j < PER; j++) {
+    const int k = threadIdx.x + j * SCAN_WARPS * 32;
+    if (k < N) braw[j] = qd.b[k == 0 ? 0 : N - k];
+  }
   const ShardDev sh = shards[qd.shard];
   const u32 gamma = qd.crs ? qd.crs->gamma : c.gamma;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -416,14 +424,6 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32, 2) k_scan(CrsDev c, const Que
     };
 #pragma unroll
     for (int it = 0; it < SCAN_STAGES - 1; it++) issue(it);
-    // b_rev in 32-bit limbs: every thread's loads of b issued together, then reduced.
-    constexpr int PER = (N + SCAN_WARPS * 32 - 1) / (SCAN_WARPS * 32);
-    u64 braw[PER];
-#pragma unroll
-    for (int j = 0; j < PER; j++) {
-      const int k = threadIdx.x + j * SCAN_WARPS * 32;
-      if (k < N) braw[j] = b[k == 0 ? 0 : N - k];
-    }
 #pragma unroll
     for (int j = 0; j < PER; j++) {
       const int k = threadIdx.x + j * SCAN_WARPS * 32;
