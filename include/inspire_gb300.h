@@ -231,8 +231,7 @@ int ig_respond_mixed_batch_device(ig_ctx* ctx, uint32_t count, const uint64_t* d
  * other allocating call. Limits: at most 64 queries per call, gamma at most 1024, a
  * registered seat (handle) and packing stores on the queried shards; larger batches are
  * refused with IG_ERR_ARG before any work. The first call on a device resolves the
- * array's device address (cudaGetSymbolAddress); make that first call before any stream
- * capture. All calls share the array, and it keeps the last call's contents: calls that
+ * array's device address (cudaGetSymbolAddress). All calls share the array, and it keeps the last call's contents: calls that
  * overlap on the GPU (from different contexts of one device) race and must be serialised
  * by the caller. Inputs and outputs are device pointers as in
  * ig_respond_seeded_batch_device. The call blocks: it synchronises the context stream,
