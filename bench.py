@@ -1160,15 +1160,22 @@ def run_cfg4(args, rank, world):
                       for j, k in enumerate(kidx)])
     errors = []
 
-    def caller(idx):
+    # The calls differ in size (1 to 512 queries), so the callers take the next call as they
+    # free up, as a server's worker pool takes the next request, not a fixed share each.
+    def caller(pending, lock):
         try:
-            for i in idx:
+            while True:
+                with lock:
+                    if not pending:
+                        return
+                    i = pending.pop()
                 pkg.respond_mixed_batch(calls[i])
         except Exception as e:  # reported below
             errors.append(e)
 
     def run_callers(indices):
-        threads = [threading.Thread(target=caller, args=(indices[t::lanes],)) for t in range(lanes)]
+        pending, lock = list(reversed(indices)), threading.Lock()
+        threads = [threading.Thread(target=caller, args=(pending, lock)) for t in range(lanes)]
         for th in threads:
             th.start()
         for th in threads:
