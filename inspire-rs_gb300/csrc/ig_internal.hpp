@@ -40,7 +40,6 @@ struct RequestView {
   char err[512];
 };
 int resolve_request(ig_ctx* c, uint64_t db, uint64_t store, uint64_t handle, uint32_t shard, RequestView* out);
-int pair_threshold(ig_ctx* c);
 // CTAs per query (1, 2 or 4) for a respond launch of `count` queries of width `gamma` on
 // ring n with `in_flight` queries expected on the device with it (its own included): the
 // forced shape, else the shape the tuned table times fastest at that many queries, else the

@@ -505,7 +505,6 @@ int scratch(ig_ctx* c, const char* name, size_t bytes, void** out) { return ::sc
 int stage_h2d(ig_ctx* c, void* dst, const void* src, size_t bytes) { return ::stage_h2d(c, dst, src, bytes); }
 void add_launches(ig_ctx* c, unsigned n) { c->launches += n; }
 void*& sm_slot(ig_ctx* c) { return c->sm; }
-int pair_threshold(ig_ctx* c) { return (int)c->pair_threshold; }
 // The tuned row for `queries` in flight: the smallest measured batch size at or above it
 // (the largest measured one beyond the grid), of the tuned width nearest gamma on ring n.
 static const std::array<double, 3>* tuned_row(ig_ctx* c, u32 n, u32 gamma, u32 queries) {
