@@ -835,7 +835,7 @@ class ServingLoop:
     requests) next to the batches in flight. A request's response equals
     respond_seeded_batch's for the same query."""
 
-    def __init__(self, ctx: Context = None, slots=2, max_batch=64, hbm_budget_bytes=0):
+    def __init__(self, ctx: Context = None, slots=4, max_batch=64, hbm_budget_bytes=0):
         self.ctx = ctx or Context.default()
         self.h = None
         self._live = {}  # tickets whose result buffers the loop may still write
