@@ -85,8 +85,8 @@ def test_mixed_stream_matches_each_query_alone(pkg, oracle, ctx, sets):
         if not ms:
             assert ps.cell.decode(idx, r.a, r.b)[0], f"index {idx} decoded to another record"
     assert st["served"] == len(reqs) and st["refused"] == 0
-    # Three launch groups at least: (exact, unswitched), (exact, 36-bit), (approximate).
-    assert st["batches"] >= 3
+    # 36 requests in batches of at most 8 (a batch may mix sets and switch targets).
+    assert st["batches"] >= 5
     assert 1.0 <= st["mean_batch"] <= 8.0
     assert 0.0 < st["p50_us"] <= st["p99_us"] <= st["max_us"]
     assert all(t.latency_us and t.latency_us > 0 for t in tickets)
