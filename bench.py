@@ -10,11 +10,15 @@ After the timed region, sampled responses of it are recomputed by the CPU oracle
 match byte for byte (`parity_checked`).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--workload served-batch|special-modulus|mixed|serving-sweep]
+                    [--workload served-batch|special-modulus|mixed|serving-sweep|one-packing|no-packing]
+                    [--headline-only]
 
 --workload special-modulus times the special_modulus batch of 256, mixed six parameter sets
 (32/512/2048 B records under both gadgets, batch sizes 1-512), serving-sweep the serving
-loop over 2^25 records and 1000 seats.
+loop over 2^25 records and 1000 seats, one-packing the tree responder, no-packing the
+NoPacking responder. On one GPU at the default database size, the served-batch run also
+runs those five after the headline, each at its own defaults, and reports them under
+`workloads` (--headline-only skips them).
 
 Prints one JSON line. `value` = queries/s over K device-resident steps (CUDA events on
 the library's stream); `e2e` = the same through the public API with host buffers;
@@ -220,6 +224,25 @@ class ClockSampler:
                 "region_s": None if self.t_end is None else round(self.t_end - self.t_begin, 3)}
 
 
+# Contexts the workloads open; closed between workloads so each starts on a free device.
+_OPEN_CONTEXTS = []
+
+
+def open_context(pkg, device):
+    ctx = pkg.Context(device)
+    _OPEN_CONTEXTS.append(ctx)
+    return ctx
+
+
+def close_contexts():
+    import torch
+
+    while _OPEN_CONTEXTS:
+        _OPEN_CONTEXTS.pop().close()
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+
+
 def dist_setup(n_gpus):
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -361,7 +384,7 @@ def run_gb300(args, rank, world):
     pkg = _package()
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
-    ctx = pkg.Context(local)
+    ctx = open_context(pkg, local)
     rng = np.random.default_rng(1000 + rank)
 
     params = pkg.InspireParams.d2048()
@@ -651,7 +674,7 @@ def run_sm(args, rank, world):
     sm = pkg.special_modulus
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
-    ctx = pkg.Context(local)
+    ctx = open_context(pkg, local)
     rng = np.random.default_rng(2 + rank)
     server = sm.Server(ctx=ctx)
     shards = args.shards if args.shards != NUM_SHARDS else 2048
@@ -804,7 +827,7 @@ def run_tree(args, rank, world):
     pkg = _package()
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
-    ctx = pkg.Context(local)
+    ctx = open_context(pkg, local)
     g = torch.Generator(device="cuda")
     g.manual_seed(1 + rank)
     rng = np.random.default_rng(2000 + rank)
@@ -885,7 +908,7 @@ def run_nopack(args, rank, world):
     pkg = _package()
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
-    ctx = pkg.Context(local)
+    ctx = open_context(pkg, local)
     g = torch.Generator(device="cuda")
     g.manual_seed(1 + rank)
     rng = np.random.default_rng(3000 + rank)
@@ -985,7 +1008,7 @@ def run_cfg4(args, rank, world):
     pkg = _package()
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
-    ctx = pkg.Context(local)
+    ctx = open_context(pkg, local)
     rng = np.random.default_rng(4 + rank)
     store = pkg.ServerSessionStore.new(ctx)
     dbs = []
@@ -1251,7 +1274,7 @@ def run_cfg5(args, rank, world):
     pkg = _package()
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
-    ctx = pkg.Context(local)
+    ctx = open_context(pkg, local)
     shards = args.shards if args.shards != NUM_SHARDS else C5_SHARDS
     rng = np.random.default_rng(6 + rank)
     crs = pkg.ServerCrs(pkg.InspireParams.d2048(), rng.integers(0, 256, 32, dtype=np.uint8).tobytes(), GAMMA)
@@ -1359,6 +1382,43 @@ def run_cfg5(args, rank, world):
     return out
 
 
+# The other workloads the library serves, each at its own default size and step count, run
+# after the headline on one GPU so that the one JSON line carries their numbers too.
+OTHER_WORKLOADS = (("special-modulus", 100), ("mixed", 60), ("serving-sweep", 0), ("one-packing", 20),
+                   ("no-packing", 300))
+
+
+def compact(line, wall_s):
+    out = {k: line[k] for k in ("metric", "value", "unit", "steps", "warmup", "ms_per_step", "parity_checked",
+                                "gpu_launches") if k in line}
+    out["config"] = (line.get("config") or {}).get("workload")
+    if "e2e" in line:
+        out["e2e"] = {"value": line["e2e"]["value"], "unit": line["e2e"]["unit"]}
+    c = line.get("clocks") or {}
+    out["clocks"] = {k: c.get(k) for k in ("sm_mhz", "sm_max_mhz", "reasons", "samples")}
+    for k in ("fixed_rule", "latency", "saturation", "poisson_sweep"):
+        if k in line:
+            out[k] = line[k]
+    out["wall_s"] = round(wall_s, 1)
+    return out
+
+
+def other_workloads(args, rank, world):
+    runs = {"special-modulus": run_sm, "mixed": run_cfg4, "serving-sweep": run_cfg5, "one-packing": run_tree,
+            "no-packing": run_nopack}
+    out = {}
+    for name, steps in OTHER_WORKLOADS:
+        sub = argparse.Namespace(**vars(args))
+        sub.workload, sub.steps, sub.warmup = name, steps, max(args.warmup, 3)
+        sub.lanes = 4 if name == "serving-sweep" else 3
+        sub.shards, sub.requests = NUM_SHARDS, 16384
+        t0 = time.perf_counter()
+        line = runs[name](sub, rank, world)
+        close_contexts()
+        out[name] = compact(line, time.perf_counter() - t0)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1382,6 +1442,9 @@ def main():
                          "serving-sweep: the serving loop over 16,384 shards and 1000 seats; one-packing: the "
                          "tree responder, batches of 152; no-packing: the NoPacking responder, batches of 16")
     ap.add_argument("--requests", type=int, default=16384, help="trace length of the serving sweep")
+    ap.add_argument("--headline-only", action="store_true",
+                    help="skip the other workloads that the default served-batch run measures after the headline "
+                         "(one GPU, default database size) and reports under `workloads`")
     ap.add_argument("--shards", type=int, default=NUM_SHARDS,
                     help="shards in the database (smaller values only for profiling captures)")
     args = ap.parse_args()
@@ -1437,6 +1500,9 @@ def main():
             print(json.dumps(line))
         return
     line = run_gb300(args, rank, world)
+    if world == 1 and args.shards == NUM_SHARDS and not args.headline_only:
+        close_contexts()
+        line["workloads"] = other_workloads(args, rank, world)
     if rank == 0:
         if not args.no_cpu_baseline:
             # Two batches of 64 over the same 512-shard shape (about 10 s of CPU work); the
