@@ -53,3 +53,12 @@ def test_reference_arm_under_torchrun():
     line = lines[0]
     assert line["impl"] == "reference" and line["value"] > 0 and line["n_gpus"] == 2
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["cpu_baseline"]["kind"] == "port"
+    # The arm reports the GPU arm's metric, unit and configuration: the same workload.
+    sys.path.insert(0, ROOT)
+    import bench
+
+    assert line["metric"] == bench.METRIC and line["unit"] == "queries/s" and line["config"] == bench.CONFIG
+    assert line["higher_is_better"] is True and line["steps"] == 1 and line["warmup"] == 3
+    for key in ("ms_per_step", "scaling", "vs_baseline", "dtype", "data", "step", "execution"):
+        assert key in line, key
+    assert line["e2e"]["value"] == line["value"] and line["cpu_baseline"]["value"] == line["value"]
