@@ -449,15 +449,19 @@ void dispatch_loop(ig_serve* s) {
     Slot& sl = s->slots[k];
     const u32 count = (u32)sl.reqs.size();
     const size_t n = ring.n;
-    // Several CTAs per query (a cluster) only onto an idle device: a cluster needs its SMs free
-    // together within one GPC, and batches of single CTAs scattered over the GPCs leave it
-    // waiting on the device behind them although enough SMs are free in all. With other
-    // batches running, one CTA per query does the same work on fewer SMs.
+    // Several CTAs per query (a cluster) only while the batches in flight and this one leave
+    // at least half the SMs free: a cluster needs its SMs free together within one GPC, and
+    // batches of single CTAs scattered over most of the GPCs leave it waiting on the device
+    // behind them although enough SMs are free in all. Otherwise one CTA per query does the
+    // same work on fewer SMs.
     int ctas;
     {
       std::lock_guard<std::mutex> lk(s->mu);
+      const u32 sms = (u32)igint::sm_count(s->ctx);
       ctas = igint::launch_ctas(s->ctx, (u32)n, sl.reqs[0]->v.crs.gamma, count, count + s->inflight_ctas);
-      if (s->inflight_ctas != 0 && ctas > 1 && !igint::forced_ctas(s->ctx)) ctas = 1;
+      if (s->inflight_ctas != 0 && ctas > 1 && !igint::forced_ctas(s->ctx) &&
+          2 * (s->inflight_ctas + (u32)ctas * count) > sms)
+        ctas = 1;
       sl.ctas = (u32)ctas * count;
       s->inflight_ctas += sl.ctas;
     }
