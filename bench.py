@@ -327,6 +327,18 @@ def serve_leg(pkg, ctx, db, store, handle, shards, rng, ms, slots, max_batch=BAT
                                     "p50_ms": float(lat_ms[len(lat_ms) // 2]),
                                     "p99_ms": float(lat_ms[int(0.99 * (len(lat_ms) - 1))]),
                                     "mean_batch": st["mean_batch"]}
+        # Light load (5% of saturation), where requests arrive about alone: 2,048 of them.
+        low = min(requests, 2048)
+        rate = 0.05 * sat
+        arr = np.cumsum(rng.exponential(1e9 / rate, low)).astype(np.uint64)
+        _, _, lat, el = loop.replay(db, store, sids[warm:warm + low], handles[warm:warm + low], seeds[warm:warm + low],
+                                    bs[warm:warm + low], ms, arrival_ns=arr)
+        st = loop.stats(reset=True)
+        lat_ms = np.sort(lat) / 1e6
+        out["poisson_light_load"] = {"offered_per_s": rate, "queries_per_s": low / el, "requests": low,
+                                     "p50_ms": float(lat_ms[len(lat_ms) // 2]),
+                                     "p99_ms": float(lat_ms[int(0.99 * (len(lat_ms) - 1))]),
+                                     "mean_batch": st["mean_batch"]}
     return out, cases
 
 
@@ -1360,7 +1372,7 @@ def run_cfg5(args, rank, world):
                              "window": 4 * slots * BATCH}
         out["clocks"] = clk.summary()
         sweep = []
-        for frac in (0.25, 0.5, 0.75, 0.9):
+        for frac in (0.05, 0.25, 0.5, 0.75, 0.9):
             rate = frac * sat
             n = min(count, max(256, int(rate * 0.6)))
             arr = np.cumsum(rng.exponential(1e9 / rate, n)).astype(np.uint64)
