@@ -1422,7 +1422,7 @@ def other_workloads(args, rank, world):
     for name, steps in OTHER_WORKLOADS:
         sub = argparse.Namespace(**vars(args))
         sub.workload, sub.steps, sub.warmup = name, steps, max(args.warmup, 3)
-        sub.lanes = 4 if name == "serving-sweep" else 3
+        sub.lanes = {"serving-sweep": 4, "mixed": 8}.get(name, 3)
         sub.shards, sub.requests = NUM_SHARDS, 16384
         t0 = time.perf_counter()
         line = runs[name](sub, rank, world)
@@ -1446,7 +1446,8 @@ def main():
     ap.add_argument("--lanes", type=int, default=None,
                     help="streams consecutive batches rotate over in the device-resident timed region, and the "
                          "caller threads and serving slots of the host-buffer legs (default: 4 for the served "
-                         "batch of 64 and the serving sweep, 3 otherwise; the measured optimum of each)")
+                         "batch of 64 and the serving sweep, 8 for the mixed launches, 3 otherwise; the measured "
+                         "optimum of each)")
     ap.add_argument("--workload", default="served-batch",
                     choices=["served-batch", "special-modulus", "mixed", "serving-sweep", "one-packing", "no-packing"],
                     help="served-batch: the InspiRING batch of 64 over 2^20 records (the headline); special-modulus: "
@@ -1462,7 +1463,7 @@ def main():
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.lanes is None:
-        args.lanes = 4 if args.workload in ("served-batch", "serving-sweep") else 3
+        args.lanes = {"served-batch": 4, "serving-sweep": 4, "mixed": 8}.get(args.workload, 3)
     if args.steps is None:
         args.steps = 20 if args.impl == "reference" else {"served-batch": 20, "special-modulus": 100, "mixed": 60,
                                                           "serving-sweep": 0, "one-packing": 20,
