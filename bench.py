@@ -1425,7 +1425,15 @@ def other_workloads(args, rank, world):
         sub.lanes = {"serving-sweep": 4, "mixed": 8}.get(name, 3)
         sub.shards, sub.requests = NUM_SHARDS, 16384
         t0 = time.perf_counter()
-        line = runs[name](sub, rank, world)
+        try:
+            line = runs[name](sub, rank, world)
+        except Exception as e:  # reported in its slot; the headline line still prints
+            out[name] = {"error": f"{type(e).__name__}: {e}"[:500], "wall_s": round(time.perf_counter() - t0, 1)}
+            try:
+                close_contexts()
+            except Exception:
+                pass
+            continue
         close_contexts()
         out[name] = compact(line, time.perf_counter() - t0)
     return out
