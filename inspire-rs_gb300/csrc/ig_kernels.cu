@@ -69,15 +69,15 @@ __device__ __forceinline__ void bf_inv4(u64& X, u64& Y, u64 w, u64 wp) {
 
 template <int LOGN, int NT, int NB>
 __device__ __forceinline__ void ntt_fwd_r4(u64* const (&x)[NB], const u64* tw, const u64* twp) {
-  constexpr int N = 1 << LOGN;
-  static_assert(NT == N / 4, "one radix-4 unit per thread");
+  constexpr int N = 1 << LOGN, UPT = N / 4 / NT;
+  static_assert(UPT >= 1 && (N / 4) % NT == 0, "whole radix-4 units per thread");
   const int tid = threadIdx.x;
   int s = 0;
   if (LOGN & 1) {
     constexpr int t = N / 2;
     const u64 w = tw[1], wp = twp[1];
 #pragma unroll
-    for (int r = 0; r < 2; r++) {
+    for (int r = 0; r < 2 * UPT; r++) {
       const int b = tid + r * NT;
 #pragma unroll
       for (int k = 0; k < NB; k++) {
@@ -93,22 +93,26 @@ __device__ __forceinline__ void ntt_fwd_r4(u64* const (&x)[NB], const u64* tw, c
 #pragma unroll 1
   for (; s < LOGN; s += 2) {
     const int t = N >> (s + 1), m = 1 << s, h = t >> 1;
-    const int i = tid / h, o = tid - i * h;
-    const int e0 = i * 2 * t + o;
-    const u64 wa = tw[m + i], wap = twp[m + i];
-    const u64 wb = tw[2 * m + 2 * i], wbp = twp[2 * m + 2 * i];
-    const u64 wc = tw[2 * m + 2 * i + 1], wcp = twp[2 * m + 2 * i + 1];
 #pragma unroll
-    for (int k = 0; k < NB; k++) {
-      u64 a0 = x[k][e0], a1 = x[k][e0 + h], a2 = x[k][e0 + t], a3 = x[k][e0 + t + h];
-      bf_fwd(a0, a2, wa, wap);
-      bf_fwd(a1, a3, wa, wap);
-      bf_fwd(a0, a1, wb, wbp);
-      bf_fwd(a2, a3, wc, wcp);
-      x[k][e0] = a0;
-      x[k][e0 + h] = a1;
-      x[k][e0 + t] = a2;
-      x[k][e0 + t + h] = a3;
+    for (int uu = 0; uu < UPT; uu++) {
+      const int u = tid + uu * NT;
+      const int i = u / h, o = u - i * h;
+      const int e0 = i * 2 * t + o;
+      const u64 wa = tw[m + i], wap = twp[m + i];
+      const u64 wb = tw[2 * m + 2 * i], wbp = twp[2 * m + 2 * i];
+      const u64 wc = tw[2 * m + 2 * i + 1], wcp = twp[2 * m + 2 * i + 1];
+#pragma unroll
+      for (int k = 0; k < NB; k++) {
+        u64 a0 = x[k][e0], a1 = x[k][e0 + h], a2 = x[k][e0 + t], a3 = x[k][e0 + t + h];
+        bf_fwd(a0, a2, wa, wap);
+        bf_fwd(a1, a3, wa, wap);
+        bf_fwd(a0, a1, wb, wbp);
+        bf_fwd(a2, a3, wc, wcp);
+        x[k][e0] = a0;
+        x[k][e0 + h] = a1;
+        x[k][e0 + t] = a2;
+        x[k][e0 + t + h] = a3;
+      }
     }
     __syncthreads();
   }
@@ -125,30 +129,34 @@ __device__ __forceinline__ void inv_twiddle(const u64* tw, const u64* twp, int m
 
 template <int LOGN, int NT, int NB>
 __device__ __forceinline__ void ntt_inv_r4(u64* const (&x)[NB], const u64* tw, const u64* twp) {
-  constexpr int N = 1 << LOGN;
-  static_assert(NT == N / 4, "one radix-4 unit per thread");
+  constexpr int N = 1 << LOGN, UPT = N / 4 / NT;
+  static_assert(UPT >= 1 && (N / 4) % NT == 0, "whole radix-4 units per thread");
   const int tid = threadIdx.x;
   int s = 0;
 #pragma unroll 1
   for (; s + 1 < LOGN; s += 2) {
     const int t = 1 << s, m = N >> (s + 1);
-    const int B = tid >> s, o = tid & (t - 1);
-    const int e0 = B * 4 * t + o;
-    u64 w0, w0p, w1, w1p, w2, w2p;
-    inv_twiddle(tw, twp, m + 2 * B, w0, w0p);
-    inv_twiddle(tw, twp, m + 2 * B + 1, w1, w1p);
-    inv_twiddle(tw, twp, (m >> 1) + B, w2, w2p);
 #pragma unroll
-    for (int k = 0; k < NB; k++) {
-      u64 a0 = x[k][e0], a1 = x[k][e0 + t], a2 = x[k][e0 + 2 * t], a3 = x[k][e0 + 3 * t];
-      bf_inv(a0, a1, w0, w0p);
-      bf_inv(a2, a3, w1, w1p);
-      bf_inv(a0, a2, w2, w2p);
-      bf_inv(a1, a3, w2, w2p);
-      x[k][e0] = a0;
-      x[k][e0 + t] = a1;
-      x[k][e0 + 2 * t] = a2;
-      x[k][e0 + 3 * t] = a3;
+    for (int uu = 0; uu < UPT; uu++) {
+      const int u = tid + uu * NT;
+      const int B = u >> s, o = u & (t - 1);
+      const int e0 = B * 4 * t + o;
+      u64 w0, w0p, w1, w1p, w2, w2p;
+      inv_twiddle(tw, twp, m + 2 * B, w0, w0p);
+      inv_twiddle(tw, twp, m + 2 * B + 1, w1, w1p);
+      inv_twiddle(tw, twp, (m >> 1) + B, w2, w2p);
+#pragma unroll
+      for (int k = 0; k < NB; k++) {
+        u64 a0 = x[k][e0], a1 = x[k][e0 + t], a2 = x[k][e0 + 2 * t], a3 = x[k][e0 + 3 * t];
+        bf_inv(a0, a1, w0, w0p);
+        bf_inv(a2, a3, w1, w1p);
+        bf_inv(a0, a2, w2, w2p);
+        bf_inv(a1, a3, w2, w2p);
+        x[k][e0] = a0;
+        x[k][e0 + t] = a1;
+        x[k][e0 + 2 * t] = a2;
+        x[k][e0 + 3 * t] = a3;
+      }
     }
     __syncthreads();
   }
@@ -157,7 +165,7 @@ __device__ __forceinline__ void ntt_inv_r4(u64* const (&x)[NB], const u64* tw, c
     u64 w, wp;
     inv_twiddle(tw, twp, 1, w, wp);
 #pragma unroll
-    for (int r = 0; r < 2; r++) {
+    for (int r = 0; r < 2 * UPT; r++) {
       const int b = tid + r * NT;
 #pragma unroll
       for (int k = 0; k < NB; k++) {
@@ -1283,7 +1291,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
 // ------------------------------------------------------------------------------------
 // Four CTAs per query (a cluster of 4), for small batches whose latency sets the tail: a
 // query's recursion spread over four SMs. CTA r owns quarter r, slots [r N/4, (r+1) N/4), of
-// every NTT-domain vector, one slot per thread. The inverse's stages 0 .. logn-3 and the
+// every NTT-domain vector, two slots per thread (N/8 threads: the quarter-local passes keep
+// half of them busy or all, where N/4 threads left three quarters or half idle at every
+// barrier). The inverse's stages 0 .. logn-3 and the
 // forward's stages 2 .. logn-1 stay inside a quarter (the part helpers above); the two
 // stages on each side that mix quarters combine the four elements b, b + N/4, b + N/2,
 // b + 3N/4 of each b < N/4, so they run as one radix-4 cross pass per link: thread b reads
@@ -1297,11 +1307,11 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
 // comes from the other two (inspiring2.rs:1094-1161), folded into the key rows as in
 // k_respond.
 template <int LOGN>
-__global__ void __cluster_dims__(4, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
+__global__ void __cluster_dims__(4, 1, 1) __launch_bounds__((1 << LOGN) / 8, 1)
     k_respond_quad(CrsDev c, const QueryDev* queries, const ShardDev* shards, const u64* b_fold, u64* a_out,
                    u64* b_out, u32* status, int force_serial) {
   namespace cg = cooperative_groups;
-  constexpr int N = 1 << LOGN, NT = N / 4, P = N / 4;
+  constexpr int N = 1 << LOGN, NT = N / 8, P = N / 4, SPT = P / NT;  // two slots a thread
   constexpr u32 M2N = 2 * N - 1;
   constexpr u64 DMASK = (1ULL << 20) - 1;
   extern __shared__ __align__(16) u64 sm[];
@@ -1327,7 +1337,7 @@ __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
   const SetView ps = set_view(c, qd.crs);
   const u32 gamma = ps.gamma;
   const bool exact = ps.approx == 0;
-  const int slot = rank * P + tid;  // this thread's slot
+  // This thread's slots: rank P + tid + j NT, j < SPT.
 
   stage_constants<N, NT>(c, ps, qd.seat_R, tw, twp, Wm, Y, e_tab, s_tab);
   expand_a<N, NT>(qd, a_ntt, status, qi, force_serial);
@@ -1335,12 +1345,16 @@ __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
     u64* const bufs[1] = {a_ntt};
     ntt_fwd_r4<LOGN, NT, 1>(bufs, tw, twp);
   }
-  const u32 et = e_tab[slot];
-  u64 cur, sb = 0;
-  {
+  u32 et[SPT];
+  u64 cur[SPT], sb[SPT];
+#pragma unroll
+  for (int j = 0; j < SPT; j++) {
+    const int slot = rank * P + tid + j * NT;
+    et[j] = e_tab[slot];
     const u32 gp = ps.gpow[gamma - 1];
-    const u32 tb = s_tab[((gp * et) & M2N) >> 1];
-    cur = mont(a_ntt[tb], sh.sums_R[(size_t)(gamma - 1) * N + slot]);
+    const u32 tb = s_tab[((gp * et[j]) & M2N) >> 1];
+    cur[j] = mont(a_ntt[tb], sh.sums_R[(size_t)(gamma - 1) * N + slot]);
+    sb[j] = 0;
   }
   // Twiddles of the cross pass: the inverse's stage logn-2 (indices 2 and 3), the forward's
   // stage 0 (index 1) and stage 1 (index 2 for the first half, 3 for the second).
@@ -1351,20 +1365,25 @@ __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
   const u64 wfs = tw[2 + (rank >> 1)], wfsp = twp[2 + (rank >> 1)];
 #pragma unroll 1
   for (int i = (int)gamma - 2; i >= 0; i--) {
-    const u64 sv = sh.sums_R[(size_t)i * N + slot];
+    u64 sv[SPT];
+#pragma unroll
+    for (int j = 0; j < SPT; j++) sv[j] = sh.sums_R[(size_t)i * N + rank * P + tid + j * NT];
     const u32 gp = ps.gpow[i];
     const int par = (i & 1) * P;
     u64* xq = X + par;
-    xq[sw(tid)] = cur;
+#pragma unroll
+    for (int j = 0; j < SPT; j++) xq[sw(tid + j * NT)] = cur[j];
     __syncthreads();
     int s = 0;
 #pragma unroll 1
     for (; s + 1 <= LOGN - 3; s += 2) inv_part_r4<LOGN, 4>(xq, s, rank, tw, twp);
     if (s == LOGN - 3) inv_part_r2<LOGN, 4>(xq, s, rank, tw, twp);
     cluster.sync();
-    {
-      u64 x0 = peer[0][par + sw(tid)], x1 = peer[1][par + sw(tid)];
-      u64 x2 = peer[2][par + sw(tid)], x3 = peer[3][par + sw(tid)];
+#pragma unroll
+    for (int j = 0; j < SPT; j++) {
+      const int b = tid + j * NT;
+      u64 x0 = peer[0][par + sw(b)], x1 = peer[1][par + sw(b)];
+      u64 x2 = peer[2][par + sw(b)], x3 = peer[3][par + sw(b)];
       bf_inv4(x0, x1, wi2, wi2p);  // (b, b + N/4), block 0 of stage logn-2
       bf_inv4(x2, x3, wi3, wi3p);  // (b + N/2, b + 3N/4), block 1
       u64 cf[4];                   // coefficients b, b + N/4, b + N/2, b + 3N/4
@@ -1399,8 +1418,8 @@ __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
         bf_fwd8(lo, hi, wfs, wfsp);
         return (rank & 1) ? hi : lo;
       };
-      D[sw(tid)] = fwd(g0);
-      D[P + sw(tid)] = fwd(g1);
+      D[sw(b)] = fwd(g0);
+      D[P + sw(b)] = fwd(g1);
     }
     __syncthreads();
     s = 2;
@@ -1410,26 +1429,34 @@ __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
     }
 #pragma unroll 1
     for (; s < LOGN; s += 2) fwd_part_r4<LOGN, 4>(D, s, rank, tw, twp);
-    const u64 d0 = D[sw(tid)], d1 = D[P + sw(tid)];
-    const u32 tb = s_tab[((gp * et) & M2N) >> 1];
-    u128 nb = wide(d0, Y[tb]) + wide(d1, Y[N + tb]);
-    u128 nc = wide(a_ntt[tb], sv) + wide(d0, Wm[tb]) + wide(d1, Wm[N + tb]);
-    if (exact) {  // the rows are folded: R_{i+1} stands in for digit 2
-      nb += wide(cur, Y[2 * N + tb]);
-      nc += wide(cur, Wm[2 * N + tb]);
+#pragma unroll
+    for (int j = 0; j < SPT; j++) {
+      const u64 d0 = D[sw(tid + j * NT)], d1 = D[P + sw(tid + j * NT)];
+      const u32 tb = s_tab[((gp * et[j]) & M2N) >> 1];
+      u128 nb = wide(d0, Y[tb]) + wide(d1, Y[N + tb]);
+      u128 nc = wide(a_ntt[tb], sv[j]) + wide(d0, Wm[tb]) + wide(d1, Wm[N + tb]);
+      if (exact) {  // the rows are folded: R_{i+1} stands in for digit 2
+        nb += wide(cur[j], Y[2 * N + tb]);
+        nc += wide(cur[j], Wm[2 * N + tb]);
+      }
+      sb[j] = addq(sb[j], redc_wide(nb));
+      cur[j] = redc_wide(nc);
     }
-    sb = addq(sb, redc_wide(nb));
-    cur = redc_wide(nc);
   }
   // Final transforms: rank 0 assembles R_0 (-> a), rank 1 the online sum (-> b), each from
   // the four quarters exchanged through X once every peer is past its last cross-pass read.
   cluster.sync();
-  X[tid] = cur;
-  X[P + tid] = sb;
+#pragma unroll
+  for (int j = 0; j < SPT; j++) {
+    X[tid + j * NT] = cur[j];
+    X[P + tid + j * NT] = sb[j];
+  }
   cluster.sync();
   if (rank < 2) {
 #pragma unroll
-    for (int k = 0; k < 4; k++) D[k * P + tid] = peer[k][rank * P + tid];
+    for (int k = 0; k < 4; k++)
+#pragma unroll
+      for (int j = 0; j < SPT; j++) D[k * P + tid + j * NT] = peer[k][rank * P + tid + j * NT];
   }
   cluster.sync();  // each CTA's X stays alive until ranks 0 and 1 have read it
   if (rank >= 2) return;
@@ -1439,7 +1466,7 @@ __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__((1 << LOGN) / 4, 1)
     ntt_inv_r4<LOGN, NT, 1>(bufs, tw, twp);
   }
 #pragma unroll
-  for (int k = 0; k < 4; k++) {
+  for (int k = 0; k < N / NT; k++) {
     const int t = tid + k * NT;
     if (rank == 0)
       a_out[(size_t)qi * N + t] = finish_a(c, D[t], qd.ms);
@@ -2359,7 +2386,7 @@ cudaError_t respond(const CrsDev& c, const QueryDev* queries, const ShardDev* sh
       auto k = k_respond_quad<L>;
       cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return e;
-      k<<<4 * nq, (1 << L) / 4, smem, s>>>(c, queries, shards, b_fold, a_out, b_out, status, force_serial_expand);
+      k<<<4 * nq, (1 << L) / 8, smem, s>>>(c, queries, shards, b_fold, a_out, b_out, status, force_serial_expand);
     } else if (ctas == 2) {
       auto k = k_respond_pair<L>;
       cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
