@@ -1396,8 +1396,11 @@ def run_cfg5(args, rank, world):
 
 # The other workloads the library serves, each at its own default size and step count, run
 # after the headline on one GPU so that the one JSON line carries their numbers too.
-OTHER_WORKLOADS = (("special-modulus", 100), ("mixed", 60), ("serving-sweep", 0), ("one-packing", 20),
-                   ("no-packing", 300))
+OTHER_WORKLOADS = ("special-modulus", "mixed", "serving-sweep", "one-packing", "no-packing")
+# Default timed steps and lanes of each workload (the measured optimum of lanes).
+DEFAULT_STEPS = {"served-batch": 20, "special-modulus": 100, "mixed": 60, "serving-sweep": 0, "one-packing": 20,
+                 "no-packing": 300}
+DEFAULT_LANES = {"served-batch": 4, "serving-sweep": 4, "mixed": 8}  # 3 otherwise
 
 
 def compact(line, wall_s):
@@ -1419,10 +1422,10 @@ def other_workloads(args, rank, world):
     runs = {"special-modulus": run_sm, "mixed": run_cfg4, "serving-sweep": run_cfg5, "one-packing": run_tree,
             "no-packing": run_nopack}
     out = {}
-    for name, steps in OTHER_WORKLOADS:
+    for name in OTHER_WORKLOADS:
         sub = argparse.Namespace(**vars(args))
-        sub.workload, sub.steps, sub.warmup = name, steps, max(args.warmup, 3)
-        sub.lanes = {"serving-sweep": 4, "mixed": 8}.get(name, 3)
+        sub.workload, sub.steps, sub.warmup = name, DEFAULT_STEPS[name], max(args.warmup, 3)
+        sub.lanes = DEFAULT_LANES.get(name, 3)
         sub.shards, sub.requests = NUM_SHARDS, 16384
         t0 = time.perf_counter()
         try:
@@ -1471,11 +1474,9 @@ def main():
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.lanes is None:
-        args.lanes = {"served-batch": 4, "serving-sweep": 4, "mixed": 8}.get(args.workload, 3)
+        args.lanes = DEFAULT_LANES.get(args.workload, 3)
     if args.steps is None:
-        args.steps = 20 if args.impl == "reference" else {"served-batch": 20, "special-modulus": 100, "mixed": 60,
-                                                          "serving-sweep": 0, "one-packing": 20,
-                                                          "no-packing": 300}[args.workload]
+        args.steps = 20 if args.impl == "reference" else DEFAULT_STEPS[args.workload]
     rank, world = dist_setup(args.gpus)
     if args.impl == "reference":
         if rank != 0:
