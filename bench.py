@@ -239,8 +239,9 @@ def close_contexts():
 
     while _OPEN_CONTEXTS:
         _OPEN_CONTEXTS.pop().close()
-    torch.cuda.synchronize()
-    torch.cuda.empty_cache()
+    if torch.cuda.is_available():
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
 
 
 def dist_setup(n_gpus):
