@@ -1440,6 +1440,8 @@ def other_workloads(args, rank, world):
             continue
         close_contexts()
         out[name] = compact(line, time.perf_counter() - t0)
+        if name == "special-modulus" and not args.no_cpu_baseline:
+            out[name]["cpu_baseline"] = sm_cpu_sample(steps=3, warmup=1)
     return out
 
 

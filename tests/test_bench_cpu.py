@@ -42,7 +42,7 @@ def test_a_failing_workload_is_reported_in_its_slot(monkeypatch):
         monkeypatch.setattr(bench, name, ok)
     monkeypatch.setattr(bench, "run_cfg4", fails)
     args = argparse.Namespace(workload="served-batch", steps=20, warmup=3, lanes=4, shards=bench.NUM_SHARDS,
-                              requests=16384)
+                              requests=16384, no_cpu_baseline=True)
     out = bench.other_workloads(args, 0, 1)
     assert list(out) == list(bench.OTHER_WORKLOADS)
     assert "oracle" in out["mixed"]["error"] and "value" not in out["mixed"]
