@@ -37,6 +37,10 @@ import time
 
 import numpy as np
 
+# The oracle's OpenMP workers (byte checks between GPU legs, the CPU samples) sleep as soon
+# as a parallel region ends instead of spinning on the host cores the GPU legs' threads use.
+os.environ.setdefault("OMP_WAIT_POLICY", "PASSIVE")
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
