@@ -492,8 +492,12 @@ def run_gb300(args, rank, world):
     a_h = d_a.cpu().numpy().view(np.uint64)
     b_h = d_b.cpu().numpy().view(np.uint64)
     cases = []
-    for i in (total - 1, total - 2):
-        for k in (0, BATCH - 1):
+    # The last batch of each lane still holds its outputs: the last two batches with two or
+    # more lanes, the last one with one lane (four queries of it then).
+    last = [total - 1, total - 2] if lanes > 1 else [total - 1]
+    picks = (0, BATCH - 1) if lanes > 1 else (0, 1, BATCH - 2, BATCH - 1)
+    for i in last:
+        for k in picks:
             cases.append((int(shard_ids[i][k]), seeds_h[i, k].tobytes(), bs_h[i, k], a_h[i % lanes, k],
                           b_h[i % lanes, k]))
 
@@ -610,9 +614,10 @@ def run_gb300(args, rank, world):
         "execution": {"parallelism": f"replicas x{world}" if world > 1 else "single GPU", "lanes": lanes,
                       "launch_shape": shape},
         "parity_checked": checked,
-        "parity_note": "outside the timing: 4 responses of the timed region's last two batches (first and last "
-                       "query of each) and 2 served by the serving loop, recomputed by the oracle's store path "
-                       "on the same 2^20-record database, key and queries, 36-bit switch: wire bytes equal",
+        "parity_note": "outside the timing: 4 responses of the timed region's last batches (first and last "
+                       "query of the last two, or four queries of the last with one lane) and 2 served by the "
+                       "serving loop, recomputed by the oracle's store path on the same 2^20-record database, "
+                       "key and queries, 36-bit switch: wire bytes equal",
         "db_gbs": value * SHARD_DB_BYTES / 1e9,
         "e2e": {"value": e2e_value, "unit": "queries/s",
                 "h2d_bytes_per_step": bps * BATCH * (32 + N_RING * 8 + 4),
